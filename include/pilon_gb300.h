@@ -1,0 +1,244 @@
+/*
+ * pilon_gb300 — C ABI of the GB300 pileup / call / k-mer-tally engine.
+ *
+ * The engine replaces the per-read and per-position hot loops of Pilon 1.24
+ * (broadinstitute/pilon).  Every entry point below names the reference code it
+ * stands in for (paths are relative to the reference project root; S/ is
+ * src/main/scala/org/broadinstitute/pilon/).
+ *
+ * Conventions
+ *   - Plain C types only: pointers, sizes, POD structs.  No exceptions cross
+ *     the boundary; every call returns a pg_status and pg_last_error() gives
+ *     the message of the last failure on that context.
+ *   - Input buffers are caller-owned.  Results stay in the context (device
+ *     memory) until the next pg_pileup_regions / pg_kmer_tally call on the
+ *     same context, and are copied out with the pg_fetch_* calls.
+ *   - One context is used by one host thread at a time; all its work is
+ *     ordered on the context's own CUDA stream.
+ *   - Coordinates are Pilon's: 1-based, closed intervals (S/Region.scala:21-45).
+ */
+#ifndef PILON_GB300_H
+#define PILON_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pg_status {
+  PG_OK = 0,
+  PG_ERR_ARG = 1,        /* bad argument (null pointer, bad size, bad option) */
+  PG_ERR_CUDA = 2,       /* CUDA runtime error; context should be closed */
+  PG_ERR_NOMEM = 3,      /* device memory budget exceeded */
+  PG_ERR_INDEX = 4,      /* an index left its array; the reference throws
+                            ArrayIndexOutOfBoundsException here (indel left
+                            shift below the region start,
+                            S/PileUpRegion.scala:155-182) */
+  PG_ERR_STATE = 5,      /* call out of order (e.g. fetch before process) */
+  PG_ERR_LIMIT = 6,      /* a documented size limit was exceeded */
+  PG_ERR_TIMEOUT = 7     /* a bounded device-side wait ran out */
+} pg_status;
+
+/* Long-read type of one BAM (S/BamFile.scala:32-47). */
+enum { PG_NOT_LONG_READ = 0, PG_NANOPORE = 1, PG_PACBIO = 2 };
+/* BAM type (S/BamFile.scala:29, S/Pilon.scala:130-231). */
+enum { PG_BAM_FRAGS = 0, PG_BAM_JUMPS = 1, PG_BAM_UNPAIRED = 2, PG_BAM_BAM = 3 };
+
+/* Options of the hot path, mirroring the global vars of S/Pilon.scala:28-73.
+ * pg_default_params() fills in Pilon's defaults. */
+typedef struct pg_params {
+  int32_t min_mq;          /* --minmq, default 0 */
+  int32_t min_qual;        /* --minqual, default 0 */
+  int32_t flank;           /* --flank, default 10 */
+  int32_t default_qual;    /* --defaultqual, default 10 */
+  int32_t min_min_depth;   /* constant 5 */
+  int32_t nonpf;           /* --nonpf */
+  int32_t duplicates;      /* --duplicates */
+  int32_t old_indel;       /* --oldindel */
+  int32_t fix_amb;         /* Pilon.iupac || Pilon.fixAmb (S/GenomeRegion.scala:235) */
+  int32_t long_read;       /* PG_NOT_LONG_READ / PG_NANOPORE / PG_PACBIO of the BAM */
+  int32_t bam_type;        /* PG_BAM_* of the BAM */
+  int32_t long_read_only;  /* Pilon.longread && no frags BAM (S/GenomeRegion.scala:147) */
+  double  min_depth;       /* --mindepth, default 0.1 */
+} pg_params;
+
+/* Aligned reads of one BAM as structure-of-arrays, in BAM (coordinate) order.
+ * Field meanings follow the htsjdk SAMRecord getters used on the hot path
+ * (S/PileUpRegion.scala:103-115, S/BamFile.scala:101-105, 137). */
+typedef struct pg_reads {
+  int64_t n_reads;
+  const int32_t *pos;         /* getAlignmentStart, 1-based */
+  const int32_t *aend;        /* getAlignmentEnd (pos + ref-consuming length - 1) */
+  const uint16_t *flag;       /* SAM flag word */
+  const uint8_t *mapq;        /* getMappingQuality */
+  const int32_t *tlen;        /* getInferredInsertSize */
+  const int32_t *ref_id;      /* getReferenceIndex */
+  const int32_t *mate_ref_id; /* getMateReferenceIndex */
+  const int64_t *cigar_off;   /* first CIGAR word of the read in `cigar` */
+  const uint16_t *n_cigar;    /* number of CIGAR words */
+  const uint32_t *cigar;      /* BAM CIGAR words: len << 4 | op (MIDNSHP=X -> 0..8) */
+  const int64_t *seq_off;     /* first byte of the read in `seq` */
+  const int32_t *l_seq;       /* getReadLength */
+  const uint8_t *seq;         /* BAM 4-bit bases, two per byte, high nibble first,
+                                 "=ACMGRSVTWYHKDBN" */
+  const int64_t *qual_off;    /* first byte of the read in `qual` */
+  const uint8_t *qual;        /* Phred bytes; a first byte of 0xFF means absent
+                                 (getBaseQualities() is empty -> defaultQual) */
+  int64_t n_cigar_words;      /* total length of `cigar` */
+  int64_t seq_bytes;          /* total length of `seq` */
+  int64_t qual_bytes;         /* total length of `qual` */
+} pg_reads;
+
+/* One region (GenomeRegion) and the reads fed to it.  The reads of
+ * [read_begin, read_end) must contain every read of `contig` that overlaps
+ * [max(start-10000,0), min(stop+10000,len)] (S/BamFile.scala:117-119); reads
+ * outside that window inside the range are skipped by the engine, exactly as
+ * the reference's query would not return them. */
+typedef struct pg_region {
+  int32_t contig;            /* index into the contigs given to pg_set_reference */
+  int32_t start;             /* 1-based first base */
+  int32_t stop;              /* 1-based last base, inclusive */
+  int32_t pad_;
+  int64_t read_begin;
+  int64_t read_end;
+} pg_region;
+
+/* Per-region scalars (PileUpRegion / GenomeRegion / BamFile fields). */
+typedef struct pg_region_stats {
+  int64_t base_count;        /* PileUpRegion.baseCount */
+  int64_t read_count;        /* PileUpRegion.readCount */
+  int32_t phys_cov_start;    /* PileUpRegion.physCovStart */
+  int32_t insert_size_start; /* PileUpRegion.insertSizeStart */
+  int32_t min_depth;         /* GenomeRegion.minDepth after postProcess */
+  int32_t n_changes;         /* entries of the change map after pass 1 */
+  /* BamFile.addInsert deltas of this region (S/BamFile.scala:194-202) */
+  int64_t fr_count, fr_sum, fr_sumsq;
+  int64_t rf_count, rf_sum, rf_sumsq;
+  int32_t error;             /* PG_ERR_INDEX when the reference would throw */
+  int32_t n_ins_strings;     /* insertion-call strings of this region */
+} pg_region_stats;
+
+/* Call flags, one uint32 per position (PileUp.BaseCall, S/PileUp.scala:132-255,
+ * and the pass-1 disposition of S/GenomeRegion.scala:237-272). */
+#define PG_CALL_BASE(f)      ((f) & 3u)          /* baseIndex (A,C,G,T) */
+#define PG_CALL_ALT(f)       (((f) >> 2) & 3u)   /* altBaseIndex */
+#define PG_CALL_HAS_BASE     (1u << 4)           /* n > 0 (else base is 'N') */
+#define PG_CALL_HOMO         (1u << 5)
+#define PG_CALL_INS          (1u << 6)           /* insertion call */
+#define PG_CALL_DEL          (1u << 7)           /* deletion call */
+#define PG_CALL_HOMO_INDEL   (1u << 8)
+#define PG_CALL_CHANGE(f)    (((f) >> 9) & 7u)   /* PG_CHANGE_* */
+#define PG_CALL_CONFIRMED    (1u << 12)
+#define PG_CALL_DELETED      (1u << 13)          /* inside a called deletion */
+enum { PG_CHANGE_NONE = 0, PG_CHANGE_SNP = 1, PG_CHANGE_INS = 2, PG_CHANGE_DEL = 3, PG_CHANGE_AMB = 4 };
+
+/* Host buffers for one region's results; every array has `size` entries
+ * (count and qual_sum have 4*size, A,C,G,T interleaved per position).  Any
+ * pointer may be NULL to skip that field. */
+typedef struct pg_region_out {
+  int32_t *count;            /* PileUp.baseCount */
+  int64_t *qual_sum;         /* PileUp.qualSum */
+  int32_t *mq_sum, *q_sum, *phys_cov, *insert_size, *bad_pair;
+  int32_t *deletions, *del_qual, *insertions, *ins_qual, *clips;
+  uint32_t *call;            /* PG_CALL_* flags */
+  int64_t *score;            /* BaseCall.score */
+  int32_t *indel_len;        /* length of the called insertion/deletion, else 0 */
+  int32_t *ins_str;          /* offset of the called insertion in ins_chars, else -1 */
+  char *ins_chars;           /* insertion-call characters (n_ins_strings total bytes
+                                = sum of their lengths), may be NULL */
+  int64_t ins_chars_cap;     /* capacity of ins_chars */
+} pg_region_out;
+
+/* One local-reassembly window for the k-mer tally: reads [read_begin,
+ * read_end) of the read store are the window's recruited reads, in the order
+ * Assembler.addReads sees them (S/GapFiller.scala:125-129). */
+typedef struct pg_window {
+  int64_t read_begin;
+  int64_t read_end;
+} pg_window;
+
+/* One graph edge of Assembler.buildGraph (S/Assembler.scala:132-154):
+ * kmer -> kmer[1:] + next; alt >= 0 adds the altGraph link kmer[1:] + alt.
+ * The K-mer (K <= 32) is given as 4-bit BAM codes ("=ACMGRSVTWYHKDBN"), so
+ * K-mers containing N or IUPAC codes are exact too: base j sits at bits
+ * 60-4*(j%16) of key_hi (j < 16) or key_lo (j >= 16). */
+typedef struct pg_kmer_edge {
+  uint64_t key_hi;
+  uint64_t key_lo;
+  int32_t window;
+  int8_t next;               /* called base index (A,C,G,T) */
+  int8_t alt;                /* alt base index, or -1 when the call is homozygous */
+  int16_t pad_;
+  int32_t depth;             /* PileUp.depth of the K-mer */
+  int32_t weight;            /* baseCount of the called base */
+} pg_kmer_edge;
+
+typedef struct pg_ctx pg_ctx;
+
+/* ---- context ----------------------------------------------------------- */
+/* Opens a context on CUDA device `device`.  Replaces nothing in the
+ * reference (which has no device); allocates the context's stream. */
+pg_status pg_open(pg_ctx **ctx, int device);
+void pg_close(pg_ctx *ctx);
+const char *pg_last_error(const pg_ctx *ctx);
+/* Fills Pilon's defaults (S/Pilon.scala:52-73). */
+void pg_default_params(pg_params *p);
+/* Library version string. */
+const char *pg_version(void);
+
+/* ---- reference ----------------------------------------------------------
+ * Replaces GenomeFile's contig load (S/GenomeFile.scala:30-42): raw FASTA
+ * bytes per contig, uploaded once and kept resident. */
+pg_status pg_set_reference(pg_ctx *ctx, int32_t n_contigs, const int64_t *lens,
+                           const uint8_t *const *bases);
+
+/* ---- reads --------------------------------------------------------------
+ * The BAM read feed (S/BamFile.scala:108-139) as packed SoA.  Host pointers:
+ * the arrays are copied into the context's device read store.  Device
+ * pointers (pg_set_reads_device): used in place, must outlive their use. */
+pg_status pg_set_reads(pg_ctx *ctx, const pg_reads *host_reads);
+pg_status pg_set_reads_device(pg_ctx *ctx, const pg_reads *device_reads);
+
+/* ---- pileup + calls -------------------------------------------------------
+ * For every region: BamFile.process + PileUpRegion.addRead
+ * (S/BamFile.scala:108-148, S/PileUpRegion.scala:102-220), computePhysCov
+ * (S/PileUpRegion.scala:90-100), PileUp.baseCall (S/PileUp.scala:132-257) and
+ * pass 1 of GenomeRegion.postProcess (S/GenomeRegion.scala:214-272), including
+ * the deletion-span update of later pileups.  `batched` = 0 launches the
+ * kernels once per region (the plain path); 1 runs all regions in one
+ * persistent launch per kernel. */
+pg_status pg_pileup_regions(pg_ctx *ctx, const pg_region *regions, int32_t n_regions,
+                            const pg_params *params, int32_t batched);
+
+/* Per-region scalars of the last pg_pileup_regions call. */
+pg_status pg_fetch_stats(pg_ctx *ctx, int32_t region, pg_region_stats *stats);
+/* Copies one region's arrays into caller host buffers. */
+pg_status pg_fetch_region(pg_ctx *ctx, int32_t region, pg_region_out *out);
+
+/* Tile width (positions per CTA tile, 1024..8192, power of two) and warps per
+ * CTA of the pileup kernel; 0 keeps the current value.  The autotuner of the
+ * host package chooses these. */
+pg_status pg_set_tuning(pg_ctx *ctx, int32_t tile_width, int32_t warps_per_cta);
+
+/* ---- k-mer tally ----------------------------------------------------------
+ * Assembler.addRead/addToPileups for every window (S/Assembler.scala:55-87)
+ * followed by buildGraph (S/Assembler.scala:132-154), K <= 32.  Returns the
+ * edges of all windows; *n_edges receives the count (up to cap). */
+pg_status pg_kmer_tally(pg_ctx *ctx, const pg_window *windows, int32_t n_windows,
+                        int32_t K, const pg_params *params, int32_t min_depth,
+                        pg_kmer_edge *edges, int64_t cap, int64_t *n_edges);
+
+/* ---- timing -------------------------------------------------------------
+ * Milliseconds of the dominant (pileup walk) kernel in the last
+ * pg_pileup_regions call, measured with CUDA events on the context stream,
+ * and its launch count. */
+pg_status pg_last_kernel_ms(pg_ctx *ctx, double *walk_ms, double *total_ms, int32_t *launches);
+/* Synchronises the context stream. */
+pg_status pg_sync(pg_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PILON_GB300_H */

@@ -1,0 +1,741 @@
+// pg_api.cu — the C ABI of include/pilon_gb300.h: context, device memory,
+// the pipeline driver and result transfer.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pg_internal.cuh"
+#include "pg_kmer.cuh"
+
+using namespace pg;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+}  // namespace
+
+struct pg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // reference
+  DevBuf ref;
+  std::vector<int64_t> ref_off, ref_len;
+  // reads
+  Reads R{};
+  bool have_reads = false;
+  DevBuf rd[15];
+  ReadExtent ext{};
+  DevBuf d_ext;
+  // per-call buffers
+  DevBuf regions, walk_tiles, call_tile_region, chunks, stats;
+  DevBuf rec_count, rec_qsum, rec_i32[10], rec_call, rec_score, rec_indel_len, rec_ins_str;
+  DevBuf bucket_count, bucket_off, bucket_fill, cand_count, cand_off, tile_sums;
+  DevBuf events, events_sorted, cands, pool, counters, run_max;
+  int64_t event_cap = 0, pool_cap = 0;
+  int32_t cand_cap = 0;
+  DevBuf staging_dev;
+  void* staging_host = nullptr;
+  size_t staging_cap = 0;
+  // last call
+  std::vector<RegionDev> regions_h;
+  std::vector<StatsDev> stats_h;
+  int32_t n_regions = 0;
+  int64_t n_positions = 0;
+  bool have_results = false;
+  int32_t n_call_tiles = 0;
+  // timing
+  cudaEvent_t e0 = nullptr, e1 = nullptr, w0 = nullptr, w1 = nullptr;
+  std::vector<cudaEvent_t> wev;  // pairs around each walk launch
+  int32_t n_runs = 0;
+  double walk_ms = 0, total_ms = 0;
+  int32_t launches = 0;
+  // k-mer tally
+  DevBuf kwin, kpre, kslot_base, kslot_cap, kx_base, kx_cap, kkeys, kcnt, kqs, kmq, kq;
+  DevBuf kx_keys, kx_used, kx_cnt, kx_qs, kx_mq, kx_q, kedges, kcount;
+  // tuning
+  int32_t tile_width = 2048, warps = 16;
+};
+
+namespace {
+
+pg_status fail(pg_ctx* c, pg_status s, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return s;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(c, PG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));        \
+  } while (0)
+
+pg_status ensure(pg_ctx* c, DevBuf& b, size_t bytes) {
+  if (bytes <= b.cap && b.p) return PG_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+  size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+  cudaError_t e = cudaMalloc(&b.p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, PG_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", want, cudaGetErrorString(e));
+  }
+  b.cap = want;
+  return PG_OK;
+}
+
+void release(DevBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+}
+
+template <class T>
+T* P(DevBuf& b) {
+  return (T*)b.p;
+}
+
+DevParams to_dev(const pg_params* p) {
+  DevParams d;
+  d.min_mq = p->min_mq; d.min_qual = p->min_qual; d.flank = p->flank; d.default_qual = p->default_qual;
+  d.min_min_depth = p->min_min_depth; d.nonpf = p->nonpf; d.duplicates = p->duplicates;
+  d.old_indel = p->old_indel; d.fix_amb = p->fix_amb; d.long_read = p->long_read; d.bam_type = p->bam_type;
+  d.long_read_only = p->long_read_only; d.min_depth = p->min_depth;
+  d.huge = 5 * (p->bam_type == PG_BAM_FRAGS ? 500 : 10000);
+  return d;
+}
+
+Records records(pg_ctx* c) {
+  Records r;
+  r.count = P<int4>(c->rec_count);
+  r.qual_sum = P<longlong2>(c->rec_qsum);
+  r.mq_sum = P<int32_t>(c->rec_i32[0]);
+  r.q_sum = P<int32_t>(c->rec_i32[1]);
+  r.bad_pair = P<int32_t>(c->rec_i32[2]);
+  r.clips = P<int32_t>(c->rec_i32[3]);
+  r.deletions = P<int32_t>(c->rec_i32[4]);
+  r.del_qual = P<int32_t>(c->rec_i32[5]);
+  r.insertions = P<int32_t>(c->rec_i32[6]);
+  r.ins_qual = P<int32_t>(c->rec_i32[7]);
+  r.phys_cov = P<int32_t>(c->rec_i32[8]);
+  r.insert_size = P<int32_t>(c->rec_i32[9]);
+  r.call = P<uint32_t>(c->rec_call);
+  r.score = P<int64_t>(c->rec_score);
+  r.indel_len = P<int32_t>(c->rec_indel_len);
+  r.ins_str = P<int32_t>(c->rec_ins_str);
+  return r;
+}
+
+// Counters kept on the device for one call: [0] events, [1] pool bytes.
+enum { CNT_EVENTS = 0, CNT_POOL = 1, CNT_N = 2 };
+// run_max: [0] max events of a run, [1] max candidates of a run
+__global__ void k_track(const unsigned long long* counters, const int32_t* cand_total, unsigned long long* run_max) {
+  atomicMax(&run_max[0], counters[CNT_EVENTS]);
+  atomicMax(&run_max[1], (unsigned long long)(*cand_total));
+}
+
+struct Plan {
+  std::vector<WalkTile> walk;
+  std::vector<int32_t> call_region;
+  std::vector<ReadChunk> chunks;
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* pg_version(void) { return "pilon_gb300 0.1 (sm_103a)"; }
+
+void pg_default_params(pg_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof *p);
+  p->min_mq = 0;
+  p->min_qual = 0;
+  p->flank = 10;
+  p->default_qual = 10;
+  p->min_min_depth = 5;
+  p->min_depth = 0.1;
+  p->bam_type = PG_BAM_FRAGS;
+}
+
+pg_status pg_open(pg_ctx** out, int device) {
+  if (!out) return PG_ERR_ARG;
+  *out = nullptr;
+  pg_ctx* c = new pg_ctx();
+  c->device = device;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    cudaGetLastError();
+    *out = c;
+    return fail(c, PG_ERR_CUDA, "no CUDA device %d", device);
+  }
+  cudaSetDevice(device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    *out = c;
+    return fail(c, PG_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  cudaEventCreate(&c->e0);
+  cudaEventCreate(&c->e1);
+  cudaEventCreate(&c->w0);
+  cudaEventCreate(&c->w1);
+  *out = c;
+  return PG_OK;
+}
+
+void pg_close(pg_ctx* c) {
+  if (!c) return;
+  if (c->stream) {
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+  }
+  DevBuf* all[] = {&c->ref, &c->d_ext, &c->regions, &c->walk_tiles, &c->call_tile_region, &c->chunks, &c->stats,
+                   &c->rec_count, &c->rec_qsum, &c->rec_call, &c->rec_score, &c->rec_indel_len, &c->rec_ins_str,
+                   &c->bucket_count, &c->bucket_off, &c->bucket_fill, &c->cand_count, &c->cand_off, &c->tile_sums,
+                   &c->events, &c->events_sorted, &c->cands, &c->pool, &c->counters, &c->run_max, &c->staging_dev};
+  for (DevBuf* b : all) release(*b);
+  DevBuf* km[] = {&c->kwin, &c->kpre, &c->kslot_base, &c->kslot_cap, &c->kx_base, &c->kx_cap, &c->kkeys, &c->kcnt,
+                  &c->kqs, &c->kmq, &c->kq, &c->kx_keys, &c->kx_used, &c->kx_cnt, &c->kx_qs, &c->kx_mq, &c->kx_q,
+                  &c->kedges, &c->kcount};
+  for (DevBuf* b : km) release(*b);
+  for (auto& b : c->rec_i32) release(b);
+  for (auto& b : c->rd) release(b);
+  if (c->staging_host) cudaFreeHost(c->staging_host);
+  if (c->e0) cudaEventDestroy(c->e0);
+  if (c->e1) cudaEventDestroy(c->e1);
+  if (c->w0) cudaEventDestroy(c->w0);
+  if (c->w1) cudaEventDestroy(c->w1);
+  for (cudaEvent_t e : c->wev) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* pg_last_error(const pg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+pg_status pg_set_tuning(pg_ctx* c, int32_t tile_width, int32_t warps_per_cta) {
+  if (!c) return PG_ERR_ARG;
+  if (tile_width) {
+    if (tile_width < 256 || tile_width > 4096 || (tile_width & (tile_width - 1)))
+      return fail(c, PG_ERR_ARG, "tile width %d must be a power of two in [256, 4096]", tile_width);
+    c->tile_width = tile_width;
+  }
+  if (warps_per_cta) {
+    if (warps_per_cta < 1 || warps_per_cta > 16) return fail(c, PG_ERR_ARG, "warps per CTA must be in [1, 16]");
+    c->warps = warps_per_cta;
+  }
+  return PG_OK;
+}
+
+pg_status pg_sync(pg_ctx* c) {
+  if (!c) return PG_ERR_ARG;
+  cudaSetDevice(c->device);
+  CK(cudaStreamSynchronize(c->stream));
+  return PG_OK;
+}
+
+pg_status pg_set_reference(pg_ctx* c, int32_t n, const int64_t* lens, const uint8_t* const* bases) {
+  if (!c || n < 0 || (n > 0 && (!lens || !bases))) return fail(c, PG_ERR_ARG, "bad reference arguments");
+  cudaSetDevice(c->device);
+  c->ref_off.assign(n, 0);
+  c->ref_len.assign(lens, lens + n);
+  int64_t total = 0;
+  for (int i = 0; i < n; i++) {
+    if (lens[i] < 0 || (lens[i] > 0 && !bases[i])) return fail(c, PG_ERR_ARG, "contig %d has no bases", i);
+    c->ref_off[i] = total;
+    total += lens[i];
+  }
+  pg_status s = ensure(c, c->ref, (size_t)std::max<int64_t>(total, 1));
+  if (s) return s;
+  for (int i = 0; i < n; i++)
+    if (lens[i] > 0)
+      CK(cudaMemcpyAsync(P<uint8_t>(c->ref) + c->ref_off[i], bases[i], lens[i], cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return PG_OK;
+}
+
+static pg_status finish_reads(pg_ctx* c) {
+  c->have_reads = false;
+  pg_status s = ensure(c, c->d_ext, sizeof(ReadExtent));
+  if (s) return s;
+  launch_read_extent(c->R, P<ReadExtent>(c->d_ext), c->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(&c->ext, c->d_ext.p, sizeof(ReadExtent), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->ext.bad_read)
+    return fail(c, PG_ERR_ARG, "read %llu: CIGAR, base or quality offsets leave their arrays",
+                (unsigned long long)c->ext.bad_read - 1);
+  if (c->ext.unsorted) return fail(c, PG_ERR_ARG, "reads are not sorted by position within each reference");
+  c->have_reads = true;
+  c->have_results = false;
+  return PG_OK;
+}
+
+pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
+  if (!c || !h || h->n_reads < 0) return fail(c, PG_ERR_ARG, "bad reads");
+  cudaSetDevice(c->device);
+  const int64_t n = h->n_reads;
+  const void* src[15] = {h->pos, h->aend, h->tlen, h->ref_id, h->mate_ref_id, h->l_seq, h->flag, h->n_cigar,
+                         h->mapq, h->seq, h->qual, h->cigar_off, h->seq_off, h->qual_off, h->cigar};
+  const size_t bytes[15] = {(size_t)n * 4, (size_t)n * 4, (size_t)n * 4, (size_t)n * 4, (size_t)n * 4,
+                            (size_t)n * 4, (size_t)n * 2, (size_t)n * 2, (size_t)n,
+                            (size_t)h->seq_bytes, (size_t)h->qual_bytes, (size_t)n * 8, (size_t)n * 8,
+                            (size_t)n * 8, (size_t)h->n_cigar_words * 4};
+  for (int k = 0; k < 15; k++) {
+    if (bytes[k] && !src[k]) return fail(c, PG_ERR_ARG, "reads field %d is null", k);
+    pg_status s = ensure(c, c->rd[k], std::max<size_t>(bytes[k], 16));
+    if (s) return s;
+    if (bytes[k]) CK(cudaMemcpyAsync(c->rd[k].p, src[k], bytes[k], cudaMemcpyHostToDevice, c->stream));
+  }
+  Reads& R = c->R;
+  R.n = n;
+  R.pos = P<int32_t>(c->rd[0]); R.aend = P<int32_t>(c->rd[1]); R.tlen = P<int32_t>(c->rd[2]);
+  R.ref_id = P<int32_t>(c->rd[3]); R.mate_ref_id = P<int32_t>(c->rd[4]); R.l_seq = P<int32_t>(c->rd[5]);
+  R.flag = P<uint16_t>(c->rd[6]); R.n_cigar = P<uint16_t>(c->rd[7]); R.mapq = P<uint8_t>(c->rd[8]);
+  R.seq = P<uint8_t>(c->rd[9]); R.qual = P<uint8_t>(c->rd[10]); R.cigar_off = P<int64_t>(c->rd[11]);
+  R.seq_off = P<int64_t>(c->rd[12]); R.qual_off = P<int64_t>(c->rd[13]); R.cigar = P<uint32_t>(c->rd[14]);
+  R.n_cigar_words = h->n_cigar_words; R.seq_bytes = h->seq_bytes; R.qual_bytes = h->qual_bytes;
+  return finish_reads(c);
+}
+
+pg_status pg_set_reads_device(pg_ctx* c, const pg_reads* d) {
+  if (!c || !d || d->n_reads < 0) return fail(c, PG_ERR_ARG, "bad reads");
+  cudaSetDevice(c->device);
+  Reads& R = c->R;
+  R.n = d->n_reads;
+  R.pos = d->pos; R.aend = d->aend; R.tlen = d->tlen; R.ref_id = d->ref_id; R.mate_ref_id = d->mate_ref_id;
+  R.l_seq = d->l_seq; R.flag = d->flag; R.n_cigar = d->n_cigar; R.mapq = d->mapq; R.seq = d->seq;
+  R.qual = d->qual; R.cigar_off = d->cigar_off; R.seq_off = d->seq_off; R.qual_off = d->qual_off;
+  R.cigar = d->cigar;
+  R.n_cigar_words = d->n_cigar_words; R.seq_bytes = d->seq_bytes; R.qual_bytes = d->qual_bytes;
+  return finish_reads(c);
+}
+
+static pg_status stage(pg_ctx* c, size_t bytes) {
+  if (bytes <= c->staging_cap) return PG_OK;
+  if (c->staging_host) cudaFreeHost(c->staging_host);
+  c->staging_host = nullptr;
+  size_t want = bytes + bytes / 4 + 4096;
+  if (cudaMallocHost(&c->staging_host, want) != cudaSuccess) {
+    c->staging_cap = 0;
+    cudaGetLastError();
+    return fail(c, PG_ERR_NOMEM, "cudaMallocHost of %zu bytes failed", want);
+  }
+  c->staging_cap = want;
+  return ensure(c, c->staging_dev, want);
+}
+
+// Runs the pipeline for regions [r0, r1) (tiles and chunks of those regions).
+static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const DevParams& dp) {
+  cudaStream_t s = c->stream;
+  const RegionDev& a = c->regions_h[r0];
+  const RegionDev& b = c->regions_h[r1 - 1];
+  const int32_t w0 = a.walk_tile0, wn = b.walk_tile0 + b.n_walk_tiles - w0;
+  const int32_t t0 = a.call_tile0, tn = b.call_tile0 + b.n_call_tiles - t0;
+  int32_t ch0 = -1, chn = 0;
+  for (int32_t k = 0; k < (int32_t)plan.chunks.size(); k++) {  // chunks are in region order
+    if (plan.chunks[k].region >= r0 && plan.chunks[k].region < r1) {
+      if (ch0 < 0) ch0 = k;
+      chn++;
+    }
+  }
+  if (ch0 < 0) ch0 = 0;
+  RegionDev* d_regions = P<RegionDev>(c->regions);
+  StatsDev* d_stats = P<StatsDev>(c->stats);
+  Records rec = records(c);
+  unsigned long long* counters = P<unsigned long long>(c->counters);
+
+  cudaMemsetAsync(P<int32_t>(c->bucket_count) + t0, 0, sizeof(int32_t) * (tn + 1), s);
+  cudaMemsetAsync(P<int32_t>(c->bucket_fill) + t0, 0, sizeof(int32_t) * (tn + 1), s);
+  cudaMemsetAsync(P<int32_t>(c->cand_count) + t0, 0, sizeof(int32_t) * (tn + 1), s);
+  cudaMemsetAsync(&counters[CNT_EVENTS], 0, sizeof(unsigned long long), s);
+
+  launch_tile_ranges(c->R, d_regions, P<WalkTile>(c->walk_tiles) + w0, wn, P<ReadExtent>(c->d_ext), s);
+
+  WalkArgs wa;
+  wa.R = c->R; wa.regions = d_regions; wa.tiles = P<WalkTile>(c->walk_tiles); wa.n_tiles = wn;
+  wa.rec = rec; wa.stats = d_stats; wa.P = dp; wa.ref = P<uint8_t>(c->ref); wa.tile_width = c->tile_width;
+  while ((int32_t)c->wev.size() < 2 * (c->n_runs + 1)) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    c->wev.push_back(e);
+  }
+  cudaEventRecord(c->wev[2 * c->n_runs], s);
+  launch_walk(wa, w0, wn, c->warps, s);
+  cudaEventRecord(c->wev[2 * c->n_runs + 1], s);
+  c->n_runs++;
+  c->launches += wn > 0;
+
+  EventArgs ea;
+  ea.R = c->R; ea.regions = d_regions; ea.chunks = P<ReadChunk>(c->chunks); ea.n_chunks = chn; ea.rec = rec;
+  ea.stats = d_stats; ea.P = dp; ea.ref = P<uint8_t>(c->ref); ea.events = P<Event>(c->events);
+  ea.n_events = &counters[CNT_EVENTS]; ea.event_cap = c->event_cap; ea.bucket_count = P<int32_t>(c->bucket_count);
+  launch_read_events(ea, ch0, chn, s);
+  c->launches += chn > 0;
+
+  launch_region_prep(d_regions + r0, d_stats + r0, r1 - r0, dp, s);
+  launch_scan_small(P<int32_t>(c->bucket_count) + t0, P<int32_t>(c->bucket_off) + t0, tn, s);
+  launch_event_scatter(P<Event>(c->events), &counters[CNT_EVENTS], d_regions, P<int32_t>(c->bucket_off),
+                       P<int32_t>(c->bucket_fill), P<Event>(c->events_sorted), s, c->event_cap);
+  launch_physcov_scan(d_regions, P<int32_t>(c->call_tile_region), t0, tn, rec, d_stats, P<int32_t>(c->tile_sums),
+                      r0, r1 - r0, s);
+
+  CallArgs ca;
+  ca.R = c->R; ca.regions = d_regions; ca.call_tile_region = P<int32_t>(c->call_tile_region);
+  ca.n_call_tiles = tn; ca.rec = rec; ca.stats = d_stats; ca.P = dp; ca.ref = P<uint8_t>(c->ref);
+  ca.ev_sorted = P<Event>(c->events_sorted); ca.bucket_off = P<int32_t>(c->bucket_off);
+  ca.event_cap = c->event_cap;
+  ca.cand_count = P<int32_t>(c->cand_count); ca.pool = P<char>(c->pool); ca.pool_fill = &counters[CNT_POOL];
+  ca.pool_cap = c->pool_cap;
+  launch_call(ca, t0, tn, s);
+  launch_scan_small(P<int32_t>(c->cand_count) + t0, P<int32_t>(c->cand_off) + t0, tn, s);
+  launch_cand_list(ca, P<int32_t>(c->cand_off), P<Cand>(c->cands), c->cand_cap, t0, tn, s);
+  launch_resolve(d_regions + r0, r1 - r0, P<int32_t>(c->cand_off), P<Cand>(c->cands), c->cand_cap, d_stats + r0, s);
+  launch_apply_spans(ca, P<Cand>(c->cands), P<int32_t>(c->cand_off) + t0 + tn, c->cand_cap, s);
+  k_track<<<1, 1, 0, s>>>(counters, P<int32_t>(c->cand_off) + t0 + tn, P<unsigned long long>(c->run_max));
+  c->launches += 12;
+}
+
+pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions, const pg_params* params,
+                            int32_t batched) {
+  if (!c || (n_regions > 0 && !regs) || !params || n_regions < 0) return fail(c, PG_ERR_ARG, "bad arguments");
+  if (!c->have_reads) return fail(c, PG_ERR_STATE, "pg_set_reads must come first");
+  if (params->min_qual < 0 || params->flank < 0 || params->min_mq < 0)
+    return fail(c, PG_ERR_ARG, "min_qual, min_mq and flank must be >= 0");
+  cudaSetDevice(c->device);
+  c->have_results = false;
+  const int T = c->tile_width;
+  // ---- plan
+  Plan plan;
+  c->regions_h.resize(n_regions);
+  int64_t pos = 0;
+  for (int32_t r = 0; r < n_regions; r++) {
+    const pg_region& q = regs[r];
+    if (q.contig < 0 || q.contig >= (int32_t)c->ref_len.size())
+      return fail(c, PG_ERR_ARG, "region %d: contig %d out of range", r, q.contig);
+    const int64_t clen = c->ref_len[q.contig];
+    if (q.start < 1 || q.stop < q.start || q.stop > clen)
+      return fail(c, PG_ERR_ARG, "region %d: [%d, %d] outside contig of length %lld", r, q.start, q.stop,
+                  (long long)clen);
+    if (q.read_begin < 0 || q.read_end < q.read_begin || q.read_end > c->R.n)
+      return fail(c, PG_ERR_ARG, "region %d: read range out of bounds", r);
+    RegionDev& g = c->regions_h[r];
+    g.contig = q.contig; g.start = q.start; g.stop = q.stop; g.size = q.stop - q.start + 1;
+    g.pos_base = pos; g.ref_off = c->ref_off[q.contig]; g.contig_len = clen;
+    g.read_begin = q.read_begin; g.read_end = q.read_end;
+    g.qs = (int32_t)std::max<int64_t>((int64_t)q.start - 10000, 0);
+    g.qe = (int32_t)std::min<int64_t>((int64_t)q.stop + 10000, clen);
+    g.walk_tile0 = (int32_t)plan.walk.size();
+    g.n_walk_tiles = (g.size + T - 1) / T;
+    for (int32_t k = 0; k < g.n_walk_tiles; k++)
+      plan.walk.push_back(WalkTile{r, k * T, std::min(T, g.size - k * T), 0, 0, 0});
+    g.call_tile0 = (int32_t)plan.call_region.size();
+    g.n_call_tiles = (g.size + kCallTile - 1) / kCallTile;
+    for (int32_t k = 0; k < g.n_call_tiles; k++) plan.call_region.push_back(r);
+    for (int64_t lo = q.read_begin; lo < q.read_end; lo += kReadsPerChunk)
+      plan.chunks.push_back(ReadChunk{r, 0, lo, std::min<int64_t>(lo + kReadsPerChunk, q.read_end)});
+    pos += g.size;
+  }
+  c->n_regions = n_regions;
+  c->n_positions = pos;
+  const int32_t n_call = (int32_t)plan.call_region.size();
+  c->n_call_tiles = n_call;
+  if (n_regions == 0) {
+    c->have_results = true;
+    return PG_OK;
+  }
+  // ---- buffers
+  pg_status s;
+#define EN(buf, bytes) \
+  if ((s = ensure(c, buf, (bytes)))) return s;
+  EN(c->regions, sizeof(RegionDev) * n_regions);
+  EN(c->stats, sizeof(StatsDev) * n_regions);
+  EN(c->walk_tiles, sizeof(WalkTile) * std::max<size_t>(plan.walk.size(), 1));
+  EN(c->call_tile_region, sizeof(int32_t) * (n_call + 1));
+  EN(c->chunks, sizeof(ReadChunk) * std::max<size_t>(plan.chunks.size(), 1));
+  EN(c->rec_count, 16 * (size_t)pos);
+  EN(c->rec_qsum, 32 * (size_t)pos);
+  for (auto& b : c->rec_i32) EN(b, 4 * (size_t)pos);
+  EN(c->rec_call, 4 * (size_t)pos);
+  EN(c->rec_score, 8 * (size_t)pos);
+  EN(c->rec_indel_len, 4 * (size_t)pos);
+  EN(c->rec_ins_str, 4 * (size_t)pos);
+  for (DevBuf* b : {&c->bucket_count, &c->bucket_off, &c->bucket_fill, &c->cand_count, &c->cand_off})
+    EN(*b, sizeof(int32_t) * (n_call + 2));
+  EN(c->tile_sums, sizeof(int32_t) * 2 * (n_call + 1));
+  EN(c->counters, sizeof(unsigned long long) * CNT_N);
+  EN(c->run_max, sizeof(unsigned long long) * 2);
+  if (c->event_cap == 0) c->event_cap = (int64_t)(2 * c->ext.n_indel_ops + 4096);
+  if (c->cand_cap == 0) c->cand_cap = (int32_t)std::min<int64_t>(pos / 16 + 4096, INT32_MAX / 2);
+  if (c->pool_cap == 0) c->pool_cap = 1 << 20;
+  // ---- upload the plan
+  const size_t b_reg = sizeof(RegionDev) * n_regions, b_walk = sizeof(WalkTile) * plan.walk.size(),
+               b_call = sizeof(int32_t) * n_call, b_ch = sizeof(ReadChunk) * plan.chunks.size();
+  if ((s = stage(c, b_reg + b_walk + b_call + b_ch + 64))) return s;
+  {
+    char* h = (char*)c->staging_host;
+    memcpy(h, c->regions_h.data(), b_reg);
+    memcpy(h + b_reg, plan.walk.data(), b_walk);
+    memcpy(h + b_reg + b_walk, plan.call_region.data(), b_call);
+    memcpy(h + b_reg + b_walk + b_call, plan.chunks.data(), b_ch);
+  }
+  const DevParams dp = to_dev(params);
+  for (int attempt = 0; attempt < 4; attempt++) {
+    if ((s = ensure(c, c->events, sizeof(Event) * c->event_cap))) return s;
+    if ((s = ensure(c, c->events_sorted, sizeof(Event) * c->event_cap))) return s;
+    if ((s = ensure(c, c->cands, sizeof(Cand) * (size_t)c->cand_cap))) return s;
+    if ((s = ensure(c, c->pool, (size_t)c->pool_cap))) return s;
+    cudaStream_t st = c->stream;
+    c->launches = 0;
+    c->n_runs = 0;
+    CK(cudaEventRecord(c->e0, st));
+    CK(cudaMemcpyAsync(c->regions.p, c->staging_host, b_reg, cudaMemcpyHostToDevice, st));
+    if (b_walk) CK(cudaMemcpyAsync(c->walk_tiles.p, (char*)c->staging_host + b_reg, b_walk, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->call_tile_region.p, (char*)c->staging_host + b_reg + b_walk, b_call, cudaMemcpyHostToDevice, st));
+    if (b_ch) CK(cudaMemcpyAsync(c->chunks.p, (char*)c->staging_host + b_reg + b_walk + b_call, b_ch,
+                                 cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(c->stats.p, 0, sizeof(StatsDev) * n_regions, st));
+    CK(cudaMemsetAsync(c->counters.p, 0, sizeof(unsigned long long) * CNT_N, st));
+    CK(cudaMemsetAsync(c->run_max.p, 0, sizeof(unsigned long long) * 2, st));
+    c->walk_ms = 0;
+    if (batched || n_regions == 1) {
+      CK(cudaEventRecord(c->w0, st));
+      run_range(c, plan, 0, n_regions, dp);
+      CK(cudaEventRecord(c->w1, st));
+    } else {
+      CK(cudaEventRecord(c->w0, st));
+      for (int32_t r = 0; r < n_regions; r++) run_range(c, plan, r, r + 1, dp);
+      CK(cudaEventRecord(c->w1, st));
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(c->e1, st));
+    c->stats_h.resize(n_regions);
+    unsigned long long hc[CNT_N], hm[2];
+    CK(cudaMemcpyAsync(c->stats_h.data(), c->stats.p, sizeof(StatsDev) * n_regions, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hc, c->counters.p, sizeof hc, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hm, c->run_max.p, sizeof hm, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->e0, c->e1);
+    c->total_ms = ms;
+    c->walk_ms = 0;
+    for (int32_t k = 0; k < c->n_runs; k++) {
+      cudaEventElapsedTime(&ms, c->wev[2 * k], c->wev[2 * k + 1]);
+      c->walk_ms += ms;
+    }
+    bool grow = false;
+    if ((int64_t)hm[0] > c->event_cap) { c->event_cap = (int64_t)hm[0] * 2 + 4096; grow = true; }
+    if ((int64_t)hm[1] > c->cand_cap) { c->cand_cap = (int32_t)std::min<int64_t>((int64_t)hm[1] * 2 + 4096, INT32_MAX / 2); grow = true; }
+    if ((int64_t)hc[CNT_POOL] > c->pool_cap) { c->pool_cap = (int64_t)hc[CNT_POOL] * 2 + 4096; grow = true; }
+    if (!grow) {
+      for (int32_t r = 0; r < n_regions; r++)
+        if (c->stats_h[r].error)
+          return fail(c, PG_ERR_INDEX, "region %d: an indel left shift left the region (the reference throws "
+                      "ArrayIndexOutOfBoundsException here)", r);
+      c->have_results = true;
+      return PG_OK;
+    }
+  }
+  return fail(c, PG_ERR_LIMIT, "event/candidate buffers kept overflowing");
+}
+
+pg_status pg_fetch_stats(pg_ctx* c, int32_t r, pg_region_stats* out) {
+  if (!c || !out) return PG_ERR_ARG;
+  if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
+  if (r < 0 || r >= c->n_regions) return fail(c, PG_ERR_ARG, "region %d out of range", r);
+  const StatsDev& s = c->stats_h[r];
+  memset(out, 0, sizeof *out);
+  out->base_count = (int64_t)s.base_count;
+  out->read_count = (int64_t)s.read_count;
+  out->phys_cov_start = s.phys_cov_start;
+  out->insert_size_start = s.insert_size_start;
+  out->min_depth = s.min_depth;
+  out->n_changes = s.n_changes;
+  out->fr_count = (int64_t)s.fr_count; out->fr_sum = (int64_t)s.fr_sum; out->fr_sumsq = (int64_t)s.fr_sumsq;
+  out->rf_count = (int64_t)s.rf_count; out->rf_sum = (int64_t)s.rf_sum; out->rf_sumsq = (int64_t)s.rf_sumsq;
+  out->error = s.error;
+  out->n_ins_strings = 0;
+  return PG_OK;
+}
+
+pg_status pg_fetch_region(pg_ctx* c, int32_t r, pg_region_out* o) {
+  if (!c || !o) return PG_ERR_ARG;
+  if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
+  if (r < 0 || r >= c->n_regions) return fail(c, PG_ERR_ARG, "region %d out of range", r);
+  cudaSetDevice(c->device);
+  const RegionDev& g = c->regions_h[r];
+  const size_t n = (size_t)g.size;
+  const int64_t b = g.pos_base;
+  cudaStream_t s = c->stream;
+  Records rc = records(c);
+  auto cp = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    if (!dst) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+  };
+  CK(cp(o->count, rc.count + b, 16 * n));
+  CK(cp(o->qual_sum, rc.qual_sum + 2 * b, 32 * n));
+  CK(cp(o->mq_sum, rc.mq_sum + b, 4 * n));
+  CK(cp(o->q_sum, rc.q_sum + b, 4 * n));
+  CK(cp(o->phys_cov, rc.phys_cov + b, 4 * n));
+  CK(cp(o->insert_size, rc.insert_size + b, 4 * n));
+  CK(cp(o->bad_pair, rc.bad_pair + b, 4 * n));
+  CK(cp(o->deletions, rc.deletions + b, 4 * n));
+  CK(cp(o->del_qual, rc.del_qual + b, 4 * n));
+  CK(cp(o->insertions, rc.insertions + b, 4 * n));
+  CK(cp(o->ins_qual, rc.ins_qual + b, 4 * n));
+  CK(cp(o->clips, rc.clips + b, 4 * n));
+  CK(cp(o->call, rc.call + b, 4 * n));
+  CK(cp(o->score, rc.score + b, 8 * n));
+  CK(cp(o->indel_len, rc.indel_len + b, 4 * n));
+  CK(cp(o->ins_str, rc.ins_str + b, 4 * n));
+  unsigned long long pool_fill = 0;
+  CK(cudaMemcpyAsync(&pool_fill, P<unsigned long long>(c->counters) + CNT_POOL, sizeof pool_fill,
+                     cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (o->ins_chars) {
+    if ((int64_t)pool_fill > o->ins_chars_cap)
+      return fail(c, PG_ERR_LIMIT, "ins_chars needs %llu bytes", (unsigned long long)pool_fill);
+    if (pool_fill) CK(cudaMemcpyAsync(o->ins_chars, c->pool.p, pool_fill, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  o->ins_chars_cap = (int64_t)pool_fill;
+  return PG_OK;
+}
+
+static int64_t next_pow2(int64_t x) {
+  int64_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K, const pg_params* params,
+                        int32_t min_depth, pg_kmer_edge* edges, int64_t cap, int64_t* n_edges) {
+  if (!c || (n_windows > 0 && !windows) || !params || n_windows < 0 || cap < 0 || !n_edges)
+    return fail(c, PG_ERR_ARG, "bad arguments");
+  if (K < 1 || K > 31) return fail(c, PG_ERR_LIMIT, "K = %d: the GPU tally packs K-mers in 64 bits (K <= 31)", K);
+  if (min_depth < 1) return fail(c, PG_ERR_ARG, "min_depth must be >= 1");
+  if (params->min_qual < 0) return fail(c, PG_ERR_ARG, "min_qual must be >= 0");
+  if (!c->have_reads) return fail(c, PG_ERR_STATE, "pg_set_reads must come first");
+  cudaSetDevice(c->device);
+  *n_edges = 0;
+  if (n_windows == 0) return PG_OK;
+  for (int32_t w = 0; w < n_windows; w++)
+    if (windows[w].read_begin < 0 || windows[w].read_end < windows[w].read_begin || windows[w].read_end > c->R.n)
+      return fail(c, PG_ERR_ARG, "window %d: read range out of bounds", w);
+  cudaStream_t st = c->stream;
+  pg_status s;
+  if ((s = ensure(c, c->kwin, sizeof(pg_window) * n_windows))) return s;
+  if ((s = ensure(c, c->kpre, sizeof(long long) * 3 * n_windows))) return s;
+  CK(cudaMemcpyAsync(c->kwin.p, windows, sizeof(pg_window) * n_windows, cudaMemcpyHostToDevice, st));
+  launch_kmer_prepass(c->R, P<pg_window>(c->kwin), n_windows, K, P<long long>(c->kpre), st);
+  std::vector<long long> pre(3 * (size_t)n_windows);
+  CK(cudaMemcpyAsync(pre.data(), c->kpre.p, sizeof(long long) * pre.size(), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::vector<int64_t> sbase(n_windows), scap(n_windows), xbase(n_windows), xcap(n_windows);
+  for (int32_t w = 0; w < n_windows; w++) {
+    // Assembler.addRead prunes K-mers with count < 2 every 100,000 reads
+    // (S/Assembler.scala:74), which makes the tally order dependent.
+    if (pre[3 * w] >= 100000)
+      return fail(c, PG_ERR_LIMIT, "window %d has %lld reads; the tally is exact below 100,000", w, pre[3 * w]);
+    scap[w] = next_pow2(std::max<int64_t>(64, pre[3 * w + 1] + pre[3 * w + 1] / 2));
+    xcap[w] = pre[3 * w + 2] > 0 ? next_pow2(std::max<int64_t>(16, 2 * pre[3 * w + 2])) : 0;
+  }
+  const int64_t edge_cap = std::max<int64_t>(cap, 1);
+  if ((s = ensure(c, c->kedges, sizeof(pg_kmer_edge) * edge_cap))) return s;
+  if ((s = ensure(c, c->kcount, 16))) return s;
+  CK(cudaMemsetAsync(c->kcount.p, 0, 16, st));
+  const int64_t budget = (int64_t)4 << 30;  // bytes of tables per batch
+  int32_t w0 = 0;
+  while (w0 < n_windows) {
+    int64_t ns = 0, nx = 0;
+    int32_t w1 = w0;
+    while (w1 < n_windows) {
+      int64_t ns2 = ns + scap[w1], nx2 = nx + xcap[w1];
+      if (w1 > w0 && ns2 * 64 + nx2 * 80 > budget) break;
+      sbase[w1] = ns; xbase[w1] = nx;
+      ns = ns2; nx = nx2;
+      w1++;
+    }
+    std::vector<int64_t> hb(4 * (size_t)n_windows, 0);
+    if ((s = ensure(c, c->kslot_base, 8 * (size_t)n_windows))) return s;
+    if ((s = ensure(c, c->kslot_cap, 8 * (size_t)n_windows))) return s;
+    if ((s = ensure(c, c->kx_base, 8 * (size_t)n_windows))) return s;
+    if ((s = ensure(c, c->kx_cap, 8 * (size_t)n_windows))) return s;
+    if ((s = ensure(c, c->kkeys, 8 * (size_t)ns))) return s;
+    if ((s = ensure(c, c->kcnt, 16 * (size_t)ns))) return s;
+    if ((s = ensure(c, c->kqs, 32 * (size_t)ns))) return s;
+    if ((s = ensure(c, c->kmq, 4 * (size_t)ns))) return s;
+    if ((s = ensure(c, c->kq, 4 * (size_t)ns))) return s;
+    const size_t nxs = (size_t)std::max<int64_t>(nx, 1);
+    if ((s = ensure(c, c->kx_keys, 16 * nxs))) return s;
+    if ((s = ensure(c, c->kx_used, nxs))) return s;
+    if ((s = ensure(c, c->kx_cnt, 16 * nxs))) return s;
+    if ((s = ensure(c, c->kx_qs, 32 * nxs))) return s;
+    if ((s = ensure(c, c->kx_mq, 4 * nxs))) return s;
+    if ((s = ensure(c, c->kx_q, 4 * nxs))) return s;
+    // table bases are relative to this batch; windows outside it are not touched
+    CK(cudaMemcpyAsync(c->kslot_base.p, sbase.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->kslot_cap.p, scap.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->kx_base.p, xbase.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->kx_cap.p, xcap.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(c->kkeys.p, 0xFF, 8 * (size_t)ns, st));
+    CK(cudaMemsetAsync(c->kcnt.p, 0, 16 * (size_t)ns, st));
+    CK(cudaMemsetAsync(c->kqs.p, 0, 32 * (size_t)ns, st));
+    CK(cudaMemsetAsync(c->kmq.p, 0, 4 * (size_t)ns, st));
+    CK(cudaMemsetAsync(c->kq.p, 0, 4 * (size_t)ns, st));
+    CK(cudaMemsetAsync(c->kx_used.p, 0, nxs, st));
+    CK(cudaMemsetAsync(c->kx_cnt.p, 0, 16 * nxs, st));
+    CK(cudaMemsetAsync(c->kx_qs.p, 0, 32 * nxs, st));
+    CK(cudaMemsetAsync(c->kx_mq.p, 0, 4 * nxs, st));
+    CK(cudaMemsetAsync(c->kx_q.p, 0, 4 * nxs, st));
+    KmerArgs a;
+    a.R = c->R; a.windows = P<pg_window>(c->kwin); a.win_begin = w0; a.K = K;
+    a.min_qual = params->min_qual; a.default_qual = params->default_qual; a.min_depth = min_depth;
+    a.slot_base = P<int64_t>(c->kslot_base); a.slot_cap = P<int64_t>(c->kslot_cap);
+    a.keys = P<unsigned long long>(c->kkeys); a.cnt = P<uint32_t>(c->kcnt); a.qs = P<unsigned long long>(c->kqs);
+    a.mq_sum = P<uint32_t>(c->kmq); a.q_sum = P<uint32_t>(c->kq);
+    a.x_base = P<int64_t>(c->kx_base); a.x_cap = P<int64_t>(c->kx_cap);
+    a.x_keys = P<unsigned long long>(c->kx_keys); a.x_used = P<uint8_t>(c->kx_used); a.x_cnt = P<uint32_t>(c->kx_cnt);
+    a.x_qs = P<unsigned long long>(c->kx_qs); a.x_mq = P<uint32_t>(c->kx_mq); a.x_q = P<uint32_t>(c->kx_q);
+    a.edges = P<pg_kmer_edge>(c->kedges); a.edge_cap = edge_cap;
+    a.n_edges = P<unsigned long long>(c->kcount); a.overflow = (int32_t*)(P<unsigned long long>(c->kcount) + 1);
+    launch_kmer_batch(a, w1 - w0, st);
+    CK(cudaGetLastError());
+    w0 = w1;
+  }
+  unsigned long long hc[2];
+  CK(cudaMemcpyAsync(hc, c->kcount.p, 16, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if ((int32_t)hc[1]) return fail(c, PG_ERR_LIMIT, "K-mer table overflow");
+  *n_edges = (int64_t)hc[0];
+  const int64_t ncopy = std::min<int64_t>((int64_t)hc[0], cap);
+  if (ncopy > 0 && edges) {
+    CK(cudaMemcpyAsync(edges, c->kedges.p, sizeof(pg_kmer_edge) * ncopy, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  return PG_OK;
+}
+
+pg_status pg_last_kernel_ms(pg_ctx* c, double* walk_ms, double* total_ms, int32_t* launches) {
+  if (!c) return PG_ERR_ARG;
+  if (walk_ms) *walk_ms = c->walk_ms;
+  if (total_ms) *total_ms = c->total_ms;
+  if (launches) *launches = c->launches;
+  return PG_OK;
+}
+
+}  // extern "C"

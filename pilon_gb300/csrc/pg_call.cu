@@ -1,0 +1,199 @@
+// pg_call.cu — per-position calls and pass 1 of GenomeRegion.postProcess.
+//
+//   k_call        PileUp.baseCall for every position (S/PileUp.scala:132-255) and
+//                 the pass-1 disposition (confirmed / INS / DEL / SNP / AMB,
+//                 S/GenomeRegion.scala:237-272) computed on the unmodified pileups
+//   k_cand_list   change candidates compacted in position order, per call tile
+//   k_resolve     the sequential part of pass 1: a homozygous deletion call marks
+//                 the next len-1 positions deleted, so later candidates inside an
+//                 accepted deletion are dropped (one thread per region walks its
+//                 sparse candidate list)
+//   k_apply_spans adds the deletion's count to the pileups it covers
+//                 (S/GenomeRegion.scala:261-264) and recomputes their calls
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "pg_internal.cuh"
+
+namespace pg {
+
+#define FULL 0xffffffffu
+
+__device__ inline CallCtx make_ctx(const CallArgs& a, const RegionDev& g, int32_t tile) {
+  CallCtx c;
+  c.ev = a.ev_sorted;
+  c.ev_lo = min((int64_t)a.bucket_off[tile], a.event_cap);
+  c.ev_hi = min((int64_t)a.bucket_off[tile + 1], a.event_cap);
+  c.R = a.R;
+  c.ref = a.ref;
+  c.ref_off = g.ref_off;
+  c.contig_len = g.contig_len;
+  c.pool = a.pool;
+  c.pool_fill = a.pool_fill;
+  c.pool_cap = a.pool_cap;
+  return c;
+}
+
+__global__ void __launch_bounds__(kCallTile) k_call(CallArgs a, int32_t tile_begin) {
+  const int32_t t = tile_begin + blockIdx.x;
+  const int32_t r = a.call_tile_region[t];
+  const RegionDev g = a.regions[r];
+  const int32_t p = (t - g.call_tile0) * kCallTile + threadIdx.x;
+  uint32_t change = 0;
+  if (p < g.size) {
+    const int64_t gp = g.pos_base + p;
+    PosRec rec;
+    load_rec(a.rec, gp, rec);
+    CallCtx c = make_ctx(a, g, t);
+    const int64_t locus0 = (int64_t)g.start - 1 + p;
+    CallOut o = base_call(rec, a.P, c, gp, locus0);
+    int32_t ins = -1;
+    if (o.flags & PG_CALL_INS) ins = pool_insertion(c, c.ev[o.win_event]);
+    uint32_t f = o.flags;
+    const StatsDev& st = a.stats[r];
+    if (st.read_count > 0) {
+      const int64_t n = rec.cnt[0] + rec.cnt[1] + rec.cnt[2] + rec.cnt[3];
+      const int64_t depth = n + rec.deletions;
+      const uint8_t rb = upper(a.ref[g.ref_off + locus0]);
+      const bool isIns = f & PG_CALL_INS, isDel = f & PG_CALL_DEL;
+      const bool called = (f & PG_CALL_HAS_BASE) || isIns || isDel;
+      if (depth >= st.min_depth && rb != 'N' && called) {
+        const uint8_t b = (f & PG_CALL_HAS_BASE) ? (uint8_t)"ACGT"[f & 3u] : (uint8_t)'N';
+        const uint8_t alt = (uint8_t)"ACGT"[(f >> 2) & 3u];
+        const bool homo = f & PG_CALL_HOMO, homoIndel = f & PG_CALL_HOMO_INDEL;
+        const int64_t q = n > 0 ? o.score / n : 0;
+        if (homo && b == rb && q >= 10 && !(isIns || isDel)) f |= PG_CALL_CONFIRMED;
+        else if (isIns && homoIndel) change = PG_CHANGE_INS;
+        else if (isDel && homoIndel) change = PG_CHANGE_DEL;
+        else if (b != rb && o.score > 0) {
+          if (homo) change = PG_CHANGE_SNP;
+          else if (a.P.fix_amb || alt != rb) change = PG_CHANGE_AMB;
+        }
+      }
+    }
+    f |= change << 9;
+    a.rec.call[gp] = f;
+    a.rec.score[gp] = o.score;
+    a.rec.indel_len[gp] = o.indel_len;
+    a.rec.ins_str[gp] = ins;
+  }
+  unsigned b = __ballot_sync(FULL, change != 0);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(&a.cand_count[t], __popc(b));
+}
+
+void launch_call(const CallArgs& a, int32_t tile_begin, int32_t n_tiles, cudaStream_t s) {
+  if (n_tiles <= 0) return;
+  k_call<<<n_tiles, kCallTile, 0, s>>>(a, tile_begin);
+}
+
+__global__ void __launch_bounds__(kCallTile) k_cand_list(CallArgs a, const int32_t* cand_off, Cand* cands,
+                                                          int32_t cand_cap, int32_t tile_begin) {
+  __shared__ int32_t s_warp[32];
+  const int32_t t = tile_begin + blockIdx.x;
+  const int32_t r = a.call_tile_region[t];
+  const RegionDev g = a.regions[r];
+  const int32_t p = (t - g.call_tile0) * kCallTile + threadIdx.x;
+  uint32_t kind = 0;
+  int64_t gp = 0;
+  if (p < g.size) {
+    gp = g.pos_base + p;
+    kind = PG_CALL_CHANGE(a.rec.call[gp]);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned b = __ballot_sync(FULL, kind != 0);
+  if (lane == 0) s_warp[warp] = __popc(b);
+  __syncthreads();
+  if (warp == 0) {
+    int32_t v = s_warp[lane];
+    int32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int32_t y = __shfl_up_sync(FULL, x, o);
+      if (lane >= o) x += y;
+    }
+    s_warp[lane] = x - v;
+  }
+  __syncthreads();
+  if (kind) {
+    int32_t rank = s_warp[warp] + __popc(b & ((1u << lane) - 1u));
+    Cand c;
+    c.gpos = gp;
+    c.region = r;
+    c.p = p;
+    c.kind = (int32_t)kind;
+    c.len = a.rec.indel_len[gp];
+    const int32_t slot = cand_off[t] + rank;
+    if (slot < cand_cap) cands[slot] = c;
+  }
+}
+
+void launch_cand_list(const CallArgs& a, const int32_t* cand_off, Cand* cands, int32_t cand_cap,
+                      int32_t tile_begin, int32_t n_tiles, cudaStream_t s) {
+  if (n_tiles <= 0) return;
+  k_cand_list<<<n_tiles, kCallTile, 0, s>>>(a, cand_off, cands, cand_cap, tile_begin);
+}
+
+// Pass 1 is a left-to-right scan: a candidate inside an earlier accepted
+// homozygous deletion is skipped (`!deleted(i)`); suppressed ones get kind < 0.
+__global__ void k_resolve(const RegionDev* regions, int32_t n_regions, const int32_t* cand_off, Cand* cands,
+                          int32_t cand_cap, StatsDev* stats) {
+  int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_regions) return;
+  const RegionDev& g = regions[r];
+  if (g.n_call_tiles == 0) return;
+  const int32_t lo = cand_off[g.call_tile0], hi = min(cand_off[g.call_tile0 + g.n_call_tiles], cand_cap);
+  int32_t lastEnd = -1, accepted = 0;
+  for (int32_t k = lo; k < hi; k++) {
+    Cand c = cands[k];
+    if (c.p <= lastEnd) {
+      cands[k].kind = -c.kind;
+      continue;
+    }
+    accepted++;
+    if (c.kind == PG_CHANGE_DEL) lastEnd = max(lastEnd, c.p + c.len - 1);
+  }
+  stats[r].n_changes = accepted;
+}
+
+void launch_resolve(const RegionDev* regions, int32_t n_regions, const int32_t* cand_off, Cand* cands,
+                    int32_t cand_cap, StatsDev* stats, cudaStream_t s) {
+  if (n_regions == 0) return;
+  k_resolve<<<(n_regions + 127) / 128, 128, 0, s>>>(regions, n_regions, cand_off, cands, cand_cap, stats);
+}
+
+__global__ void k_apply_spans(CallArgs a, const Cand* cands, const int32_t* cand_total, int32_t cand_cap) {
+  const int32_t n = min(*cand_total, cand_cap);
+  for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const Cand c = cands[k];
+    if (c.kind != PG_CHANGE_DEL) continue;
+    const RegionDev g = a.regions[c.region];
+    const int32_t d = a.rec.deletions[c.gpos];
+    for (int32_t j = 1; j < c.len; j++) {
+      const int32_t p = c.p + j;
+      if (p >= g.size) break;
+      const int64_t gp = g.pos_base + p;
+      a.rec.deletions[gp] = wadd(a.rec.deletions[gp], d);
+      PosRec rec;
+      load_rec(a.rec, gp, rec);
+      const int32_t tile = g.call_tile0 + p / kCallTile;
+      CallCtx cx = make_ctx(a, g, tile);
+      CallOut o = base_call(rec, a.P, cx, gp, (int64_t)g.start - 1 + p);
+      const uint32_t old = a.rec.call[gp];
+      int32_t ins = -1;
+      if (o.flags & PG_CALL_INS) ins = (old & PG_CALL_INS) ? a.rec.ins_str[gp] : pool_insertion(cx, cx.ev[o.win_event]);
+      a.rec.call[gp] = o.flags | PG_CALL_DELETED;
+      a.rec.score[gp] = o.score;
+      a.rec.indel_len[gp] = o.indel_len;
+      a.rec.ins_str[gp] = ins;
+    }
+  }
+}
+
+void launch_apply_spans(const CallArgs& a, const Cand* cands, const int32_t* cand_total, int32_t cand_cap,
+                        cudaStream_t s) {
+  if (cand_cap <= 0) return;
+  int blocks = std::min((cand_cap + 127) / 128, 152 * 4);
+  k_apply_spans<<<blocks, 128, 0, s>>>(a, cands, cand_total, cand_cap);
+}
+
+}  // namespace pg

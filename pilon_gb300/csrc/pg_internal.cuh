@@ -1,0 +1,369 @@
+// pg_internal.cuh — device data layout, shared device functions and kernel
+// entry points of the pilon_gb300 engine.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pilon_gb300.h"
+
+namespace pg {
+
+// ---------------------------------------------------------------------------
+// Layout in HBM
+//
+// Positions of all regions of one pg_pileup_regions call are concatenated
+// ("global positions"); region r owns [pos_base[r], pos_base[r] + size_r).
+// The pileup record of a position is structure-of-arrays:
+//   count     int4      A,C,G,T base counts           (PileUp.baseCount)
+//   qual_sum  int64[4]  A,C,G,T qual*(mq+1) sums      (PileUp.qualSum)
+//   mq_sum, q_sum, bad_pair, clips, deletions, del_qual, insertions,
+//   ins_qual  int32                                   (PileUp Int fields)
+//   phys_cov, insert_size int32: difference arrays during the walk, final
+//             values after the scan                   (PileUp.physCov/insertSize)
+// = 88 bytes per position, written once by the walk kernel.
+// Calls: call (uint32 PG_CALL_* flags), score (int64), indel_len (int32),
+// ins_str (int32 offset into the insertion-string pool or -1).
+// ---------------------------------------------------------------------------
+
+struct Reads {  // device pointers of the read store
+  int64_t n;
+  const int32_t *pos, *aend, *tlen, *ref_id, *mate_ref_id, *l_seq;
+  const uint16_t *flag, *n_cigar;
+  const uint8_t *mapq, *seq, *qual;
+  const int64_t *cigar_off, *seq_off, *qual_off;
+  const uint32_t *cigar;
+  int64_t n_cigar_words, seq_bytes, qual_bytes;
+};
+
+struct RegionDev {       // per region, device copy
+  int32_t contig, start, stop, size;
+  int64_t pos_base;      // first global position
+  int64_t ref_off;       // offset of the contig in the concatenated reference
+  int64_t contig_len;
+  int64_t read_begin, read_end;
+  int32_t qs, qe;        // query window of BamFile.process
+  int32_t walk_tile0, n_walk_tiles;
+  int32_t call_tile0, n_call_tiles;
+};
+
+struct StatsDev {        // per region, accumulated on the device
+  unsigned long long base_count;
+  unsigned long long read_count;
+  int32_t phys_cov_start, insert_size_start;
+  int32_t min_depth, n_changes;
+  unsigned long long fr_count, fr_sum, fr_sumsq, rf_count, rf_sum, rf_sumsq;
+  int32_t error;
+  int32_t n_ins;
+};
+
+struct WalkTile {
+  int32_t region, lo, len, pad;
+  int64_t read_lo, read_hi;
+};
+
+struct ReadChunk {       // reads [lo, hi) fed to region `region`
+  int32_t region, pad;
+  int64_t lo, hi;
+};
+
+struct Event {           // one insertion or deletion added to a pileup
+  int64_t gpos;
+  int64_t read;
+  int32_t region;
+  int32_t len;
+  int32_t roff;          // read offset of the indel (insertions)
+  int32_t kind_rot;      // bit 31: deletion; low bits: right rotation of the insertion
+};
+
+struct Cand {            // change candidate of pass 1, in position order
+  int64_t gpos;
+  int32_t region, p, kind, len;
+};
+
+struct Records {
+  int4 *count;
+  longlong2 *qual_sum;   // two longlong2 per position
+  int32_t *mq_sum, *q_sum, *bad_pair, *clips, *deletions, *del_qual, *insertions, *ins_qual;
+  int32_t *phys_cov, *insert_size;
+  uint32_t *call;
+  int64_t *score;
+  int32_t *indel_len, *ins_str;
+};
+
+struct ReadExtent {      // maxima over the read store, for tile read ranges
+  int32_t max_lead;      // max(pos - first touched position)
+  int32_t max_back;      // max(last touched position - pos)
+  unsigned long long n_indel_ops;
+  unsigned long long bad_read;  // 1 + index of a read whose offsets leave their arrays, else 0
+  int32_t unsorted;      // 1 if positions decrease within one reference
+  int32_t pad;
+};
+
+struct DevParams {
+  int32_t min_mq, min_qual, flank, default_qual, min_min_depth;
+  int32_t nonpf, duplicates, old_indel, fix_amb, long_read, bam_type, long_read_only;
+  double min_depth;
+  int32_t huge;          // 5 * maxInsertSizes(bamType) (S/BamFile.scala:192)
+};
+
+constexpr int kCallTile = 1024;     // positions per call / scan tile
+constexpr int kReadsPerChunk = 4096;
+constexpr int64_t kMaxReadsPerPass = 120000;  // keeps a tile's uint32 qual sums exact
+
+// ---- Java integer helpers (wrapping Int, truncating division) -------------
+__host__ __device__ inline int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+__host__ __device__ inline int32_t wsub(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
+__host__ __device__ inline int32_t wmul(int32_t a, int32_t b) { return (int32_t)((uint32_t)a * (uint32_t)b); }
+__host__ __device__ inline int32_t roundDivI(int32_t n, int32_t d) { return d > 0 ? wadd(n, d / 2) / d : 0; }
+__host__ __device__ inline int64_t roundDivL(int64_t n, int64_t d) { return d > 0 ? (n + d / 2) / d : 0; }
+__host__ __device__ inline int32_t pctI(int32_t n, int32_t d) { return roundDivI(wmul(100, n), d); }
+
+__device__ inline int nib_index(uint32_t nib) {  // BAM code -> A,C,G,T index or -1
+  return nib == 1 ? 0 : nib == 2 ? 1 : nib == 4 ? 2 : nib == 8 ? 3 : -1;
+}
+__device__ inline uint8_t nib_char(uint32_t nib) {
+  const char* t = "=ACMGRSVTWYHKDBN";
+  return (uint8_t)t[nib & 15];
+}
+__device__ inline uint32_t read_nib(const Reads& R, int64_t i, int32_t k) {
+  uint8_t b = R.seq[R.seq_off[i] + (k >> 1)];
+  return (k & 1) ? (b & 15u) : (b >> 4);
+}
+__device__ inline uint8_t upper(uint8_t c) { return (c >= 'a' && c <= 'z') ? (uint8_t)(c - 32) : c; }
+
+// ---- Per-position call (PileUp.BaseCall, S/PileUp.scala:132-255) -----------
+struct PosRec {
+  int64_t cnt[4], qs[4];
+  int32_t mq_sum, q_sum, deletions, del_qual, insertions, ins_qual;
+};
+
+__device__ inline void load_rec(const Records& Rc, int64_t gp, PosRec& r) {
+  int4 c = Rc.count[gp];
+  r.cnt[0] = c.x; r.cnt[1] = c.y; r.cnt[2] = c.z; r.cnt[3] = c.w;
+  longlong2 a = Rc.qual_sum[2 * gp], b = Rc.qual_sum[2 * gp + 1];
+  r.qs[0] = a.x; r.qs[1] = a.y; r.qs[2] = b.x; r.qs[3] = b.y;
+  r.mq_sum = Rc.mq_sum[gp]; r.q_sum = Rc.q_sum[gp];
+  r.deletions = Rc.deletions[gp]; r.del_qual = Rc.del_qual[gp];
+  r.insertions = Rc.insertions[gp]; r.ins_qual = Rc.ins_qual[gp];
+}
+
+// Stable descending order of four sums: first and second index.
+__device__ inline void order2(const int64_t v[4], int& o0, int& o1) {
+  o0 = 0;
+  for (int i = 1; i < 4; i++) if (v[i] > v[o0]) o0 = i;
+  o1 = o0 == 0 ? 1 : 0;
+  for (int i = 0; i < 4; i++) if (i != o0 && v[i] > v[o1]) o1 = i;
+}
+
+struct CallCtx {         // what the indel vote needs
+  const Event* ev;       // events bucketed by call tile
+  int64_t ev_lo, ev_hi;  // bucket of this position's tile (clamped to the buffer)
+  Reads R;
+  const uint8_t* ref;    // concatenated reference
+  int64_t ref_off;       // contig offset
+  int64_t contig_len;
+  char* pool;            // insertion-string pool
+  unsigned long long* pool_fill;
+  int64_t pool_cap;
+};
+
+__device__ inline uint32_t ins_char(const Reads& R, const Event& e, int32_t j) {
+  int32_t rot = e.kind_rot & 0x7fffffff;
+  int32_t k = j - rot;
+  if (k < 0) k += e.len;
+  return read_nib(R, e.read, e.roff + k);
+}
+
+__device__ inline bool same_indel(const Reads& R, const Event& a, const Event& b) {
+  if (a.len != b.len) return false;
+  if (a.kind_rot < 0) return true;  // deletions at one position: same length = same reference slice
+  for (int32_t j = 0; j < a.len; j++)
+    if (ins_char(R, a, j) != ins_char(R, b, j)) return false;
+  return true;
+}
+
+// Majority vote of hetIndelCall (S/PileUp.scala:209-247): returns the event
+// index of the winner, or -1.  The winner needs count >= 2 and a strict
+// majority, so the result does not depend on event order.
+__device__ inline int64_t indel_vote(const CallCtx& c, int64_t gp, bool del) {
+  int64_t cand = -1;
+  int64_t cnt = 0, total = 0;
+  for (int64_t k = c.ev_lo; k < c.ev_hi; k++) {
+    const Event& e = c.ev[k];
+    if (e.gpos != gp || ((e.kind_rot < 0) != del)) continue;
+    total++;
+    if (cnt == 0) { cand = k; cnt = 1; }
+    else if (same_indel(c.R, e, c.ev[cand])) cnt++;
+    else cnt--;
+  }
+  if (cand < 0) return -1;
+  int64_t win = 0;
+  for (int64_t k = c.ev_lo; k < c.ev_hi; k++) {
+    const Event& e = c.ev[k];
+    if (e.gpos != gp || ((e.kind_rot < 0) != del)) continue;
+    if (same_indel(c.R, e, c.ev[cand])) win++;
+  }
+  if (win < 2 || win <= total / 2) return -1;
+  return cand;
+}
+
+__device__ inline bool insertion_has_n(const CallCtx& c, const Event& e) {
+  for (int32_t j = 0; j < e.len; j++)
+    if (ins_char(c.R, e, j) == 15u) return true;  // 'N'
+  return false;
+}
+
+struct CallOut {
+  uint32_t flags;  // base/alt/homo/indel bits only
+  int64_t score;
+  int32_t indel_len;
+  int64_t win_event;  // winner event (insertion) or -1
+};
+
+// dloc0 = 0-based contig index of position p's locus minus one (locus - 1).
+__device__ inline CallOut base_call(const PosRec& r, const DevParams& P, const CallCtx& c, int64_t gp,
+                                    int64_t locus0) {
+  CallOut o;
+  int64_t n = r.cnt[0] + r.cnt[1] + r.cnt[2] + r.cnt[3];
+  int o0, o1;
+  if (r.q_sum > 0) order2(r.qs, o0, o1); else order2(r.cnt, o0, o1);
+  int64_t baseSum = r.qs[o0], altBaseSum = r.qs[o1];
+  int64_t total = r.qs[0] + r.qs[1] + r.qs[2] + r.qs[3];
+  int64_t homoScore = baseSum - (total - baseSum);
+  int64_t half = total / 2;
+  int64_t d1 = half - baseSum, d2 = half - altBaseSum;
+  int64_t heteroScore = total - (d1 < 0 ? -d1 : d1) - (d2 < 0 ? -d2 : d2);
+  bool homo = homoScore >= heteroScore;
+  int64_t diff = homoScore - heteroScore;
+  if (diff < 0) diff = -diff;
+  o.score = r.mq_sum > 0 ? diff * n / (int64_t)r.mq_sum : 0;
+  o.flags = (uint32_t)o0 | ((uint32_t)o1 << 2);
+  if (n > 0) o.flags |= PG_CALL_HAS_BASE;
+  if (homo) o.flags |= PG_CALL_HOMO;
+  o.indel_len = 0;
+  o.win_event = -1;
+  int64_t depth = n + r.deletions;
+  int32_t cnt32 = (int32_t)n;
+  bool indelCalled = false, homoIndel = true;
+  for (int pass = 0; pass < 2 && !indelCalled; pass++) {
+    bool del = pass == 1;
+    bool gate = del ? (r.deletions > 2 && r.deletions > r.insertions)
+                    : (r.insertions > 2 && r.insertions > r.deletions);
+    if (!gate) continue;
+    int32_t pct = del ? max(pctI(r.del_qual, r.mq_sum), pctI(r.deletions, wadd(cnt32, r.deletions)))
+                      : max(pctI(r.ins_qual, r.mq_sum), pctI(r.insertions, cnt32));
+    if (depth < P.min_min_depth || pct < 5) continue;
+    int64_t w = indel_vote(c, gp, del);
+    if (w < 0) continue;
+    const Event& e = c.ev[w];
+    int32_t len = e.len;
+    bool hasN = false;
+    if (del) {
+      // deletion string = reference bytes [dloc-1, dloc-1+len) of the contig
+      for (int32_t j = 0; j < len; j++) {
+        int64_t k = locus0 + j;
+        if (k >= 0 && k < c.contig_len && c.ref[c.ref_off + k] == 'N') hasN = true;
+      }
+    } else {
+      hasN = insertion_has_n(c, e);
+    }
+    if (hasN) continue;
+    bool call = false, homoI = true;
+    if (P.old_indel) {
+      if (pct >= 33 && pct >= 50 - len) { call = true; homoI = true; }
+    } else {
+      int32_t middle = max(45 - len, 10);
+      int32_t low = middle / 2;
+      int32_t high = middle + middle - low;
+      if (pct > high) { call = true; homoI = true; }
+      else if (pct >= low) { call = true; homoI = false; }
+    }
+    if (call) {
+      indelCalled = true;
+      homoIndel = homoI;
+      o.indel_len = len;
+      o.flags |= del ? PG_CALL_DEL : PG_CALL_INS;
+      if (!del) o.win_event = w;
+    }
+  }
+  if (homoIndel) o.flags |= PG_CALL_HOMO_INDEL;
+  return o;
+}
+
+// Writes the winning insertion's characters into the pool; returns the offset.
+__device__ inline int32_t pool_insertion(const CallCtx& c, const Event& e) {
+  unsigned long long off = atomicAdd(c.pool_fill, (unsigned long long)e.len);
+  if ((int64_t)(off + e.len) > c.pool_cap) return -2;  // overflow: host grows and reruns
+  for (int32_t j = 0; j < e.len; j++) c.pool[off + j] = (char)nib_char(ins_char(c.R, e, j));
+  return (int32_t)off;
+}
+
+// ---- kernels ----------------------------------------------------------------
+struct WalkArgs {
+  Reads R;
+  const RegionDev* regions;
+  const WalkTile* tiles;
+  int32_t n_tiles;
+  Records rec;
+  StatsDev* stats;
+  DevParams P;
+  const uint8_t* ref;
+  int32_t tile_width;
+};
+
+struct EventArgs {
+  Reads R;
+  const RegionDev* regions;
+  const ReadChunk* chunks;
+  int32_t n_chunks;
+  Records rec;
+  StatsDev* stats;
+  DevParams P;
+  const uint8_t* ref;
+  Event* events;
+  unsigned long long* n_events;
+  int64_t event_cap;
+  int32_t* bucket_count;  // per call tile
+};
+
+struct CallArgs {
+  Reads R;
+  const RegionDev* regions;
+  const int32_t* call_tile_region;  // region of each call tile
+  int32_t n_call_tiles;
+  Records rec;
+  StatsDev* stats;
+  DevParams P;
+  const uint8_t* ref;
+  const Event* ev_sorted;
+  const int32_t* bucket_off;  // n_call_tiles + 1
+  int64_t event_cap;
+  int32_t* cand_count;        // per call tile
+  char* pool;
+  unsigned long long* pool_fill;
+  int64_t pool_cap;
+};
+
+void launch_read_extent(const Reads& R, ReadExtent* out, cudaStream_t s);
+void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tiles, int32_t n_tiles,
+                        const ReadExtent* ext, cudaStream_t s);
+void launch_walk(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s);
+void launch_read_events(const EventArgs& a, int32_t chunk_begin, int32_t chunk_count, cudaStream_t s);
+void launch_scan_small(const int32_t* in, int32_t* out_excl, int32_t n, cudaStream_t s);
+void launch_event_scatter(const Event* ev, const unsigned long long* n_events, const RegionDev* regions,
+                          const int32_t* bucket_off, int32_t* bucket_fill, Event* out, cudaStream_t s,
+                          int64_t max_events);
+void launch_physcov_scan(const RegionDev* regions, const int32_t* call_tile_region, int32_t tile_begin,
+                         int32_t n_tiles, Records rec, const StatsDev* stats, int32_t* tile_sums,
+                         int32_t region_begin, int32_t n_regions, cudaStream_t s);
+void launch_region_prep(const RegionDev* regions, StatsDev* stats, int32_t n_regions, DevParams P,
+                        cudaStream_t s);
+void launch_call(const CallArgs& a, int32_t tile_begin, int32_t n_tiles, cudaStream_t s);
+void launch_cand_list(const CallArgs& a, const int32_t* cand_off, Cand* cands, int32_t cand_cap,
+                      int32_t tile_begin, int32_t n_tiles, cudaStream_t s);
+void launch_resolve(const RegionDev* regions, int32_t n_regions, const int32_t* cand_off, Cand* cands,
+                    int32_t cand_cap, StatsDev* stats, cudaStream_t s);
+void launch_apply_spans(const CallArgs& a, const Cand* cands, const int32_t* cand_total, int32_t cand_cap,
+                        cudaStream_t s);
+
+}  // namespace pg

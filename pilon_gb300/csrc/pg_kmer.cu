@@ -1,0 +1,250 @@
+// pg_kmer.cu — hashed K-mer -> next-base tally of Assembler.addRead /
+// addToPileups (S/Assembler.scala:55-87) and the edges of buildGraph
+// (S/Assembler.scala:132-154), for many local-reassembly windows at once.
+//
+// Every window owns a power-of-two open-addressing table in HBM keyed by the
+// 2-bit packed K-mer (K <= 31, so the all-ones word marks an empty slot).  One
+// thread walks one read, forward strand then reverse complement, and for each
+// K-mer adds the following base into the K-mer's PileUp counters with global
+// integer atomics (count[4], qualSum[4], mqSum, qSum).  K-mers containing a
+// base other than A/C/G/T (N, IUPAC codes, '=') cannot be 2-bit packed; they
+// are tallied exactly by k_kmer_exotic, one thread per window, in a private
+// table keyed by the 4-bit codes of the K-mer.
+#include <cuda_runtime.h>
+
+#include "pg_internal.cuh"
+#include "pg_kmer.cuh"
+
+namespace pg {
+
+constexpr unsigned long long kEmpty = ~0ull;
+
+__device__ inline int code2(uint32_t nib) { return nib == 1 ? 0 : nib == 2 ? 1 : nib == 4 ? 2 : nib == 8 ? 3 : -1; }
+__device__ inline uint32_t comp_nib(uint32_t n) {  // Bases.complement: A<->T, C<->G, others unchanged
+  return n == 1 ? 8u : n == 8 ? 1u : n == 2 ? 4u : n == 4 ? 2u : n;
+}
+__device__ inline unsigned long long mix64(unsigned long long x) {
+  x ^= x >> 33; x *= 0xff51afd7ed558ccdull; x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ull; x ^= x >> 33;
+  return x;
+}
+// nibble of base j of a read's strand (0 = forward, 1 = reverse complement)
+__device__ inline uint32_t strand_nib(const Reads& R, int64_t i, int32_t L, int strand, int32_t j) {
+  return strand == 0 ? read_nib(R, i, j) : comp_nib(read_nib(R, i, L - 1 - j));
+}
+__device__ inline int32_t strand_qual(const Reads& R, int64_t i, int32_t L, int strand, int32_t j, bool hasQual,
+                                      int32_t dq) {
+  if (!hasQual) return dq;
+  return (int32_t)(int8_t)R.qual[R.qual_off[i] + (strand == 0 ? j : L - 1 - j)];
+}
+
+// Per window: reads longer than K, K-mer events and exotic K-mer events.
+__global__ void k_kmer_prepass(Reads R, const pg_window* wins, int32_t K, long long* out /* 3 per window */) {
+  __shared__ unsigned long long s[3];
+  const pg_window w = wins[blockIdx.x];
+  if (threadIdx.x < 3) s[threadIdx.x] = 0;
+  __syncthreads();
+  unsigned long long nr = 0, ne = 0, nx = 0;
+  for (int64_t i = w.read_begin + threadIdx.x; i < w.read_end; i += blockDim.x) {
+    const int32_t L = R.l_seq[i];
+    if (L <= K) continue;
+    nr++;
+    ne += 2ull * (unsigned long long)(L - K);
+    for (int strand = 0; strand < 2; strand++) {
+      int32_t lastBad = -1;
+      for (int32_t j = 0; j < L - 1; j++) {
+        if (code2(strand_nib(R, i, L, strand, j)) < 0) lastBad = j;
+        int32_t o = j - K + 1;
+        if (o >= 0 && lastBad >= o) nx++;
+      }
+    }
+  }
+  atomicAdd(&s[0], nr);
+  atomicAdd(&s[1], ne);
+  atomicAdd(&s[2], nx);
+  __syncthreads();
+  if (threadIdx.x < 3) out[3 * blockIdx.x + threadIdx.x] = (long long)s[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(256) k_kmer_count(KmerArgs a) {
+  const int32_t w = a.win_begin + blockIdx.x;
+  const pg_window win = a.windows[w];
+  const int32_t K = a.K;
+  const unsigned long long mask = (K == 32) ? ~0ull : ((1ull << (2 * K)) - 1);
+  const int64_t base = a.slot_base[w], cap = a.slot_cap[w];
+  const Reads& R = a.R;
+  for (int64_t i = win.read_begin + threadIdx.x; i < win.read_end; i += blockDim.x) {
+    const int32_t L = R.l_seq[i];
+    if (L <= K) continue;
+    const uint32_t mq1 = (uint32_t)R.mapq[i] + 1u;
+    const bool hasQual = R.qual[R.qual_off[i]] != 0xFF;
+    for (int strand = 0; strand < 2; strand++) {
+      unsigned long long key = 0;
+      int32_t lastBad = -1;
+      uint32_t nib = strand_nib(R, i, L, strand, 0);
+      for (int32_t j = 0; j < L - 1; j++) {
+        int c = code2(nib);
+        if (c < 0) { lastBad = j; c = 0; }
+        key = ((key << 2) | (unsigned long long)c) & mask;
+        const uint32_t next = strand_nib(R, i, L, strand, j + 1);
+        const int32_t o = j - K + 1;
+        if (o >= 0 && lastBad < o) {
+          const int bi = code2(next);
+          const int32_t q = strand_qual(R, i, L, strand, j + 1, hasQual, a.default_qual);
+          if (bi >= 0 && q >= a.min_qual) {
+            int64_t h = (int64_t)(mix64(key) & (unsigned long long)(cap - 1));
+            int64_t slot = -1;
+            for (int64_t probe = 0; probe < cap; probe++) {
+              const int64_t s = base + h;
+              unsigned long long k = a.keys[s];
+              if (k == key) { slot = s; break; }
+              if (k == kEmpty) {
+                unsigned long long prev = atomicCAS(&a.keys[s], kEmpty, key);
+                if (prev == kEmpty || prev == key) { slot = s; break; }
+              }
+              h = (h + 1) & (cap - 1);
+            }
+            if (slot < 0) {
+              atomicExch(a.overflow, 1);
+            } else {
+              atomicAdd(&a.cnt[4 * slot + bi], 1u);
+              atomicAdd(&a.qs[4 * slot + bi], (unsigned long long)((uint32_t)q * mq1));
+              atomicAdd(&a.mq_sum[slot], mq1);
+              atomicAdd(&a.q_sum[slot], (uint32_t)q);
+            }
+          }
+        }
+        nib = next;
+      }
+    }
+  }
+}
+
+// BaseCall of a K-mer pileup (no indels): called base, alt base when not homozygous.
+__device__ inline void kmer_call(const uint32_t cnt[4], const unsigned long long qs[4], uint32_t q_sum,
+                                 int& base, int& alt) {
+  int64_t c[4], v[4];
+  for (int b = 0; b < 4; b++) { c[b] = cnt[b]; v[b] = (int64_t)qs[b]; }
+  int o0, o1;
+  if ((int32_t)q_sum > 0) order2(v, o0, o1); else order2(c, o0, o1);
+  const int64_t total = v[0] + v[1] + v[2] + v[3];
+  const int64_t homoScore = v[o0] - (total - v[o0]);
+  const int64_t half = total / 2;
+  const int64_t d1 = half - v[o0], d2 = half - v[o1];
+  const int64_t hetero = total - (d1 < 0 ? -d1 : d1) - (d2 < 0 ? -d2 : d2);
+  base = o0;
+  alt = homoScore >= hetero ? -1 : o1;
+}
+
+__device__ inline void emit_edge(const KmerArgs& a, unsigned long long hi, unsigned long long lo, int32_t w,
+                                 int base, int alt, int32_t depth, int32_t weight) {
+  unsigned long long k = atomicAdd(a.n_edges, 1ull);
+  if ((int64_t)k < a.edge_cap) {
+    pg_kmer_edge e;
+    e.key_hi = hi; e.key_lo = lo; e.window = w; e.next = (int8_t)base; e.alt = (int8_t)alt; e.pad_ = 0;
+    e.depth = depth; e.weight = weight;
+    a.edges[k] = e;
+  }
+}
+
+__global__ void k_kmer_edges(KmerArgs a) {
+  const int32_t w = a.win_begin + blockIdx.x;
+  const int64_t base = a.slot_base[w], cap = a.slot_cap[w];
+  const int32_t K = a.K;
+  for (int64_t s = base + threadIdx.x; s < base + cap; s += blockDim.x) {
+    const unsigned long long key = a.keys[s];
+    if (key == kEmpty) continue;
+    uint32_t cnt[4];
+    unsigned long long qs[4];
+    for (int b = 0; b < 4; b++) { cnt[b] = a.cnt[4 * s + b]; qs[b] = a.qs[4 * s + b]; }
+    const int32_t depth = (int32_t)(cnt[0] + cnt[1] + cnt[2] + cnt[3]);
+    if (depth < a.min_depth) continue;
+    int b0, alt;
+    kmer_call(cnt, qs, a.q_sum[s], b0, alt);
+    unsigned long long hi = 0, lo = 0;
+    for (int32_t j = 0; j < K; j++) {
+      const unsigned long long nibv = 1ull << ((key >> (2 * (K - 1 - j))) & 3ull);
+      if (j < 16) hi |= nibv << (60 - 4 * j); else lo |= nibv << (60 - 4 * (j - 16));
+    }
+    emit_edge(a, hi, lo, w, b0, alt, depth, (int32_t)cnt[b0]);
+  }
+}
+
+// Exotic K-mers: one thread per window, private table keyed by 4-bit codes.
+__global__ void k_kmer_exotic(KmerArgs a, int32_t n_win) {
+  const int32_t wl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (wl >= n_win) return;
+  const int32_t w = a.win_begin + wl;
+  const int64_t base = a.x_base[w], cap = a.x_cap[w];
+  if (cap == 0) return;
+  const pg_window win = a.windows[w];
+  const int32_t K = a.K;
+  const Reads& R = a.R;
+  for (int64_t i = win.read_begin; i < win.read_end; i++) {
+    const int32_t L = R.l_seq[i];
+    if (L <= K) continue;
+    const uint32_t mq1 = (uint32_t)R.mapq[i] + 1u;
+    const bool hasQual = R.qual[R.qual_off[i]] != 0xFF;
+    for (int strand = 0; strand < 2; strand++) {
+      int32_t lastBad = -1;
+      for (int32_t j = 0; j < L - 1; j++) {
+        if (code2(strand_nib(R, i, L, strand, j)) < 0) lastBad = j;
+        const int32_t o = j - K + 1;
+        if (o < 0 || lastBad < o) continue;
+        const uint32_t next = strand_nib(R, i, L, strand, j + 1);
+        const int bi = code2(next);
+        const int32_t q = strand_qual(R, i, L, strand, j + 1, hasQual, a.default_qual);
+        if (!(bi >= 0 && q >= a.min_qual)) continue;
+        unsigned long long hi = 0, lo = 0;
+        for (int32_t t = 0; t < K; t++) {
+          const unsigned long long nb = strand_nib(R, i, L, strand, o + t);
+          if (t < 16) hi |= nb << (60 - 4 * t); else lo |= nb << (60 - 4 * (t - 16));
+        }
+        int64_t h = (int64_t)(mix64(hi ^ mix64(lo)) & (unsigned long long)(cap - 1));
+        int64_t slot = -1;
+        for (int64_t probe = 0; probe < cap; probe++) {
+          const int64_t s = base + h;
+          if (a.x_keys[2 * s] == hi && a.x_keys[2 * s + 1] == lo && a.x_used[s]) { slot = s; break; }
+          if (!a.x_used[s]) {
+            a.x_used[s] = 1;
+            a.x_keys[2 * s] = hi;
+            a.x_keys[2 * s + 1] = lo;
+            slot = s;
+            break;
+          }
+          h = (h + 1) & (cap - 1);
+        }
+        if (slot < 0) { atomicExch(a.overflow, 1); continue; }
+        a.x_cnt[4 * slot + bi] += 1u;
+        a.x_qs[4 * slot + bi] += (unsigned long long)((uint32_t)q * mq1);
+        a.x_mq[slot] += mq1;
+        a.x_q[slot] += (uint32_t)q;
+      }
+    }
+  }
+  for (int64_t s = base; s < base + cap; s++) {
+    if (!a.x_used[s]) continue;
+    uint32_t cnt[4];
+    unsigned long long qs[4];
+    for (int b = 0; b < 4; b++) { cnt[b] = a.x_cnt[4 * s + b]; qs[b] = a.x_qs[4 * s + b]; }
+    const int32_t depth = (int32_t)(cnt[0] + cnt[1] + cnt[2] + cnt[3]);
+    if (depth < a.min_depth) continue;
+    int b0, alt;
+    kmer_call(cnt, qs, a.x_q[s], b0, alt);
+    emit_edge(a, a.x_keys[2 * s], a.x_keys[2 * s + 1], w, b0, alt, depth, (int32_t)cnt[b0]);
+  }
+}
+
+void launch_kmer_prepass(const Reads& R, const pg_window* wins, int32_t n, int32_t K, long long* out,
+                         cudaStream_t s) {
+  if (n <= 0) return;
+  k_kmer_prepass<<<n, 256, 0, s>>>(R, wins, K, out);
+}
+
+void launch_kmer_batch(const KmerArgs& a, int32_t n_win, cudaStream_t s) {
+  if (n_win <= 0) return;
+  k_kmer_count<<<n_win, 256, 0, s>>>(a);
+  k_kmer_exotic<<<(n_win + 63) / 64, 64, 0, s>>>(a, n_win);
+  k_kmer_edges<<<n_win, 256, 0, s>>>(a);
+}
+
+}  // namespace pg

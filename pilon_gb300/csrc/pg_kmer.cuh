@@ -1,0 +1,41 @@
+// pg_kmer.cuh — arguments of the K-mer tally kernels (pg_kmer.cu).
+#pragma once
+#include "pg_internal.cuh"
+
+namespace pg {
+
+struct KmerArgs {
+  Reads R;
+  const pg_window* windows;
+  int32_t win_begin;          // first window of this batch
+  int32_t K;
+  int32_t min_qual, default_qual, min_depth;
+  // 2-bit tables: slots [slot_base[w], slot_base[w] + slot_cap[w]) of window w
+  const int64_t* slot_base;
+  const int64_t* slot_cap;
+  unsigned long long* keys;   // kEmpty = free
+  uint32_t* cnt;              // 4 per slot
+  unsigned long long* qs;     // 4 per slot
+  uint32_t* mq_sum;
+  uint32_t* q_sum;
+  // exotic tables (4-bit keys), single writer per window
+  const int64_t* x_base;
+  const int64_t* x_cap;
+  unsigned long long* x_keys; // 2 per slot
+  uint8_t* x_used;
+  uint32_t* x_cnt;
+  unsigned long long* x_qs;
+  uint32_t* x_mq;
+  uint32_t* x_q;
+  // output
+  pg_kmer_edge* edges;
+  int64_t edge_cap;
+  unsigned long long* n_edges;
+  int32_t* overflow;
+};
+
+void launch_kmer_prepass(const Reads& R, const pg_window* wins, int32_t n, int32_t K, long long* out,
+                         cudaStream_t s);
+void launch_kmer_batch(const KmerArgs& a, int32_t n_win, cudaStream_t s);
+
+}  // namespace pg

@@ -1,0 +1,190 @@
+"""ctypes binding of libpilon_gb300.so, the GB300 engine behind the C ABI of
+include/pilon_gb300.h.  This is the binding a JVM host would write with JNI or
+the Java foreign-function API; see INTEGRATION.md for that side.
+
+There is no CPU fallback: if the engine library is missing or no CUDA device
+is present, every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi
+from .build import ENGINE
+
+_LIB = None
+
+
+class EngineError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{_abi.STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def lib():
+    """Loads the engine library; raises if it was not built."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(ENGINE):
+            raise EngineError(-1, f"engine library {ENGINE} is missing; run pilon_gb300.build.build()")
+        L = C.CDLL(ENGINE)
+        vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+        sig = {
+            "pg_open": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
+            "pg_close": (None, [vp]),
+            "pg_last_error": (C.c_char_p, [vp]),
+            "pg_default_params": (None, [C.POINTER(_abi.pg_params)]),
+            "pg_version": (C.c_char_p, []),
+            "pg_set_reference": (C.c_int, [vp, i32, vp, vp]),
+            "pg_set_reads": (C.c_int, [vp, C.POINTER(_abi.pg_reads)]),
+            "pg_set_reads_device": (C.c_int, [vp, C.POINTER(_abi.pg_reads)]),
+            "pg_pileup_regions": (C.c_int, [vp, vp, i32, C.POINTER(_abi.pg_params), i32]),
+            "pg_fetch_stats": (C.c_int, [vp, i32, C.POINTER(_abi.pg_region_stats)]),
+            "pg_fetch_region": (C.c_int, [vp, i32, C.POINTER(_abi.pg_region_out)]),
+            "pg_set_tuning": (C.c_int, [vp, i32, i32]),
+            "pg_kmer_tally": (C.c_int, [vp, vp, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
+                                        C.POINTER(C.c_int64)]),
+            "pg_last_kernel_ms": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_int32)]),
+            "pg_sync": (C.c_int, [vp]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+class RegionArrays:
+    """One region's pileup records and calls on the host (pg_region_out)."""
+    I32 = ["mq_sum", "q_sum", "phys_cov", "insert_size", "bad_pair", "deletions", "del_qual", "insertions",
+           "ins_qual", "clips", "indel_len", "ins_str"]
+
+    def __init__(self, size):
+        self.size = size
+        self.count = np.empty(4 * size, np.int32)
+        self.qual_sum = np.empty(4 * size, np.int64)
+        for f in self.I32:
+            setattr(self, f, np.empty(size, np.int32))
+        self.call = np.empty(size, np.uint32)
+        self.score = np.empty(size, np.int64)
+        self.ins_chars = np.zeros(0, np.uint8)
+        self.stats = _abi.pg_region_stats()
+
+    def out_struct(self, ins_cap):
+        o = _abi.pg_region_out()
+        o.count = self.count.ctypes.data
+        o.qual_sum = self.qual_sum.ctypes.data
+        for f in self.I32:
+            setattr(o, f, getattr(self, f).ctypes.data)
+        o.call = self.call.ctypes.data
+        o.score = self.score.ctypes.data
+        if self.ins_chars.size < ins_cap:
+            self.ins_chars = np.zeros(ins_cap, np.uint8)
+        o.ins_chars = self.ins_chars.ctypes.data if self.ins_chars.size else None
+        o.ins_chars_cap = self.ins_chars.size
+        return o
+
+    def insertion(self, i):
+        off = int(self.ins_str[i])
+        if off < 0:
+            return ""
+        return self.ins_chars[off:off + int(self.indel_len[i])].tobytes().decode()
+
+
+class Engine:
+    """One engine context on one CUDA device (pg_open ... pg_close)."""
+
+    def __init__(self, device=0):
+        self.L = lib()
+        self.h = C.c_void_p()
+        st = self.L.pg_open(C.byref(self.h), device)
+        if st != 0:
+            msg = self.L.pg_last_error(self.h).decode() if self.h else "pg_open failed"
+            if self.h:
+                self.L.pg_close(self.h)
+            self.h = None
+            raise EngineError(st, msg)
+        self._keep = []
+
+    def close(self):
+        if self.h:
+            self.L.pg_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != 0:
+            raise EngineError(st, self.L.pg_last_error(self.h).decode())
+
+    def set_reference(self, contigs):
+        arrs = [np.ascontiguousarray(c, np.uint8) for c in contigs]
+        lens = np.array([a.size for a in arrs], np.int64)
+        ptrs = (C.c_void_p * max(1, len(arrs)))(*[a.ctypes.data for a in arrs])
+        self._check(self.L.pg_set_reference(self.h, len(arrs), lens.ctypes.data, C.cast(ptrs, C.c_void_p)))
+        self.contig_lens = lens
+
+    def set_reads(self, reads):
+        ab = reads.to_abi()
+        self._check(self.L.pg_set_reads(self.h, C.byref(ab)))
+        self.n_reads = reads.n_reads
+
+    def set_tuning(self, tile_width=0, warps=0):
+        self._check(self.L.pg_set_tuning(self.h, tile_width, warps))
+
+    def pileup_regions(self, regions, params, batched=True):
+        """regions: list of (contig, start, stop, read_begin, read_end)."""
+        arr = (_abi.pg_region * max(1, len(regions)))()
+        for k, (c, s, e, rb, re) in enumerate(regions):
+            arr[k] = _abi.pg_region(c, s, e, 0, rb, re)
+        self._check(self.L.pg_pileup_regions(self.h, C.cast(arr, C.c_void_p), len(regions), C.byref(params),
+                                             int(batched)))
+        self.regions = list(regions)
+
+    def stats(self, r):
+        st = _abi.pg_region_stats()
+        self._check(self.L.pg_fetch_stats(self.h, r, C.byref(st)))
+        return st
+
+    def fetch(self, r, out=None):
+        c, s, e, _, _ = self.regions[r]
+        size = e - s + 1
+        out = out or RegionArrays(size)
+        o = out.out_struct(0)
+        o.ins_chars = None
+        self._check(self.L.pg_fetch_region(self.h, r, C.byref(o)))
+        pool = int(o.ins_chars_cap)
+        if pool:
+            o2 = _abi.pg_region_out()
+            out.ins_chars = np.zeros(pool, np.uint8)
+            o2.ins_chars = out.ins_chars.ctypes.data
+            o2.ins_chars_cap = pool
+            self._check(self.L.pg_fetch_region(self.h, r, C.byref(o2)))
+        out.stats = self.stats(r)
+        return out
+
+    def kmer_tally(self, windows, K, params, min_depth=5, cap=1 << 20):
+        wins = (_abi.pg_window * max(1, len(windows)))(*[_abi.pg_window(a, b) for a, b in windows])
+        while True:
+            edges = np.zeros(cap, _abi.kmer_edge_dtype())
+            n = C.c_int64()
+            self._check(self.L.pg_kmer_tally(self.h, C.cast(wins, C.c_void_p), len(windows), K, C.byref(params),
+                                             min_depth, edges.ctypes.data, cap, C.byref(n)))
+            if n.value <= cap:
+                return edges[:n.value]
+            cap = int(n.value)
+
+    def last_kernel_ms(self):
+        w, t, n = C.c_double(), C.c_double(), C.c_int32()
+        self._check(self.L.pg_last_kernel_ms(self.h, C.byref(w), C.byref(t), C.byref(n)))
+        return w.value, t.value, n.value
+
+    def sync(self):
+        self._check(self.L.pg_sync(self.h))

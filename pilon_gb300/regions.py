@@ -1,0 +1,72 @@
+"""Region partitioning and the read range fed to each region.
+
+contig_regions restates GenomeFile.contigRegions (S/GenomeFile.scala:67-74);
+read ranges reproduce the window of BamFile.process
+(S/BamFile.scala:117-119): every read overlapping
+[max(start-10000, 0), min(stop+10000, len)] is fed to the region.
+"""
+import numpy as np
+
+SLOP = 10000
+
+
+def contig_regions(contig_len, chunk_size=10_000_000):
+    """[(start, stop)] 1-based closed chunks of one contig."""
+    n_chunks = (contig_len + chunk_size - 1) // chunk_size
+    cs = (contig_len + n_chunks - 1) // n_chunks
+    return [(b, min(contig_len, b + cs - 1)) for b in range(1, contig_len + 1, cs)]
+
+
+def parse_targets(target_string, names, lens):
+    """--targets "name:start-stop,..." or whole contigs (S/GenomeFile.scala:215-236)."""
+    import re
+    out = []
+    for t in target_string.split(","):
+        m = re.match(r"^\s*(.+):([0-9]+)-([0-9]+)\s*$", t)
+        if m:
+            name, s, e = m.group(1), int(m.group(2)), int(m.group(3))
+        else:
+            name = t
+            s, e = 1, int(lens[names.index(t)])
+        ci = names.index(name)
+        if e > lens[ci]:
+            raise ValueError("GenomeRegion stop point must be within contig")
+        out.append((ci, s, e))
+    return out
+
+
+class ReadIndex:
+    """Locates the reads of each contig in a (ref_id, pos)-sorted store."""
+
+    def __init__(self, reads, n_contigs):
+        self.reads = reads
+        rid = reads.ref_id
+        self.contig_lo = np.searchsorted(rid, np.arange(n_contigs), side="left")
+        self.contig_hi = np.searchsorted(rid, np.arange(n_contigs), side="right")
+        span = (reads.aend.astype(np.int64) - reads.pos.astype(np.int64) + 1)
+        self.max_span = int(span.max()) if span.size else 0
+
+    def range_for(self, contig, start, stop, contig_len, slop=SLOP):
+        lo, hi = int(self.contig_lo[contig]), int(self.contig_hi[contig])
+        qs = max(start - slop, 0)
+        qe = min(stop + slop, contig_len)
+        pos = self.reads.pos[lo:hi]
+        a = lo + int(np.searchsorted(pos, qs - self.max_span, side="left"))
+        b = lo + int(np.searchsorted(pos, qe, side="right"))
+        return a, b
+
+
+def plan_regions(reads, contig_lens, chunk_size=10_000_000, targets=None):
+    """[(contig, start, stop, read_begin, read_end)] in processing order."""
+    idx = ReadIndex(reads, len(contig_lens))
+    regs = []
+    if targets is not None:
+        for ci, s, e in targets:
+            a, b = idx.range_for(ci, s, e, contig_lens[ci])
+            regs.append((ci, s, e, a, b))
+        return regs
+    for ci, ln in enumerate(contig_lens):
+        for s, e in contig_regions(int(ln), chunk_size):
+            a, b = idx.range_for(ci, s, e, int(ln))
+            regs.append((ci, s, e, a, b))
+    return regs

@@ -1,0 +1,66 @@
+"""GPU engine vs the CPU oracle, through the C ABI: every pileup field, call
+flag, score, indel string and region statistic must be bit-identical."""
+import numpy as np
+import pytest
+
+from pilon_gb300 import _abi, synth
+from tests.helpers import compare_region, oracle_regions, plan
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def engine():
+    from pilon_gb300.engine import Engine
+    e = Engine(0)
+    yield e
+    e.close()
+
+
+def run_both(engine, ds, params, regions, batched=True):
+    engine.set_reference(ds.contigs)
+    engine.set_reads(ds.reads)
+    engine.pileup_regions(regions, params, batched=batched)
+    ora = oracle_regions(ds, params, regions)
+    for r in range(len(regions)):
+        compare_region(engine.fetch(r), ora[r], label=f"region {r}")
+    return ora
+
+
+def test_cfg1_single_region(engine, cfg1):
+    p = _abi.default_params()
+    ora = run_both(engine, cfg1, p, plan(cfg1))
+    assert ora[0].stats.n_changes >= 20
+
+
+def test_cfg1_chunked_regions_plain_and_batched(engine, cfg1):
+    p = _abi.default_params()
+    regions = plan(cfg1, chunk_size=7000)
+    assert len(regions) > 5
+    run_both(engine, cfg1, p, regions, batched=True)
+    run_both(engine, cfg1, p, regions, batched=False)
+
+
+@pytest.mark.parametrize("opts", [dict(min_mq=20), dict(min_qual=25), dict(flank=0), dict(flank=40),
+                                  dict(nonpf=1, duplicates=1), dict(old_indel=1), dict(fix_amb=1),
+                                  dict(min_depth=12.0), dict(default_qual=30)])
+def test_cfg1_options(engine, cfg1, opts):
+    run_both(engine, cfg1, _abi.default_params(**opts), plan(cfg1))
+
+
+def test_cfg2_scaled(engine):
+    ds = synth.generate(2, scale=0.02)  # 100 kb at 100x, mapq-0 reads, indel errors
+    run_both(engine, ds, _abi.default_params(), plan(ds, chunk_size=30_000))
+
+
+def test_cfg3_many_contigs(engine):
+    ds = synth.generate(3, scale=0.01)  # 30 contigs, 1% variants
+    regions = plan(ds)
+    run_both(engine, ds, _abi.default_params(), regions, batched=True)
+    run_both(engine, ds, _abi.default_params(), regions, batched=False)
+
+
+def test_long_read_modes(engine, cfg1):
+    for lr in (_abi.PG_NANOPORE, _abi.PG_PACBIO):
+        p = _abi.default_params(long_read=lr, bam_type=_abi.PG_BAM_UNPAIRED)
+        run_both(engine, cfg1, p, plan(cfg1, chunk_size=20_000))
