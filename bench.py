@@ -1,0 +1,377 @@
+"""Benchmark: aligned bases piled per second (pileup + calls + pass 1) on GB300.
+
+Workload (default): 5 Mb bacterial genome, GC 65%, 100x 2x150 pairs, insert
+N(500, 80), 0.3% substitutions, 0.02% indel errors, 500 SNPs + 100 indels,
+3% mapq-0 reads, one 5 Mb region (Pilon's default 10 Mb chunking), synthetic
+and seeded (1002).  A step is one pg_pileup_regions call over all regions:
+BamFile.process + PileUpRegion.addRead, computePhysCov, BaseCall and pass 1.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config 2] [--impl reference]
+
+--impl reference times the CPU restatement of the reference path (the oracle;
+the Scala reference cannot run here: no JVM) on the host cores.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gbases piled/s (aligned M/=/X bases walked per region, pileup+calls+pass 1)"
+UNIT = "Gbases/s"
+
+
+def piled_bases(reads, regions, contig_lens, params):
+    """Iterations of the M/=/X loop of PileUpRegion.addRead (S/PileUpRegion.scala:184-193)
+    summed over the reads fed to each region (validated reads in the query window)."""
+    m = reads.aligned_bases()
+    fl = reads.flag.astype(np.int64)
+    ok = np.ones(reads.n_reads, bool)
+    if not params.nonpf:
+        ok &= (fl & 0x200) == 0
+    if not params.duplicates:
+        ok &= (fl & 0x400) == 0
+    ok &= (fl & 0x100) == 0
+    tot = 0
+    for (c, s, e, rb, re) in regions:
+        qs, qe = max(s - 10000, 0), min(e + 10000, int(contig_lens[c]))
+        pos = reads.pos[rb:re].astype(np.int64)
+        end = np.where((fl[rb:re] & 4) != 0, pos, reads.aend[rb:re].astype(np.int64))
+        sel = ok[rb:re] & (reads.ref_id[rb:re] == c) & (pos <= qe) & (end >= qs)
+        tot += int(m[rb:re][sel].sum())
+    return tot
+
+
+def walk_algorithmic_bytes(reads, regions):
+    """Bytes the walk must move at minimum: per read fed to a region its header
+    (32 B), CIGAR (4 B/op), 2-bit bases (L/4) and qualities (L), plus the
+    88-byte pileup record written once per position."""
+    L = reads.l_seq.astype(np.int64)
+    per_read = 32 + 4 * reads.n_cigar.astype(np.int64) + (L + 3) // 4 + L
+    csum = np.concatenate([[0], np.cumsum(per_read)])
+    b = 0
+    for (c, s, e, rb, re) in regions:
+        b += int(csum[re] - csum[rb]) + 88 * (e - s + 1)
+    return b
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.p:
+            self.p.terminate()
+            try:
+                out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def pinned_store(reads):
+    """Copies the read store into page-locked host memory (torch pinned tensors)."""
+    import torch
+    from pilon_gb300.reads import FIELDS, ReadStore
+    keep = []
+    arrs = {}
+    for f in FIELDS:
+        a = np.ascontiguousarray(getattr(reads, f))
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        v = t.numpy().view(a.dtype)
+        v[:] = a.reshape(-1)
+        keep.append(t)
+        arrs[f] = v
+    st = ReadStore(**arrs)
+    st._pinned = keep
+    return st
+
+
+class PinnedOut:
+    def __init__(self, size):
+        import torch
+        from pilon_gb300.engine import RegionArrays
+        self.t = []
+        ra = RegionArrays.__new__(RegionArrays)
+        ra.size = size
+
+        def mk(n, dt):
+            t = torch.empty(n * np.dtype(dt).itemsize, dtype=torch.uint8, pin_memory=True)
+            self.t.append(t)
+            return t.numpy().view(dt)
+        ra.count = mk(4 * size, np.int32)
+        ra.qual_sum = mk(4 * size, np.int64)
+        for f in RegionArrays.I32:
+            setattr(ra, f, mk(size, np.int32))
+        ra.call = mk(size, np.uint32)
+        ra.score = mk(size, np.int64)
+        ra.ins_chars = np.zeros(0, np.uint8)
+        self.arrays = ra
+
+    def nbytes(self):
+        return sum(t.numel() for t in self.t)
+
+
+def roofline_traffic(workload_name, units):
+    """Per-launch DRAM bytes of the walk kernel from the committed ncu summary,
+    scaled by units if it was captured on a smaller case; None if absent."""
+    path = os.path.join(ROOT, "profiles", "k_walk_ncu.md")
+    if not os.path.exists(path):
+        return None
+    cap_units = cap_bytes = None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            cap_bytes = float(line.split(":")[1])
+        if line.startswith("units_per_launch:"):
+            cap_units = float(line.split(":")[1])
+    if cap_bytes is None:
+        return None
+    if cap_units:
+        return cap_bytes * units / cap_units
+    return cap_bytes
+
+
+def oracle_sample(ds, params, threads):
+    """The oracle over the workload split in `threads` regions on as many host
+    threads; returns (piled bases, seconds)."""
+    from oracle import oracle
+    from pilon_gb300.regions import ReadIndex
+    oracle.lib()
+    jobs = []
+    idx = ReadIndex(ds.reads, len(ds.contigs))
+    for ci, ref in enumerate(ds.contigs):
+        n = max(1, min(threads, ref.size // 50_000))
+        step = (ref.size + n - 1) // n
+        for s in range(1, ref.size + 1, step):
+            e = min(ref.size, s + step - 1)
+            a, b = idx.range_for(ci, s, e, ref.size)
+            jobs.append((ci, s, e, a, b))
+    units = piled_bases(ds.reads, jobs, [c.size for c in ds.contigs], params)
+    res = [None] * len(jobs)
+    it = iter(range(len(jobs)))
+    lock = threading.Lock()
+
+    def worker():
+        while True:
+            with lock:
+                k = next(it, None)
+            if k is None:
+                return
+            ci, s, e, a, b = jobs[k]
+            res[k] = oracle.process_region(ds.reads, params, ds.contigs[ci], ci, s, e, a, b).status
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=worker) for _ in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    return units, time.perf_counter() - t0, len(jobs)
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+        return dist, int(os.environ["RANK"]), ws, int(os.environ.get("LOCAL_RANK", "0"))
+    return None, 0, 1, 0
+
+
+def barrier(dist):
+    if dist:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if not dist:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--batched", type=int, default=1)
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    dist, rank, ws, local = dist_init()
+    from pilon_gb300 import _abi, synth
+    from pilon_gb300.regions import plan_regions
+
+    params = _abi.default_params()
+    threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        ds = synth.generate(args.config, args.scale)
+        samples = []
+        for k in range(args.warmup + args.steps):
+            units, sec, njobs = oracle_sample(ds, params, threads)
+            if k >= args.warmup:
+                samples.append((units, sec))
+        units = sum(u for u, _ in samples)
+        sec = sum(s for _, s in samples)
+        v = units / sec / 1e9
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / len(samples),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64",
+                "data": "synthetic (seeded)",
+                "config": {"workload": ds.workload.name, "genome_bp": int(sum(c.size for c in ds.contigs)),
+                           "reads": ds.reads.n_reads, "coverage": ds.workload.coverage},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"whole workload per step, split into {njobs} regions over {threads} "
+                                           f"host threads (the Scala reference needs a JVM, absent here)"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    from pilon_gb300.engine import Engine
+    ds = synth.generate(args.config, args.scale)
+    lens = [c.size for c in ds.contigs]
+    regions = plan_regions(ds.reads, lens)
+    units = piled_bases(ds.reads, regions, lens, params)
+    walk_bytes = walk_algorithmic_bytes(ds.reads, regions)
+
+    eng = Engine(local)
+    if args.tile or args.warps:
+        eng.set_tuning(args.tile, args.warps)
+    eng.set_reference(ds.contigs)
+    eng.set_reads(ds.reads)
+    for _ in range(args.warmup):
+        eng.pileup_regions(regions, params, batched=bool(args.batched))
+    barrier(dist)
+    eng.sync()
+    tot_ms, walk_ms, launches = [], [], 0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            eng.pileup_regions(regions, params, batched=bool(args.batched))
+            w, t, n = eng.last_kernel_ms()
+            tot_ms.append(t)
+            walk_ms.append(w)
+            launches += n
+    eng.sync()
+    barrier(dist)
+    dev_s = max_over_ranks(dist, sum(tot_ms) / 1e3)
+    value = units * ws * args.steps / dev_s / 1e9
+    walk_avg = sum(walk_ms) / len(walk_ms) / 1e3
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = walk_bytes / walk_avg / 1e9
+    traffic = roofline_traffic(ds.workload.name, units)
+
+    # end to end through the C ABI: H2D of the read store from pinned memory,
+    # pileup + calls, D2H of every region's records and calls
+    e2e = None
+    if not args.no_e2e:
+        pin = pinned_store(ds.reads)
+        outs = [PinnedOut(e - s + 1) for (c, s, e, a, b) in regions]
+        h2d = pin.nbytes()
+        d2h = sum(o.nbytes() for o in outs)
+        for _ in range(args.warmup):
+            eng.set_reads(pin)
+            eng.pileup_regions(regions, params, batched=bool(args.batched))
+            for r, o in enumerate(outs):
+                eng.fetch(r, o.arrays)
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            eng.set_reads(pin)
+            eng.pileup_regions(regions, params, batched=bool(args.batched))
+            for r, o in enumerate(outs):
+                eng.fetch(r, o.arrays)
+        eng.sync()
+        e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+        barrier(dist)
+        e2e = {"value": units * ws * args.steps / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / args.steps,
+               "timing": "host wall clock; every call synchronises the engine stream"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        u, sec, njobs = oracle_sample(ds, params, threads)
+        cpu = {"value": u / sec / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"the whole workload split into {njobs} regions on {threads} host threads, one pass"}
+    eng.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32/int64", "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": ds.workload.name, "genome_bp": int(sum(lens)), "regions": len(regions),
+                   "reads": ds.reads.n_reads, "coverage": ds.workload.coverage, "piled_bases_per_step": units,
+                   "path": "batched" if args.batched else "per-region", "l2": "inputs larger than L2 (reads "
+                   f"{ds.reads.nbytes() / 1e6:.0f} MB)", "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "k_walk", "algorithmic_bytes_per_launch": walk_bytes,
+                     "walk_ms": walk_avg * 1e3, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"
+                     if peaks else "fallback"},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

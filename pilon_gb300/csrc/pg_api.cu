@@ -378,14 +378,12 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   launch_walk(wa, w0, wn, c->warps, s);
   cudaEventRecord(c->wev[2 * c->n_runs + 1], s);
   c->n_runs++;
-  c->launches += wn > 0;
 
   EventArgs ea;
   ea.R = c->R; ea.regions = d_regions; ea.chunks = P<ReadChunk>(c->chunks); ea.n_chunks = chn; ea.rec = rec;
   ea.stats = d_stats; ea.P = dp; ea.ref = P<uint8_t>(c->ref); ea.events = P<Event>(c->events);
   ea.n_events = &counters[CNT_EVENTS]; ea.event_cap = c->event_cap; ea.bucket_count = P<int32_t>(c->bucket_count);
   launch_read_events(ea, ch0, chn, s);
-  c->launches += chn > 0;
 
   launch_region_prep(d_regions + r0, d_stats + r0, r1 - r0, dp, s);
   launch_scan_small(P<int32_t>(c->bucket_count) + t0, P<int32_t>(c->bucket_off) + t0, tn, s);
@@ -407,7 +405,10 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   launch_resolve(d_regions + r0, r1 - r0, P<int32_t>(c->cand_off), P<Cand>(c->cands), c->cand_cap, d_stats + r0, s);
   launch_apply_spans(ca, P<Cand>(c->cands), P<int32_t>(c->cand_off) + t0 + tn, c->cand_cap, s);
   k_track<<<1, 1, 0, s>>>(counters, P<int32_t>(c->cand_off) + t0 + tn, P<unsigned long long>(c->run_max));
-  c->launches += 12;
+  // kernels of this run: tile ranges + walk, read events, region prep, two
+  // small scans, event scatter, three scan phases, call, candidate list,
+  // resolve, span update, overflow tracking
+  c->launches += 2 * (wn > 0) + (chn > 0) + 1 + 2 + 1 + 3 * (tn > 0) + 2 * (tn > 0) + 1 + 1 + 1;
 }
 
 pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions, const pg_params* params,
