@@ -238,6 +238,31 @@ pg_status pg_last_kernel_ms(pg_ctx *ctx, double *walk_ms, double *total_ms, int3
 /* Synchronises the context stream. */
 pg_status pg_sync(pg_ctx *ctx);
 
+/* ---- physical-coverage scan without device allocation ----------------------
+ * This entry point has no counterpart in the reference.  It is for callers
+ * that cannot let a library allocate device memory: a host whose own pool
+ * (a JVM allocator, a PyTorch caching allocator) already holds the device's
+ * memory, where a cudaMalloc could fail, fragment the pool or synchronise.
+ *
+ * It turns one region's physical-coverage and insert-size difference arrays
+ * (caller device buffers of n_positions int32 each, the +1/-1 and +size/-size
+ * updates of physCovIncr) into the prefix-summed values of computePhysCov,
+ * starting from the region's carry (physCovStart, insertSizeStart), and
+ * divides insert size by coverage where coverage > 0.  Output may alias input.
+ * Work is queued on `stream` (a cudaStream_t; NULL = legacy default stream);
+ * the call does not synchronise.
+ *
+ * Its only scratch is a fixed 128 KiB device array inside the library, so it
+ * allocates nothing; n_positions above PG_STATIC_SCAN_MAX_POSITIONS returns
+ * PG_ERR_LIMIT.  The first call on each device looks up that array's device
+ * address (make it before any stream capture).  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * On failure a message is written to errbuf (may be NULL). */
+#define PG_STATIC_SCAN_MAX_POSITIONS 16777216
+pg_status pg_phys_cov_scan_static(const int32_t *phys_diff, const int32_t *insert_diff, int64_t n_positions,
+                                  int32_t phys_cov_start, int32_t insert_size_start, int32_t *phys_cov,
+                                  int32_t *insert_size, void *stream, char *errbuf, int32_t errcap);
+
 #ifdef __cplusplus
 }
 #endif
