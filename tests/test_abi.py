@@ -1,0 +1,66 @@
+"""The C-ABI library loads and exports every entry point declared in
+include/*.h (no compute calls: no GPU needed)."""
+import ctypes as C
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:pg_status|void|const char\s*\*)\s*(pg_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declares_the_abi():
+    from pilon_gb300 import _abi
+    assert declared() == set(_abi.EXPORTED)
+
+
+def test_library_exports_every_declared_symbol():
+    from pilon_gb300.build import ENGINE, build
+    if not os.path.exists(ENGINE):
+        build()
+    lib = C.CDLL(ENGINE)
+    for name in declared():
+        assert hasattr(lib, name), name
+
+
+def test_struct_layouts_match_header():
+    from pilon_gb300 import _abi
+    # sizes fixed by the header's field order (LP64)
+    assert C.sizeof(_abi.pg_params) == 12 * 4 + 8  # 12 int32, then the double at offset 48
+    assert C.sizeof(_abi.pg_reads) == 8 + 15 * 8 + 3 * 8
+    assert C.sizeof(_abi.pg_region) == 32
+    assert C.sizeof(_abi.pg_kmer_edge) == 32
+    assert C.sizeof(_abi.pg_window) == 16
+
+
+def test_default_params_match_pilon():
+    from pilon_gb300 import _abi
+    from pilon_gb300.build import ENGINE, build
+    if not os.path.exists(ENGINE):
+        build()
+    lib = C.CDLL(ENGINE)
+    p = _abi.pg_params()
+    lib.pg_default_params(C.byref(p))
+    q = _abi.default_params()
+    for f, _ in _abi.pg_params._fields_:
+        assert getattr(p, f) == getattr(q, f), f
+
+
+def test_open_without_gpu_fails_cleanly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from pilon_gb300.engine import Engine, EngineError
+    with pytest.raises(EngineError):
+        Engine(0)

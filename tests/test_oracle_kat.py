@@ -1,0 +1,277 @@
+"""Known-answer tests of the CPU oracle, derived by hand from the Scala source.
+
+The reference ships no tests, fixtures or golden vectors and cannot run here
+(no JVM), so each expected value below is worked out from the cited Scala
+lines.  One case per parity hazard of the hot path:
+  H1 deletion left shift adds bases without removing them   S/PileUpRegion.scala:163-183
+  H2 a homozygous deletion updates the pileups it covers    S/GenomeRegion.scala:259-264
+  H3 a left shift below the region start throws             S/PileUpRegion.scala:155-182
+  H5 integer rounding (roundDiv, adjMq)                     S/Utils.scala:23-26, S/PileUpRegion.scala:139-142
+  H6 stable base order on ties                              S/BaseSum.scala:57-60
+  H10 Java "%.2f" rounding of AF                            S/Vcf.scala:134-152
+  H12 output names, FASTA wrapping, changes format          S/GenomeFile.scala:79-82,135-161
+"""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from pilon_gb300 import _abi
+from pilon_gb300.reads import build_store
+
+
+def ref_from(seq):
+    return np.frombuffer(seq.encode(), np.uint8).copy()
+
+
+def rand_ref(n, seed=7, avoid_runs=True):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = []
+    for _ in range(n):
+        while True:
+            c = "ACGT"[rng.integers(0, 4)]
+            if not avoid_runs or not s or c != s[-1]:
+                break
+        s.append(c)
+    return "".join(s)
+
+
+def read(pos, cigar, seq, qual=30, mapq=60, flag=0, tlen=0):
+    q = None if qual is None else ([qual] * len(seq) if isinstance(qual, int) else qual)
+    return dict(pos=pos, cigar=cigar, seq=seq, qual=q, mapq=mapq, flag=flag, tlen=tlen)
+
+
+def run(ref, records, start=1, stop=None, **pk):
+    st = build_store(records)
+    stop = len(ref) if stop is None else stop
+    return oracle.process_region(st, _abi.default_params(**pk), ref_from(ref), 0, start, stop)
+
+
+def at(res, locus, start=1):
+    i = locus - start
+    return dict(count=res.count[4 * i:4 * i + 4].tolist(), qual_sum=res.qual_sum[4 * i:4 * i + 4].tolist(),
+                mq=int(res.mq_sum[i]), q=int(res.q_sum[i]), bad=int(res.bad_pair[i]), clips=int(res.clips[i]),
+                dels=int(res.deletions[i]), ins=int(res.insertions[i]), pc=int(res.phys_cov[i]),
+                isz=int(res.insert_size[i]), call=int(res.call[i]))
+
+
+def test_single_read_trusted_flank_and_physcov():
+    ref = rand_ref(300)
+    seq = ref[100:140]                           # 40M at locus 101..140
+    res = run(ref, [read(101, [(40, "M")], seq)])
+    assert res.status == 0
+    # trusted offsets are 10..29 (flank 10): loci 111..130
+    assert at(res, 110)["count"] == [0, 0, 0, 0] and at(res, 131)["count"] == [0, 0, 0, 0]
+    b = "ACGT".index(ref[110])
+    p = at(res, 111)
+    assert p["count"][b] == 1 and p["qual_sum"][b] == 30 * 61 and p["mq"] == 61 and p["q"] == 30
+    assert res.stats.base_count == 20 and res.stats.read_count == 1
+    # unpaired: physical coverage [min(aStart,aEnd), max) = [101, 140): +1 at 101, -1 at 140
+    assert at(res, 100)["pc"] == 0 and at(res, 101)["pc"] == 1 and at(res, 139)["pc"] == 1 and at(res, 140)["pc"] == 0
+    assert at(res, 120)["isz"] == 39
+
+
+def test_soft_clips_bad_pairs_and_adjusted_mq():
+    ref = rand_ref(300)
+    seq = "ACGTA" + ref[99:129]                  # 5S30M at 100
+    res = run(ref, [read(100, [(5, "S"), (30, "M")], seq)])
+    # clipStart = locus - len = 95 (clip at read start), clipEnd = 99
+    assert at(res, 95)["clips"] == 1 and at(res, 99)["clips"] == 1 and at(res, 97)["clips"] == 0
+    assert [at(res, l)["bad"] for l in range(94, 101)] == [0, 1, 1, 1, 1, 1, 0]
+    # adjMq = roundDiv(60 * (35 - 5), 35) = (1800 + 17) / 35 = 51 -> mq + 1 = 52
+    assert at(res, 110)["mq"] == 52
+    # trailing clip: clipStart = locus (130), clipEnd = 134
+    seq2 = ref[99:129] + "TTTTT"
+    res2 = run(ref, [read(100, [(30, "M"), (5, "S")], seq2)])
+    assert at(res2, 130)["clips"] == 1 and at(res2, 134)["clips"] == 1
+    assert [at(res2, l)["bad"] for l in range(129, 136)] == [0, 1, 1, 1, 1, 1, 0]
+
+
+def test_single_base_clip_counts_twice():
+    ref = rand_ref(200)
+    res = run(ref, [read(50, [(1, "S"), (30, "M")], "A" + ref[49:79])])
+    # clipStart == clipEnd == 49: both increments land on the same pileup
+    assert at(res, 49)["clips"] == 2
+
+
+def test_H1_deletion_left_shift_double_counts():
+    # loci 146..149 = "CAAA", 150..153 "AAGT"... build: ...C A A A A G...
+    ref = list(rand_ref(300))
+    ref[148] = "C"                                # locus 149
+    for l in (150, 151, 152, 153):
+        ref[l - 1] = "A"
+    ref[153] = "G"                                # locus 154
+    ref = "".join(ref)
+    # read: 30M at 123..152, 1D at 153, 30M at 154..183
+    seq = ref[122:152] + ref[153:183]
+    res = run(ref, [read(123, [(30, "M"), (1, "D"), (30, "M")], seq)])
+    # the deletion slides from 153 to 150 (loci 149 'C' != 150 'A' stops it);
+    # each step adds the read base at rloc to locus dloc + 1 = 153, 152, 151
+    cA = lambda l: at(res, l)["count"][0]
+    assert cA(150) == 1 and cA(151) == 2 and cA(152) == 2 and cA(153) == 1
+    assert at(res, 150)["dels"] == 1 and at(res, 153)["dels"] == 0
+    # baseCount: 20 + 20 trusted M bases? offsets 10..49 of a 60-base read = 40, plus 3 shifted adds
+    assert res.stats.base_count == 43
+
+
+def test_insertion_left_shift_rotates():
+    ref = list(rand_ref(400))
+    for k, c in zip(range(300, 306), "TACACG"):  # loci 300..305
+        ref[k - 1] = c
+    ref[298] = "G"
+    ref = "".join(ref)
+    # 30M ending at 304, 2I "AC", 30M from 305
+    seq = ref[274:304] + "AC" + ref[304:334]
+    res = run(ref, [read(275, [(30, "M"), (2, "I"), (30, "M")], seq)] * 6)
+    # iloc slides 305 -> 301 over four steps; the string rotates AC->CA->AC->CA->AC
+    assert at(res, 301)["ins"] == 6 and at(res, 305)["ins"] == 0
+    i = 301 - 1
+    assert res.call[i] & _abi.PG_CALL_INS and res.insertion(i) == "AC"
+
+
+def test_H2_homozygous_deletion_updates_covered_pileups():
+    ref = rand_ref(400, seed=11)
+    recs = []
+    for k in range(8):
+        p = 150 + 2 * k
+        d = 200                                   # delete loci 200..202
+        seq = ref[p - 1:d - 1] + ref[d + 2:d + 2 + 40]
+        recs.append(read(p, [(d - p, "M"), (3, "D"), (40, "M")], seq))
+    res = run(ref, recs)
+    i = 200 - 1
+    assert at(res, 200)["dels"] == 8
+    assert (res.call[i] >> 9) & 7 == _abi.PG_CHANGE_DEL and res.indel_len[i] == 3
+    # pass 1 marks 201 and 202 deleted and adds the 8 deletions to them
+    for l in (201, 202):
+        assert at(res, l)["dels"] == 8 and at(res, l)["call"] & _abi.PG_CALL_DELETED
+        assert (at(res, l)["call"] >> 9) & 7 == 0
+    assert at(res, 203)["dels"] == 0
+
+
+def test_H3_left_shift_below_region_start_throws():
+    ref = list(rand_ref(300))
+    for l in range(95, 106):
+        ref[l - 1] = "A"
+    ref = "".join(ref)
+    seq = ref[79:101] + ref[102:130]             # 22M at 80..101, 1D at 102, 28M at 103..130
+    res = run(ref, [read(80, [(22, "M"), (1, "D"), (28, "M")], seq)], start=101, stop=300)
+    assert res.status == _abi.PG_ERR_INDEX
+    # the same read on a region starting at 1 is fine (shift stops at 95)
+    res = run(ref, [read(80, [(22, "M"), (1, "D"), (28, "M")], seq)])
+    assert res.status == 0 and at(res, 95)["dels"] == 1
+
+
+def test_H6_stable_order_on_ties():
+    ref = rand_ref(200)
+    l = 100
+    base = ref[l - 1]
+    alts = [c for c in "ACGT" if c != base]
+    a, b = alts[0], alts[1]                       # a < b in ACGT order
+    recs = []
+    for c in (a, b):
+        s = list(ref[79:129])
+        s[l - 80] = c
+        recs.append(read(80, [(50, "M")], "".join(s)))
+    res = run(ref, recs)
+    f = int(res.call[l - 1])
+    assert "ACGT"[f & 3] == a and "ACGT"[(f >> 2) & 3] == b
+    assert not f & _abi.PG_CALL_HOMO
+
+
+def test_validate_read_flags():
+    ref = rand_ref(300)
+    seq = ref[99:139]
+    recs = [read(100, [(40, "M")], seq, flag=0x400), read(100, [(40, "M")], seq, flag=0x100),
+            read(100, [(40, "M")], seq, flag=0x200), read(100, [(40, "M")], seq, flag=0x800)]
+    res = run(ref, recs)
+    assert res.stats.read_count == 1               # only the supplementary read is kept
+    res = run(ref, recs, duplicates=1, nonpf=1)
+    assert res.stats.read_count == 3               # secondary reads are always dropped
+
+
+def test_paired_read_before_region_carries_physcov():
+    ref = rand_ref(400)
+    seq = ref[49:99]
+    # proper pair, leftmost mate at 50, TLEN 300 -> insert [50, 350); region starts at 101
+    res = run(ref, [read(50, [(50, "M")], seq, flag=0x1 | 0x2 | 0x20 | 0x40, tlen=300)], start=101, stop=400)
+    assert res.stats.phys_cov_start == 1 and res.stats.insert_size_start == 300
+    assert at(res, 101, start=101)["pc"] == 1 and at(res, 349, start=101)["pc"] == 1
+    assert at(res, 350, start=101)["pc"] == 0 and at(res, 200, start=101)["isz"] == 300
+
+
+def test_invalid_pair_goes_to_bad_pairs():
+    ref = rand_ref(300)
+    seq = ref[99:139]
+    res = run(ref, [read(100, [(40, "M")], seq, flag=0x1 | 0x40, tlen=100)])  # paired, not proper
+    assert at(res, 120)["bad"] == 1 and at(res, 120)["count"] == [0, 0, 0, 0]
+    assert res.stats.base_count == 0
+
+
+def test_missing_qualities_use_default():
+    ref = rand_ref(300)
+    res = run(ref, [read(100, [(40, "M")], ref[99:139], qual=None)], default_qual=17)
+    assert at(res, 120)["q"] == 17
+
+
+@pytest.mark.parametrize("x,s", [(0.125, "0.13"), (0.375, "0.38"), (0.0, "0.00"), (1.0, "1.00"),
+                                 (float(np.float32(1) / np.float32(3)), "0.33"),
+                                 (float(np.float32(2) / np.float32(3)), "0.67"), (0.005, "0.01"),
+                                 (0.015, "0.02"), (0.994999, "0.99"), (0.995, "1.00"), (0.5, "0.50")])
+def test_H10_java_half_up_format(x, s):
+    assert oracle.java_format2(x) == s
+
+
+def test_contig_chunking():
+    # GenomeFile.contigRegions: nChunks = ceil(len/max), chunk = ceil(len/nChunks)
+    assert oracle.contig_regions(25, 10) == [(1, 9), (10, 18), (19, 25)]
+    assert oracle.contig_regions(20, 10) == [(1, 10), (11, 20)]
+    from pilon_gb300.regions import contig_regions
+    for n, c in [(25, 10), (20, 10), (1, 10), (10_000_001, 10_000_000), (123_456, 7_000)]:
+        assert contig_regions(n, c) == oracle.contig_regions(n, c)
+
+
+def test_H12_fasta_changes_naming():
+    ref = rand_ref(2000, seed=3)
+    sample = list(ref)
+    sample[999] = "ACGT"[("ACGT".index(ref[999]) + 1) % 4]   # SNP at locus 1000
+    sample = "".join(sample)
+    recs = []
+    for p in range(1, 1900, 5):
+        recs.append(read(p, [(100, "M")], sample[p - 1:p + 99]))
+    st = build_store(recs)
+    with tempfile.TemporaryDirectory() as d:
+        for name, out in [("chr1", "chr1_pilon"), ("gi|123|", "gi|123|pilon"), ("gi|123", "gi|123|pilon")]:
+            pre = os.path.join(d, "o")
+            assert oracle.polish(st, _abi.default_params(), [name], [ref_from(ref)], pre) == 0
+            fa = open(pre + ".fasta").read().splitlines()
+            assert fa[0] == ">" + out
+            assert all(len(l) == 80 for l in fa[1:-1]) and len(fa[-1]) == 2000 - 80 * (len(fa) - 2)
+            assert "".join(fa[1:])[999] == sample[999]
+            ch = open(pre + ".changes").read().splitlines()
+            assert ch == [f"{name}:1000 {out}:1000 {ref[999]} {sample[999]}"]
+            vcf = open(pre + ".vcf").read().splitlines()
+            body = [l for l in vcf if not l.startswith("#")]
+            assert len(body) == 2000
+            f = body[999].split("\t")
+            assert f[1] == "1000" and f[3] == ref[999] and f[4] == sample[999] and f[9] == "1/1"
+
+
+def test_kmer_tally_hand_case():
+    # five identical reads "ACGTTACG" (L=8), K=3: forward K-mers ACG->T, CGT->T, GTT->A, TTA->C, TAC->G
+    # reverse complement "CGTAACGT": CGT->A, GTA->A, TAA->C, AAC->G, ACG->T
+    recs = [read(10, [(8, "M")], "ACGTTACG", qual=30, mapq=20)] * 5
+    st = build_store(recs)
+    e = oracle.kmer_tally(st, _abi.default_params(), [(0, 5)], 3, min_depth=5)
+    nib = {"A": 1, "C": 2, "G": 4, "T": 8}
+    def key(k):
+        v = 0
+        for j, c in enumerate(k):
+            v |= nib[c] << (60 - 4 * j)
+        return v
+    got = {(int(x["key_hi"]), int(x["next"]), int(x["alt"]), int(x["depth"])) for x in e}
+    # CGT: 5 x T (forward) and 5 x A (reverse): tie on qual sums -> base A (lower index), het -> alt T
+    exp = {(key("ACG"), 3, -1, 10), (key("CGT"), 0, 3, 10), (key("GTT"), 0, -1, 5), (key("TTA"), 1, -1, 5),
+           (key("TAC"), 2, -1, 5), (key("GTA"), 0, -1, 5), (key("TAA"), 1, -1, 5), (key("AAC"), 2, -1, 5)}
+    assert got == exp

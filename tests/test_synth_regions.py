@@ -1,0 +1,57 @@
+"""Synthetic workloads and region planning (host logic, CPU only)."""
+import numpy as np
+
+from pilon_gb300 import synth
+from pilon_gb300.reads import CIGAR_OPS
+from pilon_gb300.regions import ReadIndex, contig_regions, parse_targets, plan_regions
+
+
+def test_generator_is_deterministic():
+    a = synth.generate(1, scale=0.2)
+    b = synth.generate(1, scale=0.2)
+    for f in ("pos", "aend", "flag", "mapq", "tlen", "cigar", "seq", "qual"):
+        assert np.array_equal(getattr(a.reads, f), getattr(b.reads, f)), f
+    assert all(np.array_equal(x, y) for x, y in zip(a.contigs, b.contigs))
+
+
+def test_reads_are_consistent():
+    d = synth.generate(2, scale=0.01)
+    r = d.reads
+    assert np.all(np.diff(r.pos) >= 0)
+    for i in range(0, r.n_reads, 97):
+        ops = r.read_cigar(i)
+        ref_len = sum(n for n, op in ops if op in "MDN=X")
+        read_len = sum(n for n, op in ops if op in "MIS=X")
+        assert r.aend[i] == r.pos[i] + ref_len - 1
+        assert read_len == r.l_seq[i]
+    # mapq-0 fraction and flags present
+    assert 0.01 < np.mean(r.mapq == 0) < 0.06
+    assert np.any(r.flag & 0x400) and np.any(r.flag & 0x100)
+
+
+def test_variants_present_in_reads():
+    d = synth.generate(1)
+    kinds = {v[1] for v in d.variants[0]}
+    assert kinds == {"snp", "ins", "del"}
+    r = d.reads
+    ops = r.cigar & 15
+    assert np.any(ops == CIGAR_OPS.index("I")) and np.any(ops == CIGAR_OPS.index("D"))
+    assert np.any(ops == CIGAR_OPS.index("S"))
+
+
+def test_region_read_ranges_cover_the_query_window():
+    d = synth.generate(3, scale=0.005)
+    lens = [c.size for c in d.contigs]
+    regs = plan_regions(d.reads, lens, chunk_size=5000)
+    r = d.reads
+    for (c, s, e, a, b) in regs:
+        qs, qe = max(s - 10000, 0), min(e + 10000, lens[c])
+        sel = (r.ref_id == c) & (r.pos <= qe) & (r.aend >= qs)
+        idx = np.nonzero(sel)[0]
+        assert idx.size == 0 or (idx.min() >= a and idx.max() < b)
+
+
+def test_targets():
+    names, lens = ["a", "b"], [1000, 500]
+    assert parse_targets("a:10-20,b", names, lens) == [(0, 10, 20), (1, 1, 500)]
+    assert contig_regions(1000, 300) == [(1, 250), (251, 500), (501, 750), (751, 1000)]
