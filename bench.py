@@ -246,7 +246,9 @@ def main():
     ap.add_argument("--batched", type=int, default=1)
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--variant", type=int, default=-1)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -291,23 +293,32 @@ def main():
     walk_bytes = walk_algorithmic_bytes(ds.reads, regions)
 
     eng = Engine(local)
-    if args.tile or args.warps:
-        eng.set_tuning(args.tile, args.warps)
+    if args.tile or args.warps or args.variant >= 0:
+        eng.set_tuning(args.tile, args.warps, args.variant)
     eng.set_reference(ds.contigs)
     eng.set_reads(ds.reads)
+    tuning = None
+    if args.autotune and not (args.tile or args.warps or args.variant >= 0):
+        from pilon_gb300.autotune import tune
+        best, table = tune(eng, regions, params, f"{ds.workload.name}:{args.scale}:{int(args.batched)}",
+                           batched=bool(args.batched))
+        tuning = {"tile_width": best[0], "warps": best[1], "variant": best[2], "walk_ms": best[3],
+                  "table": table}
+    clk = ClockSampler(local)
+    clk.__enter__()  # sampled from warm-up start to the end of the timed region
     for _ in range(args.warmup):
         eng.pileup_regions(regions, params, batched=bool(args.batched))
     barrier(dist)
     eng.sync()
     tot_ms, walk_ms, launches = [], [], 0
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            eng.pileup_regions(regions, params, batched=bool(args.batched))
-            w, t, n = eng.last_kernel_ms()
-            tot_ms.append(t)
-            walk_ms.append(w)
-            launches += n
+    for _ in range(args.steps):
+        eng.pileup_regions(regions, params, batched=bool(args.batched))
+        w, t, n = eng.last_kernel_ms()
+        tot_ms.append(t)
+        walk_ms.append(w)
+        launches += n
     eng.sync()
+    clk.__exit__()
     barrier(dist)
     dev_s = max_over_ranks(dist, sum(tot_ms) / 1e3)
     value = units * ws * args.steps / dev_s / 1e9
@@ -366,6 +377,7 @@ def main():
                      "walk_ms": walk_avg * 1e3, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"
                      if peaks else "fallback"},
         "gpu_launches": launches,
+        "tuning": tuning,
         "clocks": clk.summary(),
         "e2e": e2e,
         "cpu_baseline": cpu,

@@ -217,10 +217,11 @@ pg_status pg_fetch_stats(pg_ctx *ctx, int32_t region, pg_region_stats *stats);
 /* Copies one region's arrays into caller host buffers. */
 pg_status pg_fetch_region(pg_ctx *ctx, int32_t region, pg_region_out *out);
 
-/* Tile width (positions per CTA tile, 1024..8192, power of two) and warps per
- * CTA of the pileup kernel; 0 keeps the current value.  The autotuner of the
- * host package chooses these. */
-pg_status pg_set_tuning(pg_ctx *ctx, int32_t tile_width, int32_t warps_per_cta);
+/* Launch shape of the pileup walk kernel: tile width (positions per CTA,
+ * a power of two in [256, 4096]), warps per CTA (1..16) and variant (lanes
+ * per read: 0 = 32, 1 = 16, 2 = 8); 0 / -1 keep the current value.  The host
+ * package's autotuner picks these. */
+pg_status pg_set_tuning(pg_ctx *ctx, int32_t tile_width, int32_t warps_per_cta, int32_t variant);
 
 /* ---- k-mer tally ----------------------------------------------------------
  * Assembler.addRead/addToPileups for every window (S/Assembler.scala:55-87)

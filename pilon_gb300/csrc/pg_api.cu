@@ -38,10 +38,10 @@ struct pg_ctx {
   DevBuf d_ext;
   // per-call buffers
   DevBuf regions, walk_tiles, call_tile_region, chunks, stats;
-  DevBuf rec_count, rec_qsum, rec_i32[10], rec_call, rec_score, rec_indel_len, rec_ins_str;
-  DevBuf bucket_count, bucket_off, bucket_fill, cand_count, cand_off, tile_sums;
-  DevBuf events, events_sorted, cands, pool, counters, run_max;
-  int64_t event_cap = 0, pool_cap = 0;
+  DevBuf rec_count, rec_qsum, rec_i32[10], rec_call, rec_score, rec_indel_len, rec_ins_str, rec_ev_end;
+  DevBuf cand_count, cand_off, tile_sums;
+  DevBuf events, events_sorted, cands, pool, counters, run_max, chunk_stats, spool;
+  int64_t event_cap = 0, pool_cap = 0, spool_cap = 0;
   int32_t cand_cap = 0;
   DevBuf staging_dev;
   void* staging_host = nullptr;
@@ -63,7 +63,7 @@ struct pg_ctx {
   DevBuf kwin, kpre, kslot_base, kslot_cap, kx_base, kx_cap, kkeys, kcnt, kqs, kmq, kq;
   DevBuf kx_keys, kx_used, kx_cnt, kx_qs, kx_mq, kx_q, kedges, kcount;
   // tuning
-  int32_t tile_width = 2048, warps = 16;
+  int32_t tile_width = 2048, warps = 16, packed = 0;
 };
 
 namespace {
@@ -135,6 +135,7 @@ Records records(pg_ctx* c) {
   r.ins_qual = P<int32_t>(c->rec_i32[7]);
   r.phys_cov = P<int32_t>(c->rec_i32[8]);
   r.insert_size = P<int32_t>(c->rec_i32[9]);
+  r.ev_end = P<int32_t>(c->rec_ev_end);
   r.call = P<uint32_t>(c->rec_call);
   r.score = P<int64_t>(c->rec_score);
   r.indel_len = P<int32_t>(c->rec_indel_len);
@@ -142,12 +143,14 @@ Records records(pg_ctx* c) {
   return r;
 }
 
-// Counters kept on the device for one call: [0] events, [1] pool bytes.
-enum { CNT_EVENTS = 0, CNT_POOL = 1, CNT_N = 2 };
+// Counters kept on the device for one call: [0] events, [1] pool bytes,
+// [2] string-pool words of the current run, [3] most string-pool words of any run.
+enum { CNT_EVENTS = 0, CNT_POOL = 1, CNT_SPOOL = 2, CNT_SPOOL_MAX = 3, CNT_N = 4 };
 // run_max: [0] max events of a run, [1] max candidates of a run
-__global__ void k_track(const unsigned long long* counters, const int32_t* cand_total, unsigned long long* run_max) {
+__global__ void k_track(unsigned long long* counters, const int32_t* cand_total, unsigned long long* run_max) {
   atomicMax(&run_max[0], counters[CNT_EVENTS]);
   atomicMax(&run_max[1], (unsigned long long)(*cand_total));
+  atomicMax(&counters[CNT_SPOOL_MAX], counters[CNT_SPOOL]);
 }
 
 struct Plan {
@@ -206,8 +209,9 @@ void pg_close(pg_ctx* c) {
   }
   DevBuf* all[] = {&c->ref, &c->d_ext, &c->regions, &c->walk_tiles, &c->call_tile_region, &c->chunks, &c->stats,
                    &c->rec_count, &c->rec_qsum, &c->rec_call, &c->rec_score, &c->rec_indel_len, &c->rec_ins_str,
-                   &c->bucket_count, &c->bucket_off, &c->bucket_fill, &c->cand_count, &c->cand_off, &c->tile_sums,
-                   &c->events, &c->events_sorted, &c->cands, &c->pool, &c->counters, &c->run_max, &c->staging_dev};
+                   &c->rec_ev_end, &c->cand_count, &c->cand_off, &c->tile_sums,
+                   &c->events, &c->events_sorted, &c->cands, &c->pool, &c->counters, &c->run_max, &c->staging_dev,
+                   &c->chunk_stats, &c->spool};
   for (DevBuf* b : all) release(*b);
   DevBuf* km[] = {&c->kwin, &c->kpre, &c->kslot_base, &c->kslot_cap, &c->kx_base, &c->kx_cap, &c->kkeys, &c->kcnt,
                   &c->kqs, &c->kmq, &c->kq, &c->kx_keys, &c->kx_used, &c->kx_cnt, &c->kx_qs, &c->kx_mq, &c->kx_q,
@@ -227,7 +231,7 @@ void pg_close(pg_ctx* c) {
 
 const char* pg_last_error(const pg_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
-pg_status pg_set_tuning(pg_ctx* c, int32_t tile_width, int32_t warps_per_cta) {
+pg_status pg_set_tuning(pg_ctx* c, int32_t tile_width, int32_t warps_per_cta, int32_t variant) {
   if (!c) return PG_ERR_ARG;
   if (tile_width) {
     if (tile_width < 256 || tile_width > 4096 || (tile_width & (tile_width - 1)))
@@ -237,6 +241,10 @@ pg_status pg_set_tuning(pg_ctx* c, int32_t tile_width, int32_t warps_per_cta) {
   if (warps_per_cta) {
     if (warps_per_cta < 1 || warps_per_cta > 16) return fail(c, PG_ERR_ARG, "warps per CTA must be in [1, 16]");
     c->warps = warps_per_cta;
+  }
+  if (variant >= 0) {
+    if (variant > 2) return fail(c, PG_ERR_ARG, "variant must be 0, 1 or 2");
+    c->packed = variant;
   }
   return PG_OK;
 }
@@ -359,16 +367,16 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   Records rec = records(c);
   unsigned long long* counters = P<unsigned long long>(c->counters);
 
-  cudaMemsetAsync(P<int32_t>(c->bucket_count) + t0, 0, sizeof(int32_t) * (tn + 1), s);
-  cudaMemsetAsync(P<int32_t>(c->bucket_fill) + t0, 0, sizeof(int32_t) * (tn + 1), s);
   cudaMemsetAsync(P<int32_t>(c->cand_count) + t0, 0, sizeof(int32_t) * (tn + 1), s);
   cudaMemsetAsync(&counters[CNT_EVENTS], 0, sizeof(unsigned long long), s);
+  cudaMemsetAsync(&counters[CNT_SPOOL], 0, sizeof(unsigned long long), s);
 
   launch_tile_ranges(c->R, d_regions, P<WalkTile>(c->walk_tiles) + w0, wn, P<ReadExtent>(c->d_ext), s);
 
   WalkArgs wa;
   wa.R = c->R; wa.regions = d_regions; wa.tiles = P<WalkTile>(c->walk_tiles); wa.n_tiles = wn;
   wa.rec = rec; wa.stats = d_stats; wa.P = dp; wa.ref = P<uint8_t>(c->ref); wa.tile_width = c->tile_width;
+  wa.packed = c->packed;
   while ((int32_t)c->wev.size() < 2 * (c->n_runs + 1)) {
     cudaEvent_t e;
     cudaEventCreate(&e);
@@ -382,21 +390,23 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   EventArgs ea;
   ea.R = c->R; ea.regions = d_regions; ea.chunks = P<ReadChunk>(c->chunks); ea.n_chunks = chn; ea.rec = rec;
   ea.stats = d_stats; ea.P = dp; ea.ref = P<uint8_t>(c->ref); ea.events = P<Event>(c->events);
-  ea.n_events = &counters[CNT_EVENTS]; ea.event_cap = c->event_cap; ea.bucket_count = P<int32_t>(c->bucket_count);
+  ea.n_events = &counters[CNT_EVENTS]; ea.event_cap = c->event_cap;
+  ea.chunk_stats = P<ChunkStats>(c->chunk_stats);
+  ea.spool = P<uint64_t>(c->spool); ea.spool_fill = &counters[CNT_SPOOL]; ea.spool_cap = c->spool_cap;
   launch_read_events(ea, ch0, chn, s);
 
-  launch_region_prep(d_regions + r0, d_stats + r0, r1 - r0, dp, s);
-  launch_scan_small(P<int32_t>(c->bucket_count) + t0, P<int32_t>(c->bucket_off) + t0, tn, s);
-  launch_event_scatter(P<Event>(c->events), &counters[CNT_EVENTS], d_regions, P<int32_t>(c->bucket_off),
-                       P<int32_t>(c->bucket_fill), P<Event>(c->events_sorted), s, c->event_cap);
+  launch_region_prep(d_regions + r0, d_stats + r0, P<ChunkStats>(c->chunk_stats), r1 - r0, dp, s);
   launch_physcov_scan(d_regions, P<int32_t>(c->call_tile_region), t0, tn, rec, d_stats, P<int32_t>(c->tile_sums),
                       r0, r1 - r0, s);
+  launch_event_scatter(P<Event>(c->events), &counters[CNT_EVENTS], rec.ev_end, P<Event>(c->events_sorted), s,
+                       c->event_cap);
 
   CallArgs ca;
   ca.R = c->R; ca.regions = d_regions; ca.call_tile_region = P<int32_t>(c->call_tile_region);
   ca.n_call_tiles = tn; ca.rec = rec; ca.stats = d_stats; ca.P = dp; ca.ref = P<uint8_t>(c->ref);
-  ca.ev_sorted = P<Event>(c->events_sorted); ca.bucket_off = P<int32_t>(c->bucket_off);
+  ca.ev_sorted = P<Event>(c->events_sorted);
   ca.event_cap = c->event_cap;
+  ca.spool = P<uint64_t>(c->spool);
   ca.cand_count = P<int32_t>(c->cand_count); ca.pool = P<char>(c->pool); ca.pool_fill = &counters[CNT_POOL];
   ca.pool_cap = c->pool_cap;
   launch_call(ca, t0, tn, s);
@@ -405,10 +415,10 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   launch_resolve(d_regions + r0, r1 - r0, P<int32_t>(c->cand_off), P<Cand>(c->cands), c->cand_cap, d_stats + r0, s);
   launch_apply_spans(ca, P<Cand>(c->cands), P<int32_t>(c->cand_off) + t0 + tn, c->cand_cap, s);
   k_track<<<1, 1, 0, s>>>(counters, P<int32_t>(c->cand_off) + t0 + tn, P<unsigned long long>(c->run_max));
-  // kernels of this run: tile ranges + walk, read events, region prep, two
-  // small scans, event scatter, three scan phases, call, candidate list,
+  // kernels of this run: tile ranges + walk, read events, region prep, three
+  // scan phases, event scatter, call, candidate scan, candidate list,
   // resolve, span update, overflow tracking
-  c->launches += 2 * (wn > 0) + (chn > 0) + 1 + 2 + 1 + 3 * (tn > 0) + 2 * (tn > 0) + 1 + 1 + 1;
+  c->launches += 2 * (wn > 0) + (chn > 0) + 1 + 3 * (tn > 0) + 1 + 2 * (tn > 0) + 1 + 1 + 1 + 1;
 }
 
 pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions, const pg_params* params,
@@ -447,8 +457,10 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
     g.call_tile0 = (int32_t)plan.call_region.size();
     g.n_call_tiles = (g.size + kCallTile - 1) / kCallTile;
     for (int32_t k = 0; k < g.n_call_tiles; k++) plan.call_region.push_back(r);
+    g.chunk0 = (int32_t)plan.chunks.size();
     for (int64_t lo = q.read_begin; lo < q.read_end; lo += kReadsPerChunk)
       plan.chunks.push_back(ReadChunk{r, 0, lo, std::min<int64_t>(lo + kReadsPerChunk, q.read_end)});
+    g.n_chunks = (int32_t)plan.chunks.size() - g.chunk0;
     pos += g.size;
   }
   c->n_regions = n_regions;
@@ -468,6 +480,7 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
   EN(c->walk_tiles, sizeof(WalkTile) * std::max<size_t>(plan.walk.size(), 1));
   EN(c->call_tile_region, sizeof(int32_t) * (n_call + 1));
   EN(c->chunks, sizeof(ReadChunk) * std::max<size_t>(plan.chunks.size(), 1));
+  EN(c->chunk_stats, sizeof(ChunkStats) * std::max<size_t>(plan.chunks.size(), 1));
   EN(c->rec_count, 16 * (size_t)pos);
   EN(c->rec_qsum, 32 * (size_t)pos);
   for (auto& b : c->rec_i32) EN(b, 4 * (size_t)pos);
@@ -475,14 +488,15 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
   EN(c->rec_score, 8 * (size_t)pos);
   EN(c->rec_indel_len, 4 * (size_t)pos);
   EN(c->rec_ins_str, 4 * (size_t)pos);
-  for (DevBuf* b : {&c->bucket_count, &c->bucket_off, &c->bucket_fill, &c->cand_count, &c->cand_off})
-    EN(*b, sizeof(int32_t) * (n_call + 2));
-  EN(c->tile_sums, sizeof(int32_t) * 2 * (n_call + 1));
+  EN(c->rec_ev_end, 4 * (size_t)pos);
+  for (DevBuf* b : {&c->cand_count, &c->cand_off}) EN(*b, sizeof(int32_t) * (n_call + 2));
+  EN(c->tile_sums, sizeof(int32_t) * 3 * (n_call + 1));
   EN(c->counters, sizeof(unsigned long long) * CNT_N);
   EN(c->run_max, sizeof(unsigned long long) * 2);
   if (c->event_cap == 0) c->event_cap = (int64_t)(2 * c->ext.n_indel_ops + 4096);
   if (c->cand_cap == 0) c->cand_cap = (int32_t)std::min<int64_t>(pos / 16 + 4096, INT32_MAX / 2);
   if (c->pool_cap == 0) c->pool_cap = 1 << 20;
+  if (c->spool_cap == 0) c->spool_cap = 1 << 16;
   // ---- upload the plan
   const size_t b_reg = sizeof(RegionDev) * n_regions, b_walk = sizeof(WalkTile) * plan.walk.size(),
                b_call = sizeof(int32_t) * n_call, b_ch = sizeof(ReadChunk) * plan.chunks.size();
@@ -500,6 +514,7 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
     if ((s = ensure(c, c->events_sorted, sizeof(Event) * c->event_cap))) return s;
     if ((s = ensure(c, c->cands, sizeof(Cand) * (size_t)c->cand_cap))) return s;
     if ((s = ensure(c, c->pool, (size_t)c->pool_cap))) return s;
+    if ((s = ensure(c, c->spool, 8 * (size_t)c->spool_cap))) return s;
     cudaStream_t st = c->stream;
     c->launches = 0;
     c->n_runs = 0;
@@ -542,6 +557,7 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
     if ((int64_t)hm[0] > c->event_cap) { c->event_cap = (int64_t)hm[0] * 2 + 4096; grow = true; }
     if ((int64_t)hm[1] > c->cand_cap) { c->cand_cap = (int32_t)std::min<int64_t>((int64_t)hm[1] * 2 + 4096, INT32_MAX / 2); grow = true; }
     if ((int64_t)hc[CNT_POOL] > c->pool_cap) { c->pool_cap = (int64_t)hc[CNT_POOL] * 2 + 4096; grow = true; }
+    if ((int64_t)hc[CNT_SPOOL_MAX] > c->spool_cap) { c->spool_cap = (int64_t)hc[CNT_SPOOL_MAX] * 2 + 4096; grow = true; }
     if (!grow) {
       for (int32_t r = 0; r < n_regions; r++)
         if (c->stats_h[r].error)

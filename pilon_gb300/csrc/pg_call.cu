@@ -20,12 +20,17 @@ namespace pg {
 
 #define FULL 0xffffffffu
 
-__device__ inline CallCtx make_ctx(const CallArgs& a, const RegionDev& g, int32_t tile) {
+// n_ev = insertions + deletions of the position before any deletion-span update
+__device__ inline CallCtx make_ctx(const CallArgs& a, const RegionDev& g, int64_t gp, int32_t n_ev) {
   CallCtx c;
   c.ev = a.ev_sorted;
-  c.ev_lo = min((int64_t)a.bucket_off[tile], a.event_cap);
-  c.ev_hi = min((int64_t)a.bucket_off[tile + 1], a.event_cap);
-  c.R = a.R;
+  c.ev_lo = c.ev_hi = 0;
+  if (n_ev > 0) {
+    const int64_t hi = a.rec.ev_end[gp];
+    c.ev_hi = min(hi, a.event_cap);
+    c.ev_lo = min(max(hi - n_ev, (int64_t)0), a.event_cap);
+  }
+  c.spool = a.spool;
   c.ref = a.ref;
   c.ref_off = g.ref_off;
   c.contig_len = g.contig_len;
@@ -35,17 +40,21 @@ __device__ inline CallCtx make_ctx(const CallArgs& a, const RegionDev& g, int32_
   return c;
 }
 
-__global__ void __launch_bounds__(kCallTile) k_call(CallArgs a, int32_t tile_begin) {
-  const int32_t t = tile_begin + blockIdx.x;
+// 256 threads per CTA, kCallTile / 256 CTAs per call tile: a thread that runs
+// a long indel vote holds back only its own small CTA.
+constexpr int kCallThreads = 256;
+__global__ void __launch_bounds__(kCallThreads) k_call(CallArgs a, int32_t tile_begin) {
+  const int32_t t = tile_begin + blockIdx.x / (kCallTile / kCallThreads);
   const int32_t r = a.call_tile_region[t];
   const RegionDev g = a.regions[r];
-  const int32_t p = (t - g.call_tile0) * kCallTile + threadIdx.x;
+  const int32_t p = (t - g.call_tile0) * kCallTile + (blockIdx.x % (kCallTile / kCallThreads)) * kCallThreads +
+                    threadIdx.x;
   uint32_t change = 0;
   if (p < g.size) {
     const int64_t gp = g.pos_base + p;
     PosRec rec;
     load_rec(a.rec, gp, rec);
-    CallCtx c = make_ctx(a, g, t);
+    CallCtx c = make_ctx(a, g, gp, wadd(rec.insertions, rec.deletions));
     const int64_t locus0 = (int64_t)g.start - 1 + p;
     CallOut o = base_call(rec, a.P, c, gp, locus0);
     int32_t ins = -1;
@@ -62,7 +71,7 @@ __global__ void __launch_bounds__(kCallTile) k_call(CallArgs a, int32_t tile_beg
         const uint8_t b = (f & PG_CALL_HAS_BASE) ? (uint8_t)"ACGT"[f & 3u] : (uint8_t)'N';
         const uint8_t alt = (uint8_t)"ACGT"[(f >> 2) & 3u];
         const bool homo = f & PG_CALL_HOMO, homoIndel = f & PG_CALL_HOMO_INDEL;
-        const int64_t q = n > 0 ? o.score / n : 0;
+        const int64_t q = n > 0 ? div_s64(o.score, n) : 0;
         if (homo && b == rb && q >= 10 && !(isIns || isDel)) f |= PG_CALL_CONFIRMED;
         else if (isIns && homoIndel) change = PG_CHANGE_INS;
         else if (isDel && homoIndel) change = PG_CHANGE_DEL;
@@ -84,7 +93,7 @@ __global__ void __launch_bounds__(kCallTile) k_call(CallArgs a, int32_t tile_beg
 
 void launch_call(const CallArgs& a, int32_t tile_begin, int32_t n_tiles, cudaStream_t s) {
   if (n_tiles <= 0) return;
-  k_call<<<n_tiles, kCallTile, 0, s>>>(a, tile_begin);
+  k_call<<<n_tiles * (kCallTile / kCallThreads), kCallThreads, 0, s>>>(a, tile_begin);
 }
 
 __global__ void __launch_bounds__(kCallTile) k_cand_list(CallArgs a, const int32_t* cand_off, Cand* cands,
@@ -134,31 +143,47 @@ void launch_cand_list(const CallArgs& a, const int32_t* cand_off, Cand* cands, i
 }
 
 // Pass 1 is a left-to-right scan: a candidate inside an earlier accepted
-// homozygous deletion is skipped (`!deleted(i)`); suppressed ones get kind < 0.
+// homozygous deletion is skipped (`!deleted(i)`).  Only deletions can suppress
+// later candidates, so one warp per region walks the region's candidates 32 at
+// a time and decides the (sparse) deletion candidates in order; rejected ones
+// get kind < 0.  n_changes starts at the candidate count; k_apply_spans
+// subtracts the candidates that fall inside accepted deletions.
 __global__ void k_resolve(const RegionDev* regions, int32_t n_regions, const int32_t* cand_off, Cand* cands,
                           int32_t cand_cap, StatsDev* stats) {
-  int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (r >= n_regions) return;
   const RegionDev& g = regions[r];
   if (g.n_call_tiles == 0) return;
   const int32_t lo = cand_off[g.call_tile0], hi = min(cand_off[g.call_tile0 + g.n_call_tiles], cand_cap);
-  int32_t lastEnd = -1, accepted = 0;
-  for (int32_t k = lo; k < hi; k++) {
-    Cand c = cands[k];
-    if (c.p <= lastEnd) {
-      cands[k].kind = -c.kind;
-      continue;
+  int32_t lastEnd = -1;
+  for (int32_t base = lo; base < hi; base += 32) {
+    const int32_t k = base + lane;
+    int32_t p = 0, len = 0;
+    bool isDel = false;
+    if (k < hi) {
+      const Cand c = cands[k];
+      isDel = c.kind == PG_CHANGE_DEL;
+      p = c.p;
+      len = c.len;
     }
-    accepted++;
-    if (c.kind == PG_CHANGE_DEL) lastEnd = max(lastEnd, c.p + c.len - 1);
+    unsigned m = __ballot_sync(FULL, isDel);
+    while (m) {
+      const int j = __ffs(m) - 1;
+      m &= m - 1;
+      const int32_t pj = __shfl_sync(FULL, p, j), lj = __shfl_sync(FULL, len, j);
+      const bool accept = pj > lastEnd;
+      if (lane == j && !accept) cands[k].kind = -PG_CHANGE_DEL;
+      if (accept) lastEnd = pj + lj - 1;
+    }
   }
-  stats[r].n_changes = accepted;
+  if (lane == 0) stats[r].n_changes = max(hi - lo, 0);
 }
 
 void launch_resolve(const RegionDev* regions, int32_t n_regions, const int32_t* cand_off, Cand* cands,
                     int32_t cand_cap, StatsDev* stats, cudaStream_t s) {
   if (n_regions == 0) return;
-  k_resolve<<<(n_regions + 127) / 128, 128, 0, s>>>(regions, n_regions, cand_off, cands, cand_cap, stats);
+  k_resolve<<<(n_regions + 3) / 4, 128, 0, s>>>(regions, n_regions, cand_off, cands, cand_cap, stats);
 }
 
 __global__ void k_apply_spans(CallArgs a, const Cand* cands, const int32_t* cand_total, int32_t cand_cap) {
@@ -168,17 +193,19 @@ __global__ void k_apply_spans(CallArgs a, const Cand* cands, const int32_t* cand
     if (c.kind != PG_CHANGE_DEL) continue;
     const RegionDev g = a.regions[c.region];
     const int32_t d = a.rec.deletions[c.gpos];
+    int32_t removed = 0;
     for (int32_t j = 1; j < c.len; j++) {
       const int32_t p = c.p + j;
       if (p >= g.size) break;
       const int64_t gp = g.pos_base + p;
-      a.rec.deletions[gp] = wadd(a.rec.deletions[gp], d);
+      const int32_t del0 = a.rec.deletions[gp];
+      a.rec.deletions[gp] = wadd(del0, d);
       PosRec rec;
       load_rec(a.rec, gp, rec);
-      const int32_t tile = g.call_tile0 + p / kCallTile;
-      CallCtx cx = make_ctx(a, g, tile);
+      CallCtx cx = make_ctx(a, g, gp, wadd(rec.insertions, del0));
       CallOut o = base_call(rec, a.P, cx, gp, (int64_t)g.start - 1 + p);
       const uint32_t old = a.rec.call[gp];
+      if (PG_CALL_CHANGE(old)) removed++;
       int32_t ins = -1;
       if (o.flags & PG_CALL_INS) ins = (old & PG_CALL_INS) ? a.rec.ins_str[gp] : pool_insertion(cx, cx.ev[o.win_event]);
       a.rec.call[gp] = o.flags | PG_CALL_DELETED;
@@ -186,6 +213,7 @@ __global__ void k_apply_spans(CallArgs a, const Cand* cands, const int32_t* cand
       a.rec.indel_len[gp] = o.indel_len;
       a.rec.ins_str[gp] = ins;
     }
+    if (removed) atomicSub(&a.stats[c.region].n_changes, removed);
   }
 }
 

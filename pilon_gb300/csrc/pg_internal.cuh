@@ -37,6 +37,7 @@ struct Reads {  // device pointers of the read store
 
 struct RegionDev {       // per region, device copy
   int32_t contig, start, stop, size;
+  int32_t chunk0, n_chunks;  // read chunks of this region
   int64_t pos_base;      // first global position
   int64_t ref_off;       // offset of the contig in the concatenated reference
   int64_t contig_len;
@@ -66,9 +67,16 @@ struct ReadChunk {       // reads [lo, hi) fed to region `region`
   int64_t lo, hi;
 };
 
+struct ChunkStats {      // per read chunk: partial sums of the region statistics
+  unsigned long long read_count, base_count, fr_count, fr_sum, fr_sumsq, rf_count, rf_sum, rf_sumsq;
+  int32_t phys_cov_start, insert_size_start, error, pad;
+};
+
 struct Event {           // one insertion or deletion added to a pileup
   int64_t gpos;
   int64_t read;
+  uint64_t key;          // insertions: 4-bit codes of the (rotated) string, characters 0..15
+  int64_t sp;            // insertions longer than 16: characters 16.. packed 16 per word in the string pool
   int32_t region;
   int32_t len;
   int32_t roff;          // read offset of the indel (insertions)
@@ -85,6 +93,7 @@ struct Records {
   longlong2 *qual_sum;   // two longlong2 per position
   int32_t *mq_sum, *q_sum, *bad_pair, *clips, *deletions, *del_qual, *insertions, *ins_qual;
   int32_t *phys_cov, *insert_size;
+  int32_t *ev_end;       // events of a position: [ev_end - (insertions + deletions), ev_end)
   uint32_t *call;
   int64_t *score;
   int32_t *indel_len, *ins_str;
@@ -107,7 +116,7 @@ struct DevParams {
 };
 
 constexpr int kCallTile = 1024;     // positions per call / scan tile
-constexpr int kReadsPerChunk = 4096;
+constexpr int kReadsPerChunk = 256;   // one read per thread of k_read_events
 constexpr int64_t kMaxReadsPerPass = 120000;  // keeps a tile's uint32 qual sums exact
 
 // ---- Java integer helpers (wrapping Int, truncating division) -------------
@@ -131,6 +140,12 @@ __device__ inline uint32_t read_nib(const Reads& R, int64_t i, int32_t k) {
 }
 __device__ inline uint8_t upper(uint8_t c) { return (c >= 'a' && c <= 'z') ? (uint8_t)(c - 32) : c; }
 
+// Non-negative a / positive b, in 32 bits when both fit (same result).
+__device__ inline int64_t div_s64(int64_t a, int64_t b) {
+  if ((uint64_t)a <= 0xffffffffull && (uint64_t)b <= 0xffffffffull) return (int64_t)((uint32_t)a / (uint32_t)b);
+  return a / b;
+}
+
 // ---- Per-position call (PileUp.BaseCall, S/PileUp.scala:132-255) -----------
 struct PosRec {
   int64_t cnt[4], qs[4];
@@ -147,18 +162,29 @@ __device__ inline void load_rec(const Records& Rc, int64_t gp, PosRec& r) {
   r.insertions = Rc.insertions[gp]; r.ins_qual = Rc.ins_qual[gp];
 }
 
+// v[i] for a run-time i without dynamic indexing (keeps the array in registers)
+__device__ inline int64_t pick4(const int64_t v[4], int i) {
+  return i == 0 ? v[0] : i == 1 ? v[1] : i == 2 ? v[2] : v[3];
+}
+
 // Stable descending order of four sums: first and second index.
 __device__ inline void order2(const int64_t v[4], int& o0, int& o1) {
   o0 = 0;
-  for (int i = 1; i < 4; i++) if (v[i] > v[o0]) o0 = i;
-  o1 = o0 == 0 ? 1 : 0;
-  for (int i = 0; i < 4; i++) if (i != o0 && v[i] > v[o1]) o1 = i;
+  int64_t m0 = v[0];
+#pragma unroll
+  for (int i = 1; i < 4; i++)
+    if (v[i] > m0) { o0 = i; m0 = v[i]; }
+  o1 = -1;
+  int64_t m1 = 0;
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+    if (i != o0 && (o1 < 0 || v[i] > m1)) { o1 = i; m1 = v[i]; }
 }
 
 struct CallCtx {         // what the indel vote needs
-  const Event* ev;       // events bucketed by call tile
-  int64_t ev_lo, ev_hi;  // bucket of this position's tile (clamped to the buffer)
-  Reads R;
+  const Event* ev;       // events grouped by position
+  int64_t ev_lo, ev_hi;  // this position's events (clamped to the buffer)
+  const uint64_t* spool; // packed tails of insertions longer than 16
   const uint8_t* ref;    // concatenated reference
   int64_t ref_off;       // contig offset
   int64_t contig_len;
@@ -167,18 +193,19 @@ struct CallCtx {         // what the indel vote needs
   int64_t pool_cap;
 };
 
-__device__ inline uint32_t ins_char(const Reads& R, const Event& e, int32_t j) {
-  int32_t rot = e.kind_rot & 0x7fffffff;
-  int32_t k = j - rot;
-  if (k < 0) k += e.len;
-  return read_nib(R, e.read, e.roff + k);
+// character j (4-bit code) of an insertion event's string
+__device__ inline uint32_t ins_char(const CallCtx& c, const Event& e, int32_t j) {
+  if (j < 16) return (uint32_t)(e.key >> (60 - 4 * j)) & 15u;
+  const int32_t t = j - 16;
+  return (uint32_t)(c.spool[e.sp + (t >> 4)] >> (60 - 4 * (t & 15))) & 15u;
 }
 
-__device__ inline bool same_indel(const Reads& R, const Event& a, const Event& b) {
+__device__ inline bool same_indel(const CallCtx& c, const Event& a, const Event& b) {
   if (a.len != b.len) return false;
   if (a.kind_rot < 0) return true;  // deletions at one position: same length = same reference slice
-  for (int32_t j = 0; j < a.len; j++)
-    if (ins_char(R, a, j) != ins_char(R, b, j)) return false;
+  if (a.key != b.key) return false;
+  for (int32_t w = 0; w < (a.len - 16 + 15) / 16; w++)  // tail words (none when len <= 16)
+    if (c.spool[a.sp + w] != c.spool[b.sp + w]) return false;
   return true;
 }
 
@@ -190,18 +217,18 @@ __device__ inline int64_t indel_vote(const CallCtx& c, int64_t gp, bool del) {
   int64_t cnt = 0, total = 0;
   for (int64_t k = c.ev_lo; k < c.ev_hi; k++) {
     const Event& e = c.ev[k];
-    if (e.gpos != gp || ((e.kind_rot < 0) != del)) continue;
+    if ((e.kind_rot < 0) != del) continue;
     total++;
     if (cnt == 0) { cand = k; cnt = 1; }
-    else if (same_indel(c.R, e, c.ev[cand])) cnt++;
+    else if (same_indel(c, e, c.ev[cand])) cnt++;
     else cnt--;
   }
   if (cand < 0) return -1;
   int64_t win = 0;
   for (int64_t k = c.ev_lo; k < c.ev_hi; k++) {
     const Event& e = c.ev[k];
-    if (e.gpos != gp || ((e.kind_rot < 0) != del)) continue;
-    if (same_indel(c.R, e, c.ev[cand])) win++;
+    if ((e.kind_rot < 0) != del) continue;
+    if (same_indel(c, e, c.ev[cand])) win++;
   }
   if (win < 2 || win <= total / 2) return -1;
   return cand;
@@ -209,7 +236,7 @@ __device__ inline int64_t indel_vote(const CallCtx& c, int64_t gp, bool del) {
 
 __device__ inline bool insertion_has_n(const CallCtx& c, const Event& e) {
   for (int32_t j = 0; j < e.len; j++)
-    if (ins_char(c.R, e, j) == 15u) return true;  // 'N'
+    if (ins_char(c, e, j) == 15u) return true;  // 'N'
   return false;
 }
 
@@ -227,7 +254,7 @@ __device__ inline CallOut base_call(const PosRec& r, const DevParams& P, const C
   int64_t n = r.cnt[0] + r.cnt[1] + r.cnt[2] + r.cnt[3];
   int o0, o1;
   if (r.q_sum > 0) order2(r.qs, o0, o1); else order2(r.cnt, o0, o1);
-  int64_t baseSum = r.qs[o0], altBaseSum = r.qs[o1];
+  int64_t baseSum = pick4(r.qs, o0), altBaseSum = pick4(r.qs, o1);
   int64_t total = r.qs[0] + r.qs[1] + r.qs[2] + r.qs[3];
   int64_t homoScore = baseSum - (total - baseSum);
   int64_t half = total / 2;
@@ -236,7 +263,7 @@ __device__ inline CallOut base_call(const PosRec& r, const DevParams& P, const C
   bool homo = homoScore >= heteroScore;
   int64_t diff = homoScore - heteroScore;
   if (diff < 0) diff = -diff;
-  o.score = r.mq_sum > 0 ? diff * n / (int64_t)r.mq_sum : 0;
+  o.score = r.mq_sum > 0 ? div_s64(diff * n, (int64_t)r.mq_sum) : 0;
   o.flags = (uint32_t)o0 | ((uint32_t)o1 << 2);
   if (n > 0) o.flags |= PG_CALL_HAS_BASE;
   if (homo) o.flags |= PG_CALL_HOMO;
@@ -294,7 +321,7 @@ __device__ inline CallOut base_call(const PosRec& r, const DevParams& P, const C
 __device__ inline int32_t pool_insertion(const CallCtx& c, const Event& e) {
   unsigned long long off = atomicAdd(c.pool_fill, (unsigned long long)e.len);
   if ((int64_t)(off + e.len) > c.pool_cap) return -2;  // overflow: host grows and reruns
-  for (int32_t j = 0; j < e.len; j++) c.pool[off + j] = (char)nib_char(ins_char(c.R, e, j));
+  for (int32_t j = 0; j < e.len; j++) c.pool[off + j] = (char)nib_char(ins_char(c, e, j));
   return (int32_t)off;
 }
 
@@ -309,6 +336,7 @@ struct WalkArgs {
   DevParams P;
   const uint8_t* ref;
   int32_t tile_width;
+  int32_t packed;        // walk variant: lanes per simple read, 0 = 32, 1 = 16, 2 = 8
 };
 
 struct EventArgs {
@@ -323,7 +351,10 @@ struct EventArgs {
   Event* events;
   unsigned long long* n_events;
   int64_t event_cap;
-  int32_t* bucket_count;  // per call tile
+  ChunkStats* chunk_stats;
+  uint64_t* spool;                 // insertion tails, 16 characters per word
+  unsigned long long* spool_fill;
+  int64_t spool_cap;
 };
 
 struct CallArgs {
@@ -335,9 +366,9 @@ struct CallArgs {
   StatsDev* stats;
   DevParams P;
   const uint8_t* ref;
-  const Event* ev_sorted;
-  const int32_t* bucket_off;  // n_call_tiles + 1
+  const Event* ev_sorted;     // grouped by position (Records::ev_end)
   int64_t event_cap;
+  const uint64_t* spool;
   int32_t* cand_count;        // per call tile
   char* pool;
   unsigned long long* pool_fill;
@@ -350,14 +381,13 @@ void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tile
 void launch_walk(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s);
 void launch_read_events(const EventArgs& a, int32_t chunk_begin, int32_t chunk_count, cudaStream_t s);
 void launch_scan_small(const int32_t* in, int32_t* out_excl, int32_t n, cudaStream_t s);
-void launch_event_scatter(const Event* ev, const unsigned long long* n_events, const RegionDev* regions,
-                          const int32_t* bucket_off, int32_t* bucket_fill, Event* out, cudaStream_t s,
-                          int64_t max_events);
+void launch_event_scatter(const Event* ev, const unsigned long long* n_events, int32_t* ev_end, Event* out,
+                          cudaStream_t s, int64_t max_events);
 void launch_physcov_scan(const RegionDev* regions, const int32_t* call_tile_region, int32_t tile_begin,
                          int32_t n_tiles, Records rec, const StatsDev* stats, int32_t* tile_sums,
                          int32_t region_begin, int32_t n_regions, cudaStream_t s);
-void launch_region_prep(const RegionDev* regions, StatsDev* stats, int32_t n_regions, DevParams P,
-                        cudaStream_t s);
+void launch_region_prep(const RegionDev* regions, StatsDev* stats, const ChunkStats* chunk_stats,
+                        int32_t n_regions, DevParams P, cudaStream_t s);
 void launch_call(const CallArgs& a, int32_t tile_begin, int32_t n_tiles, cudaStream_t s);
 void launch_cand_list(const CallArgs& a, const int32_t* cand_off, Cand* cands, int32_t cand_cap,
                       int32_t tile_begin, int32_t n_tiles, cudaStream_t s);

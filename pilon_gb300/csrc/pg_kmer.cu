@@ -127,9 +127,10 @@ __device__ inline void kmer_call(const uint32_t cnt[4], const unsigned long long
   int o0, o1;
   if ((int32_t)q_sum > 0) order2(v, o0, o1); else order2(c, o0, o1);
   const int64_t total = v[0] + v[1] + v[2] + v[3];
-  const int64_t homoScore = v[o0] - (total - v[o0]);
+  const int64_t b0 = pick4(v, o0), b1 = pick4(v, o1);
+  const int64_t homoScore = b0 - (total - b0);
   const int64_t half = total / 2;
-  const int64_t d1 = half - v[o0], d2 = half - v[o1];
+  const int64_t d1 = half - b0, d2 = half - b1;
   const int64_t hetero = total - (d1 < 0 ? -d1 : d1) - (d2 < 0 ? -d2 : d2);
   base = o0;
   alt = homoScore >= hetero ? -1 : o1;
@@ -165,7 +166,7 @@ __global__ void k_kmer_edges(KmerArgs a) {
       const unsigned long long nibv = 1ull << ((key >> (2 * (K - 1 - j))) & 3ull);
       if (j < 16) hi |= nibv << (60 - 4 * j); else lo |= nibv << (60 - 4 * (j - 16));
     }
-    emit_edge(a, hi, lo, w, b0, alt, depth, (int32_t)cnt[b0]);
+    emit_edge(a, hi, lo, w, b0, alt, depth, (int32_t)(b0 == 0 ? cnt[0] : b0 == 1 ? cnt[1] : b0 == 2 ? cnt[2] : cnt[3]));
   }
 }
 
@@ -230,7 +231,8 @@ __global__ void k_kmer_exotic(KmerArgs a, int32_t n_win) {
     if (depth < a.min_depth) continue;
     int b0, alt;
     kmer_call(cnt, qs, a.x_q[s], b0, alt);
-    emit_edge(a, a.x_keys[2 * s], a.x_keys[2 * s + 1], w, b0, alt, depth, (int32_t)cnt[b0]);
+    emit_edge(a, a.x_keys[2 * s], a.x_keys[2 * s + 1], w, b0, alt, depth,
+              (int32_t)(b0 == 0 ? cnt[0] : b0 == 1 ? cnt[1] : b0 == 2 ? cnt[2] : cnt[3]));
   }
 }
 

@@ -10,7 +10,7 @@
 //                   addInsert), physCovIncr, and the I/D operators with their left
 //                   shift (S/PileUpRegion.scala:150-183), applied with global atomics
 //                   after k_walk and logged as events for the indel vote
-//   k_event_scatter events -> per-call-tile buckets
+//   k_event_scatter events -> grouped by position (offsets from the scan)
 //   k_scan_*        computePhysCov (S/PileUpRegion.scala:90-100) as a segmented scan
 #include <cuda_runtime.h>
 
@@ -124,23 +124,64 @@ void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tile
 }
 
 // ---------------------------------------------------------------------------
-// The walk kernel.  Shared memory holds 12 uint32 counters per tile position:
-//   cnt[4] | qs[4] | mq | q | bad | clips          (each an array of tile_width)
+// The walk kernel.  One CTA owns a tile of T positions (T a template
+// parameter, so every counter address is one register plus an immediate) and
+// keeps its counters in shared memory, field-major so that lanes walking
+// consecutive bases of one read hit different banks:
+//   cnt[4][T] | qs[4][T] | mq[T] | q[T] | bad[T] | clips[T]     (uint32)
 // qs fits uint32 exactly while a pass adds at most kMaxReadsPerPass reads of
-// qual <= 127 and mq <= 255 to one position; tiles with more reads run in
+// qual <= 127 and mq + 1 <= 256 to one position; tiles with more reads run
 // several passes and add each pass's sums into the records.
-__global__ void __launch_bounds__(512) k_walk(WalkArgs a, int32_t tile_begin, int32_t tile_end) {
-  extern __shared__ uint32_t sm[];
-  const int T = a.tile_width;
-  uint32_t* s_cnt = sm;
-  uint32_t* s_qs = sm + 4 * T;
-  uint32_t* s_mq = sm + 8 * T;
-  uint32_t* s_q = sm + 9 * T;
+//
+// Each warp takes the tile's reads 32 at a time.  Every lane first builds the
+// descriptor of one read in registers: the filters of BamFile.process, the
+// clipped-base count and adjusted mapping quality, the CIGAR shape and, for
+// reads whose CIGAR is [S] M|=|X [S] (optional H), everything the walk needs:
+// the trusted offsets clipped to the tile, the pointers to the read's
+// qualities and bases, the nibble parity.  The warp then walks these simple
+// reads G lanes per read (32 / G reads at once), reading the descriptors by
+// warp shuffle; the few other reads take the general CIGAR loop with the
+// whole warp.  No block-wide barrier runs inside the read loop.
+constexpr int kUnroll = 5;
+
+__device__ inline uint32_t nib_at(const uint8_t* seq, int64_t so, int32_t k) {
+  const uint8_t b = seq[so + (k >> 1)];
+  return (k & 1) ? (b & 15u) : (uint32_t)(b >> 4);
+}
+
+template <int T>
+__device__ inline void add_base(uint32_t* sm, int32_t p, uint32_t nib, int32_t qual, uint32_t mq1, int32_t min_qual) {
+  // nibble 1,2,4,8 (A,C,G,T) -> base index; anything else is not counted
+  const uint32_t bi = (0x30210u >> (2 * nib)) & 3u;
+  if (((0x116u >> nib) & 1u) && qual >= min_qual) {
+    uint32_t* c = sm + p + bi * T;
+    atomicAdd(c, 1u);
+    atomicAdd(c + 4 * T, (uint32_t)qual * mq1);
+    atomicAdd(sm + 8 * T + p, mq1);
+    atomicAdd(sm + 9 * T + p, (uint32_t)qual);
+  }
+}
+
+__device__ inline bool nanopore_exclude(const uint8_t* cref, int32_t x, int32_t size) {
+  // nanoporeExclude(index(locus)) indexes the whole contig with a region index
+  return x - 2 >= 0 && x + 2 <= size - 1 && cref[x - 2] == 'C' && cref[x - 1] == 'C' && cref[x + 1] == 'G' &&
+         cref[x + 2] == 'G';
+}
+
+// descriptor kinds
+enum : uint32_t { kSkip = 0, kFast = 1, kInvalid = 2, kSlow = 3, kComplex = 4 };
+
+// MINB: resident CTAs of 512 threads the register allocation must allow
+// (2: up to 64 registers per thread).  G: lanes per simple read (8, 16, 32).
+template <int T, int MINB, int G>
+__global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_begin, int32_t tile_end) {
+  extern __shared__ __align__(16) uint32_t sm[];
+  __shared__ unsigned long long s_bc;
   uint32_t* s_bad = sm + 10 * T;
   uint32_t* s_clip = sm + 11 * T;
-  __shared__ unsigned long long s_bc;
-
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int gl = lane % G, grp = lane / G;
+  constexpr int NG = 32 / G;
   const Reads& R = a.R;
   const DevParams& P = a.P;
 
@@ -157,82 +198,201 @@ __global__ void __launch_bounds__(512) k_walk(WalkArgs a, int32_t tile_begin, in
       for (int k = threadIdx.x; k < 12 * T; k += blockDim.x) sm[k] = 0;
       __syncthreads();
 
-      for (int64_t base = c0 + (int64_t)warp * 32; base < c1; base += (int64_t)nwarps * 32) {
+      for (int64_t base = c0 + 32 * (int64_t)warp; base < c1; base += 32 * (int64_t)nwarps) {
+        // ---- one descriptor per lane
         const int64_t i = base + lane;
-        bool ok = i < c1;
-        int32_t h_pos = 0, h_aend = 0, h_len = 0, h_nc = 0, h_tlen = 0;
-        uint16_t h_flag = 0;
-        uint8_t h_mq = 0;
-        int64_t h_co = 0, h_qo = 0;
-        if (ok) {
-          h_pos = R.pos[i]; h_aend = R.aend[i]; h_flag = R.flag[i];
-          ok = R.ref_id[i] == g.contig && in_window(h_pos, h_aend, h_flag, g) && validate_read(h_flag, P);
-        }
-        if (ok) {
-          h_len = R.l_seq[i]; h_nc = R.n_cigar[i]; h_mq = R.mapq[i]; h_co = R.cigar_off[i]; h_qo = R.qual_off[i];
-          const bool paired = h_flag & 0x1;
-          const bool valid = (h_mq >= P.min_mq) &&
-                             (!paired || ((h_flag & 0x2) && R.ref_id[i] == R.mate_ref_id[i]));
-          h_tlen = valid ? 1 : 0;  // reuse as the `valid` bit
-        }
-        unsigned todo = __ballot_sync(FULL, ok);
-        while (todo) {
-          const int src = __ffs(todo) - 1;
-          todo &= todo - 1;
-          const int64_t ri = base + src;
-          const int32_t pos = __shfl_sync(FULL, h_pos, src);
-          const int32_t length = __shfl_sync(FULL, h_len, src);
-          const int32_t nc = __shfl_sync(FULL, h_nc, src);
-          const int32_t mq = (int32_t)__shfl_sync(FULL, (int32_t)h_mq, src);
-          const bool valid = __shfl_sync(FULL, h_tlen, src) != 0;
-          const int64_t co = __shfl_sync(FULL, h_co, src);
-          const int64_t qo = __shfl_sync(FULL, h_qo, src);
-          const int64_t so = R.seq_off[ri];
-
-          // clipped bases -> adjusted mapping quality (S/PileUpRegion.scala:139-141)
-          int32_t clipped = 0;
-          for (int cb = 0; cb < nc; cb += 32) {
-            uint32_t w = (cb + lane < nc) ? R.cigar[co + cb + lane] : 0u;
-            int32_t sl = ((w & 15u) == 4u) ? (int32_t)(w >> 4) : 0;
-            clipped += __reduce_add_sync(FULL, sl);
+        uint32_t kind = kSkip, mq1 = 0, clip = 0;   // clip: lead | trail << 16
+        int32_t i0 = 0, i1 = 0, pb = 0, mlen = 0, pos = 0, nc = 0, length = 0;
+        bool valid = false, hasQual = false;
+        const uint8_t* qp = nullptr;
+        const uint8_t* sp = nullptr;
+        int64_t co = 0;
+        if (i < c1) {
+          pos = R.pos[i];
+          const uint16_t fl = R.flag[i];
+          if (R.ref_id[i] == g.contig && in_window(pos, R.aend[i], fl, g) && validate_read(fl, P)) {
+            length = R.l_seq[i];
+            const int32_t mq = R.mapq[i];
+            const bool paired = fl & 0x1;
+            valid = (mq >= P.min_mq) && (!paired || ((fl & 0x2) && R.ref_id[i] == R.mate_ref_id[i]));
+            co = R.cigar_off[i];
+            nc = R.n_cigar[i];
+            int32_t clipped = 0, lead = 0, trail = 0, nM = 0;
+            bool simple = true;
+            int32_t lo = pos, hi = pos - 1, ro = 0, fo = 0;
+            for (int k2 = 0; k2 < nc; k2++) {
+              const uint32_t w = R.cigar[co + k2];
+              const int32_t ln = (int32_t)(w >> 4);
+              const int op = (int)(w & 15u);
+              const int32_t locus = pos + fo;
+              if (op == 4) {
+                clipped += ln;
+                const int32_t cs = ro == 0 ? locus - ln : locus;
+                lo = min(lo, cs);
+                hi = max(hi, cs + ln - 1);
+                if (nM == 0) { if (lead) simple = false; lead = ln; }
+                else { if (trail) simple = false; trail = ln; }
+              } else if (op == 0 || op == 7 || op == 8) {
+                if (nM || trail) simple = false;
+                nM++;
+                mlen = ln;
+                lo = min(lo, locus);
+                hi = max(hi, locus + ln - 1);
+              } else if (op != 5) {
+                simple = false;  // I, D, N, P: general path (I and D go to k_read_events)
+              }
+              if (consumes_read(op)) ro += ln;
+              if (consumes_ref(op)) fo += ln;
+            }
+            if (nM == 0 || lead > 0xffff || trail > 0xffff) simple = false;
+            if (hi >= tileLo && lo <= tileHi) {
+              const int64_t qo = R.qual_off[i];
+              const int32_t adjMq = roundDivI(wmul(mq, length - clipped), length);
+              hasQual = length > 0 && R.qual[qo] != 0xFF;
+              mq1 = (uint32_t)(adjMq + 1);
+              const int64_t so = R.seq_off[i];
+              if (simple) {
+                // aligned bases at trusted read offsets [flank, length - flank), inside the tile
+                i0 = max(max(tileLo - pos, P.flank - lead), 0);
+                i1 = min(min(tileHi - pos + 1, length - P.flank - lead), mlen);
+                pb = pos - tileLo;
+                clip = (uint32_t)lead | ((uint32_t)trail << 16);
+                qp = R.qual + qo + lead;
+                sp = R.seq + so;
+                if (!valid) kind = kInvalid;
+                else if (hasQual && P.long_read != PG_NANOPORE) kind = kFast;
+                else kind = kSlow;
+                if (valid && i1 > i0) bc += (unsigned long long)(i1 - i0);
+                // keep the read offset of the first aligned base for the nibble parity
+                mlen |= (lead & 1) << 30;
+              } else {
+                kind = kComplex;
+                qp = R.qual + qo;
+                sp = R.seq + so;
+              }
+            }
           }
-          const int32_t adjMq = roundDivI(wmul(mq, length - clipped), length);
-          const uint32_t mq1 = (uint32_t)(adjMq + 1);
-          const bool hasQual = length > 0 && R.qual[qo] != 0xFF;
-
+        }
+        // ---- simple reads, 32 / G at a time, G lanes each
+        unsigned todo = __ballot_sync(FULL, kind != kSkip && kind != kComplex);
+        while (todo) {
+          // group grp takes the (grp+1)-th lowest set bit of todo
+          unsigned m = todo;
+          for (int k = 0; k < grp; k++) m &= m - 1;
+          const int src = m ? __ffs(m) - 1 : 32;  // 32: fewer reads than groups are left
+          const int s2 = src < 32 ? src : lane;
+          const uint32_t rk = __shfl_sync(FULL, kind, s2);
+          const int32_t ri0 = __shfl_sync(FULL, i0, s2), ri1 = __shfl_sync(FULL, i1, s2);
+          const int32_t rpb = __shfl_sync(FULL, pb, s2), rml = __shfl_sync(FULL, mlen, s2);
+          const uint32_t rmq1 = __shfl_sync(FULL, mq1, s2), rclip = __shfl_sync(FULL, clip, s2);
+          const uint8_t* rqp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)qp, s2);
+          const uint8_t* rsp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)sp, s2);
+          // drop the reads taken by this round
+#pragma unroll
+          for (int k = 0; k < NG; k++)
+            if (todo) todo &= todo - 1;
+          if (src < 32) {
+            const int32_t lead = (int32_t)(rclip & 0xffffu), trail = (int32_t)(rclip >> 16);
+            const int32_t rpos = rpb + tileLo;
+            const int32_t par = (rml >> 30) & 1, rmlen = rml & 0x3fffffff;
+            if (lead > 0) {  // clipStart = locus - len (clip at read offset 0), clipEnd = locus - 1
+              const int32_t cs = rpos - lead, ce = rpos - 1;
+              if (gl == 0) {
+                if (cs >= tileLo && cs <= tileHi) atomicAdd(&s_clip[cs - tileLo], 1u);
+                if (ce >= tileLo && ce <= tileHi) atomicAdd(&s_clip[ce - tileLo], 1u);
+              }
+              for (int32_t l = max(cs, tileLo) + gl; l <= min(ce, tileHi); l += G) atomicAdd(&s_bad[l - tileLo], 1u);
+            }
+            if (rk == kFast) {
+              // per-lane pointers fixed once per read: every unrolled access is pointer + immediate
+              const int32_t x0 = ri0 + gl;
+              const uint8_t* ql = rqp + x0;
+              const uint8_t* sl = rsp + ((lead + x0) >> 1);
+              const uint32_t sh = (~(uint32_t)(par + x0) & 1u) << 2;  // nibble half: read offset lead + x0
+              uint32_t* cl = sm + (rpb + x0);
+              const int32_t nleft = ri1 - x0;
+              for (int32_t b0 = 0; b0 < ri1 - ri0; b0 += G * kUnroll) {
+                uint32_t qv[kUnroll], sv[kUnroll];
+#pragma unroll
+                for (int u = 0; u < kUnroll; u++) {
+                  const bool in = b0 + G * u < nleft;
+                  qv[u] = in ? (uint32_t)ql[b0 + G * u] : 0u;
+                  sv[u] = in ? (uint32_t)sl[(b0 + G * u) >> 1] : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < kUnroll; u++) {
+                  if (b0 + G * u < nleft) {
+                    const uint32_t nib = (sv[u] >> sh) & 15u;
+                    const int32_t qual = (int32_t)(int8_t)qv[u];
+                    const uint32_t bi = (0x30210u >> (2 * nib)) & 3u;
+                    if (((0x116u >> nib) & 1u) && qual >= P.min_qual) {
+                      uint32_t* c = cl + b0 + G * u;
+                      atomicAdd(c + bi * T, 1u);
+                      atomicAdd(c + bi * T + 4 * T, (uint32_t)qual * rmq1);
+                      atomicAdd(c + 8 * T, rmq1);
+                      atomicAdd(c + 9 * T, (uint32_t)qual);
+                    }
+                  }
+                }
+              }
+            } else if (rk == kInvalid) {
+              for (int32_t ii = ri0 + gl; ii < ri1; ii += G) atomicAdd(&s_bad[rpb + ii], 1u);
+            } else {  // kSlow: no qualities (defaultQual) or nanopore motifs
+              const bool rhas = rqp[-lead] != 0xFF;  // qualities present unless the first byte is 0xFF
+              for (int32_t ii = ri0 + gl; ii < ri1; ii += G) {
+                const int32_t rOff = lead + ii;
+                const uint8_t b = rsp[rOff >> 1];
+                const uint32_t nib = (rOff & 1) ? (b & 15u) : (uint32_t)(b >> 4);
+                int32_t qual = rhas ? (int32_t)(int8_t)rqp[ii] : P.default_qual;
+                if (P.long_read == PG_NANOPORE && nanopore_exclude(cref, rpos + ii - g.start, g.size)) qual = 0;
+                add_base<T>(sm, rpb + ii, nib, qual, rmq1, P.min_qual);
+              }
+            }
+            if (trail > 0) {  // clipStart = locus (clip after the aligned bases), clipEnd = locus + len - 1
+              const int32_t cs = rpos + rmlen, ce = cs + trail - 1;
+              if (gl == 0) {
+                if (cs >= tileLo && cs <= tileHi) atomicAdd(&s_clip[cs - tileLo], 1u);
+                if (ce >= tileLo && ce <= tileHi) atomicAdd(&s_clip[ce - tileLo], 1u);
+              }
+              for (int32_t l = max(cs, tileLo) + gl; l <= min(ce, tileHi); l += G) atomicAdd(&s_bad[l - tileLo], 1u);
+            }
+          }
+        }
+        // ---- general CIGAR reads (S/PileUpRegion.scala:145-216), whole warp per read;
+        // I and D are handled by k_read_events
+        unsigned cx = __ballot_sync(FULL, kind == kComplex);
+        while (cx) {
+          const int src = __ffs(cx) - 1;
+          cx &= cx - 1;
+          const int32_t rpos = __shfl_sync(FULL, pos, src);
+          const int32_t rnc = __shfl_sync(FULL, nc, src), rlen = __shfl_sync(FULL, length, src);
+          const uint32_t rmq1 = __shfl_sync(FULL, mq1, src);
+          const bool rvalid = __shfl_sync(FULL, (int)valid, src) != 0;
+          const bool rhas = __shfl_sync(FULL, (int)hasQual, src) != 0;
+          const int64_t rco = __shfl_sync(FULL, co, src);
+          const uint8_t* rqp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)qp, src);
+          const uint8_t* rsp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)sp, src);
           int32_t readOffset = 0, refOffset = 0;
-          for (int cb = 0; cb < nc; cb += 32) {
-            uint32_t wl = (cb + lane < nc) ? R.cigar[co + cb + lane] : 0u;
-            const int kmax = min(32, nc - cb);
-            for (int k = 0; k < kmax; k++) {
-              const uint32_t w = __shfl_sync(FULL, wl, k);
+          for (int cb = 0; cb < rnc; cb += 32) {
+            const uint32_t wl = (cb + lane < rnc) ? R.cigar[rco + cb + lane] : 0u;
+            const int kmax = min(32, rnc - cb);
+            for (int k2 = 0; k2 < kmax; k2++) {
+              const uint32_t w = __shfl_sync(FULL, wl, k2);
               const int32_t len = (int32_t)(w >> 4);
               const int op = (int)(w & 15u);
-              const int32_t locus = pos + refOffset;
+              const int32_t locus = rpos + refOffset;
               if (op == 0 || op == 7 || op == 8) {
-                int32_t i0 = max(max(tileLo - locus, P.flank - readOffset), 0);
-                int32_t i1 = min(min(tileHi - locus + 1, length - P.flank - readOffset), len);
-                for (int32_t ii = i0 + lane; ii < i1; ii += 32) {
+                const int32_t a0 = max(max(tileLo - locus, P.flank - readOffset), 0);
+                const int32_t a1 = min(min(tileHi - locus + 1, rlen - P.flank - readOffset), len);
+                if (rvalid && lane == 0 && a1 > a0) bc += (unsigned long long)(a1 - a0);
+                for (int32_t ii = a0 + lane; ii < a1; ii += 32) {
                   const int32_t rOff = readOffset + ii;
                   const int32_t p = locus + ii - tileLo;
-                  int32_t qual = hasQual ? (int32_t)(int8_t)R.qual[qo + rOff] : P.default_qual;
-                  if (P.long_read == PG_NANOPORE) {  // nanoporeExclude(index(locusPlus)), contig-indexed
-                    const int32_t i0x = locus + ii - g.start;
-                    if (i0x - 2 >= 0 && i0x + 2 <= g.size - 1 && cref[i0x - 2] == 'C' && cref[i0x - 1] == 'C' &&
-                        cref[i0x + 1] == 'G' && cref[i0x + 2] == 'G')
-                      qual = 0;
-                  }
-                  if (valid) {
-                    const uint8_t byte = R.seq[so + (rOff >> 1)];
-                    const uint32_t nib = (rOff & 1) ? (byte & 15u) : (uint32_t)(byte >> 4);
-                    const int bi = nib_index(nib);
-                    if (bi >= 0 && qual >= P.min_qual) {
-                      atomicAdd(&s_cnt[bi * T + p], 1u);
-                      atomicAdd(&s_qs[bi * T + p], (uint32_t)qual * mq1);
-                      atomicAdd(&s_mq[p], mq1);
-                      atomicAdd(&s_q[p], (uint32_t)qual);
-                    }
-                    bc++;
+                  if (rvalid) {
+                    int32_t qual = rhas ? (int32_t)(int8_t)rqp[rOff] : P.default_qual;
+                    if (P.long_read == PG_NANOPORE && nanopore_exclude(cref, locus + ii - g.start, g.size)) qual = 0;
+                    const uint8_t b = rsp[rOff >> 1];
+                    add_base<T>(sm, p, (rOff & 1) ? (b & 15u) : (uint32_t)(b >> 4), qual, rmq1, P.min_qual);
                   } else {
                     atomicAdd(&s_bad[p], 1u);
                   }
@@ -244,12 +404,12 @@ __global__ void __launch_bounds__(512) k_walk(WalkArgs a, int32_t tile_begin, in
                   if (clipStart >= tileLo && clipStart <= tileHi) atomicAdd(&s_clip[clipStart - tileLo], 1u);
                   if (clipEnd >= tileLo && clipEnd <= tileHi) atomicAdd(&s_clip[clipEnd - tileLo], 1u);
                 }
-                int32_t i0 = max(tileLo - clipStart, 0);
-                int32_t i1 = min(tileHi - clipStart + 1, len);
-                for (int32_t ii = i0 + lane; ii < i1; ii += 32) atomicAdd(&s_bad[clipStart + ii - tileLo], 1u);
+                const int32_t a0 = max(tileLo - clipStart, 0);
+                const int32_t a1 = min(tileHi - clipStart + 1, len);
+                for (int32_t ii = a0 + lane; ii < a1; ii += 32) atomicAdd(&s_bad[clipStart + ii - tileLo], 1u);
               }
-              if (op == 0 || op == 1 || op == 4 || op == 7 || op == 8) readOffset += len;
-              if (op == 0 || op == 2 || op == 3 || op == 7 || op == 8) refOffset += len;
+              if (consumes_read(op)) readOffset += len;
+              if (consumes_ref(op)) refOffset += len;
             }
           }
         }
@@ -259,15 +419,16 @@ __global__ void __launch_bounds__(512) k_walk(WalkArgs a, int32_t tile_begin, in
       // flush: the first pass stores, later passes add (the CTA owns the tile)
       for (int32_t p = threadIdx.x; p < tile.len; p += blockDim.x) {
         const int64_t gp = g.pos_base + tile.lo + p;
-        int4 c = make_int4((int)s_cnt[p], (int)s_cnt[T + p], (int)s_cnt[2 * T + p], (int)s_cnt[3 * T + p]);
-        longlong2 q01 = make_longlong2((long long)s_qs[p], (long long)s_qs[T + p]);
-        longlong2 q23 = make_longlong2((long long)s_qs[2 * T + p], (long long)s_qs[3 * T + p]);
+        const int4 c = make_int4((int)sm[p], (int)sm[T + p], (int)sm[2 * T + p], (int)sm[3 * T + p]);
+        const longlong2 q01 = make_longlong2((long long)sm[4 * T + p], (long long)sm[5 * T + p]);
+        const longlong2 q23 = make_longlong2((long long)sm[6 * T + p], (long long)sm[7 * T + p]);
+        const int32_t mqs = (int32_t)sm[8 * T + p], qsum = (int32_t)sm[9 * T + p];
         if (pass == 0) {
           a.rec.count[gp] = c;
           a.rec.qual_sum[2 * gp] = q01;
           a.rec.qual_sum[2 * gp + 1] = q23;
-          a.rec.mq_sum[gp] = (int32_t)s_mq[p];
-          a.rec.q_sum[gp] = (int32_t)s_q[p];
+          a.rec.mq_sum[gp] = mqs;
+          a.rec.q_sum[gp] = qsum;
           a.rec.bad_pair[gp] = (int32_t)s_bad[p];
           a.rec.clips[gp] = (int32_t)s_clip[p];
           a.rec.deletions[gp] = 0;
@@ -277,13 +438,13 @@ __global__ void __launch_bounds__(512) k_walk(WalkArgs a, int32_t tile_begin, in
           a.rec.phys_cov[gp] = 0;
           a.rec.insert_size[gp] = 0;
         } else {
-          int4 o = a.rec.count[gp];
+          const int4 o = a.rec.count[gp];
           a.rec.count[gp] = make_int4(o.x + c.x, o.y + c.y, o.z + c.z, o.w + c.w);
-          longlong2 o1 = a.rec.qual_sum[2 * gp], o2 = a.rec.qual_sum[2 * gp + 1];
+          const longlong2 o1 = a.rec.qual_sum[2 * gp], o2 = a.rec.qual_sum[2 * gp + 1];
           a.rec.qual_sum[2 * gp] = make_longlong2(o1.x + q01.x, o1.y + q01.y);
           a.rec.qual_sum[2 * gp + 1] = make_longlong2(o2.x + q23.x, o2.y + q23.y);
-          a.rec.mq_sum[gp] = wadd(a.rec.mq_sum[gp], (int32_t)s_mq[p]);
-          a.rec.q_sum[gp] = wadd(a.rec.q_sum[gp], (int32_t)s_q[p]);
+          a.rec.mq_sum[gp] = wadd(a.rec.mq_sum[gp], mqs);
+          a.rec.q_sum[gp] = wadd(a.rec.q_sum[gp], qsum);
           a.rec.bad_pair[gp] = wadd(a.rec.bad_pair[gp], (int32_t)s_bad[p]);
           a.rec.clips[gp] = wadd(a.rec.clips[gp], (int32_t)s_clip[p]);
         }
@@ -299,23 +460,50 @@ __global__ void __launch_bounds__(512) k_walk(WalkArgs a, int32_t tile_begin, in
   }
 }
 
+template <int T, int MINB, int G>
+static void launch_walk_t(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s) {
+  const size_t smem = (size_t)12 * T * sizeof(uint32_t);
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_walk<T, MINB, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = true;
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<T, MINB, G>, warps * 32, smem);
+  per_sm = std::max(per_sm, 1);
+  const int blocks = std::min(tile_count, 152 * per_sm);
+  k_walk<T, MINB, G><<<blocks, warps * 32, smem, s>>>(a, tile_begin, tile_begin + tile_count);
+}
+
+template <int MINB, int G>
+static void launch_walk_v(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s) {
+  switch (a.tile_width) {
+    case 256: launch_walk_t<256, MINB, G>(a, tile_begin, tile_count, warps, s); break;
+    case 512: launch_walk_t<512, MINB, G>(a, tile_begin, tile_count, warps, s); break;
+    case 1024: launch_walk_t<1024, MINB, G>(a, tile_begin, tile_count, warps, s); break;
+    case 2048: launch_walk_t<2048, MINB, G>(a, tile_begin, tile_count, warps, s); break;
+    default: launch_walk_t<4096, MINB, G>(a, tile_begin, tile_count, warps, s); break;
+  }
+}
+
+// variant: lanes per simple read (0: 32, 1: 16, 2: 8).
 void launch_walk(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s) {
   if (tile_count <= 0) return;
-  size_t smem = (size_t)12 * a.tile_width * sizeof(uint32_t);
-  static size_t configured = 0;
-  if (smem > configured) {
-    cudaFuncSetAttribute(k_walk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = smem;
-  }
-  int per_sm = max(1, (int)((227 * 1024) / (smem + 1024)));
-  int blocks = min(tile_count, 152 * per_sm);
-  k_walk<<<blocks, warps * 32, smem, s>>>(a, tile_begin, tile_begin + tile_count);
+  const int lanes = a.packed;
+  if (lanes == 0) launch_walk_v<2, 32>(a, tile_begin, tile_count, warps, s);
+  else if (lanes == 1) launch_walk_v<2, 16>(a, tile_begin, tile_count, warps, s);
+  else launch_walk_v<2, 8>(a, tile_begin, tile_count, warps, s);
 }
 
 // ---------------------------------------------------------------------------
 // Per (region, read): readCount, insert statistics, physCovIncr and indels.
 __device__ inline int32_t read_qual(const Reads& R, int64_t i, int32_t k, bool hasQual, const DevParams& P) {
   return hasQual ? (int32_t)(int8_t)R.qual[R.qual_off[i] + k] : P.default_qual;
+}
+
+__device__ inline unsigned long long warp_sum_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+  return v;
 }
 
 __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_begin, int32_t chunk_end) {
@@ -332,12 +520,16 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
       s_pcs = s_iss = s_err = 0;
     }
     __syncthreads();
+    // per-thread partial sums, reduced once per chunk
+    unsigned long long rc_n = 0, bc_n = 0, frc = 0, frs = 0, frq = 0, rfc = 0, rfs = 0, rfq = 0;
+    uint32_t pcs = 0, iss = 0;
+    int32_t err = 0;
     auto inRegion = [&](int64_t l) { return l >= g.start && l <= g.stop; };
     for (int64_t i = C.lo + threadIdx.x; i < C.hi; i += blockDim.x) {
       const int32_t pos = R.pos[i], aend = R.aend[i];
       const uint16_t fl = R.flag[i];
       if (R.ref_id[i] != g.contig || !in_window(pos, aend, fl, g) || !validate_read(fl, P)) continue;
-      atomicAdd(&s_rc, 1ull);
+      rc_n++;
       const int32_t length = R.l_seq[i];
       const int32_t mq = R.mapq[i];
       const bool paired = fl & 0x1;
@@ -357,8 +549,8 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
           atomicAdd(&a.rec.phys_cov[gp], 1);
           atomicAdd(&a.rec.insert_size[gp], insertSize);
         } else if (s < g.start && !(e < g.start)) {
-          atomicAdd(&s_pcs, 1);
-          atomicAdd(&s_iss, insertSize);
+          pcs += 1u;
+          iss += (uint32_t)insertSize;
         }
         if (inRegion(e)) {
           int64_t gp = g.pos_base + (e - g.start);
@@ -370,8 +562,8 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
         const bool rc = fl & 0x10;
         const bool fr = (insertSize > 0) ^ rc;
         const unsigned long long sq = (unsigned long long)(long long)wmul(insertSize, insertSize);
-        if (fr) { atomicAdd(&s_frc, 1ull); atomicAdd(&s_frs, (unsigned long long)insertSize); atomicAdd(&s_frq, sq); }
-        else { atomicAdd(&s_rfc, 1ull); atomicAdd(&s_rfs, (unsigned long long)insertSize); atomicAdd(&s_rfq, sq); }
+        if (fr) { frc++; frs += (unsigned long long)insertSize; frq += sq; }
+        else { rfc++; rfs += (unsigned long long)insertSize; rfq += sq; }
       }
 
       // I and D operators (S/PileUpRegion.scala:150-183)
@@ -426,7 +618,7 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
           if (!bad && P.long_read > 0) {
             if (homoRun(iloc, bad) >= 4 && !bad) goto next_op;
           }
-          if (bad || iloc < g.start) { atomicExch(&s_err, (int)PG_ERR_INDEX); goto next_op; }
+          if (bad || iloc < g.start) { err = PG_ERR_INDEX; goto next_op; }
           {
             const int64_t gp = g.pos_base + (iloc - g.start);
             atomicAdd(&a.rec.ins_qual[gp], indelMq + 1);
@@ -436,9 +628,36 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
             if ((int64_t)slot < a.event_cap) {
               Event e;
               e.gpos = gp; e.read = i; e.region = C.region; e.len = len; e.roff = readOffset; e.kind_rot = rot;
+              // the rotated string as 4-bit codes: characters 0..15 in the key,
+              // the rest 16 per word in the string pool
+              uint64_t key = 0;
+              for (int32_t j = 0; j < min(len, 16); j++) {
+                int32_t kk = j - rot;
+                if (kk < 0) kk += len;
+                key |= (uint64_t)read_nib(R, i, readOffset + kk) << (60 - 4 * j);
+              }
+              e.key = key;
+              e.sp = -1;
+              if (len > 16) {
+                const int32_t nw = (len - 16 + 15) / 16;
+                const unsigned long long sp = atomicAdd(a.spool_fill, (unsigned long long)nw);
+                if ((int64_t)(sp + nw) <= a.spool_cap) {
+                  for (int32_t w = 0; w < nw; w++) {
+                    uint64_t word = 0;
+                    for (int32_t j = 16 + 16 * w; j < min(len, 32 + 16 * w); j++) {
+                      int32_t kk = j - rot;
+                      if (kk < 0) kk += len;
+                      word |= (uint64_t)read_nib(R, i, readOffset + kk) << (60 - 4 * (j - 16 - 16 * w));
+                    }
+                    a.spool[sp + w] = word;
+                  }
+                  e.sp = (int64_t)sp;
+                } else {
+                  e.len = -1;  // pool full: the host grows it and runs again
+                }
+              }
               a.events[slot] = e;
             }
-            atomicAdd(&a.bucket_count[g.call_tile0 + (iloc - g.start) / kCallTile], 1);
           }
         } else if (op == 2 && trusted(readOffset) && inRegion(locus) && inRegion((int64_t)locus + len - 1)) {
           int32_t dloc = locus, rloc = readOffset;
@@ -460,11 +679,11 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
                   atomicAdd(&a.rec.mq_sum[gp], adjMq + 1);
                   atomicAdd(&a.rec.q_sum[gp], q);
                 }
-                atomicAdd(&s_bc, 1ull);
+                bc_n++;
               }
             }
           }
-          if (bad) { atomicExch(&s_err, (int)PG_ERR_INDEX); goto next_op; }
+          if (bad) { err = PG_ERR_INDEX; goto next_op; }
           if (P.long_read > 0) {
             const int64_t i0 = (int64_t)dloc - g.start;  // index(dloc), used as a contig index
             if (homoRun(i0, bad) >= 4 && !bad) goto next_op;
@@ -474,7 +693,7 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
               if (ex) goto next_op;
             }
           }
-          if (bad || dloc < g.start) { atomicExch(&s_err, (int)PG_ERR_INDEX); goto next_op; }
+          if (bad || dloc < g.start) { err = PG_ERR_INDEX; goto next_op; }
           {
             const int64_t gp = g.pos_base + (dloc - g.start);
             atomicAdd(&a.rec.mq_sum[gp], indelMq + 1);
@@ -486,9 +705,10 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
               Event e;
               e.gpos = gp; e.read = i; e.region = C.region; e.len = len; e.roff = rloc;
               e.kind_rot = (int32_t)0x80000000;
+              e.key = 0;
+              e.sp = -1;
               a.events[slot] = e;
             }
-            atomicAdd(&a.bucket_count[g.call_tile0 + (dloc - g.start) / kCallTile], 1);
           }
         }
       next_op:
@@ -496,16 +716,28 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
         if (op == 0 || op == 2 || op == 3 || op == 7 || op == 8) refOffset += len;
       }
     }
+    rc_n = warp_sum_u64(rc_n); bc_n = warp_sum_u64(bc_n);
+    frc = warp_sum_u64(frc); frs = warp_sum_u64(frs); frq = warp_sum_u64(frq);
+    rfc = warp_sum_u64(rfc); rfs = warp_sum_u64(rfs); rfq = warp_sum_u64(rfq);
+    pcs = __reduce_add_sync(FULL, pcs); iss = __reduce_add_sync(FULL, iss);
+    err = __reduce_max_sync(FULL, err);
+    if ((threadIdx.x & 31) == 0) {
+      if (rc_n) atomicAdd(&s_rc, rc_n);
+      if (bc_n) atomicAdd(&s_bc, bc_n);
+      if (frc) { atomicAdd(&s_frc, frc); atomicAdd(&s_frs, frs); atomicAdd(&s_frq, frq); }
+      if (rfc) { atomicAdd(&s_rfc, rfc); atomicAdd(&s_rfs, rfs); atomicAdd(&s_rfq, rfq); }
+      if (pcs) atomicAdd(&s_pcs, (int32_t)pcs);
+      if (iss) atomicAdd(&s_iss, (int32_t)iss);
+      if (err) atomicExch(&s_err, err);
+    }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      StatsDev* st = &a.stats[C.region];
-      if (s_rc) atomicAdd(&st->read_count, s_rc);
-      if (s_bc) atomicAdd(&st->base_count, s_bc);
-      if (s_pcs) atomicAdd(&st->phys_cov_start, s_pcs);
-      if (s_iss) atomicAdd(&st->insert_size_start, s_iss);
-      if (s_frc) { atomicAdd(&st->fr_count, s_frc); atomicAdd(&st->fr_sum, s_frs); atomicAdd(&st->fr_sumsq, s_frq); }
-      if (s_rfc) { atomicAdd(&st->rf_count, s_rfc); atomicAdd(&st->rf_sum, s_rfs); atomicAdd(&st->rf_sumsq, s_rfq); }
-      if (s_err) atomicExch(&st->error, s_err);
+    if (threadIdx.x == 0) {  // partial sums of this chunk; k_region_prep adds them up per region
+      ChunkStats cs;
+      cs.read_count = s_rc; cs.base_count = s_bc;
+      cs.fr_count = s_frc; cs.fr_sum = s_frs; cs.fr_sumsq = s_frq;
+      cs.rf_count = s_rfc; cs.rf_sum = s_rfs; cs.rf_sumsq = s_rfq;
+      cs.phys_cov_start = s_pcs; cs.insert_size_start = s_iss; cs.error = s_err; cs.pad = 0;
+      a.chunk_stats[ch] = cs;
     }
     __syncthreads();
   }
@@ -513,7 +745,7 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
 
 void launch_read_events(const EventArgs& a, int32_t chunk_begin, int32_t chunk_count, cudaStream_t s) {
   if (chunk_count <= 0) return;
-  int blocks = min(chunk_count, 152 * 8);
+  int blocks = chunk_count;
   k_read_events<<<blocks, 256, 0, s>>>(a, chunk_begin, chunk_begin + chunk_count);
 }
 
@@ -558,112 +790,174 @@ void launch_scan_small(const int32_t* in, int32_t* out_excl, int32_t n, cudaStre
 }
 
 // ---------------------------------------------------------------------------
-__global__ void k_event_scatter(const Event* ev, const unsigned long long* n_events, const RegionDev* regions,
-                                const int32_t* bucket_off, int32_t* bucket_fill, Event* out, int64_t max_events) {
+// Events -> contiguous per position: the scan left each position's first slot
+// in ev_end; every event takes the next slot, so afterwards ev_end is the end.
+__global__ void k_event_scatter(const Event* ev, const unsigned long long* n_events, int32_t* ev_end, Event* out,
+                                int64_t max_events) {
   int64_t n = min((int64_t)*n_events, max_events);
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    Event e = ev[k];
-    const RegionDev& g = regions[e.region];
-    int32_t tile = g.call_tile0 + (int32_t)((e.gpos - g.pos_base) / kCallTile);
-    int32_t slot = bucket_off[tile] + atomicAdd(&bucket_fill[tile], 1);
-    if (slot < max_events) out[slot] = e;
+    const Event e = ev[k];
+    const int32_t slot = atomicAdd(&ev_end[e.gpos], 1);
+    if (slot >= 0 && slot < max_events) out[slot] = e;
   }
 }
 
-void launch_event_scatter(const Event* ev, const unsigned long long* n_events, const RegionDev* regions,
-                          const int32_t* bucket_off, int32_t* bucket_fill, Event* out, cudaStream_t s,
-                          int64_t max_events) {
+void launch_event_scatter(const Event* ev, const unsigned long long* n_events, int32_t* ev_end, Event* out,
+                          cudaStream_t s, int64_t max_events) {
   if (max_events <= 0) return;
   int blocks = (int)std::min<int64_t>((max_events + 255) / 256, 152 * 8);
-  k_event_scatter<<<blocks, 256, 0, s>>>(ev, n_events, regions, bucket_off, bucket_fill, out, max_events);
+  k_event_scatter<<<blocks, 256, 0, s>>>(ev, n_events, ev_end, out, max_events);
 }
 
 // ---------------------------------------------------------------------------
-// computePhysCov as a segmented scan over call tiles (kCallTile positions).
-// Phase A: tile sums.  Phase B: per-region exclusive scan of tile sums with the
-// region's start carry.  Phase C: in-tile scan, then insertSize /= physCov.
-__device__ inline void block_scan_pair(uint32_t& a, uint32_t& b, uint32_t* s_a, uint32_t* s_b) {
+// computePhysCov as a segmented scan over call tiles (kCallTile positions),
+// fused with the exclusive scan of per-position event counts (insertions +
+// deletions) that groups indel events by position.
+// Phase A: tile sums.  Phase B: one CTA scans all tile sums, segmented by
+// region for coverage (seeded with each region's start carry) and global for
+// events.  Phase C: in-tile scan, insertSize /= physCov, event offsets.
+__device__ inline void block_scan3(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t* s_a, uint32_t* s_b,
+                                   uint32_t* s_c) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t ya = __shfl_up_sync(FULL, a, o), yb = __shfl_up_sync(FULL, b, o);
-    if (lane >= o) { a += ya; b += yb; }
+    uint32_t ya = __shfl_up_sync(FULL, a, o), yb = __shfl_up_sync(FULL, b, o), yc = __shfl_up_sync(FULL, c, o);
+    if (lane >= o) { a += ya; b += yb; c += yc; }
   }
-  if (lane == 31) { s_a[warp] = a; s_b[warp] = b; }
+  if (lane == 31) { s_a[warp] = a; s_b[warp] = b; s_c[warp] = c; }
   __syncthreads();
   if (warp == 0) {
     const int nw = blockDim.x >> 5;
-    uint32_t wa = lane < nw ? s_a[lane] : 0u, wb = lane < nw ? s_b[lane] : 0u;
+    uint32_t wa = lane < nw ? s_a[lane] : 0u, wb = lane < nw ? s_b[lane] : 0u, wc = lane < nw ? s_c[lane] : 0u;
     for (int o = 1; o < 32; o <<= 1) {
-      uint32_t ya = __shfl_up_sync(FULL, wa, o), yb = __shfl_up_sync(FULL, wb, o);
-      if (lane >= o) { wa += ya; wb += yb; }
+      uint32_t ya = __shfl_up_sync(FULL, wa, o), yb = __shfl_up_sync(FULL, wb, o), yc = __shfl_up_sync(FULL, wc, o);
+      if (lane >= o) { wa += ya; wb += yb; wc += yc; }
     }
-    s_a[lane] = wa; s_b[lane] = wb;
+    s_a[lane] = wa; s_b[lane] = wb; s_c[lane] = wc;
   }
   __syncthreads();
-  if (warp > 0) { a += s_a[warp - 1]; b += s_b[warp - 1]; }
+  if (warp > 0) { a += s_a[warp - 1]; b += s_b[warp - 1]; c += s_c[warp - 1]; }
+  __syncthreads();
 }
 
 __global__ void __launch_bounds__(kCallTile) k_scan_tiles_a(const RegionDev* regions, const int32_t* tile_region,
                                                              Records rec, int32_t* tile_sums, int32_t tile_begin) {
-  __shared__ uint32_t s_a[32], s_b[32];
+  __shared__ uint32_t s_a[32], s_b[32], s_c[32];
   const int32_t t = tile_begin + blockIdx.x;
   const RegionDev& g = regions[tile_region[t]];
-  const int32_t lo = (t - g.call_tile0) * kCallTile;
-  const int32_t p = lo + threadIdx.x;
-  uint32_t a = 0, b = 0;
+  const int32_t p = (t - g.call_tile0) * kCallTile + threadIdx.x;
+  uint32_t a = 0, b = 0, c = 0;
   if (p < g.size) {
-    a = (uint32_t)rec.phys_cov[g.pos_base + p];
-    b = (uint32_t)rec.insert_size[g.pos_base + p];
+    const int64_t gp = g.pos_base + p;
+    a = (uint32_t)rec.phys_cov[gp];
+    b = (uint32_t)rec.insert_size[gp];
+    c = (uint32_t)rec.insertions[gp] + (uint32_t)rec.deletions[gp];
   }
-  block_scan_pair(a, b, s_a, s_b);
-  if (threadIdx.x == blockDim.x - 1) { tile_sums[2 * t] = (int32_t)a; tile_sums[2 * t + 1] = (int32_t)b; }
+  block_scan3(a, b, c, s_a, s_b, s_c);
+  if (threadIdx.x == blockDim.x - 1) {
+    tile_sums[3 * t] = (int32_t)a; tile_sums[3 * t + 1] = (int32_t)b; tile_sums[3 * t + 2] = (int32_t)c;
+  }
 }
 
-__global__ void k_scan_tiles_b(const RegionDev* regions, int32_t n_regions, const StatsDev* stats,
-                               int32_t* tile_sums) {
-  int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_regions) return;
-  const RegionDev& g = regions[r];
-  uint32_t ca = (uint32_t)stats[r].phys_cov_start, cb = (uint32_t)stats[r].insert_size_start;
-  for (int32_t t = g.call_tile0; t < g.call_tile0 + g.n_call_tiles; t++) {
-    uint32_t a = (uint32_t)tile_sums[2 * t], b = (uint32_t)tile_sums[2 * t + 1];
-    tile_sums[2 * t] = (int32_t)ca;
-    tile_sums[2 * t + 1] = (int32_t)cb;
-    ca += a;
-    cb += b;
+// One CTA over the tiles [t0, t0 + tn).  Coverage sums restart at each
+// region's first tile, seeded with physCovStart / insertSizeStart.
+__global__ void __launch_bounds__(1024) k_scan_tiles_b(const RegionDev* regions, const int32_t* tile_region,
+                                                        const StatsDev* stats, int32_t* ts, int32_t t0, int32_t tn) {
+  __shared__ uint32_t s_a[32], s_b[32], s_c[32];
+  __shared__ uint32_t s_f[32];
+  __shared__ uint32_t s_ca, s_cb, s_cc;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) { s_ca = 0; s_cb = 0; s_cc = 0; }
+  __syncthreads();
+  for (int32_t base = 0; base < tn; base += blockDim.x) {
+    const int32_t i = base + threadIdx.x;
+    const int32_t t = t0 + i;
+    uint32_t va = 0, vb = 0, vc = 0, f = 0;
+    uint32_t a = 0, b = 0;
+    if (i < tn) {
+      const int32_t r = tile_region[t];
+      va = (uint32_t)ts[3 * t]; vb = (uint32_t)ts[3 * t + 1]; vc = (uint32_t)ts[3 * t + 2];
+      f = t == regions[r].call_tile0;
+      a = va + (f ? (uint32_t)stats[r].phys_cov_start : 0u);
+      b = vb + (f ? (uint32_t)stats[r].insert_size_start : 0u);
+    }
+    uint32_t c = vc;
+    // segmented inclusive scan of (a, b) with head flags f; plain scan of c
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t ya = __shfl_up_sync(FULL, a, o), yb = __shfl_up_sync(FULL, b, o), yc = __shfl_up_sync(FULL, c, o);
+      uint32_t yf = __shfl_up_sync(FULL, f, o);
+      if (lane >= o) {
+        if (!f) { a += ya; b += yb; }
+        f |= yf;
+        c += yc;
+      }
+    }
+    if (lane == 31) { s_a[warp] = a; s_b[warp] = b; s_c[warp] = c; s_f[warp] = f; }
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t wa = s_a[lane], wb = s_b[lane], wc = s_c[lane], wf = s_f[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t ya = __shfl_up_sync(FULL, wa, o), yb = __shfl_up_sync(FULL, wb, o);
+        uint32_t yc = __shfl_up_sync(FULL, wc, o), yf = __shfl_up_sync(FULL, wf, o);
+        if (lane >= o) {
+          if (!wf) { wa += ya; wb += yb; }
+          wf |= yf;
+          wc += yc;
+        }
+      }
+      s_a[lane] = wa; s_b[lane] = wb; s_c[lane] = wc; s_f[lane] = wf;
+    }
+    __syncthreads();
+    if (warp > 0) {  // combine with the inclusive result of the previous warps
+      if (!f) { a += s_a[warp - 1]; b += s_b[warp - 1]; }
+      f |= s_f[warp - 1];
+      c += s_c[warp - 1];
+    }
+    if (!f) { a += s_ca; b += s_cb; }  // carry of the previous chunk
+    c += s_cc;
+    if (i < tn) {
+      ts[3 * t] = (int32_t)(a - va);
+      ts[3 * t + 1] = (int32_t)(b - vb);
+      ts[3 * t + 2] = (int32_t)(c - vc);
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) { s_ca = a; s_cb = b; s_cc = c; }
+    __syncthreads();
   }
 }
 
 __global__ void __launch_bounds__(kCallTile) k_scan_tiles_c(const RegionDev* regions, const int32_t* tile_region,
                                                              Records rec, const int32_t* tile_sums,
                                                              int32_t tile_begin) {
-  __shared__ uint32_t s_a[32], s_b[32];
+  __shared__ uint32_t s_a[32], s_b[32], s_c[32];
   const int32_t t = tile_begin + blockIdx.x;
   const RegionDev& g = regions[tile_region[t]];
-  const int32_t lo = (t - g.call_tile0) * kCallTile;
-  const int32_t p = lo + threadIdx.x;
-  uint32_t a = 0, b = 0;
+  const int32_t p = (t - g.call_tile0) * kCallTile + threadIdx.x;
+  uint32_t a = 0, b = 0, c = 0, vc = 0;
+  const int64_t gp = g.pos_base + p;
   if (p < g.size) {
-    a = (uint32_t)rec.phys_cov[g.pos_base + p];
-    b = (uint32_t)rec.insert_size[g.pos_base + p];
+    a = (uint32_t)rec.phys_cov[gp];
+    b = (uint32_t)rec.insert_size[gp];
+    vc = c = (uint32_t)rec.insertions[gp] + (uint32_t)rec.deletions[gp];
   }
-  block_scan_pair(a, b, s_a, s_b);
+  block_scan3(a, b, c, s_a, s_b, s_c);
   if (p < g.size) {
-    int32_t pc = (int32_t)(a + (uint32_t)tile_sums[2 * t]);
-    int32_t is = (int32_t)(b + (uint32_t)tile_sums[2 * t + 1]);
+    int32_t pc = (int32_t)(a + (uint32_t)tile_sums[3 * t]);
+    int32_t is = (int32_t)(b + (uint32_t)tile_sums[3 * t + 1]);
     if (pc > 0) is = is / pc;
-    rec.phys_cov[g.pos_base + p] = pc;
-    rec.insert_size[g.pos_base + p] = is;
+    rec.phys_cov[gp] = pc;
+    rec.insert_size[gp] = is;
+    if (vc) rec.ev_end[gp] = (int32_t)(c - vc + (uint32_t)tile_sums[3 * t + 2]);  // first slot
   }
 }
 
 void launch_physcov_scan(const RegionDev* regions, const int32_t* call_tile_region, int32_t tile_begin,
                          int32_t n_tiles, Records rec, const StatsDev* stats, int32_t* tile_sums,
                          int32_t region_begin, int32_t n_regions, cudaStream_t s) {
+  (void)region_begin;
+  (void)n_regions;
   if (n_tiles <= 0) return;
   k_scan_tiles_a<<<n_tiles, kCallTile, 0, s>>>(regions, call_tile_region, rec, tile_sums, tile_begin);
-  k_scan_tiles_b<<<(n_regions + 127) / 128, 128, 0, s>>>(regions + region_begin, n_regions, stats + region_begin,
-                                                           tile_sums);
+  k_scan_tiles_b<<<1, 1024, 0, s>>>(regions, call_tile_region, stats, tile_sums, tile_begin, n_tiles);
   k_scan_tiles_c<<<n_tiles, kCallTile, 0, s>>>(regions, call_tile_region, rec, tile_sums, tile_begin);
 }
 
@@ -674,19 +968,64 @@ __device__ inline int64_t java_round(double x) {
   return (int64_t)((x - f >= 0.5) ? f + 1.0 : f);
 }
 
-__global__ void k_region_prep(const RegionDev* regions, StatsDev* stats, int32_t n_regions, DevParams P) {
-  int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_regions) return;
-  int64_t meanCoverage = roundDivL((int64_t)stats[r].base_count, regions[r].size);
-  int32_t md;
-  if (P.min_depth >= 1) md = (int32_t)P.min_depth;
-  else md = max((int32_t)java_round(P.min_depth * (double)meanCoverage), P.min_min_depth);
-  stats[r].min_depth = md;
+// One CTA per region: adds up the per-chunk partial statistics, then
+// computes minDepth.
+__global__ void __launch_bounds__(256) k_region_prep(const RegionDev* regions, StatsDev* stats,
+                                                      const ChunkStats* cs, DevParams P) {
+  __shared__ unsigned long long s_u[8];
+  __shared__ int32_t s_i[3];
+  const int32_t r = blockIdx.x;
+  const RegionDev& g = regions[r];
+  unsigned long long u[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  uint32_t pcs = 0, iss = 0;
+  int32_t err = 0;
+  for (int32_t k = g.chunk0 + threadIdx.x; k < g.chunk0 + g.n_chunks; k += blockDim.x) {
+    const ChunkStats c = cs[k];
+    u[0] += c.read_count; u[1] += c.base_count; u[2] += c.fr_count; u[3] += c.fr_sum;
+    u[4] += c.fr_sumsq; u[5] += c.rf_count; u[6] += c.rf_sum; u[7] += c.rf_sumsq;
+    pcs += (uint32_t)c.phys_cov_start;
+    iss += (uint32_t)c.insert_size_start;
+    err = max(err, c.error);
+  }
+  if (threadIdx.x < 8) s_u[threadIdx.x] = 0;
+  if (threadIdx.x < 3) s_i[threadIdx.x] = 0;
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const unsigned long long v = warp_sum_u64(u[k]);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(&s_u[k], v);
+  }
+  pcs = __reduce_add_sync(FULL, pcs);
+  iss = __reduce_add_sync(FULL, iss);
+  err = __reduce_max_sync(FULL, err);
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s_i[0], (int32_t)pcs);
+    atomicAdd(&s_i[1], (int32_t)iss);
+    atomicMax(&s_i[2], err);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    StatsDev& st = stats[r];
+    st.read_count = s_u[0];
+    st.base_count += s_u[1];  // the walk kernel added the aligned bases already
+    st.fr_count = s_u[2]; st.fr_sum = s_u[3]; st.fr_sumsq = s_u[4];
+    st.rf_count = s_u[5]; st.rf_sum = s_u[6]; st.rf_sumsq = s_u[7];
+    st.phys_cov_start = s_i[0];
+    st.insert_size_start = s_i[1];
+    st.error = s_i[2];
+    // minDepth of GenomeRegion.postProcess (S/GenomeRegion.scala:216-224)
+    const int64_t meanCoverage = roundDivL((int64_t)st.base_count, g.size);
+    int32_t md;
+    if (P.min_depth >= 1) md = (int32_t)P.min_depth;
+    else md = max((int32_t)java_round(P.min_depth * (double)meanCoverage), P.min_min_depth);
+    st.min_depth = md;
+  }
 }
 
-void launch_region_prep(const RegionDev* regions, StatsDev* stats, int32_t n_regions, DevParams P, cudaStream_t s) {
+void launch_region_prep(const RegionDev* regions, StatsDev* stats, const ChunkStats* chunk_stats,
+                        int32_t n_regions, DevParams P, cudaStream_t s) {
   if (n_regions == 0) return;
-  k_region_prep<<<(n_regions + 127) / 128, 128, 0, s>>>(regions, stats, n_regions, P);
+  k_region_prep<<<n_regions, 256, 0, s>>>(regions, stats, chunk_stats, P);
 }
 
 }  // namespace pg

@@ -26,9 +26,10 @@ def lib():
     """Loads the engine library; raises if it was not built."""
     global _LIB
     if _LIB is None:
-        if not os.path.exists(ENGINE):
-            raise EngineError(-1, f"engine library {ENGINE} is missing; run pilon_gb300.build.build()")
-        L = C.CDLL(ENGINE)
+        path = os.environ.get("PILON_GB300_ENGINE", ENGINE)  # an alternative build of the same ABI
+        if not os.path.exists(path):
+            raise EngineError(-1, f"engine library {path} is missing; run pilon_gb300.build.build()")
+        L = C.CDLL(path)
         vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
         sig = {
             "pg_open": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
@@ -42,7 +43,7 @@ def lib():
             "pg_pileup_regions": (C.c_int, [vp, vp, i32, C.POINTER(_abi.pg_params), i32]),
             "pg_fetch_stats": (C.c_int, [vp, i32, C.POINTER(_abi.pg_region_stats)]),
             "pg_fetch_region": (C.c_int, [vp, i32, C.POINTER(_abi.pg_region_out)]),
-            "pg_set_tuning": (C.c_int, [vp, i32, i32]),
+            "pg_set_tuning": (C.c_int, [vp, i32, i32, i32]),
             "pg_kmer_tally": (C.c_int, [vp, vp, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
                                         C.POINTER(C.c_int64)]),
             "pg_last_kernel_ms": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -136,8 +137,8 @@ class Engine:
         self._check(self.L.pg_set_reads(self.h, C.byref(ab)))
         self.n_reads = reads.n_reads
 
-    def set_tuning(self, tile_width=0, warps=0):
-        self._check(self.L.pg_set_tuning(self.h, tile_width, warps))
+    def set_tuning(self, tile_width=0, warps=0, variant=-1):
+        self._check(self.L.pg_set_tuning(self.h, tile_width, warps, variant))
 
     def pileup_regions(self, regions, params, batched=True):
         """regions: list of (contig, start, stop, read_begin, read_end)."""

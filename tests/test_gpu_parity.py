@@ -64,3 +64,21 @@ def test_long_read_modes(engine, cfg1):
     for lr in (_abi.PG_NANOPORE, _abi.PG_PACBIO):
         p = _abi.default_params(long_read=lr, bam_type=_abi.PG_BAM_UNPAIRED)
         run_both(engine, cfg1, p, plan(cfg1, chunk_size=20_000))
+
+
+@pytest.mark.parametrize("tile,warps,variant", [(1024, 8, 0), (1024, 16, 1), (2048, 8, 2), (4096, 16, 0),
+                                                (512, 16, 1), (4096, 8, 2), (256, 4, 1), (2048, 16, 2)])
+def test_walk_tunings_bit_exact(engine, cfg1, tile, warps, variant):
+    engine.set_tuning(tile, warps, variant)
+    try:
+        run_both(engine, cfg1, _abi.default_params(), plan(cfg1, chunk_size=12_000))
+    finally:
+        engine.set_tuning(2048, 16, 0)
+
+
+def test_high_coverage_multi_pass(engine):
+    # 2,000x on a short contig: a 4,096-position tile sees ~55k reads per pass limit region
+    w = synth.workload(1, scale=0.04)
+    w.coverage = 2000.0
+    ds = synth.generate(w)
+    run_both(engine, ds, _abi.default_params(), plan(ds))
