@@ -231,6 +231,16 @@ pg_status pg_kmer_tally(pg_ctx *ctx, const pg_window *windows, int32_t n_windows
                         int32_t K, const pg_params *params, int32_t min_depth,
                         pg_kmer_edge *edges, int64_t cap, int64_t *n_edges);
 
+/* ---- VCF ----------------------------------------------------------------
+ * The per-position records of GenomeRegion.writeVcf / Vcf.writeRecord
+ * (S/GenomeRegion.scala:623-643, S/Vcf.scala:74-176) for one region of the
+ * last pg_pileup_regions call, formatted on the device.  `name` is the
+ * contig name.  The text (no header, no <DUP> or reassembly records) is
+ * copied into `out` when it fits in `cap` bytes; *n_bytes receives its size
+ * either way (PG_ERR_LIMIT when it does not fit). */
+pg_status pg_format_vcf(pg_ctx *ctx, int32_t region, const char *name, int32_t diploid, int32_t vcf_qe,
+                        char *out, int64_t cap, int64_t *n_bytes);
+
 /* ---- timing -------------------------------------------------------------
  * Milliseconds of the dominant (pileup walk) kernel in the last
  * pg_pileup_regions call, measured with CUDA events on the context stream,

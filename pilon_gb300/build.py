@@ -19,7 +19,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ENGINE = os.path.join(BUILD, "libpilon_gb300.so")
 SYNTH = os.path.join(BUILD, "libpg_synth.so")
 
-CU_SOURCES = ["pg_api.cu", "pg_pileup.cu", "pg_call.cu", "pg_kmer.cu", "pg_noalloc.cu"]
+CU_SOURCES = ["pg_api.cu", "pg_pileup.cu", "pg_call.cu", "pg_kmer.cu", "pg_format.cu", "pg_noalloc.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-fwrapv", "--expt-relaxed-constexpr"]
 
@@ -52,7 +52,7 @@ def _run_all(cmds):
 def build(force=False, verbose=False):
     """Compiles the engine and the simulator; returns the engine path."""
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(INCLUDE, "pilon_gb300.h"), os.path.join(CSRC, "pg_internal.cuh")]
+    headers = [os.path.join(INCLUDE, "pilon_gb300.h")] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".cuh")]
     nvcc = _nvcc()
     objs, cmds = [], []
     for s in CU_SOURCES:

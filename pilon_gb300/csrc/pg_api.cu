@@ -11,6 +11,7 @@
 
 #include "pg_internal.cuh"
 #include "pg_kmer.cuh"
+#include "pg_format.cuh"
 
 using namespace pg;
 
@@ -62,6 +63,8 @@ struct pg_ctx {
   // k-mer tally
   DevBuf kwin, kpre, kslot_base, kslot_cap, kx_base, kx_cap, kkeys, kcnt, kqs, kmq, kq;
   DevBuf kx_keys, kx_used, kx_cnt, kx_qs, kx_mq, kx_q, kedges, kcount;
+  // VCF formatting
+  DevBuf vlen, vsums, vtext, vname;
   // tuning
   int32_t tile_width = 2048, warps = 16, packed = 0;
 };
@@ -215,7 +218,7 @@ void pg_close(pg_ctx* c) {
   for (DevBuf* b : all) release(*b);
   DevBuf* km[] = {&c->kwin, &c->kpre, &c->kslot_base, &c->kslot_cap, &c->kx_base, &c->kx_cap, &c->kkeys, &c->kcnt,
                   &c->kqs, &c->kmq, &c->kq, &c->kx_keys, &c->kx_used, &c->kx_cnt, &c->kx_qs, &c->kx_mq, &c->kx_q,
-                  &c->kedges, &c->kcount};
+                  &c->kedges, &c->kcount, &c->vlen, &c->vsums, &c->vtext, &c->vname};
   for (DevBuf* b : km) release(*b);
   for (auto& b : c->rec_i32) release(b);
   for (auto& b : c->rd) release(b);
@@ -744,6 +747,47 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
     CK(cudaMemcpyAsync(edges, c->kedges.p, sizeof(pg_kmer_edge) * ncopy, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
   }
+  return PG_OK;
+}
+
+pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid, int32_t vcf_qe, char* out,
+                        int64_t cap, int64_t* n_bytes) {
+  if (!c || !name || !n_bytes || cap < 0) return fail(c, PG_ERR_ARG, "bad arguments");
+  if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
+  if (r < 0 || r >= c->n_regions) return fail(c, PG_ERR_ARG, "region %d out of range", r);
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  const RegionDev& g = c->regions_h[r];
+  const int64_t n = g.size;
+  const size_t nl = strlen(name);
+  pg_status s;
+  if ((s = ensure(c, c->vlen, 8 * (size_t)n))) return s;
+  if ((s = ensure(c, c->vsums, 8 * (size_t)((n + 1023) / 1024 + 2)))) return s;
+  if ((s = ensure(c, c->vname, nl + 1))) return s;
+  CK(cudaMemcpyAsync(c->vname.p, name, nl + 1, cudaMemcpyHostToDevice, st));
+  FormatArgs A;
+  A.region = g;
+  A.rec = records(c);
+  A.ref = P<uint8_t>(c->ref);
+  A.pool = P<char>(c->pool);
+  A.name = P<char>(c->vname);
+  A.name_len = (int32_t)nl;
+  A.min_depth = c->stats_h[r].min_depth;
+  A.diploid = diploid;
+  A.vcf_qe = vcf_qe;
+  launch_vcf_lengths(A, P<int64_t>(c->vlen), st);
+  launch_scan64(P<int64_t>(c->vlen), n, P<int64_t>(c->vsums), st);
+  int64_t total = 0;
+  const int32_t nb = (int32_t)((n + 1023) / 1024);
+  CK(cudaMemcpyAsync(&total, P<int64_t>(c->vsums) + nb, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  *n_bytes = total;
+  if (total > cap) return fail(c, PG_ERR_LIMIT, "VCF text needs %lld bytes", (long long)total);
+  if ((s = ensure(c, c->vtext, (size_t)std::max<int64_t>(total, 1)))) return s;
+  launch_vcf_write(A, P<int64_t>(c->vlen), P<char>(c->vtext), st);
+  CK(cudaGetLastError());
+  if (total && out) CK(cudaMemcpyAsync(out, c->vtext.p, (size_t)total, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
   return PG_OK;
 }
 

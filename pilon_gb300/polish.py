@@ -1,0 +1,361 @@
+"""Whole-genome polishing on the GB300 engine: the loop of
+GenomeFile.processRegions (S/GenomeFile.scala:84-176) for the fix types
+snps / indels (and amb / iupac), writing Pilon's three outputs.
+
+  pileup, BaseCall, pass 1      engine (pg_pileup_regions), batched over all regions
+  fix lists, fixIssues          host, over the sparse change list (S/GenomeRegion.scala:307-414, 557-621)
+  VCF records                   engine (pg_format_vcf); header and <DUP> records here
+  changes, FASTA                host (S/GenomeRegion.scala:645-657, S/GenomeFile.scala:79-82, 135-161)
+
+Gap filling and local reassembly (fix types gaps / local) are not part of
+this driver; their break windows feed the K-mer tally (pilon_gb300.assembler).
+"""
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from .regions import plan_regions
+
+ACGT = "ACGT"
+IUPAC = {1: "A", 2: "C", 4: "G", 8: "T", 5: "R", 10: "Y", 6: "S", 9: "W", 12: "K", 3: "M", 14: "B", 13: "D",
+         11: "H", 7: "V", 15: "N"}
+
+
+@dataclass
+class Options:
+    """The command-line switches of Pilon that this path honours (S/Pilon.scala:28-73)."""
+    fix_snps: bool = True
+    fix_indels: bool = True
+    iupac: bool = False
+    diploid: bool = False
+    vcf: bool = True
+    vcf_qe: bool = False
+    changes: bool = True
+    longread: bool = False
+    nanopore: bool = False
+    chunk_size: int = 10_000_000
+    targets: list = None            # [(contig, start, stop)] or None
+    vcf_date: str = "20260101"
+    vcf_source: str = "Pilon version [COMMIT] [DATE]"
+    vcf_args: str = ""
+    vcf_ref: str = "file:/genome.fasta"
+
+
+@dataclass
+class Fix:
+    locus: int
+    was: str
+    patch: str
+
+
+def to_iupac(a, b):  # Bases.toIUPAC (S/Bases.scala:85-88)
+    return IUPAC[(1 << ACGT.index(a)) | (1 << ACGT.index(b))]
+
+
+def fix_fix_list(fixes):
+    """GenomeRegion.fixFixList (S/GenomeRegion.scala:557-593): stable sort by
+    locus, then of two overlapping fixes keep the one with more bases."""
+    fx = sorted(fixes, key=lambda f: f.locus)
+    out = []
+    k = 0
+    while k < len(fx):
+        if k + 1 < len(fx):
+            f1, f2 = fx[k], fx[k + 1]
+            e1 = f1.locus + max(len(f1.was) - 1, 0)
+            e2 = f2.locus + max(len(f2.was) - 1, 0)
+            if f2.locus <= e1 and e2 >= f1.locus:
+                if len(f1.was) + len(f1.patch) >= len(f2.was) + len(f2.patch):
+                    fx[k + 1] = f1
+                k += 1
+            else:
+                out.append(f1)
+                k += 1
+        else:
+            out.append(fx[k])
+            k += 1
+    return out
+
+
+def fix_issues(bases, start, fixes):
+    """GenomeRegion.fixIssues (S/GenomeRegion.scala:595-621) on a bytearray."""
+    nb = bytearray(bases)
+    for f in reversed(fix_fix_list(fixes)):
+        s = f.locus - start
+        if len(f.was) == len(f.patch):
+            nb[s:s + len(f.patch)] = f.patch.encode()
+        else:
+            nb = nb[:s] + f.patch.encode() + nb[s + len(f.was):]
+    return nb
+
+
+def region_string(name, s, e):  # Region.regionString (S/Region.scala:45)
+    return f"{name}:{s}" + ("" if e + 1 - s < 2 else f"-{e}")
+
+
+def smooth(inp, window):
+    """GenomeRegion.smooth (S/GenomeRegion.scala:190-210), same integer steps."""
+    n = inp.size
+    res = np.zeros(n, np.int64)
+    half = window // 2
+    if n > window:
+        cs = np.concatenate([[0], np.cumsum(inp.astype(np.int64))])
+        i = np.arange(window + 1, n)
+        # after step i the accumulator holds input[0] + input[i-window+1 .. i]
+        acc = inp[0] + (cs[i + 1] - cs[i - window + 1])
+        res[i - half] = (acc + half) // window
+        res[:window - half] = res[window - half]
+        res[n - half:] = res[n - half - 1]
+    else:
+        res[:] = int(inp.astype(np.int64).sum()) // n
+    return res
+
+
+def java_round(x):
+    f = np.floor(x)
+    return np.where(x - f >= 0.5, f + 1, f).astype(np.int64)
+
+
+def summary_regions(test, start, stop, slop):
+    """GenomeRegion.summaryRegions (S/GenomeRegion.scala:743-763) on a boolean array."""
+    idx = np.nonzero(test)[0]
+    regs = []
+    if idx.size:
+        gaps = np.nonzero(np.diff(idx) > slop)[0]
+        firsts = np.concatenate([[idx[0]], idx[gaps + 1]])
+        lasts = np.concatenate([idx[gaps], [idx[-1]]])
+        regs = [(start + int(a), start + int(b)) for a, b in zip(firsts, lasts)]
+    return [r for r in regs if not (r[0] - start < 100 or stop - r[1] < 100)]
+
+
+@dataclass
+class RegionResult:
+    contig: int
+    start: int
+    stop: int
+    bases: bytearray
+    snp: list = field(default_factory=list)
+    small: list = field(default_factory=list)
+    dupes: list = field(default_factory=list)
+    stats: object = None
+
+    def all_fixes(self):
+        return fix_fix_list(self.snp + self.small)
+
+
+def _region_outputs(engine, r, region, ref, opts, params):
+    """Sparse change list -> fix lists and fixed bases; copy number -> <DUP> records."""
+    c, s, e, _, _ = region
+    size = e - s + 1
+    st = engine.stats(r)
+    cnt = np.empty(4 * size, np.int32)
+    dels = np.empty(size, np.int32)
+    call = np.empty(size, np.uint32)
+    ilen = np.empty(size, np.int32)
+    istr = np.empty(size, np.int32)
+    o = _abi.pg_region_out()
+    o.count = cnt.ctypes.data
+    o.deletions = dels.ctypes.data
+    o.call = call.ctypes.data
+    o.indel_len = ilen.ctypes.data
+    o.ins_str = istr.ctypes.data
+    engine._check(engine.L.pg_fetch_region(engine.h, r, C.byref(o)))
+    pool = int(o.ins_chars_cap)
+    chars = b""
+    if pool:
+        buf = np.zeros(pool, np.uint8)
+        o2 = _abi.pg_region_out()
+        o2.ins_chars = buf.ctypes.data
+        o2.ins_chars_cap = pool
+        engine._check(engine.L.pg_fetch_region(engine.h, r, C.byref(o2)))
+        chars = buf.tobytes()
+    orig = bytes(ref[s - 1:e])
+    res = RegionResult(c, s, e, bytearray(orig), stats=st)
+    kind = (call >> 9) & 7
+    chg = np.nonzero(kind)[0]
+    excluded = np.zeros(size, bool)
+    if opts.longread and opts.nanopore is not None and opts.longread_only:
+        excluded = _exclude_motifs(orig, s, e, opts.nanopore)
+    for i in chg.tolist():
+        if excluded[i]:
+            continue
+        k = int(kind[i])
+        loc = s + i
+        rb = chr(ref[loc - 1]).upper()
+        f = int(call[i])
+        cb = ACGT[f & 3] if f & _abi.PG_CALL_HAS_BASE else "N"
+        alt = ACGT[(f >> 2) & 3]
+        if k == _abi.PG_CHANGE_SNP:
+            if opts.fix_snps:
+                res.snp.append(Fix(loc, rb, cb))
+        elif k == _abi.PG_CHANGE_AMB:
+            if opts.fix_snps and not opts.longread:
+                if opts.iupac:
+                    res.small.append(Fix(loc, rb, to_iupac(cb, alt)))
+                else:
+                    res.snp.append(Fix(loc, rb, cb))
+        elif k == _abi.PG_CHANGE_INS:
+            if opts.fix_indels:
+                off = int(istr[i])
+                res.small.append(Fix(loc, "", chars[off:off + int(ilen[i])].decode()))
+        elif k == _abi.PG_CHANGE_DEL:
+            if opts.fix_indels:
+                res.small.append(Fix(loc, bytes(ref[loc - 1:loc - 1 + int(ilen[i])]).decode(), ""))
+    # the reference prepends to its lists: descending loci, then stable-sorted
+    res.snp.reverse()
+    res.small.reverse()
+    res.bases = fix_issues(res.bases, s, res.snp)
+    res.bases = fix_issues(res.bases, s, res.small)
+    if opts.vcf and st.read_count > 0:
+        # fragCoverage = depth after the BAM, before pass 1 added deletion counts
+        frag = cnt.reshape(-1, 4).astype(np.int64).sum(1) + dels
+        for i in np.nonzero(kind == _abi.PG_CHANGE_DEL)[0].tolist():
+            L = int(ilen[i])
+            frag[i + 1:i + L] -= int(dels[i])
+        mean = float(frag.sum()) / size
+        sm = smooth(frag, 200)
+        cn = java_round(sm / mean) if mean > 0 else np.zeros(size, np.int64)
+        regs = summary_regions(cn > 1, s, e, 2000)
+        res.dupes = [r2 for r2 in regs if r2[1] + 1 - r2[0] > 10000]
+        if res.dupes:
+            # records per position: one, plus one after an indel call at i > 0 outside a deletion
+            extra = ((call & (_abi.PG_CALL_INS | _abi.PG_CALL_DEL)) != 0) & ((call & _abi.PG_CALL_DELETED) == 0)
+            extra[0] = False
+            res.first_line = np.concatenate([[0], np.cumsum(1 + extra.astype(np.int64))])
+    return res
+
+
+def _exclude_motifs(orig, s, e, nano):
+    """GenomeRegion.excludeMotifs (S/GenomeRegion.scala:432-439)."""
+    b = np.frombuffer(bytes(orig).upper(), np.uint8)
+    n = b.size
+    run = np.ones(n, np.int64)
+    for i in range(n - 2, -1, -1):
+        if b[i] == b[i + 1]:
+            run[i] = run[i + 1] + 1
+    ex = run >= 4
+    if nano:
+        C, G = ord("C"), ord("G")
+        for i in range(2, n - 2):
+            if b[i - 2] == C and b[i - 1] == C and b[i + 1] == G and b[i + 2] == G:
+                ex[i] = True
+    return ex
+
+
+VCF_HEADER_TAIL = (
+    '##FILTER=<ID=LowCov,Description="Low Coverage of good reads at location">\n'
+    '##FILTER=<ID=Amb,Description="Ambiguous evidence in haploid genome">\n'
+    '##FILTER=<ID=Del,Description="This base is in a deletion or change event from another record">\n'
+    '##INFO=<ID=DP,Number=1,Type=Integer,Description="Valid read depth; some reads may have been filtered">\n'
+    '##INFO=<ID=TD,Number=1,Type=Integer,Description="Total read depth including bad pairs">\n'
+    '##INFO=<ID=PC,Number=1,Type=Integer,Description="Physical coverage of valid inserts across locus">\n'
+    '##INFO=<ID=BQ,Number=1,Type=Integer,Description="Mean base quality at locus">\n'
+    '##INFO=<ID=MQ,Number=1,Type=Integer,Description="Mean read mapping quality at locus">\n'
+    '##INFO=<ID=QD,Number=1,Type=Integer,Description="Variant confidence/quality by depth">\n'
+    '##INFO=<ID=BC,Number=4,Type=Integer,Description="Count of As, Cs, Gs, Ts at locus">\n')
+VCF_QE = '##INFO=<ID=QE,Number=4,Type=Integer,Description="Evidence for As, Cs, Gs, Ts weighted by Q & MQ at locus">\n'
+VCF_QP = ('##INFO=<ID=QP,Number=4,Type=Integer,Description="Percentage of As, Cs, Gs, Ts weighted by Q & MQ at '
+          'locus">\n')
+VCF_HEADER_END = (
+    '##INFO=<ID=IC,Number=1,Type=Integer,Description="Number of reads with insertion here">\n'
+    '##INFO=<ID=DC,Number=1,Type=Integer,Description="Number of reads with deletion here">\n'
+    '##INFO=<ID=XC,Number=1,Type=Integer,Description="Number of reads clipped here">\n'
+    '##INFO=<ID=AC,Number=A,Type=Integer,Description="Allele count in genotypes, for each ALT allele, in the same '
+    'order as listed">\n'
+    '##INFO=<ID=AF,Number=A,Type=Float,Description="Fraction of evidence in support of alternate allele(s)">\n'
+    '##INFO=<ID=SVTYPE,Number=1,Type=String,Description="Type of structural variant">\n'
+    '##INFO=<ID=SVLEN,Number=.,Type=String,Description="Difference in length between REF and ALT alleles">\n'
+    '##INFO=<ID=END,Number=1,Type=Integer,Description="End position of the variant described in this record">\n'
+    '##INFO=<ID=IMPRECISE,Number=0,Type=Flag,Description="Imprecise change from local reassembly (ALT contains '
+    'Ns)">\n'
+    '##FORMAT=<ID=GT,Number=1,Type=String,Description="Genotype">\n'
+    '##FORMAT=<ID=AD,Number=.,Type=String,Description="Allelic depths for the ref and alt alleles in the order '
+    'listed">\n'
+    '##FORMAT=<ID=DP,Number=1,Type=String,Description="Approximate read depth; some reads may have been filtered">\n'
+    '##ALT=<ID=DUP,Description="Possible segmental duplication">\n'
+    '#CHROM\tPOS\tID\tREF\tALT\tQUAL\tFILTER\tINFO\tFORMAT\tSAMPLE\n')
+
+
+def vcf_header(contigs_with_sizes, opts):
+    """Vcf.writeHeader (S/Vcf.scala:28-68)."""
+    h = (f"##fileformat=VCFv4.1\n##fileDate={opts.vcf_date}\n##source=\"{opts.vcf_source}\"\n"
+         f"##PILON=\"{opts.vcf_args}\"\n##reference={opts.vcf_ref}\n")
+    for c, s in contigs_with_sizes:
+        h += f"##contig=<ID={c},length={s}>\n"
+    return h + VCF_HEADER_TAIL + (VCF_QE if opts.vcf_qe else VCF_QP) + VCF_HEADER_END
+
+
+def new_name(name):  # S/GenomeFile.scala:137-140
+    sep = "_" if "|" not in name else ("" if name.endswith("|") else "|")
+    return name + sep + "pilon"
+
+
+def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched=True):
+    """Runs the engine over every region and writes out_prefix.{fasta,vcf,changes}.
+    Returns the per-region results."""
+    opts = opts or Options()
+    opts.longread_only = bool(opts.longread) and bool(getattr(opts, "no_frags", False))
+    lens = [int(c.size) for c in contigs]
+    regions = plan_regions(reads, lens, opts.chunk_size, opts.targets)
+    engine.set_reference(contigs)
+    engine.set_reads(reads)
+    engine.pileup_regions(regions, params, batched=batched)
+    results = [_region_outputs(engine, r, reg, contigs[reg[0]], opts, params) for r, reg in enumerate(regions)]
+    by_contig = {}
+    for r, res in enumerate(results):
+        by_contig.setdefault(res.contig, []).append(r)
+    order = []
+    for r, res in enumerate(results):
+        if res.contig not in order:
+            order.append(res.contig)
+    if opts.vcf:
+        with open(out_prefix + ".vcf", "wb") as vf:
+            sizes = [(names[c], sum(results[r].stop - results[r].start + 1 for r in by_contig[c])) for c in order]
+            vf.write(vcf_header(sizes, opts).encode())
+            for r, res in enumerate(results):
+                text = engine.format_vcf(r, names[res.contig], opts.diploid, opts.vcf_qe)
+                vf.write(_splice_dupes(text, res, names[res.contig], contigs[res.contig]))
+    if opts.changes:
+        with open(out_prefix + ".changes", "w") as cf:
+            for c in order:
+                nn = new_name(names[c])
+                offset = 0
+                for r in by_contig[c]:
+                    res = results[r]
+                    delta = 0
+                    for f in res.all_fixes():
+                        nl = f.locus + delta
+                        cf.write(region_string(names[c], f.locus, f.locus + len(f.was) - 1) + " " +
+                                 region_string(nn, nl + offset, nl + offset + len(f.patch) - 1) + " " +
+                                 (f.was or ".") + " " + (f.patch or ".") + "\n")
+                        delta += len(f.patch) - len(f.was)
+                    offset += len(res.bases) - (res.stop - res.start + 1)
+    if opts.fix_snps or opts.fix_indels:
+        with open(out_prefix + ".fasta", "wb") as ff:
+            for c in order:
+                seq = b"".join(bytes(results[r].bases) for r in by_contig[c])
+                ff.write(b">" + new_name(names[c]).encode() + b"\n")
+                for k in range(0, len(seq), 80):
+                    ff.write(seq[k:k + 80] + b"\n")
+    return results
+
+
+def _splice_dupes(text, res, name, ref):
+    """Inserts Vcf.writeDup records (S/Vcf.scala:194-202) before the records of
+    each duplication's first position (S/GenomeRegion.scala:628-631)."""
+    if not res.dupes:
+        return text
+    lines = text.split(b"\n")
+    out = []
+    prev = 0
+    for d in res.dupes:
+        k = int(res.first_line[d[0] - res.start])
+        out.extend(lines[prev:k])
+        loc = d[0] - 1
+        rb = chr(ref[loc - 1]).upper()
+        out.append(f"{name}\t{loc}\t.\t{rb}\t<DUP>\t.\tPASS\tSVTYPE=DUP;SVLEN={d[1] + 1 - d[0]};"
+                   f"END={d[1]};IMPRECISE\tGT\t./.".encode())
+        prev = k
+    out.extend(lines[prev:])
+    return b"\n".join(out)
