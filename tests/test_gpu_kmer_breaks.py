@@ -1,0 +1,101 @@
+"""K-mer tally and break detection on the GPU path against the oracle."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from pilon_gb300 import _abi, synth
+from pilon_gb300.breaks import possible_breaks, region_arrays
+from pilon_gb300.regions import ReadIndex, plan_regions
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def engine():
+    from pilon_gb300.engine import Engine
+    e = Engine(0)
+    yield e
+    e.close()
+
+
+@pytest.fixture(scope="module")
+def euk():
+    # the eukaryotic workload scaled to 600 kb: repeats with mapq 0-3, 10-200 bp indels
+    return synth.generate(4, scale=0.005)
+
+
+def edge_set(edges):
+    return {(int(e["window"]), int(e["key_hi"]), int(e["key_lo"]), int(e["next"]), int(e["alt"]), int(e["depth"]),
+             int(e["weight"])) for e in edges}
+
+
+def test_breaks_match_oracle(engine, euk):
+    ds = euk
+    p = _abi.default_params()
+    regions = plan_regions(ds.reads, [c.size for c in ds.contigs], chunk_size=200_000)
+    engine.set_reference(ds.contigs)
+    engine.set_reads(ds.reads)
+    engine.pileup_regions(regions, p)
+    total = 0
+    for r, (c, s, e, a, b) in enumerate(regions):
+        x = engine.fetch(r)
+        cov, bad, clips, frag = region_arrays(x.count, x.deletions, x.bad_pair, x.clips, x.call, x.indel_len,
+                                              x.stats.read_count)
+        got = possible_breaks(cov, bad, clips, frag, ds.contigs[c][s - 1:e], s, e)
+        want = oracle.region_breaks(ds.reads, p, ds.contigs[c], c, s, e, a, b)
+        assert got == want, (r, got[:5], want[:5])
+        total += len(want)
+    assert total > 0
+
+
+def test_kmer_tally_matches_oracle(engine, euk):
+    ds = euk
+    p = _abi.default_params()
+    idx = ReadIndex(ds.reads, len(ds.contigs))
+    n = ds.contigs[0].size
+    # windows around planted-indel neighbourhoods: reads overlapping [x - 500, x + 500]
+    wins = []
+    for (pos, kind, ref, alt) in ds.variants[0][:40]:
+        a, b = idx.range_for(0, max(1, pos - 500), min(n, pos + 500), n, slop=0)
+        wins.append((a, b))
+    engine.set_reference(ds.contigs)
+    engine.set_reads(ds.reads)
+    for K in (31, 19):
+        got = engine.kmer_tally(wins, K, p)
+        want = oracle.kmer_tally(ds.reads, p, wins, K)
+        assert len(got) > 1000
+        assert edge_set(got) == edge_set(want)
+
+
+def test_kmer_tally_exotic_kmers(engine, cfg1):
+    # reads with N bases give K-mers that cannot be 2-bit packed
+    ds = cfg1
+    r = ds.reads
+    seq = r.seq.copy()
+    rng = np.random.Generator(np.random.PCG64(5))
+    hit = rng.choice(r.n_reads, size=r.n_reads // 5, replace=False)
+    for i in hit[:2000].tolist():  # put an N (code 15) at base 40 of 2,000 reads
+        o = int(r.seq_off[i]) + 20
+        seq[o] = (seq[o] & 0x0F) | 0xF0
+    r2 = r.subset(np.arange(r.n_reads))
+    r2.seq = seq
+    engine.set_reference(ds.contigs)
+    engine.set_reads(r2)
+    p = _abi.default_params()
+    wins = [(0, 3000), (3000, 6000), (5000, 9000)]
+    got = engine.kmer_tally(wins, 25, p, min_depth=2)
+    want = oracle.kmer_tally(r2, p, wins, 25, min_depth=2)
+    assert edge_set(got) == edge_set(want)
+    assert any((int(e["key_hi"]) >> 60) == 15 or "F" in format(int(e["key_hi"]), "016x") for e in want)
+
+
+def test_assembler_graph(engine, cfg1):
+    from pilon_gb300.assembler import Assembler
+    engine.set_reference(cfg1.contigs)
+    engine.set_reads(cfg1.reads)
+    asm = Assembler(engine, K=21)
+    w = asm.add_reads(100, 900)
+    kg, ag = asm.build_graph(_abi.default_params())[w]
+    assert len(kg) > 100
+    for k, nxt in list(kg.items())[:50]:
+        assert nxt[:-1] == k[1:] and len(nxt) == 21
