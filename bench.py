@@ -132,7 +132,9 @@ def pinned_store(reads):
 
 
 class PinnedOut:
-    def __init__(self, size):
+    CALL_FIELDS = ("call", "score", "indel_len", "ins_str")
+
+    def __init__(self, size, fields="all"):
         import torch
         from pilon_gb300.engine import RegionArrays
         self.t = []
@@ -143,10 +145,11 @@ class PinnedOut:
             t = torch.empty(n * np.dtype(dt).itemsize, dtype=torch.uint8, pin_memory=True)
             self.t.append(t)
             return t.numpy().view(dt)
-        ra.count = mk(4 * size, np.int32)
-        ra.qual_sum = mk(4 * size, np.int64)
+        want = lambda f: fields == "all" or f in self.CALL_FIELDS
+        ra.count = mk(4 * size, np.int32) if want("count") else None
+        ra.qual_sum = mk(4 * size, np.int64) if want("qual_sum") else None
         for f in RegionArrays.I32:
-            setattr(ra, f, mk(size, np.int32))
+            setattr(ra, f, mk(size, np.int32) if want(f) else None)
         ra.call = mk(size, np.uint32)
         ra.score = mk(size, np.int64)
         ra.ins_chars = np.zeros(0, np.uint8)
@@ -249,6 +252,9 @@ def main():
     ap.add_argument("--variant", type=int, default=-1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--autotune", type=int, default=1)
+    ap.add_argument("--compare-plain", type=int, default=-1, help="also time the per-region path (default: on "
+                    "when there is more than one region)")
+    ap.add_argument("--e2e-fields", default="auto", help="all | calls: what the end-to-end step reads back")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -329,12 +335,29 @@ def main():
     achieved = walk_bytes / walk_avg / 1e9
     traffic = roofline_traffic(ds.workload.name, units)
 
+    # the plain path: every region through its own launches, no graph
+    plain = None
+    if (args.compare_plain == 1 or (args.compare_plain == -1 and len(regions) > 1)) and args.batched:
+        for _ in range(2):
+            eng.pileup_regions(regions, params, batched=False)
+        pm, pn = [], 0
+        for _ in range(max(2, min(args.steps, 5))):
+            eng.pileup_regions(regions, params, batched=False)
+            w, t, n = eng.last_kernel_ms()
+            pm.append(t)
+            pn = n
+        ps = max_over_ranks(dist, sum(pm) / 1e3)
+        plain = {"value": units * ws * len(pm) / ps / 1e9, "ms_per_step": 1e3 * ps / len(pm),
+                 "gpu_launches_per_step": pn, "path": "one set of launches per region, no graph"}
+        eng.pileup_regions(regions, params, batched=True)
+
     # end to end through the C ABI: H2D of the read store from pinned memory,
     # pileup + calls, D2H of every region's records and calls
     e2e = None
     if not args.no_e2e:
+        fields = args.e2e_fields if args.e2e_fields != "auto" else ("all" if sum(lens) <= 20_000_000 else "calls")
         pin = pinned_store(ds.reads)
-        outs = [PinnedOut(e - s + 1) for (c, s, e, a, b) in regions]
+        outs = [PinnedOut(e - s + 1, fields) for (c, s, e, a, b) in regions]
         h2d = pin.nbytes()
         d2h = sum(o.nbytes() for o in outs)
         for _ in range(args.warmup):
@@ -353,7 +376,7 @@ def main():
         e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
         barrier(dist)
         e2e = {"value": units * ws * args.steps / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / args.steps,
+               "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / args.steps, "read_back": fields,
                "timing": "host wall clock; every call synchronises the engine stream"}
 
     cpu = None
@@ -378,6 +401,8 @@ def main():
                      if peaks else "fallback"},
         "gpu_launches": launches,
         "tuning": tuning,
+        "plain_per_region": plain,
+        "batched_over_plain": (value / plain["value"]) if plain else None,
         "clocks": clk.summary(),
         "e2e": e2e,
         "cpu_baseline": cpu,

@@ -65,6 +65,13 @@ struct pg_ctx {
   DevBuf kx_keys, kx_used, kx_cnt, kx_qs, kx_mq, kx_q, kedges, kcount;
   // VCF formatting
   DevBuf vlen, vsums, vtext, vname;
+  // CUDA graph of the batched pipeline, replayed while the plan and buffers are unchanged
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  uint64_t graph_key = 0;
+  int32_t use_graph = 1;
+  int32_t graph_replays = 0;
+  bool capturing = false;
   // tuning
   int32_t tile_width = 2048, warps = 16, packed = 0;
 };
@@ -162,6 +169,12 @@ struct Plan {
   std::vector<ReadChunk> chunks;
 };
 
+inline uint64_t fnv(uint64_t h, const void* p, size_t n) {
+  const unsigned char* b = (const unsigned char*)p;
+  for (size_t k = 0; k < n; k++) h = (h ^ b[k]) * 0x100000001b3ull;
+  return h;
+}
+
 }  // namespace
 
 extern "C" {
@@ -228,6 +241,8 @@ void pg_close(pg_ctx* c) {
   if (c->w0) cudaEventDestroy(c->w0);
   if (c->w1) cudaEventDestroy(c->w1);
   for (cudaEvent_t e : c->wev) cudaEventDestroy(e);
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -385,9 +400,11 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
     cudaEventCreate(&e);
     c->wev.push_back(e);
   }
-  cudaEventRecord(c->wev[2 * c->n_runs], s);
+  // inside a stream capture the records must be external to become event nodes of the graph
+  const unsigned evf = c->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+  cudaEventRecordWithFlags(c->wev[2 * c->n_runs], s, evf);
   launch_walk(wa, w0, wn, c->warps, s);
-  cudaEventRecord(c->wev[2 * c->n_runs + 1], s);
+  cudaEventRecordWithFlags(c->wev[2 * c->n_runs + 1], s, evf);
   c->n_runs++;
 
   EventArgs ea;
@@ -519,26 +536,61 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
     if ((s = ensure(c, c->pool, (size_t)c->pool_cap))) return s;
     if ((s = ensure(c, c->spool, 8 * (size_t)c->spool_cap))) return s;
     cudaStream_t st = c->stream;
-    c->launches = 0;
-    c->n_runs = 0;
-    CK(cudaEventRecord(c->e0, st));
-    CK(cudaMemcpyAsync(c->regions.p, c->staging_host, b_reg, cudaMemcpyHostToDevice, st));
-    if (b_walk) CK(cudaMemcpyAsync(c->walk_tiles.p, (char*)c->staging_host + b_reg, b_walk, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(c->call_tile_region.p, (char*)c->staging_host + b_reg + b_walk, b_call, cudaMemcpyHostToDevice, st));
-    if (b_ch) CK(cudaMemcpyAsync(c->chunks.p, (char*)c->staging_host + b_reg + b_walk + b_call, b_ch,
-                                 cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(c->stats.p, 0, sizeof(StatsDev) * n_regions, st));
-    CK(cudaMemsetAsync(c->counters.p, 0, sizeof(unsigned long long) * CNT_N, st));
-    CK(cudaMemsetAsync(c->run_max.p, 0, sizeof(unsigned long long) * 2, st));
+    // identity of everything the recorded launches depend on
+    uint64_t key = 0xcbf29ce484222325ull;
+    key = fnv(key, c->staging_host, b_reg + b_walk + b_call + b_ch);
+    key = fnv(key, &dp, sizeof dp);
+    key = fnv(key, &c->R, sizeof c->R);
+    const void* ptrs[] = {c->ref.p, c->events.p, c->events_sorted.p, c->cands.p, c->pool.p, c->spool.p,
+                          c->rec_count.p, c->rec_qsum.p, c->rec_call.p, c->rec_score.p, c->rec_indel_len.p,
+                          c->rec_ins_str.p, c->rec_ev_end.p, c->chunk_stats.p, c->stats.p, c->tile_sums.p};
+    key = fnv(key, ptrs, sizeof ptrs);
+    for (auto& b : c->rec_i32) key = fnv(key, &b.p, sizeof b.p);
+    const int32_t shape[6] = {c->tile_width, c->warps, c->packed, batched, (int32_t)c->event_cap, c->cand_cap};
+    key = fnv(key, shape, sizeof shape);
+    key = fnv(key, &c->pool_cap, sizeof c->pool_cap);
+    key = fnv(key, &c->spool_cap, sizeof c->spool_cap);
+    const bool replay = c->use_graph && batched && c->graph_exec && key == c->graph_key;
+    const bool capture = c->use_graph && batched && !replay && attempt == 0 && c->graph_key == key + 1;
     c->walk_ms = 0;
-    if (batched || n_regions == 1) {
-      CK(cudaEventRecord(c->w0, st));
-      run_range(c, plan, 0, n_regions, dp);
-      CK(cudaEventRecord(c->w1, st));
+    CK(cudaEventRecord(c->e0, st));
+    if (replay) {
+      CK(cudaGraphLaunch(c->graph_exec, st));
+      c->graph_replays++;
     } else {
-      CK(cudaEventRecord(c->w0, st));
-      for (int32_t r = 0; r < n_regions; r++) run_range(c, plan, r, r + 1, dp);
-      CK(cudaEventRecord(c->w1, st));
+      if (capture) CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      c->capturing = capture;
+      c->launches = 0;
+      c->n_runs = 0;
+      cudaMemcpyAsync(c->regions.p, c->staging_host, b_reg, cudaMemcpyHostToDevice, st);
+      if (b_walk) cudaMemcpyAsync(c->walk_tiles.p, (char*)c->staging_host + b_reg, b_walk, cudaMemcpyHostToDevice, st);
+      cudaMemcpyAsync(c->call_tile_region.p, (char*)c->staging_host + b_reg + b_walk, b_call, cudaMemcpyHostToDevice,
+                      st);
+      if (b_ch) cudaMemcpyAsync(c->chunks.p, (char*)c->staging_host + b_reg + b_walk + b_call, b_ch,
+                                cudaMemcpyHostToDevice, st);
+      cudaMemsetAsync(c->stats.p, 0, sizeof(StatsDev) * n_regions, st);
+      cudaMemsetAsync(c->counters.p, 0, sizeof(unsigned long long) * CNT_N, st);
+      cudaMemsetAsync(c->run_max.p, 0, sizeof(unsigned long long) * 2, st);
+      if (batched || n_regions == 1) {
+        run_range(c, plan, 0, n_regions, dp);
+      } else {
+        for (int32_t r = 0; r < n_regions; r++) run_range(c, plan, r, r + 1, dp);
+      }
+      c->capturing = false;
+      if (capture) {
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (e != cudaSuccess || !g) return fail(c, PG_ERR_CUDA, "stream capture failed: %s", cudaGetErrorString(e));
+        if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+        if (c->graph) cudaGraphDestroy(c->graph);
+        c->graph = g;
+        c->graph_exec = nullptr;
+        CK(cudaGraphInstantiate(&c->graph_exec, g, 0));
+        CK(cudaGraphLaunch(c->graph_exec, st));
+        c->graph_key = key;
+      } else if (batched && c->use_graph && attempt == 0 && !replay) {
+        c->graph_key = key + 1;  // the next identical call records the graph
+      }
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(c->e1, st));
@@ -549,11 +601,11 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
     CK(cudaMemcpyAsync(hm, c->run_max.p, sizeof hm, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     float ms = 0;
-    cudaEventElapsedTime(&ms, c->e0, c->e1);
+    CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
     c->total_ms = ms;
     c->walk_ms = 0;
     for (int32_t k = 0; k < c->n_runs; k++) {
-      cudaEventElapsedTime(&ms, c->wev[2 * k], c->wev[2 * k + 1]);
+      CK(cudaEventElapsedTime(&ms, c->wev[2 * k], c->wev[2 * k + 1]));
       c->walk_ms += ms;
     }
     bool grow = false;

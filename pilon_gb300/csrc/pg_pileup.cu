@@ -463,14 +463,20 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
 template <int T, int MINB, int G>
 static void launch_walk_t(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s) {
   const size_t smem = (size_t)12 * T * sizeof(uint32_t);
+  // attribute and occupancy are queried once per (kernel, warps): the first
+  // launch of a shape is never inside a stream capture
   static bool configured = false;
+  static int per_sm_of[17] = {0};
   if (!configured) {
     cudaFuncSetAttribute(k_walk<T, MINB, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     configured = true;
   }
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<T, MINB, G>, warps * 32, smem);
-  per_sm = std::max(per_sm, 1);
+  if (!per_sm_of[warps]) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<T, MINB, G>, warps * 32, smem);
+    per_sm_of[warps] = std::max(per_sm, 1);
+  }
+  const int per_sm = per_sm_of[warps];
   const int blocks = std::min(tile_count, 152 * per_sm);
   k_walk<T, MINB, G><<<blocks, warps * 32, smem, s>>>(a, tile_begin, tile_begin + tile_count);
 }

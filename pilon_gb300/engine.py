@@ -77,12 +77,13 @@ class RegionArrays:
 
     def out_struct(self, ins_cap):
         o = _abi.pg_region_out()
-        o.count = self.count.ctypes.data
-        o.qual_sum = self.qual_sum.ctypes.data
+        ptr = lambda a: a.ctypes.data if a is not None else None
+        o.count = ptr(self.count)
+        o.qual_sum = ptr(self.qual_sum)
         for f in self.I32:
-            setattr(o, f, getattr(self, f).ctypes.data)
-        o.call = self.call.ctypes.data
-        o.score = self.score.ctypes.data
+            setattr(o, f, ptr(getattr(self, f)))
+        o.call = ptr(self.call)
+        o.score = ptr(self.score)
         if self.ins_chars.size < ins_cap:
             self.ins_chars = np.zeros(ins_cap, np.uint8)
         o.ins_chars = self.ins_chars.ctypes.data if self.ins_chars.size else None

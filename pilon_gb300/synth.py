@@ -201,11 +201,16 @@ class Dataset:
     variants: list         # per contig
 
 
-def generate(cfg_or_workload, scale=1.0):
+def generate(cfg_or_workload, scale=1.0, threads=None):
+    """The workload's reference, planted variants and coordinate-sorted reads.
+    Contigs are simulated concurrently; every contig has its own seed, so the
+    result does not depend on the thread count."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
     w = workload(cfg_or_workload, scale) if isinstance(cfg_or_workload, int) else cfg_or_workload
     rng = np.random.Generator(np.random.PCG64(w.seed))
     total = sum(w.contig_lengths)
-    names, contigs, stores, variants = [], [], [], []
+    names, contigs, jobs, variants = [], [], [], []
     for ci, ln in enumerate(w.contig_lengths):
         ref = random_reference(rng, ln, w.gc)
         rmask = add_repeats(rng, ref, w.repeat_frac) if w.repeat_frac > 0 else None
@@ -219,11 +224,16 @@ def generate(cfg_or_workload, scale=1.0):
             ni = int(round(w.n_indels * ln / total))
             sample, s2r, var = plant_variants(rng, ref, ns, ni, w.indel_len)
         seed = int(rng.integers(0, 2**63 - 1))
-        st = simulate_contig(sample, s2r, ln, w, ci, seed, rmask)
+        jobs.append((sample, s2r, ln, ci, seed, rmask))
         names.append(f"contig{ci + 1}" if len(w.contig_lengths) > 1 else "chr1")
         contigs.append(ref)
-        stores.append(st)
         variants.append(var)
+    nt = threads or min(len(jobs), os.cpu_count() or 1)
+    if nt > 1 and len(jobs) > 1:
+        with ThreadPoolExecutor(nt) as ex:
+            stores = list(ex.map(lambda j: simulate_contig(j[0], j[1], j[2], w, j[3], j[4], j[5]), jobs))
+    else:
+        stores = [simulate_contig(j[0], j[1], j[2], w, j[3], j[4], j[5]) for j in jobs]
     reads = stores[0] if len(stores) == 1 else concat_stores(stores)
     return Dataset(w, names, contigs, reads, variants)
 

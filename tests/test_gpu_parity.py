@@ -82,3 +82,23 @@ def test_high_coverage_multi_pass(engine):
     w.coverage = 2000.0
     ds = synth.generate(w)
     run_both(engine, ds, _abi.default_params(), plan(ds))
+
+
+def test_graph_replay_bit_exact(engine, cfg1):
+    """The batched path records a CUDA graph on the second identical call and
+    replays it afterwards; every replay must give the same results, also after
+    a different plan ran in between."""
+    p = _abi.default_params()
+    a = plan(cfg1, chunk_size=9000)
+    b = plan(cfg1, chunk_size=13000)
+    engine.set_reference(cfg1.contigs)
+    engine.set_reads(cfg1.reads)
+    ora = oracle_regions(cfg1, p, a)
+    for k in range(4):
+        engine.pileup_regions(a, p, batched=True)
+        for r in range(len(a)):
+            compare_region(engine.fetch(r), ora[r], label=f"call {k} region {r}")
+    engine.pileup_regions(b, p, batched=True)
+    engine.pileup_regions(a, p, batched=True)
+    for r in range(len(a)):
+        compare_region(engine.fetch(r), ora[r], label=f"after switch region {r}")
