@@ -77,7 +77,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "20"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.p = None
@@ -238,6 +238,65 @@ def max_over_ranks(dist, v):
     return float(t.item())
 
 
+def serve_bench(args, dist, rank, ws, local, params):
+    """Workload 5: Poisson arrivals (lambda = 200/s) of region-polish requests of
+    10 kb - 1 Mb (log-uniform) against a device-resident read store of the
+    many-contig workload; continuous batching vs the plain per-request path."""
+    from pilon_gb300 import synth
+    from pilon_gb300.serve import Server, poisson_requests, run_load
+    ds = synth.generate(3, args.scale)
+    lens = [c.size for c in ds.contigs]
+    sched = poisson_requests(lens, rate=args.rate, duration=args.duration)
+    m = ds.reads.aligned_bases()
+    from pilon_gb300.regions import ReadIndex
+    idx = ReadIndex(ds.reads, len(ds.contigs))
+
+    def summary(res, wall, label, server):
+        ok = [r for r in res if not isinstance(r, Exception)]
+        lat = np.array([r.latency for r in ok]) * 1e3
+        units = 0
+        for _, q in sched:
+            a, b = idx.range_for(q.contig, q.start, q.stop, lens[q.contig])
+            units += int(m[a:b].sum())
+        return {"path": label, "requests": len(res), "failed_like_reference": len(res) - len(ok),
+                "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                "throughput_req_s": len(res) / wall, "gbases_per_s": units / wall / 1e9, "wall_s": wall,
+                "batches": server.batches}
+    out = {}
+    srv = Server(ds.names, ds.contigs, ds.reads, params, n_workers=args.workers, device=local)
+    try:
+        run_load(srv, poisson_requests(lens, rate=args.rate, duration=min(1.0, args.duration), seed=99))  # warm-up
+        srv.batches = 0
+        res, wall = run_load(srv, sched)
+        out["batched"] = summary(res, wall, f"continuous batching, {args.workers} contexts", srv)
+    finally:
+        srv.close()
+    plain = Server(ds.names, ds.contigs, ds.reads, params, n_workers=1, budget_positions=1, batched=False,
+                   device=local)
+    try:
+        run_load(plain, poisson_requests(lens, rate=args.rate, duration=min(1.0, args.duration), seed=99))
+        plain.batches = 0
+        pres, pwall = run_load(plain, sched)
+        out["plain"] = summary(pres, pwall, "one request at a time, per-region launches", plain)
+    finally:
+        plain.close()
+    same = all((isinstance(a, Exception) and isinstance(b, Exception)) or
+               (not isinstance(a, Exception) and not isinstance(b, Exception) and a.fasta == b.fasta and
+                a.changes == b.changes and a.vcf == b.vcf) for a, b in zip(res, pres))
+    if rank != 0:
+        return
+    b = out["batched"]
+    line = {"metric": "served-region latency p99 (ms) at lambda = %g/s" % args.rate, "value": b["p99_ms"],
+            "unit": "ms", "higher_is_better": False, "n_gpus": ws, "steps": len(sched), "warmup": 1,
+            "ms_per_step": b["mean_ms"], "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64",
+            "data": "synthetic (seeded)", "config": {"workload": "serving over draft-3000-contigs-40x",
+            "genome_bp": int(sum(lens)), "reads": ds.reads.n_reads, "rate_per_s": args.rate,
+            "duration_s": args.duration, "request_bp": "10 kb - 1 Mb log-uniform"},
+            "served": out, "identical_outputs_batched_vs_plain": same}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -255,6 +314,9 @@ def main():
     ap.add_argument("--compare-plain", type=int, default=-1, help="also time the per-region path (default: on "
                     "when there is more than one region)")
     ap.add_argument("--e2e-fields", default="auto", help="all | calls: what the end-to-end step reads back")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: requests per second")
+    ap.add_argument("--duration", type=float, default=10.0, help="serving: seconds of arrivals")
+    ap.add_argument("--workers", type=int, default=2, help="serving: engine contexts")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -291,6 +353,9 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.config == 5:
+        return serve_bench(args, dist, rank, ws, local, params)
+
     from pilon_gb300.engine import Engine
     ds = synth.generate(args.config, args.scale)
     lens = [c.size for c in ds.contigs]
@@ -312,6 +377,7 @@ def main():
                   "table": table}
     clk = ClockSampler(local)
     clk.__enter__()  # sampled from warm-up start to the end of the timed region
+    time.sleep(0.3)  # let nvidia-smi start sampling
     for _ in range(args.warmup):
         eng.pileup_regions(regions, params, batched=bool(args.batched))
     barrier(dist)

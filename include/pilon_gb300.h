@@ -208,7 +208,9 @@ pg_status pg_set_reads_device(pg_ctx *ctx, const pg_reads *device_reads);
  * pass 1 of GenomeRegion.postProcess (S/GenomeRegion.scala:214-272), including
  * the deletion-span update of later pileups.  `batched` = 0 launches the
  * kernels once per region (the plain path); 1 runs all regions in one
- * persistent launch per kernel. */
+ * persistent launch per kernel.  PG_ERR_INDEX reports regions on which the
+ * reference would throw; their pg_region_stats.error is set and the results
+ * of all other regions remain available. */
 pg_status pg_pileup_regions(pg_ctx *ctx, const pg_region *regions, int32_t n_regions,
                             const pg_params *params, int32_t batched);
 
@@ -237,9 +239,10 @@ pg_status pg_kmer_tally(pg_ctx *ctx, const pg_window *windows, int32_t n_windows
  * last pg_pileup_regions call, formatted on the device.  `name` is the
  * contig name.  The text (no header, no <DUP> or reassembly records) is
  * copied into `out` when it fits in `cap` bytes; *n_bytes receives its size
- * either way (PG_ERR_LIMIT when it does not fit). */
+ * either way (PG_ERR_LIMIT when it does not fit).  variants_only = 1 keeps
+ * only records whose ALT is not "." (a delta for serving). */
 pg_status pg_format_vcf(pg_ctx *ctx, int32_t region, const char *name, int32_t diploid, int32_t vcf_qe,
-                        char *out, int64_t cap, int64_t *n_bytes);
+                        int32_t variants_only, char *out, int64_t cap, int64_t *n_bytes);
 
 /* ---- timing -------------------------------------------------------------
  * Milliseconds of the dominant (pileup walk) kernel in the last

@@ -614,11 +614,11 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
     if ((int64_t)hc[CNT_POOL] > c->pool_cap) { c->pool_cap = (int64_t)hc[CNT_POOL] * 2 + 4096; grow = true; }
     if ((int64_t)hc[CNT_SPOOL_MAX] > c->spool_cap) { c->spool_cap = (int64_t)hc[CNT_SPOOL_MAX] * 2 + 4096; grow = true; }
     if (!grow) {
+      c->have_results = true;  // regions without an error keep valid results
       for (int32_t r = 0; r < n_regions; r++)
         if (c->stats_h[r].error)
           return fail(c, PG_ERR_INDEX, "region %d: an indel left shift left the region (the reference throws "
-                      "ArrayIndexOutOfBoundsException here)", r);
-      c->have_results = true;
+                      "ArrayIndexOutOfBoundsException here); pg_region_stats.error marks every such region", r);
       return PG_OK;
     }
   }
@@ -802,8 +802,8 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
   return PG_OK;
 }
 
-pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid, int32_t vcf_qe, char* out,
-                        int64_t cap, int64_t* n_bytes) {
+pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid, int32_t vcf_qe,
+                        int32_t variants_only, char* out, int64_t cap, int64_t* n_bytes) {
   if (!c || !name || !n_bytes || cap < 0) return fail(c, PG_ERR_ARG, "bad arguments");
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
   if (r < 0 || r >= c->n_regions) return fail(c, PG_ERR_ARG, "region %d out of range", r);
@@ -827,6 +827,7 @@ pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid,
   A.min_depth = c->stats_h[r].min_depth;
   A.diploid = diploid;
   A.vcf_qe = vcf_qe;
+  A.variants_only = variants_only;
   launch_vcf_lengths(A, P<int64_t>(c->vlen), st);
   launch_scan64(P<int64_t>(c->vlen), n, P<int64_t>(c->vsums), st);
   int64_t total = 0;

@@ -145,6 +145,7 @@ __device__ void vcf_record(Out& o, const FormatArgs& A, const PosView& v, int32_
   bool dot = false;
   if (clen == 1 && c0 == 'N') dot = true;
   if (clen == 1 && rlen == 1 && c0 == r0) dot = true;
+  if (A.variants_only && dot) return;  // deltas: only records with an alternate allele
   // line
   o.bytes((const uint8_t*)A.name, A.name_len);
   o.c('\t');

@@ -14,6 +14,7 @@ struct FormatArgs {
   int32_t min_depth;     // GenomeRegion.minDepth
   int32_t diploid;       // --diploid
   int32_t vcf_qe;        // --vcfqe
+  int32_t variants_only; // skip records whose ALT is "."
 };
 
 void launch_vcf_lengths(const FormatArgs& A, int64_t* len, cudaStream_t s);

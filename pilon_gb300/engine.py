@@ -49,7 +49,7 @@ def lib():
             "pg_last_kernel_ms": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_int32)]),
             "pg_sync": (C.c_int, [vp]),
-            "pg_format_vcf": (C.c_int, [vp, i32, C.c_char_p, i32, i32, vp, i64, C.POINTER(C.c_int64)]),
+            "pg_format_vcf": (C.c_int, [vp, i32, C.c_char_p, i32, i32, i32, vp, i64, C.POINTER(C.c_int64)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -184,16 +184,22 @@ class Engine:
                 return edges[:n.value]
             cap = int(n.value)
 
-    def format_vcf(self, r, name, diploid=False, vcf_qe=False):
+    def format_vcf(self, r, name, diploid=False, vcf_qe=False, variants_only=False):
         """The region's VCF records as bytes (pg_format_vcf)."""
         n = C.c_int64()
-        st = self.L.pg_format_vcf(self.h, r, name.encode(), int(diploid), int(vcf_qe), None, 0, C.byref(n))
+        args = (self.h, r, name.encode(), int(diploid), int(vcf_qe), int(variants_only))
+        st = self.L.pg_format_vcf(*args, None, 0, C.byref(n))
         if st not in (0, _abi.PG_ERR_LIMIT):
             self._check(st)
         buf = np.empty(max(int(n.value), 1), np.uint8)
-        self._check(self.L.pg_format_vcf(self.h, r, name.encode(), int(diploid), int(vcf_qe), buf.ctypes.data,
-                                         buf.size, C.byref(n)))
+        self._check(self.L.pg_format_vcf(*args, buf.ctypes.data, buf.size, C.byref(n)))
         return buf[:n.value].tobytes()
+
+    def set_reads_device(self, dev_reads, n_reads):
+        """pg_set_reads_device: a read store already in device memory (pg_reads
+        with device pointers), shared by several contexts."""
+        self._check(self.L.pg_set_reads_device(self.h, C.byref(dev_reads)))
+        self.n_reads = n_reads
 
     def last_kernel_ms(self):
         w, t, n = C.c_double(), C.c_double(), C.c_int32()
