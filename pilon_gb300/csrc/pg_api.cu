@@ -36,7 +36,7 @@ struct pg_ctx {
   bool have_reads = false;
   DevBuf rd[15];
   ReadExtent ext{};
-  DevBuf d_ext;
+  DevBuf d_ext, rdesc;
   // per-call buffers
   DevBuf regions, walk_tiles, call_tile_region, chunks, stats;
   DevBuf rec_count, rec_qsum, rec_i32[10], rec_call, rec_score, rec_indel_len, rec_ins_str, rec_ev_end;
@@ -223,7 +223,7 @@ void pg_close(pg_ctx* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
   }
-  DevBuf* all[] = {&c->ref, &c->d_ext, &c->regions, &c->walk_tiles, &c->call_tile_region, &c->chunks, &c->stats,
+  DevBuf* all[] = {&c->ref, &c->d_ext, &c->rdesc, &c->regions, &c->walk_tiles, &c->call_tile_region, &c->chunks, &c->stats,
                    &c->rec_count, &c->rec_qsum, &c->rec_call, &c->rec_score, &c->rec_indel_len, &c->rec_ins_str,
                    &c->rec_ev_end, &c->cand_count, &c->cand_off, &c->tile_sums,
                    &c->events, &c->events_sorted, &c->cands, &c->pool, &c->counters, &c->run_max, &c->staging_dev,
@@ -298,7 +298,10 @@ static pg_status finish_reads(pg_ctx* c) {
   c->have_reads = false;
   pg_status s = ensure(c, c->d_ext, sizeof(ReadExtent));
   if (s) return s;
-  launch_read_extent(c->R, P<ReadExtent>(c->d_ext), c->stream);
+  s = ensure(c, c->rdesc, (size_t)std::max<int64_t>(c->R.n, 1) * 2 * sizeof(int4));
+  if (s) return s;
+  c->R.desc = P<int4>(c->rdesc);
+  launch_read_extent(c->R, P<ReadExtent>(c->d_ext), P<int4>(c->rdesc), c->stream);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(&c->ext, c->d_ext.p, sizeof(ReadExtent), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));

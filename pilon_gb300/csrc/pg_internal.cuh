@@ -33,7 +33,16 @@ struct Reads {  // device pointers of the read store
   const int64_t *cigar_off, *seq_off, *qual_off;
   const uint32_t *cigar;
   int64_t n_cigar_words, seq_bytes, qual_bytes;
+  // Per-read walk descriptor, two int4 per read, made once per read store by
+  // k_read_extent (everything of PileUpRegion.addRead's setup that does not
+  // depend on the region or the options):
+  //   d0 = {pos, end (alignment end, or pos when unmapped), ref_id, adjMq + 1}
+  //   d1 = {lead | trail << 16, mlen | hasQual << 30 | simple << 31,
+  //         (pos - first touched position) | pairOk << 30, last touched position - pos}
+  // simple: the CIGAR is [H][S] M|=|X [S][H] with clips < 65536 and 0 <= adjMq <= 255.
+  const int4* desc;
 };
+constexpr uint32_t kDescHasQual = 1u << 30, kDescSimple = 1u << 31, kDescPairOk = 1u << 30;
 
 struct RegionDev {       // per region, device copy
   int32_t contig, start, stop, size;
@@ -117,7 +126,10 @@ struct DevParams {
 
 constexpr int kCallTile = 1024;     // positions per call / scan tile
 constexpr int kReadsPerChunk = 256;   // one read per thread of k_read_events
-constexpr int64_t kMaxReadsPerPass = 120000;  // keeps a tile's uint32 qual sums exact
+// Reads one walk pass adds to a tile.  At most 4095 reads per position keep the
+// packed shared counters exact: count (12 bits) + mq sum (20 bits) in one word,
+// and every qual * (mq + 1) sum within int32 for either sign of qual.
+constexpr int64_t kMaxReadsPerPass = 4095;
 
 // ---- Java integer helpers (wrapping Int, truncating division) -------------
 __host__ __device__ inline int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
@@ -375,7 +387,7 @@ struct CallArgs {
   int64_t pool_cap;
 };
 
-void launch_read_extent(const Reads& R, ReadExtent* out, cudaStream_t s);
+void launch_read_extent(const Reads& R, ReadExtent* out, int4* desc, cudaStream_t s);
 void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tiles, int32_t n_tiles,
                         const ReadExtent* ext, cudaStream_t s);
 void launch_walk(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s);

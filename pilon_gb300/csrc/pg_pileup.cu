@@ -40,7 +40,7 @@ __device__ inline bool in_window(int32_t pos, int32_t aend, uint16_t fl, const R
 // ---------------------------------------------------------------------------
 // Also validates the store: every read's CIGAR, bases and qualities must lie
 // inside their arrays, and positions must not decrease within a reference.
-__global__ void k_read_extent(Reads R, ReadExtent* out) {
+__global__ void k_read_extent(Reads R, ReadExtent* out, int4* desc) {
   int32_t lead = 0, back = 0;
   unsigned long long nid = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < R.n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -78,6 +78,48 @@ __global__ void k_read_extent(Reads R, ReadExtent* out) {
     }
     lead = max(lead, (int32_t)min((long long)(pos - lo), (long long)(1 << 30)));
     back = max(back, (int32_t)min((long long)(hi - pos), (long long)(1 << 30)));
+    // the walk descriptor (the shape tests of PileUpRegion.addRead's CIGAR walk,
+    // S/PileUpRegion.scala:139-145, with the same int32 arithmetic as the walk)
+    {
+      const uint16_t fl = R.flag[i];
+      const int32_t length = R.l_seq[i], mq = R.mapq[i];
+      int32_t clipped = 0, ld = 0, tr = 0, nM = 0, mlen = 0, wlo = pos, whi = pos - 1, r2 = 0, f2 = 0;
+      bool simple = true;
+      for (int k = 0; k < nc; k++) {
+        const uint32_t w = R.cigar[co + k];
+        const int32_t ln = (int32_t)(w >> 4);
+        const int op = (int)(w & 15u);
+        const int32_t locus = pos + f2;
+        if (op == 4) {
+          clipped += ln;
+          const int32_t cs = r2 == 0 ? locus - ln : locus;
+          wlo = min(wlo, cs);
+          whi = max(whi, cs + ln - 1);
+          if (nM == 0) { if (ld) simple = false; ld = ln; }
+          else { if (tr) simple = false; tr = ln; }
+        } else if (op == 0 || op == 7 || op == 8) {
+          if (nM || tr) simple = false;
+          nM++;
+          mlen = ln;
+          wlo = min(wlo, locus);
+          whi = max(whi, locus + ln - 1);
+        } else if (op != 5) {
+          simple = false;
+        }
+        if (consumes_read(op)) r2 += ln;
+        if (consumes_ref(op)) f2 += ln;
+      }
+      const int32_t adjMq = roundDivI(wmul(mq, length - clipped), length);
+      if (nM == 0 || ld > 0xffff || tr > 0xffff || adjMq < 0 || adjMq > 255 || mlen >= (1 << 30)) simple = false;
+      const bool hasQual = length > 0 && R.qual[R.qual_off[i]] != 0xFF;
+      const bool pairOk = !(fl & 0x1) || ((fl & 0x2) && R.ref_id[i] == R.mate_ref_id[i]);
+      const int32_t lrel = (int32_t)min((long long)pos - wlo, (long long)((1 << 30) - 1));
+      desc[2 * i] = make_int4(pos, (fl & 0x4) ? pos : R.aend[i], R.ref_id[i], adjMq + 1);
+      desc[2 * i + 1] = make_int4(
+          simple ? (int32_t)((uint32_t)ld | ((uint32_t)tr << 16)) : 0,
+          (int32_t)((simple ? (uint32_t)mlen : 0u) | (hasQual ? kDescHasQual : 0u) | (simple ? kDescSimple : 0u)),
+          (int32_t)((uint32_t)lrel | (pairOk ? kDescPairOk : 0u)), whi - pos);
+    }
   }
   lead = __reduce_max_sync(FULL, lead);
   back = __reduce_max_sync(FULL, back);
@@ -89,11 +131,11 @@ __global__ void k_read_extent(Reads R, ReadExtent* out) {
   }
 }
 
-void launch_read_extent(const Reads& R, ReadExtent* out, cudaStream_t s) {
+void launch_read_extent(const Reads& R, ReadExtent* out, int4* desc, cudaStream_t s) {
   cudaMemsetAsync(out, 0, sizeof(ReadExtent), s);
   if (R.n == 0) return;
   int blocks = (int)std::min<int64_t>((R.n + 255) / 256, 152 * 16);
-  k_read_extent<<<blocks, 256, 0, s>>>(R, out);
+  k_read_extent<<<blocks, 256, 0, s>>>(R, out, desc);
 }
 
 // ---------------------------------------------------------------------------
@@ -128,10 +170,11 @@ void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tile
 // parameter, so every counter address is one register plus an immediate) and
 // keeps its counters in shared memory, field-major so that lanes walking
 // consecutive bases of one read hit different banks:
-//   cnt[4][T] | qs[4][T] | mq[T] | q[T] | bad[T] | clips[T]     (uint32)
-// qs fits uint32 exactly while a pass adds at most kMaxReadsPerPass reads of
-// qual <= 127 and mq + 1 <= 256 to one position; tiles with more reads run
-// several passes and add each pass's sums into the records.
+//   cm[4][T] | qs[4][T] | q[T] | bad[T] | clips[T]     (uint32, 44 B per position)
+// cm[b] = count of base b + (sum of mq + 1 over those bases) << 12, qs[b] = sum of
+// qual * (mq + 1), q = sum of qual.  These stay exact while a pass adds at most
+// kMaxReadsPerPass reads to a position; tiles with more reads run several passes
+// and add each pass's sums into the records.
 //
 // Each warp takes the tile's reads 32 at a time.  Every lane first builds the
 // descriptor of one read in registers: the filters of BamFile.process, the
@@ -142,8 +185,6 @@ void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tile
 // reads G lanes per read (32 / G reads at once), reading the descriptors by
 // warp shuffle; the few other reads take the general CIGAR loop with the
 // whole warp.  No block-wide barrier runs inside the read loop.
-constexpr int kUnroll = 5;
-
 __device__ inline uint32_t nib_at(const uint8_t* seq, int64_t so, int32_t k) {
   const uint8_t b = seq[so + (k >> 1)];
   return (k & 1) ? (b & 15u) : (uint32_t)(b >> 4);
@@ -155,10 +196,9 @@ __device__ inline void add_base(uint32_t* sm, int32_t p, uint32_t nib, int32_t q
   const uint32_t bi = (0x30210u >> (2 * nib)) & 3u;
   if (((0x116u >> nib) & 1u) && qual >= min_qual) {
     uint32_t* c = sm + p + bi * T;
-    atomicAdd(c, 1u);
+    atomicAdd(c, 1u + (mq1 << 12));
     atomicAdd(c + 4 * T, (uint32_t)qual * mq1);
-    atomicAdd(sm + 8 * T + p, mq1);
-    atomicAdd(sm + 9 * T + p, (uint32_t)qual);
+    atomicAdd(sm + 8 * T + p, (uint32_t)qual);
   }
 }
 
@@ -175,10 +215,11 @@ enum : uint32_t { kSkip = 0, kFast = 1, kInvalid = 2, kSlow = 3, kComplex = 4 };
 // (2: up to 64 registers per thread).  G: lanes per simple read (8, 16, 32).
 template <int T, int MINB, int G>
 __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_begin, int32_t tile_end) {
-  extern __shared__ __align__(16) uint32_t sm[];
+  extern __shared__ __align__(16) uint32_t sm_raw[];
+  uint32_t* sm = sm_raw + 4;  // 4 words of padding in front of the counters
   __shared__ unsigned long long s_bc;
-  uint32_t* s_bad = sm + 10 * T;
-  uint32_t* s_clip = sm + 11 * T;
+  uint32_t* s_bad = sm + 9 * T;
+  uint32_t* s_clip = sm + 10 * T;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int gl = lane % G, grp = lane / G;
   constexpr int NG = 32 / G;
@@ -195,91 +236,80 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
 
     for (int64_t c0 = tile.read_lo, pass = 0; pass == 0 || c0 < tile.read_hi; c0 += kMaxReadsPerPass, pass++) {
       const int64_t c1 = min(c0 + kMaxReadsPerPass, tile.read_hi);
-      for (int k = threadIdx.x; k < 12 * T; k += blockDim.x) sm[k] = 0;
+      for (int k = threadIdx.x; k < 11 * T + 4; k += blockDim.x) sm_raw[k] = 0;
       __syncthreads();
 
       for (int64_t base = c0 + 32 * (int64_t)warp; base < c1; base += 32 * (int64_t)nwarps) {
         // ---- one descriptor per lane
         const int64_t i = base + lane;
         uint32_t kind = kSkip, mq1 = 0, clip = 0;   // clip: lead | trail << 16
-        int32_t i0 = 0, i1 = 0, pb = 0, mlen = 0, pos = 0, nc = 0, length = 0;
+        int32_t i0 = 0, i1 = 0, pb = 0, mlen = 0, pos = 0, nc = 0, length = 0, cls = 0;
         bool valid = false, hasQual = false;
         const uint8_t* qp = nullptr;
         const uint8_t* sp = nullptr;
         int64_t co = 0;
         if (i < c1) {
-          pos = R.pos[i];
+          // every load of the descriptor phase is independent of the others
+          const int4 d0 = R.desc[2 * i], d1 = R.desc[2 * i + 1];
           const uint16_t fl = R.flag[i];
-          if (R.ref_id[i] == g.contig && in_window(pos, R.aend[i], fl, g) && validate_read(fl, P)) {
-            length = R.l_seq[i];
-            const int32_t mq = R.mapq[i];
-            const bool paired = fl & 0x1;
-            valid = (mq >= P.min_mq) && (!paired || ((fl & 0x2) && R.ref_id[i] == R.mate_ref_id[i]));
-            co = R.cigar_off[i];
-            nc = R.n_cigar[i];
-            int32_t clipped = 0, lead = 0, trail = 0, nM = 0;
-            bool simple = true;
-            int32_t lo = pos, hi = pos - 1, ro = 0, fo = 0;
-            for (int k2 = 0; k2 < nc; k2++) {
-              const uint32_t w = R.cigar[co + k2];
-              const int32_t ln = (int32_t)(w >> 4);
-              const int op = (int)(w & 15u);
-              const int32_t locus = pos + fo;
-              if (op == 4) {
-                clipped += ln;
-                const int32_t cs = ro == 0 ? locus - ln : locus;
-                lo = min(lo, cs);
-                hi = max(hi, cs + ln - 1);
-                if (nM == 0) { if (lead) simple = false; lead = ln; }
-                else { if (trail) simple = false; trail = ln; }
-              } else if (op == 0 || op == 7 || op == 8) {
-                if (nM || trail) simple = false;
-                nM++;
-                mlen = ln;
-                lo = min(lo, locus);
-                hi = max(hi, locus + ln - 1);
-              } else if (op != 5) {
-                simple = false;  // I, D, N, P: general path (I and D go to k_read_events)
-              }
-              if (consumes_read(op)) ro += ln;
-              if (consumes_ref(op)) fo += ln;
-            }
-            if (nM == 0 || lead > 0xffff || trail > 0xffff) simple = false;
+          const int32_t mq = R.mapq[i];
+          const int64_t qo = R.qual_off[i], so = R.seq_off[i];
+          pos = d0.x;
+          if (d0.z == g.contig && pos <= g.qe && d0.y >= g.qs && validate_read(fl, P)) {
+            valid = (mq >= P.min_mq) && ((uint32_t)d1.z & kDescPairOk);
+            const int32_t lo = pos - (int32_t)((uint32_t)d1.z & (kDescPairOk - 1u)), hi = pos + d1.w;
             if (hi >= tileLo && lo <= tileHi) {
-              const int64_t qo = R.qual_off[i];
-              const int32_t adjMq = roundDivI(wmul(mq, length - clipped), length);
-              hasQual = length > 0 && R.qual[qo] != 0xFF;
-              mq1 = (uint32_t)(adjMq + 1);
-              const int64_t so = R.seq_off[i];
-              if (simple) {
+              hasQual = ((uint32_t)d1.y & kDescHasQual) != 0;
+              mq1 = (uint32_t)d0.w;
+              if ((uint32_t)d1.y & kDescSimple) {
+                const int32_t lead = d1.x & 0xffff, trail = (int32_t)((uint32_t)d1.x >> 16);
+                mlen = (int32_t)((uint32_t)d1.y & (kDescHasQual - 1u));
+                length = lead + mlen + trail;
                 // aligned bases at trusted read offsets [flank, length - flank), inside the tile
                 i0 = max(max(tileLo - pos, P.flank - lead), 0);
                 i1 = min(min(tileHi - pos + 1, length - P.flank - lead), mlen);
                 pb = pos - tileLo;
-                clip = (uint32_t)lead | ((uint32_t)trail << 16);
+                clip = (uint32_t)d1.x;
                 qp = R.qual + qo + lead;
                 sp = R.seq + so;
                 if (!valid) kind = kInvalid;
                 else if (hasQual && P.long_read != PG_NANOPORE) kind = kFast;
                 else kind = kSlow;
                 if (valid && i1 > i0) bc += (unsigned long long)(i1 - i0);
-                // keep the read offset of the first aligned base for the nibble parity
-                mlen |= (lead & 1) << 30;
+                // position residue (mod 4) of the read's 4-base chunks, which start at
+                // the aligned quality words (see the fast path)
+                cls = (pb + i0 - (int32_t)((uintptr_t)(qp + i0) & 3u)) & 3;
               } else {
                 kind = kComplex;
+                co = R.cigar_off[i];
+                nc = R.n_cigar[i];
+                length = R.l_seq[i];
                 qp = R.qual + qo;
                 sp = R.seq + so;
               }
             }
           }
         }
-        // ---- simple reads, 32 / G at a time, G lanes each
-        unsigned todo = __ballot_sync(FULL, kind != kSkip && kind != kComplex);
-        while (todo) {
-          // group grp takes the (grp+1)-th lowest set bit of todo
-          unsigned m = todo;
-          for (int k = 0; k < grp; k++) m &= m - 1;
-          const int src = m ? __ffs(m) - 1 : 32;  // 32: fewer reads than groups are left
+        // ---- simple reads, 32 / G at a time, G lanes each.  Group g takes a read of
+        // residue class g when one is left, so the 4 groups of a warp add to 4 different
+        // position residues at every step and their shared-memory atomics hit 32
+        // different banks.
+        const bool simple_kind = kind != kSkip && kind != kComplex;
+        unsigned cm0 = __ballot_sync(FULL, simple_kind && cls == 0), cm1 = __ballot_sync(FULL, simple_kind && cls == 1);
+        unsigned cm2 = __ballot_sync(FULL, simple_kind && cls == 2), cm3 = __ballot_sync(FULL, simple_kind && cls == 3);
+        while (cm0 | cm1 | cm2 | cm3) {
+          int src = 32;  // 32: fewer reads than groups are left
+#pragma unroll
+          for (int g2 = 0; g2 < NG; g2++) {
+            const unsigned pref = g2 == 0 ? cm0 : g2 == 1 ? cm1 : g2 == 2 ? cm2 : cm3;
+            const unsigned m = pref ? pref : (cm0 | cm1 | cm2 | cm3);
+            const unsigned bit = m & (0u - m);
+            if (g2 == grp) src = bit ? __ffs(bit) - 1 : 32;
+            cm0 &= ~bit;
+            cm1 &= ~bit;
+            cm2 &= ~bit;
+            cm3 &= ~bit;
+          }
           const int s2 = src < 32 ? src : lane;
           const uint32_t rk = __shfl_sync(FULL, kind, s2);
           const int32_t ri0 = __shfl_sync(FULL, i0, s2), ri1 = __shfl_sync(FULL, i1, s2);
@@ -287,14 +317,10 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
           const uint32_t rmq1 = __shfl_sync(FULL, mq1, s2), rclip = __shfl_sync(FULL, clip, s2);
           const uint8_t* rqp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)qp, s2);
           const uint8_t* rsp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)sp, s2);
-          // drop the reads taken by this round
-#pragma unroll
-          for (int k = 0; k < NG; k++)
-            if (todo) todo &= todo - 1;
           if (src < 32) {
             const int32_t lead = (int32_t)(rclip & 0xffffu), trail = (int32_t)(rclip >> 16);
             const int32_t rpos = rpb + tileLo;
-            const int32_t par = (rml >> 30) & 1, rmlen = rml & 0x3fffffff;
+            const int32_t rmlen = rml & 0x3fffffff;
             if (lead > 0) {  // clipStart = locus - len (clip at read offset 0), clipEnd = locus - 1
               const int32_t cs = rpos - lead, ce = rpos - 1;
               if (gl == 0) {
@@ -303,37 +329,68 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               }
               for (int32_t l = max(cs, tileLo) + gl; l <= min(ce, tileHi); l += G) atomicAdd(&s_bad[l - tileLo], 1u);
             }
-            if (rk == kFast) {
-              // per-lane pointers fixed once per read: every unrolled access is pointer + immediate
-              const int32_t x0 = ri0 + gl;
-              const uint8_t* ql = rqp + x0;
-              const uint8_t* sl = rsp + ((lead + x0) >> 1);
-              const uint32_t sh = (~(uint32_t)(par + x0) & 1u) << 2;  // nibble half: read offset lead + x0
-              uint32_t* cl = sm + (rpb + x0);
-              const int32_t nleft = ri1 - x0;
-              for (int32_t b0 = 0; b0 < ri1 - ri0; b0 += G * kUnroll) {
-                uint32_t qv[kUnroll], sv[kUnroll];
-#pragma unroll
-                for (int u = 0; u < kUnroll; u++) {
-                  const bool in = b0 + G * u < nleft;
-                  qv[u] = in ? (uint32_t)ql[b0 + G * u] : 0u;
-                  sv[u] = in ? (uint32_t)sl[(b0 + G * u) >> 1] : 0u;
+            if (rk == kFast && ri1 > ri0) {
+              // Chunks of 4 consecutive aligned bases; lane gl of the group takes chunks
+              // gl, gl + G, ... and loads the next one while it adds the current one.
+              // A chunk's qualities are one aligned 32-bit word (it holds at least one
+              // trusted quality of this read, so it never leaves the pages of the quality
+              // array); its nibbles come from at most 3 sequence bytes, loaded only inside
+              // the read's trusted bytes.
+              const uintptr_t qa = (uintptr_t)(rqp + ri0);
+              const int32_t xs = ri0 - (int32_t)(qa & 3u);  // x of byte 0 of chunk 0
+              const uint32_t* qw = (const uint32_t*)(qa & ~(uintptr_t)3);
+              const int32_t blo = (lead + ri0) >> 1;
+              const uint32_t nby = (uint32_t)(((lead + ri1 - 1) >> 1) - blo);  // trusted bytes blo .. blo + nby
+              const uint8_t* sb = rsp + blo;
+              const int32_t b0 = ((lead + xs) >> 1) - blo;   // first byte of chunk c: b0 + 2c
+              const uint32_t psh = 4u * (uint32_t)((lead + xs) & 1);  // chunks start on a low half-byte
+              const uint32_t amq = 1u + (rmq1 << 12);
+              int32_t c = gl;
+              bool more = xs + 4 * c < ri1;
+              uint32_t qv = 0, sv = 0;
+              if (more) {
+                const int32_t r = b0 + 2 * c;
+                qv = qw[c];
+                sv = ((uint32_t)r <= nby ? (uint32_t)sb[r] : 0u) |
+                     ((uint32_t)(r + 1) <= nby ? (uint32_t)sb[r + 1] << 8 : 0u) |
+                     ((uint32_t)(r + 2) <= nby ? (uint32_t)sb[r + 2] << 16 : 0u);
+              }
+              while (more) {
+                const int32_t cn = c + G;
+                const bool mn = xs + 4 * cn < ri1;
+                uint32_t qn = 0, sn = 0;
+                if (mn) {
+                  const int32_t r = b0 + 2 * cn;
+                  qn = qw[cn];
+                  sn = ((uint32_t)r <= nby ? (uint32_t)sb[r] : 0u) |
+                       ((uint32_t)(r + 1) <= nby ? (uint32_t)sb[r + 1] << 8 : 0u) |
+                       ((uint32_t)(r + 2) <= nby ? (uint32_t)sb[r + 2] << 16 : 0u);
                 }
+                const int32_t xf = xs + 4 * c;
+                // nibbles in read order (BAM puts the first of a byte in its high half),
+                // base j of the chunk at bits 4j; bases outside the trusted offsets
+                // [ri0, ri1) become nibble 0, which is not counted
+                uint32_t nb = (((sv >> 4) & 0x0F0F0Fu) | ((sv & 0x0F0F0Fu) << 4)) >> psh;
+                nb &= (0xFFFFu << (4 * max(ri0 - xf, 0))) & (0xFFFFu >> (4 * max(4 - (ri1 - xf), 0)));
+                uint32_t* cl = sm + (rpb + xf);
+                // Every base adds, a rejected one adds 0: no branch per base.  A rejected
+                // base may sit up to 3 positions outside the tile; the counters have 4
+                // words of padding in front and the fields behind absorb the rest.
 #pragma unroll
-                for (int u = 0; u < kUnroll; u++) {
-                  if (b0 + G * u < nleft) {
-                    const uint32_t nib = (sv[u] >> sh) & 15u;
-                    const int32_t qual = (int32_t)(int8_t)qv[u];
-                    const uint32_t bi = (0x30210u >> (2 * nib)) & 3u;
-                    if (((0x116u >> nib) & 1u) && qual >= P.min_qual) {
-                      uint32_t* c = cl + b0 + G * u;
-                      atomicAdd(c + bi * T, 1u);
-                      atomicAdd(c + bi * T + 4 * T, (uint32_t)qual * rmq1);
-                      atomicAdd(c + 8 * T, rmq1);
-                      atomicAdd(c + 9 * T, (uint32_t)qual);
-                    }
-                  }
+                for (int j = 0; j < 4; j++) {
+                  const uint32_t nib = (nb >> (4 * j)) & 15u;
+                  const int32_t qual = (int32_t)(int8_t)(qv >> (8 * j));
+                  const uint32_t bi = (0x30210u >> (2 * nib)) & 3u;
+                  const uint32_t ok = (0x116u >> nib) & (qual >= P.min_qual ? 1u : 0u);
+                  uint32_t* cp = cl + j + bi * T;
+                  atomicAdd(cp, amq * ok);
+                  atomicAdd(cp + 4 * T, (uint32_t)qual * rmq1 * ok);
+                  atomicAdd(cl + j + 8 * T, (uint32_t)qual * ok);
                 }
+                c = cn;
+                more = mn;
+                qv = qn;
+                sv = sn;
               }
             } else if (rk == kInvalid) {
               for (int32_t ii = ri0 + gl; ii < ri1; ii += G) atomicAdd(&s_bad[rpb + ii], 1u);
@@ -419,10 +476,13 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
       // flush: the first pass stores, later passes add (the CTA owns the tile)
       for (int32_t p = threadIdx.x; p < tile.len; p += blockDim.x) {
         const int64_t gp = g.pos_base + tile.lo + p;
-        const int4 c = make_int4((int)sm[p], (int)sm[T + p], (int)sm[2 * T + p], (int)sm[3 * T + p]);
-        const longlong2 q01 = make_longlong2((long long)sm[4 * T + p], (long long)sm[5 * T + p]);
-        const longlong2 q23 = make_longlong2((long long)sm[6 * T + p], (long long)sm[7 * T + p]);
-        const int32_t mqs = (int32_t)sm[8 * T + p], qsum = (int32_t)sm[9 * T + p];
+        const uint32_t m0 = sm[p], m1 = sm[T + p], m2 = sm[2 * T + p], m3 = sm[3 * T + p];
+        const int4 c = make_int4((int)(m0 & 0xFFFu), (int)(m1 & 0xFFFu), (int)(m2 & 0xFFFu), (int)(m3 & 0xFFFu));
+        const int32_t mqs = (int32_t)((m0 >> 12) + (m1 >> 12) + (m2 >> 12) + (m3 >> 12));
+        // per-pass qual sums fit int32 for either sign of qual (4095 reads x 128 x 256 < 2^31)
+        const longlong2 q01 = make_longlong2((int32_t)sm[4 * T + p], (int32_t)sm[5 * T + p]);
+        const longlong2 q23 = make_longlong2((int32_t)sm[6 * T + p], (int32_t)sm[7 * T + p]);
+        const int32_t qsum = (int32_t)sm[8 * T + p];
         if (pass == 0) {
           a.rec.count[gp] = c;
           a.rec.qual_sum[2 * gp] = q01;
@@ -462,7 +522,7 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
 
 template <int T, int MINB, int G>
 static void launch_walk_t(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s) {
-  const size_t smem = (size_t)12 * T * sizeof(uint32_t);
+  const size_t smem = (size_t)(11 * T + 4) * sizeof(uint32_t);
   // attribute and occupancy are queried once per (kernel, warps): the first
   // launch of a shape is never inside a stream capture
   static bool configured = false;
