@@ -215,6 +215,65 @@ def oracle_sample(ds, params, threads):
     return units, time.perf_counter() - t0, len(jobs)
 
 
+def kmer_bench(eng, ds, params, args, threads, K=31, radius=500):
+    """Workload 4: the K-mer tally of Assembler.addReads/buildGraph (pg_kmer_tally)
+    over one local-reassembly window per planted indel (the reads overlapping
+    [x - 500, x + 500]), on the GPU and on the oracle over all host threads for
+    a sample of windows, with the sample's edges compared."""
+    from oracle import oracle
+    from pilon_gb300.regions import ReadIndex
+    idx = ReadIndex(ds.reads, len(ds.contigs))
+    wins = []
+    for ci, var in enumerate(ds.variants):
+        n = ds.contigs[ci].size
+        for v in var:
+            wins.append(idx.range_for(ci, max(1, v[0] - radius), min(n, v[0] + radius), n, slop=0))
+    L = ds.reads.l_seq.astype(np.int64)
+    per = np.concatenate([[0], np.cumsum(2 * np.maximum(L - K, 0))])
+    events = int(sum(per[b] - per[a] for a, b in wins))
+    for _ in range(args.warmup):
+        edges = eng.kmer_tally(wins, K, params)
+    t = []
+    for _ in range(max(3, min(args.steps, 10))):
+        t0 = time.perf_counter()
+        edges = eng.kmer_tally(wins, K, params)
+        t.append(time.perf_counter() - t0)
+    sec = sum(t) / len(t)
+    out = {"windows": len(wins), "K": K, "kmer_events": events, "edges": int(len(edges)),
+           "ms_per_call": 1e3 * sec, "value": events / sec / 1e9, "unit": "G K-mer events/s",
+           "timing": "host wall clock of pg_kmer_tally, edges read back"}
+    if not args.no_cpu:
+        sample = wins[: max(1, min(len(wins), 16 * threads))]
+        parts = [sample[k::threads] for k in range(threads)]
+        res = [None] * threads
+
+        def worker(k):
+            res[k] = oracle.kmer_tally(ds.reads, params, parts[k], K) if parts[k] else None
+        t0 = time.perf_counter()
+        ths = [threading.Thread(target=worker, args=(k,)) for k in range(threads)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        csec = time.perf_counter() - t0
+        sev = int(sum(per[b] - per[a] for a, b in sample))
+        # the GPU edges of the sampled windows, against the oracle's
+        got = eng.kmer_tally(sample, K, params)
+
+        def edge_set(e, remap):
+            return {(remap(int(x["window"])), int(x["key_hi"]), int(x["key_lo"]), int(x["next"]), int(x["alt"]),
+                     int(x["depth"]), int(x["weight"])) for x in e}
+        want = set()
+        for k in range(threads):
+            if res[k] is not None:
+                want |= edge_set(res[k], lambda w, k=k: k + threads * w)
+        out["cpu_baseline"] = {"value": sev / csec / 1e9, "unit": "G K-mer events/s", "cores": threads,
+                               "kind": "port", "sample": f"{len(sample)} of {len(wins)} windows on {threads} host "
+                                                         f"threads"}
+        out["sample_edges_identical"] = edge_set(got, lambda w: w) == want
+    return out
+
+
 def dist_init():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws > 1:
@@ -445,6 +504,8 @@ def main():
                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / args.steps, "read_back": fields,
                "timing": "host wall clock; every call synchronises the engine stream"}
 
+    kmer = kmer_bench(eng, ds, params, args, threads) if args.config == 4 and rank == 0 else None
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         u, sec, njobs = oracle_sample(ds, params, threads)
@@ -473,6 +534,8 @@ def main():
         "e2e": e2e,
         "cpu_baseline": cpu,
     }
+    if kmer:
+        line["kmer_tally"] = kmer
     print(json.dumps(line))
 
 

@@ -63,7 +63,7 @@ def build(force=False, verbose=False):
             cmds.append([nvcc] + NVCC_FLAGS + ["-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj])
     synth_src = os.path.join(CSRC, "synth.cpp")
     if force or not _newer(SYNTH, [synth_src]):
-        cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", synth_src, "-o", SYNTH])
+        cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", synth_src, "-o", SYNTH])
     if cmds:
         if verbose:
             for c in cmds:

@@ -43,7 +43,7 @@ __device__ inline CallCtx make_ctx(const CallArgs& a, const RegionDev& g, int64_
 // 256 threads per CTA, kCallTile / 256 CTAs per call tile: a thread that runs
 // a long indel vote holds back only its own small CTA.
 constexpr int kCallThreads = 256;
-__global__ void __launch_bounds__(kCallThreads) k_call(CallArgs a, int32_t tile_begin) {
+__global__ void __launch_bounds__(kCallThreads, 6) k_call(CallArgs a, int32_t tile_begin) {
   const int32_t t = tile_begin + blockIdx.x / (kCallTile / kCallThreads);
   const int32_t r = a.call_tile_region[t];
   const RegionDev g = a.regions[r];

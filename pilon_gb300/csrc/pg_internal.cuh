@@ -39,7 +39,8 @@ struct Reads {  // device pointers of the read store
   //   d0 = {pos, end (alignment end, or pos when unmapped), ref_id, adjMq + 1}
   //   d1 = {lead | trail << 16, mlen | hasQual << 30 | simple << 31,
   //         (pos - first touched position) | pairOk << 30, last touched position - pos}
-  // simple: the CIGAR is [H][S] M|=|X [S][H] with clips < 65536 and 0 <= adjMq <= 255.
+  // simple: the CIGAR is [H][S] M|=|X [S][H] with clips < 65536 and 0 <= adjMq <= 255;
+  // a read that is not simple has d1.x = 1 when its CIGAR holds an I or D, else 0.
   const int4* desc;
 };
 constexpr uint32_t kDescHasQual = 1u << 30, kDescSimple = 1u << 31, kDescPairOk = 1u << 30;

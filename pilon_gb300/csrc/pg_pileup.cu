@@ -84,7 +84,7 @@ __global__ void k_read_extent(Reads R, ReadExtent* out, int4* desc) {
       const uint16_t fl = R.flag[i];
       const int32_t length = R.l_seq[i], mq = R.mapq[i];
       int32_t clipped = 0, ld = 0, tr = 0, nM = 0, mlen = 0, wlo = pos, whi = pos - 1, r2 = 0, f2 = 0;
-      bool simple = true;
+      bool simple = true, indel = false;
       for (int k = 0; k < nc; k++) {
         const uint32_t w = R.cigar[co + k];
         const int32_t ln = (int32_t)(w >> 4);
@@ -105,6 +105,7 @@ __global__ void k_read_extent(Reads R, ReadExtent* out, int4* desc) {
           whi = max(whi, locus + ln - 1);
         } else if (op != 5) {
           simple = false;
+          if (op == 1 || op == 2) indel = true;
         }
         if (consumes_read(op)) r2 += ln;
         if (consumes_ref(op)) f2 += ln;
@@ -116,7 +117,7 @@ __global__ void k_read_extent(Reads R, ReadExtent* out, int4* desc) {
       const int32_t lrel = (int32_t)min((long long)pos - wlo, (long long)((1 << 30) - 1));
       desc[2 * i] = make_int4(pos, (fl & 0x4) ? pos : R.aend[i], R.ref_id[i], adjMq + 1);
       desc[2 * i + 1] = make_int4(
-          simple ? (int32_t)((uint32_t)ld | ((uint32_t)tr << 16)) : 0,
+          simple ? (int32_t)((uint32_t)ld | ((uint32_t)tr << 16)) : (indel ? 1 : 0),
           (int32_t)((simple ? (uint32_t)mlen : 0u) | (hasQual ? kDescHasQual : 0u) | (simple ? kDescSimple : 0u)),
           (int32_t)((uint32_t)lrel | (pairOk ? kDescPairOk : 0u)), whi - pos);
     }
@@ -563,44 +564,42 @@ void launch_walk(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int 
 
 // ---------------------------------------------------------------------------
 // Per (region, read): readCount, insert statistics, physCovIncr and indels.
-__device__ inline int32_t read_qual(const Reads& R, int64_t i, int32_t k, bool hasQual, const DevParams& P) {
-  return hasQual ? (int32_t)(int8_t)R.qual[R.qual_off[i] + k] : P.default_qual;
-}
-
 __device__ inline unsigned long long warp_sum_u64(unsigned long long v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
   return v;
 }
 
-__global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_begin, int32_t chunk_end) {
-  __shared__ unsigned long long s_rc, s_bc, s_frc, s_frs, s_frq, s_rfc, s_rfs, s_rfq;
-  __shared__ int32_t s_pcs, s_iss, s_err;
+// kEvThreads threads per CTA, kReadsPerChunk / kEvThreads CTAs per read chunk,
+// one read per thread.  Each warp adds its partial sums into the chunk's
+// (zeroed) statistics with global atomics, so no warp waits for another: the
+// few reads with indels run long left-shift loops.
+constexpr int kEvThreads = 64;
+constexpr int kEvPerChunk = kReadsPerChunk / kEvThreads;
+
+__global__ void __launch_bounds__(kEvThreads, 12) k_read_events(EventArgs a, int32_t chunk_begin, int32_t chunk_end) {
   const Reads& R = a.R;
   const DevParams& P = a.P;
-  for (int32_t ch = chunk_begin + blockIdx.x; ch < chunk_end; ch += gridDim.x) {
+  for (int32_t bq = chunk_begin * kEvPerChunk + blockIdx.x; bq < chunk_end * kEvPerChunk; bq += gridDim.x) {
+    const int32_t ch = bq / kEvPerChunk;
     const ReadChunk C = a.chunks[ch];
     const RegionDev g = a.regions[C.region];
     const uint8_t* cref = a.ref + g.ref_off;
-    if (threadIdx.x == 0) {
-      s_rc = s_bc = s_frc = s_frs = s_frq = s_rfc = s_rfs = s_rfq = 0;
-      s_pcs = s_iss = s_err = 0;
-    }
-    __syncthreads();
-    // per-thread partial sums, reduced once per chunk
     unsigned long long rc_n = 0, bc_n = 0, frc = 0, frs = 0, frq = 0, rfc = 0, rfs = 0, rfq = 0;
     uint32_t pcs = 0, iss = 0;
     int32_t err = 0;
     auto inRegion = [&](int64_t l) { return l >= g.start && l <= g.stop; };
-    for (int64_t i = C.lo + threadIdx.x; i < C.hi; i += blockDim.x) {
-      const int32_t pos = R.pos[i], aend = R.aend[i];
+    for (int64_t i = C.lo + (int64_t)(bq % kEvPerChunk) * kEvThreads + threadIdx.x; i < C.hi;
+         i += (int64_t)kEvPerChunk * kEvThreads) {
+      // all loads of a read are independent: the per-store descriptor holds the CIGAR shape
+      const int4 d0 = R.desc[2 * i], d1 = R.desc[2 * i + 1];
+      const int32_t aend = R.aend[i], tlen = R.tlen[i];
       const uint16_t fl = R.flag[i];
-      if (R.ref_id[i] != g.contig || !in_window(pos, aend, fl, g) || !validate_read(fl, P)) continue;
-      rc_n++;
-      const int32_t length = R.l_seq[i];
       const int32_t mq = R.mapq[i];
+      const int32_t pos = d0.x;
+      if (d0.z != g.contig || !(pos <= g.qe && d0.y >= g.qs) || !validate_read(fl, P)) continue;
+      rc_n++;
       const bool paired = fl & 0x1;
-      const bool valid = (mq >= P.min_mq) && (!paired || ((fl & 0x2) && R.ref_id[i] == R.mate_ref_id[i]));
-      const int32_t tlen = R.tlen[i];
+      const bool valid = (mq >= P.min_mq) && ((uint32_t)d1.z & kDescPairOk);
 
       // physCovIncr (S/PileUpRegion.scala:62-88) and addInsert (S/BamFile.scala:194-202)
       int32_t insertSize = 0;
@@ -633,20 +632,20 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
       }
 
       // I and D operators (S/PileUpRegion.scala:150-183)
+      const bool anyIndel = !((uint32_t)d1.y & kDescSimple) && d1.x != 0;
+      if (!anyIndel || !valid) continue;
       const int64_t co = R.cigar_off[i];
       const int nc = R.n_cigar[i];
-      bool anyIndel = false;
-      int32_t clipped = 0;
-      for (int k = 0; k < nc; k++) {
-        uint32_t w = R.cigar[co + k];
-        int op = (int)(w & 15u);
-        if (op == 1 || op == 2) anyIndel = true;
-        if (op == 4) clipped += (int32_t)(w >> 4);
-      }
-      if (!anyIndel || !valid) continue;
-      const int32_t adjMq = roundDivI(wmul(mq, length - clipped), length);
+      const int32_t length = R.l_seq[i];
+      const uint8_t* rseq = R.seq + R.seq_off[i];   // loaded once per read
+      const uint8_t* rqual = R.qual + R.qual_off[i];
+      auto nib = [&](int32_t k) -> uint32_t {
+        const uint8_t b = rseq[k >> 1];
+        return (k & 1) ? (b & 15u) : (uint32_t)(b >> 4);
+      };
+      const int32_t adjMq = d0.w - 1;
       const int32_t indelMq = P.long_read > 0 ? min(adjMq, 8) : adjMq;
-      const bool hasQual = length > 0 && R.qual[R.qual_off[i]] != 0xFF;
+      const bool hasQual = ((uint32_t)d1.y & kDescHasQual) != 0;
       auto trusted = [&](int32_t off) { return off >= P.flank && length - P.flank > off; };
       auto refAt = [&](int64_t k, bool& bad) -> uint8_t {
         if (k < 0 || k >= g.contig_len) { bad = true; return 0; }
@@ -676,7 +675,7 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
             if (len - 1 < 0 || len - 1 >= avail) { bad = true; break; }
             int32_t kk = len - 1 - rot;  // last character of the rotated insertion
             if (kk < 0) kk += len;
-            if (rb != nib_char(read_nib(R, i, readOffset + kk))) break;
+            if (rb != nib_char(nib(readOffset + kk))) break;
             iloc -= 1;
             rot += 1;
             if (rot == len) rot = 0;
@@ -688,7 +687,7 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
           {
             const int64_t gp = g.pos_base + (iloc - g.start);
             atomicAdd(&a.rec.ins_qual[gp], indelMq + 1);
-            atomicAdd(&a.rec.q_sum[gp], read_qual(R, i, readOffset, hasQual, P));
+            atomicAdd(&a.rec.q_sum[gp], (hasQual ? (int32_t)(int8_t)rqual[readOffset] : P.default_qual));
             atomicAdd(&a.rec.insertions[gp], 1);
             unsigned long long slot = atomicAdd(a.n_events, 1ull);
             if ((int64_t)slot < a.event_cap) {
@@ -700,7 +699,7 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
               for (int32_t j = 0; j < min(len, 16); j++) {
                 int32_t kk = j - rot;
                 if (kk < 0) kk += len;
-                key |= (uint64_t)read_nib(R, i, readOffset + kk) << (60 - 4 * j);
+                key |= (uint64_t)nib(readOffset + kk) << (60 - 4 * j);
               }
               e.key = key;
               e.sp = -1;
@@ -713,7 +712,7 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
                     for (int32_t j = 16 + 16 * w; j < min(len, 32 + 16 * w); j++) {
                       int32_t kk = j - rot;
                       if (kk < 0) kk += len;
-                      word |= (uint64_t)read_nib(R, i, readOffset + kk) << (60 - 4 * (j - 16 - 16 * w));
+                      word |= (uint64_t)nib(readOffset + kk) << (60 - 4 * (j - 16 - 16 * w));
                     }
                     a.spool[sp + w] = word;
                   }
@@ -736,8 +735,8 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
             if (trusted(rloc) && inRegion(dloc)) {
               if (inRegion((int64_t)dloc + len)) {  // add(dloc+len, base, qual, adjMq, valid = true)
                 const int64_t gp = g.pos_base + (dloc + len - g.start);
-                const int bi = nib_index(read_nib(R, i, rloc));
-                const int32_t q = read_qual(R, i, rloc, hasQual, P);
+                const int bi = nib_index(nib(rloc));
+                const int32_t q = (hasQual ? (int32_t)(int8_t)rqual[rloc] : P.default_qual);
                 if (bi >= 0 && q >= P.min_qual) {
                   atomicAdd(((int*)a.rec.count) + 4 * gp + bi, 1);
                   atomicAdd(((unsigned long long*)a.rec.qual_sum) + 4 * gp + bi,
@@ -764,7 +763,7 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
             const int64_t gp = g.pos_base + (dloc - g.start);
             atomicAdd(&a.rec.mq_sum[gp], indelMq + 1);
             atomicAdd(&a.rec.del_qual[gp], indelMq + 1);
-            atomicAdd(&a.rec.q_sum[gp], read_qual(R, i, readOffset, hasQual, P));
+            atomicAdd(&a.rec.q_sum[gp], (hasQual ? (int32_t)(int8_t)rqual[readOffset] : P.default_qual));
             atomicAdd(&a.rec.deletions[gp], 1);
             unsigned long long slot = atomicAdd(a.n_events, 1ull);
             if ((int64_t)slot < a.event_cap) {
@@ -787,32 +786,23 @@ __global__ void __launch_bounds__(256) k_read_events(EventArgs a, int32_t chunk_
     rfc = warp_sum_u64(rfc); rfs = warp_sum_u64(rfs); rfq = warp_sum_u64(rfq);
     pcs = __reduce_add_sync(FULL, pcs); iss = __reduce_add_sync(FULL, iss);
     err = __reduce_max_sync(FULL, err);
-    if ((threadIdx.x & 31) == 0) {
-      if (rc_n) atomicAdd(&s_rc, rc_n);
-      if (bc_n) atomicAdd(&s_bc, bc_n);
-      if (frc) { atomicAdd(&s_frc, frc); atomicAdd(&s_frs, frs); atomicAdd(&s_frq, frq); }
-      if (rfc) { atomicAdd(&s_rfc, rfc); atomicAdd(&s_rfs, rfs); atomicAdd(&s_rfq, rfq); }
-      if (pcs) atomicAdd(&s_pcs, (int32_t)pcs);
-      if (iss) atomicAdd(&s_iss, (int32_t)iss);
-      if (err) atomicExch(&s_err, err);
+    if ((threadIdx.x & 31) == 0) {  // k_region_prep adds the chunks up per region
+      ChunkStats& cs = a.chunk_stats[ch];
+      if (rc_n) atomicAdd(&cs.read_count, rc_n);
+      if (bc_n) atomicAdd(&cs.base_count, bc_n);
+      if (frc) { atomicAdd(&cs.fr_count, frc); atomicAdd(&cs.fr_sum, frs); atomicAdd(&cs.fr_sumsq, frq); }
+      if (rfc) { atomicAdd(&cs.rf_count, rfc); atomicAdd(&cs.rf_sum, rfs); atomicAdd(&cs.rf_sumsq, rfq); }
+      if (pcs) atomicAdd((uint32_t*)&cs.phys_cov_start, pcs);
+      if (iss) atomicAdd((uint32_t*)&cs.insert_size_start, iss);
+      if (err) atomicMax(&cs.error, err);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {  // partial sums of this chunk; k_region_prep adds them up per region
-      ChunkStats cs;
-      cs.read_count = s_rc; cs.base_count = s_bc;
-      cs.fr_count = s_frc; cs.fr_sum = s_frs; cs.fr_sumsq = s_frq;
-      cs.rf_count = s_rfc; cs.rf_sum = s_rfs; cs.rf_sumsq = s_rfq;
-      cs.phys_cov_start = s_pcs; cs.insert_size_start = s_iss; cs.error = s_err; cs.pad = 0;
-      a.chunk_stats[ch] = cs;
-    }
-    __syncthreads();
   }
 }
 
 void launch_read_events(const EventArgs& a, int32_t chunk_begin, int32_t chunk_count, cudaStream_t s) {
   if (chunk_count <= 0) return;
-  int blocks = chunk_count;
-  k_read_events<<<blocks, 256, 0, s>>>(a, chunk_begin, chunk_begin + chunk_count);
+  cudaMemsetAsync(a.chunk_stats + chunk_begin, 0, sizeof(ChunkStats) * (size_t)chunk_count, s);
+  k_read_events<<<chunk_count * kEvPerChunk, kEvThreads, 0, s>>>(a, chunk_begin, chunk_begin + chunk_count);
 }
 
 // ---------------------------------------------------------------------------

@@ -13,10 +13,12 @@
 // The random generator is splitmix64 + xoshiro256**, so the output is the same
 // on every platform for a given seed.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -164,22 +166,14 @@ bool simRead(Rng& rng, const uint8_t* sample, int64_t slen, const int64_t* s2r, 
   return true;
 }
 
-}  // namespace
-
-extern "C" {
-
-// Simulates pairs over one contig.  Returns a handle; read sizes with
-// sy_n_reads / sy_n_cigar, copy out with sy_copy, free with sy_free.
-void* sy_simulate(const uint8_t* sample, int64_t slen, const int64_t* s2r, const uint8_t* repeat_mask, int64_t ref_len,
-                  const SimParams* P, uint64_t seed) {
-  Sim* S = new Sim();
-  Rng rng(seed);
+// Simulates `count` pairs of one contig into S with rng.
+static void simPairs(Rng& rng, int64_t count, const uint8_t* sample, int64_t slen, const int64_t* s2r,
+                     const uint8_t* repeat_mask, int64_t ref_len, const SimParams* P, Sim* S) {
   const int L = P->read_len;
-  int64_t nPairs = (int64_t)std::llround(P->coverage * (double)slen / (2.0 * L));
-  S->reads.reserve(2 * nPairs);
-  S->bases.reserve((size_t)(2 * nPairs * L));
-  S->quals.reserve((size_t)(2 * nPairs * L));
-  for (int64_t p = 0; p < nPairs; p++) {
+  S->reads.reserve(2 * count);
+  S->bases.reserve((size_t)(2 * count * L));
+  S->quals.reserve((size_t)(2 * count * L));
+  for (int64_t p = 0; p < count; p++) {
     int64_t fl = (int64_t)std::llround(P->insert_mean + P->insert_sd * rng.normal());
     fl = std::max<int64_t>(fl, L);
     fl = std::min<int64_t>(fl, slen);
@@ -215,6 +209,59 @@ void* sy_simulate(const uint8_t* sample, int64_t slen, const int64_t* s2r, const
     S->reads.push_back(b);
     if (u6 < P->noqual_frac) {
       for (int k = 0; k < L; k++) S->quals[a.base_begin + k] = 0xFF;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// Simulates pairs over one contig.  Returns a handle; read sizes with
+// sy_n_reads / sy_n_cigar, copy out with sy_copy, free with sy_free.
+// Pairs are drawn in blocks of kPairBlock: block 0 from the contig's seed,
+// block b from a seed derived from (seed, b); blocks run on parallel threads
+// and the result does not depend on the thread count.
+void* sy_simulate(const uint8_t* sample, int64_t slen, const int64_t* s2r, const uint8_t* repeat_mask, int64_t ref_len,
+                  const SimParams* P, uint64_t seed) {
+  constexpr int64_t kPairBlock = 1000000;
+  Sim* S = new Sim();
+  const int L = P->read_len;
+  const int64_t nPairs = (int64_t)std::llround(P->coverage * (double)slen / (2.0 * L));
+  const int64_t nb = std::max<int64_t>(1, (nPairs + kPairBlock - 1) / kPairBlock);
+  if (nb == 1) {
+    Rng rng(seed);
+    simPairs(rng, nPairs, sample, slen, s2r, repeat_mask, ref_len, P, S);
+  } else {
+    std::vector<Sim> parts((size_t)nb);
+    std::atomic<int64_t> next{0};
+    auto work = [&]() {
+      for (int64_t b; (b = next.fetch_add(1)) < nb;) {
+        Rng rng(b == 0 ? seed : seed ^ (0xD1B54A32D192ED03ull * (uint64_t)(b + 1)));
+        simPairs(rng, std::min(kPairBlock, nPairs - b * kPairBlock), sample, slen, s2r, repeat_mask, ref_len, P,
+                 &parts[(size_t)b]);
+      }
+    };
+    const int64_t nt = std::min<int64_t>(nb, std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (int64_t k = 1; k < nt; k++) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+    for (Sim& q : parts) {  // concatenate the blocks in order
+      const uint32_t c0 = (uint32_t)S->cig.size();
+      const uint64_t b0 = S->bases.size();
+      for (Read r : q.reads) {
+        r.cig_begin += c0;
+        r.base_begin += b0;
+        S->reads.push_back(r);
+      }
+      S->cig.insert(S->cig.end(), q.cig.begin(), q.cig.end());
+      S->bases.insert(S->bases.end(), q.bases.begin(), q.bases.end());
+      S->quals.insert(S->quals.end(), q.quals.begin(), q.quals.end());
+      std::vector<Read>().swap(q.reads);
+      std::vector<uint32_t>().swap(q.cig);
+      std::vector<uint8_t>().swap(q.bases);
+      std::vector<uint8_t>().swap(q.quals);
     }
   }
   // sort by position (stable)
