@@ -62,7 +62,7 @@ struct pg_ctx {
   int32_t launches = 0;
   // k-mer tally
   DevBuf kwin, kpre, kslot_base, kslot_cap, kx_base, kx_cap, kkeys, kcnt, kqs, kmq, kq;
-  DevBuf kx_keys, kx_used, kx_cnt, kx_qs, kx_mq, kx_q, kedges, kcount;
+  DevBuf kx_keys, kx_used, kx_cnt, kx_qs, kx_mq, kx_q, kedges, kcount, kx_ev, kx_evbase, kx_evcap, kx_evfill;
   // VCF formatting
   DevBuf vlen, vsums, vtext, vname;
   // CUDA graph of the batched pipeline, replayed while the plan and buffers are unchanged
@@ -231,7 +231,8 @@ void pg_close(pg_ctx* c) {
   for (DevBuf* b : all) release(*b);
   DevBuf* km[] = {&c->kwin, &c->kpre, &c->kslot_base, &c->kslot_cap, &c->kx_base, &c->kx_cap, &c->kkeys, &c->kcnt,
                   &c->kqs, &c->kmq, &c->kq, &c->kx_keys, &c->kx_used, &c->kx_cnt, &c->kx_qs, &c->kx_mq, &c->kx_q,
-                  &c->kedges, &c->kcount, &c->vlen, &c->vsums, &c->vtext, &c->vname};
+                  &c->kedges, &c->kcount, &c->kx_ev, &c->kx_evbase, &c->kx_evcap, &c->kx_evfill, &c->vlen,
+                  &c->vsums, &c->vtext, &c->vname};
   for (DevBuf* b : km) release(*b);
   for (auto& b : c->rec_i32) release(b);
   for (auto& b : c->rd) release(b);
@@ -720,7 +721,8 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
   std::vector<long long> pre(3 * (size_t)n_windows);
   CK(cudaMemcpyAsync(pre.data(), c->kpre.p, sizeof(long long) * pre.size(), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  std::vector<int64_t> sbase(n_windows), scap(n_windows), xbase(n_windows), xcap(n_windows);
+  std::vector<int64_t> sbase(n_windows), scap(n_windows), xbase(n_windows), xcap(n_windows), evbase(n_windows),
+      evcap(n_windows);
   for (int32_t w = 0; w < n_windows; w++) {
     // Assembler.addRead prunes K-mers with count < 2 every 100,000 reads
     // (S/Assembler.scala:74), which makes the tally order dependent.
@@ -728,6 +730,7 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
       return fail(c, PG_ERR_LIMIT, "window %d has %lld reads; the tally is exact below 100,000", w, pre[3 * w]);
     scap[w] = next_pow2(std::max<int64_t>(64, pre[3 * w + 1] + pre[3 * w + 1] / 2));
     xcap[w] = pre[3 * w + 2] > 0 ? next_pow2(std::max<int64_t>(16, 2 * pre[3 * w + 2])) : 0;
+    evcap[w] = pre[3 * w + 2];
   }
   const int64_t edge_cap = std::max<int64_t>(cap, 1);
   if ((s = ensure(c, c->kedges, sizeof(pg_kmer_edge) * edge_cap))) return s;
@@ -736,13 +739,13 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
   const int64_t budget = (int64_t)4 << 30;  // bytes of tables per batch
   int32_t w0 = 0;
   while (w0 < n_windows) {
-    int64_t ns = 0, nx = 0;
+    int64_t ns = 0, nx = 0, ne = 0;
     int32_t w1 = w0;
     while (w1 < n_windows) {
-      int64_t ns2 = ns + scap[w1], nx2 = nx + xcap[w1];
-      if (w1 > w0 && ns2 * 64 + nx2 * 80 > budget) break;
-      sbase[w1] = ns; xbase[w1] = nx;
-      ns = ns2; nx = nx2;
+      int64_t ns2 = ns + scap[w1], nx2 = nx + xcap[w1], ne2 = ne + evcap[w1];
+      if (w1 > w0 && ns2 * 64 + nx2 * 80 + ne2 * 16 > budget) break;
+      sbase[w1] = ns; xbase[w1] = nx; evbase[w1] = ne;
+      ns = ns2; nx = nx2; ne = ne2;
       w1++;
     }
     std::vector<int64_t> hb(4 * (size_t)n_windows, 0);
@@ -756,6 +759,10 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
     if ((s = ensure(c, c->kmq, 4 * (size_t)ns))) return s;
     if ((s = ensure(c, c->kq, 4 * (size_t)ns))) return s;
     const size_t nxs = (size_t)std::max<int64_t>(nx, 1);
+    if ((s = ensure(c, c->kx_ev, 16 * (size_t)std::max<int64_t>(ne, 1)))) return s;
+    if ((s = ensure(c, c->kx_evbase, 8 * (size_t)n_windows))) return s;
+    if ((s = ensure(c, c->kx_evcap, 8 * (size_t)n_windows))) return s;
+    if ((s = ensure(c, c->kx_evfill, 8 * (size_t)n_windows))) return s;
     if ((s = ensure(c, c->kx_keys, 16 * nxs))) return s;
     if ((s = ensure(c, c->kx_used, nxs))) return s;
     if ((s = ensure(c, c->kx_cnt, 16 * nxs))) return s;
@@ -767,6 +774,9 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
     CK(cudaMemcpyAsync(c->kslot_cap.p, scap.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->kx_base.p, xbase.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->kx_cap.p, xcap.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->kx_evbase.p, evbase.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->kx_evcap.p, evcap.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(c->kx_evfill.p, 0, 8 * (size_t)n_windows, st));
     CK(cudaMemsetAsync(c->kkeys.p, 0xFF, 8 * (size_t)ns, st));
     CK(cudaMemsetAsync(c->kcnt.p, 0, 16 * (size_t)ns, st));
     CK(cudaMemsetAsync(c->kqs.p, 0, 32 * (size_t)ns, st));
@@ -786,6 +796,8 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
     a.x_base = P<int64_t>(c->kx_base); a.x_cap = P<int64_t>(c->kx_cap);
     a.x_keys = P<unsigned long long>(c->kx_keys); a.x_used = P<uint8_t>(c->kx_used); a.x_cnt = P<uint32_t>(c->kx_cnt);
     a.x_qs = P<unsigned long long>(c->kx_qs); a.x_mq = P<uint32_t>(c->kx_mq); a.x_q = P<uint32_t>(c->kx_q);
+    a.x_ev_base = P<int64_t>(c->kx_evbase); a.x_ev_cap = P<int64_t>(c->kx_evcap);
+    a.x_ev_fill = P<unsigned long long>(c->kx_evfill); a.x_events = P<longlong2>(c->kx_ev);
     a.edges = P<pg_kmer_edge>(c->kedges); a.edge_cap = edge_cap;
     a.n_edges = P<unsigned long long>(c->kcount); a.overflow = (int32_t*)(P<unsigned long long>(c->kcount) + 1);
     launch_kmer_batch(a, w1 - w0, st);

@@ -27,14 +27,17 @@ __device__ inline unsigned long long mix64(unsigned long long x) {
   x ^= x >> 33; x *= 0xff51afd7ed558ccdull; x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ull; x ^= x >> 33;
   return x;
 }
-// nibble of base j of a read's strand (0 = forward, 1 = reverse complement)
-__device__ inline uint32_t strand_nib(const Reads& R, int64_t i, int32_t L, int strand, int32_t j) {
-  return strand == 0 ? read_nib(R, i, j) : comp_nib(read_nib(R, i, L - 1 - j));
+// nibble of base j of a read's strand (0 = forward, 1 = reverse complement);
+// seq points at the read's first sequence byte
+__device__ inline uint32_t strand_nib(const uint8_t* seq, int32_t L, int strand, int32_t j) {
+  const int32_t k = strand == 0 ? j : L - 1 - j;
+  const uint8_t b = seq[k >> 1];
+  const uint32_t n = (k & 1) ? (b & 15u) : (uint32_t)(b >> 4);
+  return strand == 0 ? n : comp_nib(n);
 }
-__device__ inline int32_t strand_qual(const Reads& R, int64_t i, int32_t L, int strand, int32_t j, bool hasQual,
-                                      int32_t dq) {
+__device__ inline int32_t strand_qual(const uint8_t* qual, int32_t L, int strand, int32_t j, bool hasQual, int32_t dq) {
   if (!hasQual) return dq;
-  return (int32_t)(int8_t)R.qual[R.qual_off[i] + (strand == 0 ? j : L - 1 - j)];
+  return (int32_t)(int8_t)qual[strand == 0 ? j : L - 1 - j];
 }
 
 // Per window: reads longer than K, K-mer events and exotic K-mer events.
@@ -49,10 +52,11 @@ __global__ void k_kmer_prepass(Reads R, const pg_window* wins, int32_t K, long l
     if (L <= K) continue;
     nr++;
     ne += 2ull * (unsigned long long)(L - K);
+    const uint8_t* seq = R.seq + R.seq_off[i];
     for (int strand = 0; strand < 2; strand++) {
       int32_t lastBad = -1;
       for (int32_t j = 0; j < L - 1; j++) {
-        if (code2(strand_nib(R, i, L, strand, j)) < 0) lastBad = j;
+        if (code2(strand_nib(seq, L, strand, j)) < 0) lastBad = j;
         int32_t o = j - K + 1;
         if (o >= 0 && lastBad >= o) nx++;
       }
@@ -71,45 +75,55 @@ __global__ void __launch_bounds__(256) k_kmer_count(KmerArgs a) {
   const int32_t K = a.K;
   const unsigned long long mask = (K == 32) ? ~0ull : ((1ull << (2 * K)) - 1);
   const int64_t base = a.slot_base[w], cap = a.slot_cap[w];
+  const int64_t xev0 = a.x_ev_base[w], xev_cap = a.x_ev_cap[w];
   const Reads& R = a.R;
   for (int64_t i = win.read_begin + threadIdx.x; i < win.read_end; i += blockDim.x) {
     const int32_t L = R.l_seq[i];
     if (L <= K) continue;
     const uint32_t mq1 = (uint32_t)R.mapq[i] + 1u;
-    const bool hasQual = R.qual[R.qual_off[i]] != 0xFF;
+    const uint8_t* seq = R.seq + R.seq_off[i];
+    const uint8_t* qual = R.qual + R.qual_off[i];
+    const bool hasQual = qual[0] != 0xFF;
     for (int strand = 0; strand < 2; strand++) {
       unsigned long long key = 0;
       int32_t lastBad = -1;
-      uint32_t nib = strand_nib(R, i, L, strand, 0);
+      uint32_t nib = strand_nib(seq, L, strand, 0);
       for (int32_t j = 0; j < L - 1; j++) {
         int c = code2(nib);
         if (c < 0) { lastBad = j; c = 0; }
         key = ((key << 2) | (unsigned long long)c) & mask;
-        const uint32_t next = strand_nib(R, i, L, strand, j + 1);
+        const uint32_t next = strand_nib(seq, L, strand, j + 1);
         const int32_t o = j - K + 1;
-        if (o >= 0 && lastBad < o) {
+        if (o >= 0) {
           const int bi = code2(next);
-          const int32_t q = strand_qual(R, i, L, strand, j + 1, hasQual, a.default_qual);
+          const int32_t q = strand_qual(qual, L, strand, j + 1, hasQual, a.default_qual);
           if (bi >= 0 && q >= a.min_qual) {
-            int64_t h = (int64_t)(mix64(key) & (unsigned long long)(cap - 1));
-            int64_t slot = -1;
-            for (int64_t probe = 0; probe < cap; probe++) {
-              const int64_t s = base + h;
-              unsigned long long k = a.keys[s];
-              if (k == key) { slot = s; break; }
-              if (k == kEmpty) {
-                unsigned long long prev = atomicCAS(&a.keys[s], kEmpty, key);
-                if (prev == kEmpty || prev == key) { slot = s; break; }
-              }
-              h = (h + 1) & (cap - 1);
-            }
-            if (slot < 0) {
-              atomicExch(a.overflow, 1);
+            if (lastBad >= o) {
+              // a K-mer with a base other than A/C/G/T: listed for k_kmer_exotic
+              const unsigned long long k = atomicAdd(&a.x_ev_fill[w], 1ull);
+              if ((int64_t)k < xev_cap) a.x_events[xev0 + k] = make_longlong2((long long)i, ((long long)strand << 32) | (long long)o);
+              else atomicExch(a.overflow, 1);
             } else {
-              atomicAdd(&a.cnt[4 * slot + bi], 1u);
-              atomicAdd(&a.qs[4 * slot + bi], (unsigned long long)((uint32_t)q * mq1));
-              atomicAdd(&a.mq_sum[slot], mq1);
-              atomicAdd(&a.q_sum[slot], (uint32_t)q);
+              int64_t h = (int64_t)(mix64(key) & (unsigned long long)(cap - 1));
+              int64_t slot = -1;
+              for (int64_t probe = 0; probe < cap; probe++) {
+                const int64_t s = base + h;
+                unsigned long long k = a.keys[s];
+                if (k == key) { slot = s; break; }
+                if (k == kEmpty) {
+                  unsigned long long prev = atomicCAS(&a.keys[s], kEmpty, key);
+                  if (prev == kEmpty || prev == key) { slot = s; break; }
+                }
+                h = (h + 1) & (cap - 1);
+              }
+              if (slot < 0) {
+                atomicExch(a.overflow, 1);
+              } else {
+                atomicAdd(&a.cnt[4 * slot + bi], 1u);
+                atomicAdd(&a.qs[4 * slot + bi], (unsigned long long)((uint32_t)q * mq1));
+                atomicAdd(&a.mq_sum[slot], mq1);
+                atomicAdd(&a.q_sum[slot], (uint32_t)q);
+              }
             }
           }
         }
@@ -136,9 +150,8 @@ __device__ inline void kmer_call(const uint32_t cnt[4], const unsigned long long
   alt = homoScore >= hetero ? -1 : o1;
 }
 
-__device__ inline void emit_edge(const KmerArgs& a, unsigned long long hi, unsigned long long lo, int32_t w,
-                                 int base, int alt, int32_t depth, int32_t weight) {
-  unsigned long long k = atomicAdd(a.n_edges, 1ull);
+__device__ inline void store_edge(const KmerArgs& a, unsigned long long k, unsigned long long hi, unsigned long long lo,
+                                  int32_t w, int base, int alt, int32_t depth, int32_t weight) {
   if ((int64_t)k < a.edge_cap) {
     pg_kmer_edge e;
     e.key_hi = hi; e.key_lo = lo; e.window = w; e.next = (int8_t)base; e.alt = (int8_t)alt; e.pad_ = 0;
@@ -151,76 +164,91 @@ __global__ void k_kmer_edges(KmerArgs a) {
   const int32_t w = a.win_begin + blockIdx.x;
   const int64_t base = a.slot_base[w], cap = a.slot_cap[w];
   const int32_t K = a.K;
-  for (int64_t s = base + threadIdx.x; s < base + cap; s += blockDim.x) {
-    const unsigned long long key = a.keys[s];
-    if (key == kEmpty) continue;
-    uint32_t cnt[4];
-    unsigned long long qs[4];
-    for (int b = 0; b < 4; b++) { cnt[b] = a.cnt[4 * s + b]; qs[b] = a.qs[4 * s + b]; }
-    const int32_t depth = (int32_t)(cnt[0] + cnt[1] + cnt[2] + cnt[3]);
-    if (depth < a.min_depth) continue;
-    int b0, alt;
-    kmer_call(cnt, qs, a.q_sum[s], b0, alt);
-    unsigned long long hi = 0, lo = 0;
-    for (int32_t j = 0; j < K; j++) {
-      const unsigned long long nibv = 1ull << ((key >> (2 * (K - 1 - j))) & 3ull);
-      if (j < 16) hi |= nibv << (60 - 4 * j); else lo |= nibv << (60 - 4 * (j - 16));
+  const int lane = threadIdx.x & 31;
+  // every warp runs the same number of iterations, so the whole warp meets the ballot
+  for (int64_t s0 = base; s0 < base + cap; s0 += blockDim.x) {
+    const int64_t s = s0 + threadIdx.x;
+    bool emit = false;
+    uint32_t cnt[4] = {0, 0, 0, 0};
+    unsigned long long key = kEmpty;
+    int32_t depth = 0;
+    int b0 = 0, alt = -1;
+    if (s < base + cap) {
+      key = a.keys[s];
+      if (key != kEmpty) {
+        unsigned long long qs[4];
+        for (int b = 0; b < 4; b++) { cnt[b] = a.cnt[4 * s + b]; qs[b] = a.qs[4 * s + b]; }
+        depth = (int32_t)(cnt[0] + cnt[1] + cnt[2] + cnt[3]);
+        if (depth >= a.min_depth) {
+          kmer_call(cnt, qs, a.q_sum[s], b0, alt);
+          emit = true;
+        }
+      }
     }
-    emit_edge(a, hi, lo, w, b0, alt, depth, (int32_t)(b0 == 0 ? cnt[0] : b0 == 1 ? cnt[1] : b0 == 2 ? cnt[2] : cnt[3]));
+    const unsigned m = __ballot_sync(0xffffffffu, emit);
+    if (!m) continue;
+    unsigned long long first = 0;
+    if (lane == __ffs(m) - 1) first = atomicAdd(a.n_edges, (unsigned long long)__popc(m));
+    first = __shfl_sync(0xffffffffu, first, __ffs(m) - 1);
+    if (emit) {
+      unsigned long long hi = 0, lo = 0;
+      for (int32_t j = 0; j < K; j++) {
+        const unsigned long long nibv = 1ull << ((key >> (2 * (K - 1 - j))) & 3ull);
+        if (j < 16) hi |= nibv << (60 - 4 * j); else lo |= nibv << (60 - 4 * (j - 16));
+      }
+      store_edge(a, first + __popc(m & ((1u << lane) - 1u)), hi, lo, w, b0, alt, depth,
+                 (int32_t)(b0 == 0 ? cnt[0] : b0 == 1 ? cnt[1] : b0 == 2 ? cnt[2] : cnt[3]));
+    }
   }
 }
 
-// Exotic K-mers: one thread per window, private table keyed by 4-bit codes.
+// Exotic K-mers: one thread per window over the window's listed events, in a
+// private table keyed by 4-bit codes.
 __global__ void k_kmer_exotic(KmerArgs a, int32_t n_win) {
   const int32_t wl = blockIdx.x * blockDim.x + threadIdx.x;
   if (wl >= n_win) return;
   const int32_t w = a.win_begin + wl;
   const int64_t base = a.x_base[w], cap = a.x_cap[w];
   if (cap == 0) return;
-  const pg_window win = a.windows[w];
   const int32_t K = a.K;
   const Reads& R = a.R;
-  for (int64_t i = win.read_begin; i < win.read_end; i++) {
+  const int64_t nev = min((int64_t)a.x_ev_fill[w], a.x_ev_cap[w]);
+  for (int64_t k = 0; k < nev; k++) {
+    const longlong2 ev = a.x_events[a.x_ev_base[w] + k];
+    const int64_t i = ev.x;
+    const int strand = (int)(ev.y >> 32);
+    const int32_t o = (int32_t)(ev.y & 0xffffffffll);
     const int32_t L = R.l_seq[i];
-    if (L <= K) continue;
     const uint32_t mq1 = (uint32_t)R.mapq[i] + 1u;
-    const bool hasQual = R.qual[R.qual_off[i]] != 0xFF;
-    for (int strand = 0; strand < 2; strand++) {
-      int32_t lastBad = -1;
-      for (int32_t j = 0; j < L - 1; j++) {
-        if (code2(strand_nib(R, i, L, strand, j)) < 0) lastBad = j;
-        const int32_t o = j - K + 1;
-        if (o < 0 || lastBad < o) continue;
-        const uint32_t next = strand_nib(R, i, L, strand, j + 1);
-        const int bi = code2(next);
-        const int32_t q = strand_qual(R, i, L, strand, j + 1, hasQual, a.default_qual);
-        if (!(bi >= 0 && q >= a.min_qual)) continue;
-        unsigned long long hi = 0, lo = 0;
-        for (int32_t t = 0; t < K; t++) {
-          const unsigned long long nb = strand_nib(R, i, L, strand, o + t);
-          if (t < 16) hi |= nb << (60 - 4 * t); else lo |= nb << (60 - 4 * (t - 16));
-        }
-        int64_t h = (int64_t)(mix64(hi ^ mix64(lo)) & (unsigned long long)(cap - 1));
-        int64_t slot = -1;
-        for (int64_t probe = 0; probe < cap; probe++) {
-          const int64_t s = base + h;
-          if (a.x_keys[2 * s] == hi && a.x_keys[2 * s + 1] == lo && a.x_used[s]) { slot = s; break; }
-          if (!a.x_used[s]) {
-            a.x_used[s] = 1;
-            a.x_keys[2 * s] = hi;
-            a.x_keys[2 * s + 1] = lo;
-            slot = s;
-            break;
-          }
-          h = (h + 1) & (cap - 1);
-        }
-        if (slot < 0) { atomicExch(a.overflow, 1); continue; }
-        a.x_cnt[4 * slot + bi] += 1u;
-        a.x_qs[4 * slot + bi] += (unsigned long long)((uint32_t)q * mq1);
-        a.x_mq[slot] += mq1;
-        a.x_q[slot] += (uint32_t)q;
-      }
+    const uint8_t* seq = R.seq + R.seq_off[i];
+    const uint8_t* qual = R.qual + R.qual_off[i];
+    const bool hasQual = qual[0] != 0xFF;
+    const int bi = code2(strand_nib(seq, L, strand, o + K));
+    const int32_t q = strand_qual(qual, L, strand, o + K, hasQual, a.default_qual);
+    unsigned long long hi = 0, lo = 0;
+    for (int32_t t = 0; t < K; t++) {
+      const unsigned long long nb = strand_nib(seq, L, strand, o + t);
+      if (t < 16) hi |= nb << (60 - 4 * t); else lo |= nb << (60 - 4 * (t - 16));
     }
+    int64_t h = (int64_t)(mix64(hi ^ mix64(lo)) & (unsigned long long)(cap - 1));
+    int64_t slot = -1;
+    for (int64_t probe = 0; probe < cap; probe++) {
+      const int64_t s = base + h;
+      if (a.x_keys[2 * s] == hi && a.x_keys[2 * s + 1] == lo && a.x_used[s]) { slot = s; break; }
+      if (!a.x_used[s]) {
+        a.x_used[s] = 1;
+        a.x_keys[2 * s] = hi;
+        a.x_keys[2 * s + 1] = lo;
+        slot = s;
+        break;
+      }
+      h = (h + 1) & (cap - 1);
+    }
+    if (slot < 0) { atomicExch(a.overflow, 1); continue; }
+    a.x_cnt[4 * slot + bi] += 1u;
+    a.x_qs[4 * slot + bi] += (unsigned long long)((uint32_t)q * mq1);
+    a.x_mq[slot] += mq1;
+    a.x_q[slot] += (uint32_t)q;
   }
   for (int64_t s = base; s < base + cap; s++) {
     if (!a.x_used[s]) continue;
@@ -231,8 +259,8 @@ __global__ void k_kmer_exotic(KmerArgs a, int32_t n_win) {
     if (depth < a.min_depth) continue;
     int b0, alt;
     kmer_call(cnt, qs, a.x_q[s], b0, alt);
-    emit_edge(a, a.x_keys[2 * s], a.x_keys[2 * s + 1], w, b0, alt, depth,
-              (int32_t)(b0 == 0 ? cnt[0] : b0 == 1 ? cnt[1] : b0 == 2 ? cnt[2] : cnt[3]));
+    store_edge(a, atomicAdd(a.n_edges, 1ull), a.x_keys[2 * s], a.x_keys[2 * s + 1], w, b0, alt, depth,
+               (int32_t)(b0 == 0 ? cnt[0] : b0 == 1 ? cnt[1] : b0 == 2 ? cnt[2] : cnt[3]));
   }
 }
 

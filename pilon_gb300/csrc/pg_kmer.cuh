@@ -27,6 +27,11 @@ struct KmerArgs {
   unsigned long long* x_qs;
   uint32_t* x_mq;
   uint32_t* x_q;
+  // exotic K-mer events (read, strand << 32 | offset), listed per window by k_kmer_count
+  const int64_t* x_ev_base;
+  const int64_t* x_ev_cap;
+  unsigned long long* x_ev_fill;
+  longlong2* x_events;
   // output
   pg_kmer_edge* edges;
   int64_t edge_cap;

@@ -173,14 +173,17 @@ class Engine:
         out.stats = self.stats(r)
         return out
 
-    def kmer_tally(self, windows, K, params, min_depth=5, cap=1 << 20):
+    def kmer_tally(self, windows, K, params, min_depth=5, cap=None):
         wins = (_abi.pg_window * max(1, len(windows)))(*[_abi.pg_window(a, b) for a, b in windows])
+        # start from the last call's edge count, so a repeated call runs once
+        cap = cap or getattr(self, "_kmer_cap", 1 << 20)
         while True:
             edges = np.zeros(cap, _abi.kmer_edge_dtype())
             n = C.c_int64()
             self._check(self.L.pg_kmer_tally(self.h, C.cast(wins, C.c_void_p), len(windows), K, C.byref(params),
                                              min_depth, edges.ctypes.data, cap, C.byref(n)))
             if n.value <= cap:
+                self._kmer_cap = max(cap, int(n.value))
                 return edges[:n.value]
             cap = int(n.value)
 
