@@ -331,52 +331,65 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               for (int32_t l = max(cs, tileLo) + gl; l <= min(ce, tileHi); l += G) atomicAdd(&s_bad[l - tileLo], 1u);
             }
             if (rk == kFast && ri1 > ri0) {
-              // Chunks of 4 consecutive aligned bases; lane gl of the group takes chunks
-              // gl, gl + G, ... and loads the next one while it adds the current one.
-              // A chunk's qualities are one aligned 32-bit word (it holds at least one
-              // trusted quality of this read, so it never leaves the pages of the quality
-              // array); its nibbles come from at most 3 sequence bytes, loaded only inside
-              // the read's trusted bytes.
+              // Whole chunks of 4 consecutive trusted bases that start on an aligned
+              // quality word; lane gl of the group takes chunks cf + gl, cf + gl + G, ...
+              // and loads the next one while it adds the current one.  A chunk's
+              // qualities are one aligned word and its nibbles lie in at most two
+              // aligned sequence words, each holding a trusted byte, so no load leaves
+              // the pages of the read store.  The at most 6 trusted bases before the
+              // first and after the last whole chunk are added one per lane.
               const uintptr_t qa = (uintptr_t)(rqp + ri0);
-              const int32_t xs = ri0 - (int32_t)(qa & 3u);  // x of byte 0 of chunk 0
-              const uint32_t* qw = (const uint32_t*)(qa & ~(uintptr_t)3);
-              const int32_t blo = (lead + ri0) >> 1;
-              const uint32_t nby = (uint32_t)(((lead + ri1 - 1) >> 1) - blo);  // trusted bytes blo .. blo + nby
-              const uint8_t* sb = rsp + blo;
-              const int32_t b0 = ((lead + xs) >> 1) - blo;   // first byte of chunk c: b0 + 2c
-              const uint32_t psh = 4u * (uint32_t)((lead + xs) & 1);  // chunks start on a low half-byte
+              const int32_t e0 = (int32_t)(qa & 3u);
+              const int32_t xs = ri0 - e0;  // x of byte 0 of chunk 0
+              const uint32_t* qw = (const uint32_t*)(qa - (uintptr_t)e0);
+              const int32_t cf = e0 ? 1 : 0, cend = (ri1 - xs) >> 2;  // whole chunks [cf, cend)
+              const int32_t fs = xs + 4 * cf, fe = xs + 4 * max(cend, cf);
+              const int32_t he = min(fs, ri1), ts = max(fe, he), nh = he - ri0, nt = max(ri1 - ts, 0);
               const uint32_t amq = 1u + (rmq1 << 12);
-              int32_t c = gl;
-              bool more = xs + 4 * c < ri1;
+              if (gl < nh + nt) {  // head and tail bases
+                const int32_t x = gl < nh ? ri0 + gl : ts + (gl - nh);
+                const int32_t rOff = lead + x;
+                const uint8_t b = rsp[rOff >> 1];
+                const uint32_t nib = (rOff & 1) ? (b & 15u) : (uint32_t)(b >> 4);
+                const int32_t qual = (int32_t)(int8_t)rqp[x];
+                if (((0x116u >> nib) & 1u) && qual >= P.min_qual) {
+                  uint32_t* cp = sm + (rpb + x) + ((0x30210u >> (2 * nib)) & 3u) * T;
+                  atomicAdd(cp, amq);
+                  atomicAdd(cp + 4 * T, (uint32_t)qual * rmq1);
+                  atomicAdd(sm + (rpb + x) + 8 * T, (uint32_t)qual);
+                }
+              }
+              const int32_t n0 = lead + xs;          // read offset of chunk 0's first base
+              const uint32_t psh = 4u * (uint32_t)(n0 & 1);  // chunks start on a low half-byte
+              const uint32_t lastb = (uint32_t)((n0 & 1) + 3) >> 1;  // last byte of a chunk's nibbles
+              const uint8_t* sb = rsp + (n0 >> 1);   // byte of chunk c's first nibble: sb + 2c
+              int32_t c = cf + gl;
+              bool more = c < cend;
               uint32_t qv = 0, sv = 0;
               if (more) {
-                const int32_t r = b0 + 2 * c;
+                const uintptr_t ba = (uintptr_t)(sb + 2 * c);
+                const uint32_t* wp = (const uint32_t*)(ba & ~(uintptr_t)3);
+                const uint32_t lo = wp[0], hi = (ba & 3u) + lastb >= 4u ? wp[1] : 0u;
                 qv = qw[c];
-                sv = ((uint32_t)r <= nby ? (uint32_t)sb[r] : 0u) |
-                     ((uint32_t)(r + 1) <= nby ? (uint32_t)sb[r + 1] << 8 : 0u) |
-                     ((uint32_t)(r + 2) <= nby ? (uint32_t)sb[r + 2] << 16 : 0u);
+                sv = __funnelshift_r(lo, hi, 8u * (uint32_t)(ba & 3u));
               }
               while (more) {
                 const int32_t cn = c + G;
-                const bool mn = xs + 4 * cn < ri1;
+                const bool mn = cn < cend;
                 uint32_t qn = 0, sn = 0;
                 if (mn) {
-                  const int32_t r = b0 + 2 * cn;
+                  const uintptr_t ba = (uintptr_t)(sb + 2 * cn);
+                  const uint32_t* wp = (const uint32_t*)(ba & ~(uintptr_t)3);
+                  const uint32_t lo = wp[0], hi = (ba & 3u) + lastb >= 4u ? wp[1] : 0u;
                   qn = qw[cn];
-                  sn = ((uint32_t)r <= nby ? (uint32_t)sb[r] : 0u) |
-                       ((uint32_t)(r + 1) <= nby ? (uint32_t)sb[r + 1] << 8 : 0u) |
-                       ((uint32_t)(r + 2) <= nby ? (uint32_t)sb[r + 2] << 16 : 0u);
+                  sn = __funnelshift_r(lo, hi, 8u * (uint32_t)(ba & 3u));
                 }
-                const int32_t xf = xs + 4 * c;
                 // nibbles in read order (BAM puts the first of a byte in its high half),
-                // base j of the chunk at bits 4j; bases outside the trusted offsets
-                // [ri0, ri1) become nibble 0, which is not counted
-                uint32_t nb = (((sv >> 4) & 0x0F0F0Fu) | ((sv & 0x0F0F0Fu) << 4)) >> psh;
-                nb &= (0xFFFFu << (4 * max(ri0 - xf, 0))) & (0xFFFFu >> (4 * max(4 - (ri1 - xf), 0)));
-                uint32_t* cl = sm + (rpb + xf);
-                // Every base adds, a rejected one adds 0: no branch per base.  A rejected
-                // base may sit up to 3 positions outside the tile; the counters have 4
-                // words of padding in front and the fields behind absorb the rest.
+                // base j of the chunk at bits 4j
+                const uint32_t nb = (((sv >> 4) & 0x0F0F0F0Fu) | ((sv & 0x0F0F0F0Fu) << 4)) >> psh;
+                uint32_t* cl = sm + (rpb + xs + 4 * c);
+                // every base adds, a rejected one (not A/C/G/T, or below minQual) adds 0:
+                // no branch per base
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                   const uint32_t nib = (nb >> (4 * j)) & 15u;
