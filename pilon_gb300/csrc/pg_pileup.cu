@@ -219,6 +219,7 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
   extern __shared__ __align__(16) uint32_t sm_raw[];
   uint32_t* sm = sm_raw + 4;  // 4 words of padding in front of the counters
   __shared__ unsigned long long s_bc;
+  __shared__ uint8_t s_perm[16][32];  // per warp: lane of the read in each round slot
   uint32_t* s_bad = sm + 9 * T;
   uint32_t* s_clip = sm + 10 * T;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -291,26 +292,33 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
             }
           }
         }
-        // ---- simple reads, 32 / G at a time, G lanes each.  Group g takes a read of
-        // residue class g when one is left, so the 4 groups of a warp add to 4 different
-        // position residues at every step and their shared-memory atomics hit 32
-        // different banks.
+        // ---- simple reads, 32 / G at a time, G lanes each.  With 4 groups, round k
+        // gives group g the k-th read of residue class g while every class has one,
+        // so the groups add to 4 different position residues at every step and their
+        // shared-memory atomics hit 32 different banks; the reads left over follow
+        // in lane order.  Each lane computes its read's slot at once.
         const bool simple_kind = kind != kSkip && kind != kComplex;
-        unsigned cm0 = __ballot_sync(FULL, simple_kind && cls == 0), cm1 = __ballot_sync(FULL, simple_kind && cls == 1);
-        unsigned cm2 = __ballot_sync(FULL, simple_kind && cls == 2), cm3 = __ballot_sync(FULL, simple_kind && cls == 3);
-        while (cm0 | cm1 | cm2 | cm3) {
-          int src = 32;  // 32: fewer reads than groups are left
-#pragma unroll
-          for (int g2 = 0; g2 < NG; g2++) {
-            const unsigned pref = g2 == 0 ? cm0 : g2 == 1 ? cm1 : g2 == 2 ? cm2 : cm3;
-            const unsigned m = pref ? pref : (cm0 | cm1 | cm2 | cm3);
-            const unsigned bit = m & (0u - m);
-            if (g2 == grp) src = bit ? __ffs(bit) - 1 : 32;
-            cm0 &= ~bit;
-            cm1 &= ~bit;
-            cm2 &= ~bit;
-            cm3 &= ~bit;
+        const unsigned below = (1u << lane) - 1u;
+        const unsigned sm_all = __ballot_sync(FULL, simple_kind);
+        const int n_simple = __popc(sm_all);
+        if (simple_kind) {
+          int slot;
+          if (NG == 4) {
+            const unsigned c0 = __ballot_sync(sm_all, cls == 0), c1 = __ballot_sync(sm_all, cls == 1);
+            const unsigned c2 = __ballot_sync(sm_all, cls == 2), c3 = __ballot_sync(sm_all, cls == 3);
+            const int m = min(min(__popc(c0), __popc(c1)), min(__popc(c2), __popc(c3)));
+            const unsigned mine = cls == 0 ? c0 : cls == 1 ? c1 : cls == 2 ? c2 : c3;
+            const int rank = __popc(mine & below);
+            const unsigned left = __ballot_sync(sm_all, rank >= m);
+            slot = rank < m ? 4 * rank + cls : 4 * m + __popc(left & below);
+          } else {
+            slot = __popc(sm_all & below);
           }
+          s_perm[warp][slot] = (uint8_t)lane;
+        }
+        __syncwarp();
+        for (int r0 = 0; r0 < n_simple; r0 += NG) {
+          const int src = r0 + grp < n_simple ? (int)s_perm[warp][r0 + grp] : 32;  // 32: no read for this group
           const int s2 = src < 32 ? src : lane;
           const uint32_t rk = __shfl_sync(FULL, kind, s2);
           const int32_t ri0 = __shfl_sync(FULL, i0, s2), ri1 = __shfl_sync(FULL, i1, s2);
