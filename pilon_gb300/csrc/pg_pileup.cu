@@ -354,44 +354,33 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               const int32_t fs = xs + 4 * cf, fe = xs + 4 * max(cend, cf);
               const int32_t he = min(fs, ri1), ts = max(fe, he), nh = he - ri0, nt = max(ri1 - ts, 0);
               const uint32_t amq = 1u + (rmq1 << 12);
-              if (gl < nh + nt) {  // head and tail bases
-                const int32_t x = gl < nh ? ri0 + gl : ts + (gl - nh);
-                const int32_t rOff = lead + x;
-                const uint8_t b = rsp[rOff >> 1];
-                const uint32_t nib = (rOff & 1) ? (b & 15u) : (uint32_t)(b >> 4);
-                const int32_t qual = (int32_t)(int8_t)rqp[x];
-                if (((0x116u >> nib) & 1u) && qual >= P.min_qual) {
-                  uint32_t* cp = sm + (rpb + x) + ((0x30210u >> (2 * nib)) & 3u) * T;
-                  atomicAdd(cp, amq);
-                  atomicAdd(cp + 4 * T, (uint32_t)qual * rmq1);
-                  atomicAdd(sm + (rpb + x) + 8 * T, (uint32_t)qual);
-                }
+              // head and tail bases: loaded now, added after the chunks
+              const bool ht = gl < nh + nt;
+              const int32_t hx = gl < nh ? ri0 + gl : ts + (gl - nh);
+              uint32_t hb = 0, hq = 0;
+              if (ht) {
+                hb = rsp[(lead + hx) >> 1];
+                hq = rqp[hx];
               }
               const int32_t n0 = lead + xs;          // read offset of chunk 0's first base
               const uint32_t psh = 4u * (uint32_t)(n0 & 1);  // chunks start on a low half-byte
               const uint32_t lastb = (uint32_t)((n0 & 1) + 3) >> 1;  // last byte of a chunk's nibbles
               const uint8_t* sb = rsp + (n0 >> 1);   // byte of chunk c's first nibble: sb + 2c
-              int32_t c = cf + gl;
-              bool more = c < cend;
-              uint32_t qv = 0, sv = 0;
-              if (more) {
-                const uintptr_t ba = (uintptr_t)(sb + 2 * c);
+              // two chunks in flight ahead of the one being added
+              auto load_chunk = [&](int32_t cc, uint32_t& q, uint32_t& sv) {
+                const uintptr_t ba = (uintptr_t)(sb + 2 * cc);
                 const uint32_t* wp = (const uint32_t*)(ba & ~(uintptr_t)3);
                 const uint32_t lo = wp[0], hi = (ba & 3u) + lastb >= 4u ? wp[1] : 0u;
-                qv = qw[c];
+                q = qw[cc];
                 sv = __funnelshift_r(lo, hi, 8u * (uint32_t)(ba & 3u));
-              }
-              while (more) {
-                const int32_t cn = c + G;
-                const bool mn = cn < cend;
-                uint32_t qn = 0, sn = 0;
-                if (mn) {
-                  const uintptr_t ba = (uintptr_t)(sb + 2 * cn);
-                  const uint32_t* wp = (const uint32_t*)(ba & ~(uintptr_t)3);
-                  const uint32_t lo = wp[0], hi = (ba & 3u) + lastb >= 4u ? wp[1] : 0u;
-                  qn = qw[cn];
-                  sn = __funnelshift_r(lo, hi, 8u * (uint32_t)(ba & 3u));
-                }
+              };
+              int32_t c = cf + gl;
+              uint32_t qv = 0, sv = 0, q1 = 0, s1 = 0;
+              if (c < cend) load_chunk(c, qv, sv);
+              if (c + G < cend) load_chunk(c + G, q1, s1);
+              while (c < cend) {
+                uint32_t q2 = 0, s2 = 0;
+                if (c + 2 * G < cend) load_chunk(c + 2 * G, q2, s2);
                 // nibbles in read order (BAM puts the first of a byte in its high half),
                 // base j of the chunk at bits 4j
                 const uint32_t nb = (((sv >> 4) & 0x0F0F0F0Fu) | ((sv & 0x0F0F0F0Fu) << 4)) >> psh;
@@ -409,10 +398,18 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
                   atomicAdd(cp + 4 * T, (uint32_t)qual * rmq1 * ok);
                   atomicAdd(cl + j + 8 * T, (uint32_t)qual * ok);
                 }
-                c = cn;
-                more = mn;
-                qv = qn;
-                sv = sn;
+                c += G;
+                qv = q1; sv = s1; q1 = q2; s1 = s2;
+              }
+              if (ht) {
+                const uint32_t nib = ((lead + hx) & 1) ? (hb & 15u) : (hb >> 4);
+                const int32_t qual = (int32_t)(int8_t)hq;
+                if (((0x116u >> nib) & 1u) && qual >= P.min_qual) {
+                  uint32_t* cp = sm + (rpb + hx) + ((0x30210u >> (2 * nib)) & 3u) * T;
+                  atomicAdd(cp, amq);
+                  atomicAdd(cp + 4 * T, (uint32_t)qual * rmq1);
+                  atomicAdd(sm + (rpb + hx) + 8 * T, (uint32_t)qual);
+                }
               }
             } else if (rk == kInvalid) {
               for (int32_t ii = ri0 + gl; ii < ri1; ii += G) atomicAdd(&s_bad[rpb + ii], 1u);
