@@ -476,6 +476,18 @@ def main():
                  "gpu_launches_per_step": pn, "path": "one set of launches per region, no graph"}
         eng.pileup_regions(regions, params, batched=True)
 
+    # break candidates of every region on the device (pg_find_breaks), after a batched call
+    bt, n_breaks = [], 0
+    for _ in range(3):
+        eng.pileup_regions(regions, params, batched=bool(args.batched))  # breaks are found once per call
+        eng.sync()
+        t0 = time.perf_counter()
+        br = eng.find_breaks(params.min_min_depth)
+        bt.append(time.perf_counter() - t0)
+        n_breaks = sum(len(v) for v in br.values())
+    breaks = {"ms_per_call": 1e3 * min(bt), "breaks": n_breaks, "positions": int(sum(e - s + 1 for (c, s, e, a, b) in regions)),
+              "timing": "host wall clock of pg_find_breaks (device kernels, sorted list read back)"}
+
     # end to end through the C ABI: H2D of the read store from pinned memory,
     # pileup + calls, D2H of every region's records and calls
     e2e = None
@@ -534,6 +546,7 @@ def main():
         "e2e": e2e,
         "cpu_baseline": cpu,
     }
+    line["break_candidates"] = breaks
     if kmer:
         line["kmer_tally"] = kmer
     print(json.dumps(line))

@@ -175,6 +175,16 @@ typedef struct pg_kmer_edge {
   int32_t weight;            /* baseCount of the called base */
 } pg_kmer_edge;
 
+/* One break candidate of GenomeRegion.possibleBreaks (S/GenomeRegion.scala:
+ * 659-720): contig loci start..stop (1-based, inclusive) in region `region`
+ * of the last pg_pileup_regions call. */
+typedef struct pg_break {
+  int32_t region;
+  int32_t start;
+  int32_t stop;
+  int32_t pad_;
+} pg_break;
+
 typedef struct pg_ctx pg_ctx;
 
 /* ---- context ----------------------------------------------------------- */
@@ -243,6 +253,17 @@ pg_status pg_kmer_tally(pg_ctx *ctx, const pg_window *windows, int32_t n_windows
  * only records whose ALT is not "." (a delta for serving). */
 pg_status pg_format_vcf(pg_ctx *ctx, int32_t region, const char *name, int32_t diploid, int32_t vcf_qe,
                         int32_t variants_only, char *out, int64_t cap, int64_t *n_bytes);
+
+/* ---- break candidates ---------------------------------------------------
+ * GenomeRegion.possibleBreaks (S/GenomeRegion.scala:659-763) with
+ * pctBadOverall (:99-114) and fragCoverage (:287-300) for every region of the
+ * last pg_pileup_regions call, computed on the device from the resident
+ * pileups: the windows local reassembly works on (S/GenomeRegion.scala:
+ * 395-410).  `min_min_depth` is Pilon's --mindepth floor (5).  Breaks are
+ * returned sorted by region, then start; *n_breaks receives the count (up to
+ * cap).  Regions on which the reference threw (pg_region_stats.error) have
+ * none. */
+pg_status pg_find_breaks(pg_ctx *ctx, int32_t min_min_depth, pg_break *out, int64_t cap, int64_t *n_breaks);
 
 /* ---- timing -------------------------------------------------------------
  * Milliseconds of the dominant (pileup walk) kernel in the last

@@ -107,6 +107,10 @@ class pg_kmer_edge(C.Structure):
     ]
 
 
+class pg_break(C.Structure):
+    _fields_ = [("region", C.c_int32), ("start", C.c_int32), ("stop", C.c_int32), ("pad_", C.c_int32)]
+
+
 # numpy dtype of pg_kmer_edge, for bulk views of edge arrays
 def kmer_edge_dtype():
     import numpy as np
@@ -131,7 +135,7 @@ EXPORTED = [
     "pg_open", "pg_close", "pg_last_error", "pg_default_params", "pg_version",
     "pg_set_reference", "pg_set_reads", "pg_set_reads_device", "pg_pileup_regions",
     "pg_fetch_stats", "pg_fetch_region", "pg_set_tuning", "pg_kmer_tally",
-    "pg_last_kernel_ms", "pg_sync", "pg_phys_cov_scan_static", "pg_format_vcf",
+    "pg_last_kernel_ms", "pg_sync", "pg_phys_cov_scan_static", "pg_format_vcf", "pg_find_breaks",
 ]
 
 PG_STATIC_SCAN_MAX_POSITIONS = 16777216

@@ -19,7 +19,8 @@ INCLUDE = os.path.join(ROOT, "include")
 ENGINE = os.path.join(BUILD, "libpilon_gb300.so")
 SYNTH = os.path.join(BUILD, "libpg_synth.so")
 
-CU_SOURCES = ["pg_api.cu", "pg_pileup.cu", "pg_call.cu", "pg_kmer.cu", "pg_format.cu", "pg_noalloc.cu"]
+CU_SOURCES = ["pg_api.cu", "pg_pileup.cu", "pg_call.cu", "pg_kmer.cu", "pg_format.cu", "pg_noalloc.cu",
+              "pg_breaks.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-fwrapv", "--expt-relaxed-constexpr"]
 

@@ -11,6 +11,7 @@
 
 #include "pg_internal.cuh"
 #include "pg_kmer.cuh"
+#include "pg_breaks.cuh"
 #include "pg_format.cuh"
 
 using namespace pg;
@@ -65,6 +66,10 @@ struct pg_ctx {
   DevBuf kx_keys, kx_used, kx_cnt, kx_qs, kx_mq, kx_q, kedges, kcount, kx_ev, kx_evbase, kx_evcap, kx_evfill;
   // VCF formatting
   DevBuf vlen, vsums, vtext, vname;
+  // break candidates
+  DevBuf bfrag, bsums, btiles, bgaps, bout, bcount;
+  int64_t brk_n = -1;             // breaks of the last pileup call on the device, -1: not found yet
+  int32_t brk_mmd = 0;
   // CUDA graph of the batched pipeline, replayed while the plan and buffers are unchanged
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -232,7 +237,8 @@ void pg_close(pg_ctx* c) {
   DevBuf* km[] = {&c->kwin, &c->kpre, &c->kslot_base, &c->kslot_cap, &c->kx_base, &c->kx_cap, &c->kkeys, &c->kcnt,
                   &c->kqs, &c->kmq, &c->kq, &c->kx_keys, &c->kx_used, &c->kx_cnt, &c->kx_qs, &c->kx_mq, &c->kx_q,
                   &c->kedges, &c->kcount, &c->kx_ev, &c->kx_evbase, &c->kx_evcap, &c->kx_evfill, &c->vlen,
-                  &c->vsums, &c->vtext, &c->vname};
+                  &c->vsums, &c->vtext, &c->vname, &c->bfrag, &c->bsums, &c->btiles, &c->bgaps, &c->bout,
+                  &c->bcount};
   for (DevBuf* b : km) release(*b);
   for (auto& b : c->rec_i32) release(b);
   for (auto& b : c->rd) release(b);
@@ -452,6 +458,7 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
   if (params->min_qual < 0 || params->flank < 0 || params->min_mq < 0)
     return fail(c, PG_ERR_ARG, "min_qual, min_mq and flank must be >= 0");
   cudaSetDevice(c->device);
+  c->brk_n = -1;
   c->have_results = false;
   const int T = c->tile_width;
   // ---- plan
@@ -813,6 +820,68 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
   if (ncopy > 0 && edges) {
     CK(cudaMemcpyAsync(edges, c->kedges.p, sizeof(pg_kmer_edge) * ncopy, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+  }
+  return PG_OK;
+}
+
+pg_status pg_find_breaks(pg_ctx* c, int32_t min_min_depth, pg_break* out, int64_t cap, int64_t* n_breaks) {
+  if (!c || !n_breaks || cap < 0 || (cap > 0 && !out)) return fail(c, PG_ERR_ARG, "bad arguments");
+  if (!c->have_results) return fail(c, PG_ERR_STATE, "no pileup results: call pg_pileup_regions first");
+  cudaSetDevice(c->device);
+  *n_breaks = 0;
+  if (c->n_regions == 0 || c->n_call_tiles == 0) return PG_OK;
+  cudaStream_t st = c->stream;
+  pg_status s;
+  unsigned long long n = 0;
+  if (c->brk_n >= 0 && c->brk_mmd == min_min_depth) {  // found already: only copy out
+    n = (unsigned long long)c->brk_n;
+    goto copy_out;
+  }
+  {
+  const int64_t dev_cap = std::max<int64_t>(cap, 1024);
+  if ((s = ensure(c, c->bfrag, 4 * (size_t)std::max<int64_t>(c->n_positions, 1)))) return s;
+  if ((s = ensure(c, c->bsums, 24 * (size_t)c->n_regions))) return s;
+  if ((s = ensure(c, c->btiles, sizeof(BreakTile) * (size_t)c->n_call_tiles))) return s;
+  if ((s = ensure(c, c->bgaps, sizeof(int2) * (size_t)c->n_call_tiles * (kBreakStarts + 1)))) return s;
+  if ((s = ensure(c, c->bout, sizeof(pg_break) * (size_t)dev_cap))) return s;
+  if ((s = ensure(c, c->bcount, 16))) return s;
+  CK(cudaMemsetAsync(c->bsums.p, 0, 24 * (size_t)c->n_regions, st));
+  CK(cudaMemsetAsync(c->bcount.p, 0, 16, st));
+  BreakArgs a;
+  a.regions = P<RegionDev>(c->regions); a.call_tile_region = P<int32_t>(c->call_tile_region);
+  a.tile_begin = 0; a.n_tiles = c->n_call_tiles; a.rec = records(c); a.stats = P<StatsDev>(c->stats);
+  a.ref = P<uint8_t>(c->ref); a.min_min_depth = min_min_depth; a.frag = P<int32_t>(c->bfrag);
+  a.sums = P<long long>(c->bsums); a.tiles = P<BreakTile>(c->btiles); a.gap_scratch = P<int2>(c->bgaps);
+  a.out = P<pg_break>(c->bout); a.out_cap = dev_cap; a.n_out = P<unsigned long long>(c->bcount);
+  launch_breaks(a, c->n_regions, st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(&n, c->bcount.p, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if ((int64_t)n > dev_cap) {  // more than the device buffer held: run again with room for all
+    if ((s = ensure(c, c->bout, sizeof(pg_break) * (size_t)n))) return s;
+    CK(cudaMemsetAsync(c->bsums.p, 0, 24 * (size_t)c->n_regions, st));
+    CK(cudaMemsetAsync(c->bcount.p, 0, 16, st));
+    a.out = P<pg_break>(c->bout);
+    a.out_cap = (int64_t)n;
+    launch_breaks(a, c->n_regions, st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&n, c->bcount.p, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  c->brk_n = (int64_t)n;
+  c->brk_mmd = min_min_depth;
+  }
+copy_out:
+  *n_breaks = (int64_t)n;
+  if (cap > 0 && n > 0) {
+    std::vector<pg_break> all((size_t)n);
+    CK(cudaMemcpyAsync(all.data(), c->bout.p, sizeof(pg_break) * (size_t)n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    // the kernel appends in any order; the reference lists them by region, then position
+    std::sort(all.begin(), all.end(), [](const pg_break& x, const pg_break& y) {
+      return x.region != y.region ? x.region < y.region : x.start < y.start;
+    });
+    std::copy(all.begin(), all.begin() + std::min<int64_t>((int64_t)n, cap), out);
   }
   return PG_OK;
 }

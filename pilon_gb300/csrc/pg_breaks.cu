@@ -1,0 +1,275 @@
+// pg_breaks.cu — break candidates of every region of the last pileup call, on
+// the device (GenomeRegion.possibleBreaks, S/GenomeRegion.scala:659-763, with
+// pctBadOverall :99-114 and fragCoverage of processBam :287-300).
+//
+//   k_brk_frag    per position: fragCoverage = depth before the deletion-span
+//                 updates of pass 1; region sums of fragCoverage, badCoverage
+//                 and coverage
+//   k_brk_spans   takes each accepted deletion's span update back out of
+//                 fragCoverage (S/GenomeRegion.scala:259-264 adds it to depth)
+//   k_brk_tiles   per position the break test (low coverage, high clipping, too
+//                 many bad pairs, coverage dip) and the N test; per 1024-position
+//                 tile the first and last tested position and the run starts
+//                 inside the tile (summaryRegions' merge rule)
+//   k_brk_merge   one warp per region: joins the tiles' runs in order, drops
+//                 runs near the region's ends, keeps N runs of >= 10 bases as
+//                 gaps and drops breaks near a gap (Region.near, 300 bases)
+#include <cuda_runtime.h>
+
+#include "pg_breaks.cuh"
+
+namespace pg {
+
+#define FULL 0xffffffffu
+
+__device__ inline bool is_del_change(uint32_t call) { return PG_CALL_CHANGE(call) == PG_CHANGE_DEL; }
+
+__device__ inline long long block_sum(long long v, long long* s_red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) s_red[warp] = v;
+  __syncthreads();
+  long long t = 0;
+  if (warp == 0) {
+    t = lane < (int)(blockDim.x >> 5) ? s_red[lane] : 0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(FULL, t, o);
+  }
+  return t;  // valid in thread 0
+}
+
+// kBrkThreads threads per 1024-position tile, kBrkPer consecutive positions each.
+constexpr int kBrkThreads = 256;
+constexpr int kBrkPer = kCallTile / kBrkThreads;
+
+__global__ void __launch_bounds__(kBrkThreads) k_brk_frag(BreakArgs a) {
+  __shared__ long long s_red[32];
+  const int32_t t = a.tile_begin + blockIdx.x;
+  const int32_t r = a.call_tile_region[t];
+  const RegionDev g = a.regions[r];
+  const int32_t p0 = (t - g.call_tile0) * kCallTile + kBrkPer * threadIdx.x;
+  const bool reads = a.stats[r].read_count > 0;
+  long long fr = 0, bad = 0, cov = 0;
+#pragma unroll
+  for (int q = 0; q < kBrkPer; q++) {
+    const int32_t p = p0 + q;
+    if (p < g.size) {
+      const int64_t gp = g.pos_base + p;
+      const int4 c = a.rec.count[gp];
+      const int32_t depth = wadd(wadd(wadd(c.x, c.y), wadd(c.z, c.w)), a.rec.deletions[gp]);
+      a.frag[gp] = depth;
+      fr += depth;
+      if (reads) {  // postProcess leaves coverage and badCoverage at 0 for a region without reads
+        cov += depth;
+        bad += a.rec.bad_pair[gp];
+      }
+    }
+  }
+  fr = block_sum(fr, s_red);
+  if (threadIdx.x == 0) atomicAdd((unsigned long long*)&a.sums[3 * r], (unsigned long long)fr);
+  bad = block_sum(bad, s_red);
+  if (threadIdx.x == 0) atomicAdd((unsigned long long*)&a.sums[3 * r + 1], (unsigned long long)bad);
+  cov = block_sum(cov, s_red);
+  if (threadIdx.x == 0) atomicAdd((unsigned long long*)&a.sums[3 * r + 2], (unsigned long long)cov);
+}
+
+__global__ void __launch_bounds__(kCallTile) k_brk_spans(BreakArgs a) {
+  const int32_t t = a.tile_begin + blockIdx.x;
+  const int32_t r = a.call_tile_region[t];
+  const RegionDev g = a.regions[r];
+  const int32_t p = (t - g.call_tile0) * kCallTile + threadIdx.x;
+  if (p >= g.size) return;
+  const int64_t gp = g.pos_base + p;
+  if (!is_del_change(a.rec.call[gp])) return;
+  const int32_t len = a.rec.indel_len[gp], d = a.rec.deletions[gp];
+  long long total = 0;
+  for (int32_t k = 1; k < len && p + k < g.size; k++) {
+    atomicSub(&a.frag[gp + k], d);
+    total += d;
+  }
+  if (total) atomicAdd((unsigned long long*)&a.sums[3 * r], (unsigned long long)(-total));
+}
+
+// Exclusive max-scan over the block of v (>= -1); returns the maximum of the
+// values of lower threads, -1 when none.
+__device__ inline int32_t block_prev_max(int32_t v, int32_t* s_warp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t y = __shfl_up_sync(FULL, x, o);
+    if (lane >= o) x = max(x, y);
+  }
+  const int32_t excl_in_warp = __shfl_up_sync(FULL, x, 1);
+  __syncthreads();
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int32_t w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : -1;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t y = __shfl_up_sync(FULL, w, o);
+      if (lane >= o) w = max(w, y);
+    }
+    s_warp[lane] = w;  // inclusive maximum of warps 0..lane
+  }
+  __syncthreads();
+  int32_t prev = warp > 0 ? s_warp[warp - 1] : -1;
+  if (lane > 0) prev = max(prev, excl_in_warp);
+  return prev;
+}
+
+__global__ void __launch_bounds__(kBrkThreads) k_brk_tiles(BreakArgs a) {
+  __shared__ int32_t s_warp[32];
+  __shared__ int32_t s_cnt[2];
+  const int32_t t = a.tile_begin + blockIdx.x;
+  const int32_t r = a.call_tile_region[t];
+  const RegionDev g = a.regions[r];
+  const int32_t p0 = (t - g.call_tile0) * kCallTile + kBrkPer * threadIdx.x;
+  const int64_t base = g.pos_base;
+  const bool reads = a.stats[r].read_count > 0;
+  const int32_t mmd = a.min_min_depth;
+  const long long sbad = a.sums[3 * r + 1], sgood = a.sums[3 * r + 2];
+  const long long pbo = roundDivL(100 * sbad, sgood + sbad);
+  const double mean = (double)a.sums[3 * r] / (double)g.size;
+  uint32_t tb = 0, tn = 0;  // bit q: position p0 + q passes the break test / is N
+#pragma unroll
+  for (int q = 0; q < kBrkPer; q++) {
+    const int32_t p = p0 + q;
+    if (p < g.size) {
+      const int64_t gp = base + p;
+      uint8_t rb = a.ref[g.ref_off + g.start - 1 + p];
+      if (rb >= 'a' && rb <= 'z') rb -= 32;
+      const bool isN = rb == 'N';
+      const int4 c = a.rec.count[gp];
+      const int32_t depth = wadd(wadd(wadd(c.x, c.y), wadd(c.z, c.w)), a.rec.deletions[gp]);
+      const int32_t cov = reads ? depth : 0;
+      const int32_t bad = reads ? a.rec.bad_pair[gp] : 0;
+      const int32_t clips = reads ? (int32_t)(int16_t)a.rec.clips[gp] : 0;  // pu.clips.toShort
+      const bool lowCov = cov < mmd && !isN;
+      const bool highClip = cov >= mmd && pctI(clips, cov) >= 33;
+      const bool tooBad = (long long)pctI(bad, wadd(cov, bad)) > pbo + 20;
+      const int32_t left = a.frag[base + max(0, p - 100)], right = a.frag[base + min(g.size - 1, p + 100)];
+      const int32_t center = a.frag[gp];
+      const double dipF = (double)wadd(wsub(left, center), wsub(right, center)) / mean;
+      if (lowCov || highClip || tooBad || dipF >= 1.5) tb |= 1u << q;
+      if (isN) tn |= 1u << q;
+    }
+  }
+  BreakTile& T = a.tiles[t];
+  if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int32_t slop = k == 0 ? 200 : 100;
+    const uint32_t bits = k == 0 ? tb : tn;
+    // the thread's last tested position, and the last one of the lower threads
+    const int32_t mine = bits ? p0 + 31 - __clz(bits) : -1;
+    int32_t prev = block_prev_max(mine, s_warp);
+    const int32_t last = max(s_warp[(kBrkThreads >> 5) - 1], -1);
+    // a run starts inside the tile where the previous tested position is more
+    // than slop + 1 back (summaryRegions closes a run at the first untested
+    // position more than slop past its last tested one)
+#pragma unroll
+    for (int q = 0; q < kBrkPer; q++) {
+      if (!((bits >> q) & 1u)) continue;
+      const int32_t p = p0 + q;
+      if (prev < 0) {
+        T.first[k] = p;
+      } else if (p - prev > slop + 1) {
+        const int j = atomicAdd(&s_cnt[k], 1);
+        if (j < kBreakStarts) {
+          T.start[k][j] = p;
+          T.prev[k][j] = prev;
+        }
+      }
+      prev = p;
+    }
+    if (threadIdx.x == 0) {
+      T.last[k] = last;
+      if (last < 0) T.first[k] = -1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) T.n[k] = min(s_cnt[k], kBreakStarts);
+  }
+}
+
+// Sorts the (at most kBreakStarts) run starts of a tile, which the atomic slot
+// order left unordered, in place.
+__device__ inline void sort_starts(int32_t* s, int32_t* pv, int n) {
+  for (int i = 1; i < n; i++) {
+    const int32_t a = s[i], b = pv[i];
+    int j = i - 1;
+    while (j >= 0 && s[j] > a) { s[j + 1] = s[j]; pv[j + 1] = pv[j]; j--; }
+    s[j + 1] = a;
+    pv[j + 1] = b;
+  }
+}
+
+// One warp per region: the lanes test 32 tiles at a time for runs, lane 0 joins
+// the tiles that have some, in order.
+__global__ void k_brk_merge(BreakArgs a, int32_t n_regions) {
+  const int32_t r = (int32_t)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= n_regions) return;
+  const RegionDev g = a.regions[r];
+  if (a.stats[r].error) return;  // the reference threw on this region
+  int2* gaps = a.gap_scratch + (int64_t)g.call_tile0 * (kBreakStarts + 1);
+  int32_t n_gaps = 0;
+  const int32_t tend = g.call_tile0 + g.n_call_tiles;
+  // pass 0: gaps (N runs, slop 100, >= 10 bases, not near the region's ends);
+  // pass 1: breaks (slop 200, not near the ends, not near a gap)
+  for (int pass = 0; pass < 2; pass++) {
+    const int k = pass == 0 ? 1 : 0;
+    const int32_t slop = k == 0 ? 200 : 100;
+    int32_t run_first = -1, carry = -1, gp_ptr = 0;
+    auto emit = [&](int32_t f, int32_t l) {
+      if (f < 100 || (g.size - 1 - l) < 100) return;  // nearEdge: start - region.start < 100 || stop - stop < 100
+      const int32_t lf = g.start + f, ll = g.start + l;
+      if (pass == 0) {
+        if (ll + 1 - lf >= 10) gaps[n_gaps++] = make_int2(lf, ll);
+        return;
+      }
+      // Region.near(gap, 300): overlap, or an end within 300 of the other region's opposite end
+      while (gp_ptr < n_gaps && gaps[gp_ptr].y < lf - 300) gp_ptr++;
+      for (int32_t q = gp_ptr; q < n_gaps && gaps[q].x <= ll + 300; q++) {
+        const int2 G = gaps[q];
+        if ((G.x <= ll && G.y >= lf) || abs(G.y - lf) <= 300 || abs(G.x - ll) <= 300) return;
+      }
+      const unsigned long long o = atomicAdd(a.n_out, 1ull);
+      if ((int64_t)o < a.out_cap) a.out[o] = pg_break{r, lf, ll, 0};
+    };
+    for (int32_t t0 = g.call_tile0; t0 < tend; t0 += 32) {
+      const int32_t tl = t0 + lane;
+      unsigned m = __ballot_sync(FULL, tl < tend && a.tiles[tl].last[k] >= 0);
+      if (lane == 0) {
+        while (m) {
+          BreakTile& T = a.tiles[t0 + __ffs(m) - 1];
+          m &= m - 1;
+          const int32_t f0 = T.first[k];
+          if (carry < 0) run_first = f0;
+          else if (f0 - carry > slop + 1) {
+            emit(run_first, carry);
+            run_first = f0;
+          }
+          const int n = T.n[k];
+          sort_starts(T.start[k], T.prev[k], n);
+          for (int j = 0; j < n; j++) {
+            emit(run_first, T.prev[k][j]);
+            run_first = T.start[k][j];
+          }
+          carry = T.last[k];
+        }
+      }
+    }
+    if (lane == 0 && carry >= 0) emit(run_first, carry);
+    __syncwarp();
+  }
+}
+
+void launch_breaks(const BreakArgs& a, int32_t n_regions, cudaStream_t s) {
+  if (a.n_tiles <= 0) return;
+  k_brk_frag<<<a.n_tiles, kBrkThreads, 0, s>>>(a);
+  k_brk_spans<<<a.n_tiles, kCallTile, 0, s>>>(a);
+  k_brk_tiles<<<a.n_tiles, kBrkThreads, 0, s>>>(a);
+  k_brk_merge<<<(n_regions + 3) / 4, 128, 0, s>>>(a, n_regions);
+}
+
+}  // namespace pg

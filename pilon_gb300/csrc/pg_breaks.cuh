@@ -1,0 +1,33 @@
+// pg_breaks.cuh — arguments of the break-candidate kernels (pg_breaks.cu).
+#pragma once
+#include "pg_internal.cuh"
+
+namespace pg {
+
+constexpr int kBreakStarts = 12;  // run starts inside one 1024-position tile (slop 100: at most 10)
+
+struct BreakTile {                // per call tile; test 0 = break, test 1 = reference N
+  int32_t first[2], last[2], n[2];
+  int32_t start[2][kBreakStarts], prev[2][kBreakStarts];
+};
+
+struct BreakArgs {
+  const RegionDev* regions;
+  const int32_t* call_tile_region;
+  int32_t tile_begin, n_tiles;
+  Records rec;
+  const StatsDev* stats;
+  const uint8_t* ref;
+  int32_t min_min_depth;
+  int32_t* frag;                  // per position: fragCoverage
+  long long* sums;                // per region: fragCoverage, badCoverage, coverage sums
+  BreakTile* tiles;
+  int2* gap_scratch;              // per call tile kBreakStarts + 1 gap runs
+  pg_break* out;
+  int64_t out_cap;
+  unsigned long long* n_out;
+};
+
+void launch_breaks(const BreakArgs& a, int32_t n_regions, cudaStream_t s);
+
+}  // namespace pg

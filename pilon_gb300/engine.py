@@ -50,6 +50,7 @@ def lib():
                                             C.POINTER(C.c_int32)]),
             "pg_sync": (C.c_int, [vp]),
             "pg_format_vcf": (C.c_int, [vp, i32, C.c_char_p, i32, i32, i32, vp, i64, C.POINTER(C.c_int64)]),
+            "pg_find_breaks": (C.c_int, [vp, i32, vp, i64, C.POINTER(C.c_int64)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -197,6 +198,19 @@ class Engine:
         buf = np.empty(max(int(n.value), 1), np.uint8)
         self._check(self.L.pg_format_vcf(*args, buf.ctypes.data, buf.size, C.byref(n)))
         return buf[:n.value].tobytes()
+
+    def find_breaks(self, min_min_depth=5):
+        """pg_find_breaks: break candidates of every region of the last
+        pileup_regions call, as {region: [(start, stop), ...]}."""
+        n = C.c_int64()
+        self._check(self.L.pg_find_breaks(self.h, min_min_depth, None, 0, C.byref(n)))
+        buf = (_abi.pg_break * max(1, n.value))()
+        self._check(self.L.pg_find_breaks(self.h, min_min_depth, C.cast(buf, C.c_void_p), n.value, C.byref(n)))
+        out = {}
+        for k in range(n.value):
+            b = buf[k]
+            out.setdefault(int(b.region), []).append((int(b.start), int(b.stop)))
+        return out
 
     def set_reads_device(self, dev_reads, n_reads):
         """pg_set_reads_device: a read store already in device memory (pg_reads

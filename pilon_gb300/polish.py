@@ -118,11 +118,13 @@ def java_round(x):
 
 
 def summary_regions(test, start, stop, slop):
-    """GenomeRegion.summaryRegions (S/GenomeRegion.scala:743-763) on a boolean array."""
+    """GenomeRegion.summaryRegions (S/GenomeRegion.scala:743-763) on a boolean array.
+    A run closes at the first untested position more than `slop` past its last
+    tested one, so tested positions up to slop + 1 apart share a run."""
     idx = np.nonzero(test)[0]
     regs = []
     if idx.size:
-        gaps = np.nonzero(np.diff(idx) > slop)[0]
+        gaps = np.nonzero(np.diff(idx) > slop + 1)[0]
         firsts = np.concatenate([[idx[0]], idx[gaps + 1]])
         lasts = np.concatenate([idx[gaps], [idx[-1]]])
         regs = [(start + int(a), start + int(b)) for a, b in zip(firsts, lasts)]

@@ -42,6 +42,7 @@ def test_struct_layouts_match_header():
     assert C.sizeof(_abi.pg_region) == 32
     assert C.sizeof(_abi.pg_kmer_edge) == 32
     assert C.sizeof(_abi.pg_window) == 16
+    assert C.sizeof(_abi.pg_break) == 16
 
 
 def test_default_params_match_pilon():

@@ -99,3 +99,45 @@ def test_assembler_graph(engine, cfg1):
     assert len(kg) > 100
     for k, nxt in list(kg.items())[:50]:
         assert nxt[:-1] == k[1:] and len(nxt) == 21
+
+
+def _device_breaks_vs_oracle(engine, ds, regions, p):
+    engine.set_reference(ds.contigs)
+    engine.set_reads(ds.reads)
+    engine.pileup_regions(regions, p)
+    got = engine.find_breaks(p.min_min_depth)
+    total = 0
+    for r, (c, s, e, a, b) in enumerate(regions):
+        try:
+            want = oracle.region_breaks(ds.reads, p, ds.contigs[c], c, s, e, a, b)
+        except IndexError:  # the reference throws on this region: no breaks from the device either
+            want = []
+        assert got.get(r, []) == want, (r, got.get(r, [])[:5], want[:5])
+        total += len(want)
+    return total
+
+
+def test_device_breaks_match_oracle(engine, euk):
+    """pg_find_breaks (GenomeRegion.possibleBreaks on the device) on the
+    eukaryotic workload, with runs of N written into the reference so that the
+    gap rules (>= 10 bases, breaks within 300 bases of a gap dropped) apply."""
+    ds = euk
+    refs = [c.copy() for c in ds.contigs]
+    n = refs[0].size
+    rng = np.random.Generator(np.random.PCG64(11))
+    for x in rng.choice(np.arange(1000, n - 1000), size=12, replace=False).tolist():
+        refs[0][x:x + int(rng.integers(5, 60))] = ord("N")
+    from types import SimpleNamespace
+    ds2 = SimpleNamespace(contigs=refs, reads=ds.reads)
+    p = _abi.default_params()
+    regions = plan_regions(ds.reads, [c.size for c in refs], chunk_size=200_000)
+    assert _device_breaks_vs_oracle(engine, ds2, regions, p) > 0
+
+
+def test_device_breaks_many_contigs(engine):
+    ds = synth.generate(3, scale=0.02)
+    p = _abi.default_params()
+    regions = plan_regions(ds.reads, [c.size for c in ds.contigs])
+    _device_breaks_vs_oracle(engine, ds, regions, p)
+    p2 = _abi.default_params(min_min_depth=12)
+    _device_breaks_vs_oracle(engine, ds, regions, p2)

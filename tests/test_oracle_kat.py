@@ -275,3 +275,37 @@ def test_kmer_tally_hand_case():
     exp = {(key("ACG"), 3, -1, 10), (key("CGT"), 0, 3, 10), (key("GTT"), 0, -1, 5), (key("TTA"), 1, -1, 5),
            (key("TAC"), 2, -1, 5), (key("GTA"), 0, -1, 5), (key("TAA"), 1, -1, 5), (key("AAC"), 2, -1, 5)}
     assert got == exp
+
+
+def test_summary_regions_merge_rule():
+    """GenomeRegion.summaryRegions closes a run at the first untested position
+    more than slop past the last tested one (S/GenomeRegion.scala:748-757):
+    tested positions slop + 1 apart stay in one run, slop + 2 apart split."""
+    from pilon_gb300.polish import summary_regions
+
+    def scala(test, start, stop, slop):  # the loop as written in the reference
+        regs, first, last = [], -1, -1
+        for i in range(test.size):
+            if test[i]:
+                last = i
+                if first < 0:
+                    first = i
+            elif last >= 0 and i > last + slop:
+                regs.append((start + first, start + last))
+                first = last = -1
+        if last >= 0:
+            regs.append((start + first, start + last))
+        return [r for r in regs if not (r[0] - start < 100 or stop - r[1] < 100)]
+
+    n = 2000
+    for gap in (199, 200, 201, 202, 203):
+        t = np.zeros(n, bool)
+        t[[500, 500 + gap, 1500]] = True
+        got = summary_regions(t, 1, n, 200)
+        assert got == scala(t, 1, n, 200), gap
+    assert summary_regions(np.isin(np.arange(n), [500, 701]), 1, n, 200) == [(501, 702)]
+    assert summary_regions(np.isin(np.arange(n), [500, 702]), 1, n, 200) == [(501, 501), (703, 703)]
+    rng = np.random.Generator(np.random.PCG64(7))
+    for _ in range(50):
+        t = rng.random(n) < 0.004
+        assert summary_regions(t, 1, n, 100) == scala(t, 1, n, 100)
