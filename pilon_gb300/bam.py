@@ -1,0 +1,158 @@
+"""BAM input and output for the packed read store.
+
+read_bam is the host side of BamFile's input (S/BamFile.scala:117-126, which
+htsjdk decodes): the BGZF blocks of the file are inflated on parallel threads
+(zlib releases the interpreter lock) into one buffer, and libpg_bam.so splits
+the record stream into the structure-of-arrays store of the C ABI, keeping
+BAM's CIGAR words, 4-bit bases and qualities as they are.  write_bam writes a
+store as a coordinate-sorted BAM (read names r<index>, no tags), for tests and
+the benchmark.
+"""
+import ctypes as C
+import os
+import struct
+import zlib
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+from .reads import ReadStore
+
+BGZF_EOF = bytes.fromhex("1f8b08040000000000ff0600424302001b0003000000000000000000")
+_BLOCK = 65280  # uncompressed bytes per BGZF block
+_LIB = None
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        from .build import BAMLIB, build
+        if not os.path.exists(BAMLIB):
+            build()
+        L = C.CDLL(BAMLIB)
+        vp, i64 = C.c_void_p, C.c_int64
+        L.bam_count.restype = i64
+        L.bam_count.argtypes = [vp, i64, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]
+        L.bam_parse.restype = i64
+        L.bam_parse.argtypes = [vp, i64] + [vp] * 15
+        L.bam_encoded_size.restype = i64
+        L.bam_encoded_size.argtypes = [i64, vp, vp]
+        L.bam_encode.restype = i64
+        L.bam_encode.argtypes = [i64] + [vp] * 16
+        _LIB = L
+    return _LIB
+
+
+def _threads(threads):
+    return threads or min(32, os.cpu_count() or 1)
+
+
+def _bgzf_block(data):
+    c = zlib.compressobj(1, zlib.DEFLATED, -15)
+    cdata = c.compress(data) + c.flush()
+    bsize = 18 + len(cdata) + 8 - 1
+    head = struct.pack("<BBBBIBBHBBHH", 0x1F, 0x8B, 8, 4, 0, 0, 0xFF, 6, 66, 67, 2, bsize)
+    return head + cdata + struct.pack("<II", zlib.crc32(data) & 0xFFFFFFFF, len(data))
+
+
+def write_bam(path, names, lengths, reads, threads=None):
+    """Writes `reads` (a ReadStore sorted by reference and position) as BAM."""
+    text = "@HD\tVN:1.6\tSO:coordinate\n" + "".join(f"@SQ\tSN:{n}\tLN:{l}\n" for n, l in zip(names, lengths))
+    tb = text.encode()
+    hdr = bytearray(b"BAM\x01" + struct.pack("<i", len(tb)) + tb + struct.pack("<i", len(names)))
+    for n, l in zip(names, lengths):
+        nb = n.encode() + b"\0"
+        hdr += struct.pack("<i", len(nb)) + nb + struct.pack("<i", int(l))
+    r = reads
+    L = _lib()
+    n = r.n_reads
+    size = L.bam_encoded_size(n, r.n_cigar.ctypes.data, r.l_seq.ctypes.data)
+    recs = np.empty(max(size, 1), np.uint8)
+    L.bam_encode(n, r.pos.ctypes.data, r.tlen.ctypes.data, r.ref_id.ctypes.data, r.mate_ref_id.ctypes.data,
+                 r.l_seq.ctypes.data, r.flag.ctypes.data, r.n_cigar.ctypes.data, r.mapq.ctypes.data,
+                 r.seq.ctypes.data, r.qual.ctypes.data, r.cigar_off.ctypes.data, r.seq_off.ctypes.data,
+                 r.qual_off.ctypes.data, r.cigar.ctypes.data, None, recs.ctypes.data)
+    payload = memoryview(bytes(hdr) + recs[:size].tobytes())
+    chunks = [payload[k:k + _BLOCK] for k in range(0, len(payload), _BLOCK)]
+    with ThreadPoolExecutor(_threads(threads)) as ex:
+        blocks = list(ex.map(lambda ch: _bgzf_block(bytes(ch)), chunks))
+    with open(path, "wb") as f:
+        for b in blocks:
+            f.write(b)
+        f.write(BGZF_EOF)
+
+
+def _blocks(raw):
+    """(cdata offset, cdata end, uncompressed size) of every BGZF block."""
+    out, off, n = [], 0, len(raw)
+    while off < n:
+        if off + 18 > n or raw[off] != 0x1F or raw[off + 1] != 0x8B or raw[off + 3] & 4 == 0:
+            raise ValueError(f"not a BGZF block at byte {off}")
+        xlen = struct.unpack_from("<H", raw, off + 10)[0]
+        x, bsize = off + 12, None
+        if off + 12 + xlen > n:
+            raise ValueError(f"BGZF block at byte {off} is truncated")
+        while x + 4 <= off + 12 + xlen:
+            si1, si2, slen = raw[x], raw[x + 1], struct.unpack_from("<H", raw, x + 2)[0]
+            if si1 == 66 and si2 == 67 and slen == 2:
+                bsize = struct.unpack_from("<H", raw, x + 4)[0]
+            x += 4 + slen
+        if bsize is None:
+            raise ValueError(f"BGZF block at byte {off} has no BC field")
+        end = off + bsize + 1
+        if end > n or end - 8 < off + 12 + xlen:
+            raise ValueError(f"BGZF block at byte {off} is truncated")
+        isize = struct.unpack_from("<I", raw, end - 4)[0]
+        out.append((off + 12 + xlen, end - 8, isize))
+        off = end
+    return out
+
+
+def read_bam(path, threads=None):
+    """Returns (reference names, reference lengths, ReadStore) of a BAM file."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    blocks = _blocks(raw)
+    sizes = np.array([b[2] for b in blocks], np.int64)
+    starts = np.concatenate([[0], np.cumsum(sizes)])
+    data = np.empty(int(starts[-1]), np.uint8)
+
+    def inflate(k):
+        a, b, isize = blocks[k]
+        if isize:
+            out = zlib.decompress(raw[a:b], -15)
+            if len(out) != isize:
+                raise ValueError(f"BGZF block {k}: {len(out)} bytes, header says {isize}")
+            data[starts[k]:starts[k] + isize] = np.frombuffer(out, np.uint8)
+    with ThreadPoolExecutor(_threads(threads)) as ex:
+        list(ex.map(inflate, range(len(blocks))))
+    view = memoryview(data)
+    if bytes(view[:4]) != b"BAM\x01":
+        raise ValueError("not a BAM file")
+    l_text = struct.unpack_from("<i", view, 4)[0]
+    off = 8 + l_text
+    n_ref = struct.unpack_from("<i", view, off)[0]
+    off += 4
+    names, lengths = [], []
+    for _ in range(n_ref):
+        ln = struct.unpack_from("<i", view, off)[0]
+        names.append(bytes(view[off + 4:off + 4 + ln - 1]).decode())
+        lengths.append(struct.unpack_from("<i", view, off + 4 + ln)[0])
+        off += 8 + ln
+    L = _lib()
+    recs = data[off:]
+    nc, sb, qb = C.c_int64(), C.c_int64(), C.c_int64()
+    n = L.bam_count(recs.ctypes.data, recs.size, C.byref(nc), C.byref(sb), C.byref(qb))
+    if n < 0:
+        raise ValueError(f"BAM record at stream byte {off - 1 - n} runs past the end of the file")
+    st = ReadStore(pos=np.empty(n, np.int32), aend=np.empty(n, np.int32), flag=np.empty(n, np.uint16),
+                   mapq=np.empty(n, np.uint8), tlen=np.empty(n, np.int32), ref_id=np.empty(n, np.int32),
+                   mate_ref_id=np.empty(n, np.int32), cigar_off=np.empty(n, np.int64),
+                   n_cigar=np.empty(n, np.uint16), cigar=np.empty(nc.value, np.uint32),
+                   seq_off=np.empty(n, np.int64), l_seq=np.empty(n, np.int32), seq=np.empty(sb.value, np.uint8),
+                   qual_off=np.empty(n, np.int64), qual=np.empty(qb.value, np.uint8))
+    L.bam_parse(recs.ctypes.data, recs.size, st.pos.ctypes.data, st.aend.ctypes.data, st.tlen.ctypes.data,
+                st.ref_id.ctypes.data, st.mate_ref_id.ctypes.data, st.l_seq.ctypes.data, st.flag.ctypes.data,
+                st.n_cigar.ctypes.data, st.mapq.ctypes.data, st.seq.ctypes.data, st.qual.ctypes.data,
+                st.cigar_off.ctypes.data, st.seq_off.ctypes.data, st.qual_off.ctypes.data, st.cigar.ctypes.data)
+    return names, lengths, st

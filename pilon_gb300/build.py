@@ -2,6 +2,7 @@
 
 libpilon_gb300.so — the CUDA engine and its C ABI, sm_103a only.
 libpg_synth.so    — the host-side read simulator used by the benchmark.
+libpg_bam.so      — BAM records <-> the packed read store (host).
 
 Everything is compiled in-tree into pilon_gb300/_build/ with nvcc / g++
 directly (no cmake), the translation units in parallel.
@@ -18,6 +19,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ENGINE = os.path.join(BUILD, "libpilon_gb300.so")
 SYNTH = os.path.join(BUILD, "libpg_synth.so")
+BAMLIB = os.path.join(BUILD, "libpg_bam.so")
 
 CU_SOURCES = ["pg_api.cu", "pg_pileup.cu", "pg_call.cu", "pg_kmer.cu", "pg_format.cu", "pg_noalloc.cu",
               "pg_breaks.cu"]
@@ -51,7 +53,7 @@ def _run_all(cmds):
 
 
 def build(force=False, verbose=False):
-    """Compiles the engine and the simulator; returns the engine path."""
+    """Compiles the engine, the simulator and the BAM codec; returns the engine path."""
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(INCLUDE, "pilon_gb300.h")] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".cuh")]
     nvcc = _nvcc()
@@ -65,6 +67,9 @@ def build(force=False, verbose=False):
     synth_src = os.path.join(CSRC, "synth.cpp")
     if force or not _newer(SYNTH, [synth_src]):
         cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", synth_src, "-o", SYNTH])
+    bam_src = os.path.join(CSRC, "bam.cpp")
+    if force or not _newer(BAMLIB, [bam_src]):
+        cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", bam_src, "-o", BAMLIB])
     if cmds:
         if verbose:
             for c in cmds:
