@@ -239,9 +239,18 @@ def kmer_bench(eng, ds, params, args, threads, K=31, radius=500):
         edges = eng.kmer_tally(wins, K, params)
         t.append(time.perf_counter() - t0)
     sec = sum(t) / len(t)
+    # the same tally over one window per device break candidate, built on the device
+    eng.pileup_regions(ds_regions(ds), params, batched=True)
+    tb = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        nwb, eb = eng.kmer_tally_breaks(K, params, radius=radius)
+        tb.append(time.perf_counter() - t0)
+    from_breaks = {"windows": nwb, "edges": int(len(eb)), "ms_per_call": 1e3 * min(tb),
+                   "timing": "host wall clock of pg_kmer_tally_breaks (windows built on the device)"}
     out = {"windows": len(wins), "K": K, "kmer_events": events, "edges": int(len(edges)),
            "ms_per_call": 1e3 * sec, "value": events / sec / 1e9, "unit": "G K-mer events/s",
-           "timing": "host wall clock of pg_kmer_tally, edges read back"}
+           "timing": "host wall clock of pg_kmer_tally, edges read back", "from_device_breaks": from_breaks}
     if not args.no_cpu:
         sample = wins[: max(1, min(len(wins), 16 * threads))]
         parts = [sample[k::threads] for k in range(threads)]
@@ -272,6 +281,11 @@ def kmer_bench(eng, ds, params, args, threads, K=31, radius=500):
                                                          f"threads"}
         out["sample_edges_identical"] = edge_set(got, lambda w: w) == want
     return out
+
+
+def ds_regions(ds):
+    from pilon_gb300.regions import plan_regions
+    return plan_regions(ds.reads, [c.size for c in ds.contigs])
 
 
 def dist_init():

@@ -265,6 +265,18 @@ pg_status pg_format_vcf(pg_ctx *ctx, int32_t region, const char *name, int32_t d
  * none. */
 pg_status pg_find_breaks(pg_ctx *ctx, int32_t min_min_depth, pg_break *out, int64_t cap, int64_t *n_breaks);
 
+/* The K-mer tally of pg_kmer_tally over one window per break of
+ * pg_find_breaks(min_min_depth), built on the device without a host round
+ * trip: window k holds the reads of break k's contig that start in
+ * [start - radius - S, stop + radius], S the longest alignment span of the
+ * read store (every read overlapping [start - radius, stop + radius] and a
+ * few that end before it).  This stands in for GapFiller's read recruitment
+ * (S/GapFiller.scala:364-402) without mate rescue.  *n_windows receives the
+ * number of breaks. */
+pg_status pg_kmer_tally_breaks(pg_ctx *ctx, int32_t min_min_depth, int32_t radius, int32_t K,
+                               const pg_params *params, int32_t min_depth, pg_kmer_edge *edges, int64_t cap,
+                               int64_t *n_windows, int64_t *n_edges);
+
 /* ---- timing -------------------------------------------------------------
  * Milliseconds of the dominant (pileup walk) kernel in the last
  * pg_pileup_regions call, measured with CUDA events on the context stream,

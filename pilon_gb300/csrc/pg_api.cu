@@ -67,7 +67,7 @@ struct pg_ctx {
   // VCF formatting
   DevBuf vlen, vsums, vtext, vname;
   // break candidates
-  DevBuf bfrag, bsums, btiles, bgaps, bout, bcount;
+  DevBuf bfrag, bsums, btiles, bgaps, bruns, bcnt, boff, bout;
   int64_t brk_n = -1;             // breaks of the last pileup call on the device, -1: not found yet
   int32_t brk_mmd = 0;
   // CUDA graph of the batched pipeline, replayed while the plan and buffers are unchanged
@@ -237,8 +237,8 @@ void pg_close(pg_ctx* c) {
   DevBuf* km[] = {&c->kwin, &c->kpre, &c->kslot_base, &c->kslot_cap, &c->kx_base, &c->kx_cap, &c->kkeys, &c->kcnt,
                   &c->kqs, &c->kmq, &c->kq, &c->kx_keys, &c->kx_used, &c->kx_cnt, &c->kx_qs, &c->kx_mq, &c->kx_q,
                   &c->kedges, &c->kcount, &c->kx_ev, &c->kx_evbase, &c->kx_evcap, &c->kx_evfill, &c->vlen,
-                  &c->vsums, &c->vtext, &c->vname, &c->bfrag, &c->bsums, &c->btiles, &c->bgaps, &c->bout,
-                  &c->bcount};
+                  &c->vsums, &c->vtext, &c->vname, &c->bfrag, &c->bsums, &c->btiles, &c->bgaps, &c->bruns,
+                  &c->bcnt, &c->boff, &c->bout};
   for (DevBuf* b : km) release(*b);
   for (auto& b : c->rec_i32) release(b);
   for (auto& b : c->rd) release(b);
@@ -705,6 +705,9 @@ static int64_t next_pow2(int64_t x) {
   return p;
 }
 
+static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_params* params, int32_t min_depth,
+                           pg_kmer_edge* edges, int64_t cap, int64_t* n_edges);
+
 pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K, const pg_params* params,
                         int32_t min_depth, pg_kmer_edge* edges, int64_t cap, int64_t* n_edges) {
   if (!c || (n_windows > 0 && !windows) || !params || n_windows < 0 || cap < 0 || !n_edges)
@@ -719,11 +722,18 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
   for (int32_t w = 0; w < n_windows; w++)
     if (windows[w].read_begin < 0 || windows[w].read_end < windows[w].read_begin || windows[w].read_end > c->R.n)
       return fail(c, PG_ERR_ARG, "window %d: read range out of bounds", w);
-  cudaStream_t st = c->stream;
   pg_status s;
   if ((s = ensure(c, c->kwin, sizeof(pg_window) * n_windows))) return s;
+  CK(cudaMemcpyAsync(c->kwin.p, windows, sizeof(pg_window) * n_windows, cudaMemcpyHostToDevice, c->stream));
+  return kmer_core(c, n_windows, K, params, min_depth, edges, cap, n_edges);
+}
+
+// The tally over the n_windows windows in c->kwin (device).
+static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_params* params, int32_t min_depth,
+                           pg_kmer_edge* edges, int64_t cap, int64_t* n_edges) {
+  cudaStream_t st = c->stream;
+  pg_status s;
   if ((s = ensure(c, c->kpre, sizeof(long long) * 3 * n_windows))) return s;
-  CK(cudaMemcpyAsync(c->kwin.p, windows, sizeof(pg_window) * n_windows, cudaMemcpyHostToDevice, st));
   launch_kmer_prepass(c->R, P<pg_window>(c->kwin), n_windows, K, P<long long>(c->kpre), st);
   std::vector<long long> pre(3 * (size_t)n_windows);
   CK(cudaMemcpyAsync(pre.data(), c->kpre.p, sizeof(long long) * pre.size(), cudaMemcpyDeviceToHost, st));
@@ -824,66 +834,79 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
   return PG_OK;
 }
 
+// Finds the breaks of the last pileup call on the device (once per call and
+// min_min_depth); they stay in c->bout, ordered by region and position.
+static pg_status find_breaks_device(pg_ctx* c, int32_t min_min_depth) {
+  if (c->brk_n >= 0 && c->brk_mmd == min_min_depth) return PG_OK;
+  cudaStream_t st = c->stream;
+  pg_status s;
+  const size_t runs = (size_t)c->n_call_tiles * (kBreakStarts + 1);
+  if ((s = ensure(c, c->bfrag, 4 * (size_t)std::max<int64_t>(c->n_positions, 1)))) return s;
+  if ((s = ensure(c, c->bsums, 24 * (size_t)c->n_regions))) return s;
+  if ((s = ensure(c, c->btiles, sizeof(BreakTile) * (size_t)c->n_call_tiles))) return s;
+  if ((s = ensure(c, c->bgaps, sizeof(int2) * runs))) return s;
+  if ((s = ensure(c, c->bruns, sizeof(int2) * runs))) return s;
+  if ((s = ensure(c, c->bcnt, 4 * ((size_t)c->n_regions + 1)))) return s;
+  if ((s = ensure(c, c->boff, 4 * ((size_t)c->n_regions + 1)))) return s;
+  if ((s = ensure(c, c->bout, sizeof(pg_break) * runs))) return s;
+  CK(cudaMemsetAsync(c->bsums.p, 0, 24 * (size_t)c->n_regions, st));
+  CK(cudaMemsetAsync(c->bcnt.p, 0, 4 * ((size_t)c->n_regions + 1), st));
+  BreakArgs a;
+  a.regions = P<RegionDev>(c->regions); a.call_tile_region = P<int32_t>(c->call_tile_region);
+  a.tile_begin = 0; a.n_tiles = c->n_call_tiles; a.rec = records(c); a.stats = P<StatsDev>(c->stats);
+  a.ref = P<uint8_t>(c->ref); a.min_min_depth = min_min_depth; a.frag = P<int32_t>(c->bfrag);
+  a.sums = P<long long>(c->bsums); a.tiles = P<BreakTile>(c->btiles); a.gap_scratch = P<int2>(c->bgaps);
+  a.brk_scratch = P<int2>(c->bruns); a.brk_count = P<int32_t>(c->bcnt); a.brk_off = P<int32_t>(c->boff);
+  a.out = P<pg_break>(c->bout);
+  launch_breaks(a, c->n_regions, st);
+  CK(cudaGetLastError());
+  int32_t n = 0;
+  CK(cudaMemcpyAsync(&n, P<int32_t>(c->boff) + c->n_regions, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  c->brk_n = n;
+  c->brk_mmd = min_min_depth;
+  return PG_OK;
+}
+
 pg_status pg_find_breaks(pg_ctx* c, int32_t min_min_depth, pg_break* out, int64_t cap, int64_t* n_breaks) {
   if (!c || !n_breaks || cap < 0 || (cap > 0 && !out)) return fail(c, PG_ERR_ARG, "bad arguments");
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no pileup results: call pg_pileup_regions first");
   cudaSetDevice(c->device);
   *n_breaks = 0;
   if (c->n_regions == 0 || c->n_call_tiles == 0) return PG_OK;
-  cudaStream_t st = c->stream;
-  pg_status s;
-  unsigned long long n = 0;
-  if (c->brk_n >= 0 && c->brk_mmd == min_min_depth) {  // found already: only copy out
-    n = (unsigned long long)c->brk_n;
-    goto copy_out;
-  }
-  {
-  const int64_t dev_cap = std::max<int64_t>(cap, 1024);
-  if ((s = ensure(c, c->bfrag, 4 * (size_t)std::max<int64_t>(c->n_positions, 1)))) return s;
-  if ((s = ensure(c, c->bsums, 24 * (size_t)c->n_regions))) return s;
-  if ((s = ensure(c, c->btiles, sizeof(BreakTile) * (size_t)c->n_call_tiles))) return s;
-  if ((s = ensure(c, c->bgaps, sizeof(int2) * (size_t)c->n_call_tiles * (kBreakStarts + 1)))) return s;
-  if ((s = ensure(c, c->bout, sizeof(pg_break) * (size_t)dev_cap))) return s;
-  if ((s = ensure(c, c->bcount, 16))) return s;
-  CK(cudaMemsetAsync(c->bsums.p, 0, 24 * (size_t)c->n_regions, st));
-  CK(cudaMemsetAsync(c->bcount.p, 0, 16, st));
-  BreakArgs a;
-  a.regions = P<RegionDev>(c->regions); a.call_tile_region = P<int32_t>(c->call_tile_region);
-  a.tile_begin = 0; a.n_tiles = c->n_call_tiles; a.rec = records(c); a.stats = P<StatsDev>(c->stats);
-  a.ref = P<uint8_t>(c->ref); a.min_min_depth = min_min_depth; a.frag = P<int32_t>(c->bfrag);
-  a.sums = P<long long>(c->bsums); a.tiles = P<BreakTile>(c->btiles); a.gap_scratch = P<int2>(c->bgaps);
-  a.out = P<pg_break>(c->bout); a.out_cap = dev_cap; a.n_out = P<unsigned long long>(c->bcount);
-  launch_breaks(a, c->n_regions, st);
-  CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(&n, c->bcount.p, 8, cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  if ((int64_t)n > dev_cap) {  // more than the device buffer held: run again with room for all
-    if ((s = ensure(c, c->bout, sizeof(pg_break) * (size_t)n))) return s;
-    CK(cudaMemsetAsync(c->bsums.p, 0, 24 * (size_t)c->n_regions, st));
-    CK(cudaMemsetAsync(c->bcount.p, 0, 16, st));
-    a.out = P<pg_break>(c->bout);
-    a.out_cap = (int64_t)n;
-    launch_breaks(a, c->n_regions, st);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(&n, c->bcount.p, 8, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-  }
-  c->brk_n = (int64_t)n;
-  c->brk_mmd = min_min_depth;
-  }
-copy_out:
-  *n_breaks = (int64_t)n;
-  if (cap > 0 && n > 0) {
-    std::vector<pg_break> all((size_t)n);
-    CK(cudaMemcpyAsync(all.data(), c->bout.p, sizeof(pg_break) * (size_t)n, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    // the kernel appends in any order; the reference lists them by region, then position
-    std::sort(all.begin(), all.end(), [](const pg_break& x, const pg_break& y) {
-      return x.region != y.region ? x.region < y.region : x.start < y.start;
-    });
-    std::copy(all.begin(), all.begin() + std::min<int64_t>((int64_t)n, cap), out);
+  pg_status s = find_breaks_device(c, min_min_depth);
+  if (s) return s;
+  *n_breaks = c->brk_n;
+  const int64_t ncopy = std::min<int64_t>(c->brk_n, cap);
+  if (ncopy > 0) {
+    CK(cudaMemcpyAsync(out, c->bout.p, sizeof(pg_break) * (size_t)ncopy, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
   }
   return PG_OK;
+}
+
+pg_status pg_kmer_tally_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius, int32_t K, const pg_params* params,
+                               int32_t min_depth, pg_kmer_edge* edges, int64_t cap, int64_t* n_windows,
+                               int64_t* n_edges) {
+  if (!c || !params || cap < 0 || !n_edges || !n_windows || radius < 0) return fail(c, PG_ERR_ARG, "bad arguments");
+  if (K < 1 || K > 31) return fail(c, PG_ERR_LIMIT, "K = %d: the GPU tally packs K-mers in 64 bits (K <= 31)", K);
+  if (min_depth < 1) return fail(c, PG_ERR_ARG, "min_depth must be >= 1");
+  if (params->min_qual < 0) return fail(c, PG_ERR_ARG, "min_qual must be >= 0");
+  if (!c->have_results) return fail(c, PG_ERR_STATE, "no pileup results: call pg_pileup_regions first");
+  cudaSetDevice(c->device);
+  *n_edges = 0;
+  *n_windows = 0;
+  if (c->n_regions == 0 || c->n_call_tiles == 0) return PG_OK;
+  pg_status s = find_breaks_device(c, min_min_depth);
+  if (s) return s;
+  const int32_t n = (int32_t)c->brk_n;
+  *n_windows = n;
+  if (n == 0) return PG_OK;
+  if ((s = ensure(c, c->kwin, sizeof(pg_window) * (size_t)n))) return s;
+  launch_break_windows(c->R, P<RegionDev>(c->regions), P<pg_break>(c->bout), n, radius, P<ReadExtent>(c->d_ext),
+                       P<pg_window>(c->kwin), c->stream);
+  CK(cudaGetLastError());
+  return kmer_core(c, n, K, params, min_depth, edges, cap, n_edges);
 }
 
 pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid, int32_t vcf_qe,

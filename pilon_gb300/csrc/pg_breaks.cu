@@ -14,6 +14,9 @@
 //   k_brk_merge   one warp per region: joins the tiles' runs in order, drops
 //                 runs near the region's ends, keeps N runs of >= 10 bases as
 //                 gaps and drops breaks near a gap (Region.near, 300 bases)
+//   k_brk_compact the regions' breaks, placed by a scan of their counts: one
+//                 list by region, then position
+//   k_brk_windows the K-mer tally's read range of each break
 #include <cuda_runtime.h>
 
 #include "pg_breaks.cuh"
@@ -212,7 +215,7 @@ __global__ void k_brk_merge(BreakArgs a, int32_t n_regions) {
   const RegionDev g = a.regions[r];
   if (a.stats[r].error) return;  // the reference threw on this region
   int2* gaps = a.gap_scratch + (int64_t)g.call_tile0 * (kBreakStarts + 1);
-  int32_t n_gaps = 0;
+  int32_t n_gaps = 0, n_brk = 0;
   const int32_t tend = g.call_tile0 + g.n_call_tiles;
   // pass 0: gaps (N runs, slop 100, >= 10 bases, not near the region's ends);
   // pass 1: breaks (slop 200, not near the ends, not near a gap)
@@ -233,8 +236,7 @@ __global__ void k_brk_merge(BreakArgs a, int32_t n_regions) {
         const int2 G = gaps[q];
         if ((G.x <= ll && G.y >= lf) || abs(G.y - lf) <= 300 || abs(G.x - ll) <= 300) return;
       }
-      const unsigned long long o = atomicAdd(a.n_out, 1ull);
-      if ((int64_t)o < a.out_cap) a.out[o] = pg_break{r, lf, ll, 0};
+      a.brk_scratch[(int64_t)g.call_tile0 * (kBreakStarts + 1) + n_brk++] = make_int2(lf, ll);
     };
     for (int32_t t0 = g.call_tile0; t0 < tend; t0 += 32) {
       const int32_t tl = t0 + lane;
@@ -262,6 +264,42 @@ __global__ void k_brk_merge(BreakArgs a, int32_t n_regions) {
     if (lane == 0 && carry >= 0) emit(run_first, carry);
     __syncwarp();
   }
+  if (lane == 0) a.brk_count[r] = n_brk;
+}
+
+// One warp per region: its breaks into the region's place of the ordered list.
+__global__ void k_brk_compact(BreakArgs a, int32_t n_regions) {
+  const int32_t r = (int32_t)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= n_regions) return;
+  const RegionDev g = a.regions[r];
+  const int32_t n = a.brk_off[r + 1] - a.brk_off[r];
+  const int2* src = a.brk_scratch + (int64_t)g.call_tile0 * (kBreakStarts + 1);
+  for (int32_t k = lane; k < n; k += 32) a.out[a.brk_off[r] + k] = pg_break{r, src[k].x, src[k].y, 0};
+}
+
+__device__ inline int64_t lower_bound_i32(const int32_t* v, int64_t lo, int64_t hi, int64_t x) {
+  while (lo < hi) {
+    const int64_t m = (lo + hi) >> 1;
+    if ((int64_t)v[m] < x) lo = m + 1; else hi = m;
+  }
+  return lo;
+}
+
+__global__ void k_brk_windows(Reads R, const RegionDev* regions, const pg_break* brk, int32_t n, int32_t radius,
+                              const ReadExtent* ext, pg_window* out) {
+  const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const pg_break b = brk[k];
+  const RegionDev g = regions[b.region];
+  // the contig's reads: ref_id is sorted
+  const int64_t clo = lower_bound_i32(R.ref_id, 0, R.n, g.contig);
+  const int64_t chi = lower_bound_i32(R.ref_id, clo, R.n, (int64_t)g.contig + 1);
+  const int64_t qs = max((int64_t)b.start - radius, (int64_t)0);
+  const int64_t qe = min((int64_t)b.stop + radius, g.contig_len);
+  const int64_t a0 = lower_bound_i32(R.pos, clo, chi, qs - ext->max_span);
+  const int64_t a1 = lower_bound_i32(R.pos, a0, chi, qe + 1);  // positions <= qe
+  out[k] = pg_window{a0, a1};
 }
 
 void launch_breaks(const BreakArgs& a, int32_t n_regions, cudaStream_t s) {
@@ -270,6 +308,14 @@ void launch_breaks(const BreakArgs& a, int32_t n_regions, cudaStream_t s) {
   k_brk_spans<<<a.n_tiles, kCallTile, 0, s>>>(a);
   k_brk_tiles<<<a.n_tiles, kBrkThreads, 0, s>>>(a);
   k_brk_merge<<<(n_regions + 3) / 4, 128, 0, s>>>(a, n_regions);
+  launch_scan_small(a.brk_count, a.brk_off, n_regions, s);
+  k_brk_compact<<<(n_regions + 3) / 4, 128, 0, s>>>(a, n_regions);
+}
+
+void launch_break_windows(const Reads& R, const RegionDev* regions, const pg_break* brk, int32_t n,
+                          int32_t radius, const ReadExtent* ext, pg_window* out, cudaStream_t s) {
+  if (n <= 0) return;
+  k_brk_windows<<<(n + 127) / 128, 128, 0, s>>>(R, regions, brk, n, radius, ext, out);
 }
 
 }  // namespace pg

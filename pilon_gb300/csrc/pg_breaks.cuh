@@ -23,11 +23,17 @@ struct BreakArgs {
   long long* sums;                // per region: fragCoverage, badCoverage, coverage sums
   BreakTile* tiles;
   int2* gap_scratch;              // per call tile kBreakStarts + 1 gap runs
-  pg_break* out;
-  int64_t out_cap;
-  unsigned long long* n_out;
+  int2* brk_scratch;              // per call tile kBreakStarts + 1 break runs
+  int32_t* brk_count;             // per region, then the exclusive scan (n_regions + 1)
+  int32_t* brk_off;
+  pg_break* out;                  // all breaks, by region then position
 };
 
 void launch_breaks(const BreakArgs& a, int32_t n_regions, cudaStream_t s);
+// Windows of the K-mer tally from the breaks: the reads of the break's contig
+// that start in [start - radius - max_span, stop + radius] (the read store's
+// index, like the host's ReadIndex.range_for).
+void launch_break_windows(const Reads& R, const RegionDev* regions, const pg_break* brk, int32_t n,
+                          int32_t radius, const ReadExtent* ext, pg_window* out, cudaStream_t s);
 
 }  // namespace pg

@@ -115,7 +115,7 @@ struct ReadExtent {      // maxima over the read store, for tile read ranges
   unsigned long long n_indel_ops;
   unsigned long long bad_read;  // 1 + index of a read whose offsets leave their arrays, else 0
   int32_t unsorted;      // 1 if positions decrease within one reference
-  int32_t pad;
+  int32_t max_span;      // max(aend - pos + 1): how far before a window a read that overlaps it can start
 };
 
 struct DevParams {

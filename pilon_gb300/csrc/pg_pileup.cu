@@ -41,7 +41,7 @@ __device__ inline bool in_window(int32_t pos, int32_t aend, uint16_t fl, const R
 // Also validates the store: every read's CIGAR, bases and qualities must lie
 // inside their arrays, and positions must not decrease within a reference.
 __global__ void k_read_extent(Reads R, ReadExtent* out, int4* desc) {
-  int32_t lead = 0, back = 0;
+  int32_t lead = 0, back = 0, span = 0;
   unsigned long long nid = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < R.n; i += (int64_t)gridDim.x * blockDim.x) {
     int32_t pos = R.pos[i];
@@ -77,6 +77,7 @@ __global__ void k_read_extent(Reads R, ReadExtent* out, int4* desc) {
       if (consumes_ref(op)) fo += len;
     }
     lead = max(lead, (int32_t)min((long long)(pos - lo), (long long)(1 << 30)));
+    span = max(span, (int32_t)min((long long)R.aend[i] - pos + 1, (long long)(1 << 30)));
     back = max(back, (int32_t)min((long long)(hi - pos), (long long)(1 << 30)));
     // the walk descriptor (the shape tests of PileUpRegion.addRead's CIGAR walk,
     // S/PileUpRegion.scala:139-145, with the same int32 arithmetic as the walk)
@@ -124,10 +125,12 @@ __global__ void k_read_extent(Reads R, ReadExtent* out, int4* desc) {
   }
   lead = __reduce_max_sync(FULL, lead);
   back = __reduce_max_sync(FULL, back);
+  span = __reduce_max_sync(FULL, span);
   for (int o = 16; o > 0; o >>= 1) nid += __shfl_down_sync(FULL, nid, o);
   if ((threadIdx.x & 31) == 0) {
     atomicMax(&out->max_lead, lead);
     atomicMax(&out->max_back, back);
+    atomicMax(&out->max_span, span);
     atomicAdd(&out->n_indel_ops, nid);
   }
 }

@@ -51,6 +51,8 @@ def lib():
             "pg_sync": (C.c_int, [vp]),
             "pg_format_vcf": (C.c_int, [vp, i32, C.c_char_p, i32, i32, i32, vp, i64, C.POINTER(C.c_int64)]),
             "pg_find_breaks": (C.c_int, [vp, i32, vp, i64, C.POINTER(C.c_int64)]),
+            "pg_kmer_tally_breaks": (C.c_int, [vp, i32, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
+                                               C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -211,6 +213,20 @@ class Engine:
             b = buf[k]
             out.setdefault(int(b.region), []).append((int(b.start), int(b.stop)))
         return out
+
+    def kmer_tally_breaks(self, K, params, radius=500, min_depth=5, cap=None):
+        """pg_kmer_tally_breaks: the K-mer tally over one device-built window per
+        break candidate; returns (number of windows, edges)."""
+        cap = cap or getattr(self, "_kmer_cap", 1 << 20)
+        while True:
+            edges = np.zeros(cap, _abi.kmer_edge_dtype())
+            nw, n = C.c_int64(), C.c_int64()
+            self._check(self.L.pg_kmer_tally_breaks(self.h, params.min_min_depth, radius, K, C.byref(params),
+                                                    min_depth, edges.ctypes.data, cap, C.byref(nw), C.byref(n)))
+            if n.value <= cap:
+                self._kmer_cap = max(cap, int(n.value))
+                return int(nw.value), edges[:n.value]
+            cap = int(n.value)
 
     def set_reads_device(self, dev_reads, n_reads):
         """pg_set_reads_device: a read store already in device memory (pg_reads

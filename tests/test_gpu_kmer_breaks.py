@@ -141,3 +141,30 @@ def test_device_breaks_many_contigs(engine):
     _device_breaks_vs_oracle(engine, ds, regions, p)
     p2 = _abi.default_params(min_min_depth=12)
     _device_breaks_vs_oracle(engine, ds, regions, p2)
+
+
+def test_kmer_tally_over_device_break_windows(engine, euk):
+    """pg_kmer_tally_breaks builds one window per device break candidate and
+    tallies it; the windows equal the host index's read ranges, so the edges
+    equal pg_kmer_tally over the host windows and the oracle's."""
+    ds = euk
+    p = _abi.default_params()
+    lens = [c.size for c in ds.contigs]
+    regions = plan_regions(ds.reads, lens, chunk_size=200_000)
+    engine.set_reference(ds.contigs)
+    engine.set_reads(ds.reads)
+    engine.pileup_regions(regions, p)
+    brk = engine.find_breaks(p.min_min_depth)
+    idx = ReadIndex(ds.reads, len(ds.contigs))
+    wins = []
+    for r in sorted(brk):
+        c = regions[r][0]
+        for (s, e) in brk[r]:
+            wins.append(idx.range_for(c, s, e, lens[c], slop=500))
+    assert len(wins) > 10
+    nw, got = engine.kmer_tally_breaks(31, p, radius=500)
+    assert nw == len(wins)
+    want = engine.kmer_tally(wins, 31, p)
+    assert edge_set(got) == edge_set(want)
+    assert edge_set(oracle.kmer_tally(ds.reads, p, wins[:8], 31)) == edge_set(
+        [e for e in got if int(e["window"]) < 8])
