@@ -8,7 +8,7 @@ import os
 from .build import BUILD
 
 CACHE = os.path.join(BUILD, "autotune.json")
-TILES = (1024, 2048, 4096)
+TILES = (256, 512, 1024, 2048, 4096)
 WARPS = (8, 16)
 VARIANTS = (0, 1, 2)   # lanes per simple read: 32, 16, 8
 

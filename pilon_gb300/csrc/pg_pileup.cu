@@ -112,7 +112,7 @@ __global__ void k_read_extent(Reads R, ReadExtent* out, int4* desc) {
         if (consumes_ref(op)) f2 += ln;
       }
       const int32_t adjMq = roundDivI(wmul(mq, length - clipped), length);
-      if (nM == 0 || ld > 0xffff || tr > 0xffff || adjMq < 0 || adjMq > 255 || mlen >= (1 << 30)) simple = false;
+      if (nM == 0 || ld > 0xffff || tr >= 0xffff || adjMq < 0 || adjMq > 255 || mlen >= (1 << 30)) simple = false;
       const bool hasQual = length > 0 && R.qual[R.qual_off[i]] != 0xFF;
       const bool pairOk = !(fl & 0x1) || ((fl & 0x2) && R.ref_id[i] == R.mate_ref_id[i]);
       const int32_t lrel = (int32_t)min((long long)pos - wlo, (long long)((1 << 30) - 1));
@@ -215,14 +215,30 @@ __device__ inline bool nanopore_exclude(const uint8_t* cref, int32_t x, int32_t 
 // descriptor kinds
 enum : uint32_t { kSkip = 0, kFast = 1, kInvalid = 2, kSlow = 3, kComplex = 4 };
 
+// An M/=/X segment of a read with an I/D/N CIGAR, queued for the chunked walk
+// (24 bytes, per warp in shared memory behind the counters).
+struct SegQ {
+  int64_t read;    // read index
+  int32_t pb;      // segment start minus tile start
+  uint32_t i01;    // trusted in-tile segment offsets [i0, i1), 16 bits each
+  uint32_t mr;     // mq + 1 (9 bits) | read offset of the segment << 9
+  int32_t pad;
+};
+constexpr int kSegQueue = 48;
+// clip word of a queued segment: trail 0xffff marks "no clips" (simple reads
+// have trailing clips below 0xffff)
+constexpr uint32_t kSegmentClip = 0xffffu << 16;
+
 // MINB: resident CTAs of 512 threads the register allocation must allow
 // (2: up to 64 registers per thread).  G: lanes per simple read (8, 16, 32).
 template <int T, int MINB, int G>
 __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_begin, int32_t tile_end) {
   extern __shared__ __align__(16) uint32_t sm_raw[];
   uint32_t* sm = sm_raw + 4;  // 4 words of padding in front of the counters
+  SegQ* segq = reinterpret_cast<SegQ*>(sm_raw + 11 * T + 4) + (threadIdx.x >> 5) * kSegQueue;
   __shared__ unsigned long long s_bc;
   __shared__ uint8_t s_perm[16][32];  // per warp: lane of the read in each round slot
+  __shared__ int32_t s_next;          // next unclaimed read of the pass (offset)
   uint32_t* s_bad = sm + 9 * T;
   uint32_t* s_clip = sm + 10 * T;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -241,10 +257,25 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
 
     for (int64_t c0 = tile.read_lo, pass = 0; pass == 0 || c0 < tile.read_hi; c0 += kMaxReadsPerPass, pass++) {
       const int64_t c1 = min(c0 + kMaxReadsPerPass, tile.read_hi);
+      const int32_t npass = (int32_t)(c1 - c0);
       for (int k = threadIdx.x; k < 11 * T + 4; k += blockDim.x) sm_raw[k] = 0;
+      if (threadIdx.x == 0) s_next = 0;
       __syncthreads();
 
-      for (int64_t base = c0 + 32 * (int64_t)warp; base < c1; base += 32 * (int64_t)nwarps) {
+      // Warps claim batches of the pass's reads as they finish the previous one:
+      // 32 reads while many are left, then 16, then 8, so the warps reach the
+      // tile's closing barrier close together.
+      while (true) {
+        int32_t off = 0, size = 0;
+        if (lane == 0) {
+          const int32_t rem = npass - *(volatile int32_t*)&s_next;
+          size = rem > 64 * nwarps ? 32 : rem > 16 * nwarps ? 16 : 8;
+          off = atomicAdd(&s_next, size);
+        }
+        off = __shfl_sync(FULL, off, 0);
+        size = __shfl_sync(FULL, size, 0);
+        if (off >= npass) break;
+        const int64_t base = c0 + off, bend = min(base + size, c1);
         // ---- one descriptor per lane
         const int64_t i = base + lane;
         uint32_t kind = kSkip, mq1 = 0, clip = 0;   // clip: lead | trail << 16
@@ -253,7 +284,7 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
         const uint8_t* qp = nullptr;
         const uint8_t* sp = nullptr;
         int64_t co = 0;
-        if (i < c1) {
+        if (i < bend) {
           // every load of the descriptor phase is independent of the others
           const int4 d0 = R.desc[2 * i], d1 = R.desc[2 * i + 1];
           const uint16_t fl = R.flag[i];
@@ -295,11 +326,98 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
             }
           }
         }
+        // ---- general CIGAR reads (S/PileUpRegion.scala:145-216), whole warp per read;
+        // I and D are handled by k_read_events.  Their M/=/X segments that have
+        // qualities are queued and walked afterwards by the chunked rounds below.
+        int nq = 0;  // queued segments (the same in every lane)
+        unsigned cx = __ballot_sync(FULL, kind == kComplex);
+        while (cx) {
+          const int src = __ffs(cx) - 1;
+          cx &= cx - 1;
+          const int32_t rpos = __shfl_sync(FULL, pos, src);
+          const int32_t rnc = __shfl_sync(FULL, nc, src), rlen = __shfl_sync(FULL, length, src);
+          const uint32_t rmq1 = __shfl_sync(FULL, mq1, src);
+          const bool rvalid = __shfl_sync(FULL, (int)valid, src) != 0;
+          const bool rhas = __shfl_sync(FULL, (int)hasQual, src) != 0;
+          const int64_t rco = __shfl_sync(FULL, co, src);
+          const uint8_t* rqp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)qp, src);
+          const uint8_t* rsp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)sp, src);
+          int32_t readOffset = 0, refOffset = 0;
+          for (int cb = 0; cb < rnc; cb += 32) {
+            const uint32_t wl = (cb + lane < rnc) ? R.cigar[rco + cb + lane] : 0u;
+            const int kmax = min(32, rnc - cb);
+            for (int k2 = 0; k2 < kmax; k2++) {
+              const uint32_t w = __shfl_sync(FULL, wl, k2);
+              const int32_t len = (int32_t)(w >> 4);
+              const int op = (int)(w & 15u);
+              const int32_t locus = rpos + refOffset;
+              if (op == 0 || op == 7 || op == 8) {
+                const int32_t a0 = max(max(tileLo - locus, P.flank - readOffset), 0);
+                const int32_t a1 = min(min(tileHi - locus + 1, rlen - P.flank - readOffset), len);
+                if (rvalid && lane == 0 && a1 > a0) bc += (unsigned long long)(a1 - a0);
+                // a segment the fast path can walk: queued as a read of its own
+                if (rvalid && rhas && P.long_read != PG_NANOPORE && a1 > a0 && readOffset < 0xffff && len < 0x10000 &&
+                    nq < kSegQueue) {
+                  if (lane == 0) {
+                    SegQ& e = segq[nq];
+                    e.read = base + src;
+                    e.pb = locus - tileLo;
+                    e.i01 = (uint32_t)a0 | ((uint32_t)a1 << 16);
+                    e.mr = rmq1 | ((uint32_t)readOffset << 9);
+                  }
+                  nq++;
+                } else
+                for (int32_t ii = a0 + lane; ii < a1; ii += 32) {
+                  const int32_t rOff = readOffset + ii;
+                  const int32_t p = locus + ii - tileLo;
+                  if (rvalid) {
+                    int32_t qual = rhas ? (int32_t)(int8_t)rqp[rOff] : P.default_qual;
+                    if (P.long_read == PG_NANOPORE && nanopore_exclude(cref, locus + ii - g.start, g.size)) qual = 0;
+                    const uint8_t b = rsp[rOff >> 1];
+                    add_base<T>(sm, p, (rOff & 1) ? (b & 15u) : (uint32_t)(b >> 4), qual, rmq1, P.min_qual);
+                  } else {
+                    atomicAdd(&s_bad[p], 1u);
+                  }
+                }
+              } else if (op == 4) {
+                const int32_t clipStart = readOffset == 0 ? locus - len : locus;
+                const int32_t clipEnd = clipStart + len - 1;
+                if (lane == 0) {
+                  if (clipStart >= tileLo && clipStart <= tileHi) atomicAdd(&s_clip[clipStart - tileLo], 1u);
+                  if (clipEnd >= tileLo && clipEnd <= tileHi) atomicAdd(&s_clip[clipEnd - tileLo], 1u);
+                }
+                const int32_t a0 = max(tileLo - clipStart, 0);
+                const int32_t a1 = min(tileHi - clipStart + 1, len);
+                for (int32_t ii = a0 + lane; ii < a1; ii += 32) atomicAdd(&s_bad[clipStart + ii - tileLo], 1u);
+              }
+              if (consumes_read(op)) readOffset += len;
+              if (consumes_ref(op)) refOffset += len;
+            }
+          }
+        }
         // ---- simple reads, 32 / G at a time, G lanes each.  With 4 groups, round k
         // gives group g the k-th read of residue class g while every class has one,
         // so the groups add to 4 different position residues at every step and their
         // shared-memory atomics hit 32 different banks; the reads left over follow
         // in lane order.  Each lane computes its read's slot at once.
+        __syncwarp();
+        for (int q0 = -32; q0 < nq; q0 += 32) {
+        if (q0 >= 0) {  // queued segments q0 .. q0 + 31 become the lanes' reads
+          kind = kSkip;
+          if (q0 + lane < nq) {
+            const SegQ e = segq[q0 + lane];
+            const int32_t r0 = (int32_t)(e.mr >> 9);
+            kind = kFast;
+            pb = e.pb;
+            i0 = (int32_t)(e.i01 & 0xffffu);
+            i1 = (int32_t)(e.i01 >> 16);
+            mq1 = e.mr & 0x1ffu;
+            clip = (uint32_t)r0 | kSegmentClip;  // lead = r0 for the read offsets; no clips
+            qp = R.qual + R.qual_off[e.read] + r0;
+            sp = R.seq + R.seq_off[e.read];
+            cls = (pb + i0 - (int32_t)((uintptr_t)(qp + i0) & 3u)) & 3;
+          }
+        }
         const bool simple_kind = kind != kSkip && kind != kComplex;
         const unsigned below = (1u << lane) - 1u;
         const unsigned sm_all = __ballot_sync(FULL, simple_kind);
@@ -333,7 +451,8 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
             const int32_t lead = (int32_t)(rclip & 0xffffu), trail = (int32_t)(rclip >> 16);
             const int32_t rpos = rpb + tileLo;
             const int32_t rmlen = rml & 0x3fffffff;
-            if (lead > 0) {  // clipStart = locus - len (clip at read offset 0), clipEnd = locus - 1
+            const bool clips = (rclip & kSegmentClip) != kSegmentClip;
+            if (lead > 0 && clips) {  // clipStart = locus - len (clip at read offset 0), clipEnd = locus - 1
               const int32_t cs = rpos - lead, ce = rpos - 1;
               if (gl == 0) {
                 if (cs >= tileLo && cs <= tileHi) atomicAdd(&s_clip[cs - tileLo], 1u);
@@ -427,7 +546,7 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
                 add_base<T>(sm, rpb + ii, nib, qual, rmq1, P.min_qual);
               }
             }
-            if (trail > 0) {  // clipStart = locus (clip after the aligned bases), clipEnd = locus + len - 1
+            if (trail > 0 && clips) {  // clipStart = locus (clip after the aligned bases), clipEnd = locus + len - 1
               const int32_t cs = rpos + rmlen, ce = cs + trail - 1;
               if (gl == 0) {
                 if (cs >= tileLo && cs <= tileHi) atomicAdd(&s_clip[cs - tileLo], 1u);
@@ -437,60 +556,7 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
             }
           }
         }
-        // ---- general CIGAR reads (S/PileUpRegion.scala:145-216), whole warp per read;
-        // I and D are handled by k_read_events
-        unsigned cx = __ballot_sync(FULL, kind == kComplex);
-        while (cx) {
-          const int src = __ffs(cx) - 1;
-          cx &= cx - 1;
-          const int32_t rpos = __shfl_sync(FULL, pos, src);
-          const int32_t rnc = __shfl_sync(FULL, nc, src), rlen = __shfl_sync(FULL, length, src);
-          const uint32_t rmq1 = __shfl_sync(FULL, mq1, src);
-          const bool rvalid = __shfl_sync(FULL, (int)valid, src) != 0;
-          const bool rhas = __shfl_sync(FULL, (int)hasQual, src) != 0;
-          const int64_t rco = __shfl_sync(FULL, co, src);
-          const uint8_t* rqp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)qp, src);
-          const uint8_t* rsp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)sp, src);
-          int32_t readOffset = 0, refOffset = 0;
-          for (int cb = 0; cb < rnc; cb += 32) {
-            const uint32_t wl = (cb + lane < rnc) ? R.cigar[rco + cb + lane] : 0u;
-            const int kmax = min(32, rnc - cb);
-            for (int k2 = 0; k2 < kmax; k2++) {
-              const uint32_t w = __shfl_sync(FULL, wl, k2);
-              const int32_t len = (int32_t)(w >> 4);
-              const int op = (int)(w & 15u);
-              const int32_t locus = rpos + refOffset;
-              if (op == 0 || op == 7 || op == 8) {
-                const int32_t a0 = max(max(tileLo - locus, P.flank - readOffset), 0);
-                const int32_t a1 = min(min(tileHi - locus + 1, rlen - P.flank - readOffset), len);
-                if (rvalid && lane == 0 && a1 > a0) bc += (unsigned long long)(a1 - a0);
-                for (int32_t ii = a0 + lane; ii < a1; ii += 32) {
-                  const int32_t rOff = readOffset + ii;
-                  const int32_t p = locus + ii - tileLo;
-                  if (rvalid) {
-                    int32_t qual = rhas ? (int32_t)(int8_t)rqp[rOff] : P.default_qual;
-                    if (P.long_read == PG_NANOPORE && nanopore_exclude(cref, locus + ii - g.start, g.size)) qual = 0;
-                    const uint8_t b = rsp[rOff >> 1];
-                    add_base<T>(sm, p, (rOff & 1) ? (b & 15u) : (uint32_t)(b >> 4), qual, rmq1, P.min_qual);
-                  } else {
-                    atomicAdd(&s_bad[p], 1u);
-                  }
-                }
-              } else if (op == 4) {
-                const int32_t clipStart = readOffset == 0 ? locus - len : locus;
-                const int32_t clipEnd = clipStart + len - 1;
-                if (lane == 0) {
-                  if (clipStart >= tileLo && clipStart <= tileHi) atomicAdd(&s_clip[clipStart - tileLo], 1u);
-                  if (clipEnd >= tileLo && clipEnd <= tileHi) atomicAdd(&s_clip[clipEnd - tileLo], 1u);
-                }
-                const int32_t a0 = max(tileLo - clipStart, 0);
-                const int32_t a1 = min(tileHi - clipStart + 1, len);
-                for (int32_t ii = a0 + lane; ii < a1; ii += 32) atomicAdd(&s_bad[clipStart + ii - tileLo], 1u);
-              }
-              if (consumes_read(op)) readOffset += len;
-              if (consumes_ref(op)) refOffset += len;
-            }
-          }
+        __syncwarp();
         }
       }
       __syncthreads();
@@ -544,13 +610,14 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
 
 template <int T, int MINB, int G>
 static void launch_walk_t(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s) {
-  const size_t smem = (size_t)(11 * T + 4) * sizeof(uint32_t);
+  const size_t smem = (size_t)(11 * T + 4) * sizeof(uint32_t) + (size_t)warps * kSegQueue * sizeof(SegQ);
   // attribute and occupancy are queried once per (kernel, warps): the first
   // launch of a shape is never inside a stream capture
   static bool configured = false;
   static int per_sm_of[17] = {0};
-  if (!configured) {
-    cudaFuncSetAttribute(k_walk<T, MINB, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (!configured) {  // room for the largest CTA (16 warps of segment queues)
+    const size_t smem_max = (size_t)(11 * T + 4) * sizeof(uint32_t) + (size_t)16 * kSegQueue * sizeof(SegQ);
+    cudaFuncSetAttribute(k_walk<T, MINB, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     configured = true;
   }
   if (!per_sm_of[warps]) {
