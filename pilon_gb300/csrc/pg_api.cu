@@ -42,7 +42,7 @@ struct pg_ctx {
   DevBuf regions, walk_tiles, call_tile_region, chunks, stats;
   DevBuf rec_count, rec_qsum, rec_i32[10], rec_call, rec_score, rec_indel_len, rec_ins_str, rec_ev_end;
   DevBuf cand_count, cand_off, tile_sums;
-  DevBuf events, events_sorted, cands, pool, counters, run_max, chunk_stats, spool;
+  DevBuf events, events_sorted, cands, pool, counters, run_max, chunk_stats, spool, indel_list;
   int64_t event_cap = 0, pool_cap = 0, spool_cap = 0;
   int32_t cand_cap = 0;
   DevBuf staging_dev;
@@ -232,7 +232,7 @@ void pg_close(pg_ctx* c) {
                    &c->rec_count, &c->rec_qsum, &c->rec_call, &c->rec_score, &c->rec_indel_len, &c->rec_ins_str,
                    &c->rec_ev_end, &c->cand_count, &c->cand_off, &c->tile_sums,
                    &c->events, &c->events_sorted, &c->cands, &c->pool, &c->counters, &c->run_max, &c->staging_dev,
-                   &c->chunk_stats, &c->spool};
+                   &c->chunk_stats, &c->spool, &c->indel_list};
   for (DevBuf* b : all) release(*b);
   DevBuf* km[] = {&c->kwin, &c->kpre, &c->kslot_base, &c->kslot_cap, &c->kx_base, &c->kx_cap, &c->kkeys, &c->kcnt,
                   &c->kqs, &c->kmq, &c->kq, &c->kx_keys, &c->kx_used, &c->kx_cnt, &c->kx_qs, &c->kx_mq, &c->kx_q,
@@ -423,6 +423,7 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   ea.n_events = &counters[CNT_EVENTS]; ea.event_cap = c->event_cap;
   ea.chunk_stats = P<ChunkStats>(c->chunk_stats);
   ea.spool = P<uint64_t>(c->spool); ea.spool_fill = &counters[CNT_SPOOL]; ea.spool_cap = c->spool_cap;
+  ea.indel_list = P<int64_t>(c->indel_list);
   launch_read_events(ea, ch0, chn, s);
 
   launch_region_prep(d_regions + r0, d_stats + r0, P<ChunkStats>(c->chunk_stats), r1 - r0, dp, s);
@@ -512,6 +513,7 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
   EN(c->call_tile_region, sizeof(int32_t) * (n_call + 1));
   EN(c->chunks, sizeof(ReadChunk) * std::max<size_t>(plan.chunks.size(), 1));
   EN(c->chunk_stats, sizeof(ChunkStats) * std::max<size_t>(plan.chunks.size(), 1));
+  EN(c->indel_list, sizeof(int64_t) * kReadsPerChunk * std::max<size_t>(plan.chunks.size(), 1));
   EN(c->rec_count, 16 * (size_t)pos);
   EN(c->rec_qsum, 32 * (size_t)pos);
   for (auto& b : c->rec_i32) EN(b, 4 * (size_t)pos);

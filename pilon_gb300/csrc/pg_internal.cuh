@@ -79,7 +79,8 @@ struct ReadChunk {       // reads [lo, hi) fed to region `region`
 
 struct ChunkStats {      // per read chunk: partial sums of the region statistics
   unsigned long long read_count, base_count, fr_count, fr_sum, fr_sumsq, rf_count, rf_sum, rf_sumsq;
-  int32_t phys_cov_start, insert_size_start, error, pad;
+  int32_t phys_cov_start, insert_size_start, error;
+  int32_t n_indel;       // reads of the chunk with I/D operators, listed for k_read_indels
 };
 
 struct Event {           // one insertion or deletion added to a pileup
@@ -368,6 +369,7 @@ struct EventArgs {
   uint64_t* spool;                 // insertion tails, 16 characters per word
   unsigned long long* spool_fill;
   int64_t spool_cap;
+  int64_t* indel_list;             // per chunk kReadsPerChunk slots: its reads with I/D
 };
 
 struct CallArgs {

@@ -7,9 +7,10 @@
 //                   accumulates PileUp.add / badPair / clips with shared-memory
 //                   integer atomics and writes the tile's records once
 //   k_read_events   per (region, read): BamFile.process bookkeeping (readCount,
-//                   addInsert), physCovIncr, and the I/D operators with their left
-//                   shift (S/PileUpRegion.scala:150-183), applied with global atomics
-//                   after k_walk and logged as events for the indel vote
+//                   addInsert) and physCovIncr; lists the reads with I/D operators
+//   k_read_indels   per listed read: the I/D operators with their left shift
+//                   (S/PileUpRegion.scala:150-183), applied with global atomics after
+//                   k_walk and logged as events for the indel vote
 //   k_event_scatter events -> grouped by position (offsets from the scan)
 //   k_scan_*        computePhysCov (S/PileUpRegion.scala:90-100) as a segmented scan
 #include <cuda_runtime.h>
@@ -663,8 +664,9 @@ __device__ inline unsigned long long warp_sum_u64(unsigned long long v) {
 // few reads with indels run long left-shift loops.
 constexpr int kEvThreads = 64;
 constexpr int kEvPerChunk = kReadsPerChunk / kEvThreads;
+static_assert(kEvPerChunk * kEvThreads == kReadsPerChunk, "one read per thread of k_read_events");
 
-__global__ void __launch_bounds__(kEvThreads, 12) k_read_events(EventArgs a, int32_t chunk_begin, int32_t chunk_end) {
+__global__ void __launch_bounds__(kEvThreads, 16) k_read_events(EventArgs a, int32_t chunk_begin, int32_t chunk_end) {
   const Reads& R = a.R;
   const DevParams& P = a.P;
   for (int32_t bq = chunk_begin * kEvPerChunk + blockIdx.x; bq < chunk_end * kEvPerChunk; bq += gridDim.x) {
@@ -675,6 +677,7 @@ __global__ void __launch_bounds__(kEvThreads, 12) k_read_events(EventArgs a, int
     unsigned long long rc_n = 0, bc_n = 0, frc = 0, frs = 0, frq = 0, rfc = 0, rfs = 0, rfq = 0;
     uint32_t pcs = 0, iss = 0;
     int32_t err = 0;
+    int64_t indel_read = -1;  // this thread's read, when it has I or D operators
     auto inRegion = [&](int64_t l) { return l >= g.start && l <= g.stop; };
     for (int64_t i = C.lo + (int64_t)(bq % kEvPerChunk) * kEvThreads + threadIdx.x; i < C.hi;
          i += (int64_t)kEvPerChunk * kEvThreads) {
@@ -719,9 +722,59 @@ __global__ void __launch_bounds__(kEvThreads, 12) k_read_events(EventArgs a, int
         else { rfc++; rfs += (unsigned long long)insertSize; rfq += sq; }
       }
 
-      // I and D operators (S/PileUpRegion.scala:150-183)
-      const bool anyIndel = !((uint32_t)d1.y & kDescSimple) && d1.x != 0;
-      if (!anyIndel || !valid) continue;
+      // reads with I or D operators go to k_read_indels
+      if (valid && !((uint32_t)d1.y & kDescSimple) && d1.x != 0) indel_read = i;
+    }
+    {  // list them in the chunk's slots: one atomic per warp on the chunk's counter
+      const unsigned m = __ballot_sync(FULL, indel_read >= 0);
+      if (m) {
+        const int lane = threadIdx.x & 31;
+        int32_t first = 0;
+        if (lane == __ffs(m) - 1) first = atomicAdd(&a.chunk_stats[ch].n_indel, __popc(m));
+        first = __shfl_sync(FULL, first, __ffs(m) - 1);
+        if (indel_read >= 0)
+          a.indel_list[(int64_t)ch * kReadsPerChunk + first + __popc(m & ((1u << lane) - 1u))] = indel_read;
+      }
+    }
+    rc_n = warp_sum_u64(rc_n); bc_n = warp_sum_u64(bc_n);
+    frc = warp_sum_u64(frc); frs = warp_sum_u64(frs); frq = warp_sum_u64(frq);
+    rfc = warp_sum_u64(rfc); rfs = warp_sum_u64(rfs); rfq = warp_sum_u64(rfq);
+    pcs = __reduce_add_sync(FULL, pcs); iss = __reduce_add_sync(FULL, iss);
+    err = __reduce_max_sync(FULL, err);
+    if ((threadIdx.x & 31) == 0) {  // k_region_prep adds the chunks up per region
+      ChunkStats& cs = a.chunk_stats[ch];
+      if (rc_n) atomicAdd(&cs.read_count, rc_n);
+      if (bc_n) atomicAdd(&cs.base_count, bc_n);
+      if (frc) { atomicAdd(&cs.fr_count, frc); atomicAdd(&cs.fr_sum, frs); atomicAdd(&cs.fr_sumsq, frq); }
+      if (rfc) { atomicAdd(&cs.rf_count, rfc); atomicAdd(&cs.rf_sum, rfs); atomicAdd(&cs.rf_sumsq, rfq); }
+      if (pcs) atomicAdd((uint32_t*)&cs.phys_cov_start, pcs);
+      if (iss) atomicAdd((uint32_t*)&cs.insert_size_start, iss);
+      if (err) atomicMax(&cs.error, err);
+    }
+  }
+}
+
+// The I and D operators of the listed reads (S/PileUpRegion.scala:150-183):
+// left shift, H1 double count, the indel counters and the events for the
+// vote.  One thread per listed read, so a warp walks 32 reads with indels.
+constexpr int kIndelThreads = 128;
+__global__ void __launch_bounds__(kIndelThreads) k_read_indels(EventArgs a, int32_t chunk_begin) {
+  const Reads& R = a.R;
+  const DevParams& P = a.P;
+  constexpr int kPer = kReadsPerChunk / kIndelThreads;
+  const int32_t ch = chunk_begin + blockIdx.x / kPer;
+  const int32_t slot = (blockIdx.x % kPer) * kIndelThreads + threadIdx.x;
+  if (slot < a.chunk_stats[ch].n_indel) {
+    const int64_t i = a.indel_list[(int64_t)ch * kReadsPerChunk + slot];
+    const ReadChunk C = a.chunks[ch];
+    const RegionDev g = a.regions[C.region];
+    const uint8_t* cref = a.ref + g.ref_off;
+    auto inRegion = [&](int64_t l) { return l >= g.start && l <= g.stop; };
+    const int4 d0 = R.desc[2 * i], d1 = R.desc[2 * i + 1];
+    const int32_t pos = d0.x;
+    unsigned long long bc_n = 0;
+    int32_t err = 0;
+    {
       const int64_t co = R.cigar_off[i];
       const int nc = R.n_cigar[i];
       const int32_t length = R.l_seq[i];
@@ -869,21 +922,9 @@ __global__ void __launch_bounds__(kEvThreads, 12) k_read_events(EventArgs a, int
         if (op == 0 || op == 2 || op == 3 || op == 7 || op == 8) refOffset += len;
       }
     }
-    rc_n = warp_sum_u64(rc_n); bc_n = warp_sum_u64(bc_n);
-    frc = warp_sum_u64(frc); frs = warp_sum_u64(frs); frq = warp_sum_u64(frq);
-    rfc = warp_sum_u64(rfc); rfs = warp_sum_u64(rfs); rfq = warp_sum_u64(rfq);
-    pcs = __reduce_add_sync(FULL, pcs); iss = __reduce_add_sync(FULL, iss);
-    err = __reduce_max_sync(FULL, err);
-    if ((threadIdx.x & 31) == 0) {  // k_region_prep adds the chunks up per region
-      ChunkStats& cs = a.chunk_stats[ch];
-      if (rc_n) atomicAdd(&cs.read_count, rc_n);
-      if (bc_n) atomicAdd(&cs.base_count, bc_n);
-      if (frc) { atomicAdd(&cs.fr_count, frc); atomicAdd(&cs.fr_sum, frs); atomicAdd(&cs.fr_sumsq, frq); }
-      if (rfc) { atomicAdd(&cs.rf_count, rfc); atomicAdd(&cs.rf_sum, rfs); atomicAdd(&cs.rf_sumsq, rfq); }
-      if (pcs) atomicAdd((uint32_t*)&cs.phys_cov_start, pcs);
-      if (iss) atomicAdd((uint32_t*)&cs.insert_size_start, iss);
-      if (err) atomicMax(&cs.error, err);
-    }
+    ChunkStats& cs = a.chunk_stats[ch];
+    if (bc_n) atomicAdd(&cs.base_count, bc_n);
+    if (err) atomicMax(&cs.error, err);
   }
 }
 
@@ -891,6 +932,7 @@ void launch_read_events(const EventArgs& a, int32_t chunk_begin, int32_t chunk_c
   if (chunk_count <= 0) return;
   cudaMemsetAsync(a.chunk_stats + chunk_begin, 0, sizeof(ChunkStats) * (size_t)chunk_count, s);
   k_read_events<<<chunk_count * kEvPerChunk, kEvThreads, 0, s>>>(a, chunk_begin, chunk_begin + chunk_count);
+  k_read_indels<<<chunk_count * (kReadsPerChunk / kIndelThreads), kIndelThreads, 0, s>>>(a, chunk_begin);
 }
 
 // ---------------------------------------------------------------------------
