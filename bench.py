@@ -160,22 +160,24 @@ class PinnedOut:
 
 
 def roofline_traffic(workload_name, units):
-    """Per-launch DRAM bytes of the walk kernel from the committed ncu summary,
-    scaled by units if it was captured on a smaller case; None if absent."""
+    """Per-launch DRAM bytes of the walk kernel from the committed ncu summary:
+    the capture of this workload's scaled-down case (lines tagged with the
+    workload name) or else the untagged one, scaled by units (piled bases),
+    since the walk's DRAM bytes grow with the reads it walks; None if absent."""
     path = os.path.join(ROOT, "profiles", "k_walk_ncu.md")
     if not os.path.exists(path):
         return None
-    cap_units = cap_bytes = None
+    found = {}
     for line in open(path):
-        if line.startswith("traffic_bytes_per_launch:"):
-            cap_bytes = float(line.split(":")[1])
-        if line.startswith("units_per_launch:"):
-            cap_units = float(line.split(":")[1])
-    if cap_bytes is None:
-        return None
-    if cap_units:
-        return cap_bytes * units / cap_units
-    return cap_bytes
+        for key in ("traffic_bytes_per_launch", "units_per_launch"):
+            if line.startswith(key):
+                tag = line[len(key):line.index(":")].strip("[] ")
+                found[(key, tag)] = float(line.split(":")[1])
+    for tag in (workload_name, ""):
+        b, u = found.get(("traffic_bytes_per_launch", tag)), found.get(("units_per_launch", tag))
+        if b is not None:
+            return b * units / u if u else b
+    return None
 
 
 def oracle_sample(ds, params, threads):
