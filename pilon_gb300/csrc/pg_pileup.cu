@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
         const int n_simple = __popc(sm_all);
         if (simple_kind) {
           int slot;
-          if (NG == 4) {
+          if (NG == 4 || NG == 8) {  // with 8 groups, groups g and g + 4 share a residue class
             const unsigned c0 = __ballot_sync(sm_all, cls == 0), c1 = __ballot_sync(sm_all, cls == 1);
             const unsigned c2 = __ballot_sync(sm_all, cls == 2), c3 = __ballot_sync(sm_all, cls == 3);
             const int m = min(min(__popc(c0), __popc(c1)), min(__popc(c2), __popc(c3)));
@@ -478,12 +478,18 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               const int32_t he = min(fs, ri1), ts = max(fe, he), nh = he - ri0, nt = max(ri1 - ts, 0);
               const uint32_t amq = 1u + (rmq1 << 12);
               // head and tail bases: loaded now, added after the chunks
-              const bool ht = gl < nh + nt;
-              const int32_t hx = gl < nh ? ri0 + gl : ts + (gl - nh);
-              uint32_t hb = 0, hq = 0;
-              if (ht) {
-                hb = rsp[(lead + hx) >> 1];
-                hq = rqp[hx];
+              constexpr int kHT = (6 + G - 1) / G;  // head/tail bases per lane
+              int32_t hx[kHT];
+              uint32_t hb[kHT], hq[kHT];
+#pragma unroll
+              for (int h = 0; h < kHT; h++) {
+                const int32_t k = gl + h * G;
+                hx[h] = k < nh + nt ? (k < nh ? ri0 + k : ts + (k - nh)) : -1;
+                hb[h] = hq[h] = 0;
+                if (hx[h] >= 0) {
+                  hb[h] = rsp[(lead + hx[h]) >> 1];
+                  hq[h] = rqp[hx[h]];
+                }
               }
               const int32_t n0 = lead + xs;          // read offset of chunk 0's first base
               const uint32_t psh = 4u * (uint32_t)(n0 & 1);  // chunks start on a low half-byte
@@ -524,14 +530,16 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
                 c += G;
                 qv = q1; sv = s1; q1 = q2; s1 = s2;
               }
-              if (ht) {
-                const uint32_t nib = ((lead + hx) & 1) ? (hb & 15u) : (hb >> 4);
-                const int32_t qual = (int32_t)(int8_t)hq;
+#pragma unroll
+              for (int h = 0; h < kHT; h++) {
+                if (hx[h] < 0) continue;
+                const uint32_t nib = ((lead + hx[h]) & 1) ? (hb[h] & 15u) : (hb[h] >> 4);
+                const int32_t qual = (int32_t)(int8_t)hq[h];
                 if (((0x116u >> nib) & 1u) && qual >= P.min_qual) {
-                  uint32_t* cp = sm + (rpb + hx) + ((0x30210u >> (2 * nib)) & 3u) * T;
+                  uint32_t* cp = sm + (rpb + hx[h]) + ((0x30210u >> (2 * nib)) & 3u) * T;
                   atomicAdd(cp, amq);
                   atomicAdd(cp + 4 * T, (uint32_t)qual * rmq1);
-                  atomicAdd(sm + (rpb + hx) + 8 * T, (uint32_t)qual);
+                  atomicAdd(sm + (rpb + hx[h]) + 8 * T, (uint32_t)qual);
                 }
               }
             } else if (rk == kInvalid) {
@@ -642,13 +650,14 @@ static void launch_walk_v(const WalkArgs& a, int32_t tile_begin, int32_t tile_co
   }
 }
 
-// variant: lanes per simple read (0: 32, 1: 16, 2: 8).
+// variant: lanes per simple read (0: 32, 1: 16, 2: 8, 3: 4).
 void launch_walk(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s) {
   if (tile_count <= 0) return;
   const int lanes = a.packed;
   if (lanes == 0) launch_walk_v<2, 32>(a, tile_begin, tile_count, warps, s);
   else if (lanes == 1) launch_walk_v<2, 16>(a, tile_begin, tile_count, warps, s);
-  else launch_walk_v<2, 8>(a, tile_begin, tile_count, warps, s);
+  else if (lanes == 2) launch_walk_v<2, 8>(a, tile_begin, tile_count, warps, s);
+  else launch_walk_v<2, 4>(a, tile_begin, tile_count, warps, s);
 }
 
 // ---------------------------------------------------------------------------

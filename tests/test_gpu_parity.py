@@ -68,7 +68,7 @@ def test_long_read_modes(engine, cfg1):
 
 @pytest.mark.parametrize("tile,warps,variant", [(1024, 8, 0), (1024, 16, 1), (2048, 8, 2), (4096, 16, 0),
                                                 (512, 16, 1), (4096, 8, 2), (256, 4, 1), (2048, 16, 2),
-                                                (256, 8, 2), (512, 8, 2)])
+                                                (256, 8, 2), (512, 8, 2), (1024, 8, 3), (2048, 16, 3)])
 def test_walk_tunings_bit_exact(engine, cfg1, tile, warps, variant):
     engine.set_tuning(tile, warps, variant)
     try:
