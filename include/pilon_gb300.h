@@ -228,6 +228,10 @@ pg_status pg_pileup_regions(pg_ctx *ctx, const pg_region *regions, int32_t n_reg
 pg_status pg_fetch_stats(pg_ctx *ctx, int32_t region, pg_region_stats *stats);
 /* Copies one region's arrays into caller host buffers. */
 pg_status pg_fetch_region(pg_ctx *ctx, int32_t region, pg_region_out *out);
+/* Copies the arrays of all regions of the last call at once: each array of
+ * `out` holds sum(stop - start + 1) positions, the regions one after another
+ * in call order (one copy per array instead of one per region). */
+pg_status pg_fetch_all(pg_ctx *ctx, pg_region_out *out);
 
 /* Launch shape of the pileup walk kernel: tile width (positions per CTA,
  * a power of two in [256, 4096]), warps per CTA (1..16) and variant (lanes

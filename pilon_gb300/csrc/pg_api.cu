@@ -657,14 +657,9 @@ pg_status pg_fetch_stats(pg_ctx* c, int32_t r, pg_region_stats* out) {
   return PG_OK;
 }
 
-pg_status pg_fetch_region(pg_ctx* c, int32_t r, pg_region_out* o) {
-  if (!c || !o) return PG_ERR_ARG;
-  if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
-  if (r < 0 || r >= c->n_regions) return fail(c, PG_ERR_ARG, "region %d out of range", r);
-  cudaSetDevice(c->device);
-  const RegionDev& g = c->regions_h[r];
-  const size_t n = (size_t)g.size;
-  const int64_t b = g.pos_base;
+// Copies positions [b, b + n) of every non-null array of o, then the
+// insertion characters; one synchronisation.
+static pg_status fetch_positions(pg_ctx* c, int64_t b, size_t n, pg_region_out* o) {
   cudaStream_t s = c->stream;
   Records rc = records(c);
   auto cp = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
@@ -699,6 +694,22 @@ pg_status pg_fetch_region(pg_ctx* c, int32_t r, pg_region_out* o) {
   }
   o->ins_chars_cap = (int64_t)pool_fill;
   return PG_OK;
+}
+
+pg_status pg_fetch_region(pg_ctx* c, int32_t r, pg_region_out* o) {
+  if (!c || !o) return PG_ERR_ARG;
+  if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
+  if (r < 0 || r >= c->n_regions) return fail(c, PG_ERR_ARG, "region %d out of range", r);
+  cudaSetDevice(c->device);
+  const RegionDev& g = c->regions_h[r];
+  return fetch_positions(c, g.pos_base, (size_t)g.size, o);
+}
+
+pg_status pg_fetch_all(pg_ctx* c, pg_region_out* o) {
+  if (!c || !o) return PG_ERR_ARG;
+  if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
+  cudaSetDevice(c->device);
+  return fetch_positions(c, 0, (size_t)c->n_positions, o);
 }
 
 static int64_t next_pow2(int64_t x) {

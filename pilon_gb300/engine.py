@@ -43,6 +43,7 @@ def lib():
             "pg_pileup_regions": (C.c_int, [vp, vp, i32, C.POINTER(_abi.pg_params), i32]),
             "pg_fetch_stats": (C.c_int, [vp, i32, C.POINTER(_abi.pg_region_stats)]),
             "pg_fetch_region": (C.c_int, [vp, i32, C.POINTER(_abi.pg_region_out)]),
+            "pg_fetch_all": (C.c_int, [vp, C.POINTER(_abi.pg_region_out)]),
             "pg_set_tuning": (C.c_int, [vp, i32, i32, i32]),
             "pg_kmer_tally": (C.c_int, [vp, vp, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
                                         C.POINTER(C.c_int64)]),
@@ -174,6 +175,14 @@ class Engine:
             o2.ins_chars_cap = pool
             self._check(self.L.pg_fetch_region(self.h, r, C.byref(o2)))
         out.stats = self.stats(r)
+        return out
+
+    def fetch_all(self, out):
+        """pg_fetch_all into `out` (RegionArrays sized for every position of the
+        last call, regions one after another); insertion characters not read."""
+        o = out.out_struct(0)
+        o.ins_chars = None
+        self._check(self.L.pg_fetch_all(self.h, C.byref(o)))
         return out
 
     def kmer_tally(self, windows, K, params, min_depth=5, cap=None):

@@ -103,3 +103,23 @@ def test_graph_replay_bit_exact(engine, cfg1):
     engine.pileup_regions(a, p, batched=True)
     for r in range(len(a)):
         compare_region(engine.fetch(r), ora[r], label=f"after switch region {r}")
+
+
+def test_fetch_all_equals_per_region(engine, cfg1):
+    """pg_fetch_all returns every region's arrays, one region after another."""
+    from pilon_gb300.engine import RegionArrays
+    regions = plan(cfg1, chunk_size=12_000)
+    engine.set_reference(cfg1.contigs)
+    engine.set_reads(cfg1.reads)
+    engine.pileup_regions(regions, _abi.default_params())
+    total = sum(e - s + 1 for (c, s, e, a, b) in regions)
+    allr = engine.fetch_all(RegionArrays(total))
+    off = 0
+    for r, (c, s, e, a, b) in enumerate(regions):
+        one = engine.fetch(r)
+        n = e - s + 1
+        for f in ("count", "qual_sum"):
+            assert np.array_equal(getattr(allr, f)[4 * off:4 * (off + n)], getattr(one, f)), (r, f)
+        for f in list(RegionArrays.I32) + ["call", "score"]:
+            assert np.array_equal(getattr(allr, f)[off:off + n], getattr(one, f)), (r, f)
+        off += n
