@@ -79,6 +79,7 @@ struct pg_ctx {
   bool capturing = false;
   // tuning
   int32_t tile_width = 2048, warps = 16, packed = 0;
+  uint32_t mode_mq1 = 0;  // most common adjusted mq + 1 of the read store's fast-path reads
 };
 
 namespace {
@@ -316,6 +317,9 @@ static pg_status finish_reads(pg_ctx* c) {
     return fail(c, PG_ERR_ARG, "read %llu: CIGAR, base or quality offsets leave their arrays",
                 (unsigned long long)c->ext.bad_read - 1);
   if (c->ext.unsorted) return fail(c, PG_ERR_ARG, "reads are not sorted by position within each reference");
+  c->mode_mq1 = 0;
+  for (uint32_t b = 1, best = 0; b <= 256; b++)
+    if (c->ext.mq1_hist[b] > best) { best = c->ext.mq1_hist[b]; c->mode_mq1 = b; }
   c->have_reads = true;
   c->have_results = false;
   return PG_OK;
@@ -405,6 +409,8 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   wa.R = c->R; wa.regions = d_regions; wa.tiles = P<WalkTile>(c->walk_tiles); wa.n_tiles = wn;
   wa.rec = rec; wa.stats = d_stats; wa.P = dp; wa.ref = P<uint8_t>(c->ref); wa.tile_width = c->tile_width;
   wa.packed = c->packed;
+  wa.mode_mq1 = c->mode_mq1;
+  wa.reads_per_pass = walk_reads_per_pass(dp.default_qual);
   while ((int32_t)c->wev.size() < 2 * (c->n_runs + 1)) {
     cudaEvent_t e;
     cudaEventCreate(&e);
@@ -559,7 +565,8 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
                           c->rec_ins_str.p, c->rec_ev_end.p, c->chunk_stats.p, c->stats.p, c->tile_sums.p};
     key = fnv(key, ptrs, sizeof ptrs);
     for (auto& b : c->rec_i32) key = fnv(key, &b.p, sizeof b.p);
-    const int32_t shape[6] = {c->tile_width, c->warps, c->packed, batched, (int32_t)c->event_cap, c->cand_cap};
+    const int32_t shape[7] = {c->tile_width, c->warps, c->packed, batched, (int32_t)c->event_cap, c->cand_cap,
+                              (int32_t)c->mode_mq1};
     key = fnv(key, shape, sizeof shape);
     key = fnv(key, &c->pool_cap, sizeof c->pool_cap);
     key = fnv(key, &c->spool_cap, sizeof c->spool_cap);

@@ -117,6 +117,9 @@ struct ReadExtent {      // maxima over the read store, for tile read ranges
   unsigned long long bad_read;  // 1 + index of a read whose offsets leave their arrays, else 0
   int32_t unsorted;      // 1 if positions decrease within one reference
   int32_t max_span;      // max(aend - pos + 1): how far before a window a read that overlaps it can start
+  // reads with simple CIGARs and qualities, by adjusted mq + 1 (1..256); the
+  // walk adds the reads of the most common value with one atomic per base
+  unsigned int mq1_hist[257];
 };
 
 struct DevParams {
@@ -129,9 +132,14 @@ struct DevParams {
 constexpr int kCallTile = 1024;     // positions per call / scan tile
 constexpr int kReadsPerChunk = 256;   // one read per thread of k_read_events
 // Reads one walk pass adds to a tile.  At most 4095 reads per position keep the
-// packed shared counters exact: count (12 bits) + mq sum (20 bits) in one word,
-// and every qual * (mq + 1) sum within int32 for either sign of qual.
+// packed shared counters exact: sum of qual (20 bits) + count (12 bits) in one
+// word for qualities up to 256 (a larger defaultQual lowers the pass size), and
+// the qual * (mq + 1 - M) sums within int32.
 constexpr int64_t kMaxReadsPerPass = 4095;
+inline int32_t walk_reads_per_pass(int32_t default_qual) {
+  const int32_t q = default_qual > 127 ? default_qual : 127;
+  return (int32_t)(kMaxReadsPerPass < 1048575 / q ? kMaxReadsPerPass : 1048575 / q);
+}
 
 // ---- Java integer helpers (wrapping Int, truncating division) -------------
 __host__ __device__ inline int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
@@ -351,6 +359,8 @@ struct WalkArgs {
   const uint8_t* ref;
   int32_t tile_width;
   int32_t packed;        // walk variant: lanes per simple read, 0 = 32, 1 = 16, 2 = 8
+  uint32_t mode_mq1;     // the read store's most common adjusted mq + 1 (any value gives the same sums)
+  int32_t reads_per_pass;  // reads one walk pass adds to a tile (kMaxReadsPerPass or fewer)
 };
 
 struct EventArgs {

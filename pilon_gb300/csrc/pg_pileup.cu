@@ -122,6 +122,12 @@ __global__ void k_read_extent(Reads R, ReadExtent* out, int4* desc) {
           simple ? (int32_t)((uint32_t)ld | ((uint32_t)tr << 16)) : (indel ? 1 : 0),
           (int32_t)((simple ? (uint32_t)mlen : 0u) | (hasQual ? kDescHasQual : 0u) | (simple ? kDescSimple : 0u)),
           (int32_t)((uint32_t)lrel | (pairOk ? kDescPairOk : 0u)), whi - pos);
+      // histogram of adjMq + 1 over the reads the walk's fast path takes, one
+      // atomic per distinct value in the warp
+      const uint32_t bin = (simple && hasQual) ? (uint32_t)(adjMq + 1) : 0u;
+      const unsigned act = __activemask();
+      const unsigned peers = __match_any_sync(act, bin);
+      if (bin && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&out->mq1_hist[bin], (unsigned)__popc(peers));
     }
   }
   lead = __reduce_max_sync(FULL, lead);
@@ -175,11 +181,17 @@ void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tile
 // parameter, so every counter address is one register plus an immediate) and
 // keeps its counters in shared memory, field-major so that lanes walking
 // consecutive bases of one read hit different banks:
-//   cm[4][T] | qs[4][T] | q[T] | bad[T] | clips[T]     (uint32, 44 B per position)
-// cm[b] = count of base b + (sum of mq + 1 over those bases) << 12, qs[b] = sum of
-// qual * (mq + 1), q = sum of qual.  These stay exact while a pass adds at most
-// kMaxReadsPerPass reads to a position; tiles with more reads run several passes
-// and add each pass's sums into the records.
+//   md[4][T] | qx[4][T] | mx[T] | bad[T] | clips[T]     (uint32, 44 B per position)
+// md[b] = sum of qual (20 bits) + count << 20 (12 bits) over the added bases b.
+// M (mode_mq1) is the read store's most common adjusted mq + 1; a read whose
+// mq + 1 is M + d also adds qual * d to qx[b] and d to mx.  At the flush
+//   qualSum[b] = M * (sum of qual of md[b]) + qx[b]
+//   mqSum      = M * (count of all four md) + mx,   qSum = sums of qual of md
+// which holds for any M, so the reads of the most common mq add a base with one
+// shared atomic and the others with three.  The words stay exact while a pass
+// adds at most reads_per_pass reads to a position (4095, fewer when defaultQual
+// exceeds 255 so that the qual sums keep within 20 bits); tiles with more reads
+// run several passes and add each pass's sums into the records.
 //
 // Each warp takes the tile's reads 32 at a time.  Every lane first builds the
 // descriptor of one read in registers: the filters of BamFile.process, the
@@ -195,17 +207,34 @@ __device__ inline uint32_t nib_at(const uint8_t* seq, int64_t so, int32_t k) {
   return (k & 1) ? (b & 15u) : (uint32_t)(b >> 4);
 }
 
+// PileUp.add of one base (S/PileUp.scala:75-84): dmq = mq + 1 - M.
 template <int T>
-__device__ inline void add_base(uint32_t* sm, int32_t p, uint32_t nib, int32_t qual, uint32_t mq1, int32_t min_qual) {
+__device__ inline void add_base(uint32_t* sm, int32_t p, uint32_t nib, int32_t qual, int32_t dmq, int32_t min_qual) {
   // nibble 1,2,4,8 (A,C,G,T) -> base index; anything else is not counted
   const uint32_t bi = (0x30210u >> (2 * nib)) & 3u;
   if (((0x116u >> nib) & 1u) && qual >= min_qual) {
     uint32_t* c = sm + p + bi * T;
-    atomicAdd(c, 1u + (mq1 << 12));
-    atomicAdd(c + 4 * T, (uint32_t)qual * mq1);
-    atomicAdd(sm + 8 * T + p, (uint32_t)qual);
+    atomicAdd(c, (uint32_t)qual + (1u << 20));
+    if (dmq) {
+      atomicAdd(c + 4 * T, (uint32_t)(qual * dmq));
+      atomicAdd(sm + 8 * T + p, (uint32_t)dmq);
+    }
   }
 }
+
+// prmt.b32 in its default mode: byte k of the result is byte (s >> 4k) & 7 of
+// {b:a}, or that byte's sign replicated when (s >> 4k) & 8.
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t s) {
+  uint32_t d;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(s));
+  return d;
+}
+// Base codes of four BAM nibbles by one prmt with the nibbles as selectors:
+// A (1) -> 0x40, C (2) -> 0x41, G (4) -> 0x42 from bytes 1, 2, 4 of the table;
+// T (8) -> the sign of byte 0 (0x80), 0xff; '=' (0) -> 0x80 and every other code
+// -> 0x00 (bytes 3, 5-7, or the clear signs of bytes 1-7).  Bit 6 marks
+// A/C/G/T and the low two bits are the base index.
+constexpr uint32_t kCodeLo = 0x00414080u, kCodeHi = 0x00000042u;
 
 __device__ inline bool nanopore_exclude(const uint8_t* cref, int32_t x, int32_t size) {
   // nanoporeExclude(index(locus)) indexes the whole contig with a region index
@@ -226,27 +255,41 @@ struct SegQ {
   int32_t pad;
 };
 constexpr int kSegQueue = 48;
+
 // clip word of a queued segment: trail 0xffff marks "no clips" (simple reads
 // have trailing clips below 0xffff)
 constexpr uint32_t kSegmentClip = 0xffffu << 16;
 
 // MINB: resident CTAs of 512 threads the register allocation must allow
 // (2: up to 64 registers per thread).  G: lanes per simple read (8, 16, 32).
+// dynamic shared memory of a walk CTA: counters and segment queues
+template <int T>
+constexpr size_t walk_smem(int warps) {
+  return (size_t)(11 * T + 4) * sizeof(uint32_t) + (size_t)warps * kSegQueue * sizeof(SegQ);
+}
+
 template <int T, int MINB, int G>
 __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_begin, int32_t tile_end) {
+  constexpr int kWords = 11 * T;
   extern __shared__ __align__(16) uint32_t sm_raw[];
   uint32_t* sm = sm_raw + 4;  // 4 words of padding in front of the counters
-  SegQ* segq = reinterpret_cast<SegQ*>(sm_raw + 11 * T + 4) + (threadIdx.x >> 5) * kSegQueue;
+  SegQ* segq = reinterpret_cast<SegQ*>(sm_raw + kWords + 4) + (threadIdx.x >> 5) * kSegQueue;
   __shared__ unsigned long long s_bc;
   __shared__ uint8_t s_perm[16][32];  // per warp: lane of the read in each round slot
   __shared__ int32_t s_next;          // next unclaimed read of the pass (offset)
-  uint32_t* s_bad = sm + 9 * T;
+  uint32_t* s_bad = sm + 9 * T;  // md = sm, qx = sm + 4T, mx = sm + 8T
   uint32_t* s_clip = sm + 10 * T;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int gl = lane % G, grp = lane / G;
   constexpr int NG = 32 / G;
   const Reads& R = a.R;
   const DevParams& P = a.P;
+  const uint32_t mode_mq1 = a.mode_mq1;
+  // minQual in every byte: ((q | 0x80) - minQual) keeps bit 7 iff q >= minQual,
+  // for q < 128; no quality byte passes a minQual above 127
+  const uint32_t minq4 = (uint32_t)min(max(P.min_qual, 0), 127) * 0x01010101u;
+  const uint32_t okall = P.min_qual <= 127 ? 0xffffffffu : 0u;
+  const int64_t per_pass = a.reads_per_pass;
 
   for (int32_t t = tile_begin + blockIdx.x; t < tile_end; t += gridDim.x) {
     const WalkTile tile = a.tiles[t];
@@ -256,10 +299,10 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
     unsigned long long bc = 0;
     if (threadIdx.x == 0) s_bc = 0;
 
-    for (int64_t c0 = tile.read_lo, pass = 0; pass == 0 || c0 < tile.read_hi; c0 += kMaxReadsPerPass, pass++) {
-      const int64_t c1 = min(c0 + kMaxReadsPerPass, tile.read_hi);
+    for (int64_t c0 = tile.read_lo, pass = 0; pass == 0 || c0 < tile.read_hi; c0 += per_pass, pass++) {
+      const int64_t c1 = min(c0 + per_pass, tile.read_hi);
       const int32_t npass = (int32_t)(c1 - c0);
-      for (int k = threadIdx.x; k < 11 * T + 4; k += blockDim.x) sm_raw[k] = 0;
+      for (int k = threadIdx.x; k < kWords + 4; k += blockDim.x) sm_raw[k] = 0;
       if (threadIdx.x == 0) s_next = 0;
       __syncthreads();
 
@@ -375,7 +418,8 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
                     int32_t qual = rhas ? (int32_t)(int8_t)rqp[rOff] : P.default_qual;
                     if (P.long_read == PG_NANOPORE && nanopore_exclude(cref, locus + ii - g.start, g.size)) qual = 0;
                     const uint8_t b = rsp[rOff >> 1];
-                    add_base<T>(sm, p, (rOff & 1) ? (b & 15u) : (uint32_t)(b >> 4), qual, rmq1, P.min_qual);
+                    add_base<T>(sm, p, (rOff & 1) ? (b & 15u) : (uint32_t)(b >> 4), qual,
+                                (int32_t)rmq1 - (int32_t)mode_mq1, P.min_qual);
                   } else {
                     atomicAdd(&s_bad[p], 1u);
                   }
@@ -402,6 +446,7 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
         // shared-memory atomics hit 32 different banks; the reads left over follow
         // in lane order.  Each lane computes its read's slot at once.
         __syncwarp();
+        const unsigned below = (1u << lane) - 1u;
         for (int q0 = -32; q0 < nq; q0 += 32) {
         if (q0 >= 0) {  // queued segments q0 .. q0 + 31 become the lanes' reads
           kind = kSkip;
@@ -420,21 +465,28 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
           }
         }
         const bool simple_kind = kind != kSkip && kind != kComplex;
-        const unsigned below = (1u << lane) - 1u;
         const unsigned sm_all = __ballot_sync(FULL, simple_kind);
         const int n_simple = __popc(sm_all);
         if (simple_kind) {
+          // reads of the most common mq first (so that rounds mix one-atomic and
+          // three-atomic adds at most once), interleaved by residue class; the rest after
+          const bool first = kind == kFast && mq1 == mode_mq1;
+          const unsigned set_a = __ballot_sync(sm_all, first);
           int slot;
-          if (NG == 4 || NG == 8) {  // with 8 groups, groups g and g + 4 share a residue class
-            const unsigned c0 = __ballot_sync(sm_all, cls == 0), c1 = __ballot_sync(sm_all, cls == 1);
-            const unsigned c2 = __ballot_sync(sm_all, cls == 2), c3 = __ballot_sync(sm_all, cls == 3);
-            const int m = min(min(__popc(c0), __popc(c1)), min(__popc(c2), __popc(c3)));
-            const unsigned mine = cls == 0 ? c0 : cls == 1 ? c1 : cls == 2 ? c2 : c3;
-            const int rank = __popc(mine & below);
-            const unsigned left = __ballot_sync(sm_all, rank >= m);
-            slot = rank < m ? 4 * rank + cls : 4 * m + __popc(left & below);
+          if (first) {
+            if (NG == 4 || NG == 8) {  // with 8 groups, groups g and g + 4 share a residue class
+              const unsigned c0 = __ballot_sync(set_a, cls == 0), c1 = __ballot_sync(set_a, cls == 1);
+              const unsigned c2 = __ballot_sync(set_a, cls == 2), c3 = __ballot_sync(set_a, cls == 3);
+              const int m = min(min(__popc(c0), __popc(c1)), min(__popc(c2), __popc(c3)));
+              const unsigned mine = cls == 0 ? c0 : cls == 1 ? c1 : cls == 2 ? c2 : c3;
+              const int rank = __popc(mine & below);
+              const unsigned left = __ballot_sync(set_a, rank >= m);
+              slot = rank < m ? 4 * rank + cls : 4 * m + __popc(left & below);
+            } else {
+              slot = __popc(set_a & below);
+            }
           } else {
-            slot = __popc(sm_all & below);
+            slot = __popc(set_a) + __popc(sm_all & ~set_a & below);
           }
           s_perm[warp][slot] = (uint8_t)lane;
         }
@@ -476,7 +528,6 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               const int32_t cf = e0 ? 1 : 0, cend = (ri1 - xs) >> 2;  // whole chunks [cf, cend)
               const int32_t fs = xs + 4 * cf, fe = xs + 4 * max(cend, cf);
               const int32_t he = min(fs, ri1), ts = max(fe, he), nh = he - ri0, nt = max(ri1 - ts, 0);
-              const uint32_t amq = 1u + (rmq1 << 12);
               // head and tail bases: loaded now, added after the chunks
               constexpr int kHT = (6 + G - 1) / G;  // head/tail bases per lane
               int32_t hx[kHT];
@@ -492,7 +543,6 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
                 }
               }
               const int32_t n0 = lead + xs;          // read offset of chunk 0's first base
-              const uint32_t psh = 4u * (uint32_t)(n0 & 1);  // chunks start on a low half-byte
               const uint32_t lastb = (uint32_t)((n0 & 1) + 3) >> 1;  // last byte of a chunk's nibbles
               const uint8_t* sb = rsp + (n0 >> 1);   // byte of chunk c's first nibble: sb + 2c
               // two chunks in flight ahead of the one being added
@@ -507,25 +557,38 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               uint32_t qv = 0, sv = 0, q1 = 0, s1 = 0;
               if (c < cend) load_chunk(c, qv, sv);
               if (c + G < cend) load_chunk(c + G, q1, s1);
+              // mq + 1 - M: 0 for the reads of the most common mq
+              const int32_t dmq = (int32_t)rmq1 - (int32_t)mode_mq1;
+              // Four bases at a time: the nibbles of the chunk select their codes
+              // (kCodeLo/Hi) by prmt; a second prmt puts code j in byte j.  sv holds
+              // the chunk's nibbles from its first byte on: with an even read offset
+              // bases 1, 0, 3, 2 in its low four nibbles; with an odd one bases 0 and
+              // 2 in nibbles 0 and 2, base 1 in nibble 3 and base 3 in nibble 5.
+              const uint32_t comb = (n0 & 1) ? 0x7230u : 0x2301u;
               while (c < cend) {
                 uint32_t q2 = 0, s2 = 0;
                 if (c + 2 * G < cend) load_chunk(c + 2 * G, q2, s2);
-                // nibbles in read order (BAM puts the first of a byte in its high half),
-                // base j of the chunk at bits 4j
-                const uint32_t nb = (((sv >> 4) & 0x0F0F0F0Fu) | ((sv & 0x0F0F0F0Fu) << 4)) >> psh;
+                const uint32_t code = prmt(prmt(kCodeLo, kCodeHi, sv), prmt(kCodeLo, kCodeHi, sv >> 8), comb);
+                // bit 6 of byte j: base j is A/C/G/T and its quality byte is in [minQual, 127]
+                const uint32_t ok = code & ((((qv | 0x80808080u) - minq4) & ~qv & 0x80808080u) >> 1) & okall;
+                const uint32_t qm = qv & ((ok >> 6) * 0x7fu);  // accepted qualities, 0 elsewhere
+                const uint32_t one4 = ok >> 2;                 // 0x10 in the bytes of accepted bases
+                const uint32_t bix = code & 0x03030303u;       // base index of byte j (0 when rejected)
                 uint32_t* cl = sm + (rpb + xs + 4 * c);
-                // every base adds, a rejected one (not A/C/G/T, or below minQual) adds 0:
-                // no branch per base
+                // base j adds qual + (1 << 20), built by one prmt: byte 0 = quality,
+                // byte 2 = 0x10 or 0, bytes 1 and 3 = the clear sign of a byte of one4;
+                // a rejected base adds 0 to row 0 (no branch per base)
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
-                  const uint32_t nib = (nb >> (4 * j)) & 15u;
-                  const int32_t qual = (int32_t)(int8_t)(qv >> (8 * j));
-                  const uint32_t bi = (0x30210u >> (2 * nib)) & 3u;
-                  const uint32_t ok = (0x116u >> nib) & (qual >= P.min_qual ? 1u : 0u);
-                  uint32_t* cp = cl + j + bi * T;
-                  atomicAdd(cp, amq * ok);
-                  atomicAdd(cp + 4 * T, (uint32_t)qual * rmq1 * ok);
-                  atomicAdd(cl + j + 8 * T, (uint32_t)qual * ok);
+                for (int j = 0; j < 4; j++)
+                  atomicAdd(cl + j + prmt(bix, 0u, 0x4440u | (uint32_t)j) * T,
+                            prmt(qm, one4, (uint32_t)(j | (12 + j) << 4 | (4 + j) << 8 | (12 + j) << 12)));
+                if (dmq) {  // qual * dmq to qx[b], dmq to mx (0 for a rejected base)
+#pragma unroll
+                  for (int j = 0; j < 4; j++) {
+                    atomicAdd(cl + 4 * T + j + prmt(bix, 0u, 0x4440u | (uint32_t)j) * T,
+                              prmt(qm, 0u, 0x4440u | (uint32_t)j) * (uint32_t)dmq);
+                    atomicAdd(cl + 8 * T + j, ((ok >> (8 * j + 6)) & 1u) * (uint32_t)dmq);
+                  }
                 }
                 c += G;
                 qv = q1; sv = s1; q1 = q2; s1 = s2;
@@ -534,13 +597,7 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               for (int h = 0; h < kHT; h++) {
                 if (hx[h] < 0) continue;
                 const uint32_t nib = ((lead + hx[h]) & 1) ? (hb[h] & 15u) : (hb[h] >> 4);
-                const int32_t qual = (int32_t)(int8_t)hq[h];
-                if (((0x116u >> nib) & 1u) && qual >= P.min_qual) {
-                  uint32_t* cp = sm + (rpb + hx[h]) + ((0x30210u >> (2 * nib)) & 3u) * T;
-                  atomicAdd(cp, amq);
-                  atomicAdd(cp + 4 * T, (uint32_t)qual * rmq1);
-                  atomicAdd(sm + (rpb + hx[h]) + 8 * T, (uint32_t)qual);
-                }
+                add_base<T>(sm, rpb + hx[h], nib, (int32_t)(int8_t)hq[h], dmq, P.min_qual);
               }
             } else if (rk == kInvalid) {
               for (int32_t ii = ri0 + gl; ii < ri1; ii += G) atomicAdd(&s_bad[rpb + ii], 1u);
@@ -552,7 +609,7 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
                 const uint32_t nib = (rOff & 1) ? (b & 15u) : (uint32_t)(b >> 4);
                 int32_t qual = rhas ? (int32_t)(int8_t)rqp[ii] : P.default_qual;
                 if (P.long_read == PG_NANOPORE && nanopore_exclude(cref, rpos + ii - g.start, g.size)) qual = 0;
-                add_base<T>(sm, rpb + ii, nib, qual, rmq1, P.min_qual);
+                add_base<T>(sm, rpb + ii, nib, qual, (int32_t)rmq1 - (int32_t)mode_mq1, P.min_qual);
               }
             }
             if (trail > 0 && clips) {  // clipStart = locus (clip after the aligned bases), clipEnd = locus + len - 1
@@ -573,13 +630,17 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
       // flush: the first pass stores, later passes add (the CTA owns the tile)
       for (int32_t p = threadIdx.x; p < tile.len; p += blockDim.x) {
         const int64_t gp = g.pos_base + tile.lo + p;
-        const uint32_t m0 = sm[p], m1 = sm[T + p], m2 = sm[2 * T + p], m3 = sm[3 * T + p];
-        const int4 c = make_int4((int)(m0 & 0xFFFu), (int)(m1 & 0xFFFu), (int)(m2 & 0xFFFu), (int)(m3 & 0xFFFu));
-        const int32_t mqs = (int32_t)((m0 >> 12) + (m1 >> 12) + (m2 >> 12) + (m3 >> 12));
-        // per-pass qual sums fit int32 for either sign of qual (4095 reads x 128 x 256 < 2^31)
-        const longlong2 q01 = make_longlong2((int32_t)sm[4 * T + p], (int32_t)sm[5 * T + p]);
-        const longlong2 q23 = make_longlong2((int32_t)sm[6 * T + p], (int32_t)sm[7 * T + p]);
-        const int32_t qsum = (int32_t)sm[8 * T + p];
+        const uint32_t M = mode_mq1;
+        const uint32_t w0 = sm[p], w1 = sm[T + p], w2 = sm[2 * T + p], w3 = sm[3 * T + p];
+        const int4 c = make_int4((int)(w0 >> 20), (int)(w1 >> 20), (int)(w2 >> 20), (int)(w3 >> 20));
+        const uint32_t s0 = w0 & 0xFFFFFu, s1 = w1 & 0xFFFFFu, s2 = w2 & 0xFFFFFu, s3 = w3 & 0xFFFFFu;
+        // qx and mx hold signed per-pass sums within int32
+        const longlong2 q01 = make_longlong2((long long)M * s0 + (int32_t)sm[4 * T + p],
+                                             (long long)M * s1 + (int32_t)sm[5 * T + p]);
+        const longlong2 q23 = make_longlong2((long long)M * s2 + (int32_t)sm[6 * T + p],
+                                             (long long)M * s3 + (int32_t)sm[7 * T + p]);
+        const int32_t mqs = wadd((int32_t)(M * (uint32_t)(c.x + c.y + c.z + c.w)), (int32_t)sm[8 * T + p]);
+        const int32_t qsum = (int32_t)(s0 + s1 + s2 + s3);
         if (pass == 0) {
           a.rec.count[gp] = c;
           a.rec.qual_sum[2 * gp] = q01;
@@ -619,13 +680,13 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
 
 template <int T, int MINB, int G>
 static void launch_walk_t(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s) {
-  const size_t smem = (size_t)(11 * T + 4) * sizeof(uint32_t) + (size_t)warps * kSegQueue * sizeof(SegQ);
+  const size_t smem = walk_smem<T>(warps);
   // attribute and occupancy are queried once per (kernel, warps): the first
   // launch of a shape is never inside a stream capture
   static bool configured = false;
   static int per_sm_of[17] = {0};
   if (!configured) {  // room for the largest CTA (16 warps of segment queues)
-    const size_t smem_max = (size_t)(11 * T + 4) * sizeof(uint32_t) + (size_t)16 * kSegQueue * sizeof(SegQ);
+    const size_t smem_max = walk_smem<T>(16);
     cudaFuncSetAttribute(k_walk<T, MINB, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     configured = true;
   }

@@ -2,7 +2,10 @@
 store, regions without reads, a 1-bp region, unmapped placed reads, every
 CIGAR operator (M = X I D N S H P), reads that are all clips, absent
 qualities, N bases, flags that validateRead drops (S/BamFile.scala:101-105),
-improper pairs, long insertions (string pool) and reads at the contig ends."""
+improper pairs, long insertions (string pool), quality bytes of 128 and
+above (negative Java bytes), and reads at the contig ends."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -69,6 +72,9 @@ def _records(ref0, ref1):
         dict(pos=700, cigar=[(30, "M"), (20, "I"), (30, "M")], seq=s0[699:729] + "ACGTTGCAACGTTGCAACGT"
              + s0[729:759], qual=q(80)),                                                    # long insertion
         dict(pos=760, cigar=[(30, "M"), (15, "D"), (30, "M")], seq=s0[759:789] + s0[804:834], qual=q(60)),
+        dict(pos=880, cigar=[(60, "M")], seq=s0[879:939],                                  # negative Java quals
+             qual=q(10) + [130, 200, 255, 128, 127, 0, 129, 254] + q(42)),
+        dict(pos=900, cigar=[(60, "M")], seq=s0[899:959], qual=[127] * 60),                # the largest accepted
         dict(pos=1, cigar=[(20, "S"), (40, "M")], seq="A" * 20 + s0[0:40], qual=q(60)),    # clip before the start
         dict(pos=2975, cigar=[(26, "M"), (30, "S")], seq=s0[2974:3000] + "C" * 30, qual=q(56)),  # clip past the end
     ]
@@ -136,3 +142,39 @@ def test_empty_read_store(engine, edge_ds):
         got = engine.fetch(r)
         compare_region(got, want[r], f"empty store region {r}")
         assert got.stats.read_count == 0
+
+
+def _run_tuned(engine, ds, p, variant, label):
+    regions = _regions(ds)
+    engine.set_reference(ds.contigs)
+    engine.set_reads(ds.reads)
+    engine.set_tuning(1024, 16, variant)
+    try:
+        engine.pileup_regions(regions, p)
+        want = oracle_regions(ds, p, regions)
+        for r in range(len(regions)):
+            compare_region(engine.fetch(r), want[r], f"{label} variant {variant} region {regions[r][:3]}")
+    finally:
+        engine.set_tuning(2048, 16, 0)
+
+
+@pytest.mark.parametrize("variant", [0, 2])
+@pytest.mark.parametrize("min_qual", [0, 1, 127, 128, 200])
+def test_min_qual_bounds(engine, edge_ds, min_qual, variant):
+    """minQual at the bounds of a signed quality byte: 127 still accepts
+    quality 127, 128 and above accept nothing; quality bytes of 128 and above
+    are rejected at every minQual."""
+    _run_tuned(engine, edge_ds, _abi.default_params(min_qual=min_qual), variant, f"minQual {min_qual}")
+
+
+@pytest.mark.parametrize("variant", [0, 2])
+@pytest.mark.parametrize("mapq", [0, 17, 255])
+def test_store_wide_mapq(engine, edge_ds, mapq, variant):
+    """The walk adds the reads of the store's most common adjusted mapq with
+    one atomic per base and corrects the others' sums by their difference to
+    it; every most common mapq, 0 and 255 included, gives the oracle's sums.
+    A few reads keep mapq 60 beside the others."""
+    mq = np.full(edge_ds.reads.n_reads, mapq, np.uint8)
+    mq[::11] = 60
+    ds = DS(edge_ds.contigs, dataclasses.replace(edge_ds.reads, mapq=mq))
+    _run_tuned(engine, ds, _abi.default_params(), variant, f"mapq {mapq}")
