@@ -432,7 +432,9 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   ea.indel_list = P<int64_t>(c->indel_list);
   launch_read_events(ea, ch0, chn, s);
 
-  launch_region_prep(d_regions + r0, d_stats + r0, P<ChunkStats>(c->chunk_stats), r1 - r0, dp, s);
+  int32_t max_chunks = 0;
+  for (int32_t r = r0; r < r1; r++) max_chunks = std::max(max_chunks, c->regions_h[r].n_chunks);
+  launch_region_prep(d_regions + r0, d_stats + r0, P<ChunkStats>(c->chunk_stats), r1 - r0, max_chunks, dp, s);
   launch_physcov_scan(d_regions, P<int32_t>(c->call_tile_region), t0, tn, rec, d_stats, P<int32_t>(c->tile_sums),
                       r0, r1 - r0, s);
   launch_event_scatter(P<Event>(c->events), &counters[CNT_EVENTS], rec.ev_end, P<Event>(c->events_sorted), s,

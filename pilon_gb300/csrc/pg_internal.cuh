@@ -412,7 +412,7 @@ void launch_physcov_scan(const RegionDev* regions, const int32_t* call_tile_regi
                          int32_t n_tiles, Records rec, const StatsDev* stats, int32_t* tile_sums,
                          int32_t region_begin, int32_t n_regions, cudaStream_t s);
 void launch_region_prep(const RegionDev* regions, StatsDev* stats, const ChunkStats* chunk_stats,
-                        int32_t n_regions, DevParams P, cudaStream_t s);
+                        int32_t n_regions, int32_t max_chunks, DevParams P, cudaStream_t s);
 void launch_call(const CallArgs& a, int32_t tile_begin, int32_t n_tiles, cudaStream_t s);
 void launch_cand_list(const CallArgs& a, const int32_t* cand_off, Cand* cands, int32_t cand_cap,
                       int32_t tile_begin, int32_t n_tiles, cudaStream_t s);

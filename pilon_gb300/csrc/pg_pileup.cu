@@ -150,30 +150,48 @@ void launch_read_extent(const Reads& R, ReadExtent* out, int4* desc, cudaStream_
 }
 
 // ---------------------------------------------------------------------------
-__device__ inline int64_t lower_bound_pos(const int32_t* pos, int64_t lo, int64_t hi, int64_t v) {
-  while (lo < hi) {
-    int64_t m = (lo + hi) >> 1;
-    if ((int64_t)pos[m] < v) lo = m + 1; else hi = m;
+// First index in [lo, hi) whose position is >= v (hi if none), by a warp: each
+// step the 32 lanes sample the range at even strides and keep the stretch
+// between the last sample below v and the next one, so a range of n reads
+// takes about log32(n) steps of independent loads.
+__device__ inline int64_t warp_lower_bound_pos(const int32_t* pos, int64_t lo, int64_t hi, int64_t v, int lane) {
+  while (hi - lo > 32) {  // the answer lies in [lo, hi]
+    const int64_t step = (hi - lo + 31) / 32;
+    const int64_t sk = lo + lane * step;
+    const unsigned below = __ballot_sync(FULL, sk < hi && (int64_t)pos[sk] < v);
+    const int c = __popc(below);  // samples below v: lanes 0 .. c - 1
+    if (c == 0) return lo;
+    const int64_t nlo = lo + (int64_t)(c - 1) * step + 1;
+    const int64_t sc = lo + (int64_t)c * step;
+    hi = (c < 32 && sc < hi) ? sc : hi;
+    lo = nlo;
   }
-  return lo;
+  const unsigned below = __ballot_sync(FULL, lo + lane < hi && (int64_t)pos[lo + lane] < v);
+  return lo + __popc(below);
 }
 
+// One warp per tile.
 __global__ void k_tile_ranges(Reads R, const RegionDev* regions, WalkTile* tiles, int32_t n_tiles,
                               const ReadExtent* ext) {
-  int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_tiles) return;
+  const int32_t t = (int32_t)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (t >= n_tiles) return;  // whole warps leave together
   WalkTile& T = tiles[t];
   const RegionDev& g = regions[T.region];
-  int64_t tlo = (int64_t)g.start + T.lo, thi = tlo + T.len - 1;
-  int64_t a = tlo - ext->max_back, b = thi + ext->max_lead + 1;
-  T.read_lo = lower_bound_pos(R.pos, g.read_begin, g.read_end, a);
-  T.read_hi = lower_bound_pos(R.pos, T.read_lo, g.read_end, b);
+  const int64_t tlo = (int64_t)g.start + T.lo, thi = tlo + T.len - 1;
+  const int64_t a = tlo - ext->max_back, b = thi + ext->max_lead + 1;
+  const int64_t rlo = warp_lower_bound_pos(R.pos, g.read_begin, g.read_end, a, lane);
+  const int64_t rhi = warp_lower_bound_pos(R.pos, rlo, g.read_end, b, lane);
+  if (lane == 0) {
+    T.read_lo = rlo;
+    T.read_hi = rhi;
+  }
 }
 
 void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tiles, int32_t n_tiles,
                         const ReadExtent* ext, cudaStream_t s) {
   if (n_tiles == 0) return;
-  k_tile_ranges<<<(n_tiles + 255) / 256, 256, 0, s>>>(R, regions, tiles, n_tiles, ext);
+  k_tile_ranges<<<(int)(((int64_t)n_tiles * 32 + 255) / 256), 256, 0, s>>>(R, regions, tiles, n_tiles, ext);
 }
 
 // ---------------------------------------------------------------------------
@@ -826,16 +844,61 @@ __global__ void __launch_bounds__(kEvThreads, 16) k_read_events(EventArgs a, int
 
 // The I and D operators of the listed reads (S/PileUpRegion.scala:150-183):
 // left shift, H1 double count, the indel counters and the events for the
-// vote.  One thread per listed read, so a warp walks 32 reads with indels.
-constexpr int kIndelThreads = 128;
-__global__ void __launch_bounds__(kIndelThreads) k_read_indels(EventArgs a, int32_t chunk_begin) {
+// vote.  Each warp takes the lists of kIndelChunks chunks (a few per cent of
+// their reads have indels) and walks their union 32 reads at a time, one
+// read per thread: the in-warp scan of the lists' lengths gives each entry's
+// list, as the last list starting at or before it.
+constexpr int kIndelThreads = 128, kIndelChunks = 4;
+__global__ void __launch_bounds__(kIndelThreads) k_read_indels(EventArgs a, int32_t chunk_begin, int32_t chunk_end) {
+  __shared__ uint8_t s_lane[kIndelThreads / 32][32];  // per warp: lane of the k-th non-empty list
   const Reads& R = a.R;
   const DevParams& P = a.P;
-  constexpr int kPer = kReadsPerChunk / kIndelThreads;
-  const int32_t ch = chunk_begin + blockIdx.x / kPer;
-  const int32_t slot = (blockIdx.x % kPer) * kIndelThreads + threadIdx.x;
-  if (slot < a.chunk_stats[ch].n_indel) {
-    const int64_t i = a.indel_list[(int64_t)ch * kReadsPerChunk + slot];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int32_t c0 = chunk_begin + (int32_t)(((int64_t)blockIdx.x * kIndelThreads + threadIdx.x) >> 5) * kIndelChunks;
+  if (c0 >= chunk_end) return;  // whole warps leave together
+  const int32_t cnt = (lane < kIndelChunks && c0 + lane < chunk_end) ? a.chunk_stats[c0 + lane].n_indel : 0;
+  int32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t v = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int32_t E = incl - cnt, total = __shfl_sync(FULL, incl, 31);
+  const unsigned ne = __ballot_sync(FULL, cnt > 0);
+  if (cnt > 0) s_lane[wib][__popc(ne & ((1u << lane) - 1u))] = (uint8_t)lane;
+  __syncwarp();
+  for (int32_t k0 = 0; k0 < total; k0 += 32) {
+    // the non-empty list holding entry k0, then one more per list start in (k0, k0 + lane]
+    const int r0 = __popc(__ballot_sync(FULL, cnt > 0 && E <= k0)) - 1;
+    const uint32_t st = (cnt > 0 && E > k0 && E < k0 + 32) ? 1u << (E - k0) : 0u;
+    const int rk = r0 + __popc(__reduce_or_sync(FULL, st) & ((2u << lane) - 1u));
+    const int own = k0 + lane < total ? (int)s_lane[wib][rk] : lane;
+    const int32_t ownE = __shfl_sync(FULL, E, own);
+    const int32_t ch = c0 + own;
+    int64_t i = -1;
+    int32_t n_id = 0;  // I and D operators of the read: one event slot each
+    if (k0 + lane < total) {
+      i = a.indel_list[(int64_t)ch * kReadsPerChunk + (k0 + lane - ownE)];
+      const int64_t co = R.cigar_off[i];
+      const int nc = R.n_cigar[i];
+      for (int k = 0; k < nc; k++) {
+        const uint32_t op = R.cigar[co + k] & 15u;
+        n_id += (op == 1u || op == 2u);
+      }
+    }
+    // the warp's event slots, reserved with one atomic; an operator that adds
+    // no event leaves its slot empty (gpos -1), which k_event_scatter skips
+    int32_t ev_incl = n_id;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t v = __shfl_up_sync(FULL, ev_incl, o);
+      if (lane >= o) ev_incl += v;
+    }
+    unsigned long long ev_base = 0;
+    if (lane == 31 && ev_incl > 0) ev_base = atomicAdd(a.n_events, (unsigned long long)ev_incl);
+    ev_base = __shfl_sync(FULL, ev_base, 31);
+    if (i < 0) continue;
+    unsigned long long ev_next = ev_base + (unsigned long long)(ev_incl - n_id);
     const ReadChunk C = a.chunks[ch];
     const RegionDev g = a.regions[C.region];
     const uint8_t* cref = a.ref + g.ref_off;
@@ -875,6 +938,8 @@ __global__ void __launch_bounds__(kIndelThreads) k_read_indels(EventArgs a, int3
         const int32_t len = (int32_t)(w >> 4);
         const int op = (int)(w & 15u);
         const int32_t locus = pos + refOffset;
+        const unsigned long long my_slot = (op == 1 || op == 2) ? ev_next++ : 0ull;
+        bool wrote = false;
         if (op == 1 && trusted(readOffset) && inRegion(locus)) {
           int32_t iloc = locus;
           int32_t rot = 0;
@@ -900,7 +965,8 @@ __global__ void __launch_bounds__(kIndelThreads) k_read_indels(EventArgs a, int3
             atomicAdd(&a.rec.ins_qual[gp], indelMq + 1);
             atomicAdd(&a.rec.q_sum[gp], (hasQual ? (int32_t)(int8_t)rqual[readOffset] : P.default_qual));
             atomicAdd(&a.rec.insertions[gp], 1);
-            unsigned long long slot = atomicAdd(a.n_events, 1ull);
+            const unsigned long long slot = my_slot;
+            wrote = true;
             if ((int64_t)slot < a.event_cap) {
               Event e;
               e.gpos = gp; e.read = i; e.region = C.region; e.len = len; e.roff = readOffset; e.kind_rot = rot;
@@ -976,7 +1042,8 @@ __global__ void __launch_bounds__(kIndelThreads) k_read_indels(EventArgs a, int3
             atomicAdd(&a.rec.del_qual[gp], indelMq + 1);
             atomicAdd(&a.rec.q_sum[gp], (hasQual ? (int32_t)(int8_t)rqual[readOffset] : P.default_qual));
             atomicAdd(&a.rec.deletions[gp], 1);
-            unsigned long long slot = atomicAdd(a.n_events, 1ull);
+            const unsigned long long slot = my_slot;
+            wrote = true;
             if ((int64_t)slot < a.event_cap) {
               Event e;
               e.gpos = gp; e.read = i; e.region = C.region; e.len = len; e.roff = rloc;
@@ -988,6 +1055,7 @@ __global__ void __launch_bounds__(kIndelThreads) k_read_indels(EventArgs a, int3
           }
         }
       next_op:
+        if ((op == 1 || op == 2) && !wrote && (int64_t)my_slot < a.event_cap) a.events[my_slot].gpos = -1;
         if (op == 0 || op == 1 || op == 4 || op == 7 || op == 8) readOffset += len;
         if (op == 0 || op == 2 || op == 3 || op == 7 || op == 8) refOffset += len;
       }
@@ -1002,7 +1070,9 @@ void launch_read_events(const EventArgs& a, int32_t chunk_begin, int32_t chunk_c
   if (chunk_count <= 0) return;
   cudaMemsetAsync(a.chunk_stats + chunk_begin, 0, sizeof(ChunkStats) * (size_t)chunk_count, s);
   k_read_events<<<chunk_count * kEvPerChunk, kEvThreads, 0, s>>>(a, chunk_begin, chunk_begin + chunk_count);
-  k_read_indels<<<chunk_count * (kReadsPerChunk / kIndelThreads), kIndelThreads, 0, s>>>(a, chunk_begin);
+  const int64_t warps = ((int64_t)chunk_count + kIndelChunks - 1) / kIndelChunks;
+  k_read_indels<<<(int)((warps * 32 + kIndelThreads - 1) / kIndelThreads), kIndelThreads, 0, s>>>(
+      a, chunk_begin, chunk_begin + chunk_count);
 }
 
 // ---------------------------------------------------------------------------
@@ -1053,6 +1123,7 @@ __global__ void k_event_scatter(const Event* ev, const unsigned long long* n_eve
   int64_t n = min((int64_t)*n_events, max_events);
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     const Event e = ev[k];
+    if (e.gpos < 0) continue;  // a reserved slot that got no event
     const int32_t slot = atomicAdd(&ev_end[e.gpos], 1);
     if (slot >= 0 && slot < max_events) out[slot] = e;
   }
@@ -1224,10 +1295,10 @@ __device__ inline int64_t java_round(double x) {
   return (int64_t)((x - f >= 0.5) ? f + 1.0 : f);
 }
 
-// One CTA per region: adds up the per-chunk partial statistics, then
-// computes minDepth.
-__global__ void __launch_bounds__(256) k_region_prep(const RegionDev* regions, StatsDev* stats,
-                                                      const ChunkStats* cs, DevParams P) {
+// One CTA per region (256 or 1024 threads): adds up the per-chunk partial
+// statistics, then computes minDepth.
+__global__ void __launch_bounds__(1024) k_region_prep(const RegionDev* regions, StatsDev* stats,
+                                                       const ChunkStats* cs, DevParams P) {
   __shared__ unsigned long long s_u[8];
   __shared__ int32_t s_i[3];
   const int32_t r = blockIdx.x;
@@ -1279,9 +1350,9 @@ __global__ void __launch_bounds__(256) k_region_prep(const RegionDev* regions, S
 }
 
 void launch_region_prep(const RegionDev* regions, StatsDev* stats, const ChunkStats* chunk_stats,
-                        int32_t n_regions, DevParams P, cudaStream_t s) {
+                        int32_t n_regions, int32_t max_chunks, DevParams P, cudaStream_t s) {
   if (n_regions == 0) return;
-  k_region_prep<<<n_regions, 256, 0, s>>>(regions, stats, chunk_stats, P);
+  k_region_prep<<<n_regions, max_chunks > 2048 ? 1024 : 256, 0, s>>>(regions, stats, chunk_stats, P);
 }
 
 }  // namespace pg
