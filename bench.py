@@ -505,30 +505,73 @@ def main():
               "timing": "host wall clock of pg_find_breaks (device kernels, sorted list read back)"}
 
     # end to end through the C ABI: H2D of the read store from pinned memory,
-    # pileup + calls, D2H of every region's records and calls
+    # pileup + calls, D2H of every region's records and calls.  Measured with
+    # one engine context (each step's calls wait for the previous step's) and
+    # with two contexts on two host threads, the way a host serves several
+    # requests: one context's read-back overlaps the other's upload.
     e2e = None
     if not args.no_e2e:
         fields = args.e2e_fields if args.e2e_fields != "auto" else ("all" if sum(lens) <= 20_000_000 else "calls")
         pin = pinned_store(ds.reads)
-        out = PinnedOut(sum(e - s + 1 for (c, s, e, a, b) in regions), fields)  # all regions, one after another
+        n_pos = sum(e - s + 1 for (c, s, e, a, b) in regions)
+        outs = [PinnedOut(n_pos, fields)]  # all regions, one after another
         h2d = pin.nbytes()
-        d2h = out.nbytes()
+        d2h = outs[0].nbytes()
+
+        def e2e_step(e, o):
+            e.set_reads(pin)
+            e.pileup_regions(regions, params, batched=bool(args.batched))
+            e.fetch_all(o.arrays)
+
         for _ in range(args.warmup):
-            eng.set_reads(pin)
-            eng.pileup_regions(regions, params, batched=bool(args.batched))
-            eng.fetch_all(out.arrays)
+            e2e_step(eng, outs[0])
         barrier(dist)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            eng.set_reads(pin)
-            eng.pileup_regions(regions, params, batched=bool(args.batched))
-            eng.fetch_all(out.arrays)
+            e2e_step(eng, outs[0])
         eng.sync()
-        e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+        one_s = max_over_ranks(dist, time.perf_counter() - t0)
         barrier(dist)
-        e2e = {"value": units * ws * args.steps / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / args.steps, "read_back": fields,
-               "timing": "host wall clock; every call synchronises the engine stream"}
+
+        shape = (tuning["tile_width"], tuning["warps"], tuning["variant"]) if tuning else \
+            (args.tile, args.warps, args.variant)
+        eng2 = Engine(local)
+        eng2.set_tuning(*shape)
+        eng2.set_reference(ds.contigs)
+        outs.append(PinnedOut(n_pos, fields))
+        engines = [eng, eng2]
+        for _ in range(args.warmup):
+            e2e_step(eng2, outs[1])
+        import threading
+        counts = [(args.steps + 1) // 2, args.steps // 2]
+        errs = []
+
+        def worker(k):
+            try:
+                for _ in range(counts[k]):
+                    e2e_step(engines[k], outs[k])
+                engines[k].sync()
+            except Exception as ex:  # reported after the join
+                errs.append(ex)
+
+        barrier(dist)
+        t0 = time.perf_counter()
+        ths = [threading.Thread(target=worker, args=(k,)) for k in range(2)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        two_s = max_over_ranks(dist, time.perf_counter() - t0)
+        barrier(dist)
+        eng2.close()
+        if errs:
+            raise errs[0]
+        e2e = {"value": units * ws * args.steps / two_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * two_s / args.steps, "read_back": fields,
+               "contexts": 2,
+               "one_context": {"value": units * ws * args.steps / one_s / 1e9, "ms_per_step": 1e3 * one_s / args.steps},
+               "timing": "host wall clock; every call synchronises its context's stream; two contexts on two "
+                         "host threads take alternate steps"}
 
     kmer = kmer_bench(eng, ds, params, args, threads) if args.config == 4 and rank == 0 else None
 

@@ -68,11 +68,13 @@ __global__ void __launch_bounds__(kCallThreads, 6) k_call(CallArgs a, int32_t ti
       const bool isIns = f & PG_CALL_INS, isDel = f & PG_CALL_DEL;
       const bool called = (f & PG_CALL_HAS_BASE) || isIns || isDel;
       if (depth >= st.min_depth && rb != 'N' && called) {
-        const uint8_t b = (f & PG_CALL_HAS_BASE) ? (uint8_t)"ACGT"[f & 3u] : (uint8_t)'N';
-        const uint8_t alt = (uint8_t)"ACGT"[(f >> 2) & 3u];
+        // 'A','C','G','T' are the bytes of 0x54474341
+        const uint8_t b = (f & PG_CALL_HAS_BASE) ? (uint8_t)(0x54474341u >> (8 * (f & 3u))) : (uint8_t)'N';
+        const uint8_t alt = (uint8_t)(0x54474341u >> (8 * ((f >> 2) & 3u)));
         const bool homo = f & PG_CALL_HOMO, homoIndel = f & PG_CALL_HOMO_INDEL;
-        const int64_t q = n > 0 ? div_s64(o.score, n) : 0;
-        if (homo && b == rb && q >= 10 && !(isIns || isDel)) f |= PG_CALL_CONFIRMED;
+        // highConfidence: q = score / n >= 10 (q = 0 when n = 0), i.e. score >= 10 n for n > 0
+        const bool highConf = n > 0 && o.score >= 10 * n;
+        if (homo && b == rb && highConf && !(isIns || isDel)) f |= PG_CALL_CONFIRMED;
         else if (isIns && homoIndel) change = PG_CHANGE_INS;
         else if (isDel && homoIndel) change = PG_CHANGE_DEL;
         else if (b != rb && o.score > 0) {
