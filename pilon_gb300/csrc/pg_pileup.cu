@@ -848,7 +848,7 @@ __global__ void __launch_bounds__(kEvThreads, 16) k_read_events(EventArgs a, int
 // their reads have indels) and walks their union 32 reads at a time, one
 // read per thread: the in-warp scan of the lists' lengths gives each entry's
 // list, as the last list starting at or before it.
-constexpr int kIndelThreads = 128, kIndelChunks = 4;
+constexpr int kIndelThreads = 128, kIndelChunks = 2;
 __global__ void __launch_bounds__(kIndelThreads) k_read_indels(EventArgs a, int32_t chunk_begin, int32_t chunk_end) {
   __shared__ uint8_t s_lane[kIndelThreads / 32][32];  // per warp: lane of the k-th non-empty list
   const Reads& R = a.R;
