@@ -77,7 +77,7 @@ def build(force=False, verbose=False):
         _run_all(cmds)
     if force or not _newer(ENGINE, objs):
         _run_all([[nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", ENGINE] + objs
-                  + ["-lcudart"]])
+                  + ["-lcudart", "-ldl"]])
     return ENGINE
 
 

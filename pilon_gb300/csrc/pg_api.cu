@@ -9,10 +9,21 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "pg_internal.cuh"
 #include "pg_kmer.cuh"
 #include "pg_breaks.cuh"
 #include "pg_format.cuh"
+
+// NVTX range over one entry point (a profiler shows the host side of each call;
+// without a tool attached a push/pop costs a few nanoseconds)
+namespace {
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+};
+}  // namespace
 
 using namespace pg;
 
@@ -283,6 +294,7 @@ pg_status pg_sync(pg_ctx* c) {
 }
 
 pg_status pg_set_reference(pg_ctx* c, int32_t n, const int64_t* lens, const uint8_t* const* bases) {
+  const Range nvtx_range("pg_set_reference");
   if (!c || n < 0 || (n > 0 && (!lens || !bases))) return fail(c, PG_ERR_ARG, "bad reference arguments");
   cudaSetDevice(c->device);
   c->ref_off.assign(n, 0);
@@ -326,6 +338,7 @@ static pg_status finish_reads(pg_ctx* c) {
 }
 
 pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
+  const Range nvtx_range("pg_set_reads");
   if (!c || !h || h->n_reads < 0) return fail(c, PG_ERR_ARG, "bad reads");
   cudaSetDevice(c->device);
   const int64_t n = h->n_reads;
@@ -353,6 +366,7 @@ pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
 }
 
 pg_status pg_set_reads_device(pg_ctx* c, const pg_reads* d) {
+  const Range nvtx_range("pg_set_reads_device");
   if (!c || !d || d->n_reads < 0) return fail(c, PG_ERR_ARG, "bad reads");
   cudaSetDevice(c->device);
   Reads& R = c->R;
@@ -462,6 +476,7 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
 
 pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions, const pg_params* params,
                             int32_t batched) {
+  const Range nvtx_range("pg_pileup_regions");
   if (!c || (n_regions > 0 && !regs) || !params || n_regions < 0) return fail(c, PG_ERR_ARG, "bad arguments");
   if (!c->have_reads) return fail(c, PG_ERR_STATE, "pg_set_reads must come first");
   if (params->min_qual < 0 || params->flank < 0 || params->min_mq < 0)
@@ -706,6 +721,7 @@ static pg_status fetch_positions(pg_ctx* c, int64_t b, size_t n, pg_region_out* 
 }
 
 pg_status pg_fetch_region(pg_ctx* c, int32_t r, pg_region_out* o) {
+  const Range nvtx_range("pg_fetch_region");
   if (!c || !o) return PG_ERR_ARG;
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
   if (r < 0 || r >= c->n_regions) return fail(c, PG_ERR_ARG, "region %d out of range", r);
@@ -715,6 +731,7 @@ pg_status pg_fetch_region(pg_ctx* c, int32_t r, pg_region_out* o) {
 }
 
 pg_status pg_fetch_all(pg_ctx* c, pg_region_out* o) {
+  const Range nvtx_range("pg_fetch_all");
   if (!c || !o) return PG_ERR_ARG;
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
   cudaSetDevice(c->device);
@@ -732,6 +749,7 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
 
 pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K, const pg_params* params,
                         int32_t min_depth, pg_kmer_edge* edges, int64_t cap, int64_t* n_edges) {
+  const Range nvtx_range("pg_kmer_tally");
   if (!c || (n_windows > 0 && !windows) || !params || n_windows < 0 || cap < 0 || !n_edges)
     return fail(c, PG_ERR_ARG, "bad arguments");
   if (K < 1 || K > 31) return fail(c, PG_ERR_LIMIT, "K = %d: the GPU tally packs K-mers in 64 bits (K <= 31)", K);
@@ -891,6 +909,7 @@ static pg_status find_breaks_device(pg_ctx* c, int32_t min_min_depth) {
 }
 
 pg_status pg_find_breaks(pg_ctx* c, int32_t min_min_depth, pg_break* out, int64_t cap, int64_t* n_breaks) {
+  const Range nvtx_range("pg_find_breaks");
   if (!c || !n_breaks || cap < 0 || (cap > 0 && !out)) return fail(c, PG_ERR_ARG, "bad arguments");
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no pileup results: call pg_pileup_regions first");
   cudaSetDevice(c->device);
@@ -910,6 +929,7 @@ pg_status pg_find_breaks(pg_ctx* c, int32_t min_min_depth, pg_break* out, int64_
 pg_status pg_kmer_tally_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius, int32_t K, const pg_params* params,
                                int32_t min_depth, pg_kmer_edge* edges, int64_t cap, int64_t* n_windows,
                                int64_t* n_edges) {
+  const Range nvtx_range("pg_kmer_tally_breaks");
   if (!c || !params || cap < 0 || !n_edges || !n_windows || radius < 0) return fail(c, PG_ERR_ARG, "bad arguments");
   if (K < 1 || K > 31) return fail(c, PG_ERR_LIMIT, "K = %d: the GPU tally packs K-mers in 64 bits (K <= 31)", K);
   if (min_depth < 1) return fail(c, PG_ERR_ARG, "min_depth must be >= 1");
@@ -933,6 +953,7 @@ pg_status pg_kmer_tally_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius,
 
 pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid, int32_t vcf_qe,
                         int32_t variants_only, char* out, int64_t cap, int64_t* n_bytes) {
+  const Range nvtx_range("pg_format_vcf");
   if (!c || !name || !n_bytes || cap < 0) return fail(c, PG_ERR_ARG, "bad arguments");
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
   if (r < 0 || r >= c->n_regions) return fail(c, PG_ERR_ARG, "region %d out of range", r);
