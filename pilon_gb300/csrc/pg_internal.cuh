@@ -65,6 +65,8 @@ struct StatsDev {        // per region, accumulated on the device
   unsigned long long fr_count, fr_sum, fr_sumsq, rf_count, rf_sum, rf_sumsq;
   int32_t error;
   int32_t n_ins;
+  int32_t prep_done;     // CTAs of k_region_prep that have added their part
+  int32_t pad;
 };
 
 struct WalkTile {

@@ -1295,18 +1295,30 @@ __device__ inline int64_t java_round(double x) {
   return (int64_t)((x - f >= 0.5) ? f + 1.0 : f);
 }
 
-// One CTA per region (256 or 1024 threads): adds up the per-chunk partial
-// statistics, then computes minDepth.
-__global__ void __launch_bounds__(1024) k_region_prep(const RegionDev* regions, StatsDev* stats,
-                                                       const ChunkStats* cs, DevParams P) {
+__device__ inline int32_t region_min_depth(const DevParams& P, unsigned long long base_count, int32_t size) {
+  // minDepth of GenomeRegion.postProcess (S/GenomeRegion.scala:216-224)
+  const int64_t meanCoverage = roundDivL((int64_t)base_count, size);
+  if (P.min_depth >= 1) return (int32_t)P.min_depth;
+  return max((int32_t)java_round(P.min_depth * (double)meanCoverage), P.min_min_depth);
+}
+
+// `per` CTAs per region, each adding up a share of the region's per-chunk
+// partial statistics; with one CTA it stores them, with several each adds its
+// sums with atomics and the CTA that finishes last (a counter in the region's
+// statistics, after a fence) computes minDepth.
+constexpr int kPrepThreads = 256, kPrepChunksPerCta = 512;
+__global__ void __launch_bounds__(kPrepThreads) k_region_prep(const RegionDev* regions, StatsDev* stats,
+                                                               const ChunkStats* cs, DevParams P, int32_t per) {
   __shared__ unsigned long long s_u[8];
   __shared__ int32_t s_i[3];
-  const int32_t r = blockIdx.x;
+  const int32_t r = blockIdx.x / per, part = blockIdx.x % per;
   const RegionDev& g = regions[r];
+  const int32_t span = (g.n_chunks + per - 1) / per;
+  const int32_t k0 = g.chunk0 + part * span, k1 = min(g.chunk0 + g.n_chunks, k0 + span);
   unsigned long long u[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   uint32_t pcs = 0, iss = 0;
   int32_t err = 0;
-  for (int32_t k = g.chunk0 + threadIdx.x; k < g.chunk0 + g.n_chunks; k += blockDim.x) {
+  for (int32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
     const ChunkStats c = cs[k];
     u[0] += c.read_count; u[1] += c.base_count; u[2] += c.fr_count; u[3] += c.fr_sum;
     u[4] += c.fr_sumsq; u[5] += c.rf_count; u[6] += c.rf_sum; u[7] += c.rf_sumsq;
@@ -1333,26 +1345,37 @@ __global__ void __launch_bounds__(1024) k_region_prep(const RegionDev* regions, 
   __syncthreads();
   if (threadIdx.x == 0) {
     StatsDev& st = stats[r];
-    st.read_count = s_u[0];
-    st.base_count += s_u[1];  // the walk kernel added the aligned bases already
-    st.fr_count = s_u[2]; st.fr_sum = s_u[3]; st.fr_sumsq = s_u[4];
-    st.rf_count = s_u[5]; st.rf_sum = s_u[6]; st.rf_sumsq = s_u[7];
-    st.phys_cov_start = s_i[0];
-    st.insert_size_start = s_i[1];
-    st.error = s_i[2];
-    // minDepth of GenomeRegion.postProcess (S/GenomeRegion.scala:216-224)
-    const int64_t meanCoverage = roundDivL((int64_t)st.base_count, g.size);
-    int32_t md;
-    if (P.min_depth >= 1) md = (int32_t)P.min_depth;
-    else md = max((int32_t)java_round(P.min_depth * (double)meanCoverage), P.min_min_depth);
-    st.min_depth = md;
+    if (per == 1) {
+      st.read_count = s_u[0];
+      st.base_count += s_u[1];  // the walk kernel added the aligned bases already
+      st.fr_count = s_u[2]; st.fr_sum = s_u[3]; st.fr_sumsq = s_u[4];
+      st.rf_count = s_u[5]; st.rf_sum = s_u[6]; st.rf_sumsq = s_u[7];
+      st.phys_cov_start = s_i[0];
+      st.insert_size_start = s_i[1];
+      st.error = s_i[2];
+      st.min_depth = region_min_depth(P, st.base_count, g.size);
+    } else {  // the statistics start at zero (base_count at the walk's aligned bases)
+      atomicAdd(&st.read_count, s_u[0]);
+      atomicAdd(&st.base_count, s_u[1]);
+      atomicAdd(&st.fr_count, s_u[2]); atomicAdd(&st.fr_sum, s_u[3]); atomicAdd(&st.fr_sumsq, s_u[4]);
+      atomicAdd(&st.rf_count, s_u[5]); atomicAdd(&st.rf_sum, s_u[6]); atomicAdd(&st.rf_sumsq, s_u[7]);
+      atomicAdd(&st.phys_cov_start, s_i[0]);
+      atomicAdd(&st.insert_size_start, s_i[1]);
+      atomicMax(&st.error, s_i[2]);
+      __threadfence();
+      if (atomicAdd(&st.prep_done, 1) == per - 1) {  // every other part has added its sums
+        __threadfence();
+        st.min_depth = region_min_depth(P, atomicAdd(&st.base_count, 0ull), g.size);
+      }
+    }
   }
 }
 
 void launch_region_prep(const RegionDev* regions, StatsDev* stats, const ChunkStats* chunk_stats,
                         int32_t n_regions, int32_t max_chunks, DevParams P, cudaStream_t s) {
   if (n_regions == 0) return;
-  k_region_prep<<<n_regions, max_chunks > 2048 ? 1024 : 256, 0, s>>>(regions, stats, chunk_stats, P);
+  const int32_t per = std::max(1, (max_chunks + kPrepChunksPerCta - 1) / kPrepChunksPerCta);
+  k_region_prep<<<n_regions * per, kPrepThreads, 0, s>>>(regions, stats, chunk_stats, P, per);
 }
 
 }  // namespace pg
