@@ -158,10 +158,6 @@ __device__ inline uint8_t nib_char(uint32_t nib) {
   const char* t = "=ACMGRSVTWYHKDBN";
   return (uint8_t)t[nib & 15];
 }
-__device__ inline uint32_t read_nib(const Reads& R, int64_t i, int32_t k) {
-  uint8_t b = R.seq[R.seq_off[i] + (k >> 1)];
-  return (k & 1) ? (b & 15u) : (b >> 4);
-}
 __device__ inline uint8_t upper(uint8_t c) { return (c >= 'a' && c <= 'z') ? (uint8_t)(c - 32) : c; }
 
 // Non-negative a / positive b, in 32 bits when both fit (same result).

@@ -31,13 +31,6 @@ __device__ inline bool validate_read(uint16_t fl, const DevParams& P) {
   return (P.nonpf || !(fl & 0x200)) && (P.duplicates || !(fl & 0x400)) && !(fl & 0x100);
 }
 
-// queryOverlapping(name, qs, qe) keeps reads whose [start, end] overlaps the
-// window; an unmapped read placed at a position counts as [pos, pos].
-__device__ inline bool in_window(int32_t pos, int32_t aend, uint16_t fl, const RegionDev& g) {
-  int32_t e = (fl & 0x4) ? pos : aend;
-  return pos <= g.qe && e >= g.qs;
-}
-
 // ---------------------------------------------------------------------------
 // Also validates the store: every read's CIGAR, bases and qualities must lie
 // inside their arrays, and positions must not decrease within a reference.
@@ -220,11 +213,6 @@ void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tile
 // reads G lanes per read (32 / G reads at once), reading the descriptors by
 // warp shuffle; the few other reads take the general CIGAR loop with the
 // whole warp.  No block-wide barrier runs inside the read loop.
-__device__ inline uint32_t nib_at(const uint8_t* seq, int64_t so, int32_t k) {
-  const uint8_t b = seq[so + (k >> 1)];
-  return (k & 1) ? (b & 15u) : (uint32_t)(b >> 4);
-}
-
 // PileUp.add of one base (S/PileUp.scala:75-84): dmq = mq + 1 - M.
 template <int T>
 __device__ inline void add_base(uint32_t* sm, int32_t p, uint32_t nib, int32_t qual, int32_t dmq, int32_t min_qual) {
