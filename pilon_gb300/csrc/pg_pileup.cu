@@ -551,18 +551,26 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               const int32_t n0 = lead + xs;          // read offset of chunk 0's first base
               const uint32_t lastb = (uint32_t)((n0 & 1) + 3) >> 1;  // last byte of a chunk's nibbles
               const uint8_t* sb = rsp + (n0 >> 1);   // byte of chunk c's first nibble: sb + 2c
-              // two chunks in flight ahead of the one being added
-              auto load_chunk = [&](int32_t cc, uint32_t& q, uint32_t& sv) {
-                const uintptr_t ba = (uintptr_t)(sb + 2 * cc);
-                const uint32_t* wp = (const uint32_t*)(ba & ~(uintptr_t)3);
-                const uint32_t lo = wp[0], hi = (ba & 3u) + lastb >= 4u ? wp[1] : 0u;
-                q = qw[cc];
-                sv = __funnelshift_r(lo, hi, 8u * (uint32_t)(ba & 3u));
-              };
+              // This lane's chunks c, c + G, ... have their first nibble in bytes
+              // sb + 2c, 2G apart: a multiple of 4, so every one sits at the same
+              // offset in its aligned word and the loads walk two word pointers.
+              // Two chunks are in flight ahead of the one being added.
               int32_t c = cf + gl;
+              const uintptr_t ba0 = (uintptr_t)(sb + 2 * c);
+              const uint32_t sh = 8u * (uint32_t)(ba0 & 3u);
+              const bool need_hi = (ba0 & 3u) + lastb >= 4u;
+              const uint32_t* wp = (const uint32_t*)(ba0 & ~(uintptr_t)3);
+              const uint32_t* qp_next = qw + c;
+              auto load_chunk = [&](uint32_t& q, uint32_t& sv) {  // the next chunk of this lane
+                const uint32_t lo = wp[0], hi = need_hi ? wp[1] : 0u;
+                q = *qp_next;
+                sv = __funnelshift_r(lo, hi, sh);
+                wp += G / 2;
+                qp_next += G;
+              };
               uint32_t qv = 0, sv = 0, q1 = 0, s1 = 0;
-              if (c < cend) load_chunk(c, qv, sv);
-              if (c + G < cend) load_chunk(c + G, q1, s1);
+              if (c < cend) load_chunk(qv, sv);
+              if (c + G < cend) load_chunk(q1, s1);
               // mq + 1 - M: 0 for the reads of the most common mq
               const int32_t dmq = (int32_t)rmq1 - (int32_t)mode_mq1;
               // Four bases at a time: the nibbles of the chunk select their codes
@@ -573,7 +581,7 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               const uint32_t comb = (n0 & 1) ? 0x7230u : 0x2301u;
               while (c < cend) {
                 uint32_t q2 = 0, s2 = 0;
-                if (c + 2 * G < cend) load_chunk(c + 2 * G, q2, s2);
+                if (c + 2 * G < cend) load_chunk(q2, s2);
                 const uint32_t code = prmt(prmt(kCodeLo, kCodeHi, sv), prmt(kCodeLo, kCodeHi, sv >> 8), comb);
                 // bit 6 of byte j: base j is A/C/G/T and its quality byte is in [minQual, 127]
                 const uint32_t ok = code & ((((qv | 0x80808080u) - minq4) & ~qv & 0x80808080u) >> 1) & okall;
