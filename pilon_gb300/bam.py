@@ -1,14 +1,15 @@
 """BAM input and output for the packed read store.
 
 read_bam is the host side of BamFile's input (S/BamFile.scala:117-126, which
-htsjdk decodes): the BGZF blocks of the file are inflated on parallel threads
-(zlib releases the interpreter lock) into one buffer, and libpg_bam.so splits
-the record stream into the structure-of-arrays store of the C ABI, keeping
-BAM's CIGAR words, 4-bit bases and qualities as they are.  write_bam writes a
+htsjdk decodes): libpg_bam.so inflates the BGZF blocks of the file on native
+threads, each straight into its place in one buffer (its own raw-DEFLATE
+decoder), and splits the record stream into the structure-of-arrays store of
+the C ABI, keeping BAM's CIGAR words, 4-bit bases and qualities as they are.  write_bam writes a
 store as a coordinate-sorted BAM (read names r<index>, no tags), for tests and
 the benchmark.
 """
 import ctypes as C
+import mmap
 import os
 import struct
 import zlib
@@ -39,6 +40,10 @@ def _lib():
         L.bam_encoded_size.argtypes = [i64, vp, vp]
         L.bam_encode.restype = i64
         L.bam_encode.argtypes = [i64] + [vp] * 16
+        L.bam_parse_threads.restype = i64
+        L.bam_parse_threads.argtypes = [vp, i64] + [vp] * 15 + [C.c_int32]
+        L.bgzf_inflate_blocks.restype = i64
+        L.bgzf_inflate_blocks.argtypes = [vp, i64, vp, vp, vp, vp, vp, C.c_int32]
         _LIB = L
     return _LIB
 
@@ -108,24 +113,34 @@ def _blocks(raw):
     return out
 
 
+def inflate_blocks(raw, blocks, threads=None):
+    """The uncompressed bytes of the BGZF blocks (cdata start, cdata end,
+    uncompressed size) of `raw`, one after another."""
+    n = len(blocks)
+    src = np.array([b[0] for b in blocks], np.int64).reshape(n)
+    end = np.array([b[1] for b in blocks], np.int64).reshape(n)
+    sizes = np.array([b[2] for b in blocks], np.int64).reshape(n)
+    starts = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    data = np.empty(max(int(starts[-1]), 1), np.uint8)
+    inp = np.frombuffer(raw, np.uint8) if len(raw) else np.zeros(1, np.uint8)
+    rc = _lib().bgzf_inflate_blocks(inp.ctypes.data, n, src.ctypes.data, end.ctypes.data, starts.ctypes.data,
+                                    sizes.ctypes.data, data.ctypes.data, _threads(threads))
+    if rc < 0:
+        raise ValueError(f"BGZF block {-rc - 1}: damaged DEFLATE data or wrong uncompressed size")
+    return data[:int(starts[-1])]
+
+
 def read_bam(path, threads=None):
     """Returns (reference names, reference lengths, ReadStore) of a BAM file."""
     with open(path, "rb") as f:
-        raw = f.read()
-    blocks = _blocks(raw)
-    sizes = np.array([b[2] for b in blocks], np.int64)
-    starts = np.concatenate([[0], np.cumsum(sizes)])
-    data = np.empty(int(starts[-1]), np.uint8)
-
-    def inflate(k):
-        a, b, isize = blocks[k]
-        if isize:
-            out = zlib.decompress(raw[a:b], -15)
-            if len(out) != isize:
-                raise ValueError(f"BGZF block {k}: {len(out)} bytes, header says {isize}")
-            data[starts[k]:starts[k] + isize] = np.frombuffer(out, np.uint8)
-    with ThreadPoolExecutor(_threads(threads)) as ex:
-        list(ex.map(inflate, range(len(blocks))))
+        # mapped, so that reading the file overlaps the threads' inflating
+        raw = mmap.mmap(f.fileno(), 0, access=mmap.ACCESS_READ) if os.fstat(f.fileno()).st_size else b""
+    try:
+        blocks = _blocks(raw)
+        data = inflate_blocks(raw, blocks, threads)
+    finally:
+        if isinstance(raw, mmap.mmap):
+            raw.close()
     view = memoryview(data)
     if bytes(view[:4]) != b"BAM\x01":
         raise ValueError("not a BAM file")
@@ -151,8 +166,9 @@ def read_bam(path, threads=None):
                    n_cigar=np.empty(n, np.uint16), cigar=np.empty(nc.value, np.uint32),
                    seq_off=np.empty(n, np.int64), l_seq=np.empty(n, np.int32), seq=np.empty(sb.value, np.uint8),
                    qual_off=np.empty(n, np.int64), qual=np.empty(qb.value, np.uint8))
-    L.bam_parse(recs.ctypes.data, recs.size, st.pos.ctypes.data, st.aend.ctypes.data, st.tlen.ctypes.data,
-                st.ref_id.ctypes.data, st.mate_ref_id.ctypes.data, st.l_seq.ctypes.data, st.flag.ctypes.data,
-                st.n_cigar.ctypes.data, st.mapq.ctypes.data, st.seq.ctypes.data, st.qual.ctypes.data,
-                st.cigar_off.ctypes.data, st.seq_off.ctypes.data, st.qual_off.ctypes.data, st.cigar.ctypes.data)
+    L.bam_parse_threads(recs.ctypes.data, recs.size, st.pos.ctypes.data, st.aend.ctypes.data, st.tlen.ctypes.data,
+                        st.ref_id.ctypes.data, st.mate_ref_id.ctypes.data, st.l_seq.ctypes.data, st.flag.ctypes.data,
+                        st.n_cigar.ctypes.data, st.mapq.ctypes.data, st.seq.ctypes.data, st.qual.ctypes.data,
+                        st.cigar_off.ctypes.data, st.seq_off.ctypes.data, st.qual_off.ctypes.data, st.cigar.ctypes.data,
+                        _threads(threads))
     return names, lengths, st

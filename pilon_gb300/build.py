@@ -2,7 +2,7 @@
 
 libpilon_gb300.so — the CUDA engine and its C ABI, sm_103a only.
 libpg_synth.so    — the host-side read simulator used by the benchmark.
-libpg_bam.so      — BAM records <-> the packed read store (host).
+libpg_bam.so      — BAM records <-> the packed read store and the BGZF inflate (host).
 
 Everything is compiled in-tree into pilon_gb300/_build/ with nvcc / g++
 directly (no cmake), the translation units in parallel.
@@ -67,9 +67,9 @@ def build(force=False, verbose=False):
     synth_src = os.path.join(CSRC, "synth.cpp")
     if force or not _newer(SYNTH, [synth_src]):
         cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", synth_src, "-o", SYNTH])
-    bam_src = os.path.join(CSRC, "bam.cpp")
-    if force or not _newer(BAMLIB, [bam_src]):
-        cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", bam_src, "-o", BAMLIB])
+    bam_srcs = [os.path.join(CSRC, "bam.cpp"), os.path.join(CSRC, "inflate.cpp")]
+    if force or not _newer(BAMLIB, bam_srcs):
+        cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread"] + bam_srcs + ["-o", BAMLIB])
     if cmds:
         if verbose:
             for c in cmds:

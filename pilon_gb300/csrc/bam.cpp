@@ -1,10 +1,10 @@
 // bam.cpp — BAM records <-> the packed read store of the C ABI (pg_reads).
 //
 // The host side of BamFile's input (S/BamFile.scala:117-126, htsjdk's
-// SAMRecord decoding): the caller inflates the BGZF blocks (any inflater; the
-// package uses zlib on parallel threads) and passes the decompressed stream
-// after the header; these functions split it into records and fill the
-// structure-of-arrays store, or encode a store as BAM records.
+// SAMRecord decoding): the caller inflates the BGZF blocks (inflate.cpp does it
+// on parallel threads) and passes the decompressed stream after the header;
+// these functions split it into records and fill the structure-of-arrays
+// store, or encode a store as BAM records.
 //
 // Record layout (SAM/BAM specification 4.2): block_size, refID, pos (0-based),
 // l_read_name, mapq, bin, n_cigar_op, flag, l_seq, next_refID, next_pos, tlen,
@@ -15,6 +15,8 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <thread>
+#include <vector>
 
 namespace {
 
@@ -73,8 +75,71 @@ int64_t bam_count(const uint8_t* buf, int64_t n, int64_t* n_cigar, int64_t* seq_
   return recs;
 }
 
-// Fills the store from the stream (arrays sized by bam_count).  Returns the
-// record count.
+// Fills the store from a stream that bam_count accepted (arrays sized by it):
+// one pass over the record headers fixes every record's start and the offsets
+// of its CIGAR, bases and qualities, then `threads` threads fill contiguous
+// ranges of records.  Returns the record count.
+int64_t bam_parse_threads(const uint8_t* buf, int64_t n, int32_t* pos, int32_t* aend, int32_t* tlen,
+                          int32_t* ref_id, int32_t* mate_ref_id, int32_t* l_seq_out, uint16_t* flag,
+                          uint16_t* n_cigar, uint8_t* mapq, uint8_t* seq, uint8_t* qual, int64_t* cigar_off,
+                          int64_t* seq_off, int64_t* qual_off, uint32_t* cigar, int32_t threads) {
+  std::vector<int64_t> start;
+  int64_t off = 0, co = 0, so = 0, qo = 0;
+  while (off + 4 <= n) {
+    const int32_t bs = rd32(buf + off);
+    const uint8_t* r = buf + off + 4;
+    const int64_t i = (int64_t)start.size();
+    const int32_t ls = rd32(r + 16);
+    start.push_back(off);
+    cigar_off[i] = co;
+    seq_off[i] = so;
+    qual_off[i] = qo;
+    co += rd16(r + 12);
+    so += (ls + 1) / 2;
+    qo += ls;
+    off += 4 + bs;
+  }
+  const int64_t recs = (int64_t)start.size();
+  auto fill = [&](int64_t a, int64_t b) {
+    for (int64_t i = a; i < b; i++) {
+      const uint8_t* r = buf + start[i] + 4;
+      const int32_t rid = rd32(r), p0 = rd32(r + 4);
+      const uint32_t l_name = r[8];
+      const uint16_t nc = rd16(r + 12), fl = rd16(r + 14);
+      const int32_t ls = rd32(r + 16);
+      const uint8_t* cg = r + 32 + l_name;
+      const uint8_t* sq = cg + 4 * (int64_t)nc;
+      const uint8_t* ql = sq + (ls + 1) / 2;
+      int64_t reflen = 0;
+      for (uint32_t k = 0; k < nc; k++) {
+        uint32_t w;
+        std::memcpy(&w, cg + 4 * k, 4);
+        cigar[cigar_off[i] + k] = w;
+        if (consumes_ref(w & 15u)) reflen += w >> 4;
+      }
+      pos[i] = p0 + 1;
+      aend[i] = (fl & 0x4) ? 0 : (int32_t)(p0 + reflen);  // (p0 + 1) + reflen - 1
+      tlen[i] = rd32(r + 28);
+      ref_id[i] = rid;
+      mate_ref_id[i] = rd32(r + 20);
+      l_seq_out[i] = ls;
+      flag[i] = fl;
+      n_cigar[i] = nc;
+      mapq[i] = r[9];
+      std::memcpy(seq + seq_off[i], sq, (size_t)(ls + 1) / 2);
+      std::memcpy(qual + qual_off[i], ql, (size_t)ls);
+    }
+  };
+  const int64_t nt = threads < 1 ? 1 : threads;
+  std::vector<std::thread> pool;
+  for (int64_t t = 1; t < nt; t++) pool.emplace_back(fill, recs * t / nt, recs * (t + 1) / nt);
+  fill(0, recs / nt);
+  for (auto& th : pool) th.join();
+  return recs;
+}
+
+// Fills the store from the stream (arrays sized by bam_count), on one thread.
+// Returns the record count.
 int64_t bam_parse(const uint8_t* buf, int64_t n, int32_t* pos, int32_t* aend, int32_t* tlen, int32_t* ref_id,
                   int32_t* mate_ref_id, int32_t* l_seq_out, uint16_t* flag, uint16_t* n_cigar, uint8_t* mapq,
                   uint8_t* seq, uint8_t* qual, int64_t* cigar_off, int64_t* seq_off, int64_t* qual_off,
