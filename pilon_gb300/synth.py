@@ -1,7 +1,7 @@
 """Seeded synthetic genomes and read sets for the five benchmark workloads.
 
-BASELINE names no public dataset; every input is generated here from a fixed
-seed per workload (1001-1005): a random reference, planted SNPs and indels in
+No public dataset is used; every input is generated here from a fixed seed
+per workload (1001-1005): a random reference, planted SNPs and indels in
 a sample copy of it, and paired 2x150 reads drawn from the sample with CIGARs
 from their true alignment to the reference.  The per-read simulation runs in
 libpg_synth.so (C++); reference and variant planting use numpy PCG64.
