@@ -218,7 +218,7 @@ def oracle_sample(ds, params, threads):
 
 
 def kmer_bench(eng, ds, params, args, threads, K=31, radius=500):
-    """Workload 4: the K-mer tally of Assembler.addReads/buildGraph (pg_kmer_tally)
+    """120 Mb genome with repeats: the K-mer tally of Assembler.addReads/buildGraph (pg_kmer_tally)
     over one local-reassembly window per planted indel (the reads overlapping
     [x - 500, x + 500]), on the GPU and on the oracle over all host threads for
     a sample of windows, with the sample's edges compared."""
@@ -314,7 +314,7 @@ def max_over_ranks(dist, v):
 
 
 def serve_bench(args, dist, rank, ws, local, params):
-    """Workload 5: Poisson arrivals (lambda = 200/s) of region-polish requests of
+    """Serving: Poisson arrivals (lambda = 200/s) of region-polish requests of
     10 kb - 1 Mb (log-uniform) against a device-resident read store of the
     many-contig workload; continuous batching vs the plain per-request path."""
     from pilon_gb300 import synth
