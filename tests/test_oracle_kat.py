@@ -7,7 +7,11 @@ lines.  One case per parity hazard of the hot path:
   H2 a homozygous deletion updates the pileups it covers    S/GenomeRegion.scala:259-264
   H3 a left shift below the region start throws             S/PileUpRegion.scala:155-182
   H5 integer rounding (roundDiv, adjMq)                     S/Utils.scala:23-26, S/PileUpRegion.scala:139-142
+  H5 BaseCall score, q and highConfidence arithmetic        S/PileUp.scala:132-153
   H6 stable base order on ties                              S/BaseSum.scala:57-60
+  indel call thresholds (strict majority, low/high pct)     S/PileUp.scala:182-247
+  minDepth: (0.1 * meanCoverage).round max 5                S/GenomeRegion.scala:221-224
+  H9 K-mer tally read rules (length, clips, N, minQual)     S/Assembler.scala:55-87
   H10 Java "%.2f" rounding of AF                            S/Vcf.scala:134-152
   H12 output names, FASTA wrapping, changes format          S/GenomeFile.scala:79-82,135-161
 """
@@ -309,3 +313,122 @@ def test_summary_regions_merge_rule():
     for _ in range(50):
         t = rng.random(n) < 0.004
         assert summary_regions(t, 1, n, 100) == scala(t, 1, n, 100)
+
+
+def _ins_case(n_ins, n_plain, ins="CA"):
+    """Reads over a 100-bp reference: n_ins with 20M 2I 20M at 31 (the insertion
+    attaches at 51, the position after the first 20 aligned bases; the base
+    before it is not the insertion's last character, so it does not shift) and
+    n_plain 40M reads at 31.  Quality 30, mapq 60 everywhere."""
+    ref = list(rand_ref(100, seed=3))
+    ref[49] = "G"  # position 50, before the insertion: not 'A'
+    ref = "".join(ref)
+    recs = [read(31, [(20, "M"), (len(ins), "I"), (20, "M")], ref[30:50] + ins + ref[50:70]) for _ in range(n_ins)]
+    recs += [read(31, [(40, "M")], ref[30:70]) for _ in range(n_plain)]
+    return ref, run(ref, recs)
+
+
+def test_base_call_het_score_and_amb():
+    """BaseCall (S/PileUp.scala:132-153) at one position: 6 reads with A at
+    quality 30 and 4 with C at quality 20, mapq 60 (mq + 1 = 61).
+      qualSum A = 6*30*61 = 10980, C = 4*20*61 = 4880, total 15860, n = 10, mqSum = 610
+      homoScore = 10980 - 4880 = 6100; half = 7930;
+      heteroScore = 15860 - |7930 - 10980| - |7930 - 4880| = 9760 -> not homozygous
+      score = |6100 - 9760| * 10 / 610 = 60, q = 6 (not high confidence)
+    The reference base is G: base A != G, score > 0, het and altBase C != G,
+    so pass 1 records an ambiguous change (S/GenomeRegion.scala:265-269)."""
+    ref = list(rand_ref(100, seed=5))
+    ref[49] = "G"
+    ref = "".join(ref)
+    recs = []
+    for k in range(10):
+        seq = list(ref[30:70])
+        seq[19] = "A" if k < 6 else "C"
+        recs.append(read(31, [(40, "M")], "".join(seq), qual=30 if k < 6 else 20))
+    res = run(ref, recs)
+    p = at(res, 50)
+    assert p["count"] == [6, 4, 0, 0] and p["qual_sum"] == [10980, 4880, 0, 0]
+    assert p["mq"] == 610 and p["q"] == 6 * 30 + 4 * 20
+    assert int(res.score[49]) == 60
+    f = p["call"]
+    assert f & 3 == 0 and (f >> 2) & 3 == 1  # base A, alt C
+    assert f & _abi.PG_CALL_HAS_BASE and not f & _abi.PG_CALL_HOMO and f & _abi.PG_CALL_HOMO_INDEL
+    assert (f >> 9) & 7 == _abi.PG_CHANGE_AMB and not f & _abi.PG_CALL_CONFIRMED
+    assert res.stats.min_depth == 5  # 200 trusted bases / 100 positions = 2 -> (0.2).round max 5
+
+
+@pytest.mark.parametrize("n_ins,n_plain,homo", [(8, 2, True), (5, 5, False), (13, 7, False), (14, 6, True)])
+def test_insertion_call_thresholds(n_ins, n_plain, homo):
+    """hetIndelCall (S/PileUp.scala:209-247) for "CA" at position 51:
+      insPct = max(pct(insQual, mqSum), pct(insertions, count)); insQual = 61 per
+      insertion, mqSum = 61 per read (an insertion adds none), count = all reads
+      middle = max(45 - 2, 10) = 43, low = 21, high = 2*43 - 21 = 65
+    8 of 10 -> 80 > 65: homozygous, an INS change in pass 1;  5 of 10 -> 50: het;
+    13 of 20 -> pct(793, 1220) = 65, not above high: het;  14 of 20 -> 70: homozygous."""
+    ref, res = _ins_case(n_ins, n_plain)
+    p = at(res, 51)
+    n = n_ins + n_plain
+    assert p["ins"] == n_ins and p["mq"] == 61 * n
+    f = p["call"]
+    assert f & _abi.PG_CALL_INS and int(res.indel_len[50]) == 2 and res.insertion(50) == "CA"
+    assert bool(f & _abi.PG_CALL_HOMO_INDEL) == homo
+    assert (f >> 9) & 7 == (_abi.PG_CHANGE_INS if homo else _abi.PG_CHANGE_NONE)
+    # homozygous reference base: score = total * n / mqSum = (n * 30 * 61) * n / (61 n) = 30 n
+    assert int(res.score[50]) == 30 * n
+
+
+def test_insertion_gate_needs_three():
+    """insertCall needs insertions > 2 (S/PileUp.scala:182-185): 2 of 5 reads
+    (pct 40, which would be het) give no call."""
+    ref, res = _ins_case(2, 3)
+    f = at(res, 51)["call"]
+    assert not f & _abi.PG_CALL_INS and (f >> 9) & 7 == _abi.PG_CHANGE_NONE
+
+
+@pytest.mark.parametrize("n_reads,mean,min_depth", [(270, 54, 5), (275, 55, 6), (325, 65, 7), (370, 74, 7),
+                                                   (375, 75, 8)])
+def test_min_depth_rounds_half_up(n_reads, mean, min_depth):
+    """minDepth = (0.1 * meanCoverage).round max 5 (S/GenomeRegion.scala:221-224),
+    meanCoverage = roundDiv(baseCount, size): 40M reads each add 20 trusted bases
+    to a 100-bp region; 5.5 rounds to 6 and 6.5 to 7 (half up)."""
+    ref = rand_ref(100, seed=9)
+    recs = [read(1 + (k % 61), [(40, "M")], ref[k % 61:k % 61 + 40]) for k in range(n_reads)]
+    recs.sort(key=lambda r: r["pos"])
+    res = run(ref, recs)
+    assert res.stats.base_count == 20 * n_reads and (20 * n_reads + 50) // 100 == mean
+    assert res.stats.min_depth == min_depth
+
+
+def test_min_depth_option_at_least_one_is_a_count():
+    ref = rand_ref(100, seed=9)
+    recs = [read(1 + (k % 61), [(40, "M")], ref[k % 61:k % 61 + 40]) for k in range(300)]
+    recs.sort(key=lambda r: r["pos"])
+    assert run(ref, recs, min_depth=12.0).stats.min_depth == 12
+
+
+def test_kmer_tally_read_rules():
+    """Assembler.addRead/addToPileups (S/Assembler.scala:55-87), K = 4, five copies of each read:
+      a read of length K adds nothing (length > K is required);
+      getReadString includes soft-clipped bases (2S3M "TTCCA": TTCC -> A);
+      K-mers holding N are kept (ANGT -> C; its reverse complement GACN -> T);
+      a next base that is not A/C/G/T adds nothing (CCCA -> N), but NTGG -> G does;
+      a next base below minQual adds nothing (minQual 10: GATC -> G at quality 5),
+      while the reverse strand reads the reversed qualities (CGAT -> C at quality 30)."""
+    recs = []
+    for seq, cig, q in [("ACGTA", [(5, "M")], 30), ("ACGT", [(4, "M")], 30), ("TTCCA", [(2, "S"), (3, "M")], 30),
+                        ("ANGTC", [(5, "M")], 30), ("CCCAN", [(5, "M")], 30), ("GATCG", [(5, "M")], [30, 30, 30, 30, 5])]:
+        recs += [read(10, cig, seq, qual=q, mapq=20)] * 5
+    st = build_store(recs)
+    e = oracle.kmer_tally(st, _abi.default_params(min_qual=10), [(0, len(recs))], 4, min_depth=5)
+    nib = {"A": 1, "C": 2, "G": 4, "T": 8, "N": 15}
+
+    def key(k):
+        v = 0
+        for j, c in enumerate(k):
+            v |= nib[c] << (60 - 4 * j)
+        return v
+    got = {(int(x["key_hi"]), int(x["next"]), int(x["alt"]), int(x["depth"])) for x in e}
+    idx = {"A": 0, "C": 1, "G": 2, "T": 3}
+    exp = {(key(k), idx[b], -1, 5) for k, b in [("ACGT", "A"), ("TACG", "T"), ("TTCC", "A"), ("TGGA", "A"),
+                                               ("ANGT", "C"), ("GACN", "T"), ("NTGG", "G"), ("CGAT", "C")]}
+    assert got == exp
