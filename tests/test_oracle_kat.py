@@ -9,7 +9,8 @@ lines.  One case per parity hazard of the hot path:
   H5 integer rounding (roundDiv, adjMq)                     S/Utils.scala:23-26, S/PileUpRegion.scala:139-142
   H5 BaseCall score, q and highConfidence arithmetic        S/PileUp.scala:132-153
   H6 stable base order on ties                              S/BaseSum.scala:57-60
-  indel call thresholds (strict majority, low/high pct)     S/PileUp.scala:182-247
+  indel call thresholds (insertions and deletions)          S/PileUp.scala:182-247
+  H7 insert-size statistics per region (FR / RF)            S/BamFile.scala:194-202
   minDepth: (0.1 * meanCoverage).round max 5                S/GenomeRegion.scala:221-224
   H9 K-mer tally read rules (length, clips, N, minQual)     S/Assembler.scala:55-87
   H10 Java "%.2f" rounding of AF                            S/Vcf.scala:134-152
@@ -432,3 +433,52 @@ def test_kmer_tally_read_rules():
     exp = {(key(k), idx[b], -1, 5) for k, b in [("ACGT", "A"), ("TACG", "T"), ("TTCC", "A"), ("TGGA", "A"),
                                                ("ANGT", "C"), ("GACN", "T"), ("NTGG", "G"), ("CGAT", "C")]}
     assert got == exp
+
+
+@pytest.mark.parametrize("n_del,n_plain,homo", [(8, 2, True), (5, 5, False), (13, 7, False), (14, 6, True)])
+def test_deletion_call_thresholds(n_del, n_plain, homo):
+    """deletionCall and hetIndelCall (S/PileUp.scala:187-247) for a 2-bp deletion
+    of loci 51-52 (20M 2D 20M at 31; the base before it differs from its last
+    base, so it does not shift).  addDeletion adds mq + 1 to mqSum
+    (S/PileUp.scala:107-114), so delPct = max(pct(61 d, 61 n), pct(d, n)) = pct(d, n)
+    with n = all reads; len 2: low 21, high 65.  A homozygous call is a DEL change
+    and marks locus 52 deleted, adding the deletions to it (S/GenomeRegion.scala:259-264).
+    The score comes from the plain reads' bases: 30 * 61 * p * p / (61 n) with p plain reads."""
+    ref = list(rand_ref(100, seed=4))
+    ref[49], ref[51] = "C", "G"  # loci 50 and 52 differ
+    ref = "".join(ref)
+    recs = [read(31, [(20, "M"), (2, "D"), (20, "M")], ref[30:50] + ref[52:72]) for _ in range(n_del)]
+    recs += [read(31, [(40, "M")], ref[30:70]) for _ in range(n_plain)]
+    res = run(ref, recs)
+    n = n_del + n_plain
+    p = at(res, 51)
+    assert p["dels"] == n_del and p["mq"] == 61 * n and p["count"][("ACGT".index(ref[50]))] == n_plain
+    f = p["call"]
+    assert f & _abi.PG_CALL_DEL and int(res.indel_len[50]) == 2
+    assert bool(f & _abi.PG_CALL_HOMO_INDEL) == homo
+    assert (f >> 9) & 7 == (_abi.PG_CHANGE_DEL if homo else _abi.PG_CHANGE_NONE)
+    assert int(res.score[50]) == 30 * 61 * n_plain * n_plain // (61 * n)
+    q52 = at(res, 52)
+    assert bool(q52["call"] & _abi.PG_CALL_DELETED) == homo and q52["dels"] == (n_del if homo else 0)
+
+
+def test_insert_size_statistics():
+    """BamFile.addInsert (S/BamFile.scala:194-202) with the size physCovIncr
+    returns (S/PileUpRegion.scala:62-88): FR when (size > 0) xor reverse strand,
+    else RF; 0 (not added) for invalid reads and pairs with TLEN <= 0; unpaired
+    reads count too (end - start of the alignment).
+      unpaired forward 40M at 101: 39 -> FR     unpaired reverse 40M at 150: 39 -> RF
+      proper pair, forward, TLEN 300 -> FR      proper pair, reverse, TLEN -300 -> none
+      proper pair, reverse, TLEN 250 -> RF      improper pair, TLEN 200 -> none (invalid)"""
+    ref = rand_ref(600, seed=2)
+    P = 0x1 | 0x2
+    recs = [read(101, [(40, "M")], ref[100:140]),
+            read(150, [(40, "M")], ref[149:189], flag=0x10),
+            read(160, [(40, "M")], ref[159:199], flag=P | 0x20, tlen=300),
+            read(170, [(40, "M")], ref[169:209], flag=P | 0x10, tlen=-300),
+            read(180, [(40, "M")], ref[179:219], flag=P | 0x10, tlen=250),
+            read(190, [(40, "M")], ref[189:229], flag=0x1, tlen=200)]
+    st = run(ref, recs).stats
+    assert (st.fr_count, st.fr_sum, st.fr_sumsq) == (2, 39 + 300, 39 * 39 + 300 * 300)
+    assert (st.rf_count, st.rf_sum, st.rf_sumsq) == (2, 39 + 250, 39 * 39 + 250 * 250)
+    assert st.read_count == 6
