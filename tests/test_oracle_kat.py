@@ -482,3 +482,42 @@ def test_insert_size_statistics():
     assert (st.fr_count, st.fr_sum, st.fr_sumsq) == (2, 39 + 300, 39 * 39 + 300 * 300)
     assert (st.rf_count, st.rf_sum, st.rf_sumsq) == (2, 39 + 250, 39 * 39 + 250 * 250)
     assert st.read_count == 6
+
+
+@pytest.mark.parametrize("hole", [(400, 449), (600, 615), (300, 303)])
+def test_possible_breaks_low_coverage_and_dip(hole):
+    """possibleBreaks (S/GenomeRegion.scala:659-763) on a 1,000-bp region read by
+    40M reads starting at every locus 1..961 except a hole of starts: with no
+    clips, bad pairs or N, breakp(i) = coverage < 5 || dip(fragCoverage, i, 100) /
+    mean >= 1.5, where coverage = fragCoverage = the trusted bases at i and mean
+    is the plain average (S/NormalDistribution.scala:25-28); runs merge with slop
+    200 and runs within 100 of the region's ends are dropped.  The expectation
+    below restates those lines directly."""
+    ref = rand_ref(1000, seed=13)
+    starts = [s for s in range(1, 962) if not hole[0] <= s <= hole[1]]
+    res = run(ref, [read(s, [(40, "M")], ref[s - 1:s + 39]) for s in starts])
+    cov = np.zeros(1000, np.int64)
+    for s in starts:
+        cov[s - 1 + 10:s - 1 + 30] += 1  # trusted offsets 10..29
+    assert np.array_equal(res.count.reshape(-1, 4).sum(1), cov)
+    mean = cov.sum() / cov.size
+    size = cov.size
+
+    def breakp(i):
+        left, right = cov[max(0, i - 100)], cov[min(size - 1, i + 100)]
+        return cov[i] < 5 or ((left - cov[i]) + (right - cov[i])) / mean >= 1.5
+
+    regs, first, last = [], -1, -1
+    for i in range(size):
+        if breakp(i):
+            last = i
+            first = i if first < 0 else first
+        elif last >= 0 and i > last + 200:
+            regs.append((1 + first, 1 + last))
+            first = last = -1
+    if last >= 0:
+        regs.append((1 + first, 1 + last))
+    want = [r for r in regs if not (r[0] - 1 < 100 or 1000 - r[1] < 100)]
+    assert oracle.region_breaks(build_store([read(s, [(40, "M")], ref[s - 1:s + 39]) for s in starts]),
+                                _abi.default_params(), ref_from(ref), 0, 1, 1000) == want
+    assert len(want) == (1 if hole[1] - hole[0] > 10 else 0)
