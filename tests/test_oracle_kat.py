@@ -14,6 +14,7 @@ lines.  One case per parity hazard of the hot path:
   minDepth: (0.1 * meanCoverage).round max 5                S/GenomeRegion.scala:221-224
   H9 K-mer tally read rules (length, clips, N, minQual)     S/Assembler.scala:55-87
   H10 Java "%.2f" rounding of AF                            S/Vcf.scala:134-152
+  VCF records: REF/ALT/GT, filters, BQ/MQ/QD/QP/AF fields  S/Vcf.scala:74-176, S/PileUp.scala:55-71
   H12 output names, FASTA wrapping, changes format          S/GenomeFile.scala:79-82,135-161
 """
 import os
@@ -521,3 +522,39 @@ def test_possible_breaks_low_coverage_and_dip(hole):
     assert oracle.region_breaks(build_store([read(s, [(40, "M")], ref[s - 1:s + 39]) for s in starts]),
                                 _abi.default_params(), ref_from(ref), 0, 1, 1000) == want
     assert len(want) == (1 if hole[1] - hole[0] > 10 else 0)
+
+
+def test_vcf_records_by_hand():
+    """Vcf.writeRecord (S/Vcf.scala:74-176) for three positions of the 6A/4C case
+    above (reads 31..70, trusted loci 41..60, reference G at locus 50, no pairs):
+    locus 50, het A over C:  not homo and rBase G != A -> (G, A, "0/1", refDP 4880, altDP 10980);
+      FILTER Amb (haploid, 0/1; depth 10 >= minDepth 5); QUAL = score 60
+      BQ = roundDiv(15860, roundDiv(610 * 10, 10)) = 26; MQ = roundDiv(610 - 10, 10) = 60; QD = q = 6
+      QP = toStringPct: (100 * 10980 + 7930) / 15860 = 69, (100 * 4880 + 7930) / 15860 = 31
+      PC = 10 (unpaired reads [31, 70)); AC = 1; AF = 10980 / 15860 = 0.692 -> "0.69"
+    locus 45, homozygous reference: total 15860, heteroScore = 15860 - 7930 - 7930 = 0,
+      score = 15860 * 10 / 610 = 260, q = 26; ALT "." (cBase == rBase), PASS, AC 0, AF 0.00
+    locus 5, no reads: base N, homo (0 >= 0), score 0; ALT "."; LowCov (0 < 5); all sums 0."""
+    ref = list(rand_ref(100, seed=5))
+    ref[49] = "G"
+    ref = "".join(ref)
+    recs = []
+    for k in range(10):
+        seq = list(ref[30:70])
+        seq[19] = "A" if k < 6 else "C"
+        recs.append(read(31, [(40, "M")], "".join(seq), qual=30 if k < 6 else 20))
+    st = build_store(recs)
+    with tempfile.TemporaryDirectory() as d:
+        pre = os.path.join(d, "o")
+        assert oracle.polish(st, _abi.default_params(), ["chr1"], [ref_from(ref)], pre) == 0
+        body = [l for l in open(pre + ".vcf").read().splitlines() if not l.startswith("#")]
+    assert len(body) == 100
+    info = "DP=10;TD=10;BQ=26;MQ=60;QD=6;BC=6,4,0,0;QP=69,31,0,0;PC=10;IC=0;DC=0;XC=0;AC=1;AF=0.69"
+    assert body[49] == "\t".join(["chr1", "50", ".", "G", "A", "60", "Amb", info, "GT", "0/1"])
+    r = ref[44]
+    bc = ",".join("10" if b == r else "0" for b in "ACGT")
+    qp = ",".join("100" if b == r else "0" for b in "ACGT")
+    info = f"DP=10;TD=10;BQ=26;MQ=60;QD=26;BC={bc};QP={qp};PC=10;IC=0;DC=0;XC=0;AC=0;AF=0.00"
+    assert body[44] == "\t".join(["chr1", "45", ".", r, ".", "260", "PASS", info, "GT", "0/0"])
+    info = "DP=0;TD=0;BQ=0;MQ=0;QD=0;BC=0,0,0,0;QP=0,0,0,0;PC=0;IC=0;DC=0;XC=0;AC=0;AF=0.00"
+    assert body[4] == "\t".join(["chr1", "5", ".", ref[4], ".", "0", "LowCov", info, "GT", "0/0"])
