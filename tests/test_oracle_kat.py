@@ -558,3 +558,69 @@ def test_vcf_records_by_hand():
     assert body[44] == "\t".join(["chr1", "45", ".", r, ".", "260", "PASS", info, "GT", "0/0"])
     info = "DP=0;TD=0;BQ=0;MQ=0;QD=0;BC=0,0,0,0;QP=0,0,0,0;PC=0;IC=0;DC=0;XC=0;AC=0;AF=0.00"
     assert body[4] == "\t".join(["chr1", "5", ".", ref[4], ".", "0", "LowCov", info, "GT", "0/0"])
+
+
+def _vcf_body(ref, recs, name="chr1"):
+    st = build_store(recs)
+    with tempfile.TemporaryDirectory() as d:
+        pre = os.path.join(d, "o")
+        assert oracle.polish(st, _abi.default_params(), [name], [ref_from(ref)], pre) == 0
+        return [l for l in open(pre + ".vcf").read().splitlines() if not l.startswith("#")]
+
+
+def _counts(base, n):
+    return ",".join(str(n) if b == base else "0" for b in "ACGT")
+
+
+def test_vcf_het_insertion_records():
+    """An indel call writes its record at locus - 1 with the base there prefixed,
+    then the position's own record without the indel (S/Vcf.scala:90-104, 175).
+    5 of 10 reads insert "CA" before locus 51 (the het case of the insertion
+    thresholds): insPct = max(pct(305, 610), pct(5, 10)) = 50 -> refDP 50, altDP 50;
+    callType 0/1 -> Amb, AC 1, AF 0.50; QUAL = score of the reference base at 51
+    = 18300 * 10 / 610 = 300, q 30; IC = 5 at locus 51."""
+    ref = list(rand_ref(100, seed=3))
+    ref[49] = "G"
+    ref = "".join(ref)
+    recs = [read(31, [(20, "M"), (2, "I"), (20, "M")], ref[30:50] + "CA" + ref[50:70]) for _ in range(5)]
+    recs += [read(31, [(40, "M")], ref[30:70]) for _ in range(5)]
+    body = _vcf_body(ref, recs)
+    assert len(body) == 101 and body[49].split("\t")[1] == "50"
+    r = ref[50]
+    info = (f"DP=10;TD=10;BQ=30;MQ=60;QD=30;BC={_counts(r, 10)};QP={_counts(r, 100)};PC=10;IC=5;DC=0;XC=0;"
+            "AC=1;AF=0.50")
+    assert body[50] == "\t".join(["chr1", "50", ".", "G", "GCA", "300", "Amb", info, "GT", "0/1"])
+    info = info.replace("AC=1;AF=0.50", "AC=0;AF=0.00")
+    assert body[51] == "\t".join(["chr1", "51", ".", r, ".", "300", "PASS", info, "GT", "0/0"])
+
+
+def test_vcf_homozygous_deletion_records():
+    """8 of 10 reads delete loci 51-52 (the homozygous deletion case).
+    Locus 51 gives three things (S/Vcf.scala:81-90, 120-176):
+      the deletion record at 50: REF C + deleted bases, ALT C, QUAL ".", 1/1,
+        delPct = pct(8, 10) = 80 -> AF 0.80, AC 2, PASS; DP = depth = 2 bases + 8 deletions
+        BQ = roundDiv(3660, roundDiv(610 * 2, 10) = 122) = 30, MQ = roundDiv(600, 10) = 60,
+        QD = q = score / n = (3660 * 2 / 610 = 12) / 2 = 6
+      the embedded record at 51 (embedded = homozygous deletion): filter Del, DP = count = 2,
+        QUAL = score 12, 0/0.
+    The pass-1 DEL adds the 8 deletions to locus 52 and marks it deleted
+    (S/GenomeRegion.scala:259-264), and writeVcf passes deleted(i) as embedded
+    (S/GenomeRegion.scala:641): filter Del, DP = count = 2, depth 10, mqSum 122, so
+    BQ = roundDiv(3660, roundDiv(122 * 2, 10) = 24) = 153, MQ = roundDiv(122 - 10, 10) = 11,
+    score = 3660 * 2 / 122 = 60, q 30, DC 8; its deletion list is empty, so no indel call there."""
+    ref = list(rand_ref(100, seed=4))
+    ref[49], ref[51] = "C", "G"
+    ref = "".join(ref)
+    recs = [read(31, [(20, "M"), (2, "D"), (20, "M")], ref[30:50] + ref[52:72]) for _ in range(8)]
+    recs += [read(31, [(40, "M")], ref[30:70]) for _ in range(2)]
+    body = _vcf_body(ref, recs)
+    assert len(body) == 101 and body[49].split("\t")[1] == "50"
+    r51 = ref[50]
+    info = (f"DP=10;TD=10;BQ=30;MQ=60;QD=6;BC={_counts(r51, 2)};QP={_counts(r51, 100)};PC=10;IC=0;DC=8;XC=0;"
+            "AC=2;AF=0.80")
+    assert body[50] == "\t".join(["chr1", "50", ".", "C" + ref[50:52], "C", ".", "PASS", info, "GT", "1/1"])
+    info = info.replace("DP=10;", "DP=2;").replace("AC=2;AF=0.80", "AC=0;AF=0.00")
+    assert body[51] == "\t".join(["chr1", "51", ".", r51, ".", "12", "Del", info, "GT", "0/0"])
+    info = (f"DP=2;TD=10;BQ=153;MQ=11;QD=30;BC={_counts('G', 2)};QP={_counts('G', 100)};PC=10;IC=0;DC=8;"
+            "XC=0;AC=0;AF=0.00")
+    assert body[52] == "\t".join(["chr1", "52", ".", "G", ".", "60", "Del", info, "GT", "0/0"])
