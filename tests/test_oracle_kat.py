@@ -624,3 +624,62 @@ def test_vcf_homozygous_deletion_records():
     info = (f"DP=2;TD=10;BQ=153;MQ=11;QD=30;BC={_counts('G', 2)};QP={_counts('G', 100)};PC=10;IC=0;DC=8;"
             "XC=0;AC=0;AF=0.00")
     assert body[52] == "\t".join(["chr1", "52", ".", "G", ".", "60", "Del", info, "GT", "0/0"])
+
+
+def test_changes_and_fasta_after_indel_fixes():
+    """A homozygous SNP at 100, an insertion of "CA" before 301 and a deletion
+    of 501-502, every read carrying them.  The fix list (S/GenomeRegion.scala:328-349)
+    is [(100, r, s), (301, "", "CA"), (501, r501 r502, "")]; writeChanges
+    (S/GenomeRegion.scala:645-657) prints old and new regions with
+    Region.regionString (S/Region.scala:41: no "-stop" when size < 2, and an empty
+    side has size 0) and shifts new loci by the length change so far:
+      chr1:100 chr1_pilon:100 r s
+      chr1:301 chr1_pilon:301-302 . CA          (delta becomes 2)
+      chr1:501-502 chr1_pilon:503 r501r502 .
+    fixIssues (S/GenomeRegion.scala:595-621) applies them from the right, giving
+    the sample sequence."""
+    ref = list(rand_ref(700, seed=11))
+    ref[299] = "G" if ref[298] != "G" and ref[300] != "G" else "T"   # locus 300 is not 'A': no left shift
+    ref[99] = "C" if ref[99] != "C" else "A"
+    while ref[499] == ref[501]:                                      # locus 500 differs from locus 502
+        ref[499] = "ACGT"[("ACGT".index(ref[499]) + 1) % 4]
+    ref = "".join(ref)
+    snp = "ACGT"[("ACGT".index(ref[99]) + 2) % 4]
+    assert ref[299] != "A" and ref[298] != ref[299] and ref[499] != ref[501]
+    # sample coordinate of each reference locus; the insertion sits between 300 and 301
+    sample = ref[:99] + snp + ref[100:300] + "CA" + ref[300:500] + ref[502:]
+
+    def to_sample(locus):
+        return locus - 1 + (2 if locus >= 301 else 0) - (2 if locus >= 503 else 0)
+
+    recs = []
+    for p in range(1, 700 - 59, 2):
+        last = p + 59
+        if {p, last} & {300, 301, 500, 501, 502, 503}:
+            continue
+        cigar, seq, loc = [], "", p
+        while loc <= last:
+            if loc == 301 and p < 301:
+                cigar.append((2, "I"))
+                seq += "CA"
+            if loc == 501 and p < 501:
+                cigar.append((2, "D"))
+                loc = 503
+                last += 2
+                continue
+            if cigar and cigar[-1][1] == "M":
+                cigar[-1] = (cigar[-1][0] + 1, "M")
+            else:
+                cigar.append((1, "M"))
+            seq += sample[to_sample(loc)]
+            loc += 1
+        recs.append(read(p, cigar, seq))
+    st = build_store(recs)
+    with tempfile.TemporaryDirectory() as d:
+        pre = os.path.join(d, "o")
+        assert oracle.polish(st, _abi.default_params(), ["chr1"], [ref_from(ref)], pre) == 0
+        ch = open(pre + ".changes").read().splitlines()
+        fa = "".join(open(pre + ".fasta").read().splitlines()[1:])
+    assert ch == [f"chr1:100 chr1_pilon:100 {ref[99]} {snp}", "chr1:301 chr1_pilon:301-302 . CA",
+                  f"chr1:501-502 chr1_pilon:503 {ref[500:502]} ."]
+    assert fa == sample
