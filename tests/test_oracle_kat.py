@@ -14,6 +14,8 @@ lines.  One case per parity hazard of the hot path:
   minDepth: (0.1 * meanCoverage).round max 5                S/GenomeRegion.scala:221-224
   H9 K-mer tally read rules (length, clips, N, minQual)     S/Assembler.scala:55-87
   H10 Java "%.2f" rounding of AF                            S/Vcf.scala:134-152
+  AMB fixes: base, IUPAC code, --fix amb, long reads        S/GenomeRegion.scala:265-269,331-340
+  changes lines and FASTA after indel fixes                 S/GenomeRegion.scala:595-657
   VCF records: REF/ALT/GT, filters, BQ/MQ/QD/QP/AF fields  S/Vcf.scala:74-176, S/PileUp.scala:55-71
   H12 output names, FASTA wrapping, changes format          S/GenomeFile.scala:79-82,135-161
 """
@@ -330,6 +332,17 @@ def _ins_case(n_ins, n_plain, ins="CA"):
     return ref, run(ref, recs)
 
 
+def _het_reads(ref):
+    """10 reads 40M at 31 over `ref`: 6 with A at quality 30 and 4 with C at
+    quality 20 at locus 50, mapq 60."""
+    recs = []
+    for k in range(10):
+        seq = list(ref[30:70])
+        seq[19] = "A" if k < 6 else "C"
+        recs.append(read(31, [(40, "M")], "".join(seq), qual=30 if k < 6 else 20))
+    return recs
+
+
 def test_base_call_het_score_and_amb():
     """BaseCall (S/PileUp.scala:132-153) at one position: 6 reads with A at
     quality 30 and 4 with C at quality 20, mapq 60 (mq + 1 = 61).
@@ -342,11 +355,7 @@ def test_base_call_het_score_and_amb():
     ref = list(rand_ref(100, seed=5))
     ref[49] = "G"
     ref = "".join(ref)
-    recs = []
-    for k in range(10):
-        seq = list(ref[30:70])
-        seq[19] = "A" if k < 6 else "C"
-        recs.append(read(31, [(40, "M")], "".join(seq), qual=30 if k < 6 else 20))
+    recs = _het_reads(ref)
     res = run(ref, recs)
     p = at(res, 50)
     assert p["count"] == [6, 4, 0, 0] and p["qual_sum"] == [10980, 4880, 0, 0]
@@ -538,11 +547,7 @@ def test_vcf_records_by_hand():
     ref = list(rand_ref(100, seed=5))
     ref[49] = "G"
     ref = "".join(ref)
-    recs = []
-    for k in range(10):
-        seq = list(ref[30:70])
-        seq[19] = "A" if k < 6 else "C"
-        recs.append(read(31, [(40, "M")], "".join(seq), qual=30 if k < 6 else 20))
+    recs = _het_reads(ref)
     st = build_store(recs)
     with tempfile.TemporaryDirectory() as d:
         pre = os.path.join(d, "o")
@@ -683,3 +688,46 @@ def test_changes_and_fasta_after_indel_fixes():
     assert ch == [f"chr1:100 chr1_pilon:100 {ref[99]} {snp}", "chr1:301 chr1_pilon:301-302 . CA",
                   f"chr1:501-502 chr1_pilon:503 {ref[500:502]} ."]
     assert fa == sample
+
+
+@pytest.mark.parametrize("ref_base,pk,iupac,fixed", [("G", {}, False, "A"), ("G", {}, True, "M"), ("C", {}, False, None),
+                                                      ("C", {"fix_amb": 1}, False, "A"),
+                                                      ("G", {"long_read": 1}, False, None)])
+def test_ambiguous_fix_options(ref_base, pk, iupac, fixed):
+    """The 6A/4C position (base A, alt C) under the AMB options:
+    pass 1 adds an AMB change when fixamb or altBase != ref (S/GenomeRegion.scala:265-269);
+    identifyAndFixIssues fixes it to the base, or to the IUPAC code of base and
+    alt (A|C = M) with --iupac, and not at all with long reads
+    (S/GenomeRegion.scala:331-340, S/Bases.scala:85-88).
+      ref G: alt C != G -> change; fix "A", or "M" with iupac; none with long reads
+      ref C: alt C == ref -> change only with fixamb."""
+    ref = list(rand_ref(100, seed=5))
+    ref[49] = ref_base
+    ref = "".join(ref)
+    recs = _het_reads(ref)
+    st = build_store(recs)
+    with tempfile.TemporaryDirectory() as d:
+        pre = os.path.join(d, "o")
+        assert oracle.polish(st, _abi.default_params(**pk), ["chr1"], [ref_from(ref)], pre, iupac=iupac) == 0
+        ch = open(pre + ".changes").read().splitlines()
+        fa = "".join(open(pre + ".fasta").read().splitlines()[1:])
+    if fixed is None:
+        assert ch == [] and fa == ref
+    else:
+        assert ch == [f"chr1:50 chr1_pilon:50 {ref_base} {fixed}"] and fa == ref[:49] + fixed + ref[50:]
+
+
+@pytest.mark.parametrize("diploid,filt", [(False, "Amb"), (True, "PASS")])
+def test_vcf_diploid_filter(diploid, filt):
+    """--diploid drops the Amb filter of 0/1 records (S/Vcf.scala:122-123)."""
+    ref = list(rand_ref(100, seed=5))
+    ref[49] = "G"
+    ref = "".join(ref)
+    recs = _het_reads(ref)
+    st = build_store(recs)
+    with tempfile.TemporaryDirectory() as d:
+        pre = os.path.join(d, "o")
+        assert oracle.polish(st, _abi.default_params(), ["chr1"], [ref_from(ref)], pre, diploid=diploid) == 0
+        body = [l for l in open(pre + ".vcf").read().splitlines() if not l.startswith("#")]
+    f = body[49].split("\t")
+    assert f[4] == "A" and f[6] == filt and f[9] == "0/1"
