@@ -6,6 +6,8 @@ lines.  One case per parity hazard of the hot path:
   H1 deletion left shift adds bases without removing them   S/PileUpRegion.scala:163-183
   H2 a homozygous deletion updates the pileups it covers    S/GenomeRegion.scala:259-264
   H3 a left shift below the region start throws             S/PileUpRegion.scala:155-182
+  H4 indels count by their region bounds (pre-shift locus)  S/PileUpRegion.scala:155,166
+  long-read indels: mq min 8, homopolymer runs dropped      S/PileUpRegion.scala:120-126,142-183
   H5 integer rounding (roundDiv, adjMq)                     S/Utils.scala:23-26, S/PileUpRegion.scala:139-142
   H5 BaseCall score, q and highConfidence arithmetic        S/PileUp.scala:132-153
   H6 stable base order on ties                              S/BaseSum.scala:57-60
@@ -731,3 +733,80 @@ def test_vcf_diploid_filter(diploid, filt):
         body = [l for l in open(pre + ".vcf").read().splitlines() if not l.startswith("#")]
     f = body[49].split("\t")
     assert f[4] == "A" and f[6] == filt and f[9] == "0/1"
+
+
+def _long_read_ref(ins_run, del_run):
+    """120 bp: locus 49 'A', then a C run of ins_run bases from locus 50 and 'T';
+    locus 79 'G', then a T run of del_run bases from locus 80 and 'A'."""
+    ref = list(rand_ref(120, seed=21))
+    ref[48] = "A"
+    ref[49:49 + ins_run] = "C" * ins_run
+    ref[49 + ins_run] = "T"
+    ref[78] = "G"
+    ref[79:79 + del_run] = "T" * del_run
+    ref[79 + del_run] = "A"
+    return "".join(ref)
+
+
+@pytest.mark.parametrize("long_read", [_abi.PG_NOT_LONG_READ, _abi.PG_NANOPORE, _abi.PG_PACBIO])
+@pytest.mark.parametrize("ins_run,del_run", [(4, 3), (5, 4)])
+def test_long_read_indels_next_to_homopolymers(long_read, ins_run, del_run):
+    """Long-read indel rules of addRead (S/PileUpRegion.scala:120-126, 142, 150-183):
+    indelMq = adjMq min 8, and an indel is dropped when homoRun >= 4.
+    homoRun takes a 0-based index into the contig: for an insertion it is given
+    the 1-based locus iloc, so it measures the run from locus iloc + 1; for a
+    deletion it is given index(dloc) = dloc - start, which in a region starting at
+    1 is the run from locus dloc.
+      "G" inserted before locus 50, C run from 50 of ins_run: homoRun = ins_run - 1
+        (3: kept, 4: dropped); locus 49 'A' != 'G', so no left shift
+      locus 80 deleted, T run from 80 of del_run: homoRun = del_run (3 kept, 4 dropped);
+        locus 79 'G' != locus 80 'T', so no left shift; no CC?GG motif around it
+    Five reads each, mapq 60: short reads add 61 per indel, long reads 9."""
+    ref = _long_read_ref(ins_run, del_run)
+    recs = [read(30, [(20, "M"), (1, "I"), (20, "M")], ref[29:49] + "G" + ref[49:69]) for _ in range(5)]
+    recs += [read(60, [(20, "M"), (1, "D"), (20, "M")], ref[59:79] + ref[80:100]) for _ in range(5)]
+    res = run(ref, recs, long_read=long_read)
+    assert res.status == 0
+    kept = long_read == _abi.PG_NOT_LONG_READ or (ins_run, del_run) == (4, 3)
+    mq1 = 61 if long_read == _abi.PG_NOT_LONG_READ else 9
+    p, q = at(res, 50), at(res, 80)
+    assert (p["ins"], int(res.ins_qual[49])) == ((5, 5 * mq1) if kept else (0, 0))
+    assert (q["dels"], int(res.del_qual[79])) == ((5, 5 * mq1) if kept else (0, 0))
+
+
+@pytest.mark.parametrize("stop,counted", [(81, True), (80, False)])
+def test_H4_deletion_must_end_inside_the_region(stop, counted):
+    """A deletion counts only when both its first and last loci are in the region
+    (S/PileUpRegion.scala:166): loci 80-81 deleted by 5 reads (20M 2D 20M at 60;
+    locus 79 differs from locus 81, so no left shift).  Region [41, 81] counts it at
+    80; region [41, 80] does not, while the reads' trusted M bases still count."""
+    ref = list(rand_ref(120, seed=22))
+    while ref[78] == ref[80]:
+        ref[78] = "ACGT"[("ACGT".index(ref[78]) + 1) % 4]
+    ref = "".join(ref)
+    recs = [read(60, [(20, "M"), (2, "D"), (20, "M")], ref[59:79] + ref[81:101]) for _ in range(5)]
+    st = build_store(recs)
+    res = oracle.process_region(st, _abi.default_params(), ref_from(ref), 0, 41, stop)
+    assert res.status == 0
+    assert at(res, 80, start=41)["dels"] == (5 if counted else 0)
+    assert sum(at(res, 79, start=41)["count"]) == 5
+
+
+@pytest.mark.parametrize("start,counted", [(41, True), (42, False)])
+def test_H4_insertion_locus_checked_before_shift(start, counted):
+    """An insertion counts when its pre-shift locus is in the region
+    (S/PileUpRegion.scala:155): "G" inserted before locus 41 (20M 1I 20M at 21,
+    locus 40 is not 'G', so it stays at 41) counts at 41 in a region starting at 41
+    and nowhere in one starting at 42."""
+    ref = list(rand_ref(120, seed=23))
+    if ref[39] == "G":
+        ref[39] = "T" if ref[38] != "T" and ref[40] != "T" else "A"
+    ref = "".join(ref)
+    assert ref[39] != "G"
+    recs = [read(21, [(20, "M"), (1, "I"), (20, "M")], ref[20:40] + "G" + ref[40:60]) for _ in range(5)]
+    st = build_store(recs)
+    res = oracle.process_region(st, _abi.default_params(), ref_from(ref), 0, start, 100)
+    assert res.status == 0
+    assert int(res.insertions.sum()) == (5 if counted else 0)
+    if counted:
+        assert at(res, 41, start=start)["ins"] == 5
