@@ -810,3 +810,18 @@ def test_H4_insertion_locus_checked_before_shift(start, counted):
     assert int(res.insertions.sum()) == (5 if counted else 0)
     if counted:
         assert at(res, 41, start=start)["ins"] == 5
+
+
+@pytest.mark.parametrize("start,ins_run,kept", [(1, 5, True), (31, 5, False), (31, 3, True)])
+def test_long_read_deletion_run_is_read_at_the_region_index(start, ins_run, kept):
+    """The long-read deletion test homoRun(index(dloc)) (S/PileUpRegion.scala:178)
+    passes the region index dloc - start as a contig index.  Locus 80 deleted
+    inside a T run of 3 (kept on its own); with the region starting at 31 the run
+    measured is the one at contig index 49, locus 50: the C run of ins_run bases
+    there (5 -> dropped, 3 -> kept)."""
+    ref = _long_read_ref(ins_run, 3)
+    recs = [read(60, [(20, "M"), (1, "D"), (20, "M")], ref[59:79] + ref[80:100]) for _ in range(5)]
+    st = build_store(recs)
+    res = oracle.process_region(st, _abi.default_params(long_read=_abi.PG_PACBIO), ref_from(ref), 0, start, 120)
+    assert res.status == 0
+    assert at(res, 80, start=start)["dels"] == (5 if kept else 0)
