@@ -825,3 +825,36 @@ def test_long_read_deletion_run_is_read_at_the_region_index(start, ins_run, kept
     res = oracle.process_region(st, _abi.default_params(long_read=_abi.PG_PACBIO), ref_from(ref), 0, start, 120)
     assert res.status == 0
     assert at(res, 80, start=start)["dels"] == (5 if kept else 0)
+
+
+def test_H8_non_acgt_and_low_quality_bases():
+    """PileUp.add (S/PileUp.scala:75-84) drops bases outside ACGT and bases below
+    minQual, but PileUpRegion.add (S/PileUpRegion.scala:38-47) counts every valid
+    trusted base in the region's baseCount first.  One 40M read at 101 (trusted
+    loci 111..130) with N at 115, IUPAC R at 116, '=' at 117 and quality 5 at 118,
+    minQual 10: those four loci stay empty; baseCount = 20."""
+    ref = rand_ref(200, seed=31)
+    seq = list(ref[100:140])
+    seq[14], seq[15], seq[16] = "N", "R", "="
+    qual = [30] * 40
+    qual[17] = 5
+    res = run(ref, [read(101, [(40, "M")], "".join(seq), qual=qual)], min_qual=10)
+    assert res.status == 0 and res.stats.base_count == 20
+    for locus in (115, 116, 117, 118):
+        p = at(res, locus)
+        assert p["count"] == [0, 0, 0, 0] and p["mq"] == 0 and p["q"] == 0
+    b = "ACGT".index(ref[118])
+    p = at(res, 119)
+    assert p["count"][b] == 1 and p["qual_sum"][b] == 30 * 61 and p["mq"] == 61
+
+
+def test_H8_indel_string_with_N_is_not_called():
+    """hetIndelCall rejects a winning indel string that contains N
+    (S/PileUp.scala:219): 8 of 10 reads insert "NA" before 51, which would be a
+    homozygous insertion as "CA" is; the insertions still count."""
+    ref, res = _ins_case(8, 2, ins="NA")
+    p = at(res, 51)
+    assert p["ins"] == 8
+    assert not p["call"] & _abi.PG_CALL_INS and (p["call"] >> 9) & 7 == _abi.PG_CHANGE_NONE
+    ref, res = _ins_case(8, 2, ins="CA")
+    assert at(res, 51)["call"] & _abi.PG_CALL_INS
