@@ -189,7 +189,11 @@ typedef struct pg_ctx pg_ctx;
 
 /* ---- context ----------------------------------------------------------- */
 /* Opens a context on CUDA device `device`.  Replaces nothing in the
- * reference (which has no device); allocates the context's stream. */
+ * reference (which has no device); allocates the context's stream.
+ * PG_ERR_ARG when ctx is NULL.  When there is no such device (or the stream
+ * cannot be made) it returns PG_ERR_CUDA and still sets *ctx, so that
+ * pg_last_error can say why; calls that use the device then return
+ * PG_ERR_STATE on it, and pg_close frees it. */
 pg_status pg_open(pg_ctx **ctx, int device);
 void pg_close(pg_ctx *ctx);
 const char *pg_last_error(const pg_ctx *ctx);

@@ -40,6 +40,7 @@ struct pg_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
+  std::string open_err;  // why pg_open failed, when it did
   // reference
   DevBuf ref;
   std::vector<int64_t> ref_off, ref_len;
@@ -219,12 +220,17 @@ pg_status pg_open(pg_ctx** out, int device) {
   if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
     cudaGetLastError();
     *out = c;
-    return fail(c, PG_ERR_CUDA, "no CUDA device %d", device);
+    fail(c, PG_ERR_CUDA, "no CUDA device %d", device);
+    c->open_err = c->err;
+    return PG_ERR_CUDA;
   }
   cudaSetDevice(device);
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    c->stream = nullptr;
     *out = c;
-    return fail(c, PG_ERR_CUDA, "cudaStreamCreate failed");
+    fail(c, PG_ERR_CUDA, "cudaStreamCreate failed");
+    c->open_err = c->err;
+    return PG_ERR_CUDA;
   }
   cudaEventCreate(&c->e0);
   cudaEventCreate(&c->e1);
@@ -286,8 +292,15 @@ pg_status pg_set_tuning(pg_ctx* c, int32_t tile_width, int32_t warps_per_cta, in
   return PG_OK;
 }
 
+// A context whose pg_open failed has no stream; calls that would use the
+// device on it fail with PG_ERR_STATE instead of running on the legacy stream.
+static pg_status not_open(pg_ctx* c) {
+  return fail(c, PG_ERR_STATE, "the context is not open (pg_open failed: %s)", c->open_err.c_str());
+}
+
 pg_status pg_sync(pg_ctx* c) {
   if (!c) return PG_ERR_ARG;
+  if (!c->stream) return not_open(c);
   cudaSetDevice(c->device);
   CK(cudaStreamSynchronize(c->stream));
   return PG_OK;
@@ -296,6 +309,7 @@ pg_status pg_sync(pg_ctx* c) {
 pg_status pg_set_reference(pg_ctx* c, int32_t n, const int64_t* lens, const uint8_t* const* bases) {
   const Range nvtx_range("pg_set_reference");
   if (!c || n < 0 || (n > 0 && (!lens || !bases))) return fail(c, PG_ERR_ARG, "bad reference arguments");
+  if (!c->stream) return not_open(c);
   cudaSetDevice(c->device);
   c->ref_off.assign(n, 0);
   c->ref_len.assign(lens, lens + n);
@@ -340,6 +354,7 @@ static pg_status finish_reads(pg_ctx* c) {
 pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
   const Range nvtx_range("pg_set_reads");
   if (!c || !h || h->n_reads < 0) return fail(c, PG_ERR_ARG, "bad reads");
+  if (!c->stream) return not_open(c);
   cudaSetDevice(c->device);
   const int64_t n = h->n_reads;
   const void* src[15] = {h->pos, h->aend, h->tlen, h->ref_id, h->mate_ref_id, h->l_seq, h->flag, h->n_cigar,
@@ -368,6 +383,7 @@ pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
 pg_status pg_set_reads_device(pg_ctx* c, const pg_reads* d) {
   const Range nvtx_range("pg_set_reads_device");
   if (!c || !d || d->n_reads < 0) return fail(c, PG_ERR_ARG, "bad reads");
+  if (!c->stream) return not_open(c);
   cudaSetDevice(c->device);
   Reads& R = c->R;
   R.n = d->n_reads;

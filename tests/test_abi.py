@@ -65,3 +65,48 @@ def test_open_without_gpu_fails_cleanly():
     from pilon_gb300.engine import Engine, EngineError
     with pytest.raises(EngineError):
         Engine(0)
+
+
+def _lib():
+    from pilon_gb300.build import ENGINE, build
+    if not os.path.exists(ENGINE):
+        build()
+    lib = C.CDLL(ENGINE)
+    lib.pg_last_error.restype = C.c_char_p
+    lib.pg_last_error.argtypes = [C.c_void_p]
+    lib.pg_close.argtypes = [C.c_void_p]
+    return lib
+
+
+def test_open_errors_are_statuses():
+    """pg_open with a NULL out pointer, a negative device, or no device at all
+    returns a status and a message; a context that failed to open refuses the
+    device calls with PG_ERR_STATE and closes cleanly."""
+    from pilon_gb300 import _abi
+    lib = _lib()
+    assert lib.pg_open(None, 0) == _abi.PG_ERR_ARG
+    bad = C.c_void_p()
+    assert lib.pg_open(C.byref(bad), -1) == _abi.PG_ERR_CUDA
+    assert lib.pg_last_error(bad) == b"no CUDA device -1"
+    lens = (C.c_int64 * 1)(4)
+    base = (C.c_uint8 * 4)(*b"ACGT")
+    bases = (C.c_void_p * 1)(C.addressof(base))
+    assert lib.pg_set_reference(bad, 1, lens, bases) == _abi.PG_ERR_STATE
+    assert lib.pg_last_error(bad) == b"the context is not open (pg_open failed: no CUDA device -1)"
+    assert lib.pg_sync(bad) == _abi.PG_ERR_STATE
+    reads = _abi.pg_reads()
+    assert lib.pg_set_reads(bad, C.byref(reads)) == _abi.PG_ERR_STATE
+    assert lib.pg_set_reads_device(bad, C.byref(reads)) == _abi.PG_ERR_STATE
+    p = _abi.default_params()
+    assert lib.pg_pileup_regions(bad, None, 0, C.byref(p), 1) == _abi.PG_ERR_STATE
+    stats = _abi.pg_region_stats()
+    assert lib.pg_fetch_stats(bad, 0, C.byref(stats)) == _abi.PG_ERR_STATE
+    lib.pg_close(bad)
+
+    ctx = C.c_void_p()
+    st = lib.pg_open(C.byref(ctx), 0)
+    if st == _abi.PG_OK:
+        lib.pg_close(ctx)
+        pytest.skip("a CUDA device is present")
+    assert st == _abi.PG_ERR_CUDA and lib.pg_last_error(ctx) == b"no CUDA device 0"
+    lib.pg_close(ctx)
