@@ -99,7 +99,7 @@ def _blocks(raw):
             raise ValueError(f"BGZF block at byte {off} is truncated")
         while x + 4 <= off + 12 + xlen:
             si1, si2, slen = raw[x], raw[x + 1], struct.unpack_from("<H", raw, x + 2)[0]
-            if si1 == 66 and si2 == 67 and slen == 2:
+            if si1 == 66 and si2 == 67 and slen == 2 and x + 6 <= off + 12 + xlen:
                 bsize = struct.unpack_from("<H", raw, x + 4)[0]
             x += 4 + slen
         if bsize is None:
@@ -108,6 +108,8 @@ def _blocks(raw):
         if end > n or end - 8 < off + 12 + xlen:
             raise ValueError(f"BGZF block at byte {off} is truncated")
         isize = struct.unpack_from("<I", raw, end - 4)[0]
+        if isize > 65536:  # a BGZF block holds at most 64 KiB of data
+            raise ValueError(f"BGZF block at byte {off} claims {isize} uncompressed bytes")
         out.append((off + 12 + xlen, end - 8, isize))
         off = end
     return out
@@ -130,6 +132,36 @@ def inflate_blocks(raw, blocks, threads=None):
     return data[:int(starts[-1])]
 
 
+def _header(view):
+    """Reference names and lengths of the BAM header (magic, l_text, text,
+    n_ref, then l_name, name with its NUL, l_ref per reference) and the offset
+    of the first record."""
+    n = len(view)
+
+    def i32(at):
+        if at < 0 or at + 4 > n:
+            raise ValueError("BAM header is truncated")
+        return struct.unpack_from("<i", view, at)[0]
+
+    l_text = i32(4)
+    if l_text < 0:
+        raise ValueError("BAM header text length is negative")
+    off = 8 + l_text
+    n_ref = i32(off)
+    if n_ref < 0:
+        raise ValueError("BAM header reference count is negative")
+    off += 4
+    names, lengths = [], []
+    for _ in range(n_ref):
+        ln = i32(off)
+        if ln < 1 or off + 8 + ln > n:
+            raise ValueError("BAM header reference entry is damaged")
+        names.append(bytes(view[off + 4:off + 4 + ln - 1]).decode("utf-8", "replace"))
+        lengths.append(i32(off + 4 + ln))
+        off += 8 + ln
+    return names, lengths, off
+
+
 def read_bam(path, threads=None):
     """Returns (reference names, reference lengths, ReadStore) of a BAM file."""
     with open(path, "rb") as f:
@@ -144,16 +176,7 @@ def read_bam(path, threads=None):
     view = memoryview(data)
     if bytes(view[:4]) != b"BAM\x01":
         raise ValueError("not a BAM file")
-    l_text = struct.unpack_from("<i", view, 4)[0]
-    off = 8 + l_text
-    n_ref = struct.unpack_from("<i", view, off)[0]
-    off += 4
-    names, lengths = [], []
-    for _ in range(n_ref):
-        ln = struct.unpack_from("<i", view, off)[0]
-        names.append(bytes(view[off + 4:off + 4 + ln - 1]).decode())
-        lengths.append(struct.unpack_from("<i", view, off + 4 + ln)[0])
-        off += 8 + ln
+    names, lengths, off = _header(view)
     L = _lib()
     recs = data[off:]
     nc, sb, qb = C.c_int64(), C.c_int64(), C.c_int64()

@@ -61,9 +61,10 @@ int64_t bam_count(const uint8_t* buf, int64_t n, int64_t* n_cigar, int64_t* seq_
     const uint8_t* r = buf + off + 4;
     const int32_t l_seq = rd32(r + 16);
     const uint32_t l_name = r[8], n_cig = rd16(r + 12);
-    if (l_seq < 0 || 32 + (int64_t)l_name + 4 * (int64_t)n_cig + (l_seq + 1) / 2 + l_seq > bs) return -1 - off;
+    if (l_seq < 0 || 32 + (int64_t)l_name + 4 * (int64_t)n_cig + ((int64_t)l_seq + 1) / 2 + l_seq > bs)
+      return -1 - off;
     nc += n_cig;
-    sb += (l_seq + 1) / 2;
+    sb += ((int64_t)l_seq + 1) / 2;
     qb += l_seq;
     recs++;
     off += 4 + bs;
@@ -117,7 +118,7 @@ int64_t bam_parse_threads(const uint8_t* buf, int64_t n, int32_t* pos, int32_t* 
         cigar[cigar_off[i] + k] = w;
         if (consumes_ref(w & 15u)) reflen += w >> 4;
       }
-      pos[i] = p0 + 1;
+      pos[i] = (int32_t)((uint32_t)p0 + 1u);  // Java int arithmetic: wraps
       aend[i] = (fl & 0x4) ? 0 : (int32_t)(p0 + reflen);  // (p0 + 1) + reflen - 1
       tlen[i] = rd32(r + 28);
       ref_id[i] = rid;
@@ -162,7 +163,7 @@ int64_t bam_parse(const uint8_t* buf, int64_t n, int32_t* pos, int32_t* aend, in
       cigar[co + k] = w;
       if (consumes_ref(w & 15u)) reflen += w >> 4;
     }
-    pos[i] = p0 + 1;
+    pos[i] = (int32_t)((uint32_t)p0 + 1u);  // Java int arithmetic: wraps
     aend[i] = (fl & 0x4) ? 0 : (int32_t)(p0 + reflen);  // (p0 + 1) + reflen - 1
     tlen[i] = rd32(r + 28);
     ref_id[i] = rid;

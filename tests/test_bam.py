@@ -74,3 +74,66 @@ def test_truncated_file_is_an_error(cfg1):
         open(bad, "wb").write(head + cd + struct.pack("<II", zlib.crc32(cut) & 0xFFFFFFFF, len(cut)) + bam.BGZF_EOF)
         with pytest.raises(ValueError):
             bam.read_bam(bad)
+
+
+def _bam_of(payload):
+    """A BGZF file holding `payload` in blocks of at most 60,000 bytes."""
+    blocks = [bam._bgzf_block(payload[k:k + 60000]) for k in range(0, max(len(payload), 1), 60000)]
+    return b"".join(blocks) + bam.BGZF_EOF
+
+
+def _payload(cfg1, n=20):
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "r.bam")
+        bam.write_bam(path, cfg1.names, [c.size for c in cfg1.contigs], cfg1.reads.subset(np.arange(n)))
+        raw = open(path, "rb").read()
+    import zlib
+    return bytearray(b"".join(zlib.decompress(raw[a:b], -15) for a, b, _ in bam._blocks(raw)))
+
+
+def _read(raw):
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "x.bam")
+        open(path, "wb").write(raw)
+        return bam.read_bam(path)
+
+
+def test_damaged_headers_and_blocks_are_value_errors(cfg1):
+    """Every damaged field a reader meets before the records raises ValueError:
+    a block claiming more than 64 KiB, a header text or reference list that runs
+    past the data, negative counts, an empty reference name entry."""
+    good = _payload(cfg1)
+    _read(_bam_of(bytes(good)))  # the rebuilt file itself reads
+    blk = bytearray(_bam_of(bytes(good)))
+    struct.pack_into("<I", blk, len(blk) - len(bam.BGZF_EOF) - 4, 70000)  # ISIZE of the last data block
+    with pytest.raises(ValueError, match="uncompressed bytes"):
+        _read(bytes(blk))
+    l_text = struct.unpack_from("<i", good, 4)[0]
+    for at, value in [(4, 1 << 30), (4, -5), (8 + l_text, -1), (8 + l_text, 1 << 20), (12 + l_text, 0),
+                      (12 + l_text, 1 << 30)]:
+        bad = bytearray(good)
+        struct.pack_into("<i", bad, at, value)
+        with pytest.raises(ValueError):
+            _read(_bam_of(bytes(bad)))
+
+
+def test_record_length_fields_are_checked(cfg1):
+    """bam_count rejects a record whose l_seq, read-name length or CIGAR count
+    does not fit its block_size (l_seq = 2^31 - 1 included); a position of
+    2^31 - 1 reads back as htsjdk's wrapped Java int."""
+    good = _payload(cfg1)
+    l_text = struct.unpack_from("<i", good, 4)[0]
+    off = 12 + l_text
+    for _ in range(struct.unpack_from("<i", good, 8 + l_text)[0]):
+        off += 8 + struct.unpack_from("<i", good, off)[0]
+    rec = off + 4  # first record, after its block_size
+    for field, fmt, value in [(16, "<i", 2 ** 31 - 1), (16, "<i", -1), (16, "<i", 10_000), (8, "<B", 255),
+                              (12, "<H", 65535)]:
+        bad = bytearray(good)
+        struct.pack_into(fmt, bad, rec + field, value)
+        with pytest.raises(ValueError, match="runs past"):
+            _read(_bam_of(bytes(bad)))
+    bad = bytearray(good)
+    struct.pack_into("<i", bad, rec + 4, 2 ** 31 - 1)
+    _, _, st = _read(_bam_of(bytes(bad)))
+    assert st.pos[0] == -2 ** 31
