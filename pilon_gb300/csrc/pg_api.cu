@@ -354,6 +354,8 @@ static pg_status finish_reads(pg_ctx* c) {
 pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
   const Range nvtx_range("pg_set_reads");
   if (!c || !h || h->n_reads < 0) return fail(c, PG_ERR_ARG, "bad reads");
+  if (h->n_cigar_words < 0 || h->seq_bytes < 0 || h->qual_bytes < 0)
+    return fail(c, PG_ERR_ARG, "negative array length in the read store");
   if (!c->stream) return not_open(c);
   cudaSetDevice(c->device);
   const int64_t n = h->n_reads;
@@ -383,6 +385,8 @@ pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
 pg_status pg_set_reads_device(pg_ctx* c, const pg_reads* d) {
   const Range nvtx_range("pg_set_reads_device");
   if (!c || !d || d->n_reads < 0) return fail(c, PG_ERR_ARG, "bad reads");
+  if (d->n_cigar_words < 0 || d->seq_bytes < 0 || d->qual_bytes < 0)
+    return fail(c, PG_ERR_ARG, "negative array length in the read store");
   if (!c->stream) return not_open(c);
   cudaSetDevice(c->device);
   Reads& R = c->R;
