@@ -309,13 +309,17 @@ pg_status pg_sync(pg_ctx* c) {
 pg_status pg_set_reference(pg_ctx* c, int32_t n, const int64_t* lens, const uint8_t* const* bases) {
   const Range nvtx_range("pg_set_reference");
   if (!c || n < 0 || (n > 0 && (!lens || !bases))) return fail(c, PG_ERR_ARG, "bad reference arguments");
+  for (int i = 0; i < n; i++) {
+    if (lens[i] < 0 || (lens[i] > 0 && !bases[i])) return fail(c, PG_ERR_ARG, "contig %d has no bases", i);
+    // positions are 32-bit, as Pilon's (Scala Int; a contig is one JVM byte array)
+    if (lens[i] > INT32_MAX) return fail(c, PG_ERR_ARG, "contig %d is longer than 2^31 - 1 bases", i);
+  }
   if (!c->stream) return not_open(c);
   cudaSetDevice(c->device);
   c->ref_off.assign(n, 0);
   c->ref_len.assign(lens, lens + n);
   int64_t total = 0;
   for (int i = 0; i < n; i++) {
-    if (lens[i] < 0 || (lens[i] > 0 && !bases[i])) return fail(c, PG_ERR_ARG, "contig %d has no bases", i);
     c->ref_off[i] = total;
     total += lens[i];
   }

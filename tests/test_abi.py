@@ -91,6 +91,9 @@ def test_open_errors_are_statuses():
     lens = (C.c_int64 * 1)(4)
     base = (C.c_uint8 * 4)(*b"ACGT")
     bases = (C.c_void_p * 1)(C.addressof(base))
+    long_lens = (C.c_int64 * 1)(2 ** 31)
+    assert lib.pg_set_reference(bad, 1, long_lens, bases) == _abi.PG_ERR_ARG
+    assert lib.pg_last_error(bad) == b"contig 0 is longer than 2^31 - 1 bases"
     assert lib.pg_set_reference(bad, 1, lens, bases) == _abi.PG_ERR_STATE
     assert lib.pg_last_error(bad) == b"the context is not open (pg_open failed: no CUDA device -1)"
     assert lib.pg_sync(bad) == _abi.PG_ERR_STATE
