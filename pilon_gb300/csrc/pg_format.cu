@@ -88,7 +88,7 @@ __device__ void vcf_record(Out& o, const FormatArgs& A, const PosView& v, int32_
   const char base = (f & PG_CALL_HAS_BASE) ? "ACGT"[b] : 'N';
   const char altBase = "ACGT"[ab];
   const bool homo = f & PG_CALL_HOMO, isIns = f & PG_CALL_INS, isDel = f & PG_CALL_DEL;
-  const bool homoIndel = f & PG_CALL_HOMO_INDEL, indel = isIns || isDel;
+  const bool homoIndel = f & PG_CALL_HOMO_INDEL;
   const int64_t baseSum = pick4(v.qs, b), altBaseSum = pick4(v.qs, ab);
   const int32_t baseDP = (int32_t)baseSum, altBaseDP = (int32_t)altBaseSum;
   const int32_t depth = (int32_t)depthL;
@@ -105,7 +105,6 @@ __device__ void vcf_record(Out& o, const FormatArgs& A, const PosView& v, int32_
   int32_t rtl = 0;
   const uint8_t* ct = nullptr;
   int32_t ctl = 0;
-  bool cIsBaseStr = false;  // cBase is the single base character
   int callType;             // 0 "0/0", 1 "0/1", 2 "1/1"
   int32_t refDP, altDP;
   if (indelOk && !embedded && isDel) {
@@ -128,7 +127,6 @@ __device__ void vcf_record(Out& o, const FormatArgs& A, const PosView& v, int32_
     const char rb = refBase(loc);
     r0 = rb;
     c0 = base;
-    cIsBaseStr = true;
     const bool bcIsN = !csIns && !csDel && base == 'N';
     if (rb == base || bcIsN) { callType = 0; refDP = baseDP; altDP = altBaseDP; }
     else { callType = 2; refDP = altBaseDP; altDP = baseDP; }
@@ -137,9 +135,7 @@ __device__ void vcf_record(Out& o, const FormatArgs& A, const PosView& v, int32_
     r0 = rb;
     if (rb == base) { c0 = altBase; callType = 1; refDP = baseDP; altDP = altBaseDP; }
     else { c0 = base; callType = 1; refDP = altBaseDP; altDP = baseDP; }
-    cIsBaseStr = true;
   }
-  (void)cIsBaseStr;
   // cBaseVcf: "." when cBase is "N" or equals rBase
   const int32_t rlen = 1 + rtl, clen = 1 + ctl;
   bool dot = false;

@@ -757,7 +757,6 @@ __global__ void __launch_bounds__(kEvThreads, 16) k_read_events(EventArgs a, int
     const int32_t ch = bq / kEvPerChunk;
     const ReadChunk C = a.chunks[ch];
     const RegionDev g = a.regions[C.region];
-    const uint8_t* cref = a.ref + g.ref_off;
     unsigned long long rc_n = 0, bc_n = 0, frc = 0, frs = 0, frq = 0, rfc = 0, rfs = 0, rfq = 0;
     uint32_t pcs = 0, iss = 0;
     int32_t err = 0;
