@@ -12,7 +12,6 @@ BamFile.process + PileUpRegion.addRead, computePhysCov, BaseCall and pass 1.
 the Scala reference cannot run here: no JVM) on the host cores.
 """
 import argparse
-import ctypes as C
 import json
 import os
 import statistics

@@ -6,8 +6,6 @@ and its reverse complement, the following base with its quality and mapping
 quality (pg_kmer_tally), and returns the graph edges of the K-mers with depth
 >= minDepth.  The graph walk (S/Assembler.scala:164-327) stays on the host.
 """
-import numpy as np
-
 NIB = "=ACMGRSVTWYHKDBN"
 
 

@@ -1,6 +1,5 @@
 """End-to-end outputs: FASTA, VCF and changes written through the GB300
 engine must be byte-identical to the oracle's restatement of Pilon's writers."""
-import filecmp
 import os
 import tempfile
 

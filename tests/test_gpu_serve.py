@@ -1,9 +1,8 @@
 """Serving: requests batched together (continuous batching over two engine
 contexts) must get exactly the answers they get alone."""
-import numpy as np
 import pytest
 
-from pilon_gb300 import _abi, synth
+from pilon_gb300 import synth
 from pilon_gb300.serve import Request, Server, poisson_requests
 
 pytestmark = pytest.mark.gpu

@@ -3,7 +3,7 @@ import numpy as np
 
 from pilon_gb300 import synth
 from pilon_gb300.reads import CIGAR_OPS
-from pilon_gb300.regions import ReadIndex, contig_regions, parse_targets, plan_regions
+from pilon_gb300.regions import contig_regions, parse_targets, plan_regions
 
 
 def test_generator_is_deterministic():
