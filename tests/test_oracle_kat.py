@@ -17,7 +17,7 @@ lines.  One case per parity hazard of the hot path:
   H9 K-mer tally read rules (length, clips, N, minQual)     S/Assembler.scala:55-87
   H10 Java "%.2f" rounding of AF                            S/Vcf.scala:134-152
   AMB fixes: base, IUPAC code, --fix amb, long reads        S/GenomeRegion.scala:265-269,331-340
-  changes lines and FASTA after indel fixes                 S/GenomeRegion.scala:595-657
+  changes lines and FASTA after indel fixes, across chunks  S/GenomeRegion.scala:595-657, S/GenomeFile.scala:140-160
   VCF records: REF/ALT/GT, filters, BQ/MQ/QD/QP/AF fields  S/Vcf.scala:74-176, S/PileUp.scala:55-71
   H12 output names, FASTA wrapping, changes format          S/GenomeFile.scala:79-82,135-161
 """
@@ -653,34 +653,8 @@ def test_changes_and_fasta_after_indel_fixes():
     ref = "".join(ref)
     snp = "ACGT"[("ACGT".index(ref[99]) + 2) % 4]
     assert ref[299] != "A" and ref[298] != ref[299] and ref[499] != ref[501]
-    # sample coordinate of each reference locus; the insertion sits between 300 and 301
-    sample = ref[:99] + snp + ref[100:300] + "CA" + ref[300:500] + ref[502:]
-
-    def to_sample(locus):
-        return locus - 1 + (2 if locus >= 301 else 0) - (2 if locus >= 503 else 0)
-
-    recs = []
-    for p in range(1, 700 - 59, 2):
-        last = p + 59
-        if {p, last} & {300, 301, 500, 501, 502, 503}:
-            continue
-        cigar, seq, loc = [], "", p
-        while loc <= last:
-            if loc == 301 and p < 301:
-                cigar.append((2, "I"))
-                seq += "CA"
-            if loc == 501 and p < 501:
-                cigar.append((2, "D"))
-                loc = 503
-                last += 2
-                continue
-            if cigar and cigar[-1][1] == "M":
-                cigar[-1] = (cigar[-1][0] + 1, "M")
-            else:
-                cigar.append((1, "M"))
-            seq += sample[to_sample(loc)]
-            loc += 1
-        recs.append(read(p, cigar, seq))
+    recs, sample = _tile_reads(ref, snps={100: snp}, ins={301: "CA"}, dels={501: 502})
+    assert sample == ref[:99] + snp + ref[100:300] + "CA" + ref[300:500] + ref[502:]
     st = build_store(recs)
     with tempfile.TemporaryDirectory() as d:
         pre = os.path.join(d, "o")
@@ -858,3 +832,76 @@ def test_H8_indel_string_with_N_is_not_called():
     assert not p["call"] & _abi.PG_CALL_INS and (p["call"] >> 9) & 7 == _abi.PG_CHANGE_NONE
     ref, res = _ins_case(8, 2, ins="CA")
     assert at(res, 51)["call"] & _abi.PG_CALL_INS
+
+
+def _tile_reads(ref, snps=None, ins=None, dels=None, length=60, step=2):
+    """Reads of `length` bases starting every `step` loci, carrying the sample's
+    edits with matching CIGARs: snps {locus: base}, ins {locus: bases inserted
+    before locus}, dels {first locus: last locus}.  Reads start on a plain
+    reference base and end inside an M run, as an aligner would place them.
+    Returns (records, sample sequence)."""
+    snps, ins, dels = snps or {}, ins or {}, dels or {}
+    sample, loc = [], 1
+    while loc <= len(ref):
+        if loc in ins:
+            sample.append(ins[loc])
+        if loc in dels:
+            loc = dels[loc] + 1
+            continue
+        sample.append(snps.get(loc, ref[loc - 1]))
+        loc += 1
+    deleted = {x for a, b in dels.items() for x in range(a, b + 1)}
+    recs = []
+    for p in range(1, len(ref) + 1, step):
+        if p in deleted or p in ins:
+            continue
+        cigar, seq, loc = [], "", p
+        while len(seq) < length and loc <= len(ref):
+            if loc > p and loc in ins:
+                cigar.append((len(ins[loc]), "I"))
+                seq += ins[loc]
+                if len(seq) >= length:
+                    break
+            if loc > p and loc in dels:
+                cigar.append((dels[loc] - loc + 1, "D"))
+                loc = dels[loc] + 1
+                continue
+            if cigar and cigar[-1][1] == "M":
+                cigar[-1] = (cigar[-1][0] + 1, "M")
+            else:
+                cigar.append((1, "M"))
+            seq += snps.get(loc, ref[loc - 1])
+            loc += 1
+        if len(seq) != length or cigar[-1][1] != "M":
+            continue
+        recs.append(read(p, cigar, seq))
+    return recs, "".join(sample)
+
+
+def test_changes_offsets_across_region_chunks():
+    """A 700-bp contig polished in two 350-bp regions (GenomeFile.contigRegions,
+    S/GenomeFile.scala:67-74).  writeChanges (S/GenomeRegion.scala:645-657) adds
+    the delta of the region's earlier fixes, and GenomeFile adds the length
+    change of the contig's earlier regions as the offset (S/GenomeFile.scala:150-153):
+      chr1:101 chr1_pilon:101-102 . CA           region 1, offset 0
+      chr1:501-502 chr1_pilon:503 r501r502 .     region 2, offset +2, delta 0
+      chr1:600 chr1_pilon:600 r600 s             offset +2, delta -2
+    The FASTA joins the two fixed regions into the sample sequence."""
+    ref = list(rand_ref(700, seed=12))
+    if ref[99] == "A":   # locus 100 is not 'A': the insertion does not shift
+        ref[99] = "T" if ref[98] != "T" and ref[100] != "T" else "G"
+    while ref[499] == ref[501]:  # locus 500 differs from locus 502: the deletion does not shift
+        ref[499] = "ACGT"[("ACGT".index(ref[499]) + 1) % 4]
+    ref = "".join(ref)
+    assert ref[99] != "A" and ref[98] != ref[99] != ref[100]
+    snp = "ACGT"[("ACGT".index(ref[599]) + 2) % 4]
+    recs, sample = _tile_reads(ref, snps={600: snp}, ins={101: "CA"}, dels={501: 502})
+    st = build_store(recs)
+    with tempfile.TemporaryDirectory() as d:
+        pre = os.path.join(d, "o")
+        assert oracle.polish(st, _abi.default_params(), ["chr1"], [ref_from(ref)], pre, chunk_size=350) == 0
+        ch = open(pre + ".changes").read().splitlines()
+        fa = "".join(open(pre + ".fasta").read().splitlines()[1:])
+    assert ch == ["chr1:101 chr1_pilon:101-102 . CA", f"chr1:501-502 chr1_pilon:503 {ref[500:502]} .",
+                  f"chr1:600 chr1_pilon:600 {ref[599]} {snp}"]
+    assert fa == sample and len(fa) == 700
