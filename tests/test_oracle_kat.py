@@ -287,6 +287,16 @@ def test_kmer_tally_hand_case():
     assert got == exp
 
 
+
+def test_kmer_tally_depth_cut():
+    """buildGraph keeps K-mers with depth >= minDepth (S/Assembler.scala:138):
+    four copies of the read above give depth 8 to ACG and CGT (both strands) and
+    4 to the rest, so only those two have edges; CGT ties 4 T against 4 A."""
+    st = build_store([read(10, [(8, "M")], "ACGTTACG", qual=30, mapq=20)] * 4)
+    e = oracle.kmer_tally(st, _abi.default_params(), [(0, 4)], 3, min_depth=5)
+    got = {(int(x["next"]), int(x["alt"]), int(x["depth"])) for x in e}
+    assert len(e) == 2 and got == {(3, -1, 8), (0, 3, 8)}
+
 def test_summary_regions_merge_rule():
     """GenomeRegion.summaryRegions closes a run at the first untested position
     more than slop past the last tested one (S/GenomeRegion.scala:748-757):
