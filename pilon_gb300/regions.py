@@ -41,9 +41,17 @@ class ReadIndex:
     def __init__(self, reads, n_contigs):
         self.reads = reads
         rid = reads.ref_id
-        self.contig_lo = np.searchsorted(rid, np.arange(n_contigs), side="left")
-        self.contig_hi = np.searchsorted(rid, np.arange(n_contigs), side="right")
-        span = (reads.aend.astype(np.int64) - reads.pos.astype(np.int64) + 1)
+        # A coordinate-sorted BAM ends with its unplaced reads (reference -1),
+        # which no region query returns; the placed reads before them are
+        # sorted by reference.
+        placed = np.nonzero(rid >= 0)[0]
+        m = int(placed[-1]) + 1 if placed.size else 0
+        head = rid[:m]
+        if m and (int(head.min()) < 0 or bool(np.any(head[1:] < head[:-1]))):
+            raise ValueError("reads are not coordinate-sorted: unplaced reads (reference -1) must come last")
+        self.contig_lo = np.searchsorted(head, np.arange(n_contigs), side="left")
+        self.contig_hi = np.searchsorted(head, np.arange(n_contigs), side="right")
+        span = (reads.aend[:m].astype(np.int64) - reads.pos[:m].astype(np.int64) + 1)
         self.max_span = int(span.max()) if span.size else 0
 
     def range_for(self, contig, start, stop, contig_len, slop=SLOP):

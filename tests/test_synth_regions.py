@@ -1,8 +1,9 @@
 """Synthetic workloads and region planning (host logic, CPU only)."""
 import numpy as np
+import pytest
 
 from pilon_gb300 import synth
-from pilon_gb300.reads import CIGAR_OPS
+from pilon_gb300.reads import CIGAR_OPS, build_store, concat_stores
 from pilon_gb300.regions import contig_regions, parse_targets, plan_regions
 
 
@@ -55,3 +56,21 @@ def test_targets():
     names, lens = ["a", "b"], [1000, 500]
     assert parse_targets("a:10-20,b", names, lens) == [(0, 10, 20), (1, 1, 500)]
     assert contig_regions(1000, 300) == [(1, 250), (251, 500), (501, 750), (751, 1000)]
+
+
+def test_unplaced_reads_at_the_end_are_left_out():
+    """A coordinate-sorted BAM ends with its unplaced reads (reference -1, BAM
+    position -1); no region query returns them, so the plan of a store with
+    such a tail equals the plan without it, the last contig included.  A
+    reference -1 read before placed reads is not coordinate order."""
+    d = synth.generate(3, scale=0.005)
+    lens = [c.size for c in d.contigs]
+    rec = dict(pos=0, cigar=[], seq="ACGT" * 10, qual=[30] * 40, flag=4, mapq=0, ref_id=-1, mate_ref_id=-1)
+    tail = build_store([rec] * 7)
+    tail.aend = np.zeros(7, np.int32)
+    plain = plan_regions(d.reads, lens, chunk_size=5000)
+    assert plan_regions(concat_stores([d.reads, tail]), lens, chunk_size=5000) == plain
+    last = [r for r in plain if r[0] == len(lens) - 1]
+    assert last and all(b > a for (_, _, _, a, b) in last)
+    with pytest.raises(ValueError, match="coordinate-sorted"):
+        plan_regions(concat_stores([tail, d.reads]), lens, chunk_size=5000)
