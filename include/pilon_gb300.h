@@ -95,7 +95,10 @@ typedef struct pg_reads {
  * [read_begin, read_end) must contain every read of `contig` that overlaps
  * [max(start-10000,0), min(stop+10000,len)] (S/BamFile.scala:117-119); reads
  * outside that window inside the range are skipped by the engine, exactly as
- * the reference's query would not return them. */
+ * the reference's query would not return them.  The range must hold reads of
+ * `contig` only, in position order (it is searched by position): not the
+ * neighbouring contigs' reads nor the unplaced reads (reference -1) at the end
+ * of a coordinate-sorted store. */
 typedef struct pg_region {
   int32_t contig;            /* index into the contigs given to pg_set_reference */
   int32_t start;             /* 1-based first base */
