@@ -1,0 +1,124 @@
+"""The host side of pilon_gb300.polish on the CPU: fix lists, the AMB options,
+fixFixList, fixIssues, the changes offsets across region chunks and the FASTA
+(S/GenomeRegion.scala:307-414, 557-657, S/GenomeFile.scala:135-161).
+
+A test-only stand-in answers the engine calls polish() makes (set_reference,
+set_reads, pileup_regions, stats and the pg_fetch_region ctypes call) from the
+oracle's per-region results; the FASTA and changes files polish() writes must
+then equal the oracle's own restatement of GenomeFile.processRegions byte for
+byte.  The VCF records come from the engine's device formatter and are compared
+in the GPU tests, so VCF output is off here.
+"""
+import ctypes as C
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from pilon_gb300 import _abi, synth
+from pilon_gb300.polish import Options, polish
+
+FIELDS = ["count", "qual_sum", "mq_sum", "q_sum", "phys_cov", "insert_size", "bad_pair", "deletions", "del_qual",
+          "insertions", "ins_qual", "clips", "call", "score", "indel_len", "ins_str"]
+
+
+class _OracleFetch:
+    """pg_fetch_region's contract (include/pilon_gb300.h) over an oracle result:
+    fills every non-NULL field; with ins_chars NULL it only reports the pool's
+    size in ins_chars_cap, else it copies the pool when it fits."""
+
+    def __init__(self, owner):
+        self.owner = owner
+
+    def pg_fetch_region(self, h, r, oref):
+        o = oref._obj
+        res = self.owner.results[r]
+        for f in FIELDS:
+            dst = getattr(o, f)
+            if dst:
+                a = np.ascontiguousarray(getattr(res, f))
+                C.memmove(dst, a.ctypes.data, a.nbytes)
+        ins = np.nonzero(res.ins_str >= 0)[0]
+        used = int((res.ins_str[ins].astype(np.int64) + res.indel_len[ins]).max()) if ins.size else 0
+        if o.ins_chars:
+            if used > o.ins_chars_cap:
+                return _abi.PG_ERR_LIMIT
+            C.memmove(o.ins_chars, res.ins_chars.ctypes.data, used)
+        o.ins_chars_cap = used
+        return _abi.PG_OK
+
+
+class OracleEngine:
+    """Test-only stand-in for pilon_gb300.engine.Engine, backed by the oracle."""
+    h = None
+
+    def __init__(self):
+        self.L = _OracleFetch(self)
+
+    def set_reference(self, contigs):
+        self.contigs = contigs
+
+    def set_reads(self, reads):
+        self.reads = reads
+
+    def pileup_regions(self, regions, params, batched=True):
+        self.results = [oracle.process_region(self.reads, params, self.contigs[c], c, s, e, rb, re)
+                        for (c, s, e, rb, re) in regions]
+        assert all(r.status == 0 for r in self.results)
+
+    def stats(self, r):
+        return self.results[r].stats
+
+    def _check(self, st):
+        assert st == _abi.PG_OK, st
+
+    def format_vcf(self, *a, **k):
+        raise AssertionError("the VCF records are the engine's; VCF output is off in these tests")
+
+
+def compare(ds, params=None, chunk=10_000_000, **kw):
+    params = params or _abi.default_params()
+    opts = Options(chunk_size=chunk, vcf=False, **kw)
+    with tempfile.TemporaryDirectory() as d:
+        h, o = os.path.join(d, "host"), os.path.join(d, "ora")
+        polish(OracleEngine(), ds.names, ds.contigs, ds.reads, params, h, opts)
+        assert oracle.polish(ds.reads, params, ds.names, ds.contigs, o, chunk_size=chunk, fix_snps=opts.fix_snps,
+                             fix_indels=opts.fix_indels, iupac=opts.iupac, diploid=opts.diploid) == 0
+        for ext in ("fasta", "changes"):
+            a, b = open(f"{h}.{ext}", "rb").read(), open(f"{o}.{ext}", "rb").read()
+            assert a == b, ext
+        return open(f"{h}.changes").read().count("\n")
+
+
+def test_defaults(cfg1):
+    assert compare(cfg1) >= 20
+
+
+@pytest.mark.parametrize("kw,pk", [(dict(chunk=9000, iupac=True), dict(fix_amb=1)),
+                                   (dict(chunk=20000), dict(fix_amb=1)),
+                                   (dict(fix_indels=False), {}),
+                                   (dict(fix_snps=False), {})])
+def test_options_and_chunks(cfg1, kw, pk):
+    compare(cfg1, params=_abi.default_params(**pk), **kw)
+
+
+def test_many_contigs():
+    compare(synth.generate(3, scale=0.01))
+
+
+@pytest.mark.parametrize("ref_base,kw,pk", [("G", {}, {}), ("G", dict(iupac=True), {}), ("C", {}, {}),
+                                            ("C", dict(iupac=True), dict(fix_amb=1))])
+def test_ambiguous_fixes(ref_base, kw, pk):
+    """The AMB branches (base or IUPAC code, --fix amb) on the hand-worked
+    6A/4C position, which the synthetic workloads do not produce."""
+    from types import SimpleNamespace
+    from pilon_gb300.reads import build_store
+    from tests.test_oracle_kat import _het_reads, rand_ref, ref_from
+    ref = list(rand_ref(100, seed=5))
+    ref[49] = ref_base
+    ref = "".join(ref)
+    ds = SimpleNamespace(names=["chr1"], contigs=[ref_from(ref)], reads=build_store(_het_reads(ref)))
+    n = compare(ds, params=_abi.default_params(**pk), **kw)
+    assert n == (1 if ref_base == "G" or pk else 0)
