@@ -12,7 +12,7 @@ lines.  One case per parity hazard of the hot path:
   H5 BaseCall score, q and highConfidence arithmetic        S/PileUp.scala:132-153
   H6 stable base order on ties                              S/BaseSum.scala:57-60
   indel call thresholds (insertions and deletions)          S/PileUp.scala:182-247
-  H7 insert-size statistics per region (FR / RF)            S/BamFile.scala:194-202
+  H7 insert-size statistics per region (FR / RF), cutoff    S/BamFile.scala:161-165,192-202
   minDepth: (0.1 * meanCoverage).round max 5                S/GenomeRegion.scala:221-224
   H9 K-mer tally read rules (length, clips, N, minQual)     S/Assembler.scala:55-87
   H10 Java "%.2f" rounding of AF                            S/Vcf.scala:134-152
@@ -505,6 +505,27 @@ def test_insert_size_statistics():
     assert (st.rf_count, st.rf_sum, st.rf_sumsq) == (2, 39 + 250, 39 * 39 + 250 * 250)
     assert st.read_count == 6
 
+
+def _wrap32(x):
+    return (x + 2 ** 31) % 2 ** 32 - 2 ** 31
+
+
+@pytest.mark.parametrize("bam_type,tlen,counted", [(_abi.PG_BAM_FRAGS, 2499, True), (_abi.PG_BAM_FRAGS, 2500, False),
+                                                   (_abi.PG_BAM_JUMPS, 2500, True),
+                                                   (_abi.PG_BAM_JUMPS, 49999, True),
+                                                   (_abi.PG_BAM_JUMPS, 50000, False)])
+def test_insert_size_cutoff_and_int_square(bam_type, tlen, counted):
+    """addInsert counts sizes below huge = 5 * maxInsertSizes(bamType): 2,500 for
+    frags, 50,000 for jumps (S/BamFile.scala:29, 192-202; the 10x `huge` of
+    process only guards a commented-out warning).  InsertSizeStats.add squares
+    the size as a Scala Int before widening it (S/BamFile.scala:161-165), so
+    49,999^2 = 2,499,900,001 wraps to -1,795,067,295 in sumSq."""
+    ref = rand_ref(600, seed=2)
+    rec = read(160, [(40, "M")], ref[159:199], flag=0x1 | 0x2 | 0x20, tlen=tlen)
+    st = run(ref, [rec], bam_type=bam_type).stats
+    want = (1, tlen, _wrap32(tlen * tlen)) if counted else (0, 0, 0)
+    assert (st.fr_count, st.fr_sum, st.fr_sumsq) == want
+    assert st.rf_count == 0
 
 @pytest.mark.parametrize("hole", [(400, 449), (600, 615), (300, 303)])
 def test_possible_breaks_low_coverage_and_dip(hole):
