@@ -118,3 +118,48 @@ def test_open_errors_are_statuses():
         pytest.skip("a CUDA device is present")
     assert st == _abi.PG_ERR_CUDA and lib.pg_last_error(ctx) == b"no CUDA device 0"
     lib.pg_close(ctx)
+
+
+C_CLIENT = r"""
+#include <stdio.h>
+#include <string.h>
+#include "pilon_gb300.h"
+
+int main(void) {
+  pg_params p;
+  pg_default_params(&p);
+  if (p.flank != 10 || p.default_qual != 10 || p.min_min_depth != 5) return 2;
+  pg_ctx *ctx = NULL;
+  pg_status st = pg_open(&ctx, -1);
+  if (st != PG_ERR_CUDA || ctx == NULL) return 3;
+  if (strcmp(pg_last_error(ctx), "no CUDA device -1") != 0) return 4;
+  if (pg_sync(ctx) != PG_ERR_STATE) return 5;
+  pg_close(ctx);
+  printf("%s|%zu|%zu|%zu\n", pg_version(), sizeof(pg_region), sizeof(pg_params), sizeof(pg_kmer_edge));
+  return 0;
+}
+"""
+
+
+def test_header_compiles_as_c99_and_links(tmp_path):
+    """A C client (what a JNI glue file is) compiles against the header with
+    -std=c99 -Wall -Werror, links the library and calls it."""
+    import shutil
+    import subprocess
+    from pilon_gb300.build import ENGINE, build
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    if not os.path.exists(ENGINE):
+        build()
+    src = tmp_path / "client.c"
+    src.write_text(C_CLIENT)
+    exe = tmp_path / "client"
+    lib_dir = os.path.dirname(ENGINE)
+    lib_name = os.path.basename(ENGINE)[3:-3]  # libX.so -> X
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-o", str(exe), "-L", lib_dir, "-l" + lib_name, "-Wl,-rpath," + lib_dir],
+                   check=True, capture_output=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, (out.returncode, out.stderr)
+    version, r, p, e = out.stdout.strip().split("|")
+    assert version.startswith("pilon_gb300") and (int(r), int(p), int(e)) == (32, 56, 32)
