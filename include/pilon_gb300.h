@@ -52,7 +52,7 @@ typedef struct pg_params {
   int32_t min_mq;          /* --minmq, default 0 */
   int32_t min_qual;        /* --minqual, default 0 */
   int32_t flank;           /* --flank, default 10 */
-  int32_t default_qual;    /* --defaultqual, default 10 */
+  int32_t default_qual;    /* --defaultqual, default 10; a byte (-128..127) as in Pilon */
   int32_t min_min_depth;   /* constant 5 */
   int32_t nonpf;           /* --nonpf */
   int32_t duplicates;      /* --duplicates */

@@ -292,6 +292,14 @@ pg_status pg_set_tuning(pg_ctx* c, int32_t tile_width, int32_t warps_per_cta, in
   return PG_OK;
 }
 
+// Pilon's --defaultqual is a Byte (S/Pilon.scala:53, 144: value.toByte throws
+// outside -128..127); the walk's packed counters rely on that range too.
+static pg_status check_default_qual(pg_ctx* c, const pg_params* p) {
+  if (p->default_qual < -128 || p->default_qual > 127)
+    return fail(c, PG_ERR_ARG, "default_qual %d is outside a byte (-128..127)", p->default_qual);
+  return PG_OK;
+}
+
 // A context whose pg_open failed has no stream; calls that would use the
 // device on it fail with PG_ERR_STATE instead of running on the legacy stream.
 static pg_status not_open(pg_ctx* c) {
@@ -502,9 +510,10 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
                             int32_t batched) {
   const Range nvtx_range("pg_pileup_regions");
   if (!c || (n_regions > 0 && !regs) || !params || n_regions < 0) return fail(c, PG_ERR_ARG, "bad arguments");
-  if (!c->have_reads) return fail(c, PG_ERR_STATE, "pg_set_reads must come first");
   if (params->min_qual < 0 || params->flank < 0 || params->min_mq < 0)
     return fail(c, PG_ERR_ARG, "min_qual, min_mq and flank must be >= 0");
+  if (pg_status s0 = check_default_qual(c, params)) return s0;
+  if (!c->have_reads) return fail(c, PG_ERR_STATE, "pg_set_reads must come first");
   cudaSetDevice(c->device);
   c->brk_n = -1;
   c->have_results = false;
@@ -779,6 +788,7 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
   if (K < 1 || K > 31) return fail(c, PG_ERR_LIMIT, "K = %d: the GPU tally packs K-mers in 64 bits (K <= 31)", K);
   if (min_depth < 1) return fail(c, PG_ERR_ARG, "min_depth must be >= 1");
   if (params->min_qual < 0) return fail(c, PG_ERR_ARG, "min_qual must be >= 0");
+  if (pg_status s0 = check_default_qual(c, params)) return s0;
   if (!c->have_reads) return fail(c, PG_ERR_STATE, "pg_set_reads must come first");
   cudaSetDevice(c->device);
   *n_edges = 0;
@@ -958,6 +968,7 @@ pg_status pg_kmer_tally_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius,
   if (K < 1 || K > 31) return fail(c, PG_ERR_LIMIT, "K = %d: the GPU tally packs K-mers in 64 bits (K <= 31)", K);
   if (min_depth < 1) return fail(c, PG_ERR_ARG, "min_depth must be >= 1");
   if (params->min_qual < 0) return fail(c, PG_ERR_ARG, "min_qual must be >= 0");
+  if (pg_status s0 = check_default_qual(c, params)) return s0;
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no pileup results: call pg_pileup_regions first");
   cudaSetDevice(c->device);
   *n_edges = 0;

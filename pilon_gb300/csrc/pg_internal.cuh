@@ -135,12 +135,14 @@ constexpr int kCallTile = 1024;     // positions per call / scan tile
 constexpr int kReadsPerChunk = 256;   // one read per thread of k_read_events
 // Reads one walk pass adds to a tile.  At most 4095 reads per position keep the
 // packed shared counters exact: sum of qual (20 bits) + count (12 bits) in one
-// word for qualities up to 256 (a larger defaultQual lowers the pass size), and
-// the qual * (mq + 1 - M) sums within int32.
+// word for qualities up to 256 (the API keeps defaultQual within a byte; a
+// larger one would lower the pass size here, never to 0), and the
+// qual * (mq + 1 - M) sums within int32.
 constexpr int64_t kMaxReadsPerPass = 4095;
 inline int32_t walk_reads_per_pass(int32_t default_qual) {
   const int32_t q = default_qual > 127 ? default_qual : 127;
-  return (int32_t)(kMaxReadsPerPass < 1048575 / q ? kMaxReadsPerPass : 1048575 / q);
+  const int64_t n = kMaxReadsPerPass < 1048575 / q ? kMaxReadsPerPass : 1048575 / q;
+  return (int32_t)(n > 0 ? n : 1);  // a pass always advances
 }
 
 // ---- Java integer helpers (wrapping Int, truncating division) -------------

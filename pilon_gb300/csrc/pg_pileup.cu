@@ -200,9 +200,10 @@ void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tile
 //   mqSum      = M * (count of all four md) + mx,   qSum = sums of qual of md
 // which holds for any M, so the reads of the most common mq add a base with one
 // shared atomic and the others with three.  The words stay exact while a pass
-// adds at most reads_per_pass reads to a position (4095, fewer when defaultQual
-// exceeds 255 so that the qual sums keep within 20 bits); tiles with more reads
-// run several passes and add each pass's sums into the records.
+// adds at most reads_per_pass reads to a position (4095: qualities are bytes,
+// at most 127, so the qual sums keep within 20 bits; the API refuses a
+// defaultQual outside a byte); tiles with more reads run several passes and add
+// each pass's sums into the records.
 //
 // Each warp takes the tile's reads 32 at a time.  Every lane first builds the
 // descriptor of one read in registers: the filters of BamFile.process, the

@@ -109,6 +109,16 @@ def test_open_errors_are_statuses():
     assert lib.pg_pileup_regions(bad, None, 0, C.byref(p), 1) == _abi.PG_ERR_STATE
     stats = _abi.pg_region_stats()
     assert lib.pg_fetch_stats(bad, 0, C.byref(stats)) == _abi.PG_ERR_STATE
+    # --defaultqual is a Byte in Pilon: values outside -128..127 are argument errors
+    n1, n2 = C.c_int64(), C.c_int64()
+    for dq, want in [(128, _abi.PG_ERR_ARG), (-129, _abi.PG_ERR_ARG), (2 ** 21, _abi.PG_ERR_ARG),
+                     (127, _abi.PG_ERR_STATE), (-128, _abi.PG_ERR_STATE)]:
+        q = _abi.default_params(default_qual=dq)
+        assert lib.pg_pileup_regions(bad, None, 0, C.byref(q), 1) == want, dq
+        assert lib.pg_kmer_tally(bad, None, 0, 31, C.byref(q), 5, None, C.c_int64(0), C.byref(n1)) == want, dq
+        assert lib.pg_kmer_tally_breaks(bad, 5, 100, 31, C.byref(q), 5, None, C.c_int64(0), C.byref(n1),
+                                        C.byref(n2)) == want, dq
+    assert lib.pg_last_error(bad) == b"no pileup results: call pg_pileup_regions first"
     lib.pg_close(bad)
 
     ctx = C.c_void_p()
