@@ -40,11 +40,28 @@ inline int32_t roundDivI(int32_t n, int32_t d) { return d > 0 ? (n + d / 2) / d 
 inline int64_t pctL(int64_t n, int64_t d) { return roundDivL(100 * n, d); }
 inline int32_t pctI(int32_t n, int32_t d) { return roundDivI(100 * n, d); }
 
-// java.lang.Math.round(double): nearest, ties toward positive infinity.
+// java.lang.Math.round(double): nearest, ties toward positive infinity; NaN
+// gives 0 and values beyond the long range saturate (JLS 5.1.3).
 inline int64_t javaRound(double x) {
+  if (std::isnan(x)) return 0;
   double f = std::floor(x);
-  return (int64_t)((x - f >= 0.5) ? f + 1.0 : f);
+  double r = (x - f >= 0.5) ? f + 1.0 : f;
+  if (r >= 9223372036854775807.0) return INT64_MAX;
+  if (r <= -9223372036854775808.0) return INT64_MIN;
+  return (int64_t)r;
 }
+
+// Java's double-to-int conversion (Scala Double.toInt): truncation toward
+// zero, NaN gives 0, values beyond the int range saturate (JLS 5.1.3).
+inline int32_t javaD2I(double x) {
+  if (std::isnan(x)) return 0;
+  if (x >= 2147483647.0) return INT32_MAX;
+  if (x <= -2147483648.0) return INT32_MIN;
+  return (int32_t)x;
+}
+
+// Scala Long.toInt: the low 32 bits.
+inline int32_t javaL2I(int64_t x) { return (int32_t)(uint32_t)(uint64_t)x; }
 
 inline int baseIndex(char c) {  // S/PileUp.scala:55-61
   switch (c) {
@@ -576,8 +593,8 @@ struct GenomeRegion {
       for (int32_t i = 0; i < size(); i++)
         excluded[i] = homoRunG(locus(i)) >= 4 || (nano && nanoporeExcludeG(locus(i)));
     }
-    if (P.minDepth >= 1) minDepth = (int32_t)P.minDepth;
-    else minDepth = std::max((int32_t)javaRound(P.minDepth * (double)meanCoverage), P.minMinDepth);
+    if (P.minDepth >= 1) minDepth = javaD2I(P.minDepth);
+    else minDepth = std::max(javaL2I(javaRound(P.minDepth * (double)meanCoverage)), P.minMinDepth);
     if (nReads == 0) return;
     bool fixamb = P.fixAmb;
     for (int32_t i = 0; i < size(); i++) {

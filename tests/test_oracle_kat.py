@@ -429,6 +429,19 @@ def test_min_depth_option_at_least_one_is_a_count():
     assert run(ref, recs, min_depth=12.0).stats.min_depth == 12
 
 
+@pytest.mark.parametrize("md,want", [(12.9, 12), (1e10, 2 ** 31 - 1), (float("inf"), 2 ** 31 - 1),
+                                     (float("nan"), 5), (float("-inf"), 5), (-3.0, 5)])
+def test_min_depth_option_java_conversions(md, want):
+    """minDepth (S/GenomeRegion.scala:221-224) with Java's conversions:
+    minDepth >= 1 takes Double.toInt (truncates; saturates at Int.MaxValue);
+    otherwise Math.round (NaN -> 0, -inf -> Long.MinValue) then Long.toInt (low
+    32 bits: 0) and max 5."""
+    ref = rand_ref(100, seed=9)
+    recs = [read(1 + (k % 61), [(40, "M")], ref[k % 61:k % 61 + 40]) for k in range(300)]
+    recs.sort(key=lambda r: r["pos"])
+    assert run(ref, recs, min_depth=md).stats.min_depth == want
+
+
 def test_kmer_tally_read_rules():
     """Assembler.addRead/addToPileups (S/Assembler.scala:55-87), K = 4, five copies of each read:
       a read of length K adds nothing (length > K is required);
