@@ -8,6 +8,7 @@ lines.  One case per parity hazard of the hot path:
   H3 a left shift below the region start throws             S/PileUpRegion.scala:155-182
   H4 indels count by their region bounds (pre-shift locus)  S/PileUpRegion.scala:155,166
   long-read indels: mq min 8, homopolymer runs dropped      S/PileUpRegion.scala:120-126,142-183
+  nanopore CC?GG motif bases at quality 0 (region index)    S/PileUpRegion.scala:128-134,189
   H5 integer rounding (roundDiv, adjMq)                     S/Utils.scala:23-26, S/PileUpRegion.scala:139-142
   H5 BaseCall score, q and highConfidence arithmetic        S/PileUp.scala:132-153
   H6 stable base order on ties                              S/BaseSum.scala:57-60
@@ -949,3 +950,28 @@ def test_changes_offsets_across_region_chunks():
     assert ch == ["chr1:101 chr1_pilon:101-102 . CA", f"chr1:501-502 chr1_pilon:503 {ref[500:502]} .",
                   f"chr1:600 chr1_pilon:600 {ref[599]} {snp}"]
     assert fa == sample and len(fa) == 700
+
+
+@pytest.mark.parametrize("long_read,start,zeroed", [(_abi.PG_NANOPORE, 1, 50), (_abi.PG_NANOPORE, 31, 80),
+                                                    (_abi.PG_PACBIO, 1, None)])
+def test_nanopore_motif_quality_zero(long_read, start, zeroed):
+    """Nanopore reads add the base at the centre of a CC?GG motif with quality 0
+    (S/PileUpRegion.scala:128-134, 189).  nanoporeExclude(index(locus)) reads the
+    contig at the region index: with the motif centred on locus 50, a region
+    starting at 1 zeroes locus 50, one starting at 31 zeroes locus 80 (index 49)
+    and not 50.  PacBio reads keep their qualities.  Ten reads 40M at 31 and at
+    61, quality 30, mapq 60: a zeroed locus has count 10, qualSum 0, mqSum 610."""
+    ref = list(rand_ref(120, seed=41))
+    ref[47:52] = "CCAGG"
+    ref = "".join(ref)
+    motif = lambda c: ref[c - 3] == "C" and ref[c - 2] == "C" and ref[c] == "G" and ref[c + 1] == "G"
+    assert motif(50) and not motif(80) and not motif(20)
+    recs = [read(31, [(40, "M")], ref[30:70]) for _ in range(10)]
+    recs += [read(61, [(40, "M")], ref[60:100]) for _ in range(10)]
+    res = run(ref, recs, start=start, long_read=long_read)
+    assert res.status == 0
+    for locus in (50, 80):
+        p = at(res, locus, start=start)
+        b = "ACGT".index(ref[locus - 1])
+        assert p["count"][b] == 10 and p["mq"] == 610
+        assert p["qual_sum"][b] == (0 if locus == zeroed else 10 * 30 * 61), locus
