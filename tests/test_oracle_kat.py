@@ -9,6 +9,7 @@ lines.  One case per parity hazard of the hot path:
   H4 indels count by their region bounds (pre-shift locus)  S/PileUpRegion.scala:155,166
   long-read indels: mq min 8, homopolymer runs dropped      S/PileUpRegion.scala:120-126,142-183
   nanopore CC?GG motif bases at quality 0 (region index)    S/PileUpRegion.scala:128-134,189
+  long reads only: run starts of 4+ bases are not fixed     S/GenomeRegion.scala:326,416-439
   H5 integer rounding (roundDiv, adjMq)                     S/Utils.scala:23-26, S/PileUpRegion.scala:139-142
   H5 BaseCall score, q and highConfidence arithmetic        S/PileUp.scala:132-153
   H6 stable base order on ties                              S/BaseSum.scala:57-60
@@ -975,3 +976,28 @@ def test_nanopore_motif_quality_zero(long_read, start, zeroed):
         b = "ACGT".index(ref[locus - 1])
         assert p["count"][b] == 10 and p["mq"] == 610
         assert p["qual_sum"][b] == (0 if locus == zeroed else 10 * 30 * 61), locus
+
+
+@pytest.mark.parametrize("snp_locus,fixed", [(61, False), (62, True), (40, True)])
+def test_long_read_only_excludes_run_starts(snp_locus, fixed):
+    """With long reads only, excludeMotifs (S/GenomeRegion.scala:416-439) marks
+    the loci whose forward reference run (to the region's end) has 4 or more
+    bases, and identifyAndFixIssues skips their changes (S/GenomeRegion.scala:326).
+    In an A run at loci 60-64 that is 60 (run 5) and 61 (run 4), not 62 (run 3):
+    a homozygous SNP at 61 is not fixed, one at 62 or outside the run is."""
+    ref = list(rand_ref(120, seed=43))
+    ref[58], ref[59:64], ref[64] = "C", "AAAAA", "G"
+    ref = "".join(ref)
+    snp = "T" if ref[snp_locus - 1] != "T" else "G"
+    recs, sample = _tile_reads(ref, snps={snp_locus: snp}, length=40, step=1)
+    st = build_store(recs)
+    params = _abi.default_params(long_read=_abi.PG_PACBIO, long_read_only=1)
+    with tempfile.TemporaryDirectory() as d:
+        pre = os.path.join(d, "o")
+        assert oracle.polish(st, params, ["chr1"], [ref_from(ref)], pre) == 0
+        ch = open(pre + ".changes").read().splitlines()
+        fa = "".join(open(pre + ".fasta").read().splitlines()[1:])
+    if fixed:
+        assert ch == [f"chr1:{snp_locus} chr1_pilon:{snp_locus} {ref[snp_locus - 1]} {snp}"] and fa == sample
+    else:
+        assert ch == [] and fa == ref

@@ -78,9 +78,10 @@ class OracleEngine:
         raise AssertionError("the VCF records are the engine's; VCF output is off in these tests")
 
 
-def compare(ds, params=None, chunk=10_000_000, **kw):
+def compare(ds, params=None, chunk=10_000_000, no_frags=False, **kw):
     params = params or _abi.default_params()
     opts = Options(chunk_size=chunk, vcf=False, **kw)
+    opts.no_frags = no_frags  # long reads only: excludeMotifs applies
     with tempfile.TemporaryDirectory() as d:
         h, o = os.path.join(d, "host"), os.path.join(d, "ora")
         polish(OracleEngine(), ds.names, ds.contigs, ds.reads, params, h, opts)
@@ -122,3 +123,21 @@ def test_ambiguous_fixes(ref_base, kw, pk):
     ds = SimpleNamespace(names=["chr1"], contigs=[ref_from(ref)], reads=build_store(_het_reads(ref)))
     n = compare(ds, params=_abi.default_params(**pk), **kw)
     assert n == (1 if ref_base == "G" or pk else 0)
+
+
+@pytest.mark.parametrize("snp_locus", [61, 62, 40])
+def test_long_read_only_motif_exclusion(snp_locus):
+    """excludeMotifs with long reads only (run starts of 4+ bases are not fixed),
+    on the hand-worked A run at loci 60-64."""
+    from types import SimpleNamespace
+    from pilon_gb300.reads import build_store
+    from tests.test_oracle_kat import _tile_reads, rand_ref, ref_from
+    ref = list(rand_ref(120, seed=43))
+    ref[58], ref[59:64], ref[64] = "C", "AAAAA", "G"
+    ref = "".join(ref)
+    snp = "T" if ref[snp_locus - 1] != "T" else "G"
+    recs, _ = _tile_reads(ref, snps={snp_locus: snp}, length=40, step=1)
+    ds = SimpleNamespace(names=["chr1"], contigs=[ref_from(ref)], reads=build_store(recs))
+    params = _abi.default_params(long_read=_abi.PG_PACBIO, long_read_only=1)
+    n = compare(ds, params=params, longread=True, no_frags=True)
+    assert n == (0 if snp_locus == 61 else 1)
