@@ -6,8 +6,9 @@ A test-only stand-in answers the engine calls polish() makes (set_reference,
 set_reads, pileup_regions, stats and the pg_fetch_region ctypes call) from the
 oracle's per-region results; the FASTA and changes files polish() writes must
 then equal the oracle's own restatement of GenomeFile.processRegions byte for
-byte.  The VCF records come from the engine's device formatter and are compared
-in the GPU tests, so VCF output is off here.
+byte.  The per-position VCF records are the engine's device formatter's (compared
+in the GPU tests); here the stand-in cuts them from the oracle's VCF, so a VCF
+comparison checks what polish() adds: the header, copy number and <DUP> records.
 """
 import ctypes as C
 import os
@@ -51,11 +52,15 @@ class _OracleFetch:
 
 
 class OracleEngine:
-    """Test-only stand-in for pilon_gb300.engine.Engine, backed by the oracle."""
+    """Test-only stand-in for pilon_gb300.engine.Engine, backed by the oracle.
+    format_vcf returns a region's records cut from the oracle's own VCF of the
+    same store (a region's records all have POS inside it), without the <DUP>
+    records, which polish() splices in itself."""
     h = None
 
-    def __init__(self):
+    def __init__(self, names=None, chunk=10_000_000):
         self.L = _OracleFetch(self)
+        self.names, self.chunk, self._vcf = names, chunk, {}
 
     def set_reference(self, contigs):
         self.contigs = contigs
@@ -64,6 +69,7 @@ class OracleEngine:
         self.reads = reads
 
     def pileup_regions(self, regions, params, batched=True):
+        self.regions, self.params = regions, params
         self.results = [oracle.process_region(self.reads, params, self.contigs[c], c, s, e, rb, re)
                         for (c, s, e, rb, re) in regions]
         assert all(r.status == 0 for r in self.results)
@@ -74,27 +80,43 @@ class OracleEngine:
     def _check(self, st):
         assert st == _abi.PG_OK, st
 
-    def format_vcf(self, *a, **k):
-        raise AssertionError("the VCF records are the engine's; VCF output is off in these tests")
+    def format_vcf(self, r, name, diploid, vcf_qe, variants_only=False):
+        assert not variants_only
+        key = (bool(diploid), bool(vcf_qe))
+        if key not in self._vcf:
+            with tempfile.TemporaryDirectory() as d:
+                pre = os.path.join(d, "v")
+                assert oracle.polish(self.reads, self.params, self.names, self.contigs, pre, chunk_size=self.chunk,
+                                     diploid=diploid, vcf_qe=vcf_qe) == 0
+                body = [l for l in open(pre + ".vcf", "rb").read().split(b"\n") if l and not l.startswith(b"#")]
+            self._vcf[key] = [l for l in body if l.split(b"\t")[4] != b"<DUP>"]
+        c, s, e = self.regions[r][:3]
+        nm = name.encode()
+        out = [l for l in self._vcf[key] if l.split(b"\t")[0] == nm and s <= int(l.split(b"\t")[1]) <= e]
+        return b"".join(l + b"\n" for l in out)
 
 
-def compare(ds, params=None, chunk=10_000_000, no_frags=False, **kw):
+def compare(ds, params=None, chunk=10_000_000, no_frags=False, vcf=False, **kw):
     params = params or _abi.default_params()
-    opts = Options(chunk_size=chunk, vcf=False, **kw)
+    opts = Options(chunk_size=chunk, vcf=vcf, **kw)
     opts.no_frags = no_frags  # long reads only: excludeMotifs applies
     with tempfile.TemporaryDirectory() as d:
         h, o = os.path.join(d, "host"), os.path.join(d, "ora")
-        polish(OracleEngine(), ds.names, ds.contigs, ds.reads, params, h, opts)
+        polish(OracleEngine(ds.names, chunk), ds.names, ds.contigs, ds.reads, params, h, opts)
         assert oracle.polish(ds.reads, params, ds.names, ds.contigs, o, chunk_size=chunk, fix_snps=opts.fix_snps,
-                             fix_indels=opts.fix_indels, iupac=opts.iupac, diploid=opts.diploid) == 0
-        for ext in ("fasta", "changes"):
+                             fix_indels=opts.fix_indels, iupac=opts.iupac, diploid=opts.diploid,
+                             vcf_qe=opts.vcf_qe, vcf_date=opts.vcf_date, vcf_source=opts.vcf_source,
+                             vcf_args=opts.vcf_args, vcf_ref=opts.vcf_ref) == 0
+        out = {}
+        for ext in ("fasta", "changes") + (("vcf",) if vcf else ()):
             a, b = open(f"{h}.{ext}", "rb").read(), open(f"{o}.{ext}", "rb").read()
             assert a == b, ext
-        return open(f"{h}.changes").read().count("\n")
+            out[ext] = a
+        return out["changes"].count(b"\n"), out
 
 
 def test_defaults(cfg1):
-    assert compare(cfg1) >= 20
+    assert compare(cfg1)[0] >= 20
 
 
 @pytest.mark.parametrize("kw,pk", [(dict(chunk=9000, iupac=True), dict(fix_amb=1)),
@@ -121,7 +143,7 @@ def test_ambiguous_fixes(ref_base, kw, pk):
     ref[49] = ref_base
     ref = "".join(ref)
     ds = SimpleNamespace(names=["chr1"], contigs=[ref_from(ref)], reads=build_store(_het_reads(ref)))
-    n = compare(ds, params=_abi.default_params(**pk), **kw)
+    n, _ = compare(ds, params=_abi.default_params(**pk), **kw)
     assert n == (1 if ref_base == "G" or pk else 0)
 
 
@@ -139,5 +161,21 @@ def test_long_read_only_motif_exclusion(snp_locus):
     recs, _ = _tile_reads(ref, snps={snp_locus: snp}, length=40, step=1)
     ds = SimpleNamespace(names=["chr1"], contigs=[ref_from(ref)], reads=build_store(recs))
     params = _abi.default_params(long_read=_abi.PG_PACBIO, long_read_only=1)
-    n = compare(ds, params=params, longread=True, no_frags=True)
+    n, _ = compare(ds, params=params, longread=True, no_frags=True)
     assert n == (0 if snp_locus == 61 else 1)
+
+
+def test_vcf_header_and_duplication_record():
+    """The VCF header and the <DUP> record of copy number 2 over a 14 kb stretch
+    read twice (GenomeRegion copy number and writeDup, S/GenomeRegion.scala:
+    272-283, 623-631, S/Vcf.scala:28-68, 194-202), with the per-position records
+    taken from the oracle."""
+    w = synth.workload(1, scale=1.2)
+    ds = synth.generate(w)
+    r = ds.reads
+    sel = np.nonzero((r.pos > 20_000) & (r.aend < 34_000))[0]
+    ds.reads = r.subset(np.sort(np.concatenate([np.arange(r.n_reads), sel]), kind="stable"))
+    _, out = compare(ds, vcf=True)
+    dup = [l for l in out["vcf"].split(b"\n") if b"<DUP>" in l]
+    assert len(dup) == 1 and b"SVTYPE=DUP" in dup[0]
+    compare(ds, vcf=True, chunk=25_000, vcf_qe=True, diploid=True)
