@@ -18,7 +18,21 @@ def contig_regions(contig_len, chunk_size=10_000_000):
 
 
 def parse_targets(target_string, names, lens):
-    """--targets "name:start-stop,..." or whole contigs (S/GenomeFile.scala:215-236)."""
+    """--targets (S/GenomeFile.scala:239-249): a file whose lines are target
+    strings, or else the argument itself as one.  As in the reference, any error
+    while reading or parsing the file (a missing file, a bad or blank line) makes
+    it fall back to parsing the argument as a target string."""
+    try:
+        with open(target_string) as f:
+            lines = f.read().splitlines()
+        out = [t for line in lines for t in parse_target_string(line, names, lens)]
+    except Exception:
+        out = []
+    return out or parse_target_string(target_string, names, lens)
+
+
+def parse_target_string(target_string, names, lens):
+    """"name:start-stop,..." or whole contigs (S/GenomeFile.scala:215-236)."""
     import re
     out = []
     for t in target_string.split(","):

@@ -55,6 +55,20 @@ def test_region_read_ranges_cover_the_query_window():
 def test_targets():
     names, lens = ["a", "b"], [1000, 500]
     assert parse_targets("a:10-20,b", names, lens) == [(0, 10, 20), (1, 1, 500)]
+
+
+def test_targets_file(tmp_path):
+    """parseTargets reads a file of target strings first (S/GenomeFile.scala:
+    239-249); a file it cannot parse falls back to the argument as a string."""
+    names, lens = ["a", "b"], [1000, 500]
+    f = tmp_path / "targets.txt"
+    f.write_text("a:10-20,b\nb:5-6\n")
+    assert parse_targets(str(f), names, lens) == [(0, 10, 20), (1, 1, 500), (1, 5, 6)]
+    f.write_text("a:10-20\n\nb:5-6\n")  # a blank line fails the file; its name is no contig
+    with pytest.raises(ValueError):
+        parse_targets(str(f), names, lens)
+    with pytest.raises(ValueError, match="within contig"):
+        parse_targets("b:1-501", names, lens)
     assert contig_regions(1000, 300) == [(1, 250), (251, 500), (501, 750), (751, 1000)]
 
 
