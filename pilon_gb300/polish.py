@@ -304,26 +304,28 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
     engine.set_reads(reads)
     engine.pileup_regions(regions, params, batched=batched)
     results = [_region_outputs(engine, r, reg, contigs[reg[0]], opts, params) for r, reg in enumerate(regions)]
-    by_contig = {}
+    # The output groups of GenomeFile.regions (S/GenomeFile.scala:49-54): a contig
+    # with its chunks, or with --targets one group per target (two targets on one
+    # contig give two FASTA records, and each restarts the changes offset).
+    groups = []
     for r, res in enumerate(results):
-        by_contig.setdefault(res.contig, []).append(r)
-    order = []
-    for r, res in enumerate(results):
-        if res.contig not in order:
-            order.append(res.contig)
+        if opts.targets is None and groups and groups[-1][0] == res.contig:
+            groups[-1][1].append(r)
+        else:
+            groups.append((res.contig, [r]))
     if opts.vcf:
         with open(out_prefix + ".vcf", "wb") as vf:
-            sizes = [(names[c], sum(results[r].stop - results[r].start + 1 for r in by_contig[c])) for c in order]
+            sizes = [(names[c], sum(results[r].stop - results[r].start + 1 for r in rs)) for c, rs in groups]
             vf.write(vcf_header(sizes, opts).encode())
             for r, res in enumerate(results):
                 text = engine.format_vcf(r, names[res.contig], opts.diploid, opts.vcf_qe)
                 vf.write(_splice_dupes(text, res, names[res.contig], contigs[res.contig]))
     if opts.changes:
         with open(out_prefix + ".changes", "w") as cf:
-            for c in order:
+            for c, rs in groups:
                 nn = new_name(names[c])
                 offset = 0
-                for r in by_contig[c]:
+                for r in rs:
                     res = results[r]
                     delta = 0
                     for f in res.all_fixes():
@@ -335,8 +337,8 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
                     offset += len(res.bases) - (res.stop - res.start + 1)
     if opts.fix_snps or opts.fix_indels:
         with open(out_prefix + ".fasta", "wb") as ff:
-            for c in order:
-                seq = b"".join(bytes(results[r].bases) for r in by_contig[c])
+            for c, rs in groups:
+                seq = b"".join(bytes(results[r].bases) for r in rs)
                 ff.write(b">" + new_name(names[c]).encode() + b"\n")
                 for k in range(0, len(seq), 80):
                     ff.write(seq[k:k + 80] + b"\n")

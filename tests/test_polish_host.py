@@ -179,3 +179,34 @@ def test_vcf_header_and_duplication_record():
     dup = [l for l in out["vcf"].split(b"\n") if b"<DUP>" in l]
     assert len(dup) == 1 and b"SVTYPE=DUP" in dup[0]
     compare(ds, vcf=True, chunk=25_000, vcf_qe=True, diploid=True)
+
+
+def test_targets_are_separate_outputs():
+    """--targets makes every target its own entry of GenomeFile.regions
+    (S/GenomeFile.scala:49-54, 215-236), and the writers loop over those entries
+    (S/GenomeFile.scala:135-161): two targets on one contig give two FASTA
+    records of their fixed bases, and the second target's changes are not
+    shifted by the first one's insertion (the offset restarts per entry)."""
+    from types import SimpleNamespace
+    from pilon_gb300.reads import build_store
+    from tests.test_oracle_kat import _tile_reads, rand_ref, ref_from
+    ref = list(rand_ref(2000, seed=51))
+    if ref[308] == "A":  # locus 309 is not 'A': the insertion before 310 does not shift
+        ref[308] = "G" if ref[307] != "G" and ref[309] != "G" else "T"
+    ref = "".join(ref)
+    s1 = "ACGT"[("ACGT".index(ref[299]) + 1) % 4]
+    s2 = "ACGT"[("ACGT".index(ref[1499]) + 1) % 4]
+    recs, _ = _tile_reads(ref, snps={300: s1, 1500: s2}, ins={310: "CA"})
+    ds = SimpleNamespace(names=["chr1"], contigs=[ref_from(ref)], reads=build_store(recs))
+    opts = Options(vcf=False, targets=[(0, 200, 800), (0, 1000, 1800)])
+    with tempfile.TemporaryDirectory() as d:
+        pre = os.path.join(d, "t")
+        polish(OracleEngine(ds.names), ds.names, ds.contigs, ds.reads, _abi.default_params(), pre, opts)
+        fa = open(pre + ".fasta").read()
+        ch = open(pre + ".changes").read().splitlines()
+    t1 = ref[199:299] + s1 + ref[300:309] + "CA" + ref[309:800]
+    t2 = ref[999:1499] + s2 + ref[1500:1800]
+    wrap = lambda s: "".join(s[k:k + 80] + "\n" for k in range(0, len(s), 80))
+    assert fa == ">chr1_pilon\n" + wrap(t1) + ">chr1_pilon\n" + wrap(t2)
+    assert ch == [f"chr1:300 chr1_pilon:300 {ref[299]} {s1}", "chr1:310 chr1_pilon:310-311 . CA",
+                  f"chr1:1500 chr1_pilon:1500 {ref[1499]} {s2}"]
