@@ -144,7 +144,9 @@ def build_store(records):
         qa = np.full(L, 0xFF, np.uint8) if r.get("qual") is None else np.array(r["qual"], np.uint8)
         qo.append(q); q += L; qualb.append(qa)
         rl = sum(k for k, op in r["cigar"] if op in "MDN=X")
-        aend.append(r["pos"] + rl - 1 if rl > 0 else r["pos"])
+        # htsjdk getAlignmentEnd: 0 for an unmapped read, else start + reference
+        # length - 1 (start - 1 when no operator consumes the reference)
+        aend.append(0 if r.get("flag", 0) & 0x4 else r["pos"] + rl - 1)
     cat = lambda xs, dt: np.concatenate(xs).astype(dt) if xs else np.zeros(0, dt)
     return ReadStore(
         pos=np.array([r["pos"] for r in records], np.int32),

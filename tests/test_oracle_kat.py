@@ -1001,3 +1001,25 @@ def test_long_read_only_excludes_run_starts(snp_locus, fixed):
         assert ch == [f"chr1:{snp_locus} chr1_pilon:{snp_locus} {ref[snp_locus - 1]} {snp}"] and fa == sample
     else:
         assert ch == [] and fa == ref
+
+
+def test_placed_unmapped_read():
+    """queryOverlapping returns an unmapped read placed inside the window, and
+    htsjdk's getAlignmentEnd is 0 for it.  addRead (S/PileUpRegion.scala:102-220)
+    piles nothing (no CIGAR) but counts the read, and physCovIncr(150, 0, ...) for
+    an unpaired valid read (mapq 0 >= minMq 0) covers [min(150, 0), max) = [0, 150):
+    the start lies before the region, so physCovStart += 1 and insertSizeStart +=
+    150, and position 150 takes them back (S/PileUpRegion.scala:62-100).  So loci
+    1-149 get physical coverage 1 and insert size 150, and addInsert counts an FR
+    insert of 150 (S/BamFile.scala:137, 194-202)."""
+    ref = rand_ref(300, seed=44)
+    st = build_store([read(150, [], "ACGTACGTAC", mapq=0, flag=0x4)])
+    assert st.aend[0] == 0
+    res = oracle.process_region(st, _abi.default_params(), ref_from(ref), 0, 1, 300)
+    assert res.status == 0
+    assert res.stats.read_count == 1 and res.stats.base_count == 0
+    assert res.stats.phys_cov_start == 1 and res.stats.insert_size_start == 150
+    assert at(res, 1)["pc"] == 1 and at(res, 149)["pc"] == 1 and at(res, 150)["pc"] == 0
+    assert at(res, 1)["isz"] == 150 and at(res, 150)["isz"] == 0
+    assert (res.stats.fr_count, res.stats.fr_sum) == (1, 150) and res.stats.rf_count == 0
+    assert int(res.count.sum()) == 0
