@@ -15,6 +15,7 @@ lines.  One case per parity hazard of the hot path:
   H6 stable base order on ties                              S/BaseSum.scala:57-60
   indel call thresholds (insertions and deletions)          S/PileUp.scala:182-247
   H7 insert-size statistics per region (FR / RF), cutoff    S/BamFile.scala:161-165,192-202
+  a placed unmapped read (alignment end 0): physCov [0,pos)  S/PileUpRegion.scala:62-100
   minDepth: (0.1 * meanCoverage).round max 5                S/GenomeRegion.scala:221-224
   H9 K-mer tally read rules (length, clips, N, minQual)     S/Assembler.scala:55-87
   H10 Java "%.2f" rounding of AF                            S/Vcf.scala:134-152
