@@ -65,21 +65,51 @@ struct Bits {
     drop(n);
     return v;
   }
+  // at least n (<= 56) bits in the buffer from here on
+  void need(int n) {
+    if (cnt < n) refill();
+  }
+  // n bits that need() has already made available
+  uint32_t take_have(int n) {
+    const uint32_t v = (uint32_t)(buf & ((1ull << n) - 1));
+    drop(n);
+    return v;
+  }
   // the bits consumed past the end: those supplied there minus the ones still held
   bool overrun() const { return over > (int64_t)cnt; }
 };
 
+// The alphabets a code is built for, and the kinds of combined entries.
+enum Alphabet { kCodeLengths = 0, kLitLen = 1, kDist = 2 };
+enum Kind : uint32_t { kSlow = 0, kLiteral = 1, kLength = 2, kEnd = 3, kDistance = 4 };
+
 // A canonical Huffman code: counts and symbols in code order (for the slow
-// path) and the 10-bit table: entry = symbol | length << 16, or 0 when the
-// code is longer than 10 bits (or the bits match no code).
+// path) and two 10-bit tables.  fast[] = symbol | length << 16, or 0 when the
+// code is longer than 10 bits (or the bits match no code).  entry[] holds what
+// the symbol loop needs in one load: the value (literal byte, length or
+// distance base) << 16 | kind << 9 | code length << 5 | code length + extra
+// bits; kind kSlow sends the loop to the generic path.
 struct Huff {
   uint16_t count[kMaxBits + 1];
   uint16_t symbol[320];
   uint32_t fast[1 << kFastBits];
+  uint32_t entry[1 << kFastBits];
+
+  static uint32_t combined(int alpha, int sym, int l) {
+    uint32_t value = 0, extra = 0, kind = kSlow;
+    if (alpha == kLitLen) {
+      if (sym < 256) { value = (uint32_t)sym; kind = kLiteral; }
+      else if (sym == 256) { kind = kEnd; }
+      else if (sym < 286) { value = kLenBase[sym - 257]; extra = kLenExtra[sym - 257]; kind = kLength; }
+    } else if (alpha == kDist && sym < 30) {
+      value = kDistBase[sym]; extra = kDistExtra[sym]; kind = kDistance;
+    }
+    return value << 16 | kind << 9 | (uint32_t)l << 5 | ((uint32_t)l + extra);
+  }
 
   // false for an over-subscribed set of lengths; incomplete codes (allowed
   // for a single distance code) decode as long as no missing code is met
-  bool build(const uint8_t* len, int n) {
+  bool build(const uint8_t* len, int n, int alpha = kCodeLengths) {
     std::memset(count, 0, sizeof count);
     for (int s = 0; s < n; s++) count[len[s]]++;
     count[0] = 0;
@@ -95,6 +125,7 @@ struct Huff {
     for (int s = 0; s < n; s++)
       if (len[s]) symbol[offs[len[s]]++] = (uint16_t)s;
     std::memset(fast, 0, sizeof fast);
+    std::memset(entry, 0, sizeof entry);  // kSlow
     // canonical codes in order of length, then symbol
     uint32_t code = 0;
     int idx = 0;
@@ -103,7 +134,11 @@ struct Huff {
         if (l > kFastBits) continue;
         uint32_t rev = 0;  // the stream holds the code's bits from its top bit down
         for (int b = 0; b < l; b++) rev |= ((code >> b) & 1u) << (l - 1 - b);
-        for (uint32_t f = rev; f < (1u << kFastBits); f += 1u << l) fast[f] = symbol[idx] | ((uint32_t)l << 16);
+        const uint32_t fe = symbol[idx] | ((uint32_t)l << 16), ce = combined(alpha, symbol[idx], l);
+        for (uint32_t f = rev; f < (1u << kFastBits); f += 1u << l) {
+          fast[f] = fe;
+          entry[f] = ce;
+        }
       }
       code <<= 1;
     }
@@ -111,8 +146,10 @@ struct Huff {
   }
 
   // next symbol, or -1 when the bits match no code
-  int decode(Bits& in) const {
-    const uint32_t v = in.peek(kMaxBits);
+  int decode(Bits& in) const { return decode_bits(in, in.peek(kMaxBits)); }
+  // the same when the caller has made 15 bits available
+  int decode_have(Bits& in) const { return decode_bits(in, (uint32_t)in.buf & ((1u << kMaxBits) - 1)); }
+  int decode_bits(Bits& in, uint32_t v) const {
     const uint32_t e = fast[v & ((1u << kFastBits) - 1)];
     if (e) {
       in.drop((int)(e >> 16));
@@ -166,39 +203,139 @@ struct Decoder {
         for (int s = 144; s < 256; s++) l[s] = 9;
         for (int s = 256; s < 280; s++) l[s] = 7;
         for (int s = 280; s < 288; s++) l[s] = 8;
-        lit.build(l, 288);
+        lit.build(l, 288, kLitLen);
         for (int s = 0; s < 30; s++) l[s] = 5;
-        dist.build(l, 30);
+        dist.build(l, 30, kDist);
       } else if (!read_tables(in)) {
         return -1;
       }
-      while (true) {
-        const int sym = lit.decode(in);
-        if (sym < 0) return -1;
-        if (sym < 256) {
-          if (o >= cap) return -1;
-          dst[o++] = (uint8_t)sym;
-        } else if (sym == 256) {
-          break;
+      // Symbols until end of block, from the combined entries: a literal, a
+      // length or a distance with its extra bits in one load and one shift.
+      // One refill gives the bits of two literals and a length (10 + 10 + 20
+      // <= 48); the distance (15 + 13) refills if needed.  Codes longer than
+      // the table take the generic path.  Bits read past the end of the input
+      // are zeros; every pass emits output (bounded by cap), ends the block
+      // or fails, so the overrun is checked per block.
+      constexpr uint32_t kMask = (1u << kFastBits) - 1;
+      // the bit reader's state in locals (registers) for the loop; it is
+      // written back around the generic path and at the end of the block
+      uint64_t bb = in.buf;
+      int bc = in.cnt;
+      const uint8_t* ip = in.p;
+      int64_t over = in.over;
+      const uint8_t* const iend = in.end;
+      auto need = [&](int nb) {
+        if (bc >= nb) return;
+        if (iend - ip >= 8) {
+          uint64_t w;
+          std::memcpy(&w, ip, 8);
+          bb |= w << bc;
+          ip += (63 - bc) >> 3;
+          bc |= 56;
         } else {
-          const int li = sym - 257;
+          while (bc <= 56) {
+            if (ip < iend) bb |= (uint64_t)*ip++ << bc;
+            else over += 8;
+            bc += 8;
+          }
+        }
+      };
+      auto drop = [&](int nb) {
+        bb >>= nb;
+        bc -= nb;
+      };
+      auto store = [&]() {
+        in.buf = bb;
+        in.cnt = bc;
+        in.p = ip;
+        in.over = over;
+      };
+      auto load = [&]() {
+        bb = in.buf;
+        bc = in.cnt;
+        ip = in.p;
+        over = in.over;
+      };
+      while (true) {
+        need(48);
+        uint32_t e = lit.entry[bb & kMask];
+        if ((e >> 9 & 7) == kLiteral) {
+          drop((int)(e & 31));
+          if (o >= cap) return -1;
+          dst[o++] = (uint8_t)(e >> 16);
+          e = lit.entry[bb & kMask];
+          if ((e >> 9 & 7) == kLiteral) {
+            drop((int)(e & 31));
+            if (o >= cap) return -1;
+            dst[o++] = (uint8_t)(e >> 16);
+            continue;
+          }
+        }
+        int64_t len;
+        const uint32_t kind = e >> 9 & 7;
+        if (kind == kLength) {
+          const uint32_t cl = e >> 5 & 15, tot = e & 31;
+          len = (int64_t)(e >> 16) + (int64_t)((bb >> cl) & ((1ull << (tot - cl)) - 1));
+          drop((int)tot);
+        } else if (kind == kEnd) {
+          drop((int)(e & 31));
+          break;
+        } else {  // a code longer than the table, or no code: >= 38 bits remain
+          store();
+          const int sym = lit.decode_have(in);
+          int li = -1;
+          if (sym >= 257) {
+            li = sym - 257;
+            if (li < 29) len = kLenBase[li] + in.take_have(kLenExtra[li]);
+          }
+          load();
+          if (sym < 0) return -1;
+          if (sym < 256) {
+            if (o >= cap) return -1;
+            dst[o++] = (uint8_t)sym;
+            continue;
+          }
+          if (sym == 256) break;
           if (li >= 29) return -1;
-          const int64_t len = kLenBase[li] + in.take(kLenExtra[li]);
-          const int ds = dist.decode(in);
-          if (ds < 0 || ds >= 30) return -1;
-          const int64_t d = kDistBase[ds] + in.take(kDistExtra[ds]);
+        }
+        {
+          need(28);
+          const uint32_t de = dist.entry[bb & kMask];
+          int64_t d;
+          if ((de >> 9 & 7) == kDistance) {
+            const uint32_t cl = de >> 5 & 15, tot = de & 31;
+            d = (int64_t)(de >> 16) + (int64_t)((bb >> cl) & ((1ull << (tot - cl)) - 1));
+            drop((int)tot);
+          } else {
+            store();
+            const int ds = dist.decode_have(in);
+            d = (ds >= 0 && ds < 30) ? kDistBase[ds] + in.take_have(kDistExtra[ds]) : -1;
+            load();
+            if (d < 0) return -1;
+          }
           if (d > o || len > cap - o) return -1;
           uint8_t* w = dst + o;
           const uint8_t* r = w - d;
-          if (d >= len) {
+          if (d >= 8 && cap - o >= len + 8) {
+            // 8 bytes at a time: each source word lies at least 8 bytes behind its
+            // destination, so overlapping matches repeat their pattern correctly;
+            // the last word may write up to 7 bytes past the match, inside dst
+            for (int64_t k = 0; k < len; k += 8) {
+              uint64_t v;
+              std::memcpy(&v, r + k, 8);
+              std::memcpy(w + k, &v, 8);
+            }
+          } else if (d == 1) {
+            std::memset(w, *r, (size_t)len);
+          } else if (d >= len) {
             std::memcpy(w, r, (size_t)len);
           } else {
             for (int64_t k = 0; k < len; k++) w[k] = r[k];  // overlapping copy repeats the pattern
           }
           o += len;
         }
-        if (in.overrun()) return -1;
       }
+      store();
       if (in.overrun()) return -1;
     }
     return o;
@@ -235,7 +372,7 @@ struct Decoder {
       while (rep--) lens[k++] = v;
     }
     if (in.overrun() || lens[256] == 0) return false;  // no end-of-block code
-    return lit.build(lens, hlit) && dist.build(lens + hlit, hdist);
+    return lit.build(lens, hlit, kLitLen) && dist.build(lens + hlit, hdist, kDist);
   }
 };
 
