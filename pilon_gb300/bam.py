@@ -32,16 +32,14 @@ def _lib():
             build()
         L = C.CDLL(BAMLIB)
         vp, i64 = C.c_void_p, C.c_int64
-        L.bam_count.restype = i64
-        L.bam_count.argtypes = [vp, i64, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]
-        L.bam_parse.restype = i64
-        L.bam_parse.argtypes = [vp, i64] + [vp] * 15
+        L.bam_index.restype = i64
+        L.bam_index.argtypes = [vp, i64, vp, i64, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]
+        L.bam_fill.restype = i64
+        L.bam_fill.argtypes = [vp, vp, i64] + [vp] * 15 + [C.c_int32]
         L.bam_encoded_size.restype = i64
         L.bam_encoded_size.argtypes = [i64, vp, vp]
         L.bam_encode.restype = i64
         L.bam_encode.argtypes = [i64] + [vp] * 16
-        L.bam_parse_threads.restype = i64
-        L.bam_parse_threads.argtypes = [vp, i64] + [vp] * 15 + [C.c_int32]
         L.bgzf_inflate_blocks.restype = i64
         L.bgzf_inflate_blocks.argtypes = [vp, i64, vp, vp, vp, vp, vp, C.c_int32]
         _LIB = L
@@ -180,7 +178,11 @@ def read_bam(path, threads=None):
     L = _lib()
     recs = data[off:]
     nc, sb, qb = C.c_int64(), C.c_int64(), C.c_int64()
-    n = L.bam_count(recs.ctypes.data, recs.size, C.byref(nc), C.byref(sb), C.byref(qb))
+    # one walk of the record chain; a record takes at least 36 bytes, and the
+    # pages of the unused tail of `starts` are never touched
+    starts = np.empty(recs.size // 36 + 1, np.int64)
+    n = L.bam_index(recs.ctypes.data, recs.size, starts.ctypes.data, starts.size, C.byref(nc), C.byref(sb),
+                    C.byref(qb))
     if n < 0:
         raise ValueError(f"BAM record at stream byte {off - 1 - n} runs past the end of the file")
     st = ReadStore(pos=np.empty(n, np.int32), aend=np.empty(n, np.int32), flag=np.empty(n, np.uint16),
@@ -189,9 +191,9 @@ def read_bam(path, threads=None):
                    n_cigar=np.empty(n, np.uint16), cigar=np.empty(nc.value, np.uint32),
                    seq_off=np.empty(n, np.int64), l_seq=np.empty(n, np.int32), seq=np.empty(sb.value, np.uint8),
                    qual_off=np.empty(n, np.int64), qual=np.empty(qb.value, np.uint8))
-    L.bam_parse_threads(recs.ctypes.data, recs.size, st.pos.ctypes.data, st.aend.ctypes.data, st.tlen.ctypes.data,
-                        st.ref_id.ctypes.data, st.mate_ref_id.ctypes.data, st.l_seq.ctypes.data, st.flag.ctypes.data,
-                        st.n_cigar.ctypes.data, st.mapq.ctypes.data, st.seq.ctypes.data, st.qual.ctypes.data,
-                        st.cigar_off.ctypes.data, st.seq_off.ctypes.data, st.qual_off.ctypes.data, st.cigar.ctypes.data,
-                        _threads(threads))
+    L.bam_fill(recs.ctypes.data, starts.ctypes.data, n, st.pos.ctypes.data, st.aend.ctypes.data, st.tlen.ctypes.data,
+               st.ref_id.ctypes.data, st.mate_ref_id.ctypes.data, st.l_seq.ctypes.data, st.flag.ctypes.data,
+               st.n_cigar.ctypes.data, st.mapq.ctypes.data, st.seq.ctypes.data, st.qual.ctypes.data,
+               st.cigar_off.ctypes.data, st.seq_off.ctypes.data, st.qual_off.ctypes.data, st.cigar.ctypes.data,
+               _threads(threads))
     return names, lengths, st

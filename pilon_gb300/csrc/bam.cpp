@@ -12,6 +12,7 @@
 // The store keeps BAM's CIGAR words, nibbles and qualities unchanged; pos is
 // 1-based (htsjdk getAlignmentStart) and aend is htsjdk getAlignmentEnd: the
 // start plus the reference length of the CIGAR minus one, 0 for an unmapped read.
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -50,10 +51,13 @@ inline uint16_t reg2bin(int32_t beg, int32_t end) {
 
 extern "C" {
 
-// Counts the records of a decompressed record stream and the sizes of the
-// store's variable arrays.  Returns the record count, or -1 - offset of a
-// record that runs past the end of the stream.
-int64_t bam_count(const uint8_t* buf, int64_t n, int64_t* n_cigar, int64_t* seq_bytes, int64_t* qual_bytes) {
+// One walk of the record chain of a decompressed record stream: checks that
+// every record fits its block_size and the stream, writes each record's offset
+// to starts (cap entries; a record takes at least 36 bytes, so n / 36 + 1
+// always suffice) and the sizes of the store's variable arrays.  Returns the
+// record count, or -1 - offset of the first record that does not fit.
+int64_t bam_index(const uint8_t* buf, int64_t n, int64_t* starts, int64_t cap, int64_t* n_cigar, int64_t* seq_bytes,
+                  int64_t* qual_bytes) {
   int64_t off = 0, recs = 0, nc = 0, sb = 0, qb = 0;
   while (off + 4 <= n) {
     const int32_t bs = rd32(buf + off);
@@ -63,10 +67,11 @@ int64_t bam_count(const uint8_t* buf, int64_t n, int64_t* n_cigar, int64_t* seq_
     const uint32_t l_name = r[8], n_cig = rd16(r + 12);
     if (l_seq < 0 || 32 + (int64_t)l_name + 4 * (int64_t)n_cig + ((int64_t)l_seq + 1) / 2 + l_seq > bs)
       return -1 - off;
+    if (recs >= cap) return -1 - off;
+    starts[recs++] = off;
     nc += n_cig;
     sb += ((int64_t)l_seq + 1) / 2;
     qb += l_seq;
-    recs++;
     off += 4 + bs;
   }
   if (off != n) return -1 - off;
@@ -76,46 +81,57 @@ int64_t bam_count(const uint8_t* buf, int64_t n, int64_t* n_cigar, int64_t* seq_
   return recs;
 }
 
-// Fills the store from a stream that bam_count accepted (arrays sized by it):
-// one pass over the record headers fixes every record's start and the offsets
-// of its CIGAR, bases and qualities, then `threads` threads fill contiguous
-// ranges of records.  Returns the record count.
-int64_t bam_parse_threads(const uint8_t* buf, int64_t n, int32_t* pos, int32_t* aend, int32_t* tlen,
-                          int32_t* ref_id, int32_t* mate_ref_id, int32_t* l_seq_out, uint16_t* flag,
-                          uint16_t* n_cigar, uint8_t* mapq, uint8_t* seq, uint8_t* qual, int64_t* cigar_off,
-                          int64_t* seq_off, int64_t* qual_off, uint32_t* cigar, int32_t threads) {
-  std::vector<int64_t> start;
-  int64_t off = 0, co = 0, so = 0, qo = 0;
-  while (off + 4 <= n) {
-    const int32_t bs = rd32(buf + off);
-    const uint8_t* r = buf + off + 4;
-    const int64_t i = (int64_t)start.size();
-    const int32_t ls = rd32(r + 16);
-    start.push_back(off);
-    cigar_off[i] = co;
-    seq_off[i] = so;
-    qual_off[i] = qo;
-    co += rd16(r + 12);
-    so += (ls + 1) / 2;
-    qo += ls;
-    off += 4 + bs;
+// Fills the store (arrays sized by bam_index) from the records at starts, on
+// `threads` threads over contiguous ranges of records: each thread first sums
+// its records' CIGAR words, base bytes and qualities, and after a prefix over
+// the threads fills its range from its own offsets.  Returns the record count.
+int64_t bam_fill(const uint8_t* buf, const int64_t* starts, int64_t recs, int32_t* pos, int32_t* aend, int32_t* tlen,
+                 int32_t* ref_id, int32_t* mate_ref_id, int32_t* l_seq_out, uint16_t* flag, uint16_t* n_cigar,
+                 uint8_t* mapq, uint8_t* seq, uint8_t* qual, int64_t* cigar_off, int64_t* seq_off, int64_t* qual_off,
+                 uint32_t* cigar, int32_t threads) {
+  const int64_t nt = std::max<int64_t>(1, std::min<int64_t>(threads < 1 ? 1 : threads, recs));
+  std::vector<int64_t> tc(nt + 1, 0), ts(nt + 1, 0), tq(nt + 1, 0);
+  auto lo = [&](int64_t t) { return recs * t / nt; };
+  auto run = [&](auto&& body) {
+    std::vector<std::thread> pool;
+    for (int64_t t = 1; t < nt; t++) pool.emplace_back(body, t);
+    body(0);
+    for (auto& th : pool) th.join();
+  };
+  run([&](int64_t t) {
+    int64_t c = 0, sb = 0, qb = 0;
+    for (int64_t i = lo(t); i < lo(t + 1); i++) {
+      const uint8_t* r = buf + starts[i] + 4;
+      const int32_t ls = rd32(r + 16);
+      c += rd16(r + 12);
+      sb += ((int64_t)ls + 1) / 2;
+      qb += ls;
+    }
+    tc[t + 1] = c;
+    ts[t + 1] = sb;
+    tq[t + 1] = qb;
+  });
+  for (int64_t t = 0; t < nt; t++) {
+    tc[t + 1] += tc[t];
+    ts[t + 1] += ts[t];
+    tq[t + 1] += tq[t];
   }
-  const int64_t recs = (int64_t)start.size();
-  auto fill = [&](int64_t a, int64_t b) {
-    for (int64_t i = a; i < b; i++) {
-      const uint8_t* r = buf + start[i] + 4;
+  run([&](int64_t t) {
+    int64_t co = tc[t], so = ts[t], qo = tq[t];
+    for (int64_t i = lo(t); i < lo(t + 1); i++) {
+      const uint8_t* r = buf + starts[i] + 4;
       const int32_t rid = rd32(r), p0 = rd32(r + 4);
       const uint32_t l_name = r[8];
       const uint16_t nc = rd16(r + 12), fl = rd16(r + 14);
       const int32_t ls = rd32(r + 16);
       const uint8_t* cg = r + 32 + l_name;
       const uint8_t* sq = cg + 4 * (int64_t)nc;
-      const uint8_t* ql = sq + (ls + 1) / 2;
+      const uint8_t* ql = sq + ((int64_t)ls + 1) / 2;
       int64_t reflen = 0;
       for (uint32_t k = 0; k < nc; k++) {
         uint32_t w;
         std::memcpy(&w, cg + 4 * k, 4);
-        cigar[cigar_off[i] + k] = w;
+        cigar[co + k] = w;
         if (consumes_ref(w & 15u)) reflen += w >> 4;
       }
       pos[i] = (int32_t)((uint32_t)p0 + 1u);  // Java int arithmetic: wraps
@@ -127,63 +143,17 @@ int64_t bam_parse_threads(const uint8_t* buf, int64_t n, int32_t* pos, int32_t* 
       flag[i] = fl;
       n_cigar[i] = nc;
       mapq[i] = r[9];
-      std::memcpy(seq + seq_off[i], sq, (size_t)(ls + 1) / 2);
-      std::memcpy(qual + qual_off[i], ql, (size_t)ls);
+      cigar_off[i] = co;
+      seq_off[i] = so;
+      qual_off[i] = qo;
+      std::memcpy(seq + so, sq, (size_t)(((int64_t)ls + 1) / 2));
+      std::memcpy(qual + qo, ql, (size_t)ls);
+      co += nc;
+      so += ((int64_t)ls + 1) / 2;
+      qo += ls;
     }
-  };
-  const int64_t nt = threads < 1 ? 1 : threads;
-  std::vector<std::thread> pool;
-  for (int64_t t = 1; t < nt; t++) pool.emplace_back(fill, recs * t / nt, recs * (t + 1) / nt);
-  fill(0, recs / nt);
-  for (auto& th : pool) th.join();
+  });
   return recs;
-}
-
-// Fills the store from the stream (arrays sized by bam_count), on one thread.
-// Returns the record count.
-int64_t bam_parse(const uint8_t* buf, int64_t n, int32_t* pos, int32_t* aend, int32_t* tlen, int32_t* ref_id,
-                  int32_t* mate_ref_id, int32_t* l_seq_out, uint16_t* flag, uint16_t* n_cigar, uint8_t* mapq,
-                  uint8_t* seq, uint8_t* qual, int64_t* cigar_off, int64_t* seq_off, int64_t* qual_off,
-                  uint32_t* cigar) {
-  int64_t off = 0, i = 0, co = 0, so = 0, qo = 0;
-  while (off + 4 <= n) {
-    const int32_t bs = rd32(buf + off);
-    const uint8_t* r = buf + off + 4;
-    const int32_t rid = rd32(r), p0 = rd32(r + 4);
-    const uint32_t l_name = r[8];
-    const uint16_t nc = rd16(r + 12), fl = rd16(r + 14);
-    const int32_t ls = rd32(r + 16);
-    const uint8_t* cg = r + 32 + l_name;
-    const uint8_t* sq = cg + 4 * (int64_t)nc;
-    const uint8_t* ql = sq + (ls + 1) / 2;
-    int64_t reflen = 0;
-    for (uint32_t k = 0; k < nc; k++) {
-      uint32_t w;
-      std::memcpy(&w, cg + 4 * k, 4);
-      cigar[co + k] = w;
-      if (consumes_ref(w & 15u)) reflen += w >> 4;
-    }
-    pos[i] = (int32_t)((uint32_t)p0 + 1u);  // Java int arithmetic: wraps
-    aend[i] = (fl & 0x4) ? 0 : (int32_t)(p0 + reflen);  // (p0 + 1) + reflen - 1
-    tlen[i] = rd32(r + 28);
-    ref_id[i] = rid;
-    mate_ref_id[i] = rd32(r + 20);
-    l_seq_out[i] = ls;
-    flag[i] = fl;
-    n_cigar[i] = nc;
-    mapq[i] = r[9];
-    cigar_off[i] = co;
-    seq_off[i] = so;
-    qual_off[i] = qo;
-    std::memcpy(seq + so, sq, (size_t)(ls + 1) / 2);
-    std::memcpy(qual + qo, ql, (size_t)ls);
-    co += nc;
-    so += (ls + 1) / 2;
-    qo += ls;
-    off += 4 + bs;
-    i++;
-  }
-  return i;
 }
 
 // Bytes of the BAM records of reads [0, n) (read names "r<index>").

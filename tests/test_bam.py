@@ -118,7 +118,7 @@ def test_damaged_headers_and_blocks_are_value_errors(cfg1):
 
 
 def test_record_length_fields_are_checked(cfg1):
-    """bam_count rejects a record whose l_seq, read-name length or CIGAR count
+    """bam_index rejects a record whose l_seq, read-name length or CIGAR count
     does not fit its block_size (l_seq = 2^31 - 1 included); a position of
     2^31 - 1 reads back as htsjdk's wrapped Java int."""
     good = _payload(cfg1)
