@@ -40,6 +40,8 @@ def _lib():
         L.bam_encoded_size.argtypes = [i64, vp, vp]
         L.bam_encode.restype = i64
         L.bam_encode.argtypes = [i64] + [vp] * 16
+        L.bgzf_scan.restype = i64
+        L.bgzf_scan.argtypes = [vp, i64, vp, vp, vp, i64, C.POINTER(i64), C.POINTER(C.c_int32)]
         L.bgzf_inflate_blocks.restype = i64
         L.bgzf_inflate_blocks.argtypes = [vp, i64, vp, vp, vp, vp, vp, C.c_int32]
         _LIB = L
@@ -85,46 +87,49 @@ def write_bam(path, names, lengths, reads, threads=None):
         f.write(BGZF_EOF)
 
 
+_SCAN_ERRORS = {1: "is not a BGZF block", 2: "is truncated", 3: "has no BC field",
+                4: "claims more than 65536 uncompressed bytes", 5: "exceeds the block count bound"}
+
+
+def _block_table(raw):
+    """(cdata offsets, cdata ends, uncompressed sizes) of every BGZF block, as
+    int64 arrays, from the native scan of the gzip member headers."""
+    n = len(raw)
+    inp = np.frombuffer(raw, np.uint8) if n else np.zeros(1, np.uint8)
+    cap = n // 28 + 1
+    src, end, size = (np.empty(cap, np.int64) for _ in range(3))
+    err_off, err_kind = C.c_int64(), C.c_int32()
+    k = _lib().bgzf_scan(inp.ctypes.data, n, src.ctypes.data, end.ctypes.data, size.ctypes.data, cap,
+                         C.byref(err_off), C.byref(err_kind))
+    del inp  # a view of a mapped file must not outlive this call (the caller closes the map)
+    if k < 0:
+        raise ValueError(f"BGZF block at byte {err_off.value} {_SCAN_ERRORS.get(err_kind.value, 'is damaged')}")
+    return src[:k], end[:k], size[:k]
+
+
 def _blocks(raw):
     """(cdata offset, cdata end, uncompressed size) of every BGZF block."""
-    out, off, n = [], 0, len(raw)
-    while off < n:
-        if off + 18 > n or raw[off] != 0x1F or raw[off + 1] != 0x8B or raw[off + 3] & 4 == 0:
-            raise ValueError(f"not a BGZF block at byte {off}")
-        xlen = struct.unpack_from("<H", raw, off + 10)[0]
-        x, bsize = off + 12, None
-        if off + 12 + xlen > n:
-            raise ValueError(f"BGZF block at byte {off} is truncated")
-        while x + 4 <= off + 12 + xlen:
-            si1, si2, slen = raw[x], raw[x + 1], struct.unpack_from("<H", raw, x + 2)[0]
-            if si1 == 66 and si2 == 67 and slen == 2 and x + 6 <= off + 12 + xlen:
-                bsize = struct.unpack_from("<H", raw, x + 4)[0]
-            x += 4 + slen
-        if bsize is None:
-            raise ValueError(f"BGZF block at byte {off} has no BC field")
-        end = off + bsize + 1
-        if end > n or end - 8 < off + 12 + xlen:
-            raise ValueError(f"BGZF block at byte {off} is truncated")
-        isize = struct.unpack_from("<I", raw, end - 4)[0]
-        if isize > 65536:  # a BGZF block holds at most 64 KiB of data
-            raise ValueError(f"BGZF block at byte {off} claims {isize} uncompressed bytes")
-        out.append((off + 12 + xlen, end - 8, isize))
-        off = end
-    return out
+    return [tuple(int(x) for x in t) for t in zip(*_block_table(raw))]
 
 
 def inflate_blocks(raw, blocks, threads=None):
     """The uncompressed bytes of the BGZF blocks (cdata start, cdata end,
-    uncompressed size) of `raw`, one after another."""
-    n = len(blocks)
-    src = np.array([b[0] for b in blocks], np.int64).reshape(n)
-    end = np.array([b[1] for b in blocks], np.int64).reshape(n)
-    sizes = np.array([b[2] for b in blocks], np.int64).reshape(n)
+    uncompressed size) of `raw`, one after another; `blocks` is a list of such
+    triples or the three arrays of _block_table."""
+    if isinstance(blocks, tuple) and len(blocks) == 3 and isinstance(blocks[0], np.ndarray):
+        src, end, sizes = (np.ascontiguousarray(b, np.int64) for b in blocks)
+        n = src.size
+    else:
+        n = len(blocks)
+        src = np.array([b[0] for b in blocks], np.int64).reshape(n)
+        end = np.array([b[1] for b in blocks], np.int64).reshape(n)
+        sizes = np.array([b[2] for b in blocks], np.int64).reshape(n)
     starts = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
     data = np.empty(max(int(starts[-1]), 1), np.uint8)
     inp = np.frombuffer(raw, np.uint8) if len(raw) else np.zeros(1, np.uint8)
     rc = _lib().bgzf_inflate_blocks(inp.ctypes.data, n, src.ctypes.data, end.ctypes.data, starts.ctypes.data,
                                     sizes.ctypes.data, data.ctypes.data, _threads(threads))
+    del inp  # no view of a mapped file may outlive this call
     if rc < 0:
         raise ValueError(f"BGZF block {-rc - 1}: damaged DEFLATE data or wrong uncompressed size")
     return data[:int(starts[-1])]
@@ -166,8 +171,7 @@ def read_bam(path, threads=None):
         # mapped, so that reading the file overlaps the threads' inflating
         raw = mmap.mmap(f.fileno(), 0, access=mmap.ACCESS_READ) if os.fstat(f.fileno()).st_size else b""
     try:
-        blocks = _blocks(raw)
-        data = inflate_blocks(raw, blocks, threads)
+        data = inflate_blocks(raw, _block_table(raw), threads)
     finally:
         if isinstance(raw, mmap.mmap):
             raw.close()

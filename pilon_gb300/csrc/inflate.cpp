@@ -380,6 +380,48 @@ struct Decoder {
 
 extern "C" {
 
+// The BGZF blocks of a file (SAM/BAM specification 4.1): gzip members with
+// FEXTRA and a BC subfield holding the block size.  Writes each block's
+// compressed data [src_off, src_end) and its uncompressed size (at most
+// 64 KiB); cap entries suffice when cap >= n / 28 + 1, a block taking at least
+// 28 bytes.  Returns the block count, or -1 with *err_off the block's offset
+// and *err_kind 1 (not a BGZF block), 2 (truncated), 3 (no BC subfield),
+// 4 (more than 64 KiB uncompressed) or 5 (more blocks than cap).
+int64_t bgzf_scan(const uint8_t* raw, int64_t n, int64_t* src_off, int64_t* src_end, int64_t* out_size, int64_t cap,
+                  int64_t* err_off, int32_t* err_kind) {
+  int64_t off = 0, k = 0;
+  auto fail = [&](int32_t kind) {
+    *err_off = off;
+    *err_kind = kind;
+    return (int64_t)-1;
+  };
+  while (off < n) {
+    if (off + 18 > n || raw[off] != 0x1F || raw[off + 1] != 0x8B || (raw[off + 3] & 4) == 0) return fail(1);
+    const int64_t xlen = raw[off + 10] | (int64_t)raw[off + 11] << 8;
+    if (off + 12 + xlen > n) return fail(2);
+    int64_t x = off + 12, bsize = -1;
+    while (x + 4 <= off + 12 + xlen) {
+      const int64_t slen = raw[x + 2] | (int64_t)raw[x + 3] << 8;
+      if (raw[x] == 66 && raw[x + 1] == 67 && slen == 2 && x + 6 <= off + 12 + xlen)
+        bsize = raw[x + 4] | (int64_t)raw[x + 5] << 8;
+      x += 4 + slen;
+    }
+    if (bsize < 0) return fail(3);
+    const int64_t end = off + bsize + 1;
+    if (end > n || end - 8 < off + 12 + xlen) return fail(2);
+    const int64_t isize = raw[end - 4] | (int64_t)raw[end - 3] << 8 | (int64_t)raw[end - 2] << 16 |
+                          (int64_t)raw[end - 1] << 24;
+    if (isize > 65536) return fail(4);
+    if (k >= cap) return fail(5);
+    src_off[k] = off + 12 + xlen;
+    src_end[k] = end - 8;
+    out_size[k] = isize;
+    k++;
+    off = end;
+  }
+  return k;
+}
+
 // Inflates n_blocks raw DEFLATE streams: block k is in[src_off[k], src_end[k])
 // of `in` and must produce exactly out_size[k] bytes at out + out_off[k].
 // Returns 0, or -(k + 1) for the first damaged block found.
