@@ -37,6 +37,7 @@ class Options:
     nanopore: bool = False
     chunk_size: int = 10_000_000
     targets: list = None            # [(contig, start, stop)] or None
+    contig_order: list = None       # contig indices to process and write, in order (FASTA order); None = all
     vcf_date: str = "20260101"
     vcf_source: str = "Pilon version [COMMIT] [DATE]"
     vcf_args: str = ""
@@ -299,7 +300,7 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
     opts = opts or Options()
     opts.longread_only = bool(opts.longread) and bool(getattr(opts, "no_frags", False))
     lens = [int(c.size) for c in contigs]
-    regions = plan_regions(reads, lens, opts.chunk_size, opts.targets)
+    regions = plan_regions(reads, lens, opts.chunk_size, opts.targets, opts.contig_order)
     engine.set_reference(contigs)
     engine.set_reads(reads)
     engine.pileup_regions(regions, params, batched=batched)

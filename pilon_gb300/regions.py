@@ -78,8 +78,10 @@ class ReadIndex:
         return a, b
 
 
-def plan_regions(reads, contig_lens, chunk_size=10_000_000, targets=None):
-    """[(contig, start, stop, read_begin, read_end)] in processing order."""
+def plan_regions(reads, contig_lens, chunk_size=10_000_000, targets=None, order=None):
+    """[(contig, start, stop, read_begin, read_end)] in processing order: the
+    targets, or the chunks of every contig in `order` (contig indices; all of
+    them in index order by default)."""
     idx = ReadIndex(reads, len(contig_lens))
     regs = []
     if targets is not None:
@@ -87,7 +89,8 @@ def plan_regions(reads, contig_lens, chunk_size=10_000_000, targets=None):
             a, b = idx.range_for(ci, s, e, contig_lens[ci])
             regs.append((ci, s, e, a, b))
         return regs
-    for ci, ln in enumerate(contig_lens):
+    for ci in (range(len(contig_lens)) if order is None else order):
+        ln = contig_lens[ci]
         for s, e in contig_regions(int(ln), chunk_size):
             a, b = idx.range_for(ci, s, e, int(ln))
             regs.append((ci, s, e, a, b))

@@ -21,6 +21,7 @@ lines.  One case per parity hazard of the hot path:
   H10 Java "%.2f" rounding of AF                            S/Vcf.scala:134-152
   AMB fixes: base, IUPAC code, --fix amb, long reads        S/GenomeRegion.scala:265-269,331-340
   changes lines and FASTA after indel fixes, across chunks  S/GenomeRegion.scala:595-657, S/GenomeFile.scala:140-160
+  soft-masked (lowercase) reference: raw in indel shifts     S/PileUpRegion.scala:156, S/GenomeRegion.scala:783-787
   VCF records: REF/ALT/GT, filters, BQ/MQ/QD/QP/AF fields  S/Vcf.scala:74-176, S/PileUp.scala:55-71
   H12 output names, FASTA wrapping, changes format          S/GenomeFile.scala:79-82,135-161
 """
@@ -1024,3 +1025,31 @@ def test_placed_unmapped_read():
     assert at(res, 1)["isz"] == 150 and at(res, 150)["isz"] == 0
     assert (res.stats.fr_count, res.stats.fr_sum) == (1, 150) and res.stats.rf_count == 0
     assert int(res.count.sum()) == 0
+
+
+@pytest.mark.parametrize("base,shifted", [("A", True), ("a", False)])
+def test_soft_masked_reference_compares_raw(base, shifted):
+    """Soft-masked (lowercase) reference bytes: the insertion left shift
+    compares them raw with the read's bases (S/PileUpRegion.scala:156), so
+    "CA" inserted before 51 shifts to 50 after an 'A' at 50 but not after an 'a';
+    reference bases elsewhere are upper-cased (refBase, S/GenomeRegion.scala:783-787),
+    and the polished FASTA keeps the file's case where nothing is fixed."""
+    ref = list(rand_ref(100, seed=3))
+    ref[48] = "G" if ref[47] != "G" else "T"   # locus 49 stops a shift past 50
+    ref[49] = base
+    ref = "".join(ref)
+    seqref = ref.upper()
+    recs = [read(31, [(20, "M"), (2, "I"), (20, "M")], seqref[30:50] + "CA" + seqref[50:70]) for _ in range(8)]
+    recs += [read(31, [(40, "M")], seqref[30:70]) for _ in range(2)]
+    res = run(ref, recs)
+    assert res.status == 0
+    at_locus = 50 if shifted else 51
+    assert at(res, at_locus)["ins"] == 8 and at(res, 101 - at_locus)["ins"] == 0
+    if not shifted:
+        low = ref.lower()
+        st = build_store(recs)
+        with tempfile.TemporaryDirectory() as d:
+            pre = os.path.join(d, "o")
+            assert oracle.polish(st, _abi.default_params(), ["chr1"], [ref_from(low)], pre) == 0
+            fa = "".join(open(pre + ".fasta").read().splitlines()[1:])
+        assert fa == low[:50] + "CA" + low[50:]  # the homozygous insertion is fixed; the rest keeps its case

@@ -210,3 +210,43 @@ def test_targets_are_separate_outputs():
     assert fa == ">chr1_pilon\n" + wrap(t1) + ">chr1_pilon\n" + wrap(t2)
     assert ch == [f"chr1:300 chr1_pilon:300 {ref[299]} {s1}", "chr1:310 chr1_pilon:310-311 . CA",
                   f"chr1:1500 chr1_pilon:1500 {ref[1499]} {s2}"]
+
+
+def test_contig_order_is_the_output_order():
+    """Options.contig_order (the FASTA's order, pilon_gb300.fasta.reference_for_bam)
+    sets the order contigs are processed and written in, as GenomeFile.regions
+    follows the FASTA (S/GenomeFile.scala:49-54): reversing it reverses the FASTA
+    records and the contigs' blocks of changes lines."""
+    ds = synth.generate(3, scale=0.01)
+    n = len(ds.contigs)
+    outs = []
+    for order in (None, list(range(n))[::-1]):
+        with tempfile.TemporaryDirectory() as d:
+            pre = os.path.join(d, "o")
+            polish(OracleEngine(ds.names), ds.names, ds.contigs, ds.reads, _abi.default_params(), pre,
+                   Options(vcf=False, contig_order=order))
+            fa = open(pre + ".fasta").read().split(">")[1:]
+            ch = open(pre + ".changes").read().splitlines()
+        outs.append((fa, ch))
+    (fa0, ch0), (fa1, ch1) = outs
+    assert len(fa0) == n and fa1 == fa0[::-1]
+    by_contig = lambda lines: [[l for l in lines if l.split(":")[0] == nm] for nm in ds.names]
+    assert by_contig(ch1) == by_contig(ch0)
+    assert [l.split(":")[0] for l in ch1] == sorted((l.split(":")[0] for l in ch0),
+                                                    key=lambda nm: -ds.names.index(nm))
+
+
+def test_soft_masked_reference():
+    """A reference with a lowercase (soft-masked) stretch holding a SNP, an
+    insertion and a deletion: the host driver's fixes and FASTA equal the
+    oracle's, which keeps the file's case wherever nothing is fixed."""
+    from types import SimpleNamespace
+    from pilon_gb300.reads import build_store
+    from tests.test_oracle_kat import _tile_reads, rand_ref, ref_from
+    up = rand_ref(900, seed=61)
+    snp = "ACGT"[("ACGT".index(up[299]) + 1) % 4]
+    recs, _ = _tile_reads(up, snps={300: snp}, ins={501: "GT"}, dels={601: 602})
+    ref = up[:200] + up[200:700].lower() + up[700:]
+    ds = SimpleNamespace(names=["chr1"], contigs=[ref_from(ref)], reads=build_store(recs))
+    n, out = compare(ds)
+    assert n >= 2 and any(c.islower() for c in out["fasta"].decode())
