@@ -65,11 +65,7 @@ struct Bits {
     drop(n);
     return v;
   }
-  // at least n (<= 56) bits in the buffer from here on
-  void need(int n) {
-    if (cnt < n) refill();
-  }
-  // n bits that need() has already made available
+  // n bits that the caller has already made available
   uint32_t take_have(int n) {
     const uint32_t v = (uint32_t)(buf & ((1ull << n) - 1));
     drop(n);
