@@ -177,3 +177,18 @@ def concat_stores(stores):
         cat([s.seq_off + b for s, b in zip(stores, seq_base)]), cat([s.l_seq for s in stores]),
         cat([s.seq for s in stores]),
         cat([s.qual_off + b for s, b in zip(stores, qual_base)]), cat([s.qual for s in stores]))
+
+
+def merge_sorted(stores):
+    """One coordinate-sorted store from several (the BAMs of one type that
+    Pilon reads one after another into the same pileups, S/GenomeRegion.scala:
+    287-300): reads ordered by reference, the unplaced reads (reference -1)
+    last, then by position, ties kept in input order.  Within one BAM type the
+    pileups, calls and region statistics do not depend on the order reads are
+    added, so the merged store gives the same results; the insert-size
+    statistics come out summed over the BAMs instead of per BAM."""
+    cat = concat_stores(stores)
+    rid = cat.ref_id.astype(np.int64)
+    key_ref = np.where(rid < 0, np.int64(1) << 40, rid)
+    order = np.lexsort((np.arange(cat.n_reads), cat.pos.astype(np.int64), key_ref))
+    return cat.subset(order)

@@ -88,3 +88,27 @@ def test_unplaced_reads_at_the_end_are_left_out():
     assert last and all(b > a for (_, _, _, a, b) in last)
     with pytest.raises(ValueError, match="coordinate-sorted"):
         plan_regions(concat_stores([tail, d.reads]), lens, chunk_size=5000)
+
+
+def test_merged_stores_give_the_same_pileups():
+    """Two BAMs of one type merged into one coordinate-sorted store pile up as
+    Pilon's sequential per-BAM processing does: the oracle over the merged store
+    equals the oracle over the two stores one after the other (it scans a
+    region's reads linearly, in any order)."""
+    from oracle import oracle
+    from pilon_gb300 import _abi
+    from pilon_gb300.reads import merge_sorted
+    d = synth.generate(1)
+    r = d.reads
+    a, b = r.subset(np.arange(0, r.n_reads, 2)), r.subset(np.arange(1, r.n_reads, 2))
+    m = merge_sorted([a, b])
+    seq = concat_stores([a, b])
+    assert np.array_equal(m.pos, np.sort(r.pos, kind="stable")) and m.n_reads == r.n_reads
+    L = d.contigs[0].size
+    p = _abi.default_params()
+    x = oracle.process_region(m, p, d.contigs[0], 0, 1, L)
+    y = oracle.process_region(seq, p, d.contigs[0], 0, 1, L)
+    for f in ("count", "qual_sum", "mq_sum", "q_sum", "phys_cov", "insert_size", "deletions", "insertions", "call",
+              "score", "indel_len"):
+        assert np.array_equal(getattr(x, f), getattr(y, f)), f
+    assert x.stats.read_count == y.stats.read_count and x.stats.fr_sum == y.stats.fr_sum
