@@ -1,0 +1,78 @@
+"""CPU restatement of the pileup walk's slot assignment (k_walk, the rounds of
+simple reads): each lane holding a simple read computes the slot its read takes
+in the warp's round order from ballots and population counts.  The slots must
+be a permutation of 0 .. n_simple - 1 (every read walked exactly once), and with
+4 or 8 lane groups the first 4 * m slots of the reads of the most common mq
+must hold one read of each position residue class in every group of four
+(their shared-memory atomics then fall in different banks)."""
+import random
+
+import pytest
+
+
+def popc(x):
+    return bin(x).count("1")
+
+
+def assign(sm_all, set_a, cls, ng):
+    """slot per lane, as the kernel computes it (one lane at a time here)."""
+    def ballot(mask, pred):
+        return sum(1 << ln for ln in range(32) if mask >> ln & 1 and pred(ln))
+
+    c = [ballot(set_a, lambda ln, k=k: cls[ln] == k) for k in range(4)]
+    m = min(popc(x) for x in c)
+    rank = {ln: popc(c[cls[ln]] & ((1 << ln) - 1)) for ln in range(32) if set_a >> ln & 1}
+    left = ballot(set_a, lambda ln: rank[ln] >= m)
+    slots = {}
+    for ln in range(32):
+        if not sm_all >> ln & 1:
+            continue
+        below = (1 << ln) - 1
+        if set_a >> ln & 1:
+            if ng in (4, 8):
+                r = rank[ln]
+                slots[ln] = 4 * r + cls[ln] if r < m else 4 * m + popc(left & below)
+            else:
+                slots[ln] = popc(set_a & below)
+        else:
+            slots[ln] = popc(set_a) + popc(sm_all & ~set_a & below)
+    return slots, m
+
+
+def check(sm_all, set_a, cls, ng):
+    slots, m = assign(sm_all, set_a, cls, ng)
+    assert sorted(slots.values()) == list(range(popc(sm_all))), (hex(sm_all), hex(set_a))
+    if ng in (4, 8):
+        by_slot = {s: ln for ln, s in slots.items()}
+        for k in range(m):
+            assert sorted(cls[by_slot[4 * k + j]] for j in range(4)) == [0, 1, 2, 3]
+
+
+@pytest.mark.parametrize("ng", [2, 4, 8])
+def test_random_lane_sets(ng):
+    rng = random.Random(ng)
+    for _ in range(3000):
+        sm_all = rng.getrandbits(32) & rng.getrandbits(32) if rng.random() < 0.5 else rng.getrandbits(32)
+        set_a = sm_all & (rng.getrandbits(32) if rng.random() < 0.7 else 0xFFFFFFFF)
+        cls = [rng.randrange(4) if rng.random() < 0.8 else 0 for _ in range(32)]
+        check(sm_all, set_a, cls, ng)
+
+
+@pytest.mark.parametrize("ng", [4, 8])
+def test_edge_lane_sets(ng):
+    full = 0xFFFFFFFF
+    for sm_all, set_a in [(0, 0), (1, 1), (full, full), (full, 0), (full, 0x0000FFFF), (0x80000000, 0x80000000)]:
+        for cls in ([0] * 32, [ln % 4 for ln in range(32)], [3 - ln % 4 for ln in range(32)],
+                    [ln // 8 for ln in range(32)]):
+            check(sm_all, set_a, cls, ng)
+
+
+def test_kernel_still_uses_these_formulas():
+    """The restatement above follows these lines of the walk kernel; a change
+    there must be carried over here."""
+    import os
+    src = open(os.path.join(os.path.dirname(__file__), "..", "pilon_gb300", "csrc", "pg_pileup.cu")).read()
+    for line in ["slot = rank < m ? 4 * rank + cls : 4 * m + __popc(left & below);",
+                 "slot = __popc(set_a & below);",
+                 "slot = __popc(set_a) + __popc(sm_all & ~set_a & below);"]:
+        assert line in src, line
