@@ -115,3 +115,18 @@ def test_random_chunks_match_per_base_rule():
                 assert got[j][1:] == (0, 0, 0)
             else:
                 assert got[j] == want
+
+
+def test_kernel_still_uses_these_formulas():
+    """decode_chunk above restates these lines of the walk kernel; a change
+    there must be carried over here."""
+    src = open(SRC).read()
+    for line in ["const uint32_t code = prmt(prmt(kCodeLo, kCodeHi, sv), prmt(kCodeLo, kCodeHi, sv >> 8), comb);",
+                 "const uint32_t ok = code & ((((qv | 0x80808080u) - minq4) & ~qv & 0x80808080u) >> 1) & okall;",
+                 "const uint32_t qm = qv & ((ok >> 6) * 0x7fu);",
+                 "const uint32_t one4 = ok >> 2;",
+                 "const uint32_t bix = code & 0x03030303u;",
+                 "prmt(qm, one4, (uint32_t)(j | (12 + j) << 4 | (4 + j) << 8 | (12 + j) << 12))",
+                 "const uint32_t minq4 = (uint32_t)min(max(P.min_qual, 0), 127) * 0x01010101u;",
+                 "const uint32_t okall = P.min_qual <= 127 ? 0xffffffffu : 0u;"]:
+        assert line in src, line
