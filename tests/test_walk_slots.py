@@ -1,10 +1,16 @@
-"""CPU restatement of the pileup walk's slot assignment (k_walk, the rounds of
-simple reads): each lane holding a simple read computes the slot its read takes
-in the warp's round order from ballots and population counts.  The slots must
-be a permutation of 0 .. n_simple - 1 (every read walked exactly once), and with
-4 or 8 lane groups the first 4 * m slots of the reads of the most common mq
-must hold one read of each position residue class in every group of four
-(their shared-memory atomics then fall in different banks)."""
+"""CPU restatements of the pileup walk's index arithmetic, each tied to the
+kernel's source lines.
+
+Slot assignment (k_walk, the rounds of simple reads): each lane holding a simple
+read computes its read's slot in the warp's round order from ballots and
+population counts.  The slots must be a permutation of 0 .. n_simple - 1 (every
+read walked exactly once), and with 4 or 8 lane groups the first 4 * m slots of
+the reads of the most common mq must hold one read of each position residue
+class in every group of four (their shared-memory atomics then fall in
+different banks).
+
+Read ranges (k_tile_ranges): the warp's 32-ary lower bound over a tile's
+position-sorted reads must equal a binary search, with every load in range."""
 import random
 
 import pytest
@@ -75,4 +81,49 @@ def test_kernel_still_uses_these_formulas():
     for line in ["slot = rank < m ? 4 * rank + cls : 4 * m + __popc(left & below);",
                  "slot = __popc(set_a & below);",
                  "slot = __popc(set_a) + __popc(sm_all & ~set_a & below);"]:
+        assert line in src, line
+
+
+def warp_lower_bound(pos, lo, hi, v):
+    """k_tile_ranges' warp_lower_bound_pos: 32 lanes sample [lo, hi) at even
+    strides per step; every load stays below hi."""
+    while hi - lo > 32:
+        step = (hi - lo + 31) // 32
+        below = 0
+        for lane in range(32):
+            sk = lo + lane * step
+            if sk < hi and pos[sk] < v:
+                below |= 1 << lane
+        c = popc(below)
+        if c == 0:
+            return lo
+        nlo = lo + (c - 1) * step + 1
+        sc = lo + c * step
+        hi = sc if (c < 32 and sc < hi) else hi
+        lo = nlo
+    return lo + sum(1 for lane in range(32) if lo + lane < hi and pos[lo + lane] < v)
+
+
+def test_warp_lower_bound_matches_bisect():
+    """The first index of [lo, hi) whose position is >= v, for sorted positions
+    with many duplicates, empty and short ranges, and v outside the values."""
+    import bisect
+    rng = random.Random(9)
+    for _ in range(2500):
+        n = rng.choice([0, 1, 5, 31, 32, 33, 64, 100, 1000, 5000])
+        pos = sorted(rng.randrange(0, max(1, n // rng.choice([1, 3, 50]))) for _ in range(n))
+        lo = rng.randrange(0, n + 1)
+        hi = rng.randrange(lo, n + 1)
+        v = rng.randrange(-2, (pos[-1] + 3) if pos else 3)
+        assert warp_lower_bound(pos, lo, hi, v) == bisect.bisect_left(pos, v, lo, hi), (n, lo, hi, v)
+
+
+def test_kernel_lower_bound_lines():
+    import os
+    src = open(os.path.join(os.path.dirname(__file__), "..", "pilon_gb300", "csrc", "pg_pileup.cu")).read()
+    for line in ["const int64_t step = (hi - lo + 31) / 32;",
+                 "const unsigned below = __ballot_sync(FULL, sk < hi && (int64_t)pos[sk] < v);",
+                 "const int64_t nlo = lo + (int64_t)(c - 1) * step + 1;",
+                 "hi = (c < 32 && sc < hi) ? sc : hi;",
+                 "const unsigned below = __ballot_sync(FULL, lo + lane < hi && (int64_t)pos[lo + lane] < v);"]:
         assert line in src, line
