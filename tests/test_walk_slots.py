@@ -10,7 +10,10 @@ class in every group of four (their shared-memory atomics then fall in
 different banks).
 
 Read ranges (k_tile_ranges): the warp's 32-ary lower bound over a tile's
-position-sorted reads must equal a binary search, with every load in range."""
+position-sorted reads must equal a binary search, with every load in range.
+
+Flush (k_walk): the packed per-position counters must give PileUp.add's sums
+exactly for any most common mq and up to 4095 reads per pass."""
 import random
 
 import pytest
@@ -126,4 +129,62 @@ def test_kernel_lower_bound_lines():
                  "const int64_t nlo = lo + (int64_t)(c - 1) * step + 1;",
                  "hi = (c < 32 && sc < hi) ? sc : hi;",
                  "const unsigned below = __ballot_sync(FULL, lo + lane < hi && (int64_t)pos[lo + lane] < v);"]:
+        assert line in src, line
+
+
+def _flush(reads, M):
+    """One position of one walk pass: the packed shared-memory words as the walk
+    adds to them (md[b] += qual + (1 << 20); for mq + 1 != M also qx[b] +=
+    qual * (mq + 1 - M) and mx += mq + 1 - M, all uint32) and the flush that
+    turns them into qualSum, mqSum, qSum and the counts."""
+    U = 0xFFFFFFFF
+    md, qx, mx = [0] * 4, [0] * 4, 0
+    for b, q, mq1 in reads:
+        md[b] = (md[b] + q + (1 << 20)) & U
+        d = mq1 - M
+        if d:
+            qx[b] = (qx[b] + q * d) & U
+            mx = (mx + d) & U
+    s32 = lambda x: x - (1 << 32) if x >= 1 << 31 else x
+    counts = [w >> 20 for w in md]
+    sums = [w & 0xFFFFF for w in md]
+    qual_sum = [M * sums[b] + s32(qx[b]) for b in range(4)]
+    mq_sum = s32((M * sum(counts) + mx) & U)
+    return counts, qual_sum, mq_sum, sum(sums)
+
+
+@pytest.mark.parametrize("case", ["max_up", "max_down", "random"])
+def test_walk_flush_is_exact_up_to_4095_reads(case):
+    """PileUp.add sums (count, qualSum as Long, mqSum, qSum) from the packed
+    counters, exact for any most common mq + 1 = M and up to 4095 reads per pass
+    (qualities are bytes, at most 127): 4095 reads at quality 127 and mq + 1 = 256
+    with M = 1, the reverse, and random mixes."""
+    rng = random.Random(17)
+    trials = 1 if case != "random" else 300
+    for _ in range(trials):
+        if case == "max_up":
+            M, reads = 1, [(rng.randrange(4), 127, 256) for _ in range(4095)]
+        elif case == "max_down":
+            M, reads = 256, [(rng.randrange(4), 127, 1) for _ in range(4095)]
+        else:
+            M = rng.randrange(1, 257)
+            reads = [(rng.randrange(4), rng.randrange(128), rng.randrange(1, 257))
+                     for _ in range(rng.randrange(0, 4096))]
+        counts, qual_sum, mq_sum, q_sum = _flush(reads, M)
+        assert counts == [sum(1 for b, _, _ in reads if b == k) for k in range(4)]
+        assert qual_sum == [sum(q * m for b, q, m in reads if b == k) for k in range(4)]
+        assert mq_sum == sum(m for _, _, m in reads) and q_sum == sum(q for _, q, _ in reads)
+
+
+def test_kernel_flush_lines():
+    import os
+    csrc = os.path.join(os.path.dirname(__file__), "..", "pilon_gb300", "csrc")
+    src = open(os.path.join(csrc, "pg_pileup.cu")).read() + open(os.path.join(csrc, "pg_internal.cuh")).read()
+    for line in ["const uint32_t s0 = w0 & 0xFFFFFu, s1 = w1 & 0xFFFFFu, s2 = w2 & 0xFFFFFu, s3 = w3 & 0xFFFFFu;",
+                 "const longlong2 q01 = make_longlong2((long long)M * s0 + (int32_t)sm[4 * T + p],",
+                 "const int32_t mqs = wadd((int32_t)(M * (uint32_t)(c.x + c.y + c.z + c.w)), (int32_t)sm[8 * T + p]);",
+                 "atomicAdd(c, (uint32_t)qual + (1u << 20));",
+                 "atomicAdd(c + 4 * T, (uint32_t)(qual * dmq));",
+                 "atomicAdd(sm + 8 * T + p, (uint32_t)dmq);",
+                 "constexpr int64_t kMaxReadsPerPass = 4095;"]:
         assert line in src, line
