@@ -1,0 +1,33 @@
+"""The Python examples of INTEGRATION.md compile and name functions the
+package has."""
+import ast
+import importlib
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _blocks():
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    return re.findall(r"```python\n(.*?)```", text, flags=re.S)
+
+
+def test_examples_compile_and_name_real_functions():
+    blocks = _blocks()
+    assert blocks
+    for code in blocks:
+        tree = ast.parse(code)
+        for node in ast.walk(tree):
+            if isinstance(node, ast.ImportFrom) and node.module and node.module.startswith("pilon_gb300"):
+                mod = importlib.import_module(node.module)
+                for a in node.names:
+                    assert hasattr(mod, a.name) or importlib.util.find_spec(f"{node.module}.{a.name}"), \
+                        f"{node.module}.{a.name}"
+            if (isinstance(node, ast.Attribute) and isinstance(node.value, ast.Name)
+                    and node.value.id in ("bam", "fasta", "synth", "_abi")):
+                mod = importlib.import_module(f"pilon_gb300.{node.value.id}")
+                assert hasattr(mod, node.attr), f"{node.value.id}.{node.attr}"
+            if isinstance(node, ast.Attribute) and isinstance(node.value, ast.Name) and node.value.id == "e":
+                from pilon_gb300.engine import Engine
+                assert hasattr(Engine, node.attr), f"Engine.{node.attr}"
