@@ -89,10 +89,18 @@ class OracleEngine:
                 assert oracle.polish(self.reads, self.params, self.names, self.contigs, pre, chunk_size=self.chunk,
                                      diploid=diploid, vcf_qe=vcf_qe) == 0
                 body = [l for l in open(pre + ".vcf", "rb").read().split(b"\n") if l and not l.startswith(b"#")]
-            self._vcf[key] = [l for l in body if l.split(b"\t")[4] != b"<DUP>"]
-        c, s, e = self.regions[r][:3]
-        nm = name.encode()
-        out = [l for l in self._vcf[key] if l.split(b"\t")[0] == nm and s <= int(l.split(b"\t")[1]) <= e]
+            by_contig = {}
+            for l in body:
+                f = l.split(b"\t", 5)
+                if f[4] != b"<DUP>":
+                    lines, locs = by_contig.setdefault(f[0], ([], []))
+                    lines.append(l)
+                    locs.append(int(f[1]))
+            self._vcf[key] = by_contig
+        import bisect
+        s, e = self.regions[r][1:3]
+        lines, locs = self._vcf[key].get(name.encode(), ([], []))
+        out = lines[bisect.bisect_left(locs, s):bisect.bisect_right(locs, e)]
         return b"".join(l + b"\n" for l in out)
 
 
@@ -250,3 +258,21 @@ def test_soft_masked_reference():
     ds = SimpleNamespace(names=["chr1"], contigs=[ref_from(ref)], reads=build_store(recs))
     n, out = compare(ds)
     assert n >= 2 and any(c.islower() for c in out["fasta"].decode())
+
+
+@pytest.mark.parametrize("wl,kw,pk", [
+    (2, dict(chunk=20000, iupac=True, vcf=True), dict(fix_amb=1, min_qual=20)),
+    (2, dict(chunk=33333, fix_indels=False, diploid=True, vcf=True), dict(flank=25)),
+    (2, dict(fix_snps=False), dict(min_mq=10, flank=0)),
+    (3, dict(chunk=20000, vcf=True, vcf_qe=True), dict(fix_amb=1)),
+    (3, dict(longread=True, nanopore=True), dict(long_read=_abi.PG_NANOPORE, bam_type=_abi.PG_BAM_UNPAIRED)),
+    (3, dict(chunk=33333, longread=True, nanopore=False, vcf=True),
+     dict(long_read=_abi.PG_PACBIO, bam_type=_abi.PG_BAM_UNPAIRED, min_qual=20)),
+])
+def test_option_combinations_on_other_workloads(wl, kw, pk):
+    """The host driver against the oracle on the 100x workload with mapq-0
+    reads and indel errors and on the many-contig workload (both scaled), over
+    combinations of chunking, fix types, AMB options, read filters, flank,
+    long-read modes and VCF flavours."""
+    ds = synth.generate(wl, scale=0.01)
+    compare(ds, params=_abi.default_params(**pk), **kw)
