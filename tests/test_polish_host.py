@@ -276,3 +276,42 @@ def test_option_combinations_on_other_workloads(wl, kw, pk):
     long-read modes and VCF flavours."""
     ds = synth.generate(wl, scale=0.01)
     compare(ds, params=_abi.default_params(**pk), **kw)
+
+
+def test_served_requests_equal_target_outputs():
+    """A served request's answer (serve.request_result) equals what --targets
+    writes for that target: its fixed bases and its changes lines (each target
+    its own entry, the offset restarting)."""
+    from types import SimpleNamespace
+    from pilon_gb300.reads import build_store
+    from pilon_gb300.regions import plan_regions
+    from pilon_gb300.serve import Request, request_result
+    from tests.test_oracle_kat import _tile_reads, rand_ref, ref_from
+    ref = list(rand_ref(2000, seed=51))
+    if ref[308] == "A":
+        ref[308] = "G" if ref[307] != "G" and ref[309] != "G" else "T"
+    ref = "".join(ref)
+    s1 = "ACGT"[("ACGT".index(ref[299]) + 1) % 4]
+    s2 = "ACGT"[("ACGT".index(ref[1499]) + 1) % 4]
+    recs, _ = _tile_reads(ref, snps={300: s1, 1500: s2}, ins={310: "CA"}, dels={1601: 1602})
+    ds = SimpleNamespace(names=["chr1"], contigs=[ref_from(ref)], reads=build_store(recs))
+    targets = [(0, 200, 800), (0, 1000, 1800)]
+    opts = Options(vcf=False, targets=targets)
+    with tempfile.TemporaryDirectory() as d:
+        pre = os.path.join(d, "t")
+        polish(OracleEngine(ds.names), ds.names, ds.contigs, ds.reads, _abi.default_params(), pre, opts)
+        fasta = open(pre + ".fasta").read().split(">chr1_pilon\n")[1:]
+        changes = open(pre + ".changes").read()
+    eng = OracleEngine(ds.names)
+    eng.set_reference(ds.contigs)
+    eng.set_reads(ds.reads)
+    eng.pileup_regions(plan_regions(ds.reads, [len(ref)], targets=targets), _abi.default_params())
+    eng.format_vcf = lambda *a, **k: b""
+    got_fa, got_ch = [], ""
+    for r, (c, s, e) in enumerate(targets):
+        res = request_result(eng, r, Request(contig=c, start=s, stop=e), ds.names, ds.contigs,
+                             _abi.default_params(), Options(vcf=False))
+        got_fa.append(res.fasta.decode() if isinstance(res.fasta, bytes) else res.fasta)
+        got_ch += res.changes
+    assert [f.replace("\n", "") for f in fasta] == got_fa
+    assert got_ch == changes and changes.count("\n") == 4
