@@ -137,3 +137,22 @@ def test_record_length_fields_are_checked(cfg1):
     struct.pack_into("<i", bad, rec + 4, 2 ** 31 - 1)
     _, _, st = _read(_bam_of(bytes(bad)))
     assert st.pos[0] == -2 ** 31
+
+
+def test_unplaced_tail_round_trip_and_plan(cfg1, tmp_path):
+    """A coordinate-sorted BAM ending with unplaced reads (reference -1, BAM
+    position -1): they read back with htsjdk's start 0 and end 0, and the region
+    plan of the store leaves them out."""
+    from pilon_gb300.reads import build_store, concat_stores
+    from pilon_gb300.regions import plan_regions
+    base = cfg1.reads.subset(np.arange(3000))
+    rec = dict(pos=0, cigar=[], seq="ACGTNACGTT", qual=[20] * 10, flag=0x4, mapq=0, ref_id=-1, mate_ref_id=-1)
+    store = concat_stores([base, build_store([rec] * 3)])
+    lens = [c.size for c in cfg1.contigs]
+    path = str(tmp_path / "u.bam")
+    bam.write_bam(path, cfg1.names, lens, store)
+    _, _, st = bam.read_bam(path)
+    assert list(st.ref_id[-3:]) == [-1] * 3 and list(st.pos[-3:]) == [0] * 3 and list(st.aend[-3:]) == [0] * 3
+    for f in FIELDS:
+        assert np.array_equal(getattr(st, f), getattr(store, f)), f
+    assert plan_regions(st, lens, 20000) == plan_regions(base, lens, 20000)
