@@ -295,6 +295,13 @@ pg_status pg_kmer_tally_breaks(pg_ctx *ctx, int32_t min_min_depth, int32_t radiu
 pg_status pg_last_kernel_ms(pg_ctx *ctx, double *walk_ms, double *total_ms, int32_t *launches);
 /* Synchronises the context stream. */
 pg_status pg_sync(pg_ctx *ctx);
+/* Number of pg_pileup_regions calls on this context that replayed a recorded
+ * CUDA graph instead of launching the kernels one by one.  A batched call is
+ * recorded on its second identical occurrence and replayed after that while
+ * the plan, the options and every buffer the graph uses stay the same; a call
+ * that reallocates one of those buffers ends the replays until the next
+ * recording.  No counterpart in the reference (a measurement hook). */
+pg_status pg_graph_replays(pg_ctx *ctx, int32_t *replays);
 
 /* ---- physical-coverage scan without device allocation ----------------------
  * This entry point has no counterpart in the reference.  It is for callers
@@ -313,7 +320,9 @@ pg_status pg_sync(pg_ctx *ctx);
  * Its only scratch is a fixed 128 KiB device array inside the library, so it
  * allocates nothing; n_positions above PG_STATIC_SCAN_MAX_POSITIONS returns
  * PG_ERR_LIMIT.  The first call on each device looks up that array's device
- * address (make it before any stream capture).  All calls share the array:
+ * address (make it before any stream capture) and keeps it for the life of the
+ * process; a host that destroys the device's primary context (cudaDeviceReset)
+ * must not call this entry point afterwards.  All calls share the array:
  * calls that overlap on the GPU race and must be serialised by the caller.
  * On failure a message is written to errbuf (may be NULL). */
 #define PG_STATIC_SCAN_MAX_POSITIONS 16777216

@@ -86,6 +86,7 @@ struct pg_ctx {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   uint64_t graph_key = 0;
+  bool graph_valid = false;  // cleared whenever a buffer the graph uses is reallocated
   int32_t use_graph = 1;
   int32_t graph_replays = 0;
   bool capturing = false;
@@ -115,6 +116,9 @@ pg_status fail(pg_ctx* c, pg_status s, const char* fmt, ...) {
 
 pg_status ensure(pg_ctx* c, DevBuf& b, size_t bytes) {
   if (bytes <= b.cap && b.p) return PG_OK;
+  // a captured graph holds the old address: it must not be replayed again
+  c->graph_valid = false;
+  c->graph_key = 0;
   if (b.p) cudaFree(b.p);
   b.p = nullptr;
   b.cap = 0;
@@ -413,6 +417,8 @@ pg_status pg_set_reads_device(pg_ctx* c, const pg_reads* d) {
 
 static pg_status stage(pg_ctx* c, size_t bytes) {
   if (bytes <= c->staging_cap) return PG_OK;
+  c->graph_valid = false;  // the graph's copy nodes read the old staging buffer
+  c->graph_key = 0;
   if (c->staging_host) cudaFreeHost(c->staging_host);
   c->staging_host = nullptr;
   size_t want = bytes + bytes / 4 + 4096;
@@ -449,7 +455,7 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   cudaMemsetAsync(&counters[CNT_EVENTS], 0, sizeof(unsigned long long), s);
   cudaMemsetAsync(&counters[CNT_SPOOL], 0, sizeof(unsigned long long), s);
 
-  launch_tile_ranges(c->R, d_regions, P<WalkTile>(c->walk_tiles) + w0, wn, P<ReadExtent>(c->d_ext), s);
+  launch_tile_ranges(c->R, d_regions, P<WalkTile>(c->walk_tiles) + w0, wn, P<ReadExtent>(c->d_ext), d_stats, s);
 
   WalkArgs wa;
   wa.R = c->R; wa.regions = d_regions; wa.tiles = P<WalkTile>(c->walk_tiles); wa.n_tiles = wn;
@@ -610,9 +616,13 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
     key = fnv(key, c->staging_host, b_reg + b_walk + b_call + b_ch);
     key = fnv(key, &dp, sizeof dp);
     key = fnv(key, &c->R, sizeof c->R);
+    // every buffer the recorded launches and copies read or write, host staging included
     const void* ptrs[] = {c->ref.p, c->events.p, c->events_sorted.p, c->cands.p, c->pool.p, c->spool.p,
                           c->rec_count.p, c->rec_qsum.p, c->rec_call.p, c->rec_score.p, c->rec_indel_len.p,
-                          c->rec_ins_str.p, c->rec_ev_end.p, c->chunk_stats.p, c->stats.p, c->tile_sums.p};
+                          c->rec_ins_str.p, c->rec_ev_end.p, c->chunk_stats.p, c->stats.p, c->tile_sums.p,
+                          c->regions.p, c->walk_tiles.p, c->call_tile_region.p, c->chunks.p, c->cand_count.p,
+                          c->cand_off.p, c->indel_list.p, c->counters.p, c->run_max.p, c->d_ext.p, c->rdesc.p,
+                          c->staging_host};
     key = fnv(key, ptrs, sizeof ptrs);
     for (auto& b : c->rec_i32) key = fnv(key, &b.p, sizeof b.p);
     const int32_t shape[7] = {c->tile_width, c->warps, c->packed, batched, (int32_t)c->event_cap, c->cand_cap,
@@ -620,7 +630,7 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
     key = fnv(key, shape, sizeof shape);
     key = fnv(key, &c->pool_cap, sizeof c->pool_cap);
     key = fnv(key, &c->spool_cap, sizeof c->spool_cap);
-    const bool replay = c->use_graph && batched && c->graph_exec && key == c->graph_key;
+    const bool replay = c->use_graph && batched && c->graph_exec && c->graph_valid && key == c->graph_key;
     const bool capture = c->use_graph && batched && !replay && attempt == 0 && c->graph_key == key + 1;
     c->walk_ms = 0;
     CK(cudaEventRecord(c->e0, st));
@@ -658,6 +668,7 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
         CK(cudaGraphInstantiate(&c->graph_exec, g, 0));
         CK(cudaGraphLaunch(c->graph_exec, st));
         c->graph_key = key;
+        c->graph_valid = true;
       } else if (batched && c->use_graph && attempt == 0 && !replay) {
         c->graph_key = key + 1;  // the next identical call records the graph
       }
@@ -684,6 +695,11 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
     if ((int64_t)hc[CNT_POOL] > c->pool_cap) { c->pool_cap = (int64_t)hc[CNT_POOL] * 2 + 4096; grow = true; }
     if ((int64_t)hc[CNT_SPOOL_MAX] > c->spool_cap) { c->spool_cap = (int64_t)hc[CNT_SPOOL_MAX] * 2 + 4096; grow = true; }
     if (!grow) {
+      for (int32_t r = 0; r < n_regions; r++)
+        if (c->stats_h[r].range_error)
+          return fail(c, PG_ERR_ARG, "region %d: its read range [%lld, %lld) holds reads of another reference "
+                      "(a range must hold the region contig's reads only, in position order)", r,
+                      (long long)regs[r].read_begin, (long long)regs[r].read_end);
       c->have_results = true;  // regions without an error keep valid results
       for (int32_t r = 0; r < n_regions; r++)
         if (c->stats_h[r].error)
@@ -1026,6 +1042,12 @@ pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid,
   CK(cudaGetLastError());
   if (total && out) CK(cudaMemcpyAsync(out, c->vtext.p, (size_t)total, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  return PG_OK;
+}
+
+pg_status pg_graph_replays(pg_ctx* c, int32_t* replays) {
+  if (!c || !replays) return PG_ERR_ARG;
+  *replays = c->graph_replays;
   return PG_OK;
 }
 

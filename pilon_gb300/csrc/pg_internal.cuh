@@ -66,7 +66,7 @@ struct StatsDev {        // per region, accumulated on the device
   int32_t error;
   int32_t n_ins;
   int32_t prep_done;     // CTAs of k_region_prep that have added their part
-  int32_t pad;
+  int32_t range_error;   // 1: the region's read range holds reads of another reference
 };
 
 struct WalkTile {
@@ -118,6 +118,10 @@ struct ReadExtent {      // maxima over the read store, for tile read ranges
   unsigned long long n_indel_ops;
   unsigned long long bad_read;  // 1 + index of a read whose offsets leave their arrays, else 0
   int32_t unsorted;      // 1 if positions decrease within one reference
+  // 1 if the references are not in one run each: a reference id below the one
+  // before it, or a placed read after an unplaced one (negative id).  A
+  // coordinate-sorted BAM has each reference in one run, unplaced reads last.
+  int32_t ungrouped;
   int32_t max_span;      // max(aend - pos + 1): how far before a window a read that overlaps it can start
   // reads with simple CIGARs and qualities, by adjusted mq + 1 (1..256); the
   // walk adds the reads of the most common value with one atomic per base
@@ -402,7 +406,7 @@ struct CallArgs {
 
 void launch_read_extent(const Reads& R, ReadExtent* out, int4* desc, cudaStream_t s);
 void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tiles, int32_t n_tiles,
-                        const ReadExtent* ext, cudaStream_t s);
+                        const ReadExtent* ext, StatsDev* stats, cudaStream_t s);
 void launch_walk(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s);
 void launch_read_events(const EventArgs& a, int32_t chunk_begin, int32_t chunk_count, cudaStream_t s);
 void launch_scan_small(const int32_t* in, int32_t* out_excl, int32_t n, cudaStream_t s);

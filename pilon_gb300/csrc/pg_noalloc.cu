@@ -136,7 +136,9 @@ extern "C" pg_status pg_phys_cov_scan_static(const int32_t* phys_diff, const int
     // Set-up, once per device, with that device current: the device address
     // of the scratch array.  (In host code the array's name is only a host
     // stand-in.)  This first call on a device must come before any stream
-    // capture that includes this entry point.
+    // capture that includes this entry point.  The address is kept until the
+    // process exits: cudaDeviceReset (which destroys the primary context and
+    // this array with it) ends the use of this entry point on that device.
     std::lock_guard<std::mutex> lock(g_mu);
     if (!g_scratch_ptr[dev]) {
       void* p = nullptr;

@@ -48,7 +48,11 @@ __global__ void k_read_extent(Reads R, ReadExtent* out, int4* desc) {
         atomicCAS(&out->bad_read, 0ull, (unsigned long long)i + 1);
         continue;
       }
-      if (i > 0 && R.ref_id[i] == R.ref_id[i - 1] && pos < R.pos[i - 1]) out->unsorted = 1;
+      if (i > 0) {
+        const int32_t r0 = R.ref_id[i - 1], r1 = R.ref_id[i];
+        if (r1 == r0 && pos < R.pos[i - 1]) out->unsorted = 1;
+        if ((r0 < 0 && r1 >= 0) || (r1 >= 0 && r1 < r0)) out->ungrouped = 1;
+      }
     }
     int64_t lo = pos, hi = pos;
     int32_t ro = 0, fo = 0;
@@ -163,14 +167,28 @@ __device__ inline int64_t warp_lower_bound_pos(const int32_t* pos, int64_t lo, i
   return lo + __popc(below);
 }
 
-// One warp per tile.
+// One warp per tile.  The warp of a region's first tile also checks that the
+// region's read range holds reads of the region's reference only (the range
+// is searched by position, so reads of another reference would be dropped
+// silently; the reference's queryOverlapping is per contig,
+// S/BamFile.scala:117-119).  In a store whose references come one run each
+// the first and last read decide; otherwise every read is checked.
 __global__ void k_tile_ranges(Reads R, const RegionDev* regions, WalkTile* tiles, int32_t n_tiles,
-                              const ReadExtent* ext) {
+                              const ReadExtent* ext, StatsDev* stats) {
   const int32_t t = (int32_t)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (t >= n_tiles) return;  // whole warps leave together
   WalkTile& T = tiles[t];
   const RegionDev& g = regions[T.region];
+  if (T.lo == 0 && g.read_end > g.read_begin) {
+    bool bad = false;
+    if (!ext->ungrouped) {
+      bad = lane == 0 && (R.ref_id[g.read_begin] != g.contig || R.ref_id[g.read_end - 1] != g.contig);
+    } else {
+      for (int64_t i = g.read_begin + lane; i < g.read_end && !bad; i += 32) bad = R.ref_id[i] != g.contig;
+    }
+    if (__any_sync(FULL, bad) && lane == 0) stats[T.region].range_error = 1;
+  }
   const int64_t tlo = (int64_t)g.start + T.lo, thi = tlo + T.len - 1;
   const int64_t a = tlo - ext->max_back, b = thi + ext->max_lead + 1;
   const int64_t rlo = warp_lower_bound_pos(R.pos, g.read_begin, g.read_end, a, lane);
@@ -182,9 +200,9 @@ __global__ void k_tile_ranges(Reads R, const RegionDev* regions, WalkTile* tiles
 }
 
 void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tiles, int32_t n_tiles,
-                        const ReadExtent* ext, cudaStream_t s) {
+                        const ReadExtent* ext, StatsDev* stats, cudaStream_t s) {
   if (n_tiles == 0) return;
-  k_tile_ranges<<<(int)(((int64_t)n_tiles * 32 + 255) / 256), 256, 0, s>>>(R, regions, tiles, n_tiles, ext);
+  k_tile_ranges<<<(int)(((int64_t)n_tiles * 32 + 255) / 256), 256, 0, s>>>(R, regions, tiles, n_tiles, ext, stats);
 }
 
 // ---------------------------------------------------------------------------

@@ -1,6 +1,6 @@
 """ctypes binding of libpilon_gb300.so, the GB300 engine behind the C ABI of
-include/pilon_gb300.h.  This is the binding a JVM host would write with JNI or
-the Java foreign-function API; see INTEGRATION.md for that side.
+include/pilon_gb300.h.  A JVM host would make the same calls through JNI or
+the Java foreign-function API.
 
 There is no CPU fallback: if the engine library is missing or no CUDA device
 is present, every call raises.
@@ -50,6 +50,7 @@ def lib():
             "pg_last_kernel_ms": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_int32)]),
             "pg_sync": (C.c_int, [vp]),
+            "pg_graph_replays": (C.c_int, [vp, C.POINTER(C.c_int32)]),
             "pg_format_vcf": (C.c_int, [vp, i32, C.c_char_p, i32, i32, i32, vp, i64, C.POINTER(C.c_int64)]),
             "pg_find_breaks": (C.c_int, [vp, i32, vp, i64, C.POINTER(C.c_int64)]),
             "pg_kmer_tally_breaks": (C.c_int, [vp, i32, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
@@ -250,3 +251,9 @@ class Engine:
 
     def sync(self):
         self._check(self.L.pg_sync(self.h))
+
+    def graph_replays(self):
+        """pg_graph_replays: calls of this context that replayed a recorded graph."""
+        n = C.c_int32()
+        self._check(self.L.pg_graph_replays(self.h, C.byref(n)))
+        return n.value

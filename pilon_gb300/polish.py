@@ -8,7 +8,7 @@ snps / indels (and amb / iupac), writing Pilon's three outputs.
   changes, FASTA                host (S/GenomeRegion.scala:645-657, S/GenomeFile.scala:79-82, 135-161)
 
 Gap filling and local reassembly (fix types gaps / local) are not part of
-this driver; their break windows feed the K-mer tally (pilon_gb300.assembler).
+this driver; their break windows feed the K-mer tally (pg_kmer_tally_breaks).
 """
 import ctypes as C
 from dataclasses import dataclass, field

@@ -1,4 +1,5 @@
-"""K-mer graphs of local-reassembly windows on the GB300 engine.
+"""Test support: K-mer graphs of local-reassembly windows from the engine's
+tally edges.
 
 Mirrors Assembler.addReads / buildGraph (S/Assembler.scala:46-154) for many
 windows at once: the engine tallies, for every K-mer of every recruited read

@@ -1,10 +1,10 @@
-"""Break candidates of a region (GenomeRegion.possibleBreaks,
-S/GenomeRegion.scala:659-763 and pctBadOverall :99-114), computed from the
-engine's per-position arrays.  These regions are the windows whose reads the
+"""Test support: break candidates of a region (GenomeRegion.possibleBreaks,
+S/GenomeRegion.scala:659-763 and pctBadOverall :99-114), computed on the host
+from the engine's per-position arrays, to check the device's pg_find_breaks.  These regions are the windows whose reads the
 K-mer tally consumes (S/GenomeRegion.scala:395-410)."""
 import numpy as np
 
-from .polish import summary_regions
+from pilon_gb300.polish import summary_regions
 
 
 def _pct_int(n, d):

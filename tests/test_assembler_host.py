@@ -1,4 +1,4 @@
-"""The host side of pilon_gb300.assembler on the CPU: Assembler.buildGraph's
+"""The host graph builder of tests/assembler_host.py on the CPU: Assembler.buildGraph's
 kGraph / altGraph maps (S/Assembler.scala:132-154) built from the tally's edge
 records, with a test-only stand-in whose kmer_tally returns the oracle's edges.
 Each K-mer is visited once in buildGraph, so its kGraph entry is the called
@@ -6,7 +6,7 @@ base's successor and altGraph holds the alternate base's when the call is not
 homozygous."""
 from oracle import oracle
 from pilon_gb300 import _abi
-from pilon_gb300.assembler import Assembler, kmer_string
+from tests.assembler_host import Assembler, kmer_string
 from pilon_gb300.reads import build_store
 
 

@@ -4,7 +4,7 @@ import pytest
 
 from oracle import oracle
 from pilon_gb300 import _abi, synth
-from pilon_gb300.breaks import possible_breaks, region_arrays
+from tests.breaks_host import possible_breaks, region_arrays
 from pilon_gb300.regions import ReadIndex, plan_regions
 
 pytestmark = pytest.mark.gpu
@@ -90,7 +90,7 @@ def test_kmer_tally_exotic_kmers(engine, cfg1):
 
 
 def test_assembler_graph(engine, cfg1):
-    from pilon_gb300.assembler import Assembler
+    from tests.assembler_host import Assembler
     engine.set_reference(cfg1.contigs)
     engine.set_reads(cfg1.reads)
     asm = Assembler(engine, K=21)

@@ -141,3 +141,85 @@ def test_fetch_all_equals_per_region(engine, cfg1):
         for f in list(RegionArrays.I32) + ["call", "score"]:
             assert np.array_equal(getattr(allr, f)[off:off + n], getattr(one, f)), (r, f)
         off += n
+
+
+def test_graph_not_replayed_after_reallocation(cfg1):
+    """A recorded graph holds the addresses of the context's buffers.  A call
+    that grows one of them (here a plan with four times the regions, on the
+    per-region path) must end the replays: the next batched call of the first
+    plan runs its launches again and matches the oracle, and only the call
+    after it records a new graph."""
+    from pilon_gb300.engine import Engine
+    p = _abi.default_params()
+    a = plan(cfg1, chunk_size=9000)
+    b = plan(cfg1, chunk_size=2000)
+    assert len(b) >= 4 * len(a)
+    ora_a = oracle_regions(cfg1, p, a)
+    ora_b = oracle_regions(cfg1, p, b)
+    eng = Engine(0)
+    try:
+        eng.set_reference(cfg1.contigs)
+        eng.set_reads(cfg1.reads)
+
+        def check(regs, ora, label):
+            for r in range(len(regs)):
+                compare_region(eng.fetch(r), ora[r], label=f"{label} region {r}")
+        for k in range(3):  # eager, recorded, replayed
+            eng.pileup_regions(a, p, batched=True)
+            check(a, ora_a, f"a{k}")
+        r0 = eng.graph_replays()
+        assert r0 == 1
+        eng.pileup_regions(b, p, batched=False)
+        check(b, ora_b, "b plain")
+        eng.pileup_regions(a, p, batched=True)
+        check(a, ora_a, "a after b")
+        assert eng.graph_replays() == r0, "a graph with freed buffers was replayed"
+        eng.pileup_regions(b, p, batched=True)
+        check(b, ora_b, "b batched")
+        for k in range(3):
+            eng.pileup_regions(a, p, batched=True)
+            check(a, ora_a, f"a again {k}")
+        assert eng.graph_replays() == r0 + 1
+    finally:
+        eng.close()
+
+
+def test_region_range_of_another_reference_refused(cfg1):
+    """A region whose read range holds reads of another reference is refused
+    (PG_ERR_ARG), in a store with one run per reference and in a store whose
+    references interleave; a well-formed call afterwards still matches the
+    oracle."""
+    from pilon_gb300.engine import Engine, EngineError
+    from pilon_gb300.reads import concat_stores
+    p = _abi.default_params()
+    one = cfg1.reads
+    two = concat_stores([one, one])
+    two.ref_id[one.n_reads:] = 1
+    two.mate_ref_id[one.n_reads:] = 1
+    n = one.n_reads
+    size = cfg1.contigs[0].size
+    eng = Engine(0)
+    try:
+        eng.set_reference([cfg1.contigs[0], cfg1.contigs[0]])
+        eng.set_reads(two)
+        for bad in ([(0, 1, size, 0, n + 10)], [(1, 1, size, n - 5, 2 * n)], [(1, 1, size, 0, n)]):
+            with pytest.raises(EngineError) as ei:
+                eng.pileup_regions(bad, p, batched=True)
+            assert ei.value.status == _abi.PG_ERR_ARG and "another reference" in str(ei.value)
+        good = [(0, 1, size, 0, n), (1, 1, size, n, 2 * n)]
+        eng.pileup_regions(good, p, batched=True)
+        ora = oracle_regions(cfg1, p, [(0, 1, size, 0, n)])
+        compare_region(eng.fetch(0), ora[0], label="contig 0")
+        compare_region(eng.fetch(1), ora[0], label="contig 1")
+        # references interleaved (1 before 0): every read of a range is checked
+        swapped = concat_stores([one, one])
+        swapped.ref_id[:n] = 1
+        swapped.mate_ref_id[:n] = 1
+        eng.set_reads(swapped)
+        with pytest.raises(EngineError) as ei:
+            eng.pileup_regions([(0, 1, size, n - 3, 2 * n)], p, batched=True)
+        assert ei.value.status == _abi.PG_ERR_ARG
+        eng.pileup_regions([(1, 1, size, 0, n), (0, 1, size, n, 2 * n)], p, batched=True)
+        compare_region(eng.fetch(1), ora[0], label="swapped contig 0")
+    finally:
+        eng.close()

@@ -98,13 +98,64 @@ def test_static_scan_matches_pileup_regions():
         assert np.array_equal(d_is.cpu().numpy(), ex.insert_size), f"region {r}: insert size differs"
 
 
-def test_static_scan_rejects_oversize():
+def _scan_fn():
     from pilon_gb300.engine import lib
-    L = lib()
-    f = L.pg_phys_cov_scan_static
+    f = lib().pg_phys_cov_scan_static
     f.restype = C.c_int
     f.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                   C.c_char_p, C.c_int32]
+    return f
+
+
+def _expected_scan(pd, idf, carry_pc, carry_is):
+    """computePhysCov (S/PileUpRegion.scala:90-100) in numpy: Int prefix sums
+    that wrap at 32 bits, then insertSize / physCov (truncating) where
+    physCov > 0."""
+    wrap = lambda x: ((x + 2**31) % 2**32 - 2**31)
+    pc = wrap(np.cumsum(pd.astype(np.int64)) + carry_pc)
+    isz = wrap(np.cumsum(idf.astype(np.int64)) + carry_is)
+    q = np.sign(isz) * (np.abs(isz) // np.where(pc > 0, pc, 1))
+    return pc.astype(np.int32), np.where(pc > 0, q, isz).astype(np.int32)
+
+
+@pytest.mark.parametrize("n", [3_000_017, _abi.PG_STATIC_SCAN_MAX_POSITIONS])
+def test_static_scan_long_regions_and_in_place(n):
+    """Regions above 1,048,576 positions take the tile scan over several rounds
+    of 1024 tiles, up to the size limit; output written over the input gives the
+    same values.  Random difference arrays, small and full-range (wrapping)."""
+    import torch
+    f = _scan_fn()
+    err = C.create_string_buffer(256)
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev)
+    rng = np.random.default_rng(n)
+    cases = [(rng.integers(-3, 4, n).astype(np.int32), rng.integers(-900, 901, n).astype(np.int32), 7, 3500),
+             (rng.integers(-2**31, 2**31, n, dtype=np.int64).astype(np.int32),
+              rng.integers(-2**31, 2**31, n, dtype=np.int64).astype(np.int32), -5, 2**31 - 9)]
+    for pd, idf, c_pc, c_is in cases:
+        want_pc, want_is = _expected_scan(pd, idf, c_pc, c_is)
+        d_pd = torch.from_numpy(pd).to(dev)
+        d_id = torch.from_numpy(idf).to(dev)
+        d_pc = torch.full_like(d_pd, -7)
+        d_is = torch.full_like(d_id, -7)
+        torch.cuda.synchronize(dev)
+        rc = f(d_pd.data_ptr(), d_id.data_ptr(), n, c_pc, c_is, d_pc.data_ptr(), d_is.data_ptr(),
+               C.c_void_p(stream.cuda_stream), err, 256)
+        assert rc == _abi.PG_OK, err.value.decode()
+        # in place: the output arrays are the input arrays
+        rc = f(d_pd.data_ptr(), d_id.data_ptr(), n, c_pc, c_is, d_pd.data_ptr(), d_id.data_ptr(),
+               C.c_void_p(stream.cuda_stream), err, 256)
+        assert rc == _abi.PG_OK, err.value.decode()
+        torch.cuda.synchronize(dev)
+        assert np.array_equal(d_pc.cpu().numpy(), want_pc)
+        assert np.array_equal(d_is.cpu().numpy(), want_is)
+        assert np.array_equal(d_pd.cpu().numpy(), want_pc), "in place"
+        assert np.array_equal(d_id.cpu().numpy(), want_is), "in place"
+        del d_pd, d_id, d_pc, d_is
+
+
+def test_static_scan_rejects_oversize():
+    f = _scan_fn()
     err = C.create_string_buffer(256)
     one = np.zeros(1, np.int32)
     p = one.ctypes.data  # never dereferenced: the size check comes first
