@@ -1,12 +1,16 @@
 """Benchmark: aligned bases piled per second (pileup + calls + pass 1) on GB300.
 
-Workload (default): 5 Mb bacterial genome, GC 65%, 100x 2x150 pairs, insert
-N(500, 80), 0.3% substitutions, 0.02% indel errors, 500 SNPs + 100 indels,
-3% mapq-0 reads, one 5 Mb region (Pilon's default 10 Mb chunking), synthetic
-and seeded (1002).  A step is one pg_pileup_regions call over all regions:
+Workload (default, --config 3): a draft assembly of 3,000 contigs with
+log-normal lengths (median 20 kb, 1 kb - 2 Mb, 132.8 Mb in all), 40x 2x150
+pairs, 1% of the bases carrying planted SNPs and indels, synthetic and seeded
+(1003); every contig is one region and all 3,000 run as one batched,
+graph-replayed plan.  A step is one pg_pileup_regions call over all regions:
 BamFile.process + PileUpRegion.addRead, computePhysCov, BaseCall and pass 1.
+The line also carries the 5 Mb / 100x bacterial workload (--config 2) measured
+the same way under "bacterial_5mb", and "parity_full": every region of the
+full-size workload compared with the oracle (outside the timed region).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--config 2] [--impl reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config 3] [--impl reference]
 
 --impl reference times the CPU restatement of the reference path (the oracle;
 the Scala reference cannot run here: no JVM) on the host cores.
@@ -179,21 +183,26 @@ def roofline_traffic(workload_name, units):
     return None
 
 
-def oracle_sample(ds, params, threads):
-    """The oracle over the workload split in `threads` regions on as many host
-    threads; returns (piled bases, seconds)."""
+def oracle_sample(ds, params, threads, regions=None):
+    """The oracle over the whole workload on `threads` host threads: on the
+    GPU arm's own regions when there are at least as many as threads (then both
+    arms pile the same units), else with each contig split in up to `threads`
+    regions; largest regions first.  Returns (piled bases, seconds, regions)."""
     from oracle import oracle
     from pilon_gb300.regions import ReadIndex
     oracle.lib()
-    jobs = []
-    idx = ReadIndex(ds.reads, len(ds.contigs))
-    for ci, ref in enumerate(ds.contigs):
-        n = max(1, min(threads, ref.size // 50_000))
-        step = (ref.size + n - 1) // n
-        for s in range(1, ref.size + 1, step):
-            e = min(ref.size, s + step - 1)
-            a, b = idx.range_for(ci, s, e, ref.size)
-            jobs.append((ci, s, e, a, b))
+    if regions is not None and len(regions) >= threads:
+        jobs = sorted(regions, key=lambda r: r[1] - r[2])
+    else:
+        jobs = []
+        idx = ReadIndex(ds.reads, len(ds.contigs))
+        for ci, ref in enumerate(ds.contigs):
+            n = max(1, min(threads, ref.size // 50_000))
+            step = (ref.size + n - 1) // n
+            for s in range(1, ref.size + 1, step):
+                e = min(ref.size, s + step - 1)
+                a, b = idx.range_for(ci, s, e, ref.size)
+                jobs.append((ci, s, e, a, b))
     units = piled_bases(ds.reads, jobs, [c.size for c in ds.contigs], params)
     res = [None] * len(jobs)
     it = iter(range(len(jobs)))
@@ -282,6 +291,48 @@ def kmer_bench(eng, ds, params, args, threads, K=31, radius=500):
                                                          f"threads"}
         out["sample_edges_identical"] = edge_set(got, lambda w: w) == want
     return out
+
+
+def extra_workload(config, args, params, device, peak, peaks):
+    """A second workload on its own engine context: device-timed steps (CUDA
+    events, after warm-up) and the walk kernel's roofline, as for the main one."""
+    from pilon_gb300 import synth
+    from pilon_gb300.engine import Engine
+    from pilon_gb300.regions import plan_regions
+    ds = synth.generate(config, args.scale)
+    lens = [c.size for c in ds.contigs]
+    regions = plan_regions(ds.reads, lens)
+    units = piled_bases(ds.reads, regions, lens, params)
+    walk_bytes = walk_algorithmic_bytes(ds.reads, regions)
+    eng = Engine(device)
+    try:
+        eng.set_reference(ds.contigs)
+        eng.set_reads(ds.reads)
+        from pilon_gb300.autotune import tune
+        best, _ = tune(eng, regions, params, f"{ds.workload.name}:{args.scale}:1", batched=True)
+        for _ in range(args.warmup):
+            eng.pileup_regions(regions, params, batched=True)
+        eng.sync()
+        tot, walk = [], []
+        for _ in range(max(3, min(args.steps, 20))):
+            eng.pileup_regions(regions, params, batched=True)
+            w, t, _ = eng.last_kernel_ms()
+            tot.append(t)
+            walk.append(w)
+        eng.sync()
+    finally:
+        eng.close()
+    walk_s = sum(walk) / len(walk) / 1e3
+    achieved = walk_bytes / walk_s / 1e9
+    return {"key": "bacterial_5mb" if config == 2 else f"workload_{config}", "workload": ds.workload.name,
+            "value": units * len(tot) / (sum(tot) / 1e3) / 1e9, "unit": UNIT, "ms_per_step": sum(tot) / len(tot),
+            "piled_bases_per_step": units, "steps": len(tot),
+            "tuning": {"tile_width": best[0], "warps": best[1], "variant": best[2]},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": roofline_traffic(ds.workload.name, units), "kernel": "k_walk",
+                         "algorithmic_bytes_per_launch": walk_bytes, "walk_ms": walk_s * 1e3,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback"},
+            "timing": "CUDA events on the engine stream, inputs resident in HBM (larger than L2)"}
 
 
 def ds_regions(ds):
@@ -376,7 +427,10 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--config", type=int, default=3)
+    ap.add_argument("--extra-config", type=int, default=-1, help="a second workload measured the same way "
+                    "(device-timed steps and the walk roofline); default 2 when --config is 3, 0 = none")
+    ap.add_argument("--no-parity", action="store_true", help="skip the full-size comparison with the oracle")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--batched", type=int, default=1)
@@ -406,9 +460,10 @@ def main():
         if rank != 0:
             return
         ds = synth.generate(args.config, args.scale)
+        ref_regions = plan_regions(ds.reads, [c.size for c in ds.contigs])
         samples = []
         for k in range(args.warmup + args.steps):
-            units, sec, njobs = oracle_sample(ds, params, threads)
+            units, sec, njobs = oracle_sample(ds, params, threads, ref_regions)
             if k >= args.warmup:
                 samples.append((units, sec))
         units = sum(u for u, _ in samples)
@@ -598,10 +653,32 @@ def main():
             bam_decode = {"error": f"{type(ex).__name__}: {ex}"}
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu:
-        u, sec, njobs = oracle_sample(ds, params, threads)
+        u, sec, njobs = oracle_sample(ds, params, threads, regions)
+        same = njobs == len(regions) and u == units
         cpu = {"value": u / sec / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"the whole workload split into {njobs} regions on {threads} host threads, one pass"}
+               "sample": (f"the whole workload on the GPU arm's {njobs} regions" if same else
+                          f"the whole workload split into {njobs} regions") + f" on {threads} host threads, one pass",
+               "same_units_as_gpu": same}
+        if not args.no_parity:
+            # every region of the full-size workload against the oracle (the
+            # checker), outside the timed region
+            from oracle.parity import full_parity
+            t0 = time.perf_counter()
+            try:
+                n_reg, n_pos = full_parity(eng, ds, params, regions, threads, batched=bool(args.batched))
+                parity = {"identical": True, "regions": n_reg, "positions": n_pos}
+            except AssertionError as ex:
+                parity = {"identical": False, "first_difference": str(ex)[:300]}
+            parity.update({"workload": ds.workload.name, "path": "batched" if args.batched else "per-region",
+                           "compared": "every pileup counter, call flag, score, indel length and string and "
+                                       "region statistic of every region, bit for bit",
+                           "seconds": time.perf_counter() - t0})
+    extra = None
+    xc = args.extra_config if args.extra_config >= 0 else (2 if args.config == 3 else 0)
+    if xc and xc != args.config and rank == 0:
+        extra = extra_workload(xc, args, params, local, peak, peaks)
     eng.close()
     if rank != 0:
         return
@@ -626,6 +703,10 @@ def main():
         "cpu_baseline": cpu,
     }
     line["break_candidates"] = breaks
+    if parity:
+        line["parity_full"] = parity
+    if extra:
+        line[extra.pop("key")] = extra
     if bam_decode:
         line["bam_decode"] = bam_decode
     if kmer:
