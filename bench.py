@@ -364,19 +364,21 @@ def max_over_ranks(dist, v):
 
 
 def serve_bench(args, dist, rank, ws, local, params):
-    """Serving: Poisson arrivals (lambda = 200/s) of region-polish requests of
-    10 kb - 1 Mb (log-uniform) against a device-resident read store of the
-    many-contig workload; continuous batching vs the plain per-request path."""
+    """Serving through the C ABI (pg_serve_*): Poisson arrivals (lambda = 200/s)
+    of region-polish requests of 10 kb - 1 Mb (log-uniform) against the
+    device-resident read store of the many-contig workload; continuous batching
+    admitted by device bytes vs the plain path (one request per batch,
+    per-region launches), then the same at a rate that saturates the plain
+    path, for the throughput of both."""
     from pilon_gb300 import synth
     from pilon_gb300.serve import Server, poisson_requests, run_load
     ds = synth.generate(3, args.scale)
     lens = [c.size for c in ds.contigs]
-    sched = poisson_requests(lens, rate=args.rate, duration=args.duration)
     m = ds.reads.aligned_bases()
     from pilon_gb300.regions import ReadIndex
     idx = ReadIndex(ds.reads, len(ds.contigs))
 
-    def summary(res, wall, label, server):
+    def summary(sched, res, wall, label, batches):
         ok = [r for r in res if not isinstance(r, Exception)]
         lat = np.array([r.latency for r in ok]) * 1e3
         units = 0
@@ -387,38 +389,49 @@ def serve_bench(args, dist, rank, ws, local, params):
                 "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
                 "throughput_req_s": len(res) / wall, "gbases_per_s": units / wall / 1e9, "wall_s": wall,
-                "batches": server.batches}
+                "batches": batches}
+
+    def run(rate, duration, batched_path):
+        sched = poisson_requests(lens, rate=rate, duration=duration)
+        kw = dict(n_workers=args.workers, budget_bytes=args.budget) if batched_path else \
+            dict(n_workers=1, batched=False, max_batch=1)
+        srv = Server(ds.names, ds.contigs, ds.reads, params, device=local, **kw)
+        try:
+            run_load(srv, poisson_requests(lens, rate=rate, duration=min(1.0, duration), seed=99))  # warm-up
+            b0 = srv.batches
+            res, wall = run_load(srv, sched)
+            label = (f"continuous batching, {args.workers} contexts, {args.budget / 2**30:.1f} GiB budget"
+                     if batched_path else "one request per batch, per-region launches")
+            out = summary(sched, res, wall, label, srv.batches - b0)
+            if batched_path:
+                out["peak_in_flight_bytes"] = srv.peak_in_flight_bytes()
+            return out, res
+        finally:
+            srv.close()
+
     out = {}
-    srv = Server(ds.names, ds.contigs, ds.reads, params, n_workers=args.workers, device=local)
-    try:
-        run_load(srv, poisson_requests(lens, rate=args.rate, duration=min(1.0, args.duration), seed=99))  # warm-up
-        srv.batches = 0
-        res, wall = run_load(srv, sched)
-        out["batched"] = summary(res, wall, f"continuous batching, {args.workers} contexts", srv)
-    finally:
-        srv.close()
-    plain = Server(ds.names, ds.contigs, ds.reads, params, n_workers=1, budget_positions=1, batched=False,
-                   device=local)
-    try:
-        run_load(plain, poisson_requests(lens, rate=args.rate, duration=min(1.0, args.duration), seed=99))
-        plain.batches = 0
-        pres, pwall = run_load(plain, sched)
-        out["plain"] = summary(pres, pwall, "one request at a time, per-region launches", plain)
-    finally:
-        plain.close()
+    out["batched"], res = run(args.rate, args.duration, True)
+    out["plain"], pres = run(args.rate, args.duration, False)
     same = all((isinstance(a, Exception) and isinstance(b, Exception)) or
                (not isinstance(a, Exception) and not isinstance(b, Exception) and a.fasta == b.fasta and
                 a.changes == b.changes and a.vcf == b.vcf) for a, b in zip(res, pres))
+    sat = None
+    if args.saturate_rate > 0:
+        sb, _ = run(args.saturate_rate, args.saturate_duration, True)
+        sp, _ = run(args.saturate_rate, args.saturate_duration, False)
+        sat = {"rate_per_s": args.saturate_rate, "duration_s": args.saturate_duration, "batched": sb, "plain": sp,
+               "throughput_batched_over_plain": sb["throughput_req_s"] / sp["throughput_req_s"]}
     if rank != 0:
         return
     b = out["batched"]
     line = {"metric": "served-region latency p99 (ms) at lambda = %g/s" % args.rate, "value": b["p99_ms"],
-            "unit": "ms", "higher_is_better": False, "n_gpus": ws, "steps": len(sched), "warmup": 1,
+            "unit": "ms", "higher_is_better": False, "n_gpus": ws, "steps": b["requests"], "warmup": 1,
             "ms_per_step": b["mean_ms"], "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64",
             "data": "synthetic (seeded)", "config": {"workload": "serving over draft-3000-contigs-40x",
             "genome_bp": int(sum(lens)), "reads": ds.reads.n_reads, "rate_per_s": args.rate,
             "duration_s": args.duration, "request_bp": "10 kb - 1 Mb log-uniform"},
-            "served": out, "identical_outputs_batched_vs_plain": same}
+            "served": out, "identical_outputs_batched_vs_plain": same, "saturated": sat,
+            "path": "C ABI server (pg_serve_submit / pg_serve_poll), latency from submit to answer"}
     print(json.dumps(line))
 
 
@@ -445,6 +458,10 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="serving: requests per second")
     ap.add_argument("--duration", type=float, default=10.0, help="serving: seconds of arrivals")
     ap.add_argument("--workers", type=int, default=2, help="serving: engine contexts")
+    ap.add_argument("--budget", type=float, default=float(8 << 30), help="serving: device bytes in flight")
+    ap.add_argument("--saturate-rate", type=float, default=1500.0, help="serving: a rate that saturates the "
+                    "plain path (0 = skip)")
+    ap.add_argument("--saturate-duration", type=float, default=3.0)
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

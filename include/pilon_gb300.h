@@ -303,6 +303,93 @@ pg_status pg_sync(pg_ctx *ctx);
  * recording.  No counterpart in the reference (a measurement hook). */
 pg_status pg_graph_replays(pg_ctx *ctx, int32_t *replays);
 
+/* ---- serving ------------------------------------------------------------
+ * Region-polish requests with continuous batching.  A request is the work of
+ * `pilon --targets contig:start-stop --fix snps,indels --vcf --changes` on one
+ * region (S/GenomeFile.scala:215-250): GenomeRegion.processBam, postProcess,
+ * identifyAndFixIssues and fixIssues (S/GenomeRegion.scala:214-414, 557-621),
+ * writeChanges (:645-657) and Vcf.writeRecord (S/Vcf.scala:74-176).
+ *
+ * pg_serve_open uploads the reference and the read store once and keeps them
+ * resident on the device; n_workers host threads each own an engine context
+ * (own CUDA stream and buffers) over that store.  A free worker takes, from
+ * the head of the queue, every request whose device bytes still fit
+ * hbm_budget beside the batches already running (at most max_batch when it is
+ * > 0) and runs them as one pg_pileup_regions call; requests arriving
+ * meanwhile wait until memory and a worker free up, and the batches of
+ * different workers overlap on the GPU.  A request's device bytes are 116 per
+ * position of the region plus 16 per read of its query window (the pileup and
+ * call records and per-read state of one call); a request needing more than
+ * the whole budget is refused at submit with PG_ERR_NOMEM.  Each worker
+ * context keeps its buffers between batches, and also holds event buffers
+ * sized once from the store.
+ *
+ * Each answer holds the region's polished bases (no FASTA header or line
+ * breaks), its changes-file lines (the target as its own output entry) and its
+ * VCF records whose ALT is not "." (no header; no <DUP> records).  A target on
+ * which the reference throws (PG_ERR_INDEX, see pg_pileup_regions) fails only
+ * that request.  The server object is thread-safe. */
+typedef struct pg_server pg_server;
+
+typedef struct pg_serve_config {
+  int32_t device;
+  int32_t n_workers;       /* engine contexts working at once, 1..64 */
+  int64_t hbm_budget;      /* device bytes the requests in flight may need together */
+  int32_t max_batch;       /* most requests in one batch; 0 = no limit */
+  int32_t batched;         /* 1: one batched launch per batch; 0: the plain per-region path */
+  int32_t fix_snps;        /* --fix snps (with amb through pg_params.fix_amb) */
+  int32_t fix_indels;      /* --fix indels */
+  int32_t iupac;           /* --iupac */
+  int32_t diploid;         /* --diploid */
+  int32_t vcf_qe;          /* --vcfqe */
+  int32_t pad_;
+} pg_serve_config;
+
+typedef struct pg_request {
+  int32_t contig;          /* index into the contigs given to pg_serve_open */
+  int32_t start, stop;     /* 1-based, inclusive */
+  int32_t pad_;
+} pg_request;
+
+typedef struct pg_result {
+  int32_t status;          /* PG_OK or this request's error */
+  int32_t batch;           /* batch number it ran in, from 1 */
+  const char *fasta;       /* polished bases of the region */
+  int64_t fasta_len;
+  const char *changes;     /* changes-file lines */
+  int64_t changes_len;
+  const char *vcf;         /* VCF records with an ALT */
+  int64_t vcf_len;
+  const char *message;     /* why the request failed, else "" */
+  double queue_ms;         /* submit -> start of its batch */
+  double run_ms;           /* start of its batch -> answered */
+  double latency_ms;       /* submit -> answered */
+  int64_t device_bytes;    /* the bytes it was admitted with */
+} pg_result;
+
+/* Fills the defaults: device 0, 2 workers, an 8 GiB budget, batched,
+ * --fix snps,indels. */
+void pg_default_serve_config(pg_serve_config *cfg);
+/* Starts a server over one coordinate-sorted read store (host arrays, copied
+ * to the device).  Like pg_open, *srv is set even on failure so that
+ * pg_serve_error can say why; pg_serve_close frees it. */
+pg_status pg_serve_open(pg_server **srv, const pg_serve_config *cfg, const pg_params *params, int32_t n_contigs,
+                        const char *const *names, const int64_t *lens, const uint8_t *const *bases,
+                        const pg_reads *host_reads);
+/* Queues one request; *ticket identifies it. */
+pg_status pg_serve_submit(pg_server *srv, const pg_request *req, uint64_t *ticket);
+/* The request's answer: waits up to wait_ms (-1: until answered); returns
+ * PG_ERR_STATE when it is not answered yet.  The strings stay valid until
+ * pg_serve_release of the ticket. */
+pg_status pg_serve_poll(pg_server *srv, uint64_t ticket, int32_t wait_ms, pg_result *out);
+/* Frees an answered request's result. */
+pg_status pg_serve_release(pg_server *srv, uint64_t ticket);
+/* Batches run so far, device bytes of the requests in flight and their peak. */
+pg_status pg_serve_stats(pg_server *srv, int64_t *batches, int64_t *in_flight_bytes, int64_t *peak_in_flight_bytes);
+const char *pg_serve_error(const pg_server *srv);
+/* Answers every queued request, then stops the workers and frees the server. */
+void pg_serve_close(pg_server *srv);
+
 /* ---- physical-coverage scan without device allocation ----------------------
  * This entry point has no counterpart in the reference.  It is for callers
  * that cannot let a library allocate device memory: a host whose own pool

@@ -46,6 +46,10 @@ def lib():
         L.or_kmer_tally.restype = C.c_int64
         L.or_kmer_tally.argtypes = [C.POINTER(_abi.pg_reads), C.POINTER(_abi.pg_params), C.c_void_p, C.c_int32,
                                     C.c_int32, C.c_int32, C.c_void_p, C.c_int64]
+        L.or_target.restype = C.c_int
+        L.or_target.argtypes = [C.POINTER(_abi.pg_reads), C.POINTER(_abi.pg_params), C.c_char_p, C.c_void_p,
+                                C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.c_int32,
+                                C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_char_p, C.c_char_p, C.c_char_p]
         L.or_java_format2.restype = C.c_int
         L.or_java_format2.argtypes = [C.c_double, C.c_char_p, C.c_int]
         _lib = L
@@ -129,6 +133,24 @@ def polish(reads, params, names, contigs, out_prefix, chunk_size=10_000_000, fix
                      (out_prefix + ".changes").encode(), vcf_date.encode(), vcf_source.encode(), vcf_args.encode(),
                      vcf_ref.encode())
     return rc
+
+
+def target(reads, params, name, contig, contig_id, start, stop, read_begin, read_end, fix_snps=True,
+           fix_indels=True, iupac=False, diploid=False, vcf_qe=False):
+    """`pilon --targets name:start-stop` on one region: returns (status, fixed
+    bases, changes text, VCF records without header)."""
+    import tempfile
+    L = lib()
+    contig = np.ascontiguousarray(contig, np.uint8)
+    ab = reads.to_abi()
+    with tempfile.TemporaryDirectory() as d:
+        paths = [os.path.join(d, x) for x in ("bases", "changes", "vcf")]
+        rc = L.or_target(C.byref(ab), C.byref(params), name.encode(), contig.ctypes.data, contig.size, contig_id,
+                         start, stop, read_begin, read_end, int(fix_snps), int(fix_indels), int(iupac),
+                         int(diploid), int(vcf_qe), *[x.encode() for x in paths])
+        if rc:
+            return rc, None, None, None
+        return rc, open(paths[0], "rb").read(), open(paths[1]).read(), open(paths[2], "rb").read()
 
 
 def region_breaks(reads, params, contig, contig_id, start, stop, read_begin=0, read_end=None):

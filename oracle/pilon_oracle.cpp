@@ -1142,6 +1142,51 @@ int or_polish(const pg_reads* R, const pg_params* params, int32_t n_contigs, con
   return 0;
 }
 
+// One --targets region end to end (S/GenomeFile.scala:215-250): processBam,
+// postProcess, identifyAndFixIssues; writes the fixed bases (no header, no line
+// breaks), the region's changes lines (the target is its own output entry, so
+// the offset is 0) and the region's VCF records (GenomeRegion.writeVcf, no
+// header).  Returns 0, or PG_ERR_INDEX where the reference would throw.
+int or_target(const pg_reads* R, const pg_params* params, const char* name, const uint8_t* contig, int64_t contig_len,
+              int32_t contig_id, int32_t start, int32_t stop, int64_t rb, int64_t re, int32_t fix_snps,
+              int32_t fix_indels, int32_t iupac, int32_t diploid, int32_t vcf_qe, const char* bases_path,
+              const char* changes_path, const char* vcf_path) {
+  Params P = toParams(params);
+  try {
+    GenomeRegion g(name, contig_id, contig, contig_len, start, stop, P);
+    g.processBam(R, rb, re);
+    g.postProcess();
+    g.identifyAndFixIssues(fix_snps, fix_indels, iupac, P.longRead != 0);
+    std::string nm = name;
+    std::string sep = nm.find('|') == std::string::npos ? "_" : (nm.back() == '|' ? "" : "|");
+    std::string newName = nm + sep + "pilon";
+    if (FILE* fb = bases_path ? fopen(bases_path, "wb") : nullptr) {
+      fwrite(g.bases.data(), 1, g.bases.size(), fb);
+      fclose(fb);
+    }
+    if (FILE* fc = changes_path ? fopen(changes_path, "w") : nullptr) {
+      int32_t delta = 0;
+      for (auto& fx : g.allFixes()) {
+        int32_t newLoc = fx.locus + delta;
+        std::string o = regionString(g.name, fx.locus, fx.locus + (int32_t)fx.was.size() - 1);
+        std::string nw = regionString(newName, newLoc, newLoc + (int32_t)fx.patch.size() - 1);
+        fprintf(fc, "%s %s %s %s\n", o.c_str(), nw.c_str(), fx.was.empty() ? "." : fx.was.c_str(),
+                fx.patch.empty() ? "." : fx.patch.c_str());
+        delta += (int32_t)fx.patch.size() - (int32_t)fx.was.size();
+      }
+      fclose(fc);
+    }
+    if (FILE* fv = vcf_path ? fopen(vcf_path, "w") : nullptr) {
+      VcfWriter vw{fv, (bool)diploid, (bool)vcf_qe, P};
+      vw.writeRegion(g);
+      fclose(fv);
+    }
+  } catch (IndexError&) {
+    return PG_ERR_INDEX;
+  }
+  return 0;
+}
+
 // Break candidates of one region (possibleBreaks, S/GenomeRegion.scala:719-720),
 // after process + postProcess.  Writes (start, stop) loci; returns the count.
 int32_t or_region_breaks(const pg_reads* R, const pg_params* params, const uint8_t* contig, int64_t contig_len,

@@ -107,6 +107,27 @@ class pg_kmer_edge(C.Structure):
     ]
 
 
+class pg_serve_config(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32), ("n_workers", C.c_int32), ("hbm_budget", C.c_int64), ("max_batch", C.c_int32),
+        ("batched", C.c_int32), ("fix_snps", C.c_int32), ("fix_indels", C.c_int32), ("iupac", C.c_int32),
+        ("diploid", C.c_int32), ("vcf_qe", C.c_int32), ("pad_", C.c_int32),
+    ]
+
+
+class pg_request(C.Structure):
+    _fields_ = [("contig", C.c_int32), ("start", C.c_int32), ("stop", C.c_int32), ("pad_", C.c_int32)]
+
+
+class pg_result(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32), ("batch", C.c_int32), ("fasta", C.c_void_p), ("fasta_len", C.c_int64),
+        ("changes", C.c_void_p), ("changes_len", C.c_int64), ("vcf", C.c_void_p), ("vcf_len", C.c_int64),
+        ("message", C.c_char_p), ("queue_ms", C.c_double), ("run_ms", C.c_double), ("latency_ms", C.c_double),
+        ("device_bytes", C.c_int64),
+    ]
+
+
 class pg_break(C.Structure):
     _fields_ = [("region", C.c_int32), ("start", C.c_int32), ("stop", C.c_int32), ("pad_", C.c_int32)]
 
@@ -137,6 +158,8 @@ EXPORTED = [
     "pg_fetch_stats", "pg_fetch_region", "pg_set_tuning", "pg_kmer_tally",
     "pg_last_kernel_ms", "pg_sync", "pg_phys_cov_scan_static", "pg_format_vcf", "pg_find_breaks",
     "pg_kmer_tally_breaks", "pg_fetch_all", "pg_graph_replays",
+    "pg_default_serve_config", "pg_serve_open", "pg_serve_submit", "pg_serve_poll", "pg_serve_release",
+    "pg_serve_stats", "pg_serve_error", "pg_serve_close",
 ]
 
 PG_STATIC_SCAN_MAX_POSITIONS = 16777216

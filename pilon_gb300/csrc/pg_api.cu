@@ -50,6 +50,8 @@ struct pg_ctx {
   DevBuf rd[15];
   ReadExtent ext{};
   DevBuf d_ext, rdesc;
+  DevBuf ent_off, ent_sums, entries;  // walk entries of the read store
+  int64_t n_entries = 0;
   // per-call buffers
   DevBuf regions, walk_tiles, call_tile_region, chunks, stats;
   DevBuf rec_count, rec_qsum, rec_i32[10], rec_call, rec_score, rec_indel_len, rec_ins_str, rec_ev_end;
@@ -250,7 +252,7 @@ void pg_close(pg_ctx* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
   }
-  DevBuf* all[] = {&c->ref, &c->d_ext, &c->rdesc, &c->regions, &c->walk_tiles, &c->call_tile_region, &c->chunks, &c->stats,
+  DevBuf* all[] = {&c->ref, &c->d_ext, &c->rdesc, &c->ent_off, &c->ent_sums, &c->entries, &c->regions, &c->walk_tiles, &c->call_tile_region, &c->chunks, &c->stats,
                    &c->rec_count, &c->rec_qsum, &c->rec_call, &c->rec_score, &c->rec_indel_len, &c->rec_ins_str,
                    &c->rec_ev_end, &c->cand_count, &c->cand_off, &c->tile_sums,
                    &c->events, &c->events_sorted, &c->cands, &c->pool, &c->counters, &c->run_max, &c->staging_dev,
@@ -359,6 +361,21 @@ static pg_status finish_reads(pg_ctx* c) {
     return fail(c, PG_ERR_ARG, "read %llu: CIGAR, base or quality offsets leave their arrays",
                 (unsigned long long)c->ext.bad_read - 1);
   if (c->ext.unsorted) return fail(c, PG_ERR_ARG, "reads are not sorted by position within each reference");
+  // the walk entries (one per M/=/X or S operator), made once per read store
+  const int64_t n = c->R.n;
+  if ((s = ensure(c, c->ent_off, 8 * (size_t)(n + 1)))) return s;
+  if ((s = ensure(c, c->ent_sums, 8 * (size_t)((n + 1 + 1023) / 1024 + 2)))) return s;
+  c->R.entry_off = P<int64_t>(c->ent_off);
+  launch_entry_count(c->R, P<int64_t>(c->ent_off), P<int64_t>(c->ent_sums), c->stream);
+  CK(cudaGetLastError());
+  int64_t total = 0;
+  CK(cudaMemcpyAsync(&total, P<int64_t>(c->ent_off) + n, 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if ((s = ensure(c, c->entries, 48 * (size_t)std::max<int64_t>(total, 1)))) return s;
+  c->R.entries = P<int4>(c->entries);
+  c->n_entries = total;
+  launch_entry_fill(c->R, P<int64_t>(c->ent_off), P<int4>(c->entries), c->stream);
+  CK(cudaGetLastError());
   c->mode_mq1 = 0;
   for (uint32_t b = 1, best = 0; b <= 256; b++)
     if (c->ext.mq1_hist[b] > best) { best = c->ext.mq1_hist[b]; c->mode_mq1 = b; }

@@ -42,8 +42,20 @@ struct Reads {  // device pointers of the read store
   // simple: the CIGAR is [H][S] M|=|X [S][H] with clips < 65536 and 0 <= adjMq <= 255;
   // a read that is not simple has d1.x = 1 when its CIGAR holds an I or D, else 0.
   const int4* desc;
+  // Walk entries, made once per read store by k_entry_fill: one per M/=/X or S
+  // operator of every read, in read order; the entries of read i are
+  // [entry_off[i], entry_off[i + 1]).  Three int4 per entry:
+  //   e0 = {pos, end (alignment end, or pos when unmapped), first locus of the
+  //         operator (S: clipStart of S/PileUpRegion.scala:195), length}
+  //   e1 = {read offset of the operator, read length, adjMq + 1, meta}
+  //   e2 = {qual_off + read offset (int64), 2 * seq_off + read offset (int64, a nibble index)}
+  //   meta = mapq | (flag >> 8 & 7) << 8 (secondary, qc-fail, duplicate) |
+  //          kEntClip | kEntHasQual | kEntPairOk
+  const int4* entries;
+  const int64_t* entry_off;   // n + 1 offsets
 };
 constexpr uint32_t kDescHasQual = 1u << 30, kDescSimple = 1u << 31, kDescPairOk = 1u << 30;
+constexpr uint32_t kEntClip = 1u << 11, kEntHasQual = 1u << 12, kEntPairOk = 1u << 13;
 
 struct RegionDev {       // per region, device copy
   int32_t contig, start, stop, size;
@@ -71,7 +83,7 @@ struct StatsDev {        // per region, accumulated on the device
 
 struct WalkTile {
   int32_t region, lo, len, pad;
-  int64_t read_lo, read_hi;
+  int64_t ent_lo, ent_hi;  // walk entries of the reads that can touch the tile
 };
 
 struct ReadChunk {       // reads [lo, hi) fed to region `region`
@@ -405,6 +417,11 @@ struct CallArgs {
 };
 
 void launch_read_extent(const Reads& R, ReadExtent* out, int4* desc, cudaStream_t s);
+// Builds R.entry_off (n + 1 int64; `sums` holds (n + 1) / 1024 + 2 int64 of
+// scan scratch) and R.entries (3 int4 per entry), after the store passed
+// k_read_extent's checks.  Returns nothing: the host reads entry_off[n].
+void launch_entry_count(const Reads& R, int64_t* entry_off, int64_t* sums, cudaStream_t s);
+void launch_entry_fill(const Reads& R, const int64_t* entry_off, int4* entries, cudaStream_t s);
 void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tiles, int32_t n_tiles,
                         const ReadExtent* ext, StatsDev* stats, cudaStream_t s);
 void launch_walk(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s);

@@ -18,6 +18,7 @@
 #include <algorithm>
 
 #include "pg_internal.cuh"
+#include "pg_format.cuh"
 
 namespace pg {
 
@@ -147,6 +148,78 @@ void launch_read_extent(const Reads& R, ReadExtent* out, int4* desc, cudaStream_
 }
 
 // ---------------------------------------------------------------------------
+// Walk entries: one per M/=/X or S operator (the operators whose bases the walk
+// adds, S/PileUpRegion.scala:184-206), with everything of the read the walk
+// needs beside it, so that a walk tile reads its entries as one coalesced
+// stream and never interprets a CIGAR.
+__device__ inline bool entry_op(int op) { return op == 0 || op == 4 || op == 7 || op == 8; }
+
+__global__ void k_entry_count(Reads R, int64_t* cnt) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= R.n; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t n = 0;
+    if (i < R.n) {
+      const int64_t co = R.cigar_off[i];
+      const int nc = R.n_cigar[i];
+      for (int k = 0; k < nc; k++) n += entry_op((int)(R.cigar[co + k] & 15u));
+    }
+    cnt[i] = n;  // entry n of the array is 0: after the exclusive scan it holds the total
+  }
+}
+
+__global__ void k_entry_fill(Reads R, const int64_t* off, int4* E) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < R.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t pos = R.pos[i];
+    const uint16_t fl = R.flag[i];
+    const int32_t end = (fl & 0x4) ? pos : R.aend[i];
+    const int32_t mq = R.mapq[i], length = R.l_seq[i];
+    const int64_t co = R.cigar_off[i], qo = R.qual_off[i], so = R.seq_off[i];
+    const int nc = R.n_cigar[i];
+    int32_t clipped = 0;
+    for (int k = 0; k < nc; k++) {
+      const uint32_t w = R.cigar[co + k];
+      if ((w & 15u) == 4u) clipped += (int32_t)(w >> 4);
+    }
+    // PileUpRegion.addRead's setup (S/PileUpRegion.scala:103-142)
+    const int32_t mq1 = roundDivI(wmul(mq, length - clipped), length) + 1;
+    const bool hasQual = length > 0 && R.qual[qo] != 0xFF;
+    const bool pairOk = !(fl & 0x1) || ((fl & 0x2) && R.ref_id[i] == R.mate_ref_id[i]);
+    const uint32_t meta = (uint32_t)mq | ((uint32_t)(fl >> 8) & 7u) << 8 | (hasQual ? kEntHasQual : 0u) |
+                          (pairOk ? kEntPairOk : 0u);
+    int64_t e = off[i];
+    int32_t ro = 0, fo = 0;
+    for (int k = 0; k < nc; k++) {
+      const uint32_t w = R.cigar[co + k];
+      const int32_t len = (int32_t)(w >> 4);
+      const int op = (int)(w & 15u);
+      const int32_t locus = pos + fo;
+      if (entry_op(op)) {
+        const bool clip = op == 4;
+        const int32_t first = clip && ro == 0 ? locus - len : locus;  // clipStart for S
+        const int64_t qa = qo + ro, na = 2 * so + ro;
+        E[3 * e] = make_int4(pos, end, first, len);
+        E[3 * e + 1] = make_int4(ro, length, mq1, (int32_t)(meta | (clip ? kEntClip : 0u)));
+        E[3 * e + 2] = make_int4((int32_t)(uint32_t)qa, (int32_t)(qa >> 32), (int32_t)(uint32_t)na, (int32_t)(na >> 32));
+        e++;
+      }
+      if (consumes_read(op)) ro += len;
+      if (consumes_ref(op)) fo += len;
+    }
+  }
+}
+
+void launch_entry_count(const Reads& R, int64_t* entry_off, int64_t* sums, cudaStream_t s) {
+  const int blocks = (int)std::min<int64_t>((R.n + 1 + 255) / 256, 152 * 16);
+  k_entry_count<<<blocks, 256, 0, s>>>(R, entry_off);
+  launch_scan64(entry_off, R.n + 1, sums, s);
+}
+
+void launch_entry_fill(const Reads& R, const int64_t* entry_off, int4* entries, cudaStream_t s) {
+  if (R.n == 0) return;
+  const int blocks = (int)std::min<int64_t>((R.n + 255) / 256, 152 * 16);
+  k_entry_fill<<<blocks, 256, 0, s>>>(R, entry_off, entries);
+}
+
+// ---------------------------------------------------------------------------
 // First index in [lo, hi) whose position is >= v (hi if none), by a warp: each
 // step the 32 lanes sample the range at even strides and keep the stretch
 // between the last sample below v and the next one, so a range of n reads
@@ -194,8 +267,8 @@ __global__ void k_tile_ranges(Reads R, const RegionDev* regions, WalkTile* tiles
   const int64_t rlo = warp_lower_bound_pos(R.pos, g.read_begin, g.read_end, a, lane);
   const int64_t rhi = warp_lower_bound_pos(R.pos, rlo, g.read_end, b, lane);
   if (lane == 0) {
-    T.read_lo = rlo;
-    T.read_hi = rhi;
+    T.ent_lo = R.entry_off[rlo];
+    T.ent_hi = R.entry_off[rhi];
   }
 }
 
@@ -223,15 +296,15 @@ void launch_tile_ranges(const Reads& R, const RegionDev* regions, WalkTile* tile
 // defaultQual outside a byte); tiles with more reads run several passes and add
 // each pass's sums into the records.
 //
-// Each warp takes the tile's reads 32 at a time.  Every lane first builds the
-// descriptor of one read in registers: the filters of BamFile.process, the
-// clipped-base count and adjusted mapping quality, the CIGAR shape and, for
-// reads whose CIGAR is [S] M|=|X [S] (optional H), everything the walk needs:
-// the trusted offsets clipped to the tile, the pointers to the read's
-// qualities and bases, the nibble parity.  The warp then walks these simple
-// reads G lanes per read (32 / G reads at once), reading the descriptors by
-// warp shuffle; the few other reads take the general CIGAR loop with the
-// whole warp.  No block-wide barrier runs inside the read loop.
+// Each warp claims the tile's walk entries 32 at a time (one M/=/X or S
+// operator of a read each, made once per read store).  Every lane reads one
+// entry with three coalesced 16-byte loads and reduces it to two words and two
+// addresses: the filters of BamFile.process (query window, validateRead), the
+// trusted offsets of the operator inside the tile, validity and the adjusted
+// mapping quality, or for an S operator its clip positions.  The warp then
+// walks the lanes' entries G lanes per entry (32 / G at once), reading them by
+// warp shuffle.  No CIGAR is interpreted here and no block-wide barrier runs
+// inside the entry loop.
 // PileUp.add of one base (S/PileUp.scala:75-84): dmq = mq + 1 - M.
 template <int T>
 __device__ inline void add_base(uint32_t* sm, int32_t p, uint32_t nib, int32_t qual, int32_t dmq, int32_t min_qual) {
@@ -267,41 +340,26 @@ __device__ inline bool nanopore_exclude(const uint8_t* cref, int32_t x, int32_t 
          cref[x + 2] == 'G';
 }
 
-// descriptor kinds
-enum : uint32_t { kSkip = 0, kFast = 1, kInvalid = 2, kSlow = 3, kComplex = 4 };
+// entry kinds of a lane's word w1
+enum : uint32_t { kSkip = 0, kFast = 1, kInvalid = 2, kSlow = 3, kClip = 4 };
 
-// An M/=/X segment of a read with an I/D/N CIGAR, queued for the chunked walk
-// (24 bytes, per warp in shared memory behind the counters).
-struct SegQ {
-  int64_t read;    // read index
-  int32_t pb;      // segment start minus tile start
-  uint32_t i01;    // trusted in-tile segment offsets [i0, i1), 16 bits each
-  uint32_t mr;     // mq + 1 (9 bits) | read offset of the segment << 9
-  int32_t pad;
-};
-constexpr int kSegQueue = 48;
-
-// clip word of a queued segment: trail 0xffff marks "no clips" (simple reads
-// have trailing clips below 0xffff)
-constexpr uint32_t kSegmentClip = 0xffffu << 16;
-
-// MINB: resident CTAs of 512 threads the register allocation must allow
-// (2: up to 64 registers per thread).  G: lanes per simple read (8, 16, 32).
-// dynamic shared memory of a walk CTA: counters and segment queues
+// dynamic shared memory of a walk CTA: the counters and 4 words of padding
 template <int T>
-constexpr size_t walk_smem(int warps) {
-  return (size_t)(11 * T + 4) * sizeof(uint32_t) + (size_t)warps * kSegQueue * sizeof(SegQ);
+constexpr size_t walk_smem() {
+  return (size_t)(11 * T + 4) * sizeof(uint32_t);
 }
 
+// MINB: resident CTAs of 512 threads the register allocation must allow
+// (2: up to 64 registers per thread).  G: lanes per entry (4, 8, 16, 32).
 template <int T, int MINB, int G>
 __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_begin, int32_t tile_end) {
   constexpr int kWords = 11 * T;
+  static_assert((kWords + 4) % 4 == 0, "counters are cleared 16 bytes at a time");
   extern __shared__ __align__(16) uint32_t sm_raw[];
   uint32_t* sm = sm_raw + 4;  // 4 words of padding in front of the counters
-  SegQ* segq = reinterpret_cast<SegQ*>(sm_raw + kWords + 4) + (threadIdx.x >> 5) * kSegQueue;
   __shared__ unsigned long long s_bc;
-  __shared__ uint8_t s_perm[16][32];  // per warp: lane of the read in each round slot
-  __shared__ int32_t s_next;          // next unclaimed read of the pass (offset)
+  __shared__ uint8_t s_perm[16][32];  // per warp: lane of the entry in each round slot
+  __shared__ int32_t s_next;          // next unclaimed entry of the pass (offset)
   uint32_t* s_bad = sm + 9 * T;  // md = sm, qx = sm + 4T, mx = sm + 8T
   uint32_t* s_clip = sm + 10 * T;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -315,6 +373,11 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
   const uint32_t minq4 = (uint32_t)min(max(P.min_qual, 0), 127) * 0x01010101u;
   const uint32_t okall = P.min_qual <= 127 ? 0xffffffffu : 0u;
   const int64_t per_pass = a.reads_per_pass;
+  // validateRead (S/BamFile.scala:101-105) on the entry's flag bits 0x100
+  // (always dropped), 0x200 (unless --nonpf) and 0x400 (unless --duplicates)
+  const uint32_t drop = (1u | (P.nonpf ? 0u : 2u) | (P.duplicates ? 0u : 4u)) << 8;
+  const bool nanopore = P.long_read == PG_NANOPORE;
+  const int4* __restrict__ ent = R.entries;
 
   for (int32_t t = tile_begin + blockIdx.x; t < tile_end; t += gridDim.x) {
     const WalkTile tile = a.tiles[t];
@@ -324,15 +387,16 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
     unsigned long long bc = 0;
     if (threadIdx.x == 0) s_bc = 0;
 
-    for (int64_t c0 = tile.read_lo, pass = 0; pass == 0 || c0 < tile.read_hi; c0 += per_pass, pass++) {
-      const int64_t c1 = min(c0 + per_pass, tile.read_hi);
+    for (int64_t c0 = tile.ent_lo, pass = 0; pass == 0 || c0 < tile.ent_hi; c0 += per_pass, pass++) {
+      const int64_t c1 = min(c0 + per_pass, tile.ent_hi);
       const int32_t npass = (int32_t)(c1 - c0);
-      for (int k = threadIdx.x; k < kWords + 4; k += blockDim.x) sm_raw[k] = 0;
+      for (int k = threadIdx.x; k < (kWords + 4) / 4; k += blockDim.x)
+        reinterpret_cast<uint4*>(sm_raw)[k] = make_uint4(0u, 0u, 0u, 0u);
       if (threadIdx.x == 0) s_next = 0;
       __syncthreads();
 
-      // Warps claim batches of the pass's reads as they finish the previous one:
-      // 32 reads while many are left, then 16, then 8, so the warps reach the
+      // Warps claim batches of the pass's entries as they finish the previous
+      // one: 32 while many are left, then 16, then 8, so the warps reach the
       // tile's closing barrier close together.
       while (true) {
         int32_t off = 0, size = 0;
@@ -345,165 +409,74 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
         size = __shfl_sync(FULL, size, 0);
         if (off >= npass) break;
         const int64_t base = c0 + off, bend = min(base + size, c1);
-        // ---- one descriptor per lane
-        const int64_t i = base + lane;
-        uint32_t kind = kSkip, mq1 = 0, clip = 0;   // clip: lead | trail << 16
-        int32_t i0 = 0, i1 = 0, pb = 0, mlen = 0, pos = 0, nc = 0, length = 0, cls = 0;
-        bool valid = false, hasQual = false;
-        const uint8_t* qp = nullptr;
-        const uint8_t* sp = nullptr;
-        int64_t co = 0;
-        if (i < bend) {
-          // every load of the descriptor phase is independent of the others
-          const int4 d0 = R.desc[2 * i], d1 = R.desc[2 * i + 1];
-          const uint16_t fl = R.flag[i];
-          const int32_t mq = R.mapq[i];
-          const int64_t qo = R.qual_off[i], so = R.seq_off[i];
-          pos = d0.x;
-          if (d0.z == g.contig && pos <= g.qe && d0.y >= g.qs && validate_read(fl, P)) {
-            valid = (mq >= P.min_mq) && ((uint32_t)d1.z & kDescPairOk);
-            const int32_t lo = pos - (int32_t)((uint32_t)d1.z & (kDescPairOk - 1u)), hi = pos + d1.w;
-            if (hi >= tileLo && lo <= tileHi) {
-              hasQual = ((uint32_t)d1.y & kDescHasQual) != 0;
-              mq1 = (uint32_t)d0.w;
-              if ((uint32_t)d1.y & kDescSimple) {
-                const int32_t lead = d1.x & 0xffff, trail = (int32_t)((uint32_t)d1.x >> 16);
-                mlen = (int32_t)((uint32_t)d1.y & (kDescHasQual - 1u));
-                length = lead + mlen + trail;
-                // aligned bases at trusted read offsets [flank, length - flank), inside the tile
-                i0 = max(max(tileLo - pos, P.flank - lead), 0);
-                i1 = min(min(tileHi - pos + 1, length - P.flank - lead), mlen);
-                pb = pos - tileLo;
-                clip = (uint32_t)d1.x;
-                qp = R.qual + qo + lead;
-                sp = R.seq + so;
-                if (!valid) kind = kInvalid;
-                else if (hasQual && P.long_read != PG_NANOPORE) kind = kFast;
-                else kind = kSlow;
-                if (valid && i1 > i0) bc += (unsigned long long)(i1 - i0);
-                // position residue (mod 4) of the read's 4-base chunks, which start at
-                // the aligned quality words (see the fast path)
-                cls = (pb + i0 - (int32_t)((uintptr_t)(qp + i0) & 3u)) & 3;
-              } else {
-                kind = kComplex;
-                co = R.cigar_off[i];
-                nc = R.n_cigar[i];
-                length = R.l_seq[i];
-                qp = R.qual + qo;
-                sp = R.seq + so;
+        // ---- one entry per lane, reduced to w0 = first tile position | count << 16,
+        // w1 = kind | flags | (adjMq + 1 or clip positions) << 8, and the quality
+        // byte and nibble index of the first base
+        const int64_t k = base + lane;
+        uint32_t w0 = 0, w1 = kSkip;
+        uint64_t qa = 0, na = 0;
+        int32_t cls = 0;
+        if (k < bend) {
+          const int4 e0 = __ldg(ent + 3 * k), e1 = __ldg(ent + 3 * k + 1), e2 = __ldg(ent + 3 * k + 2);
+          const uint32_t meta = (uint32_t)e1.w;
+          if (e0.x <= g.qe && e0.y >= g.qs && !(meta & drop)) {
+            const int32_t first = e0.z, len = e0.w;
+            if (meta & kEntClip) {
+              // S (S/PileUpRegion.scala:194-206): clips at clipStart and clipEnd, and
+              // every clipped base is added as a bad pair, for valid and invalid reads
+              const int32_t ce = first + len - 1;
+              const int32_t lo = max(first, tileLo), hi = min(ce, tileHi);
+              const bool csin = first >= tileLo && first <= tileHi, cein = ce >= tileLo && ce <= tileHi;
+              if (lo <= hi || csin || cein) {
+                w0 = lo <= hi ? (uint32_t)(lo - tileLo) | (uint32_t)(hi - lo + 1) << 16 : 0u;
+                w1 = kClip | (csin ? 8u : 0u) | (cein ? 16u : 0u) | ((uint32_t)(first - tileLo) & 0xfffu) << 8 |
+                     ((uint32_t)(ce - tileLo) & 0xfffu) << 20;
+              }
+            } else {
+              // M/=/X (S/PileUpRegion.scala:184-193): the trusted read offsets
+              // [flank, length - flank) of the operator, inside the tile
+              const int32_t roff = e1.x, rlen = e1.y, mq1 = e1.z;
+              const int32_t i0 = max(max(tileLo - first, P.flank - roff), 0);
+              const int32_t i1 = min(min(tileHi - first + 1, rlen - P.flank - roff), len);
+              if (i1 > i0) {
+                const bool valid = (int32_t)(meta & 0xffu) >= P.min_mq && (meta & kEntPairOk);
+                const bool hasQual = (meta & kEntHasQual) != 0;
+                if (valid) bc += (unsigned long long)(i1 - i0);
+                const uint32_t kind =
+                    !valid ? kInvalid : (hasQual && !nanopore && mq1 >= 1 && mq1 <= 256) ? kFast : kSlow;
+                const int32_t pb = first + i0 - tileLo;
+                w0 = (uint32_t)pb | (uint32_t)(i1 - i0) << 16;
+                w1 = kind | (hasQual ? 8u : 0u) | (uint32_t)mq1 << 8;
+                qa = ((uint64_t)(uint32_t)e2.y << 32 | (uint32_t)e2.x) + (uint64_t)i0;
+                na = ((uint64_t)(uint32_t)e2.w << 32 | (uint32_t)e2.z) + (uint64_t)i0;
+                // position residue (mod 4) of the entry's 4-base chunks, which start
+                // at the aligned quality words (see the fast path)
+                cls = (pb - (int32_t)((uintptr_t)(R.qual + qa) & 3u)) & 3;
               }
             }
           }
         }
-        // ---- general CIGAR reads (S/PileUpRegion.scala:145-216), whole warp per read;
-        // I and D are handled by k_read_events.  Their M/=/X segments that have
-        // qualities are queued and walked afterwards by the chunked rounds below.
-        int nq = 0;  // queued segments (the same in every lane)
-        unsigned cx = __ballot_sync(FULL, kind == kComplex);
-        while (cx) {
-          const int src = __ffs(cx) - 1;
-          cx &= cx - 1;
-          const int32_t rpos = __shfl_sync(FULL, pos, src);
-          const int32_t rnc = __shfl_sync(FULL, nc, src), rlen = __shfl_sync(FULL, length, src);
-          const uint32_t rmq1 = __shfl_sync(FULL, mq1, src);
-          const bool rvalid = __shfl_sync(FULL, (int)valid, src) != 0;
-          const bool rhas = __shfl_sync(FULL, (int)hasQual, src) != 0;
-          const int64_t rco = __shfl_sync(FULL, co, src);
-          const uint8_t* rqp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)qp, src);
-          const uint8_t* rsp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)sp, src);
-          int32_t readOffset = 0, refOffset = 0;
-          for (int cb = 0; cb < rnc; cb += 32) {
-            const uint32_t wl = (cb + lane < rnc) ? R.cigar[rco + cb + lane] : 0u;
-            const int kmax = min(32, rnc - cb);
-            for (int k2 = 0; k2 < kmax; k2++) {
-              const uint32_t w = __shfl_sync(FULL, wl, k2);
-              const int32_t len = (int32_t)(w >> 4);
-              const int op = (int)(w & 15u);
-              const int32_t locus = rpos + refOffset;
-              if (op == 0 || op == 7 || op == 8) {
-                const int32_t a0 = max(max(tileLo - locus, P.flank - readOffset), 0);
-                const int32_t a1 = min(min(tileHi - locus + 1, rlen - P.flank - readOffset), len);
-                if (rvalid && lane == 0 && a1 > a0) bc += (unsigned long long)(a1 - a0);
-                // a segment the fast path can walk: queued as a read of its own
-                if (rvalid && rhas && P.long_read != PG_NANOPORE && a1 > a0 && readOffset < 0xffff && len < 0x10000 &&
-                    nq < kSegQueue) {
-                  if (lane == 0) {
-                    SegQ& e = segq[nq];
-                    e.read = base + src;
-                    e.pb = locus - tileLo;
-                    e.i01 = (uint32_t)a0 | ((uint32_t)a1 << 16);
-                    e.mr = rmq1 | ((uint32_t)readOffset << 9);
-                  }
-                  nq++;
-                } else
-                for (int32_t ii = a0 + lane; ii < a1; ii += 32) {
-                  const int32_t rOff = readOffset + ii;
-                  const int32_t p = locus + ii - tileLo;
-                  if (rvalid) {
-                    int32_t qual = rhas ? (int32_t)(int8_t)rqp[rOff] : P.default_qual;
-                    if (P.long_read == PG_NANOPORE && nanopore_exclude(cref, locus + ii - g.start, g.size)) qual = 0;
-                    const uint8_t b = rsp[rOff >> 1];
-                    add_base<T>(sm, p, (rOff & 1) ? (b & 15u) : (uint32_t)(b >> 4), qual,
-                                (int32_t)rmq1 - (int32_t)mode_mq1, P.min_qual);
-                  } else {
-                    atomicAdd(&s_bad[p], 1u);
-                  }
-                }
-              } else if (op == 4) {
-                const int32_t clipStart = readOffset == 0 ? locus - len : locus;
-                const int32_t clipEnd = clipStart + len - 1;
-                if (lane == 0) {
-                  if (clipStart >= tileLo && clipStart <= tileHi) atomicAdd(&s_clip[clipStart - tileLo], 1u);
-                  if (clipEnd >= tileLo && clipEnd <= tileHi) atomicAdd(&s_clip[clipEnd - tileLo], 1u);
-                }
-                const int32_t a0 = max(tileLo - clipStart, 0);
-                const int32_t a1 = min(tileHi - clipStart + 1, len);
-                for (int32_t ii = a0 + lane; ii < a1; ii += 32) atomicAdd(&s_bad[clipStart + ii - tileLo], 1u);
-              }
-              if (consumes_read(op)) readOffset += len;
-              if (consumes_ref(op)) refOffset += len;
-            }
-          }
-        }
-        // ---- simple reads, 32 / G at a time, G lanes each.  With 4 groups, round k
-        // gives group g the k-th read of residue class g while every class has one,
+        // ---- the lanes' entries, NG at a time, G lanes each.  With 4 groups, round k
+        // gives group g the k-th entry of residue class g while every class has one,
         // so the groups add to 4 different position residues at every step and their
-        // shared-memory atomics hit 32 different banks; the reads left over follow
-        // in lane order.  Each lane computes its read's slot at once.
-        __syncwarp();
+        // shared-memory atomics hit 32 different banks; the entries left over follow
+        // in lane order.  Each lane computes its entry's slot at once.
+        const uint32_t kind = w1 & 7u;
         const unsigned below = (1u << lane) - 1u;
-        for (int q0 = -32; q0 < nq; q0 += 32) {
-        if (q0 >= 0) {  // queued segments q0 .. q0 + 31 become the lanes' reads
-          kind = kSkip;
-          if (q0 + lane < nq) {
-            const SegQ e = segq[q0 + lane];
-            const int32_t r0 = (int32_t)(e.mr >> 9);
-            kind = kFast;
-            pb = e.pb;
-            i0 = (int32_t)(e.i01 & 0xffffu);
-            i1 = (int32_t)(e.i01 >> 16);
-            mq1 = e.mr & 0x1ffu;
-            clip = (uint32_t)r0 | kSegmentClip;  // lead = r0 for the read offsets; no clips
-            qp = R.qual + R.qual_off[e.read] + r0;
-            sp = R.seq + R.seq_off[e.read];
-            cls = (pb + i0 - (int32_t)((uintptr_t)(qp + i0) & 3u)) & 3;
-          }
-        }
-        const bool simple_kind = kind != kSkip && kind != kComplex;
-        const unsigned sm_all = __ballot_sync(FULL, simple_kind);
-        const int n_simple = __popc(sm_all);
-        if (simple_kind) {
-          // reads of the most common mq first (so that rounds mix one-atomic and
+        const unsigned act_all = __ballot_sync(FULL, kind != kSkip);
+        const int n_act = __popc(act_all);
+        if (kind != kSkip) {
+          // entries of the most common mq first (so that rounds mix one-atomic and
           // three-atomic adds at most once), interleaved by residue class; the rest after
-          const bool first = kind == kFast && mq1 == mode_mq1;
-          const unsigned set_a = __ballot_sync(sm_all, first);
+          const bool first = kind == kFast && (uint32_t)((int32_t)w1 >> 8) == mode_mq1;
+          const unsigned set_a = __ballot_sync(act_all, first);
           int slot;
           if (first) {
             if (NG == 4 || NG == 8) {  // with 8 groups, groups g and g + 4 share a residue class
-              const unsigned c0 = __ballot_sync(set_a, cls == 0), c1 = __ballot_sync(set_a, cls == 1);
-              const unsigned c2 = __ballot_sync(set_a, cls == 2), c3 = __ballot_sync(set_a, cls == 3);
-              const int m = min(min(__popc(c0), __popc(c1)), min(__popc(c2), __popc(c3)));
-              const unsigned mine = cls == 0 ? c0 : cls == 1 ? c1 : cls == 2 ? c2 : c3;
+              const unsigned c0m = __ballot_sync(set_a, cls == 0), c1m = __ballot_sync(set_a, cls == 1);
+              const unsigned c2m = __ballot_sync(set_a, cls == 2), c3m = __ballot_sync(set_a, cls == 3);
+              const int m = min(min(__popc(c0m), __popc(c1m)), min(__popc(c2m), __popc(c3m)));
+              const unsigned mine = cls == 0 ? c0m : cls == 1 ? c1m : cls == 2 ? c2m : c3m;
               const int rank = __popc(mine & below);
               const unsigned left = __ballot_sync(set_a, rank >= m);
               slot = rank < m ? 4 * rank + cls : 4 * m + __popc(left & below);
@@ -511,71 +484,59 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               slot = __popc(set_a & below);
             }
           } else {
-            slot = __popc(set_a) + __popc(sm_all & ~set_a & below);
+            slot = __popc(set_a) + __popc(act_all & ~set_a & below);
           }
           s_perm[warp][slot] = (uint8_t)lane;
         }
         __syncwarp();
-        for (int r0 = 0; r0 < n_simple; r0 += NG) {
-          const int src = r0 + grp < n_simple ? (int)s_perm[warp][r0 + grp] : 32;  // 32: no read for this group
+        for (int r0 = 0; r0 < n_act; r0 += NG) {
+          const int src = r0 + grp < n_act ? (int)s_perm[warp][r0 + grp] : 32;  // 32: no entry for this group
           const int s2 = src < 32 ? src : lane;
-          const uint32_t rk = __shfl_sync(FULL, kind, s2);
-          const int32_t ri0 = __shfl_sync(FULL, i0, s2), ri1 = __shfl_sync(FULL, i1, s2);
-          const int32_t rpb = __shfl_sync(FULL, pb, s2), rml = __shfl_sync(FULL, mlen, s2);
-          const uint32_t rmq1 = __shfl_sync(FULL, mq1, s2), rclip = __shfl_sync(FULL, clip, s2);
-          const uint8_t* rqp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)qp, s2);
-          const uint8_t* rsp = (const uint8_t*)__shfl_sync(FULL, (unsigned long long)sp, s2);
+          const uint32_t rw0 = __shfl_sync(FULL, w0, s2), rw1 = __shfl_sync(FULL, w1, s2);
+          const uint64_t rqa = __shfl_sync(FULL, qa, s2), rna = __shfl_sync(FULL, na, s2);
           if (src < 32) {
-            const int32_t lead = (int32_t)(rclip & 0xffffu), trail = (int32_t)(rclip >> 16);
-            const int32_t rpos = rpb + tileLo;
-            const int32_t rmlen = rml & 0x3fffffff;
-            const bool clips = (rclip & kSegmentClip) != kSegmentClip;
-            if (lead > 0 && clips) {  // clipStart = locus - len (clip at read offset 0), clipEnd = locus - 1
-              const int32_t cs = rpos - lead, ce = rpos - 1;
-              if (gl == 0) {
-                if (cs >= tileLo && cs <= tileHi) atomicAdd(&s_clip[cs - tileLo], 1u);
-                if (ce >= tileLo && ce <= tileHi) atomicAdd(&s_clip[ce - tileLo], 1u);
-              }
-              for (int32_t l = max(cs, tileLo) + gl; l <= min(ce, tileHi); l += G) atomicAdd(&s_bad[l - tileLo], 1u);
-            }
-            if (rk == kFast && ri1 > ri0) {
-              // Whole chunks of 4 consecutive trusted bases that start on an aligned
-              // quality word; lane gl of the group takes chunks cf + gl, cf + gl + G, ...
-              // and loads the next one while it adds the current one.  A chunk's
-              // qualities are one aligned word and its nibbles lie in at most two
-              // aligned sequence words, each holding a trusted byte, so no load leaves
-              // the pages of the read store.  The at most 6 trusted bases before the
+            const uint32_t rk = rw1 & 7u;
+            const int32_t rpb = (int32_t)(rw0 & 0xffffu), rn = (int32_t)(rw0 >> 16);
+            if (rk == kFast) {
+              // Whole chunks of 4 consecutive bases that start on an aligned quality
+              // word; lane gl of the group takes chunks cf + gl, cf + gl + G, ... and
+              // loads the next one while it adds the current one.  A chunk's qualities
+              // are one aligned word and its nibbles lie in at most two aligned
+              // sequence words, each holding one of the entry's bytes, so no load
+              // leaves the pages of the read store.  The at most 6 bases before the
               // first and after the last whole chunk are added one per lane.
-              const uintptr_t qa = (uintptr_t)(rqp + ri0);
-              const int32_t e0 = (int32_t)(qa & 3u);
-              const int32_t xs = ri0 - e0;  // x of byte 0 of chunk 0
-              const uint32_t* qw = (const uint32_t*)(qa - (uintptr_t)e0);
-              const int32_t cf = e0 ? 1 : 0, cend = (ri1 - xs) >> 2;  // whole chunks [cf, cend)
+              const uint8_t* rqp = R.qual + rqa;  // quality of base 0 (tile position rpb)
+              const uintptr_t qaddr = (uintptr_t)rqp;
+              const int32_t e0 = (int32_t)(qaddr & 3u);
+              const int32_t xs = -e0;  // base index of byte 0 of chunk 0
+              const uint32_t* qw = (const uint32_t*)(qaddr - (uintptr_t)e0);
+              const int32_t cf = e0 ? 1 : 0, cend = (rn - xs) >> 2;  // whole chunks [cf, cend)
               const int32_t fs = xs + 4 * cf, fe = xs + 4 * max(cend, cf);
-              const int32_t he = min(fs, ri1), ts = max(fe, he), nh = he - ri0, nt = max(ri1 - ts, 0);
+              const int32_t he = min(fs, rn), ts = max(fe, he), nh = he, nt = max(rn - ts, 0);
               // head and tail bases: loaded now, added after the chunks
               constexpr int kHT = (6 + G - 1) / G;  // head/tail bases per lane
               int32_t hx[kHT];
               uint32_t hb[kHT], hq[kHT];
 #pragma unroll
               for (int h = 0; h < kHT; h++) {
-                const int32_t k = gl + h * G;
-                hx[h] = k < nh + nt ? (k < nh ? ri0 + k : ts + (k - nh)) : -1;
+                const int32_t kk = gl + h * G;
+                hx[h] = kk < nh + nt ? (kk < nh ? kk : ts + (kk - nh)) : -1;
                 hb[h] = hq[h] = 0;
                 if (hx[h] >= 0) {
-                  hb[h] = rsp[(lead + hx[h]) >> 1];
+                  hb[h] = R.seq[(rna + (uint64_t)hx[h]) >> 1];
                   hq[h] = rqp[hx[h]];
                 }
               }
-              const int32_t n0 = lead + xs;          // read offset of chunk 0's first base
+              const int64_t n0 = (int64_t)rna + xs;  // nibble index of chunk 0's first base
               const uint32_t lastb = (uint32_t)((n0 & 1) + 3) >> 1;  // last byte of a chunk's nibbles
-              const uint8_t* sb = rsp + (n0 >> 1);   // byte of chunk c's first nibble: sb + 2c
+              // byte of chunk c's first nibble: (n0 >> 1) + 2c (chunk 0 is used only when n0 >= 0)
+              const int64_t sb = n0 >> 1;
               // This lane's chunks c, c + G, ... have their first nibble in bytes
               // sb + 2c, 2G apart: a multiple of 4, so every one sits at the same
               // offset in its aligned word and the loads walk two word pointers.
               // Two chunks are in flight ahead of the one being added.
               int32_t c = cf + gl;
-              const uintptr_t ba0 = (uintptr_t)(sb + 2 * c);
+              const uintptr_t ba0 = (uintptr_t)(R.seq + sb + 2 * c);
               const uint32_t sh = 8u * (uint32_t)(ba0 & 3u);
               const bool need_hi = (ba0 & 3u) + lastb >= 4u;
               const uint32_t* wp = (const uint32_t*)(ba0 & ~(uintptr_t)3);
@@ -590,17 +551,17 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               uint32_t qv = 0, sv = 0, q1 = 0, s1 = 0;
               if (c < cend) load_chunk(qv, sv);
               if (c + G < cend) load_chunk(q1, s1);
-              // mq + 1 - M: 0 for the reads of the most common mq
-              const int32_t dmq = (int32_t)rmq1 - (int32_t)mode_mq1;
+              // mq + 1 - M: 0 for the entries of the most common mq
+              const int32_t dmq = ((int32_t)rw1 >> 8) - (int32_t)mode_mq1;
               // Four bases at a time: the nibbles of the chunk select their codes
               // (kCodeLo/Hi) by prmt; a second prmt puts code j in byte j.  sv holds
-              // the chunk's nibbles from its first byte on: with an even read offset
+              // the chunk's nibbles from its first byte on: with an even nibble index
               // bases 1, 0, 3, 2 in its low four nibbles; with an odd one bases 0 and
               // 2 in nibbles 0 and 2, base 1 in nibble 3 and base 3 in nibble 5.
               const uint32_t comb = (n0 & 1) ? 0x7230u : 0x2301u;
               while (c < cend) {
-                uint32_t q2 = 0, s2 = 0;
-                if (c + 2 * G < cend) load_chunk(q2, s2);
+                uint32_t q2 = 0, s2v = 0;
+                if (c + 2 * G < cend) load_chunk(q2, s2v);
                 const uint32_t code = prmt(prmt(kCodeLo, kCodeHi, sv), prmt(kCodeLo, kCodeHi, sv >> 8), comb);
                 // bit 6 of byte j: base j is A/C/G/T and its quality byte is in [minQual, 127]
                 const uint32_t ok = code & ((((qv | 0x80808080u) - minq4) & ~qv & 0x80808080u) >> 1) & okall;
@@ -624,39 +585,37 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
                   }
                 }
                 c += G;
-                qv = q1; sv = s1; q1 = q2; s1 = s2;
+                qv = q1; sv = s1; q1 = q2; s1 = s2v;
               }
 #pragma unroll
               for (int h = 0; h < kHT; h++) {
                 if (hx[h] < 0) continue;
-                const uint32_t nib = ((lead + hx[h]) & 1) ? (hb[h] & 15u) : (hb[h] >> 4);
+                const uint32_t nib = ((rna + (uint64_t)hx[h]) & 1u) ? (hb[h] & 15u) : (hb[h] >> 4);
                 add_base<T>(sm, rpb + hx[h], nib, (int32_t)(int8_t)hq[h], dmq, P.min_qual);
               }
-            } else if (rk == kInvalid) {
-              for (int32_t ii = ri0 + gl; ii < ri1; ii += G) atomicAdd(&s_bad[rpb + ii], 1u);
-            } else {  // kSlow: no qualities (defaultQual) or nanopore motifs
-              const bool rhas = rqp[-lead] != 0xFF;  // qualities present unless the first byte is 0xFF
-              for (int32_t ii = ri0 + gl; ii < ri1; ii += G) {
-                const int32_t rOff = lead + ii;
-                const uint8_t b = rsp[rOff >> 1];
-                const uint32_t nib = (rOff & 1) ? (b & 15u) : (uint32_t)(b >> 4);
-                int32_t qual = rhas ? (int32_t)(int8_t)rqp[ii] : P.default_qual;
-                if (P.long_read == PG_NANOPORE && nanopore_exclude(cref, rpos + ii - g.start, g.size)) qual = 0;
-                add_base<T>(sm, rpb + ii, nib, qual, (int32_t)rmq1 - (int32_t)mode_mq1, P.min_qual);
+            } else if (rk == kInvalid) {  // add() of an invalid read: badPair (S/PileUpRegion.scala:38-48)
+              for (int32_t ii = gl; ii < rn; ii += G) atomicAdd(&s_bad[rpb + ii], 1u);
+            } else if (rk == kSlow) {  // no qualities (defaultQual), nanopore motifs, or an mq outside a byte
+              const bool rhas = (rw1 & 8u) != 0;
+              const int32_t dmq = ((int32_t)rw1 >> 8) - (int32_t)mode_mq1;
+              for (int32_t ii = gl; ii < rn; ii += G) {
+                const uint64_t ni = rna + (uint64_t)ii;
+                const uint8_t b = R.seq[ni >> 1];
+                const uint32_t nib = (ni & 1u) ? (b & 15u) : (uint32_t)(b >> 4);
+                int32_t qual = rhas ? (int32_t)(int8_t)R.qual[rqa + (uint64_t)ii] : P.default_qual;
+                if (nanopore && nanopore_exclude(cref, tileLo + rpb + ii - g.start, g.size)) qual = 0;
+                add_base<T>(sm, rpb + ii, nib, qual, dmq, P.min_qual);
               }
-            }
-            if (trail > 0 && clips) {  // clipStart = locus (clip after the aligned bases), clipEnd = locus + len - 1
-              const int32_t cs = rpos + rmlen, ce = cs + trail - 1;
+            } else {  // kClip
               if (gl == 0) {
-                if (cs >= tileLo && cs <= tileHi) atomicAdd(&s_clip[cs - tileLo], 1u);
-                if (ce >= tileLo && ce <= tileHi) atomicAdd(&s_clip[ce - tileLo], 1u);
+                if (rw1 & 8u) atomicAdd(&s_clip[(rw1 >> 8) & 0xfffu], 1u);
+                if (rw1 & 16u) atomicAdd(&s_clip[rw1 >> 20], 1u);
               }
-              for (int32_t l = max(cs, tileLo) + gl; l <= min(ce, tileHi); l += G) atomicAdd(&s_bad[l - tileLo], 1u);
+              for (int32_t ii = gl; ii < rn; ii += G) atomicAdd(&s_bad[rpb + ii], 1u);
             }
           }
         }
         __syncwarp();
-        }
       }
       __syncthreads();
 
@@ -713,14 +672,13 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
 
 template <int T, int MINB, int G>
 static void launch_walk_t(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s) {
-  const size_t smem = walk_smem<T>(warps);
+  const size_t smem = walk_smem<T>();
   // attribute and occupancy are queried once per (kernel, warps): the first
   // launch of a shape is never inside a stream capture
   static bool configured = false;
   static int per_sm_of[17] = {0};
-  if (!configured) {  // room for the largest CTA (16 warps of segment queues)
-    const size_t smem_max = walk_smem<T>(16);
-    cudaFuncSetAttribute(k_walk<T, MINB, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+  if (!configured) {
+    cudaFuncSetAttribute(k_walk<T, MINB, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     configured = true;
   }
   if (!per_sm_of[warps]) {

@@ -51,6 +51,15 @@ def lib():
                                             C.POINTER(C.c_int32)]),
             "pg_sync": (C.c_int, [vp]),
             "pg_graph_replays": (C.c_int, [vp, C.POINTER(C.c_int32)]),
+            "pg_default_serve_config": (None, [C.POINTER(_abi.pg_serve_config)]),
+            "pg_serve_open": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(_abi.pg_serve_config),
+                                        C.POINTER(_abi.pg_params), i32, vp, vp, vp, C.POINTER(_abi.pg_reads)]),
+            "pg_serve_submit": (C.c_int, [vp, C.POINTER(_abi.pg_request), C.POINTER(C.c_uint64)]),
+            "pg_serve_poll": (C.c_int, [vp, C.c_uint64, i32, C.POINTER(_abi.pg_result)]),
+            "pg_serve_release": (C.c_int, [vp, C.c_uint64]),
+            "pg_serve_stats": (C.c_int, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+            "pg_serve_error": (C.c_char_p, [vp]),
+            "pg_serve_close": (None, [vp]),
             "pg_format_vcf": (C.c_int, [vp, i32, C.c_char_p, i32, i32, i32, vp, i64, C.POINTER(C.c_int64)]),
             "pg_find_breaks": (C.c_int, [vp, i32, vp, i64, C.POINTER(C.c_int64)]),
             "pg_kmer_tally_breaks": (C.c_int, [vp, i32, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,

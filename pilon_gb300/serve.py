@@ -2,18 +2,17 @@
 
 A request is the work of `pilon --targets contig:start-stop --fix snps,indels
 --vcf --changes` on one region (S/GenomeFile.scala:215-250 for --targets).
-The reads of the whole genome stay in device memory once; every worker owns
-an engine context (its own CUDA stream and buffers) on the same GPU.  A
-worker takes all queued requests that fit its position budget, runs them as
-one batched pg_pileup_regions call and answers each with
+The server is the engine library's own (pg_serve_open / pg_serve_submit /
+pg_serve_poll of include/pilon_gb300.h): it keeps the reference and the read
+store resident on the device, admits queued requests by the device bytes they
+need against a budget, and runs each batch on one of several engine contexts
+so that batches overlap on the GPU.  Each answer holds
 
   fasta    the polished sequence of the region (GenomeRegion.bases after fixIssues)
   changes  the changes-file lines of the region
   vcf      the region's VCF records whose ALT is not "." (a delta)
-
-Requests that arrive while batches run wait only until a worker is free, and
-the batches of different workers overlap on the device.
 """
+import ctypes as C
 import threading
 import time
 from collections import deque
@@ -23,8 +22,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _abi
-from .polish import Options, _region_outputs, new_name, region_string
-from .regions import ReadIndex
+from .polish import Options
 
 
 @dataclass
@@ -46,145 +44,107 @@ class Result:
     batch: int = 0
 
 
-def device_read_store(reads, device=0):
-    """Uploads the read store once (torch tensors as device memory) and returns
-    a pg_reads struct of device pointers plus the tensors that own them."""
-    import torch
-    from .reads import FIELDS
-    dev = torch.device(f"cuda:{device}")
-    keep = {}
-    r = _abi.pg_reads()
-    r.n_reads = reads.n_reads
-    for f in FIELDS:
-        a = np.ascontiguousarray(getattr(reads, f))
-        t = torch.from_numpy(a.view(np.uint8).reshape(-1)).to(dev) if a.size else torch.zeros(16, dtype=torch.uint8,
-                                                                                             device=dev)
-        keep[f] = t
-        setattr(r, f, t.data_ptr())
-    r.n_cigar_words = int(reads.cigar.size)
-    r.seq_bytes = int(reads.seq.size)
-    r.qual_bytes = int(reads.qual.size)
-    torch.cuda.synchronize(dev)
-    return r, keep
-
-
-def request_result(engine, r, req, names, contigs, params, opts):
-    """One region of the last engine call -> the request's answer."""
-    region = (req.contig, req.start, req.stop, 0, 0)
-    res = _region_outputs(engine, r, region, contigs[req.contig], opts, params)
-    nn = new_name(names[req.contig])
-    lines = []
-    delta = 0
-    for f in res.all_fixes():
-        nl = f.locus + delta
-        lines.append(region_string(names[req.contig], f.locus, f.locus + len(f.was) - 1) + " " +
-                     region_string(nn, nl, nl + len(f.patch) - 1) + " " + (f.was or ".") + " " + (f.patch or "."))
-        delta += len(f.patch) - len(f.was)
-    vcf = engine.format_vcf(r, names[req.contig], opts.diploid, opts.vcf_qe, variants_only=True)
-    return Result(req.rid, bytes(res.bases), "".join(l + "\n" for l in lines), vcf)
-
-
 class Server:
-    """Continuous batching over `n_workers` engine contexts on one GPU."""
+    """The native server of the C ABI (pg_serve_open ... pg_serve_close).
 
-    def __init__(self, names, contigs, reads, params=None, opts=None, n_workers=2, budget_positions=40_000_000,
-                 device=0, batched=True):
-        from .engine import Engine
-        self.names, self.contigs = names, contigs
-        self.params = params or _abi.default_params()
+    budget_bytes is the device memory the requests in flight may need together
+    (116 bytes per region position and 16 per read of the query window);
+    max_batch limits the requests of one batch (0: none); batched=False runs
+    each batch on the plain per-region path.  submit() returns a Future of a
+    Result, or of an IndexError for a target on which Pilon throws."""
+
+    def __init__(self, names, contigs, reads, params=None, opts=None, n_workers=2, budget_bytes=8 << 30,
+                 device=0, batched=True, max_batch=0):
+        from .engine import EngineError, lib
+        self.L = lib()
         self.opts = opts or Options()
-        self.opts.longread_only = False
-        self.opts.vcf = False  # no <DUP> pass for deltas
-        self.budget = budget_positions
-        self.batched = batched
-        self.index = ReadIndex(reads, len(contigs))
-        self.dev_reads, self._keep = device_read_store(reads, device)
-        self.engines = []
-        for _ in range(n_workers):
-            e = Engine(device)
-            e.set_reference(contigs)
-            e.set_reads_device(self.dev_reads, reads.n_reads)
-            self.engines.append(e)
-        self.q = deque()
-        self.cv = threading.Condition()
-        self.closed = False
-        self.batches = 0
-        self.threads = [threading.Thread(target=self._worker, args=(e,), daemon=True) for e in self.engines]
-        for t in self.threads:
-            t.start()
+        self.params = params or _abi.default_params()
+        cfg = _abi.pg_serve_config()
+        self.L.pg_default_serve_config(C.byref(cfg))
+        cfg.device, cfg.n_workers, cfg.hbm_budget, cfg.max_batch = device, n_workers, int(budget_bytes), max_batch
+        cfg.batched = int(batched)
+        cfg.fix_snps, cfg.fix_indels = int(self.opts.fix_snps), int(self.opts.fix_indels)
+        cfg.iupac, cfg.diploid, cfg.vcf_qe = int(self.opts.iupac), int(self.opts.diploid), int(self.opts.vcf_qe)
+        arrs = [np.ascontiguousarray(c, np.uint8) for c in contigs]
+        lens = np.array([a.size for a in arrs], np.int64)
+        bases = (C.c_void_p * max(1, len(arrs)))(*[a.ctypes.data for a in arrs])
+        nm = [n.encode() for n in names]
+        nptr = (C.c_char_p * max(1, len(nm)))(*nm)
+        ab = reads.to_abi()
+        self.h = C.c_void_p()
+        st = self.L.pg_serve_open(C.byref(self.h), C.byref(cfg), C.byref(self.params), len(arrs),
+                                  C.cast(nptr, C.c_void_p), lens.ctypes.data, C.cast(bases, C.c_void_p), C.byref(ab))
+        if st != 0:
+            msg = self.L.pg_serve_error(self.h).decode()
+            self.L.pg_serve_close(self.h)
+            self.h = None
+            raise EngineError(st, msg)
+        self._pending = deque()
+        self._cv = threading.Condition()
+        self._closed = False
+        self._poller = threading.Thread(target=self._poll_loop, daemon=True)
+        self._poller.start()
+
+    @property
+    def batches(self):
+        b = C.c_int64()
+        self.L.pg_serve_stats(self.h, C.byref(b), None, None)
+        return b.value
+
+    def peak_in_flight_bytes(self):
+        p = C.c_int64()
+        self.L.pg_serve_stats(self.h, None, None, C.byref(p))
+        return p.value
 
     def submit(self, req):
+        from .engine import EngineError
         fut = Future()
-        if not req.arrival:
-            req.arrival = time.perf_counter()
-        with self.cv:
-            self.q.append((req, fut))
-            self.cv.notify()
+        q = _abi.pg_request(req.contig, req.start, req.stop, 0)
+        t = C.c_uint64()
+        st = self.L.pg_serve_submit(self.h, C.byref(q), C.byref(t))
+        if st != 0:
+            fut.set_exception(EngineError(st, self.L.pg_serve_error(self.h).decode()))
+            return fut
+        with self._cv:
+            self._pending.append((t.value, req, fut))
+            self._cv.notify()
         return fut
 
-    def _take(self):
-        with self.cv:
-            while not self.q and not self.closed:
-                self.cv.wait()
-            if not self.q:
-                return []
-            batch, used = [], 0
-            while self.q:
-                req, fut = self.q[0]
-                size = req.stop - req.start + 1
-                if batch and used + size > self.budget:
-                    break
-                self.q.popleft()
-                batch.append((req, fut))
-                used += size
-            return batch
-
-    def _worker(self, engine):
+    def _poll_loop(self):
         from .engine import EngineError
         while True:
-            batch = self._take()
-            if not batch:
-                return
-            try:
-                regions = []
-                for req, _ in batch:
-                    n = int(self.contigs[req.contig].size)
-                    a, b = self.index.range_for(req.contig, req.start, req.stop, n)
-                    regions.append((req.contig, req.start, req.stop, a, b))
-                failed = set()
-                try:
-                    engine.pileup_regions(regions, self.params, batched=self.batched)
-                except EngineError as exc:
-                    if exc.status != _abi.PG_ERR_INDEX:
-                        raise
-                    # the reference throws on these targets; the other requests are unaffected
-                    failed = {r for r in range(len(batch)) if engine.stats(r).error}
-                with self.cv:
-                    self.batches += 1
-                    bno = self.batches
-                for r, (req, fut) in enumerate(batch):
-                    if r in failed:
-                        fut.set_exception(IndexError(
-                            f"target {self.names[req.contig]}:{req.start}-{req.stop}: an indel left shift leaves "
-                            f"the region (Pilon throws ArrayIndexOutOfBoundsException)"))
-                        continue
-                    out = request_result(engine, r, req, self.names, self.contigs, self.params, self.opts)
-                    out.latency = time.perf_counter() - req.arrival
-                    out.batch = bno
-                    fut.set_result(out)
-            except Exception as exc:  # every request of a failed batch sees the error
-                for _, fut in batch:
-                    if not fut.done():
-                        fut.set_exception(exc)
+            with self._cv:
+                while not self._pending and not self._closed:
+                    self._cv.wait()
+                if not self._pending:
+                    return
+                t, req, fut = self._pending.popleft()
+            res = _abi.pg_result()
+            st = self.L.pg_serve_poll(self.h, t, -1, C.byref(res))
+            if st != 0:
+                fut.set_exception(EngineError(st, self.L.pg_serve_error(self.h).decode()))
+                continue
+            if res.status == _abi.PG_ERR_INDEX:
+                fut.set_exception(IndexError(f"target {req.contig}:{req.start}-{req.stop}: {res.message.decode()}"))
+            elif res.status != 0:
+                fut.set_exception(EngineError(res.status, res.message.decode()))
+            else:
+                out = Result(req.rid, C.string_at(res.fasta, res.fasta_len), C.string_at(res.changes,
+                             res.changes_len).decode(), C.string_at(res.vcf, res.vcf_len),
+                             latency=res.latency_ms / 1e3, batch=res.batch)
+                out.queue_ms, out.run_ms, out.device_bytes = res.queue_ms, res.run_ms, res.device_bytes
+                fut.set_result(out)
+            self.L.pg_serve_release(self.h, t)
 
     def close(self):
-        with self.cv:
-            self.closed = True
-            self.cv.notify_all()
-        for t in self.threads:
-            t.join()
-        for e in self.engines:
-            e.close()
+        if self.h is None:
+            return
+        with self._cv:
+            self._closed = True
+            self._cv.notify_all()
+        self._poller.join()
+        self.L.pg_serve_close(self.h)
+        self.h = None
 
 
 def poisson_requests(contig_lens, rate, duration, seed=1005, min_len=10_000, max_len=1_000_000):

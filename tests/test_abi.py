@@ -43,6 +43,10 @@ def test_struct_layouts_match_header():
     assert C.sizeof(_abi.pg_kmer_edge) == 32
     assert C.sizeof(_abi.pg_window) == 16
     assert C.sizeof(_abi.pg_break) == 16
+    assert C.sizeof(_abi.pg_request) == 16
+    assert C.sizeof(_abi.pg_serve_config) == 48  # 4 + 4, the int64 budget at 8, then 7 int32 + padding
+    assert C.sizeof(_abi.pg_result) == 96
+    assert _abi.pg_result.latency_ms.offset == 80 and _abi.pg_serve_config.hbm_budget.offset == 8
 
 
 def test_default_params_match_pilon():

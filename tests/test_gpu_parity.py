@@ -147,8 +147,9 @@ def test_graph_not_replayed_after_reallocation(cfg1):
     """A recorded graph holds the addresses of the context's buffers.  A call
     that grows one of them (here a plan with four times the regions, on the
     per-region path) must end the replays: the next batched call of the first
-    plan runs its launches again and matches the oracle, and only the call
-    after it records a new graph."""
+    plan runs its launches again and matches the oracle, and replays resume
+    only after the plan has been recorded anew (a call marks a plan, the next
+    identical one records it, later ones replay it)."""
     from pilon_gb300.engine import Engine
     p = _abi.default_params()
     a = plan(cfg1, chunk_size=9000)
@@ -164,11 +165,13 @@ def test_graph_not_replayed_after_reallocation(cfg1):
         def check(regs, ora, label):
             for r in range(len(regs)):
                 compare_region(eng.fetch(r), ora[r], label=f"{label} region {r}")
-        for k in range(3):  # eager, recorded, replayed
+        for k in range(6):  # marked, recorded, replayed (later when a first call grows its buffers)
             eng.pileup_regions(a, p, batched=True)
             check(a, ora_a, f"a{k}")
+            if eng.graph_replays():
+                break
         r0 = eng.graph_replays()
-        assert r0 == 1
+        assert r0 >= 1
         eng.pileup_regions(b, p, batched=False)
         check(b, ora_b, "b plain")
         eng.pileup_regions(a, p, batched=True)
@@ -176,10 +179,10 @@ def test_graph_not_replayed_after_reallocation(cfg1):
         assert eng.graph_replays() == r0, "a graph with freed buffers was replayed"
         eng.pileup_regions(b, p, batched=True)
         check(b, ora_b, "b batched")
-        for k in range(3):
+        for k in range(4):  # marked, recorded, replayed
             eng.pileup_regions(a, p, batched=True)
             check(a, ora_a, f"a again {k}")
-        assert eng.graph_replays() == r0 + 1
+        assert eng.graph_replays() > r0
     finally:
         eng.close()
 

@@ -278,14 +278,35 @@ def test_option_combinations_on_other_workloads(wl, kw, pk):
     compare(ds, params=_abi.default_params(**pk), **kw)
 
 
+def request_result(engine, r, req, names, contigs, params, opts):
+    """One served answer restated on the host from region r of the last engine
+    call: the fixed bases, the changes lines of the target as its own output
+    entry (offset 0) and the variant records, as the native server builds them
+    (pilon_gb300/csrc/pg_serve.cu)."""
+    from pilon_gb300.polish import _region_outputs, new_name, region_string
+    from pilon_gb300.serve import Result
+    region = (req.contig, req.start, req.stop, 0, 0)
+    res = _region_outputs(engine, r, region, contigs[req.contig], opts, params)
+    nn = new_name(names[req.contig])
+    lines = []
+    delta = 0
+    for f in res.all_fixes():
+        nl = f.locus + delta
+        lines.append(region_string(names[req.contig], f.locus, f.locus + len(f.was) - 1) + " " +
+                     region_string(nn, nl, nl + len(f.patch) - 1) + " " + (f.was or ".") + " " + (f.patch or "."))
+        delta += len(f.patch) - len(f.was)
+    vcf = engine.format_vcf(r, names[req.contig], opts.diploid, opts.vcf_qe, variants_only=True)
+    return Result(req.rid, bytes(res.bases), "".join(l + "\n" for l in lines), vcf)
+
+
 def test_served_requests_equal_target_outputs():
-    """A served request's answer (serve.request_result) equals what --targets
-    writes for that target: its fixed bases and its changes lines (each target
-    its own entry, the offset restarting)."""
+    """A served answer, restated on the host (request_result), equals what
+    --targets writes for that target: its fixed bases and its changes lines
+    (each target its own entry, the offset restarting)."""
     from types import SimpleNamespace
     from pilon_gb300.reads import build_store
     from pilon_gb300.regions import plan_regions
-    from pilon_gb300.serve import Request, request_result
+    from pilon_gb300.serve import Request
     from tests.test_oracle_kat import _tile_reads, rand_ref, ref_from
     ref = list(rand_ref(2000, seed=51))
     if ref[308] == "A":

@@ -1,13 +1,13 @@
 """CPU restatements of the pileup walk's index arithmetic, each tied to the
 kernel's source lines.
 
-Slot assignment (k_walk, the rounds of simple reads): each lane holding a simple
-read computes its read's slot in the warp's round order from ballots and
-population counts.  The slots must be a permutation of 0 .. n_simple - 1 (every
-read walked exactly once), and with 4 or 8 lane groups the first 4 * m slots of
-the reads of the most common mq must hold one read of each position residue
-class in every group of four (their shared-memory atomics then fall in
-different banks).
+Slot assignment (k_walk, the rounds of walk entries): each lane holding an
+entry (one M/=/X or S operator of a read) computes its entry's slot in the
+warp's round order from ballots and population counts.  The slots must be a
+permutation of 0 .. n_active - 1 (every entry walked exactly once), and with 4
+or 8 lane groups the first 4 * m slots of the entries of the most common mq
+must hold one entry of each position residue class in every group of four
+(their shared-memory atomics then fall in different banks).
 
 Read ranges (k_tile_ranges): the warp's 32-ary lower bound over a tile's
 position-sorted reads must equal a binary search, with every load in range.
@@ -83,7 +83,7 @@ def test_kernel_still_uses_these_formulas():
     src = open(os.path.join(os.path.dirname(__file__), "..", "pilon_gb300", "csrc", "pg_pileup.cu")).read()
     for line in ["slot = rank < m ? 4 * rank + cls : 4 * m + __popc(left & below);",
                  "slot = __popc(set_a & below);",
-                 "slot = __popc(set_a) + __popc(sm_all & ~set_a & below);"]:
+                 "slot = __popc(set_a) + __popc(act_all & ~set_a & below);"]:
         assert line in src, line
 
 
