@@ -340,6 +340,71 @@ __device__ inline bool nanopore_exclude(const uint8_t* cref, int32_t x, int32_t 
          cref[x + 2] == 'G';
 }
 
+// PileUp.add (S/PileUp.scala:75-84) of the four bases of one chunk: qv holds
+// their quality bytes, sv their nibbles from the chunk's first byte on (see
+// comb in the walk).  The nibbles select their codes (kCodeLo/Hi) by prmt; a
+// second prmt puts code j in byte j.  DMQ: the entry's mq + 1 differs from the
+// store's most common value, so qual * dmq and dmq go to the correction words.
+template <int T, bool DMQ>
+__device__ __forceinline__ void add_chunk(uint32_t* cl, uint32_t qv, uint32_t sv, uint32_t comb, uint32_t minq4,
+                                          uint32_t okall, int32_t dmq) {
+  const uint32_t code = prmt(prmt(kCodeLo, kCodeHi, sv), prmt(kCodeLo, kCodeHi, sv >> 8), comb);
+  // bit 6 of byte j: base j is A/C/G/T and its quality byte is in [minQual, 127]
+  const uint32_t ok = code & ((((qv | 0x80808080u) - minq4) & ~qv & 0x80808080u) >> 1) & okall;
+  const uint32_t qm = qv & ((ok >> 6) * 0x7fu);  // accepted qualities, 0 elsewhere
+  const uint32_t one4 = ok >> 2;                 // 0x10 in the bytes of accepted bases
+  const uint32_t bix = code & 0x03030303u;       // base index of byte j (0 when rejected)
+  // base j adds qual + (1 << 20), built by one prmt: byte 0 = quality, byte 2 =
+  // 0x10 or 0, bytes 1 and 3 = the clear sign of a byte of one4; a rejected base
+  // adds 0 to row 0 (no branch per base)
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+    atomicAdd(cl + j + prmt(bix, 0u, 0x4440u | (uint32_t)j) * T,
+              prmt(qm, one4, (uint32_t)(j | (12 + j) << 4 | (4 + j) << 8 | (12 + j) << 12)));
+  if (DMQ) {  // qual * dmq to qx[b], dmq to mx (0 for a rejected base)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      atomicAdd(cl + 4 * T + j + prmt(bix, 0u, 0x4440u | (uint32_t)j) * T,
+                prmt(qm, 0u, 0x4440u | (uint32_t)j) * (uint32_t)dmq);
+      atomicAdd(cl + 8 * T + j, ((ok >> (8 * j + 6)) & 1u) * (uint32_t)dmq);
+    }
+  }
+}
+
+// The whole chunks c = c0, c0 + G, ... < cend of one entry for one lane: chunk
+// c's qualities are word c of qw, its nibbles start at byte sb + 2c of the
+// sequence (every such byte sits at the same offset in its aligned word, so two
+// aligned words and a funnel shift give them).  Two chunks are added per
+// iteration while the next two load.
+template <int T, int G, bool DMQ>
+__device__ __forceinline__ void walk_chunks(uint32_t* cbase, const uint32_t* qw, const uint8_t* seq, int64_t sb,
+                                            int32_t c0, int32_t cend, uint32_t lastb, uint32_t comb, uint32_t minq4,
+                                            uint32_t okall, int32_t dmq) {
+  if (c0 >= cend) return;
+  const uintptr_t ba0 = (uintptr_t)(seq + sb + 2 * c0);
+  const uint32_t sh = 8u * (uint32_t)(ba0 & 3u);
+  const bool need_hi = (ba0 & 3u) + lastb >= 4u;
+  const uint32_t* wp = (const uint32_t*)(ba0 & ~(uintptr_t)3);  // word of chunk c0; chunk c0 + kG at wp + k G / 2
+  auto load = [&](int32_t k, uint32_t& q, uint32_t& sv) {  // the lane's k-th chunk
+    const uint32_t* w = wp + k * (G / 2);
+    const uint32_t lo = w[0], hi = need_hi ? w[1] : 0u;
+    q = qw[c0 + k * G];
+    sv = __funnelshift_r(lo, hi, sh);
+  };
+  const int32_t n = (cend - c0 + G - 1) / G;  // chunks of this lane
+  uint32_t qa = 0, sa = 0, qb = 0, sb2 = 0;
+  load(0, qa, sa);
+  if (n > 1) load(1, qb, sb2);
+  for (int32_t k = 0; k < n; k += 2) {
+    uint32_t qc = 0, sc = 0, qd = 0, sd = 0;
+    if (k + 2 < n) load(k + 2, qc, sc);
+    if (k + 3 < n) load(k + 3, qd, sd);
+    add_chunk<T, DMQ>(cbase + 4 * (c0 + k * G), qa, sa, comb, minq4, okall, dmq);
+    if (k + 1 < n) add_chunk<T, DMQ>(cbase + 4 * (c0 + (k + 1) * G), qb, sb2, comb, minq4, okall, dmq);
+    qa = qc; sa = sc; qb = qd; sb2 = sd;
+  }
+}
+
 // entry kinds of a lane's word w1
 enum : uint32_t { kSkip = 0, kFast = 1, kInvalid = 2, kSlow = 3, kClip = 4 };
 
@@ -349,10 +414,13 @@ constexpr size_t walk_smem() {
   return (size_t)(11 * T + 4) * sizeof(uint32_t);
 }
 
-// MINB: resident CTAs of 512 threads the register allocation must allow
-// (2: up to 64 registers per thread).  G: lanes per entry (4, 8, 16, 32).
+// MINB: resident CTAs the register allocation must allow: 2 CTAs of up to 512
+// threads (16 warps, up to 64 registers per thread) or 5 CTAs of up to 256
+// threads (8 warps, up to 48 registers: 40 warps per SM).  G: lanes per entry
+// (4, 8, 16, 32).
 template <int T, int MINB, int G>
-__global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_begin, int32_t tile_end) {
+__global__ void __launch_bounds__(MINB >= 4 ? 256 : 512, MINB) k_walk(WalkArgs a, int32_t tile_begin,
+                                                                      int32_t tile_end) {
   constexpr int kWords = 11 * T;
   static_assert((kWords + 4) % 4 == 0, "counters are cleared 16 bytes at a time");
   extern __shared__ __align__(16) uint32_t sm_raw[];
@@ -499,8 +567,8 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
             const int32_t rpb = (int32_t)(rw0 & 0xffffu), rn = (int32_t)(rw0 >> 16);
             if (rk == kFast) {
               // Whole chunks of 4 consecutive bases that start on an aligned quality
-              // word; lane gl of the group takes chunks cf + gl, cf + gl + G, ... and
-              // loads the next one while it adds the current one.  A chunk's qualities
+              // word; lane gl of the group takes chunks cf + gl, cf + gl + G, ...
+              // (walk_chunks: two added while the next two load).  A chunk's qualities
               // are one aligned word and its nibbles lie in at most two aligned
               // sequence words, each holding one of the entry's bytes, so no load
               // leaves the pages of the read store.  The at most 6 bases before the
@@ -529,64 +597,19 @@ __global__ void __launch_bounds__(512, MINB) k_walk(WalkArgs a, int32_t tile_beg
               }
               const int64_t n0 = (int64_t)rna + xs;  // nibble index of chunk 0's first base
               const uint32_t lastb = (uint32_t)((n0 & 1) + 3) >> 1;  // last byte of a chunk's nibbles
-              // byte of chunk c's first nibble: (n0 >> 1) + 2c (chunk 0 is used only when n0 >= 0)
-              const int64_t sb = n0 >> 1;
-              // This lane's chunks c, c + G, ... have their first nibble in bytes
-              // sb + 2c, 2G apart: a multiple of 4, so every one sits at the same
-              // offset in its aligned word and the loads walk two word pointers.
-              // Two chunks are in flight ahead of the one being added.
-              int32_t c = cf + gl;
-              const uintptr_t ba0 = (uintptr_t)(R.seq + sb + 2 * c);
-              const uint32_t sh = 8u * (uint32_t)(ba0 & 3u);
-              const bool need_hi = (ba0 & 3u) + lastb >= 4u;
-              const uint32_t* wp = (const uint32_t*)(ba0 & ~(uintptr_t)3);
-              const uint32_t* qp_next = qw + c;
-              auto load_chunk = [&](uint32_t& q, uint32_t& sv) {  // the next chunk of this lane
-                const uint32_t lo = wp[0], hi = need_hi ? wp[1] : 0u;
-                q = *qp_next;
-                sv = __funnelshift_r(lo, hi, sh);
-                wp += G / 2;
-                qp_next += G;
-              };
-              uint32_t qv = 0, sv = 0, q1 = 0, s1 = 0;
-              if (c < cend) load_chunk(qv, sv);
-              if (c + G < cend) load_chunk(q1, s1);
+              // sv holds a chunk's nibbles from its first byte on: with an even nibble
+              // index bases 1, 0, 3, 2 in its low four nibbles; with an odd one bases 0
+              // and 2 in nibbles 0 and 2, base 1 in nibble 3 and base 3 in nibble 5
+              const uint32_t comb = (n0 & 1) ? 0x7230u : 0x2301u;
               // mq + 1 - M: 0 for the entries of the most common mq
               const int32_t dmq = ((int32_t)rw1 >> 8) - (int32_t)mode_mq1;
-              // Four bases at a time: the nibbles of the chunk select their codes
-              // (kCodeLo/Hi) by prmt; a second prmt puts code j in byte j.  sv holds
-              // the chunk's nibbles from its first byte on: with an even nibble index
-              // bases 1, 0, 3, 2 in its low four nibbles; with an odd one bases 0 and
-              // 2 in nibbles 0 and 2, base 1 in nibble 3 and base 3 in nibble 5.
-              const uint32_t comb = (n0 & 1) ? 0x7230u : 0x2301u;
-              while (c < cend) {
-                uint32_t q2 = 0, s2v = 0;
-                if (c + 2 * G < cend) load_chunk(q2, s2v);
-                const uint32_t code = prmt(prmt(kCodeLo, kCodeHi, sv), prmt(kCodeLo, kCodeHi, sv >> 8), comb);
-                // bit 6 of byte j: base j is A/C/G/T and its quality byte is in [minQual, 127]
-                const uint32_t ok = code & ((((qv | 0x80808080u) - minq4) & ~qv & 0x80808080u) >> 1) & okall;
-                const uint32_t qm = qv & ((ok >> 6) * 0x7fu);  // accepted qualities, 0 elsewhere
-                const uint32_t one4 = ok >> 2;                 // 0x10 in the bytes of accepted bases
-                const uint32_t bix = code & 0x03030303u;       // base index of byte j (0 when rejected)
-                uint32_t* cl = sm + (rpb + xs + 4 * c);
-                // base j adds qual + (1 << 20), built by one prmt: byte 0 = quality,
-                // byte 2 = 0x10 or 0, bytes 1 and 3 = the clear sign of a byte of one4;
-                // a rejected base adds 0 to row 0 (no branch per base)
-#pragma unroll
-                for (int j = 0; j < 4; j++)
-                  atomicAdd(cl + j + prmt(bix, 0u, 0x4440u | (uint32_t)j) * T,
-                            prmt(qm, one4, (uint32_t)(j | (12 + j) << 4 | (4 + j) << 8 | (12 + j) << 12)));
-                if (dmq) {  // qual * dmq to qx[b], dmq to mx (0 for a rejected base)
-#pragma unroll
-                  for (int j = 0; j < 4; j++) {
-                    atomicAdd(cl + 4 * T + j + prmt(bix, 0u, 0x4440u | (uint32_t)j) * T,
-                              prmt(qm, 0u, 0x4440u | (uint32_t)j) * (uint32_t)dmq);
-                    atomicAdd(cl + 8 * T + j, ((ok >> (8 * j + 6)) & 1u) * (uint32_t)dmq);
-                  }
-                }
-                c += G;
-                qv = q1; sv = s1; q1 = q2; s1 = s2v;
-              }
+              // chunk c's counters start at tile position rpb + xs + 4c; its first
+              // nibble is in byte (n0 >> 1) + 2c (chunk 0 is used only when n0 >= 0)
+              uint32_t* cbase = sm + (rpb + xs);
+              if (dmq == 0)
+                walk_chunks<T, G, false>(cbase, qw, R.seq, n0 >> 1, cf + gl, cend, lastb, comb, minq4, okall, 0);
+              else
+                walk_chunks<T, G, true>(cbase, qw, R.seq, n0 >> 1, cf + gl, cend, lastb, comb, minq4, okall, dmq);
 #pragma unroll
               for (int h = 0; h < kHT; h++) {
                 if (hx[h] < 0) continue;
@@ -706,10 +729,17 @@ static void launch_walk_v(const WalkArgs& a, int32_t tile_begin, int32_t tile_co
 void launch_walk(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s) {
   if (tile_count <= 0) return;
   const int lanes = a.packed;
-  if (lanes == 0) launch_walk_v<2, 32>(a, tile_begin, tile_count, warps, s);
-  else if (lanes == 1) launch_walk_v<2, 16>(a, tile_begin, tile_count, warps, s);
-  else if (lanes == 2) launch_walk_v<2, 8>(a, tile_begin, tile_count, warps, s);
-  else launch_walk_v<2, 4>(a, tile_begin, tile_count, warps, s);
+  if (warps <= 8) {  // 256-thread CTAs, 5 resident per SM
+    if (lanes == 0) launch_walk_v<5, 32>(a, tile_begin, tile_count, warps, s);
+    else if (lanes == 1) launch_walk_v<5, 16>(a, tile_begin, tile_count, warps, s);
+    else if (lanes == 2) launch_walk_v<5, 8>(a, tile_begin, tile_count, warps, s);
+    else launch_walk_v<5, 4>(a, tile_begin, tile_count, warps, s);
+  } else {
+    if (lanes == 0) launch_walk_v<2, 32>(a, tile_begin, tile_count, warps, s);
+    else if (lanes == 1) launch_walk_v<2, 16>(a, tile_begin, tile_count, warps, s);
+    else if (lanes == 2) launch_walk_v<2, 8>(a, tile_begin, tile_count, warps, s);
+    else launch_walk_v<2, 4>(a, tile_begin, tile_count, warps, s);
+  }
 }
 
 // ---------------------------------------------------------------------------
