@@ -249,6 +249,24 @@ def kmer_bench(eng, ds, params, args, threads, K=31, radius=500):
         edges = eng.kmer_tally(wins, K, params)
         t.append(time.perf_counter() - t0)
     sec = sum(t) / len(t)
+    dev_ms, dev_events, distinct, batch_bytes, batches = eng.last_tally_stats()
+    # algorithmic bytes: every window read once (2-bit bases, qualities and 16 B of
+    # offsets, length and mapq), then per distinct K-mer its 8-byte key and 48-byte
+    # value written once
+    rb = np.concatenate([[0], np.cumsum((L + 3) // 4 + L + 16)])
+    read_bytes = int(sum(rb[b] - rb[a] for a, b in wins))
+    tally_bytes = read_bytes + 56 * distinct
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
+    hbm = peaks["hbm_gbs"] if peaks else 6800.0
+    device = {"ms": dev_ms, "value": dev_events / (dev_ms / 1e3) / 1e9, "unit": "G K-mer events/s",
+              "kmer_events": dev_events, "distinct_kmers": distinct, "batches": batches,
+              "max_batch_table_bytes": batch_bytes, "l2_bytes": 129 * 2**20,
+              "tables_within_l2": batch_bytes <= 129 * 2**20,
+              "roofline": {"bound": "hbm", "achieved": tally_bytes / (dev_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                           "frac": tally_bytes / (dev_ms / 1e3) / 1e9 / hbm, "algorithmic_bytes": tally_bytes,
+                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback"},
+              "timing": "CUDA events around the tally kernels on the engine stream (pg_last_tally_stats)"}
     # the same tally over one window per device break candidate, built on the device
     eng.pileup_regions(ds_regions(ds), params, batched=True)
     tb = []
@@ -260,7 +278,8 @@ def kmer_bench(eng, ds, params, args, threads, K=31, radius=500):
                    "timing": "host wall clock of pg_kmer_tally_breaks (windows built on the device)"}
     out = {"windows": len(wins), "K": K, "kmer_events": events, "edges": int(len(edges)),
            "ms_per_call": 1e3 * sec, "value": events / sec / 1e9, "unit": "G K-mer events/s",
-           "timing": "host wall clock of pg_kmer_tally, edges read back", "from_device_breaks": from_breaks}
+           "timing": "host wall clock of pg_kmer_tally, edges read back", "device": device,
+           "from_device_breaks": from_breaks}
     if not args.no_cpu:
         sample = wins[: max(1, min(len(wins), 16 * threads))]
         parts = [sample[k::threads] for k in range(threads)]

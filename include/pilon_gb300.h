@@ -293,6 +293,14 @@ pg_status pg_kmer_tally_breaks(pg_ctx *ctx, int32_t min_min_depth, int32_t radiu
  * pg_pileup_regions call, measured with CUDA events on the context stream,
  * and its launch count. */
 pg_status pg_last_kernel_ms(pg_ctx *ctx, double *walk_ms, double *total_ms, int32_t *launches);
+/* The last pg_kmer_tally / pg_kmer_tally_breaks call on this context: the
+ * device time of its tally kernels (CUDA events on the context stream, table
+ * clearing and host copies excluded), its K-mer events (2 (L - K) per read of
+ * length L > K in a window), the distinct K-mers of all windows, the largest
+ * batch's table bytes and the number of batches.  A measurement hook; no
+ * counterpart in the reference. */
+pg_status pg_last_tally_stats(pg_ctx *ctx, double *kernel_ms, int64_t *kmer_events, int64_t *distinct_kmers,
+                              int64_t *max_batch_table_bytes, int32_t *batches);
 /* Synchronises the context stream. */
 pg_status pg_sync(pg_ctx *ctx);
 /* Number of pg_pileup_regions calls on this context that replayed a recorded

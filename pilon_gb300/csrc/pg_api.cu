@@ -78,6 +78,10 @@ struct pg_ctx {
   // k-mer tally
   DevBuf kwin, kpre, kslot_base, kslot_cap, kx_base, kx_cap, kkeys, kcnt, kqs, kmq, kq;
   DevBuf kx_keys, kx_used, kx_cnt, kx_qs, kx_mq, kx_q, kedges, kcount, kx_ev, kx_evbase, kx_evcap, kx_evfill;
+  DevBuf kwflag, kused, kchunks;
+  double tally_ms = 0;  // kernel time of the last tally (CUDA events)
+  int64_t tally_events = 0, tally_distinct = 0, tally_max_batch_bytes = 0;
+  int32_t tally_batches = 0;
   // VCF formatting
   DevBuf vlen, vsums, vtext, vname;
   // break candidates
@@ -260,7 +264,8 @@ void pg_close(pg_ctx* c) {
   for (DevBuf* b : all) release(*b);
   DevBuf* km[] = {&c->kwin, &c->kpre, &c->kslot_base, &c->kslot_cap, &c->kx_base, &c->kx_cap, &c->kkeys, &c->kcnt,
                   &c->kqs, &c->kmq, &c->kq, &c->kx_keys, &c->kx_used, &c->kx_cnt, &c->kx_qs, &c->kx_mq, &c->kx_q,
-                  &c->kedges, &c->kcount, &c->kx_ev, &c->kx_evbase, &c->kx_evcap, &c->kx_evfill, &c->vlen,
+                  &c->kedges, &c->kcount, &c->kx_ev, &c->kx_evbase, &c->kx_evcap, &c->kx_evfill, &c->kwflag,
+                  &c->kused, &c->kchunks, &c->vlen,
                   &c->vsums, &c->vtext, &c->vname, &c->bfrag, &c->bsums, &c->btiles, &c->bgaps, &c->bruns,
                   &c->bcnt, &c->boff, &c->bout};
   for (DevBuf* b : km) release(*b);
@@ -836,14 +841,33 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
 }
 
 // The tally over the n_windows windows in c->kwin (device).
+//
+// Tables are sized at a quarter of each window's K-mer events (the distinct
+// K-mers are fewer: every error-free K-mer recurs once per covering read and
+// strand; 13% of the events on the 120 Mb workload) and windows are grouped
+// into batches of about kTallyBatchBytes of tables.  A batch of a few dozen
+// windows would keep its tables in L2 but runs too few CTAs to fill the GPU
+// (measured: 2.4 warps per SM, five times slower), so a batch holds hundreds of
+// windows, each walked by CTAs of kTallyReadsPerChunk reads.  A window whose
+// table fills up (a probe sequence longer than the kernel's bound) is counted
+// again with a table four times larger before its edges are built; the
+// results do not depend on the table size.
+constexpr int64_t kTallyBatchBytes = (int64_t)1 << 30;
+constexpr int64_t kTallyReadsPerChunk = 64;
+
 static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_params* params, int32_t min_depth,
                            pg_kmer_edge* edges, int64_t cap, int64_t* n_edges) {
   cudaStream_t st = c->stream;
   pg_status s;
+  c->tally_ms = 0;
+  c->tally_events = c->tally_distinct = c->tally_max_batch_bytes = 0;
+  c->tally_batches = 0;
   if ((s = ensure(c, c->kpre, sizeof(long long) * 3 * n_windows))) return s;
   launch_kmer_prepass(c->R, P<pg_window>(c->kwin), n_windows, K, P<long long>(c->kpre), st);
   std::vector<long long> pre(3 * (size_t)n_windows);
+  std::vector<pg_window> wins(n_windows);
   CK(cudaMemcpyAsync(pre.data(), c->kpre.p, sizeof(long long) * pre.size(), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(wins.data(), c->kwin.p, sizeof(pg_window) * wins.size(), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   std::vector<int64_t> sbase(n_windows), scap(n_windows), xbase(n_windows), xcap(n_windows), evbase(n_windows),
       evcap(n_windows);
@@ -852,85 +876,134 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
     // (S/Assembler.scala:74), which makes the tally order dependent.
     if (pre[3 * w] >= 100000)
       return fail(c, PG_ERR_LIMIT, "window %d has %lld reads; the tally is exact below 100,000", w, pre[3 * w]);
-    scap[w] = next_pow2(std::max<int64_t>(64, pre[3 * w + 1] + pre[3 * w + 1] / 2));
+    scap[w] = next_pow2(std::max<int64_t>(256, pre[3 * w + 1] / 4));
     xcap[w] = pre[3 * w + 2] > 0 ? next_pow2(std::max<int64_t>(16, 2 * pre[3 * w + 2])) : 0;
     evcap[w] = pre[3 * w + 2];
+    c->tally_events += pre[3 * w + 1];
   }
   const int64_t edge_cap = std::max<int64_t>(cap, 1);
   if ((s = ensure(c, c->kedges, sizeof(pg_kmer_edge) * edge_cap))) return s;
   if ((s = ensure(c, c->kcount, 16))) return s;
+  if ((s = ensure(c, c->kwflag, 4 * (size_t)n_windows))) return s;
+  if ((s = ensure(c, c->kused, 8 * (size_t)n_windows))) return s;
+  if ((s = ensure(c, c->kslot_base, 8 * (size_t)n_windows))) return s;
+  if ((s = ensure(c, c->kslot_cap, 8 * (size_t)n_windows))) return s;
+  if ((s = ensure(c, c->kx_base, 8 * (size_t)n_windows))) return s;
+  if ((s = ensure(c, c->kx_cap, 8 * (size_t)n_windows))) return s;
+  if ((s = ensure(c, c->kx_evbase, 8 * (size_t)n_windows))) return s;
+  if ((s = ensure(c, c->kx_evcap, 8 * (size_t)n_windows))) return s;
+  if ((s = ensure(c, c->kx_evfill, 8 * (size_t)n_windows))) return s;
   CK(cudaMemsetAsync(c->kcount.p, 0, 16, st));
-  const int64_t budget = (int64_t)4 << 30;  // bytes of tables per batch
+  CK(cudaMemsetAsync(c->kused.p, 0, 8 * (size_t)n_windows, st));
+  auto table_bytes = [&](int32_t w) { return scap[w] * 64 + xcap[w] * 80 + evcap[w] * 16; };
+  std::vector<KmerChunk> chunks;
+  std::vector<int32_t> flags;
   int32_t w0 = 0;
   while (w0 < n_windows) {
-    int64_t ns = 0, nx = 0, ne = 0;
     int32_t w1 = w0;
-    while (w1 < n_windows) {
-      int64_t ns2 = ns + scap[w1], nx2 = nx + xcap[w1], ne2 = ne + evcap[w1];
-      if (w1 > w0 && ns2 * 64 + nx2 * 80 + ne2 * 16 > budget) break;
-      sbase[w1] = ns; xbase[w1] = nx; evbase[w1] = ne;
-      ns = ns2; nx = nx2; ne = ne2;
-      w1++;
+    int64_t bytes = 0;
+    while (w1 < n_windows && (w1 == w0 || bytes + table_bytes(w1) <= kTallyBatchBytes)) bytes += table_bytes(w1++);
+    // read chunks of the batch: several CTAs per window
+    chunks.clear();
+    for (int32_t w = w0; w < w1; w++)
+      for (int64_t lo = wins[w].read_begin; lo < wins[w].read_end; lo += kTallyReadsPerChunk)
+        chunks.push_back(KmerChunk{lo, std::min<int64_t>(lo + kTallyReadsPerChunk, wins[w].read_end), w, 0});
+    if ((s = ensure(c, c->kchunks, sizeof(KmerChunk) * std::max<size_t>(chunks.size(), 1)))) return s;
+    if (!chunks.empty())
+      CK(cudaMemcpyAsync(c->kchunks.p, chunks.data(), sizeof(KmerChunk) * chunks.size(), cudaMemcpyHostToDevice, st));
+    for (int attempt = 0;; attempt++) {
+      int64_t ns = 0, nx = 0, ne = 0;
+      for (int32_t w = w0; w < w1; w++) {  // table bases are relative to this batch
+        sbase[w] = ns; xbase[w] = nx; evbase[w] = ne;
+        ns += scap[w]; nx += xcap[w]; ne += evcap[w];
+      }
+      c->tally_max_batch_bytes = std::max(c->tally_max_batch_bytes, ns * 64 + nx * 80 + ne * 16);
+      const size_t nxs = (size_t)std::max<int64_t>(nx, 1);
+      if ((s = ensure(c, c->kkeys, 8 * (size_t)ns))) return s;
+      if ((s = ensure(c, c->kcnt, 16 * (size_t)ns))) return s;
+      if ((s = ensure(c, c->kqs, 32 * (size_t)ns))) return s;
+      if ((s = ensure(c, c->kmq, 4 * (size_t)ns))) return s;
+      if ((s = ensure(c, c->kq, 4 * (size_t)ns))) return s;
+      if ((s = ensure(c, c->kx_ev, 16 * (size_t)std::max<int64_t>(ne, 1)))) return s;
+      if ((s = ensure(c, c->kx_keys, 16 * nxs))) return s;
+      if ((s = ensure(c, c->kx_used, nxs))) return s;
+      if ((s = ensure(c, c->kx_cnt, 16 * nxs))) return s;
+      if ((s = ensure(c, c->kx_qs, 32 * nxs))) return s;
+      if ((s = ensure(c, c->kx_mq, 4 * nxs))) return s;
+      if ((s = ensure(c, c->kx_q, 4 * nxs))) return s;
+      const size_t nw = (size_t)(w1 - w0);
+      CK(cudaMemcpyAsync(P<int64_t>(c->kslot_base) + w0, sbase.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(P<int64_t>(c->kslot_cap) + w0, scap.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(P<int64_t>(c->kx_base) + w0, xbase.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(P<int64_t>(c->kx_cap) + w0, xcap.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(P<int64_t>(c->kx_evbase) + w0, evbase.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(P<int64_t>(c->kx_evcap) + w0, evcap.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
+      CK(cudaMemsetAsync(P<unsigned long long>(c->kx_evfill) + w0, 0, 8 * nw, st));
+      CK(cudaMemsetAsync(P<int32_t>(c->kwflag) + w0, 0, 4 * nw, st));
+      CK(cudaMemsetAsync(P<unsigned long long>(c->kused) + w0, 0, 8 * nw, st));
+      CK(cudaMemsetAsync(c->kkeys.p, 0xFF, 8 * (size_t)ns, st));
+      CK(cudaMemsetAsync(c->kcnt.p, 0, 16 * (size_t)ns, st));
+      CK(cudaMemsetAsync(c->kqs.p, 0, 32 * (size_t)ns, st));
+      CK(cudaMemsetAsync(c->kmq.p, 0, 4 * (size_t)ns, st));
+      CK(cudaMemsetAsync(c->kq.p, 0, 4 * (size_t)ns, st));
+      CK(cudaMemsetAsync(c->kx_used.p, 0, nxs, st));
+      CK(cudaMemsetAsync(c->kx_cnt.p, 0, 16 * nxs, st));
+      CK(cudaMemsetAsync(c->kx_qs.p, 0, 32 * nxs, st));
+      CK(cudaMemsetAsync(c->kx_mq.p, 0, 4 * nxs, st));
+      CK(cudaMemsetAsync(c->kx_q.p, 0, 4 * nxs, st));
+      KmerArgs a;
+      a.R = c->R; a.windows = P<pg_window>(c->kwin); a.win_begin = w0; a.K = K;
+      a.min_qual = params->min_qual; a.default_qual = params->default_qual; a.min_depth = min_depth;
+      a.chunks = P<KmerChunk>(c->kchunks); a.n_chunks = (int32_t)chunks.size();
+      a.slot_base = P<int64_t>(c->kslot_base); a.slot_cap = P<int64_t>(c->kslot_cap);
+      a.keys = P<unsigned long long>(c->kkeys); a.cnt = P<uint32_t>(c->kcnt); a.qs = P<unsigned long long>(c->kqs);
+      a.mq_sum = P<uint32_t>(c->kmq); a.q_sum = P<uint32_t>(c->kq);
+      a.full = P<int32_t>(c->kwflag); a.used = P<unsigned long long>(c->kused);
+      a.x_base = P<int64_t>(c->kx_base); a.x_cap = P<int64_t>(c->kx_cap);
+      a.x_keys = P<unsigned long long>(c->kx_keys); a.x_used = P<uint8_t>(c->kx_used);
+      a.x_cnt = P<uint32_t>(c->kx_cnt); a.x_qs = P<unsigned long long>(c->kx_qs); a.x_mq = P<uint32_t>(c->kx_mq);
+      a.x_q = P<uint32_t>(c->kx_q);
+      a.x_ev_base = P<int64_t>(c->kx_evbase); a.x_ev_cap = P<int64_t>(c->kx_evcap);
+      a.x_ev_fill = P<unsigned long long>(c->kx_evfill); a.x_events = P<longlong2>(c->kx_ev);
+      a.edges = P<pg_kmer_edge>(c->kedges); a.edge_cap = edge_cap;
+      a.n_edges = P<unsigned long long>(c->kcount); a.overflow = (int32_t*)(P<unsigned long long>(c->kcount) + 1);
+      CK(cudaEventRecord(c->e0, st));
+      launch_kmer_count(a, w1 - w0, st);
+      CK(cudaEventRecord(c->e1, st));
+      CK(cudaGetLastError());
+      flags.assign(nw, 0);
+      CK(cudaMemcpyAsync(flags.data(), P<int32_t>(c->kwflag) + w0, 4 * nw, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+      c->tally_ms += ms;
+      bool full = false;
+      for (size_t k = 0; k < nw; k++)
+        if (flags[k]) {
+          full = true;
+          scap[w0 + k] *= 4;
+        }
+      if (!full) {
+        CK(cudaEventRecord(c->e0, st));
+        launch_kmer_edges(a, w1 - w0, st);
+        CK(cudaEventRecord(c->e1, st));
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+        c->tally_ms += ms;
+        break;
+      }
+      if (attempt >= 8) return fail(c, PG_ERR_LIMIT, "K-mer table overflow");
     }
-    std::vector<int64_t> hb(4 * (size_t)n_windows, 0);
-    if ((s = ensure(c, c->kslot_base, 8 * (size_t)n_windows))) return s;
-    if ((s = ensure(c, c->kslot_cap, 8 * (size_t)n_windows))) return s;
-    if ((s = ensure(c, c->kx_base, 8 * (size_t)n_windows))) return s;
-    if ((s = ensure(c, c->kx_cap, 8 * (size_t)n_windows))) return s;
-    if ((s = ensure(c, c->kkeys, 8 * (size_t)ns))) return s;
-    if ((s = ensure(c, c->kcnt, 16 * (size_t)ns))) return s;
-    if ((s = ensure(c, c->kqs, 32 * (size_t)ns))) return s;
-    if ((s = ensure(c, c->kmq, 4 * (size_t)ns))) return s;
-    if ((s = ensure(c, c->kq, 4 * (size_t)ns))) return s;
-    const size_t nxs = (size_t)std::max<int64_t>(nx, 1);
-    if ((s = ensure(c, c->kx_ev, 16 * (size_t)std::max<int64_t>(ne, 1)))) return s;
-    if ((s = ensure(c, c->kx_evbase, 8 * (size_t)n_windows))) return s;
-    if ((s = ensure(c, c->kx_evcap, 8 * (size_t)n_windows))) return s;
-    if ((s = ensure(c, c->kx_evfill, 8 * (size_t)n_windows))) return s;
-    if ((s = ensure(c, c->kx_keys, 16 * nxs))) return s;
-    if ((s = ensure(c, c->kx_used, nxs))) return s;
-    if ((s = ensure(c, c->kx_cnt, 16 * nxs))) return s;
-    if ((s = ensure(c, c->kx_qs, 32 * nxs))) return s;
-    if ((s = ensure(c, c->kx_mq, 4 * nxs))) return s;
-    if ((s = ensure(c, c->kx_q, 4 * nxs))) return s;
-    // table bases are relative to this batch; windows outside it are not touched
-    CK(cudaMemcpyAsync(c->kslot_base.p, sbase.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(c->kslot_cap.p, scap.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(c->kx_base.p, xbase.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(c->kx_cap.p, xcap.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(c->kx_evbase.p, evbase.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(c->kx_evcap.p, evcap.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(c->kx_evfill.p, 0, 8 * (size_t)n_windows, st));
-    CK(cudaMemsetAsync(c->kkeys.p, 0xFF, 8 * (size_t)ns, st));
-    CK(cudaMemsetAsync(c->kcnt.p, 0, 16 * (size_t)ns, st));
-    CK(cudaMemsetAsync(c->kqs.p, 0, 32 * (size_t)ns, st));
-    CK(cudaMemsetAsync(c->kmq.p, 0, 4 * (size_t)ns, st));
-    CK(cudaMemsetAsync(c->kq.p, 0, 4 * (size_t)ns, st));
-    CK(cudaMemsetAsync(c->kx_used.p, 0, nxs, st));
-    CK(cudaMemsetAsync(c->kx_cnt.p, 0, 16 * nxs, st));
-    CK(cudaMemsetAsync(c->kx_qs.p, 0, 32 * nxs, st));
-    CK(cudaMemsetAsync(c->kx_mq.p, 0, 4 * nxs, st));
-    CK(cudaMemsetAsync(c->kx_q.p, 0, 4 * nxs, st));
-    KmerArgs a;
-    a.R = c->R; a.windows = P<pg_window>(c->kwin); a.win_begin = w0; a.K = K;
-    a.min_qual = params->min_qual; a.default_qual = params->default_qual; a.min_depth = min_depth;
-    a.slot_base = P<int64_t>(c->kslot_base); a.slot_cap = P<int64_t>(c->kslot_cap);
-    a.keys = P<unsigned long long>(c->kkeys); a.cnt = P<uint32_t>(c->kcnt); a.qs = P<unsigned long long>(c->kqs);
-    a.mq_sum = P<uint32_t>(c->kmq); a.q_sum = P<uint32_t>(c->kq);
-    a.x_base = P<int64_t>(c->kx_base); a.x_cap = P<int64_t>(c->kx_cap);
-    a.x_keys = P<unsigned long long>(c->kx_keys); a.x_used = P<uint8_t>(c->kx_used); a.x_cnt = P<uint32_t>(c->kx_cnt);
-    a.x_qs = P<unsigned long long>(c->kx_qs); a.x_mq = P<uint32_t>(c->kx_mq); a.x_q = P<uint32_t>(c->kx_q);
-    a.x_ev_base = P<int64_t>(c->kx_evbase); a.x_ev_cap = P<int64_t>(c->kx_evcap);
-    a.x_ev_fill = P<unsigned long long>(c->kx_evfill); a.x_events = P<longlong2>(c->kx_ev);
-    a.edges = P<pg_kmer_edge>(c->kedges); a.edge_cap = edge_cap;
-    a.n_edges = P<unsigned long long>(c->kcount); a.overflow = (int32_t*)(P<unsigned long long>(c->kcount) + 1);
-    launch_kmer_batch(a, w1 - w0, st);
-    CK(cudaGetLastError());
+    c->tally_batches++;
     w0 = w1;
   }
   unsigned long long hc[2];
+  std::vector<unsigned long long> used(n_windows);
   CK(cudaMemcpyAsync(hc, c->kcount.p, 16, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(used.data(), c->kused.p, 8 * (size_t)n_windows, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  for (unsigned long long u : used) c->tally_distinct += (int64_t)u;
   if ((int32_t)hc[1]) return fail(c, PG_ERR_LIMIT, "K-mer table overflow");
   *n_edges = (int64_t)hc[0];
   const int64_t ncopy = std::min<int64_t>((int64_t)hc[0], cap);
@@ -1059,6 +1132,17 @@ pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid,
   CK(cudaGetLastError());
   if (total && out) CK(cudaMemcpyAsync(out, c->vtext.p, (size_t)total, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  return PG_OK;
+}
+
+pg_status pg_last_tally_stats(pg_ctx* c, double* kernel_ms, int64_t* kmer_events, int64_t* distinct_kmers,
+                              int64_t* max_batch_table_bytes, int32_t* batches) {
+  if (!c) return PG_ERR_ARG;
+  if (kernel_ms) *kernel_ms = c->tally_ms;
+  if (kmer_events) *kmer_events = c->tally_events;
+  if (distinct_kmers) *distinct_kmers = c->tally_distinct;
+  if (max_batch_table_bytes) *max_batch_table_bytes = c->tally_max_batch_bytes;
+  if (batches) *batches = c->tally_batches;
   return PG_OK;
 }
 

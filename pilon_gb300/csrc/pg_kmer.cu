@@ -2,11 +2,14 @@
 // addToPileups (S/Assembler.scala:55-87) and the edges of buildGraph
 // (S/Assembler.scala:132-154), for many local-reassembly windows at once.
 //
-// Every window owns a power-of-two open-addressing table in HBM keyed by the
-// 2-bit packed K-mer (K <= 31, so the all-ones word marks an empty slot).  One
-// thread walks one read, forward strand then reverse complement, and for each
-// K-mer adds the following base into the K-mer's PileUp counters with global
-// integer atomics (count[4], qualSum[4], mqSum, qSum).  K-mers containing a
+// Every window owns a power-of-two open-addressing table keyed by the 2-bit
+// packed K-mer (K <= 31, so the all-ones word marks an empty slot); the host
+// groups windows into batches of tables.  One thread walks one read (several
+// CTAs per window, each a chunk of its reads), forward strand then reverse
+// complement, and for each K-mer adds the following base into the K-mer's
+// PileUp counters with global integer atomics (count[4], qualSum[4], mqSum,
+// qSum).  A probe sequence is at most kMaxProbe slots: a longer one marks the
+// window full and the host counts it again in a table four times larger.  K-mers containing a
 // base other than A/C/G/T (N, IUPAC codes, '=') cannot be 2-bit packed; they
 // are tallied exactly by k_kmer_exotic, one thread per window, in a private
 // table keyed by the 4-bit codes of the K-mer.
@@ -69,15 +72,17 @@ __global__ void k_kmer_prepass(Reads R, const pg_window* wins, int32_t K, long l
   if (threadIdx.x < 3) out[3 * blockIdx.x + threadIdx.x] = (long long)s[threadIdx.x];
 }
 
-__global__ void __launch_bounds__(256) k_kmer_count(KmerArgs a) {
-  const int32_t w = a.win_begin + blockIdx.x;
-  const pg_window win = a.windows[w];
+constexpr int64_t kMaxProbe = 256;
+
+__global__ void __launch_bounds__(64) k_kmer_count(KmerArgs a) {
+  const KmerChunk ch = a.chunks[blockIdx.x];
+  const int32_t w = ch.w;
   const int32_t K = a.K;
   const unsigned long long mask = (K == 32) ? ~0ull : ((1ull << (2 * K)) - 1);
   const int64_t base = a.slot_base[w], cap = a.slot_cap[w];
   const int64_t xev0 = a.x_ev_base[w], xev_cap = a.x_ev_cap[w];
   const Reads& R = a.R;
-  for (int64_t i = win.read_begin + threadIdx.x; i < win.read_end; i += blockDim.x) {
+  for (int64_t i = ch.lo + threadIdx.x; i < ch.hi; i += blockDim.x) {
     const int32_t L = R.l_seq[i];
     if (L <= K) continue;
     const uint32_t mq1 = (uint32_t)R.mapq[i] + 1u;
@@ -106,18 +111,20 @@ __global__ void __launch_bounds__(256) k_kmer_count(KmerArgs a) {
             } else {
               int64_t h = (int64_t)(mix64(key) & (unsigned long long)(cap - 1));
               int64_t slot = -1;
-              for (int64_t probe = 0; probe < cap; probe++) {
+              const int64_t probes = cap < kMaxProbe ? cap : kMaxProbe;
+              for (int64_t probe = 0; probe < probes; probe++) {
                 const int64_t s = base + h;
                 unsigned long long k = a.keys[s];
                 if (k == key) { slot = s; break; }
                 if (k == kEmpty) {
                   unsigned long long prev = atomicCAS(&a.keys[s], kEmpty, key);
+                  if (prev == kEmpty) atomicAdd(&a.used[w], 1ull);
                   if (prev == kEmpty || prev == key) { slot = s; break; }
                 }
                 h = (h + 1) & (cap - 1);
               }
               if (slot < 0) {
-                atomicExch(a.overflow, 1);
+                a.full[w] = 1;  // counted again with a larger table
               } else {
                 atomicAdd(&a.cnt[4 * slot + bi], 1u);
                 atomicAdd(&a.qs[4 * slot + bi], (unsigned long long)((uint32_t)q * mq1));
@@ -270,10 +277,14 @@ void launch_kmer_prepass(const Reads& R, const pg_window* wins, int32_t n, int32
   k_kmer_prepass<<<n, 256, 0, s>>>(R, wins, K, out);
 }
 
-void launch_kmer_batch(const KmerArgs& a, int32_t n_win, cudaStream_t s) {
+void launch_kmer_count(const KmerArgs& a, int32_t n_win, cudaStream_t s) {
   if (n_win <= 0) return;
-  k_kmer_count<<<n_win, 256, 0, s>>>(a);
+  if (a.n_chunks > 0) k_kmer_count<<<a.n_chunks, 64, 0, s>>>(a);
   k_kmer_exotic<<<(n_win + 63) / 64, 64, 0, s>>>(a, n_win);
+}
+
+void launch_kmer_edges(const KmerArgs& a, int32_t n_win, cudaStream_t s) {
+  if (n_win <= 0) return;
   k_kmer_edges<<<n_win, 256, 0, s>>>(a);
 }
 

@@ -4,12 +4,22 @@
 
 namespace pg {
 
+// reads [lo, hi) of window w, walked by one CTA of k_kmer_count
+struct KmerChunk {
+  int64_t lo, hi;
+  int32_t w, pad;
+};
+
 struct KmerArgs {
   Reads R;
   const pg_window* windows;
   int32_t win_begin;          // first window of this batch
   int32_t K;
   int32_t min_qual, default_qual, min_depth;
+  const KmerChunk* chunks;    // the batch's read chunks
+  int32_t n_chunks;
+  int32_t* full;              // per window: 1 when a probe sequence ran past the bound (count again, larger)
+  unsigned long long* used;   // per window: distinct K-mers inserted
   // 2-bit tables: slots [slot_base[w], slot_base[w] + slot_cap[w]) of window w
   const int64_t* slot_base;
   const int64_t* slot_cap;
@@ -41,6 +51,9 @@ struct KmerArgs {
 
 void launch_kmer_prepass(const Reads& R, const pg_window* wins, int32_t n, int32_t K, long long* out,
                          cudaStream_t s);
-void launch_kmer_batch(const KmerArgs& a, int32_t n_win, cudaStream_t s);
+// k_kmer_count over the batch's chunks, then k_kmer_exotic
+void launch_kmer_count(const KmerArgs& a, int32_t n_win, cudaStream_t s);
+// k_kmer_edges over the batch's windows
+void launch_kmer_edges(const KmerArgs& a, int32_t n_win, cudaStream_t s);
 
 }  // namespace pg

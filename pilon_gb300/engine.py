@@ -51,6 +51,8 @@ def lib():
                                             C.POINTER(C.c_int32)]),
             "pg_sync": (C.c_int, [vp]),
             "pg_graph_replays": (C.c_int, [vp, C.POINTER(C.c_int32)]),
+            "pg_last_tally_stats": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                                              C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
             "pg_default_serve_config": (None, [C.POINTER(_abi.pg_serve_config)]),
             "pg_serve_open": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(_abi.pg_serve_config),
                                         C.POINTER(_abi.pg_params), i32, vp, vp, vp, C.POINTER(_abi.pg_reads)]),
@@ -260,6 +262,14 @@ class Engine:
 
     def sync(self):
         self._check(self.L.pg_sync(self.h))
+
+    def last_tally_stats(self):
+        """pg_last_tally_stats: (kernel ms, K-mer events, distinct K-mers, largest
+        batch's table bytes, batches) of the last K-mer tally."""
+        ms, ev, dk, tb, nb = C.c_double(), C.c_int64(), C.c_int64(), C.c_int64(), C.c_int32()
+        self._check(self.L.pg_last_tally_stats(self.h, C.byref(ms), C.byref(ev), C.byref(dk), C.byref(tb),
+                                               C.byref(nb)))
+        return ms.value, ev.value, dk.value, tb.value, nb.value
 
     def graph_replays(self):
         """pg_graph_replays: calls of this context that replayed a recorded graph."""
