@@ -40,108 +40,139 @@ __device__ inline CallCtx make_ctx(const CallArgs& a, const RegionDev& g, int64_
   return c;
 }
 
-// 256 threads per CTA, kCallTile / 256 CTAs per call tile: a thread that runs
-// a long indel vote holds back only its own small CTA.
-constexpr int kCallThreads = 256;
-__global__ void __launch_bounds__(kCallThreads, 6) k_call(CallArgs a, int32_t tile_begin) {
-  const int32_t t = tile_begin + blockIdx.x / (kCallTile / kCallThreads);
-  const int32_t r = a.call_tile_region[t];
-  const RegionDev g = a.regions[r];
-  const int32_t p = (t - g.call_tile0) * kCallTile + (blockIdx.x % (kCallTile / kCallThreads)) * kCallThreads +
-                    threadIdx.x;
+// BaseCall and the pass-1 disposition of position p of region r (global
+// position gp) from its loaded record; writes the call record and returns the
+// change kind (0: none).
+__device__ __forceinline__ uint32_t call_position(const CallArgs& a, const RegionDev& g, int32_t p, int64_t gp,
+                                                  const PosRec& rec, bool reads, int32_t min_depth) {
   uint32_t change = 0;
-  if (p < g.size) {
-    const int64_t gp = g.pos_base + p;
-    PosRec rec;
-    load_rec(a.rec, gp, rec);
-    CallCtx c = make_ctx(a, g, gp, wadd(rec.insertions, rec.deletions));
-    const int64_t locus0 = (int64_t)g.start - 1 + p;
-    CallOut o = base_call(rec, a.P, c, gp, locus0);
-    int32_t ins = -1;
-    if (o.flags & PG_CALL_INS) ins = pool_insertion(c, c.ev[o.win_event]);
-    uint32_t f = o.flags;
-    const StatsDev& st = a.stats[r];
-    if (st.read_count > 0) {
-      const int64_t n = rec.cnt[0] + rec.cnt[1] + rec.cnt[2] + rec.cnt[3];
-      const int64_t depth = n + rec.deletions;
-      const uint8_t rb = upper(a.ref[g.ref_off + locus0]);
-      const bool isIns = f & PG_CALL_INS, isDel = f & PG_CALL_DEL;
-      const bool called = (f & PG_CALL_HAS_BASE) || isIns || isDel;
-      if (depth >= st.min_depth && rb != 'N' && called) {
-        // 'A','C','G','T' are the bytes of 0x54474341
-        const uint8_t b = (f & PG_CALL_HAS_BASE) ? (uint8_t)(0x54474341u >> (8 * (f & 3u))) : (uint8_t)'N';
-        const uint8_t alt = (uint8_t)(0x54474341u >> (8 * ((f >> 2) & 3u)));
-        const bool homo = f & PG_CALL_HOMO, homoIndel = f & PG_CALL_HOMO_INDEL;
-        // highConfidence: q = score / n >= 10 (q = 0 when n = 0), i.e. score >= 10 n for n > 0
-        const bool highConf = n > 0 && o.score >= 10 * n;
-        if (homo && b == rb && highConf && !(isIns || isDel)) f |= PG_CALL_CONFIRMED;
-        else if (isIns && homoIndel) change = PG_CHANGE_INS;
-        else if (isDel && homoIndel) change = PG_CHANGE_DEL;
-        else if (b != rb && o.score > 0) {
-          if (homo) change = PG_CHANGE_SNP;
-          else if (a.P.fix_amb || alt != rb) change = PG_CHANGE_AMB;
-        }
+  CallCtx c = make_ctx(a, g, gp, wadd(rec.insertions, rec.deletions));
+  const int64_t locus0 = (int64_t)g.start - 1 + p;
+  CallOut o = base_call(rec, a.P, c, gp, locus0);
+  int32_t ins = -1;
+  if (o.flags & PG_CALL_INS) ins = pool_insertion(c, c.ev[o.win_event]);
+  uint32_t f = o.flags;
+  if (reads) {
+    const int64_t n = rec.cnt[0] + rec.cnt[1] + rec.cnt[2] + rec.cnt[3];
+    const int64_t depth = n + rec.deletions;
+    const uint8_t rb = upper(a.ref[g.ref_off + locus0]);
+    const bool isIns = f & PG_CALL_INS, isDel = f & PG_CALL_DEL;
+    const bool called = (f & PG_CALL_HAS_BASE) || isIns || isDel;
+    if (depth >= min_depth && rb != 'N' && called) {
+      // 'A','C','G','T' are the bytes of 0x54474341
+      const uint8_t b = (f & PG_CALL_HAS_BASE) ? (uint8_t)(0x54474341u >> (8 * (f & 3u))) : (uint8_t)'N';
+      const uint8_t alt = (uint8_t)(0x54474341u >> (8 * ((f >> 2) & 3u)));
+      const bool homo = f & PG_CALL_HOMO, homoIndel = f & PG_CALL_HOMO_INDEL;
+      // highConfidence: q = score / n >= 10 (q = 0 when n = 0), i.e. score >= 10 n for n > 0
+      const bool highConf = n > 0 && o.score >= 10 * n;
+      if (homo && b == rb && highConf && !(isIns || isDel)) f |= PG_CALL_CONFIRMED;
+      else if (isIns && homoIndel) change = PG_CHANGE_INS;
+      else if (isDel && homoIndel) change = PG_CHANGE_DEL;
+      else if (b != rb && o.score > 0) {
+        if (homo) change = PG_CHANGE_SNP;
+        else if (a.P.fix_amb || alt != rb) change = PG_CHANGE_AMB;
       }
     }
-    f |= change << 9;
-    a.rec.call[gp] = f;
-    a.rec.score[gp] = o.score;
-    a.rec.indel_len[gp] = o.indel_len;
-    a.rec.ins_str[gp] = ins;
   }
-  unsigned b = __ballot_sync(FULL, change != 0);
-  if ((threadIdx.x & 31) == 0 && b) atomicAdd(&a.cand_count[t], __popc(b));
+  f |= change << 9;
+  a.rec.call[gp] = f;
+  a.rec.score[gp] = o.score;
+  a.rec.indel_len[gp] = o.indel_len;
+  a.rec.ins_str[gp] = ins;
+  return change;
+}
+
+// 256 threads per CTA, two positions per thread (p and p + 256), two CTAs per
+// call tile: both records are loaded before either call is made, and a thread
+// that runs a long indel vote holds back only its own small CTA.
+constexpr int kCallThreads = 256;
+constexpr int kCallPer = 2;
+constexpr int kCallCtas = kCallTile / (kCallThreads * kCallPer);
+static_assert(kCallCtas * kCallThreads * kCallPer == kCallTile, "call tile split");
+
+__global__ void __launch_bounds__(kCallThreads, 3) k_call(CallArgs a, int32_t tile_begin) {
+  const int32_t t = tile_begin + blockIdx.x / kCallCtas;
+  const int32_t r = a.call_tile_region[t];
+  const RegionDev g = a.regions[r];
+  const int32_t p0 = (t - g.call_tile0) * kCallTile + (blockIdx.x % kCallCtas) * (kCallThreads * kCallPer) +
+                     threadIdx.x;
+  const StatsDev& st = a.stats[r];
+  const bool reads = st.read_count > 0;
+  const int32_t min_depth = st.min_depth;
+  PosRec rec[kCallPer];
+#pragma unroll
+  for (int k = 0; k < kCallPer; k++)
+    if (p0 + k * kCallThreads < g.size) load_rec(a.rec, g.pos_base + p0 + k * kCallThreads, rec[k]);
+  uint32_t changes = 0;
+#pragma unroll
+  for (int k = 0; k < kCallPer; k++) {
+    const int32_t p = p0 + k * kCallThreads;
+    if (p < g.size) changes += call_position(a, g, p, g.pos_base + p, rec[k], reads, min_depth) != 0;
+  }
+  changes = __reduce_add_sync(FULL, changes);
+  if ((threadIdx.x & 31) == 0 && changes) atomicAdd(&a.cand_count[t], (int32_t)changes);
 }
 
 void launch_call(const CallArgs& a, int32_t tile_begin, int32_t n_tiles, cudaStream_t s) {
   if (n_tiles <= 0) return;
-  k_call<<<n_tiles * (kCallTile / kCallThreads), kCallThreads, 0, s>>>(a, tile_begin);
+  k_call<<<n_tiles * kCallCtas, kCallThreads, 0, s>>>(a, tile_begin);
 }
 
-__global__ void __launch_bounds__(kCallTile) k_cand_list(CallArgs a, const int32_t* cand_off, Cand* cands,
-                                                          int32_t cand_cap, int32_t tile_begin) {
-  __shared__ int32_t s_warp[32];
+// The change candidates of a call tile in position order, at the tile's offset
+// from the scan of k_call's per-tile counts.  256 threads per 1024-position
+// tile: the call words are loaded coalesced into shared memory, each thread
+// ranks four consecutive positions, and a block scan joins the threads.
+constexpr int kCandThreads = 256;
+__global__ void __launch_bounds__(kCandThreads) k_cand_list(CallArgs a, const int32_t* cand_off, Cand* cands,
+                                                             int32_t cand_cap, int32_t tile_begin) {
+  __shared__ __align__(16) uint32_t s_k[kCallTile];
+  __shared__ int32_t s_w[kCandThreads / 32];
   const int32_t t = tile_begin + blockIdx.x;
+  if (a.cand_count[t] == 0) return;  // k_call counted the tile's changes: none (the whole CTA leaves)
   const int32_t r = a.call_tile_region[t];
   const RegionDev g = a.regions[r];
-  const int32_t p = (t - g.call_tile0) * kCallTile + threadIdx.x;
-  uint32_t kind = 0;
-  int64_t gp = 0;
-  if (p < g.size) {
-    gp = g.pos_base + p;
-    kind = PG_CALL_CHANGE(a.rec.call[gp]);
-  }
+  const int32_t p0 = (t - g.call_tile0) * kCallTile;
+  const int32_t n = min(kCallTile, g.size - p0);
+  for (int32_t i = threadIdx.x; i < kCallTile; i += kCandThreads)
+    s_k[i] = i < n ? PG_CALL_CHANGE(a.rec.call[g.pos_base + p0 + i]) : 0u;
+  __syncthreads();
+  const uint4 k4 = reinterpret_cast<const uint4*>(s_k)[threadIdx.x];  // positions 4 tid .. 4 tid + 3
+  const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
+  const int32_t mine = (k4.x != 0) + (k4.y != 0) + (k4.z != 0) + (k4.w != 0);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned b = __ballot_sync(FULL, kind != 0);
-  if (lane == 0) s_warp[warp] = __popc(b);
-  __syncthreads();
-  if (warp == 0) {
-    int32_t v = s_warp[lane];
-    int32_t x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-      int32_t y = __shfl_up_sync(FULL, x, o);
-      if (lane >= o) x += y;
-    }
-    s_warp[lane] = x - v;
+  int32_t incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t y = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += y;
   }
+  if (lane == 31) s_w[warp] = incl;
   __syncthreads();
-  if (kind) {
-    int32_t rank = s_warp[warp] + __popc(b & ((1u << lane) - 1u));
-    Cand c;
-    c.gpos = gp;
-    c.region = r;
-    c.p = p;
-    c.kind = (int32_t)kind;
-    c.len = a.rec.indel_len[gp];
-    const int32_t slot = cand_off[t] + rank;
-    if (slot < cand_cap) cands[slot] = c;
+  int32_t before = incl - mine;
+  for (int w = 0; w < warp; w++) before += s_w[w];
+  if (mine) {
+    int32_t slot = cand_off[t] + before;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (!kk[j]) continue;
+      const int32_t p = p0 + 4 * (int32_t)threadIdx.x + j;
+      const int64_t gp = g.pos_base + p;
+      Cand c;
+      c.gpos = gp;
+      c.region = r;
+      c.p = p;
+      c.kind = (int32_t)kk[j];
+      c.len = a.rec.indel_len[gp];
+      if (slot < cand_cap) cands[slot] = c;
+      slot++;
+    }
   }
 }
 
 void launch_cand_list(const CallArgs& a, const int32_t* cand_off, Cand* cands, int32_t cand_cap,
                       int32_t tile_begin, int32_t n_tiles, cudaStream_t s) {
   if (n_tiles <= 0) return;
-  k_cand_list<<<n_tiles, kCallTile, 0, s>>>(a, cand_off, cands, cand_cap, tile_begin);
+  k_cand_list<<<n_tiles, kCandThreads, 0, s>>>(a, cand_off, cands, cand_cap, tile_begin);
 }
 
 // Pass 1 is a left-to-right scan: a candidate inside an earlier accepted

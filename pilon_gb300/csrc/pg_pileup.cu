@@ -1168,22 +1168,45 @@ __device__ inline void block_scan3(uint32_t& a, uint32_t& b, uint32_t& c, uint32
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kCallTile) k_scan_tiles_a(const RegionDev* regions, const int32_t* tile_region,
-                                                             Records rec, int32_t* tile_sums, int32_t tile_begin) {
-  __shared__ uint32_t s_a[32], s_b[32], s_c[32];
+// Phase a: per call tile the sums of the physical-coverage and insert-size
+// difference words and of the event counts (insertions + deletions).  256
+// threads per 1024-position tile, four positions each (coalesced, all loads of
+// a thread in flight at once), then a block reduction.
+constexpr int kScanThreads = 256;
+constexpr int kScanPer = kCallTile / kScanThreads;
+static_assert(kScanPer * kScanThreads == kCallTile, "four positions per scan thread");
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles_a(const RegionDev* regions, const int32_t* tile_region,
+                                                                Records rec, int32_t* tile_sums, int32_t tile_begin) {
+  __shared__ uint32_t s_r[3][kScanThreads / 32];
   const int32_t t = tile_begin + blockIdx.x;
   const RegionDev& g = regions[tile_region[t]];
-  const int32_t p = (t - g.call_tile0) * kCallTile + threadIdx.x;
-  uint32_t a = 0, b = 0, c = 0;
-  if (p < g.size) {
-    const int64_t gp = g.pos_base + p;
-    a = (uint32_t)rec.phys_cov[gp];
-    b = (uint32_t)rec.insert_size[gp];
-    c = (uint32_t)rec.insertions[gp] + (uint32_t)rec.deletions[gp];
+  const int32_t p0 = (t - g.call_tile0) * kCallTile;
+  uint32_t va[kScanPer], vb[kScanPer], vc[kScanPer];
+#pragma unroll
+  for (int k = 0; k < kScanPer; k++) {
+    const int32_t p = p0 + threadIdx.x + k * kScanThreads;
+    va[k] = vb[k] = vc[k] = 0;
+    if (p < g.size) {
+      const int64_t gp = g.pos_base + p;
+      va[k] = (uint32_t)rec.phys_cov[gp];
+      vb[k] = (uint32_t)rec.insert_size[gp];
+      vc[k] = (uint32_t)rec.insertions[gp] + (uint32_t)rec.deletions[gp];
+    }
   }
-  block_scan3(a, b, c, s_a, s_b, s_c);
-  if (threadIdx.x == blockDim.x - 1) {
-    tile_sums[3 * t] = (int32_t)a; tile_sums[3 * t + 1] = (int32_t)b; tile_sums[3 * t + 2] = (int32_t)c;
+  uint32_t a = 0, b = 0, c = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; k++) { a += va[k]; b += vb[k]; c += vc[k]; }
+  a = __reduce_add_sync(FULL, a);
+  b = __reduce_add_sync(FULL, b);
+  c = __reduce_add_sync(FULL, c);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { s_r[0][warp] = a; s_r[1][warp] = b; s_r[2][warp] = c; }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    uint32_t v = 0;
+    for (int w = 0; w < kScanThreads / 32; w++) v += s_r[threadIdx.x][w];
+    tile_sums[3 * t + threadIdx.x] = (int32_t)v;
   }
 }
 
@@ -1254,28 +1277,67 @@ __global__ void __launch_bounds__(1024) k_scan_tiles_b(const RegionDev* regions,
   }
 }
 
-__global__ void __launch_bounds__(kCallTile) k_scan_tiles_c(const RegionDev* regions, const int32_t* tile_region,
-                                                             Records rec, const int32_t* tile_sums,
-                                                             int32_t tile_begin) {
+// Phase c: the inclusive scan inside each tile plus the tile's prefix from
+// phase b, then insertSize /= physCov where physCov > 0 (S/PileUpRegion.scala:
+// 90-100), and each position's first event slot.  The tile's words are loaded
+// coalesced into shared memory, each thread scans four consecutive positions,
+// a block scan joins the threads, and the results go back coalesced.
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles_c(const RegionDev* regions, const int32_t* tile_region,
+                                                                Records rec, const int32_t* tile_sums,
+                                                                int32_t tile_begin) {
+  __shared__ __align__(16) uint32_t s_v[3][kCallTile];
   __shared__ uint32_t s_a[32], s_b[32], s_c[32];
   const int32_t t = tile_begin + blockIdx.x;
   const RegionDev& g = regions[tile_region[t]];
-  const int32_t p = (t - g.call_tile0) * kCallTile + threadIdx.x;
-  uint32_t a = 0, b = 0, c = 0, vc = 0;
-  const int64_t gp = g.pos_base + p;
-  if (p < g.size) {
-    a = (uint32_t)rec.phys_cov[gp];
-    b = (uint32_t)rec.insert_size[gp];
-    vc = c = (uint32_t)rec.insertions[gp] + (uint32_t)rec.deletions[gp];
+  const int32_t p0 = (t - g.call_tile0) * kCallTile;
+  const int32_t n = min(kCallTile, g.size - p0);
+#pragma unroll
+  for (int k = 0; k < kScanPer; k++) {
+    const int32_t i = threadIdx.x + k * kScanThreads;
+    uint32_t a = 0, b = 0, c = 0;
+    if (i < n) {
+      const int64_t gp = g.pos_base + p0 + i;
+      a = (uint32_t)rec.phys_cov[gp];
+      b = (uint32_t)rec.insert_size[gp];
+      c = (uint32_t)rec.insertions[gp] + (uint32_t)rec.deletions[gp];
+    }
+    s_v[0][i] = a; s_v[1][i] = b; s_v[2][i] = c;
   }
-  block_scan3(a, b, c, s_a, s_b, s_c);
-  if (p < g.size) {
-    int32_t pc = (int32_t)(a + (uint32_t)tile_sums[3 * t]);
-    int32_t is = (int32_t)(b + (uint32_t)tile_sums[3 * t + 1]);
-    if (pc > 0) is = is / pc;
-    rec.phys_cov[gp] = pc;
-    rec.insert_size[gp] = is;
-    if (vc) rec.ev_end[gp] = (int32_t)(c - vc + (uint32_t)tile_sums[3 * t + 2]);  // first slot
+  __syncthreads();
+  // positions 4 * tid .. 4 * tid + 3
+  const uint4 xa = reinterpret_cast<const uint4*>(s_v[0])[threadIdx.x];
+  const uint4 xb = reinterpret_cast<const uint4*>(s_v[1])[threadIdx.x];
+  const uint4 xc = reinterpret_cast<const uint4*>(s_v[2])[threadIdx.x];
+  uint32_t a = xa.x + xa.y + xa.z + xa.w, b = xb.x + xb.y + xb.z + xb.w, c = xc.x + xc.y + xc.z + xc.w;
+  const uint32_t ta = a, tb = b, tc = c;
+  block_scan3(a, b, c, s_a, s_b, s_c);  // inclusive over threads
+  // exclusive prefix of this thread's first position, with the tile's prefix
+  uint32_t pa = a - ta + (uint32_t)tile_sums[3 * t], pb = b - tb + (uint32_t)tile_sums[3 * t + 1];
+  uint32_t pc = c - tc + (uint32_t)tile_sums[3 * t + 2];
+  const uint32_t ea[4] = {xa.x, xa.y, xa.z, xa.w}, eb[4] = {xb.x, xb.y, xb.z, xb.w}, ec[4] = {xc.x, xc.y, xc.z, xc.w};
+  uint32_t oa[4], ob[4], oc[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    oc[j] = ec[j] ? pc : 0xffffffffu;  // first event slot of the position, or none
+    pa += ea[j]; pb += eb[j]; pc += ec[j];
+    int32_t cov = (int32_t)pa, is = (int32_t)pb;
+    if (cov > 0) is = is / cov;
+    oa[j] = (uint32_t)cov; ob[j] = (uint32_t)is;
+  }
+  __syncthreads();  // every thread has read its words
+  reinterpret_cast<uint4*>(s_v[0])[threadIdx.x] = make_uint4(oa[0], oa[1], oa[2], oa[3]);
+  reinterpret_cast<uint4*>(s_v[1])[threadIdx.x] = make_uint4(ob[0], ob[1], ob[2], ob[3]);
+  reinterpret_cast<uint4*>(s_v[2])[threadIdx.x] = make_uint4(oc[0], oc[1], oc[2], oc[3]);
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kScanPer; k++) {
+    const int32_t i = threadIdx.x + k * kScanThreads;
+    if (i < n) {
+      const int64_t gp = g.pos_base + p0 + i;
+      rec.phys_cov[gp] = (int32_t)s_v[0][i];
+      rec.insert_size[gp] = (int32_t)s_v[1][i];
+      if (s_v[2][i] != 0xffffffffu) rec.ev_end[gp] = (int32_t)s_v[2][i];  // first slot
+    }
   }
 }
 
@@ -1285,9 +1347,9 @@ void launch_physcov_scan(const RegionDev* regions, const int32_t* call_tile_regi
   (void)region_begin;
   (void)n_regions;
   if (n_tiles <= 0) return;
-  k_scan_tiles_a<<<n_tiles, kCallTile, 0, s>>>(regions, call_tile_region, rec, tile_sums, tile_begin);
+  k_scan_tiles_a<<<n_tiles, kScanThreads, 0, s>>>(regions, call_tile_region, rec, tile_sums, tile_begin);
   k_scan_tiles_b<<<1, 1024, 0, s>>>(regions, call_tile_region, stats, tile_sums, tile_begin, n_tiles);
-  k_scan_tiles_c<<<n_tiles, kCallTile, 0, s>>>(regions, call_tile_region, rec, tile_sums, tile_begin);
+  k_scan_tiles_c<<<n_tiles, kScanThreads, 0, s>>>(regions, call_tile_region, rec, tile_sums, tile_begin);
 }
 
 // ---------------------------------------------------------------------------
