@@ -276,6 +276,16 @@ pg_status pg_format_vcf(pg_ctx *ctx, int32_t region, const char *name, int32_t d
  * none. */
 pg_status pg_find_breaks(pg_ctx *ctx, int32_t min_min_depth, pg_break *out, int64_t cap, int64_t *n_breaks);
 
+/* GenomeRegion.duplicationEvents (S/GenomeRegion.scala:735-741) for every
+ * region of the last pg_pileup_regions call, on the device: pass 2 of
+ * postProcess, copyNumber = Math.round(smooth(fragCoverage, 200) / mean
+ * fragCoverage) (S/GenomeRegion.scala:190-210, 274-283), then summaryRegions of
+ * copyNumber > 1 with slop 2000, away from the region's ends, longer than
+ * 10,000 bases: the <DUP> records of Vcf.writeDup (S/Vcf.scala:194-202).
+ * Sorted by region, then start (pg_break records); *n_dups receives the count
+ * (up to cap).  Regions without reads have none. */
+pg_status pg_find_duplications(pg_ctx *ctx, pg_break *out, int64_t cap, int64_t *n_dups);
+
 /* The K-mer tally of pg_kmer_tally over one window per break of
  * pg_find_breaks(min_min_depth), built on the device without a host round
  * trip: window k holds the reads of break k's contig that start in

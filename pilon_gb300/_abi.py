@@ -158,6 +158,7 @@ EXPORTED = [
     "pg_fetch_stats", "pg_fetch_region", "pg_set_tuning", "pg_kmer_tally",
     "pg_last_kernel_ms", "pg_sync", "pg_phys_cov_scan_static", "pg_format_vcf", "pg_find_breaks",
     "pg_kmer_tally_breaks", "pg_fetch_all", "pg_graph_replays", "pg_last_tally_stats",
+    "pg_find_duplications",
     "pg_default_serve_config", "pg_serve_open", "pg_serve_submit", "pg_serve_poll", "pg_serve_release",
     "pg_serve_stats", "pg_serve_error", "pg_serve_close",
 ]

@@ -86,6 +86,7 @@ struct pg_ctx {
   DevBuf vlen, vsums, vtext, vname;
   // break candidates
   DevBuf bfrag, bsums, btiles, bgaps, bruns, bcnt, boff, bout;
+  DevBuf druns, dout, dcount;  // duplication events
   int64_t brk_n = -1;             // breaks of the last pileup call on the device, -1: not found yet
   int32_t brk_mmd = 0;
   // CUDA graph of the batched pipeline, replayed while the plan and buffers are unchanged
@@ -267,7 +268,7 @@ void pg_close(pg_ctx* c) {
                   &c->kedges, &c->kcount, &c->kx_ev, &c->kx_evbase, &c->kx_evcap, &c->kx_evfill, &c->kwflag,
                   &c->kused, &c->kchunks, &c->vlen,
                   &c->vsums, &c->vtext, &c->vname, &c->bfrag, &c->bsums, &c->btiles, &c->bgaps, &c->bruns,
-                  &c->bcnt, &c->boff, &c->bout};
+                  &c->bcnt, &c->boff, &c->bout, &c->druns, &c->dout, &c->dcount};
   for (DevBuf* b : km) release(*b);
   for (auto& b : c->rec_i32) release(b);
   for (auto& b : c->rd) release(b);
@@ -1063,6 +1064,45 @@ pg_status pg_find_breaks(pg_ctx* c, int32_t min_min_depth, pg_break* out, int64_
     CK(cudaMemcpyAsync(out, c->bout.p, sizeof(pg_break) * (size_t)ncopy, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
   }
+  return PG_OK;
+}
+
+pg_status pg_find_duplications(pg_ctx* c, pg_break* out, int64_t cap, int64_t* n_dups) {
+  const Range nvtx_range("pg_find_duplications");
+  if (!c || !n_dups || cap < 0 || (cap > 0 && !out)) return fail(c, PG_ERR_ARG, "bad arguments");
+  if (!c->have_results) return fail(c, PG_ERR_STATE, "no pileup results: call pg_pileup_regions first");
+  cudaSetDevice(c->device);
+  *n_dups = 0;
+  if (c->n_regions == 0 || c->n_call_tiles == 0) return PG_OK;
+  // fragCoverage and its region sums are made with the break candidates
+  pg_status s = find_breaks_device(c, c->brk_n >= 0 ? c->brk_mmd : 5);
+  if (s) return s;
+  cudaStream_t st = c->stream;
+  const int64_t dcap = c->n_positions / 2000 + c->n_regions + 16;  // runs are > 2001 apart
+  if ((s = ensure(c, c->druns, sizeof(int2) * (size_t)c->n_call_tiles))) return s;
+  if ((s = ensure(c, c->dout, sizeof(pg_break) * (size_t)dcap))) return s;
+  if ((s = ensure(c, c->dcount, 8))) return s;
+  CK(cudaMemsetAsync(c->dcount.p, 0, 8, st));
+  BreakArgs a;
+  a.regions = P<RegionDev>(c->regions); a.call_tile_region = P<int32_t>(c->call_tile_region);
+  a.tile_begin = 0; a.n_tiles = c->n_call_tiles; a.rec = records(c); a.stats = P<StatsDev>(c->stats);
+  a.ref = P<uint8_t>(c->ref); a.min_min_depth = c->brk_mmd; a.frag = P<int32_t>(c->bfrag);
+  a.sums = P<long long>(c->bsums);
+  launch_duplications(a, c->n_regions, P<int2>(c->druns), P<pg_break>(c->dout), dcap,
+                      P<unsigned long long>(c->dcount), st);
+  CK(cudaGetLastError());
+  unsigned long long n = 0;
+  CK(cudaMemcpyAsync(&n, c->dcount.p, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::vector<pg_break> v(std::min<uint64_t>(n, (uint64_t)dcap));
+  if (!v.empty())
+    CK(cudaMemcpyAsync(v.data(), c->dout.p, sizeof(pg_break) * v.size(), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::sort(v.begin(), v.end(), [](const pg_break& x, const pg_break& y) {
+    return x.region != y.region ? x.region < y.region : x.start < y.start;
+  });
+  *n_dups = (int64_t)v.size();
+  for (int64_t k = 0; k < std::min<int64_t>(cap, (int64_t)v.size()); k++) out[k] = v[k];
   return PG_OK;
 }
 

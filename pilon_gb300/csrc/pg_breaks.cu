@@ -312,6 +312,138 @@ void launch_breaks(const BreakArgs& a, int32_t n_regions, cudaStream_t s) {
   k_brk_compact<<<(n_regions + 3) / 4, 128, 0, s>>>(a, n_regions);
 }
 
+// ---------------------------------------------------------------------------
+// Pass 2 of GenomeRegion.postProcess (S/GenomeRegion.scala:274-283) and
+// duplicationEvents (:735-741) on the fragCoverage of k_brk_frag / k_brk_spans:
+//   smoothCov = smooth(fragCoverage, 200)          (S/GenomeRegion.scala:190-210)
+//   copyNumber(i) = Math.round(smoothCov(i) / mean).toShort, 0 when mean <= 0
+//   duplications = summaryRegions(copyNumber > 1, 2000) filter (size > 10000)
+// smooth keeps the reference's arithmetic: the Int accumulator starts with
+// input(0) and never drops it, so for a region of n > 200 positions
+//   smoothCov(x) = (input(0) + sum input(x-99 .. x+100) + 100) / 200   for 101 <= x <= n-101,
+//   smoothCov(x) = 0 for x <= 100 (result(100) is never written before it is
+//   copied) and result(n-101) for x >= n-100 (0 itself when n <= 201); for
+//   n <= 200 every position gets sum(input) / n.  With a merge slop of 2000
+//   every tested position of a 1024-position tile belongs to one run, so each
+//   tile reports its first and last tested position and one thread per region
+//   joins the tiles in order.
+constexpr int kDupHalo = 200;                      // positions loaded before and after a tile
+constexpr int kDupSpan = kCallTile + 2 * kDupHalo;  // 1424
+constexpr int kDupPer = (kDupSpan + kBrkThreads - 1) / kBrkThreads;  // 6 per thread
+
+__global__ void __launch_bounds__(kBrkThreads) k_dup_tiles(BreakArgs a, int2* tile_runs) {
+  __shared__ uint32_t s_p[kBrkThreads * kDupPer + 1];  // prefix sums of the window (wrapping Int)
+  __shared__ uint32_t s_w[32];
+  __shared__ int32_t s_fl[2][32];
+  const int32_t t = a.tile_begin + blockIdx.x;
+  const int32_t r = a.call_tile_region[t];
+  const RegionDev g = a.regions[r];
+  const int32_t n = g.size;
+  const int32_t x0 = (t - g.call_tile0) * kCallTile;
+  const int32_t w0 = x0 - kDupHalo;  // region index of window slot 0
+  const bool reads = a.stats[r].read_count > 0;
+  const double mean = (double)a.sums[3 * r] / (double)n;
+  // prefix sums over the slots [w0, w0 + kBrkThreads * kDupPer), positions outside the region 0
+  uint32_t v[kDupPer], tot = 0;
+#pragma unroll
+  for (int q = 0; q < kDupPer; q++) {
+    const int32_t x = w0 + kDupPer * (int32_t)threadIdx.x + q;
+    v[q] = (x >= 0 && x < n) ? (uint32_t)a.frag[g.pos_base + x] : 0u;
+    tot += v[q];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = tot;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_w[warp] = incl;
+  __syncthreads();
+  uint32_t run = incl - tot;
+  for (int w = 0; w < warp; w++) run += s_w[w];
+#pragma unroll
+  for (int q = 0; q < kDupPer; q++) {
+    s_p[kDupPer * threadIdx.x + q] = run;  // sum of the slots before this one
+    run += v[q];
+  }
+  if (threadIdx.x == kBrkThreads - 1) s_p[kBrkThreads * kDupPer] = run;
+  __syncthreads();
+  const uint32_t in0 = (uint32_t)a.frag[g.pos_base];
+  // for n <= 200 the window holds the whole region: its input sum
+  const uint32_t all = s_p[kBrkThreads * kDupPer];
+  // smoothCov of region index x (101 <= x <= n - 101, n > 200): slots x - 99 .. x + 100
+  auto smooth_at = [&](int32_t x) -> int32_t {
+    const uint32_t win = s_p[x + 101 - w0] - s_p[x - 99 - w0];
+    return (int32_t)wadd((int32_t)(in0 + win), 100) / 200;
+  };
+  int32_t first = -1, last = -1;
+  if (reads && mean > 0) {
+    for (int32_t x = x0 + threadIdx.x; x < min(x0 + kCallTile, n); x += kBrkThreads) {
+      int32_t sm;
+      if (n <= 200) sm = (int32_t)all / n;
+      else if (x <= 100) sm = 0;
+      else if (x >= n - 100) sm = n - 101 >= 101 ? smooth_at(n - 101) : 0;  // result(n-101), written when n >= 202
+      else sm = smooth_at(x);
+      const double y = (double)sm / mean;
+      const double f = floor(y);
+      const long long cn = (long long)(y - f >= 0.5 ? f + 1.0 : f);  // Math.round: ties up
+      if ((int16_t)cn > 1) {
+        if (first < 0) first = x;
+        last = x;
+      }
+    }
+  }
+  // the tile's first and last tested index (threads hold strided positions)
+  int32_t fmin = first < 0 ? INT32_MAX : first, lmax = last;
+  for (int o = 16; o > 0; o >>= 1) {
+    fmin = min(fmin, __shfl_down_sync(FULL, fmin, o));
+    lmax = max(lmax, __shfl_down_sync(FULL, lmax, o));
+  }
+  if (lane == 0) { s_fl[0][warp] = fmin; s_fl[1][warp] = lmax; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int32_t f2 = INT32_MAX, l2 = -1;
+    for (int w = 0; w < kBrkThreads / 32; w++) { f2 = min(f2, s_fl[0][w]); l2 = max(l2, s_fl[1][w]); }
+    tile_runs[t] = make_int2(l2 < 0 ? -1 : f2, l2);
+  }
+}
+
+// One thread per region: summaryRegions(copyNumber > 1, 2000) over the tiles'
+// runs, then the filters !nearEdge and size > 10000; appends (region, start,
+// stop) loci to out (order fixed by the host).
+__global__ void k_dup_merge(BreakArgs a, int32_t n_regions, const int2* tile_runs, pg_break* out, int64_t cap,
+                            unsigned long long* n_out) {
+  const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_regions) return;
+  const RegionDev g = a.regions[r];
+  int32_t first = -1, last = -1;
+  auto emit = [&]() {
+    // nearEdge: within 100 of the region's ends; size = last - first + 1
+    if (first >= 100 && g.size - 1 - last >= 100 && last - first + 1 > 10000) {
+      const unsigned long long k = atomicAdd(n_out, 1ull);
+      if ((int64_t)k < cap) out[k] = pg_break{r, g.start + first, g.start + last, 0};
+    }
+  };
+  for (int32_t t = g.call_tile0; t < g.call_tile0 + g.n_call_tiles; t++) {
+    const int2 fl = tile_runs[t];
+    if (fl.y < 0) continue;
+    if (last >= 0 && fl.x - last > 2001) {  // untested more than slop past the run's last tested position
+      emit();
+      first = -1;
+    }
+    if (first < 0) first = fl.x;
+    last = fl.y;
+  }
+  if (last >= 0) emit();
+}
+
+void launch_duplications(const BreakArgs& a, int32_t n_regions, int2* tile_runs, pg_break* out, int64_t cap,
+                         unsigned long long* n_out, cudaStream_t s) {
+  if (a.n_tiles <= 0) return;
+  k_dup_tiles<<<a.n_tiles, kBrkThreads, 0, s>>>(a, tile_runs);
+  k_dup_merge<<<(n_regions + 127) / 128, 128, 0, s>>>(a, n_regions, tile_runs, out, cap, n_out);
+}
+
 void launch_break_windows(const Reads& R, const RegionDev* regions, const pg_break* brk, int32_t n,
                           int32_t radius, const ReadExtent* ext, pg_window* out, cudaStream_t s) {
   if (n <= 0) return;

@@ -30,6 +30,11 @@ struct BreakArgs {
 };
 
 void launch_breaks(const BreakArgs& a, int32_t n_regions, cudaStream_t s);
+// GenomeRegion.duplicationEvents of every region from the fragCoverage and sums
+// that launch_breaks computed: tile_runs holds one int2 per call tile; the
+// duplications go to out (unordered) and their number to *n_out.
+void launch_duplications(const BreakArgs& a, int32_t n_regions, int2* tile_runs, pg_break* out, int64_t cap,
+                         unsigned long long* n_out, cudaStream_t s);
 // Windows of the K-mer tally from the breaks: the reads of the break's contig
 // that start in [start - radius - max_span, stop + radius] (the read store's
 // index, like the host's ReadIndex.range_for).

@@ -64,6 +64,7 @@ def lib():
             "pg_serve_close": (None, [vp]),
             "pg_format_vcf": (C.c_int, [vp, i32, C.c_char_p, i32, i32, i32, vp, i64, C.POINTER(C.c_int64)]),
             "pg_find_breaks": (C.c_int, [vp, i32, vp, i64, C.POINTER(C.c_int64)]),
+            "pg_find_duplications": (C.c_int, [vp, vp, i64, C.POINTER(C.c_int64)]),
             "pg_kmer_tally_breaks": (C.c_int, [vp, i32, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
                                                C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         }
@@ -229,6 +230,19 @@ class Engine:
         self._check(self.L.pg_find_breaks(self.h, min_min_depth, None, 0, C.byref(n)))
         buf = (_abi.pg_break * max(1, n.value))()
         self._check(self.L.pg_find_breaks(self.h, min_min_depth, C.cast(buf, C.c_void_p), n.value, C.byref(n)))
+        out = {}
+        for k in range(n.value):
+            b = buf[k]
+            out.setdefault(int(b.region), []).append((int(b.start), int(b.stop)))
+        return out
+
+    def find_duplications(self):
+        """pg_find_duplications: the <DUP> regions (duplicationEvents) of every
+        region of the last pileup_regions call, as {region: [(start, stop), ...]}."""
+        n = C.c_int64()
+        self._check(self.L.pg_find_duplications(self.h, None, 0, C.byref(n)))
+        buf = (_abi.pg_break * max(1, n.value))()
+        self._check(self.L.pg_find_duplications(self.h, C.cast(buf, C.c_void_p), n.value, C.byref(n)))
         out = {}
         for k in range(n.value):
             b = buf[k]

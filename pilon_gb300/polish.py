@@ -95,43 +95,6 @@ def region_string(name, s, e):  # Region.regionString (S/Region.scala:45)
     return f"{name}:{s}" + ("" if e + 1 - s < 2 else f"-{e}")
 
 
-def smooth(inp, window):
-    """GenomeRegion.smooth (S/GenomeRegion.scala:190-210), same integer steps."""
-    n = inp.size
-    res = np.zeros(n, np.int64)
-    half = window // 2
-    if n > window:
-        cs = np.concatenate([[0], np.cumsum(inp.astype(np.int64))])
-        i = np.arange(window + 1, n)
-        # after step i the accumulator holds input[0] + input[i-window+1 .. i]
-        acc = inp[0] + (cs[i + 1] - cs[i - window + 1])
-        res[i - half] = (acc + half) // window
-        res[:window - half] = res[window - half]
-        res[n - half:] = res[n - half - 1]
-    else:
-        res[:] = int(inp.astype(np.int64).sum()) // n
-    return res
-
-
-def java_round(x):
-    f = np.floor(x)
-    return np.where(x - f >= 0.5, f + 1, f).astype(np.int64)
-
-
-def summary_regions(test, start, stop, slop):
-    """GenomeRegion.summaryRegions (S/GenomeRegion.scala:743-763) on a boolean array.
-    A run closes at the first untested position more than `slop` past its last
-    tested one, so tested positions up to slop + 1 apart share a run."""
-    idx = np.nonzero(test)[0]
-    regs = []
-    if idx.size:
-        gaps = np.nonzero(np.diff(idx) > slop + 1)[0]
-        firsts = np.concatenate([[idx[0]], idx[gaps + 1]])
-        lasts = np.concatenate([idx[gaps], [idx[-1]]])
-        regs = [(start + int(a), start + int(b)) for a, b in zip(firsts, lasts)]
-    return [r for r in regs if not (r[0] - start < 100 or stop - r[1] < 100)]
-
-
 @dataclass
 class RegionResult:
     contig: int
@@ -147,19 +110,16 @@ class RegionResult:
         return fix_fix_list(self.snp + self.small)
 
 
-def _region_outputs(engine, r, region, ref, opts, params):
-    """Sparse change list -> fix lists and fixed bases; copy number -> <DUP> records."""
+def _region_outputs(engine, r, region, ref, opts, params, dupes=()):
+    """Sparse change list -> fix lists and fixed bases; the region's duplication
+    events (pg_find_duplications) -> where its <DUP> records go."""
     c, s, e, _, _ = region
     size = e - s + 1
     st = engine.stats(r)
-    cnt = np.empty(4 * size, np.int32)
-    dels = np.empty(size, np.int32)
     call = np.empty(size, np.uint32)
     ilen = np.empty(size, np.int32)
     istr = np.empty(size, np.int32)
     o = _abi.pg_region_out()
-    o.count = cnt.ctypes.data
-    o.deletions = dels.ctypes.data
     o.call = call.ctypes.data
     o.indel_len = ilen.ctypes.data
     o.ins_str = istr.ctypes.data
@@ -210,22 +170,12 @@ def _region_outputs(engine, r, region, ref, opts, params):
     res.small.reverse()
     res.bases = fix_issues(res.bases, s, res.snp)
     res.bases = fix_issues(res.bases, s, res.small)
-    if opts.vcf and st.read_count > 0:
-        # fragCoverage = depth after the BAM, before pass 1 added deletion counts
-        frag = cnt.reshape(-1, 4).astype(np.int64).sum(1) + dels
-        for i in np.nonzero(kind == _abi.PG_CHANGE_DEL)[0].tolist():
-            L = int(ilen[i])
-            frag[i + 1:i + L] -= int(dels[i])
-        mean = float(frag.sum()) / size
-        sm = smooth(frag, 200)
-        cn = java_round(sm / mean) if mean > 0 else np.zeros(size, np.int64)
-        regs = summary_regions(cn > 1, s, e, 2000)
-        res.dupes = [r2 for r2 in regs if r2[1] + 1 - r2[0] > 10000]
-        if res.dupes:
-            # records per position: one, plus one after an indel call at i > 0 outside a deletion
-            extra = ((call & (_abi.PG_CALL_INS | _abi.PG_CALL_DEL)) != 0) & ((call & _abi.PG_CALL_DELETED) == 0)
-            extra[0] = False
-            res.first_line = np.concatenate([[0], np.cumsum(1 + extra.astype(np.int64))])
+    res.dupes = list(dupes)
+    if res.dupes:
+        # records per position: one, plus one after an indel call at i > 0 outside a deletion
+        extra = ((call & (_abi.PG_CALL_INS | _abi.PG_CALL_DEL)) != 0) & ((call & _abi.PG_CALL_DELETED) == 0)
+        extra[0] = False
+        res.first_line = np.concatenate([[0], np.cumsum(1 + extra.astype(np.int64))])
     return res
 
 
@@ -304,7 +254,10 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
     engine.set_reference(contigs)
     engine.set_reads(reads)
     engine.pileup_regions(regions, params, batched=batched)
-    results = [_region_outputs(engine, r, reg, contigs[reg[0]], opts, params) for r, reg in enumerate(regions)]
+    # pass 2 of postProcess and duplicationEvents, on the device (the <DUP> records)
+    dups = engine.find_duplications() if opts.vcf else {}
+    results = [_region_outputs(engine, r, reg, contigs[reg[0]], opts, params, dups.get(r, ()))
+               for r, reg in enumerate(regions)]
     # The output groups of GenomeFile.regions (S/GenomeFile.scala:49-54): a contig
     # with its chunks, or with --targets one group per target (two targets on one
     # contig give two FASTA records, and each restarts the changes offset).

@@ -4,7 +4,43 @@ from the engine's per-position arrays, to check the device's pg_find_breaks.  Th
 K-mer tally consumes (S/GenomeRegion.scala:395-410)."""
 import numpy as np
 
-from pilon_gb300.polish import summary_regions
+
+def smooth(inp, window):
+    """GenomeRegion.smooth (S/GenomeRegion.scala:190-210), same integer steps."""
+    n = inp.size
+    res = np.zeros(n, np.int64)
+    half = window // 2
+    if n > window:
+        cs = np.concatenate([[0], np.cumsum(inp.astype(np.int64))])
+        i = np.arange(window + 1, n)
+        # after step i the accumulator holds input[0] + input[i-window+1 .. i]
+        acc = inp[0] + (cs[i + 1] - cs[i - window + 1])
+        res[i - half] = (acc + half) // window
+        res[:window - half] = res[window - half]
+        res[n - half:] = res[n - half - 1]
+    else:
+        res[:] = int(inp.astype(np.int64).sum()) // n
+    return res
+
+
+def java_round(x):
+    f = np.floor(x)
+    return np.where(x - f >= 0.5, f + 1, f).astype(np.int64)
+
+
+def summary_regions(test, start, stop, slop):
+    """GenomeRegion.summaryRegions (S/GenomeRegion.scala:743-763) on a boolean array.
+    A run closes at the first untested position more than `slop` past its last
+    tested one, so tested positions up to slop + 1 apart share a run."""
+    idx = np.nonzero(test)[0]
+    regs = []
+    if idx.size:
+        gaps = np.nonzero(np.diff(idx) > slop + 1)[0]
+        firsts = np.concatenate([[idx[0]], idx[gaps + 1]])
+        lasts = np.concatenate([idx[gaps], [idx[-1]]])
+        regs = [(start + int(a), start + int(b)) for a, b in zip(firsts, lasts)]
+    return [r for r in regs if not (r[0] - start < 100 or stop - r[1] < 100)]
+
 
 
 def _pct_int(n, d):

@@ -305,7 +305,7 @@ def test_summary_regions_merge_rule():
     """GenomeRegion.summaryRegions closes a run at the first untested position
     more than slop past the last tested one (S/GenomeRegion.scala:748-757):
     tested positions slop + 1 apart stay in one run, slop + 2 apart split."""
-    from pilon_gb300.polish import summary_regions
+    from tests.breaks_host import summary_regions
 
     def scala(test, start, stop, slop):  # the loop as written in the reference
         regs, first, last = [], -1, -1

@@ -77,6 +77,29 @@ class OracleEngine:
     def stats(self, r):
         return self.results[r].stats
 
+    def find_duplications(self):
+        """duplicationEvents restated on the host from the oracle's arrays: pass 2
+        of postProcess (smooth, copyNumber) and summaryRegions, as the device's
+        pg_find_duplications computes them."""
+        from tests.breaks_host import java_round, smooth, summary_regions
+        out = {}
+        for r, (c, s, e, rb, re) in enumerate(self.regions):
+            res = self.results[r]
+            if res.stats.read_count <= 0:
+                continue
+            size = e - s + 1
+            # fragCoverage = depth after the BAM, before pass 1 added deletion counts
+            frag = res.count.reshape(-1, 4).astype(np.int64).sum(1) + res.deletions
+            for i in np.nonzero(((res.call >> 9) & 7) == _abi.PG_CHANGE_DEL)[0].tolist():
+                frag[i + 1:i + int(res.indel_len[i])] -= int(res.deletions[i])
+            mean = float(frag.sum()) / size
+            sm = smooth(frag, 200)
+            cn = java_round(sm / mean) if mean > 0 else np.zeros(size, np.int64)
+            d = [x for x in summary_regions(cn > 1, s, e, 2000) if x[1] + 1 - x[0] > 10000]
+            if d:
+                out[r] = d
+        return out
+
     def _check(self, st):
         assert st == _abi.PG_OK, st
 
