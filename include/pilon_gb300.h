@@ -178,6 +178,19 @@ typedef struct pg_kmer_edge {
   int32_t weight;            /* baseCount of the called base */
 } pg_kmer_edge;
 
+/* One graph edge for any K <= 63 (pg_kmer_tally_wide): the K-mer as 4-bit BAM
+ * codes, base j at bits 60-4*(j%16) of key[j/16]; other fields as in
+ * pg_kmer_edge. */
+typedef struct pg_kmer_edge_wide {
+  uint64_t key[4];
+  int32_t window;
+  int8_t next;
+  int8_t alt;
+  int16_t pad_;
+  int32_t depth;
+  int32_t weight;
+} pg_kmer_edge_wide;
+
 /* One break candidate of GenomeRegion.possibleBreaks (S/GenomeRegion.scala:
  * 659-720): contig loci start..stop (1-based, inclusive) in region `region`
  * of the last pg_pileup_regions call. */
@@ -253,6 +266,13 @@ pg_status pg_set_tuning(pg_ctx *ctx, int32_t tile_width, int32_t warps_per_cta, 
 pg_status pg_kmer_tally(pg_ctx *ctx, const pg_window *windows, int32_t n_windows,
                         int32_t K, const pg_params *params, int32_t min_depth,
                         pg_kmer_edge *edges, int64_t cap, int64_t *n_edges);
+/* The same tally for 1 <= K <= 63, Pilon's default K = 47 included
+ * (S/Assembler.scala:25), with 4-word K-mer keys in the edges.  K-mers of
+ * A/C/G/T only are counted in tables of 2-bit keys (128 bits, inserted with a
+ * 16-byte compare-and-swap); the others in tables of 4-bit keys. */
+pg_status pg_kmer_tally_wide(pg_ctx *ctx, const pg_window *windows, int32_t n_windows,
+                             int32_t K, const pg_params *params, int32_t min_depth,
+                             pg_kmer_edge_wide *edges, int64_t cap, int64_t *n_edges);
 
 /* ---- VCF ----------------------------------------------------------------
  * The per-position records of GenomeRegion.writeVcf / Vcf.writeRecord
@@ -297,6 +317,10 @@ pg_status pg_find_duplications(pg_ctx *ctx, pg_break *out, int64_t cap, int64_t 
 pg_status pg_kmer_tally_breaks(pg_ctx *ctx, int32_t min_min_depth, int32_t radius, int32_t K,
                                const pg_params *params, int32_t min_depth, pg_kmer_edge *edges, int64_t cap,
                                int64_t *n_windows, int64_t *n_edges);
+/* pg_kmer_tally_breaks for 1 <= K <= 63 (see pg_kmer_tally_wide). */
+pg_status pg_kmer_tally_breaks_wide(pg_ctx *ctx, int32_t min_min_depth, int32_t radius, int32_t K,
+                                    const pg_params *params, int32_t min_depth, pg_kmer_edge_wide *edges,
+                                    int64_t cap, int64_t *n_windows, int64_t *n_edges);
 
 /* ---- timing -------------------------------------------------------------
  * Milliseconds of the dominant (pileup walk) kernel in the last

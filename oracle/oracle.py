@@ -46,6 +46,8 @@ def lib():
         L.or_kmer_tally.restype = C.c_int64
         L.or_kmer_tally.argtypes = [C.POINTER(_abi.pg_reads), C.POINTER(_abi.pg_params), C.c_void_p, C.c_int32,
                                     C.c_int32, C.c_int32, C.c_void_p, C.c_int64]
+        L.or_kmer_tally_wide.restype = C.c_int64
+        L.or_kmer_tally_wide.argtypes = L.or_kmer_tally.argtypes
         L.or_target.restype = C.c_int
         L.or_target.argtypes = [C.POINTER(_abi.pg_reads), C.POINTER(_abi.pg_params), C.c_char_p, C.c_void_p,
                                 C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.c_int32,
@@ -177,6 +179,22 @@ def kmer_tally(reads, params, windows, K, min_depth=5):
         edges = np.zeros(cap, _abi.kmer_edge_dtype())
         n = L.or_kmer_tally(C.byref(ab), C.byref(params), C.cast(wins, C.c_void_p), len(windows), K, min_depth,
                             edges.ctypes.data, cap)
+        if n <= cap:
+            return edges[:n]
+        cap = int(n)
+
+
+def kmer_tally_wide(reads, params, windows, K, min_depth=5):
+    """Edges of Assembler.buildGraph per window for any K <= 64
+    (pg_kmer_edge_wide records, four words of 4-bit keys)."""
+    L = lib()
+    wins = (_abi.pg_window * max(1, len(windows)))(*[_abi.pg_window(a, b) for a, b in windows])
+    ab = reads.to_abi()
+    cap = 1
+    while True:
+        edges = np.zeros(cap, _abi.kmer_edge_wide_dtype())
+        n = L.or_kmer_tally_wide(C.byref(ab), C.byref(params), C.cast(wins, C.c_void_p), len(windows), K, min_depth,
+                                 edges.ctypes.data, cap)
         if n <= cap:
             return edges[:n]
         cap = int(n)

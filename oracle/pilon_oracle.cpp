@@ -1205,14 +1205,14 @@ int32_t or_region_breaks(const pg_reads* R, const pg_params* params, const uint8
   }
 }
 
+}  // extern "C"
+
 // Assembler.addReads + buildGraph (S/Assembler.scala:46-87, 132-162) for each
-// window.  Edges are written sorted by (window, K-mer string); K-mers are
-// returned as 4-bit BAM codes, base j at nibble (15 - j%16) of word j/16.
-int64_t or_kmer_tally(const pg_reads* R, const pg_params* params, const pg_window* wins, int32_t n_wins, int32_t K,
-                      int32_t min_depth, pg_kmer_edge* edges, int64_t cap) {
-  Params P = toParams(params);
-  int64_t ne = 0;
-  auto nibOf = [](char c) -> uint64_t { return (uint64_t)(strchr(kNib, c) - kNib); };
+// window; emit(window, K-mer string, its pileup, its call) for every K-mer of
+// depth >= min_depth, in (window, K-mer string) order.
+template <class Emit>
+static void tally_windows(const pg_reads* R, const Params& P, const pg_window* wins, int32_t n_wins, int32_t K,
+                          int32_t min_depth, Emit emit) {
   for (int32_t w = 0; w < n_wins; w++) {
     std::unordered_map<std::string, PileUp> pileups;
     int64_t nReads = 0;
@@ -1249,26 +1249,63 @@ int64_t or_kmer_tally(const pg_reads* R, const pg_params* params, const pg_windo
     std::sort(ks.begin(), ks.end());
     for (auto& k : ks) {
       const PileUp& pu = pileups[k];
-      BaseCall bc = baseCall(pu, P);
-      if (ne < cap) {
-        uint64_t hi = 0, lo = 0;
-        for (int32_t j = 0; j < K; j++) {
-          uint64_t nb = nibOf(k[j]);
-          if (j < 16) hi |= nb << (60 - 4 * j); else lo |= nb << (60 - 4 * (j - 16));
-        }
-        pg_kmer_edge& e = edges[ne];
-        e.key_hi = hi;
-        e.key_lo = lo;
-        e.window = w;
-        e.next = (int8_t)bc.baseIdx;
-        e.alt = bc.homo ? (int8_t)-1 : (int8_t)bc.altIdx;
-        e.pad_ = 0;
-        e.depth = (int32_t)pu.depth();
-        e.weight = (int32_t)pu.baseCount[bc.baseIdx];
-      }
-      ne++;
+      emit(w, k, pu, baseCall(pu, P));
     }
   }
+}
+
+static uint64_t nib_of(char c) { return (uint64_t)(strchr(kNib, c) - kNib); }
+
+extern "C" {
+
+// The tally of tally_windows for K <= 32: K-mers as 4-bit BAM codes, base j at
+// nibble (15 - j%16) of word j/16.
+int64_t or_kmer_tally(const pg_reads* R, const pg_params* params, const pg_window* wins, int32_t n_wins, int32_t K,
+                      int32_t min_depth, pg_kmer_edge* edges, int64_t cap) {
+  Params P = toParams(params);
+  int64_t ne = 0;
+  tally_windows(R, P, wins, n_wins, K, min_depth, [&](int32_t w, const std::string& k, const PileUp& pu,
+                                                      const BaseCall& bc) {
+    if (ne < cap) {
+      uint64_t hi = 0, lo = 0;
+      for (int32_t j = 0; j < K; j++) {
+        if (j < 16) hi |= nib_of(k[j]) << (60 - 4 * j); else lo |= nib_of(k[j]) << (60 - 4 * (j - 16));
+      }
+      pg_kmer_edge& e = edges[ne];
+      e.key_hi = hi;
+      e.key_lo = lo;
+      e.window = w;
+      e.next = (int8_t)bc.baseIdx;
+      e.alt = bc.homo ? (int8_t)-1 : (int8_t)bc.altIdx;
+      e.pad_ = 0;
+      e.depth = (int32_t)pu.depth();
+      e.weight = (int32_t)pu.baseCount[bc.baseIdx];
+    }
+    ne++;
+  });
+  return ne;
+}
+
+// The same tally for any K <= 64 (the reference's K is unbounded; its default
+// is 47, S/Assembler.scala:25): base j at bits 60 - 4 (j % 16) of key[j / 16].
+int64_t or_kmer_tally_wide(const pg_reads* R, const pg_params* params, const pg_window* wins, int32_t n_wins,
+                           int32_t K, int32_t min_depth, pg_kmer_edge_wide* edges, int64_t cap) {
+  Params P = toParams(params);
+  int64_t ne = 0;
+  tally_windows(R, P, wins, n_wins, K, min_depth, [&](int32_t w, const std::string& k, const PileUp& pu,
+                                                      const BaseCall& bc) {
+    if (ne < cap) {
+      pg_kmer_edge_wide& e = edges[ne];
+      memset(&e, 0, sizeof e);
+      for (int32_t j = 0; j < K && j < 64; j++) e.key[j / 16] |= nib_of(k[j]) << (60 - 4 * (j % 16));
+      e.window = w;
+      e.next = (int8_t)bc.baseIdx;
+      e.alt = bc.homo ? (int8_t)-1 : (int8_t)bc.altIdx;
+      e.depth = (int32_t)pu.depth();
+      e.weight = (int32_t)pu.baseCount[bc.baseIdx];
+    }
+    ne++;
+  });
   return ne;
 }
 

@@ -817,14 +817,33 @@ static int64_t next_pow2(int64_t x) {
 }
 
 static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_params* params, int32_t min_depth,
-                           pg_kmer_edge* edges, int64_t cap, int64_t* n_edges);
+                           bool wide, void* edges, int64_t cap, int64_t* n_edges);
+static pg_status kmer_windows(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K,
+                              const pg_params* params, int32_t min_depth, bool wide, void* edges, int64_t cap,
+                              int64_t* n_edges);
 
 pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K, const pg_params* params,
                         int32_t min_depth, pg_kmer_edge* edges, int64_t cap, int64_t* n_edges) {
   const Range nvtx_range("pg_kmer_tally");
+  if (c && (K < 1 || K > 31))
+    return fail(c, PG_ERR_LIMIT, "K = %d: pg_kmer_tally packs K-mers in 64 bits (K <= 31); pg_kmer_tally_wide "
+                "takes K <= 63", K);
+  return kmer_windows(c, windows, n_windows, K, params, min_depth, false, edges, cap, n_edges);
+}
+
+pg_status pg_kmer_tally_wide(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K,
+                             const pg_params* params, int32_t min_depth, pg_kmer_edge_wide* edges, int64_t cap,
+                             int64_t* n_edges) {
+  const Range nvtx_range("pg_kmer_tally_wide");
+  if (c && (K < 1 || K > 63)) return fail(c, PG_ERR_LIMIT, "K = %d: pg_kmer_tally_wide takes K <= 63", K);
+  return kmer_windows(c, windows, n_windows, K, params, min_depth, true, edges, cap, n_edges);
+}
+
+static pg_status kmer_windows(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K,
+                              const pg_params* params, int32_t min_depth, bool wide, void* edges, int64_t cap,
+                              int64_t* n_edges) {
   if (!c || (n_windows > 0 && !windows) || !params || n_windows < 0 || cap < 0 || !n_edges)
     return fail(c, PG_ERR_ARG, "bad arguments");
-  if (K < 1 || K > 31) return fail(c, PG_ERR_LIMIT, "K = %d: the GPU tally packs K-mers in 64 bits (K <= 31)", K);
   if (min_depth < 1) return fail(c, PG_ERR_ARG, "min_depth must be >= 1");
   if (params->min_qual < 0) return fail(c, PG_ERR_ARG, "min_qual must be >= 0");
   if (pg_status s0 = check_default_qual(c, params)) return s0;
@@ -838,7 +857,7 @@ pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, 
   pg_status s;
   if ((s = ensure(c, c->kwin, sizeof(pg_window) * n_windows))) return s;
   CK(cudaMemcpyAsync(c->kwin.p, windows, sizeof(pg_window) * n_windows, cudaMemcpyHostToDevice, c->stream));
-  return kmer_core(c, n_windows, K, params, min_depth, edges, cap, n_edges);
+  return kmer_core(c, n_windows, K, params, min_depth, wide, edges, cap, n_edges);
 }
 
 // The tally over the n_windows windows in c->kwin (device).
@@ -857,8 +876,12 @@ constexpr int64_t kTallyBatchBytes = (int64_t)1 << 30;
 constexpr int64_t kTallyReadsPerChunk = 64;
 
 static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_params* params, int32_t min_depth,
-                           pg_kmer_edge* edges, int64_t cap, int64_t* n_edges) {
+                           bool wide, void* edges, int64_t cap, int64_t* n_edges) {
   cudaStream_t st = c->stream;
+  // bytes per slot: key (8 or 16), count 4 x 4, qualSum 4 x 8, mqSum, qSum; exotic slots hold
+  // 2 or 4 key words and a used byte (rounded up)
+  const int64_t slot_b = wide ? 72 : 64, xslot_b = wide ? 96 : 80, kw = wide ? 2 : 1, xkw = wide ? 4 : 2;
+  const size_t edge_b = wide ? sizeof(pg_kmer_edge_wide) : sizeof(pg_kmer_edge);
   pg_status s;
   c->tally_ms = 0;
   c->tally_events = c->tally_distinct = c->tally_max_batch_bytes = 0;
@@ -883,7 +906,7 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
     c->tally_events += pre[3 * w + 1];
   }
   const int64_t edge_cap = std::max<int64_t>(cap, 1);
-  if ((s = ensure(c, c->kedges, sizeof(pg_kmer_edge) * edge_cap))) return s;
+  if ((s = ensure(c, c->kedges, edge_b * edge_cap))) return s;
   if ((s = ensure(c, c->kcount, 16))) return s;
   if ((s = ensure(c, c->kwflag, 4 * (size_t)n_windows))) return s;
   if ((s = ensure(c, c->kused, 8 * (size_t)n_windows))) return s;
@@ -896,7 +919,7 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
   if ((s = ensure(c, c->kx_evfill, 8 * (size_t)n_windows))) return s;
   CK(cudaMemsetAsync(c->kcount.p, 0, 16, st));
   CK(cudaMemsetAsync(c->kused.p, 0, 8 * (size_t)n_windows, st));
-  auto table_bytes = [&](int32_t w) { return scap[w] * 64 + xcap[w] * 80 + evcap[w] * 16; };
+  auto table_bytes = [&](int32_t w) { return scap[w] * slot_b + xcap[w] * xslot_b + evcap[w] * 16; };
   std::vector<KmerChunk> chunks;
   std::vector<int32_t> flags;
   int32_t w0 = 0;
@@ -918,15 +941,15 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
         sbase[w] = ns; xbase[w] = nx; evbase[w] = ne;
         ns += scap[w]; nx += xcap[w]; ne += evcap[w];
       }
-      c->tally_max_batch_bytes = std::max(c->tally_max_batch_bytes, ns * 64 + nx * 80 + ne * 16);
+      c->tally_max_batch_bytes = std::max(c->tally_max_batch_bytes, ns * slot_b + nx * xslot_b + ne * 16);
       const size_t nxs = (size_t)std::max<int64_t>(nx, 1);
-      if ((s = ensure(c, c->kkeys, 8 * (size_t)ns))) return s;
+      if ((s = ensure(c, c->kkeys, 8 * kw * (size_t)ns))) return s;
       if ((s = ensure(c, c->kcnt, 16 * (size_t)ns))) return s;
       if ((s = ensure(c, c->kqs, 32 * (size_t)ns))) return s;
       if ((s = ensure(c, c->kmq, 4 * (size_t)ns))) return s;
       if ((s = ensure(c, c->kq, 4 * (size_t)ns))) return s;
       if ((s = ensure(c, c->kx_ev, 16 * (size_t)std::max<int64_t>(ne, 1)))) return s;
-      if ((s = ensure(c, c->kx_keys, 16 * nxs))) return s;
+      if ((s = ensure(c, c->kx_keys, 8 * xkw * nxs))) return s;
       if ((s = ensure(c, c->kx_used, nxs))) return s;
       if ((s = ensure(c, c->kx_cnt, 16 * nxs))) return s;
       if ((s = ensure(c, c->kx_qs, 32 * nxs))) return s;
@@ -942,7 +965,7 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
       CK(cudaMemsetAsync(P<unsigned long long>(c->kx_evfill) + w0, 0, 8 * nw, st));
       CK(cudaMemsetAsync(P<int32_t>(c->kwflag) + w0, 0, 4 * nw, st));
       CK(cudaMemsetAsync(P<unsigned long long>(c->kused) + w0, 0, 8 * nw, st));
-      CK(cudaMemsetAsync(c->kkeys.p, 0xFF, 8 * (size_t)ns, st));
+      CK(cudaMemsetAsync(c->kkeys.p, 0xFF, 8 * kw * (size_t)ns, st));
       CK(cudaMemsetAsync(c->kcnt.p, 0, 16 * (size_t)ns, st));
       CK(cudaMemsetAsync(c->kqs.p, 0, 32 * (size_t)ns, st));
       CK(cudaMemsetAsync(c->kmq.p, 0, 4 * (size_t)ns, st));
@@ -953,7 +976,7 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
       CK(cudaMemsetAsync(c->kx_mq.p, 0, 4 * nxs, st));
       CK(cudaMemsetAsync(c->kx_q.p, 0, 4 * nxs, st));
       KmerArgs a;
-      a.R = c->R; a.windows = P<pg_window>(c->kwin); a.win_begin = w0; a.K = K;
+      a.R = c->R; a.windows = P<pg_window>(c->kwin); a.win_begin = w0; a.K = K; a.wide = wide;
       a.min_qual = params->min_qual; a.default_qual = params->default_qual; a.min_depth = min_depth;
       a.chunks = P<KmerChunk>(c->kchunks); a.n_chunks = (int32_t)chunks.size();
       a.slot_base = P<int64_t>(c->kslot_base); a.slot_cap = P<int64_t>(c->kslot_cap);
@@ -966,7 +989,7 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
       a.x_q = P<uint32_t>(c->kx_q);
       a.x_ev_base = P<int64_t>(c->kx_evbase); a.x_ev_cap = P<int64_t>(c->kx_evcap);
       a.x_ev_fill = P<unsigned long long>(c->kx_evfill); a.x_events = P<longlong2>(c->kx_ev);
-      a.edges = P<pg_kmer_edge>(c->kedges); a.edge_cap = edge_cap;
+      a.edges = P<pg_kmer_edge>(c->kedges); a.wedges = P<pg_kmer_edge_wide>(c->kedges); a.edge_cap = edge_cap;
       a.n_edges = P<unsigned long long>(c->kcount); a.overflow = (int32_t*)(P<unsigned long long>(c->kcount) + 1);
       CK(cudaEventRecord(c->e0, st));
       launch_kmer_count(a, w1 - w0, st);
@@ -1009,7 +1032,7 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
   *n_edges = (int64_t)hc[0];
   const int64_t ncopy = std::min<int64_t>((int64_t)hc[0], cap);
   if (ncopy > 0 && edges) {
-    CK(cudaMemcpyAsync(edges, c->kedges.p, sizeof(pg_kmer_edge) * ncopy, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(edges, c->kedges.p, edge_b * ncopy, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
   }
   return PG_OK;
@@ -1106,12 +1129,32 @@ pg_status pg_find_duplications(pg_ctx* c, pg_break* out, int64_t cap, int64_t* n
   return PG_OK;
 }
 
+static pg_status kmer_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius, int32_t K, const pg_params* params,
+                             int32_t min_depth, bool wide, void* edges, int64_t cap, int64_t* n_windows,
+                             int64_t* n_edges);
+
 pg_status pg_kmer_tally_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius, int32_t K, const pg_params* params,
                                int32_t min_depth, pg_kmer_edge* edges, int64_t cap, int64_t* n_windows,
                                int64_t* n_edges) {
   const Range nvtx_range("pg_kmer_tally_breaks");
+  if (c && (K < 1 || K > 31))
+    return fail(c, PG_ERR_LIMIT, "K = %d: pg_kmer_tally_breaks packs K-mers in 64 bits (K <= 31); "
+                "pg_kmer_tally_breaks_wide takes K <= 63", K);
+  return kmer_breaks(c, min_min_depth, radius, K, params, min_depth, false, edges, cap, n_windows, n_edges);
+}
+
+pg_status pg_kmer_tally_breaks_wide(pg_ctx* c, int32_t min_min_depth, int32_t radius, int32_t K,
+                                    const pg_params* params, int32_t min_depth, pg_kmer_edge_wide* edges,
+                                    int64_t cap, int64_t* n_windows, int64_t* n_edges) {
+  const Range nvtx_range("pg_kmer_tally_breaks_wide");
+  if (c && (K < 1 || K > 63)) return fail(c, PG_ERR_LIMIT, "K = %d: pg_kmer_tally_breaks_wide takes K <= 63", K);
+  return kmer_breaks(c, min_min_depth, radius, K, params, min_depth, true, edges, cap, n_windows, n_edges);
+}
+
+static pg_status kmer_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius, int32_t K, const pg_params* params,
+                             int32_t min_depth, bool wide, void* edges, int64_t cap, int64_t* n_windows,
+                             int64_t* n_edges) {
   if (!c || !params || cap < 0 || !n_edges || !n_windows || radius < 0) return fail(c, PG_ERR_ARG, "bad arguments");
-  if (K < 1 || K > 31) return fail(c, PG_ERR_LIMIT, "K = %d: the GPU tally packs K-mers in 64 bits (K <= 31)", K);
   if (min_depth < 1) return fail(c, PG_ERR_ARG, "min_depth must be >= 1");
   if (params->min_qual < 0) return fail(c, PG_ERR_ARG, "min_qual must be >= 0");
   if (pg_status s0 = check_default_qual(c, params)) return s0;
@@ -1129,7 +1172,7 @@ pg_status pg_kmer_tally_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius,
   launch_break_windows(c->R, P<RegionDev>(c->regions), P<pg_break>(c->bout), n, radius, P<ReadExtent>(c->d_ext),
                        P<pg_window>(c->kwin), c->stream);
   CK(cudaGetLastError());
-  return kmer_core(c, n, K, params, min_depth, edges, cap, n_edges);
+  return kmer_core(c, n, K, params, min_depth, wide, edges, cap, n_edges);
 }
 
 pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid, int32_t vcf_qe,

@@ -74,11 +74,24 @@ __global__ void k_kmer_prepass(Reads R, const pg_window* wins, int32_t K, long l
 
 constexpr int64_t kMaxProbe = 256;
 
+// A 2-bit packed K-mer of up to 63 bases (the wide tables): bases in the low
+// 2K bits of hi:lo, so hi < 2^62 and the all-ones key marks an empty slot.
+struct __align__(16) Key128 {
+  unsigned long long lo, hi;
+};
+__device__ inline bool same_key(const Key128& a, const Key128& b) { return a.lo == b.lo && a.hi == b.hi; }
+
+// WIDE = 0: 64-bit keys (K <= 31); WIDE = 1: 128-bit keys (K <= 63), inserted
+// with the 16-byte compare-and-swap of sm_90 and later (the compare-and-swap is
+// also the probe's read, so a probe never sees half of a key).
+template <bool WIDE>
 __global__ void __launch_bounds__(64) k_kmer_count(KmerArgs a) {
   const KmerChunk ch = a.chunks[blockIdx.x];
   const int32_t w = ch.w;
   const int32_t K = a.K;
-  const unsigned long long mask = (K == 32) ? ~0ull : ((1ull << (2 * K)) - 1);
+  const unsigned long long mask = (K >= 32) ? ~0ull : ((1ull << (2 * K)) - 1);
+  const unsigned long long mask_hi = (K > 32) ? ((1ull << (2 * K - 64)) - 1) : 0ull;
+  Key128* const keys2 = reinterpret_cast<Key128*>(a.keys);
   const int64_t base = a.slot_base[w], cap = a.slot_cap[w];
   const int64_t xev0 = a.x_ev_base[w], xev_cap = a.x_ev_cap[w];
   const Reads& R = a.R;
@@ -90,12 +103,13 @@ __global__ void __launch_bounds__(64) k_kmer_count(KmerArgs a) {
     const uint8_t* qual = R.qual + R.qual_off[i];
     const bool hasQual = qual[0] != 0xFF;
     for (int strand = 0; strand < 2; strand++) {
-      unsigned long long key = 0;
+      unsigned long long key = 0, key_hi = 0;
       int32_t lastBad = -1;
       uint32_t nib = strand_nib(seq, L, strand, 0);
       for (int32_t j = 0; j < L - 1; j++) {
         int c = code2(nib);
         if (c < 0) { lastBad = j; c = 0; }
+        if (WIDE) key_hi = ((key_hi << 2) | (key >> 62)) & mask_hi;
         key = ((key << 2) | (unsigned long long)c) & mask;
         const uint32_t next = strand_nib(seq, L, strand, j + 1);
         const int32_t o = j - K + 1;
@@ -109,17 +123,24 @@ __global__ void __launch_bounds__(64) k_kmer_count(KmerArgs a) {
               if ((int64_t)k < xev_cap) a.x_events[xev0 + k] = make_longlong2((long long)i, ((long long)strand << 32) | (long long)o);
               else atomicExch(a.overflow, 1);
             } else {
-              int64_t h = (int64_t)(mix64(key) & (unsigned long long)(cap - 1));
+              int64_t h = (int64_t)((WIDE ? mix64(key ^ mix64(key_hi)) : mix64(key)) & (unsigned long long)(cap - 1));
               int64_t slot = -1;
               const int64_t probes = cap < kMaxProbe ? cap : kMaxProbe;
               for (int64_t probe = 0; probe < probes; probe++) {
                 const int64_t s = base + h;
-                unsigned long long k = a.keys[s];
-                if (k == key) { slot = s; break; }
-                if (k == kEmpty) {
-                  unsigned long long prev = atomicCAS(&a.keys[s], kEmpty, key);
-                  if (prev == kEmpty) atomicAdd(&a.used[w], 1ull);
-                  if (prev == kEmpty || prev == key) { slot = s; break; }
+                if (WIDE) {
+                  const Key128 kk{key, key_hi}, empty{kEmpty, kEmpty};
+                  const Key128 prev = atomicCAS(&keys2[s], empty, kk);
+                  if (same_key(prev, empty)) atomicAdd(&a.used[w], 1ull);
+                  if (same_key(prev, empty) || same_key(prev, kk)) { slot = s; break; }
+                } else {
+                  unsigned long long k = a.keys[s];
+                  if (k == key) { slot = s; break; }
+                  if (k == kEmpty) {
+                    unsigned long long prev = atomicCAS(&a.keys[s], kEmpty, key);
+                    if (prev == kEmpty) atomicAdd(&a.used[w], 1ull);
+                    if (prev == kEmpty || prev == key) { slot = s; break; }
+                  }
                 }
                 h = (h + 1) & (cap - 1);
               }
@@ -157,18 +178,28 @@ __device__ inline void kmer_call(const uint32_t cnt[4], const unsigned long long
   alt = homoScore >= hetero ? -1 : o1;
 }
 
-__device__ inline void store_edge(const KmerArgs& a, unsigned long long k, unsigned long long hi, unsigned long long lo,
+// Edge k: key4 = the K-mer as 4-bit codes in four words (the narrow edge keeps
+// the first two, K <= 32).
+__device__ inline void store_edge(const KmerArgs& a, unsigned long long k, const unsigned long long key4[4],
                                   int32_t w, int base, int alt, int32_t depth, int32_t weight) {
-  if ((int64_t)k < a.edge_cap) {
+  if ((int64_t)k >= a.edge_cap) return;
+  if (a.wide) {
+    pg_kmer_edge_wide e;
+    for (int q = 0; q < 4; q++) e.key[q] = key4[q];
+    e.window = w; e.next = (int8_t)base; e.alt = (int8_t)alt; e.pad_ = 0; e.depth = depth; e.weight = weight;
+    a.wedges[k] = e;
+  } else {
     pg_kmer_edge e;
-    e.key_hi = hi; e.key_lo = lo; e.window = w; e.next = (int8_t)base; e.alt = (int8_t)alt; e.pad_ = 0;
+    e.key_hi = key4[0]; e.key_lo = key4[1]; e.window = w; e.next = (int8_t)base; e.alt = (int8_t)alt; e.pad_ = 0;
     e.depth = depth; e.weight = weight;
     a.edges[k] = e;
   }
 }
 
+template <bool WIDE>
 __global__ void k_kmer_edges(KmerArgs a) {
   const int32_t w = a.win_begin + blockIdx.x;
+  const Key128* const keys2 = reinterpret_cast<const Key128*>(a.keys);
   const int64_t base = a.slot_base[w], cap = a.slot_cap[w];
   const int32_t K = a.K;
   const int lane = threadIdx.x & 31;
@@ -177,12 +208,18 @@ __global__ void k_kmer_edges(KmerArgs a) {
     const int64_t s = s0 + threadIdx.x;
     bool emit = false;
     uint32_t cnt[4] = {0, 0, 0, 0};
-    unsigned long long key = kEmpty;
+    unsigned long long key = kEmpty, key_hi = kEmpty;
     int32_t depth = 0;
     int b0 = 0, alt = -1;
     if (s < base + cap) {
-      key = a.keys[s];
-      if (key != kEmpty) {
+      if (WIDE) {
+        const Key128 k2 = keys2[s];
+        key = k2.lo;
+        key_hi = k2.hi;
+      } else {
+        key = a.keys[s];
+      }
+      if (key != kEmpty || key_hi != kEmpty) {
         unsigned long long qs[4];
         for (int b = 0; b < 4; b++) { cnt[b] = a.cnt[4 * s + b]; qs[b] = a.qs[4 * s + b]; }
         depth = (int32_t)(cnt[0] + cnt[1] + cnt[2] + cnt[3]);
@@ -198,12 +235,14 @@ __global__ void k_kmer_edges(KmerArgs a) {
     if (lane == __ffs(m) - 1) first = atomicAdd(a.n_edges, (unsigned long long)__popc(m));
     first = __shfl_sync(0xffffffffu, first, __ffs(m) - 1);
     if (emit) {
-      unsigned long long hi = 0, lo = 0;
+      // 2-bit digit of base j at bit 2 (K - 1 - j) of hi:lo -> its 4-bit code 1 << digit
+      unsigned long long key4[4] = {0, 0, 0, 0};
       for (int32_t j = 0; j < K; j++) {
-        const unsigned long long nibv = 1ull << ((key >> (2 * (K - 1 - j))) & 3ull);
-        if (j < 16) hi |= nibv << (60 - 4 * j); else lo |= nibv << (60 - 4 * (j - 16));
+        const int32_t bit = 2 * (K - 1 - j);
+        const unsigned long long d = bit < 64 ? (key >> bit) & 3ull : (key_hi >> (bit - 64)) & 3ull;
+        key4[j >> 4] |= (1ull << d) << (60 - 4 * (j & 15));
       }
-      store_edge(a, first + __popc(m & ((1u << lane) - 1u)), hi, lo, w, b0, alt, depth,
+      store_edge(a, first + __popc(m & ((1u << lane) - 1u)), key4, w, b0, alt, depth,
                  (int32_t)(b0 == 0 ? cnt[0] : b0 == 1 ? cnt[1] : b0 == 2 ? cnt[2] : cnt[3]));
     }
   }
@@ -211,7 +250,9 @@ __global__ void k_kmer_edges(KmerArgs a) {
 
 // Exotic K-mers: one thread per window over the window's listed events, in a
 // private table keyed by 4-bit codes.
+template <bool WIDE>
 __global__ void k_kmer_exotic(KmerArgs a, int32_t n_win) {
+  constexpr int NW = WIDE ? 4 : 2;  // key words per slot
   const int32_t wl = blockIdx.x * blockDim.x + threadIdx.x;
   if (wl >= n_win) return;
   const int32_t w = a.win_begin + wl;
@@ -232,20 +273,28 @@ __global__ void k_kmer_exotic(KmerArgs a, int32_t n_win) {
     const bool hasQual = qual[0] != 0xFF;
     const int bi = code2(strand_nib(seq, L, strand, o + K));
     const int32_t q = strand_qual(qual, L, strand, o + K, hasQual, a.default_qual);
-    unsigned long long hi = 0, lo = 0;
+    unsigned long long kw[NW];
+#pragma unroll
+    for (int q = 0; q < NW; q++) kw[q] = 0;
     for (int32_t t = 0; t < K; t++) {
       const unsigned long long nb = strand_nib(seq, L, strand, o + t);
-      if (t < 16) hi |= nb << (60 - 4 * t); else lo |= nb << (60 - 4 * (t - 16));
+      kw[t >> 4] |= nb << (60 - 4 * (t & 15));
     }
-    int64_t h = (int64_t)(mix64(hi ^ mix64(lo)) & (unsigned long long)(cap - 1));
+    unsigned long long hv = 0;
+#pragma unroll
+    for (int q = 0; q < NW; q++) hv = mix64(hv ^ kw[q]);
+    int64_t h = (int64_t)(hv & (unsigned long long)(cap - 1));
     int64_t slot = -1;
     for (int64_t probe = 0; probe < cap; probe++) {
       const int64_t s = base + h;
-      if (a.x_keys[2 * s] == hi && a.x_keys[2 * s + 1] == lo && a.x_used[s]) { slot = s; break; }
+      bool same = a.x_used[s] != 0;
+#pragma unroll
+      for (int q = 0; q < NW; q++) same = same && a.x_keys[NW * s + q] == kw[q];
+      if (same) { slot = s; break; }
       if (!a.x_used[s]) {
         a.x_used[s] = 1;
-        a.x_keys[2 * s] = hi;
-        a.x_keys[2 * s + 1] = lo;
+#pragma unroll
+        for (int q = 0; q < NW; q++) a.x_keys[NW * s + q] = kw[q];
         slot = s;
         break;
       }
@@ -266,7 +315,10 @@ __global__ void k_kmer_exotic(KmerArgs a, int32_t n_win) {
     if (depth < a.min_depth) continue;
     int b0, alt;
     kmer_call(cnt, qs, a.x_q[s], b0, alt);
-    store_edge(a, atomicAdd(a.n_edges, 1ull), a.x_keys[2 * s], a.x_keys[2 * s + 1], w, b0, alt, depth,
+    unsigned long long key4[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < NW; q++) key4[q] = a.x_keys[NW * s + q];
+    store_edge(a, atomicAdd(a.n_edges, 1ull), key4, w, b0, alt, depth,
                (int32_t)(b0 == 0 ? cnt[0] : b0 == 1 ? cnt[1] : b0 == 2 ? cnt[2] : cnt[3]));
   }
 }
@@ -279,13 +331,19 @@ void launch_kmer_prepass(const Reads& R, const pg_window* wins, int32_t n, int32
 
 void launch_kmer_count(const KmerArgs& a, int32_t n_win, cudaStream_t s) {
   if (n_win <= 0) return;
-  if (a.n_chunks > 0) k_kmer_count<<<a.n_chunks, 64, 0, s>>>(a);
-  k_kmer_exotic<<<(n_win + 63) / 64, 64, 0, s>>>(a, n_win);
+  if (a.wide) {
+    if (a.n_chunks > 0) k_kmer_count<true><<<a.n_chunks, 64, 0, s>>>(a);
+    k_kmer_exotic<true><<<(n_win + 63) / 64, 64, 0, s>>>(a, n_win);
+  } else {
+    if (a.n_chunks > 0) k_kmer_count<false><<<a.n_chunks, 64, 0, s>>>(a);
+    k_kmer_exotic<false><<<(n_win + 63) / 64, 64, 0, s>>>(a, n_win);
+  }
 }
 
 void launch_kmer_edges(const KmerArgs& a, int32_t n_win, cudaStream_t s) {
   if (n_win <= 0) return;
-  k_kmer_edges<<<n_win, 256, 0, s>>>(a);
+  if (a.wide) k_kmer_edges<true><<<n_win, 256, 0, s>>>(a);
+  else k_kmer_edges<false><<<n_win, 256, 0, s>>>(a);
 }
 
 }  // namespace pg

@@ -16,6 +16,7 @@ struct KmerArgs {
   int32_t win_begin;          // first window of this batch
   int32_t K;
   int32_t min_qual, default_qual, min_depth;
+  int32_t wide;               // 1: 128-bit 2-bit keys (K <= 63), 4-word exotic keys, pg_kmer_edge_wide output
   const KmerChunk* chunks;    // the batch's read chunks
   int32_t n_chunks;
   int32_t* full;              // per window: 1 when a probe sequence ran past the bound (count again, larger)
@@ -23,7 +24,7 @@ struct KmerArgs {
   // 2-bit tables: slots [slot_base[w], slot_base[w] + slot_cap[w]) of window w
   const int64_t* slot_base;
   const int64_t* slot_cap;
-  unsigned long long* keys;   // kEmpty = free
+  unsigned long long* keys;   // kEmpty = free; wide: two words per slot (16-byte aligned)
   uint32_t* cnt;              // 4 per slot
   unsigned long long* qs;     // 4 per slot
   uint32_t* mq_sum;
@@ -31,7 +32,7 @@ struct KmerArgs {
   // exotic tables (4-bit keys), single writer per window
   const int64_t* x_base;
   const int64_t* x_cap;
-  unsigned long long* x_keys; // 2 per slot
+  unsigned long long* x_keys; // 2 per slot (wide: 4)
   uint8_t* x_used;
   uint32_t* x_cnt;
   unsigned long long* x_qs;
@@ -44,6 +45,7 @@ struct KmerArgs {
   longlong2* x_events;
   // output
   pg_kmer_edge* edges;
+  pg_kmer_edge_wide* wedges;  // output of the wide tally
   int64_t edge_cap;
   unsigned long long* n_edges;
   int32_t* overflow;

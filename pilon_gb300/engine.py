@@ -47,6 +47,10 @@ def lib():
             "pg_set_tuning": (C.c_int, [vp, i32, i32, i32]),
             "pg_kmer_tally": (C.c_int, [vp, vp, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
                                         C.POINTER(C.c_int64)]),
+            "pg_kmer_tally_wide": (C.c_int, [vp, vp, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
+                                             C.POINTER(C.c_int64)]),
+            "pg_kmer_tally_breaks_wide": (C.c_int, [vp, i32, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
+                                                    C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
             "pg_last_kernel_ms": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_int32)]),
             "pg_sync": (C.c_int, [vp]),
@@ -198,15 +202,20 @@ class Engine:
         self._check(self.L.pg_fetch_all(self.h, C.byref(o)))
         return out
 
-    def kmer_tally(self, windows, K, params, min_depth=5, cap=None):
+    def kmer_tally(self, windows, K, params, min_depth=5, cap=None, wide=None):
+        """Edges of every window (pg_kmer_tally, K <= 31, or pg_kmer_tally_wide,
+        K <= 63: the wide form, four key words, when wide or K > 31)."""
+        wide = K > 31 if wide is None else wide
         wins = (_abi.pg_window * max(1, len(windows)))(*[_abi.pg_window(a, b) for a, b in windows])
+        fn = self.L.pg_kmer_tally_wide if wide else self.L.pg_kmer_tally
+        dt = _abi.kmer_edge_wide_dtype() if wide else _abi.kmer_edge_dtype()
         # start from the last call's edge count, so a repeated call runs once
         cap = cap or getattr(self, "_kmer_cap", 1 << 20)
         while True:
-            edges = np.zeros(cap, _abi.kmer_edge_dtype())
+            edges = np.zeros(cap, dt)
             n = C.c_int64()
-            self._check(self.L.pg_kmer_tally(self.h, C.cast(wins, C.c_void_p), len(windows), K, C.byref(params),
-                                             min_depth, edges.ctypes.data, cap, C.byref(n)))
+            self._check(fn(self.h, C.cast(wins, C.c_void_p), len(windows), K, C.byref(params), min_depth,
+                           edges.ctypes.data, cap, C.byref(n)))
             if n.value <= cap:
                 self._kmer_cap = max(cap, int(n.value))
                 return edges[:n.value]
@@ -249,15 +258,19 @@ class Engine:
             out.setdefault(int(b.region), []).append((int(b.start), int(b.stop)))
         return out
 
-    def kmer_tally_breaks(self, K, params, radius=500, min_depth=5, cap=None):
-        """pg_kmer_tally_breaks: the K-mer tally over one device-built window per
-        break candidate; returns (number of windows, edges)."""
+    def kmer_tally_breaks(self, K, params, radius=500, min_depth=5, cap=None, wide=None):
+        """pg_kmer_tally_breaks (K <= 31) or pg_kmer_tally_breaks_wide (K <= 63):
+        the K-mer tally over one device-built window per break candidate;
+        returns (number of windows, edges)."""
+        wide = K > 31 if wide is None else wide
+        fn = self.L.pg_kmer_tally_breaks_wide if wide else self.L.pg_kmer_tally_breaks
+        dt = _abi.kmer_edge_wide_dtype() if wide else _abi.kmer_edge_dtype()
         cap = cap or getattr(self, "_kmer_cap", 1 << 20)
         while True:
-            edges = np.zeros(cap, _abi.kmer_edge_dtype())
+            edges = np.zeros(cap, dt)
             nw, n = C.c_int64(), C.c_int64()
-            self._check(self.L.pg_kmer_tally_breaks(self.h, params.min_min_depth, radius, K, C.byref(params),
-                                                    min_depth, edges.ctypes.data, cap, C.byref(nw), C.byref(n)))
+            self._check(fn(self.h, params.min_min_depth, radius, K, C.byref(params), min_depth, edges.ctypes.data,
+                           cap, C.byref(nw), C.byref(n)))
             if n.value <= cap:
                 self._kmer_cap = max(cap, int(n.value))
                 return int(nw.value), edges[:n.value]

@@ -168,3 +168,54 @@ def test_kmer_tally_over_device_break_windows(engine, euk):
     assert edge_set(got) == edge_set(want)
     assert edge_set(oracle.kmer_tally(ds.reads, p, wins[:8], 31)) == edge_set(
         [e for e in got if int(e["window"]) < 8])
+
+
+def wide_edge_set(edges):
+    return {(int(e["window"]), int(e["key0"]), int(e["key1"]), int(e["key2"]), int(e["key3"]), int(e["next"]),
+             int(e["alt"]), int(e["depth"]), int(e["weight"])) for e in edges}
+
+
+def test_kmer_tally_wide_matches_oracle(engine, euk):
+    """pg_kmer_tally_wide at Pilon's default K = 47 (S/Assembler.scala:25), at
+    K = 63 and at K = 32 (the first K a 64-bit key cannot hold) equals the
+    oracle's tally; at K = 31 it equals pg_kmer_tally's edges."""
+    ds = euk
+    p = _abi.default_params()
+    idx = ReadIndex(ds.reads, len(ds.contigs))
+    n = ds.contigs[0].size
+    wins = [idx.range_for(0, max(1, pos - 500), min(n, pos + 500), n, slop=0)
+            for (pos, kind, ref, alt) in ds.variants[0][:30]]
+    engine.set_reference(ds.contigs)
+    engine.set_reads(ds.reads)
+    for K in (47, 63, 32):
+        got = engine.kmer_tally(wins, K, p)
+        want = oracle.kmer_tally_wide(ds.reads, p, wins, K)
+        assert len(got) > 1000, K
+        assert wide_edge_set(got) == wide_edge_set(want), K
+    narrow = engine.kmer_tally(wins, 31, p)
+    wide = engine.kmer_tally(wins, 31, p, wide=True)
+    assert {(w, a, b, x, y, d, g) for (w, a, b, c2, d2, x, y, d, g) in wide_edge_set(wide)} == edge_set(narrow)
+    assert all(int(e["key2"]) == 0 and int(e["key3"]) == 0 for e in wide)
+
+
+def test_kmer_tally_wide_exotic_kmers(engine, cfg1):
+    """K = 47 with reads holding N bases: the K-mers with N are tallied in the
+    4-word exotic tables."""
+    ds = cfg1
+    r = ds.reads
+    seq = r.seq.copy()
+    rng = np.random.Generator(np.random.PCG64(5))
+    hit = rng.choice(r.n_reads, size=r.n_reads // 5, replace=False)
+    for i in hit[:2000].tolist():
+        o = int(r.seq_off[i]) + 20
+        seq[o] = (seq[o] & 0x0F) | 0xF0
+    r2 = r.subset(np.arange(r.n_reads))
+    r2.seq = seq
+    engine.set_reference(ds.contigs)
+    engine.set_reads(r2)
+    p = _abi.default_params()
+    wins = [(0, 3000), (3000, 6000), (5000, 9000)]
+    got = engine.kmer_tally(wins, 47, p, min_depth=2)
+    want = oracle.kmer_tally_wide(r2, p, wins, 47, min_depth=2)
+    assert wide_edge_set(got) == wide_edge_set(want)
+    assert any("f" in "".join(format(int(e[f"key{q}"]), "016x") for q in range(3)) for e in want)
