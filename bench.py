@@ -473,7 +473,8 @@ def main():
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--compare-plain", type=int, default=-1, help="also time the per-region path (default: on "
                     "when there is more than one region)")
-    ap.add_argument("--e2e-fields", default="auto", help="all | calls: what the end-to-end step reads back")
+    ap.add_argument("--e2e-fields", default="auto", help="changes (default) | all | calls: what the end-to-end "
+                    "step reads back")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: requests per second")
     ap.add_argument("--duration", type=float, default=10.0, help="serving: seconds of arrivals")
     ap.add_argument("--workers", type=int, default=2, help="serving: engine contexts")
@@ -595,23 +596,34 @@ def main():
               "timing": "host wall clock of pg_find_breaks (device kernels, sorted list read back)"}
 
     # end to end through the C ABI: H2D of the read store from pinned memory,
-    # pileup + calls, D2H of every region's records and calls.  Measured with
-    # one engine context (each step's calls wait for the previous step's) and
-    # with two contexts on two host threads, the way a host serves several
-    # requests: one context's read-back overlaps the other's upload.
+    # pileup + calls, D2H of the step's result: by default the pass-1 changes of
+    # every region with their insertion strings (pg_fetch_changes, what the fix
+    # lists, FASTA and changes file are made from), or with --e2e-fields all |
+    # calls every position's records / calls.  Measured with one engine context
+    # (each step's calls wait for the previous step's) and with two contexts on
+    # two host threads, the way a host serves several requests: one context's
+    # read-back overlaps the other's upload.
     e2e = None
     if not args.no_e2e:
-        fields = args.e2e_fields if args.e2e_fields != "auto" else ("all" if sum(lens) <= 20_000_000 else "calls")
+        fields = args.e2e_fields if args.e2e_fields != "auto" else "changes"
         pin = pinned_store(ds.reads)
         n_pos = sum(e - s + 1 for (c, s, e, a, b) in regions)
-        outs = [PinnedOut(n_pos, fields)]  # all regions, one after another
+        outs = [PinnedOut(n_pos, fields) if fields != "changes" else None]  # all regions, one after another
         h2d = pin.nbytes()
-        d2h = outs[0].nbytes()
+        if fields == "changes":
+            eng.pileup_regions(regions, params, batched=bool(args.batched))
+            ch, chars = eng.fetch_changes()
+            d2h = ch.nbytes + len(chars)
+        else:
+            d2h = outs[0].nbytes()
 
         def e2e_step(e, o):
             e.set_reads(pin)
             e.pileup_regions(regions, params, batched=bool(args.batched))
-            e.fetch_all(o.arrays)
+            if o is None:
+                e.fetch_changes()
+            else:
+                e.fetch_all(o.arrays)
 
         for _ in range(args.warmup):
             e2e_step(eng, outs[0])
@@ -628,7 +640,7 @@ def main():
         eng2 = Engine(local)
         eng2.set_tuning(*shape)
         eng2.set_reference(ds.contigs)
-        outs.append(PinnedOut(n_pos, fields))
+        outs.append(PinnedOut(n_pos, fields) if fields != "changes" else None)
         engines = [eng, eng2]
         for _ in range(args.warmup):
             e2e_step(eng2, outs[1])

@@ -253,6 +253,27 @@ pg_status pg_fetch_region(pg_ctx *ctx, int32_t region, pg_region_out *out);
  * in call order (one copy per array instead of one per region). */
 pg_status pg_fetch_all(pg_ctx *ctx, pg_region_out *out);
 
+/* One change of pass 1 of GenomeRegion.postProcess (S/GenomeRegion.scala:
+ * 233-272): a position whose call became a SNP, INS, DEL or AMB change after
+ * the deletion-span update.  These are what identifyAndFixIssues turns into
+ * fixes (S/GenomeRegion.scala:307-414). */
+typedef struct pg_change {
+  int32_t region;            /* region of the last pg_pileup_regions call */
+  int32_t locus;             /* 1-based contig locus */
+  uint32_t call;             /* PG_CALL_* flags: base, alt, change kind */
+  int32_t indel_len;         /* inserted or deleted bases, else 0 */
+  int32_t ins_str;           /* offset of the inserted bases in ins_chars, else -1 */
+  int32_t pad_;
+} pg_change;
+
+/* The changes of every region of the last call, ordered by region and locus,
+ * and the insertion characters they point into (copied when ins_chars is not
+ * NULL and they fit in ins_cap).  *n_changes and *n_ins_chars receive the
+ * full sizes; the changes are copied up to cap.  This is what the fix lists
+ * need, a small fraction of the per-position arrays. */
+pg_status pg_fetch_changes(pg_ctx *ctx, pg_change *out, int64_t cap, int64_t *n_changes, char *ins_chars,
+                           int64_t ins_cap, int64_t *n_ins_chars);
+
 /* Launch shape of the pileup walk kernel: tile width (positions per CTA,
  * a power of two in [256, 4096]), warps per CTA (1..16) and variant (lanes
  * per read: 0 = 32, 1 = 16, 2 = 8, 3 = 4); 0 / -1 keep the current value.  The host

@@ -139,6 +139,13 @@ def kmer_edge_dtype():
                      ("pad_", "<i2"), ("depth", "<i4"), ("weight", "<i4")])
 
 
+# numpy dtype of pg_change
+def change_dtype():
+    import numpy as np
+    return np.dtype([("region", "<i4"), ("locus", "<i4"), ("call", "<u4"), ("indel_len", "<i4"), ("ins_str", "<i4"),
+                     ("pad_", "<i4")])
+
+
 # numpy dtype of pg_kmer_edge_wide (K <= 63)
 def kmer_edge_wide_dtype():
     import numpy as np
@@ -165,7 +172,7 @@ EXPORTED = [
     "pg_fetch_stats", "pg_fetch_region", "pg_set_tuning", "pg_kmer_tally",
     "pg_last_kernel_ms", "pg_sync", "pg_phys_cov_scan_static", "pg_format_vcf", "pg_find_breaks",
     "pg_kmer_tally_breaks", "pg_fetch_all", "pg_graph_replays", "pg_last_tally_stats",
-    "pg_find_duplications", "pg_kmer_tally_wide", "pg_kmer_tally_breaks_wide",
+    "pg_find_duplications", "pg_kmer_tally_wide", "pg_kmer_tally_breaks_wide", "pg_fetch_changes",
     "pg_default_serve_config", "pg_serve_open", "pg_serve_submit", "pg_serve_poll", "pg_serve_release",
     "pg_serve_stats", "pg_serve_error", "pg_serve_close",
 ]

@@ -87,6 +87,7 @@ struct pg_ctx {
   // break candidates
   DevBuf bfrag, bsums, btiles, bgaps, bruns, bcnt, boff, bout;
   DevBuf druns, dout, dcount;  // duplication events
+  DevBuf chg_count, chg_off, chg_out;  // changes of the last call (pg_fetch_changes)
   int64_t brk_n = -1;             // breaks of the last pileup call on the device, -1: not found yet
   int32_t brk_mmd = 0;
   // CUDA graph of the batched pipeline, replayed while the plan and buffers are unchanged
@@ -268,7 +269,8 @@ void pg_close(pg_ctx* c) {
                   &c->kedges, &c->kcount, &c->kx_ev, &c->kx_evbase, &c->kx_evcap, &c->kx_evfill, &c->kwflag,
                   &c->kused, &c->kchunks, &c->vlen,
                   &c->vsums, &c->vtext, &c->vname, &c->bfrag, &c->bsums, &c->btiles, &c->bgaps, &c->bruns,
-                  &c->bcnt, &c->boff, &c->bout, &c->druns, &c->dout, &c->dcount};
+                  &c->bcnt, &c->boff, &c->bout, &c->druns, &c->dout, &c->dcount, &c->chg_count, &c->chg_off,
+                  &c->chg_out};
   for (DevBuf* b : km) release(*b);
   for (auto& b : c->rec_i32) release(b);
   for (auto& b : c->rd) release(b);
@@ -808,6 +810,42 @@ pg_status pg_fetch_all(pg_ctx* c, pg_region_out* o) {
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
   cudaSetDevice(c->device);
   return fetch_positions(c, 0, (size_t)c->n_positions, o);
+}
+
+pg_status pg_fetch_changes(pg_ctx* c, pg_change* out, int64_t cap, int64_t* n_changes, char* ins_chars,
+                           int64_t ins_cap, int64_t* n_ins_chars) {
+  const Range nvtx_range("pg_fetch_changes");
+  if (!c || !n_changes || !n_ins_chars || cap < 0 || (cap > 0 && !out) || ins_cap < 0)
+    return fail(c, PG_ERR_ARG, "bad arguments");
+  if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  *n_changes = *n_ins_chars = 0;
+  const int32_t nt = c->n_call_tiles;
+  if (nt == 0) return PG_OK;
+  pg_status s;
+  if ((s = ensure(c, c->chg_count, 4 * ((size_t)nt + 2)))) return s;
+  if ((s = ensure(c, c->chg_off, 4 * ((size_t)nt + 2)))) return s;
+  launch_change_count(P<RegionDev>(c->regions), P<int32_t>(c->call_tile_region), P<uint32_t>(c->rec_call),
+                      P<int32_t>(c->chg_count), nt, st);
+  launch_scan_small(P<int32_t>(c->chg_count), P<int32_t>(c->chg_off), nt, st);
+  int32_t total = 0;
+  unsigned long long pool_fill = 0;
+  CK(cudaMemcpyAsync(&total, P<int32_t>(c->chg_off) + nt, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&pool_fill, P<unsigned long long>(c->counters) + CNT_POOL, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if ((s = ensure(c, c->chg_out, sizeof(pg_change) * (size_t)std::max(total, 1)))) return s;
+  launch_change_write(P<RegionDev>(c->regions), P<int32_t>(c->call_tile_region), records(c),
+                      P<int32_t>(c->chg_count), P<int32_t>(c->chg_off), P<pg_change>(c->chg_out), nt, st);
+  CK(cudaGetLastError());
+  const int64_t ncopy = std::min<int64_t>(total, cap);
+  if (ncopy > 0) CK(cudaMemcpyAsync(out, c->chg_out.p, sizeof(pg_change) * ncopy, cudaMemcpyDeviceToHost, st));
+  if (ins_chars && pool_fill > 0 && (int64_t)pool_fill <= ins_cap)
+    CK(cudaMemcpyAsync(ins_chars, c->pool.p, pool_fill, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  *n_changes = total;
+  *n_ins_chars = (int64_t)pool_fill;
+  return PG_OK;
 }
 
 static int64_t next_pow2(int64_t x) {

@@ -169,6 +169,83 @@ __global__ void __launch_bounds__(kCandThreads) k_cand_list(CallArgs a, const in
   }
 }
 
+// The changes of every call tile (final call flags), for pg_fetch_changes:
+// k_change_count counts a tile's changes, k_change_write places them at the
+// tile's offset from the scan of the counts, in position order.
+__global__ void __launch_bounds__(kCandThreads) k_change_count(const RegionDev* regions, const int32_t* tile_region,
+                                                                const uint32_t* call, int32_t* count) {
+  __shared__ int32_t s_w[kCandThreads / 32];
+  const int32_t t = blockIdx.x;
+  const RegionDev& g = regions[tile_region[t]];
+  const int32_t p0 = (t - g.call_tile0) * kCallTile;
+  int32_t n = 0;
+  for (int32_t i = threadIdx.x; i < kCallTile; i += kCandThreads)
+    if (p0 + i < g.size) n += PG_CALL_CHANGE(call[g.pos_base + p0 + i]) != 0;
+  n = __reduce_add_sync(FULL, n);
+  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int32_t v = 0;
+    for (int w = 0; w < kCandThreads / 32; w++) v += s_w[w];
+    count[t] = v;
+  }
+}
+
+__global__ void __launch_bounds__(kCandThreads) k_change_write(const RegionDev* regions, const int32_t* tile_region,
+                                                                Records rec, const int32_t* count, const int32_t* off,
+                                                                pg_change* out) {
+  __shared__ __align__(16) uint32_t s_c[kCallTile];
+  __shared__ int32_t s_w[kCandThreads / 32];
+  const int32_t t = blockIdx.x;
+  if (count[t] == 0) return;  // the whole CTA leaves
+  const int32_t r = tile_region[t];
+  const RegionDev g = regions[r];
+  const int32_t p0 = (t - g.call_tile0) * kCallTile;
+  const int32_t n = min(kCallTile, g.size - p0);
+  for (int32_t i = threadIdx.x; i < kCallTile; i += kCandThreads) s_c[i] = i < n ? rec.call[g.pos_base + p0 + i] : 0u;
+  __syncthreads();
+  const uint4 c4 = reinterpret_cast<const uint4*>(s_c)[threadIdx.x];  // positions 4 tid .. 4 tid + 3
+  const uint32_t cc[4] = {c4.x, c4.y, c4.z, c4.w};
+  int32_t mine = 0;
+#pragma unroll
+  for (int j = 0; j < 4; j++) mine += PG_CALL_CHANGE(cc[j]) != 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int32_t incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t y = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_w[warp] = incl;
+  __syncthreads();
+  int32_t slot = off[t] + incl - mine;
+  for (int w = 0; w < warp; w++) slot += s_w[w];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    if (!PG_CALL_CHANGE(cc[j])) continue;
+    const int32_t p = p0 + 4 * (int32_t)threadIdx.x + j;
+    const int64_t gp = g.pos_base + p;
+    pg_change ch;
+    ch.region = r;
+    ch.locus = g.start + p;
+    ch.call = cc[j];
+    ch.indel_len = rec.indel_len[gp];
+    ch.ins_str = rec.ins_str[gp];
+    ch.pad_ = 0;
+    out[slot++] = ch;
+  }
+}
+
+void launch_change_count(const RegionDev* regions, const int32_t* tile_region, const uint32_t* call, int32_t* count,
+                         int32_t n_tiles, cudaStream_t s) {
+  if (n_tiles > 0) k_change_count<<<n_tiles, kCandThreads, 0, s>>>(regions, tile_region, call, count);
+}
+
+void launch_change_write(const RegionDev* regions, const int32_t* tile_region, const Records& rec,
+                         const int32_t* count, const int32_t* off, pg_change* out, int32_t n_tiles, cudaStream_t s) {
+  if (n_tiles > 0) k_change_write<<<n_tiles, kCandThreads, 0, s>>>(regions, tile_region, rec, count, off, out);
+}
+
 void launch_cand_list(const CallArgs& a, const int32_t* cand_off, Cand* cands, int32_t cand_cap,
                       int32_t tile_begin, int32_t n_tiles, cudaStream_t s) {
   if (n_tiles <= 0) return;

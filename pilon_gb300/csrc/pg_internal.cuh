@@ -441,5 +441,9 @@ void launch_resolve(const RegionDev* regions, int32_t n_regions, const int32_t* 
                     int32_t cand_cap, StatsDev* stats, cudaStream_t s);
 void launch_apply_spans(const CallArgs& a, const Cand* cands, const int32_t* cand_total, int32_t cand_cap,
                         cudaStream_t s);
+void launch_change_count(const RegionDev* regions, const int32_t* tile_region, const uint32_t* call, int32_t* count,
+                         int32_t n_tiles, cudaStream_t s);
+void launch_change_write(const RegionDev* regions, const int32_t* tile_region, const Records& rec,
+                         const int32_t* count, const int32_t* off, pg_change* out, int32_t n_tiles, cudaStream_t s);
 
 }  // namespace pg

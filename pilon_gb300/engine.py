@@ -69,6 +69,7 @@ def lib():
             "pg_format_vcf": (C.c_int, [vp, i32, C.c_char_p, i32, i32, i32, vp, i64, C.POINTER(C.c_int64)]),
             "pg_find_breaks": (C.c_int, [vp, i32, vp, i64, C.POINTER(C.c_int64)]),
             "pg_find_duplications": (C.c_int, [vp, vp, i64, C.POINTER(C.c_int64)]),
+            "pg_fetch_changes": (C.c_int, [vp, vp, i64, C.POINTER(C.c_int64), vp, i64, C.POINTER(C.c_int64)]),
             "pg_kmer_tally_breaks": (C.c_int, [vp, i32, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
                                                C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         }
@@ -244,6 +245,22 @@ class Engine:
             b = buf[k]
             out.setdefault(int(b.region), []).append((int(b.start), int(b.stop)))
         return out
+
+    def fetch_changes(self, cap=None, ins_cap=None):
+        """pg_fetch_changes: (changes as a pg_change array ordered by region and
+        locus, insertion characters) of the last pileup_regions call."""
+        cap = cap or getattr(self, "_chg_cap", 1 << 16)
+        ins_cap = ins_cap or getattr(self, "_ins_cap", 1 << 16)
+        while True:
+            out = np.zeros(cap, _abi.change_dtype())
+            chars = np.zeros(ins_cap, np.uint8)
+            n, ni = C.c_int64(), C.c_int64()
+            self._check(self.L.pg_fetch_changes(self.h, out.ctypes.data, cap, C.byref(n), chars.ctypes.data, ins_cap,
+                                                C.byref(ni)))
+            if n.value <= cap and ni.value <= ins_cap:
+                self._chg_cap, self._ins_cap = cap, ins_cap
+                return out[:n.value], chars[:ni.value].tobytes()
+            cap, ins_cap = max(cap, int(n.value)), max(ins_cap, int(ni.value))
 
     def find_duplications(self):
         """pg_find_duplications: the <DUP> regions (duplicationEvents) of every

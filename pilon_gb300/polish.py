@@ -110,43 +110,25 @@ class RegionResult:
         return fix_fix_list(self.snp + self.small)
 
 
-def _region_outputs(engine, r, region, ref, opts, params, dupes=()):
-    """Sparse change list -> fix lists and fixed bases; the region's duplication
-    events (pg_find_duplications) -> where its <DUP> records go."""
+def _region_outputs(engine, r, region, ref, opts, params, changes, chars, dupes=()):
+    """The region's changes (pg_fetch_changes: pass-1 changes in locus order,
+    insertion characters) -> fix lists and fixed bases; its duplication events
+    (pg_find_duplications) -> where its <DUP> records go."""
     c, s, e, _, _ = region
     size = e - s + 1
     st = engine.stats(r)
-    call = np.empty(size, np.uint32)
-    ilen = np.empty(size, np.int32)
-    istr = np.empty(size, np.int32)
-    o = _abi.pg_region_out()
-    o.call = call.ctypes.data
-    o.indel_len = ilen.ctypes.data
-    o.ins_str = istr.ctypes.data
-    engine._check(engine.L.pg_fetch_region(engine.h, r, C.byref(o)))
-    pool = int(o.ins_chars_cap)
-    chars = b""
-    if pool:
-        buf = np.zeros(pool, np.uint8)
-        o2 = _abi.pg_region_out()
-        o2.ins_chars = buf.ctypes.data
-        o2.ins_chars_cap = pool
-        engine._check(engine.L.pg_fetch_region(engine.h, r, C.byref(o2)))
-        chars = buf.tobytes()
     orig = bytes(ref[s - 1:e])
     res = RegionResult(c, s, e, bytearray(orig), stats=st)
-    kind = (call >> 9) & 7
-    chg = np.nonzero(kind)[0]
-    excluded = np.zeros(size, bool)
+    excluded = None
     if opts.longread and opts.nanopore is not None and opts.longread_only:
         excluded = _exclude_motifs(orig, s, e, opts.nanopore)
-    for i in chg.tolist():
-        if excluded[i]:
+    for ch in changes:
+        loc = int(ch["locus"])
+        if excluded is not None and excluded[loc - s]:
             continue
-        k = int(kind[i])
-        loc = s + i
+        f = int(ch["call"])
+        k = (f >> 9) & 7
         rb = chr(ref[loc - 1]).upper()
-        f = int(call[i])
         cb = ACGT[f & 3] if f & _abi.PG_CALL_HAS_BASE else "N"
         alt = ACGT[(f >> 2) & 3]
         if k == _abi.PG_CHANGE_SNP:
@@ -160,11 +142,11 @@ def _region_outputs(engine, r, region, ref, opts, params, dupes=()):
                     res.snp.append(Fix(loc, rb, cb))
         elif k == _abi.PG_CHANGE_INS:
             if opts.fix_indels:
-                off = int(istr[i])
-                res.small.append(Fix(loc, "", chars[off:off + int(ilen[i])].decode()))
+                off = int(ch["ins_str"])
+                res.small.append(Fix(loc, "", chars[off:off + int(ch["indel_len"])].decode()))
         elif k == _abi.PG_CHANGE_DEL:
             if opts.fix_indels:
-                res.small.append(Fix(loc, bytes(ref[loc - 1:loc - 1 + int(ilen[i])]).decode(), ""))
+                res.small.append(Fix(loc, bytes(ref[loc - 1:loc - 1 + int(ch["indel_len"])]).decode(), ""))
     # the reference prepends to its lists: descending loci, then stable-sorted
     res.snp.reverse()
     res.small.reverse()
@@ -173,6 +155,10 @@ def _region_outputs(engine, r, region, ref, opts, params, dupes=()):
     res.dupes = list(dupes)
     if res.dupes:
         # records per position: one, plus one after an indel call at i > 0 outside a deletion
+        call = np.empty(size, np.uint32)
+        o = _abi.pg_region_out()
+        o.call = call.ctypes.data
+        engine._check(engine.L.pg_fetch_region(engine.h, r, C.byref(o)))
         extra = ((call & (_abi.PG_CALL_INS | _abi.PG_CALL_DEL)) != 0) & ((call & _abi.PG_CALL_DELETED) == 0)
         extra[0] = False
         res.first_line = np.concatenate([[0], np.cumsum(1 + extra.astype(np.int64))])
@@ -256,8 +242,11 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
     engine.pileup_regions(regions, params, batched=batched)
     # pass 2 of postProcess and duplicationEvents, on the device (the <DUP> records)
     dups = engine.find_duplications() if opts.vcf else {}
-    results = [_region_outputs(engine, r, reg, contigs[reg[0]], opts, params, dups.get(r, ()))
-               for r, reg in enumerate(regions)]
+    # the pass-1 changes of all regions at once, ordered by region and locus
+    changes, chars = engine.fetch_changes()
+    bounds = np.searchsorted(changes["region"], np.arange(len(regions) + 1))
+    results = [_region_outputs(engine, r, reg, contigs[reg[0]], opts, params, changes[bounds[r]:bounds[r + 1]],
+                               chars, dups.get(r, ())) for r, reg in enumerate(regions)]
     # The output groups of GenomeFile.regions (S/GenomeFile.scala:49-54): a contig
     # with its chunks, or with --targets one group per target (two targets on one
     # contig give two FASTA records, and each restarts the changes offset).

@@ -226,3 +226,24 @@ def test_region_range_of_another_reference_refused(cfg1):
         compare_region(eng.fetch(1), ora[0], label="swapped contig 0")
     finally:
         eng.close()
+
+
+def test_fetch_changes_equals_call_arrays(engine):
+    """pg_fetch_changes returns exactly the positions whose call carries a
+    change, in region and locus order, with the calls, indel lengths and
+    insertion strings of the per-region arrays."""
+    ds = synth.generate(3, scale=0.01)
+    regions = plan(ds)
+    engine.set_reference(ds.contigs)
+    engine.set_reads(ds.reads)
+    engine.pileup_regions(regions, _abi.default_params())
+    changes, chars = engine.fetch_changes()
+    want = []
+    for r, (c, s, e, a, b) in enumerate(regions):
+        x = engine.fetch(r)
+        for i in np.nonzero((x.call >> 9) & 7)[0].tolist():
+            want.append((r, s + i, int(x.call[i]), int(x.indel_len[i]), x.insertion(i)))
+    got = [(int(ch["region"]), int(ch["locus"]), int(ch["call"]), int(ch["indel_len"]),
+            chars[int(ch["ins_str"]):int(ch["ins_str"]) + int(ch["indel_len"])].decode() if ch["ins_str"] >= 0 else "")
+           for ch in changes]
+    assert len(want) > 100 and got == want

@@ -77,6 +77,21 @@ class OracleEngine:
     def stats(self, r):
         return self.results[r].stats
 
+    def fetch_changes(self):
+        """pg_fetch_changes' contract over the oracle's per-region arrays: the
+        changed positions of every region in locus order, with insertion offsets
+        into one pool of all regions' insertion characters."""
+        rows, pool = [], b""
+        for r, (c, s, e, rb, re) in enumerate(self.regions):
+            res = self.results[r]
+            for i in np.nonzero((res.call >> 9) & 7)[0].tolist():
+                off = -1
+                if int(res.ins_str[i]) >= 0:
+                    off = len(pool)
+                    pool += res.insertion(i).encode()
+                rows.append((r, s + i, int(res.call[i]), int(res.indel_len[i]), off, 0))
+        return np.array(rows, dtype=_abi.change_dtype()), pool
+
     def find_duplications(self):
         """duplicationEvents restated on the host from the oracle's arrays: pass 2
         of postProcess (smooth, copyNumber) and summaryRegions, as the device's
@@ -309,7 +324,9 @@ def request_result(engine, r, req, names, contigs, params, opts):
     from pilon_gb300.polish import _region_outputs, new_name, region_string
     from pilon_gb300.serve import Result
     region = (req.contig, req.start, req.stop, 0, 0)
-    res = _region_outputs(engine, r, region, contigs[req.contig], opts, params)
+    changes, chars = engine.fetch_changes()
+    res = _region_outputs(engine, r, region, contigs[req.contig], opts, params, changes[changes["region"] == r],
+                          chars)
     nn = new_name(names[req.contig])
     lines = []
     delta = 0
