@@ -82,15 +82,16 @@ __device__ __forceinline__ uint32_t call_position(const CallArgs& a, const Regio
   return change;
 }
 
-// 256 threads per CTA, two positions per thread (p and p + 256), two CTAs per
-// call tile: both records are loaded before either call is made, and a thread
-// that runs a long indel vote holds back only its own small CTA.
+// 256 threads per CTA, one position per thread, four CTAs per call tile: a
+// thread that runs a long indel vote holds back only its own small CTA.  (Two
+// positions per thread, both records loaded before either call, needed 80
+// registers, fell to 3 CTAs per SM and made the kernel 1.5x slower.)
 constexpr int kCallThreads = 256;
-constexpr int kCallPer = 2;
+constexpr int kCallPer = 1;
 constexpr int kCallCtas = kCallTile / (kCallThreads * kCallPer);
 static_assert(kCallCtas * kCallThreads * kCallPer == kCallTile, "call tile split");
 
-__global__ void __launch_bounds__(kCallThreads, 3) k_call(CallArgs a, int32_t tile_begin) {
+__global__ void __launch_bounds__(kCallThreads, 6) k_call(CallArgs a, int32_t tile_begin) {
   const int32_t t = tile_begin + blockIdx.x / kCallCtas;
   const int32_t r = a.call_tile_region[t];
   const RegionDev g = a.regions[r];
