@@ -76,8 +76,8 @@ struct pg_ctx {
   double walk_ms = 0, total_ms = 0;
   int32_t launches = 0;
   // k-mer tally
-  DevBuf kwin, kpre, kslot_base, kslot_cap, kx_base, kx_cap, kkeys, kcnt, kqs, kmq, kq;
-  DevBuf kx_keys, kx_used, kx_cnt, kx_qs, kx_mq, kx_q, kedges, kcount, kx_ev, kx_evbase, kx_evcap, kx_evfill;
+  DevBuf kwin, kpre, kslot_base, kslot_cap, kx_base, kx_cap, kslots, kwlist;
+  DevBuf kx_keys, kx_used, kx_cnt, kx_qs, kx_q, kedges, kcount, kx_ev, kx_evbase, kx_evcap, kx_evfill;
   DevBuf kwflag, kused, kchunks;
   double tally_ms = 0;  // kernel time of the last tally (CUDA events)
   int64_t tally_events = 0, tally_distinct = 0, tally_max_batch_bytes = 0;
@@ -264,8 +264,8 @@ void pg_close(pg_ctx* c) {
                    &c->events, &c->events_sorted, &c->cands, &c->pool, &c->counters, &c->run_max, &c->staging_dev,
                    &c->chunk_stats, &c->spool, &c->indel_list};
   for (DevBuf* b : all) release(*b);
-  DevBuf* km[] = {&c->kwin, &c->kpre, &c->kslot_base, &c->kslot_cap, &c->kx_base, &c->kx_cap, &c->kkeys, &c->kcnt,
-                  &c->kqs, &c->kmq, &c->kq, &c->kx_keys, &c->kx_used, &c->kx_cnt, &c->kx_qs, &c->kx_mq, &c->kx_q,
+  DevBuf* km[] = {&c->kwin, &c->kpre, &c->kslot_base, &c->kslot_cap, &c->kx_base, &c->kx_cap, &c->kslots, &c->kwlist,
+                  &c->kx_keys, &c->kx_used, &c->kx_cnt, &c->kx_qs, &c->kx_q,
                   &c->kedges, &c->kcount, &c->kx_ev, &c->kx_evbase, &c->kx_evcap, &c->kx_evfill, &c->kwflag,
                   &c->kused, &c->kchunks, &c->vlen,
                   &c->vsums, &c->vtext, &c->vname, &c->bfrag, &c->bsums, &c->btiles, &c->bgaps, &c->bruns,
@@ -903,22 +903,23 @@ static pg_status kmer_windows(pg_ctx* c, const pg_window* windows, int32_t n_win
 // Tables are sized at a quarter of each window's K-mer events (the distinct
 // K-mers are fewer: every error-free K-mer recurs once per covering read and
 // strand; 13% of the events on the 120 Mb workload) and windows are grouped
-// into batches of about kTallyBatchBytes of tables.  A batch of a few dozen
-// windows would keep its tables in L2 but runs too few CTAs to fill the GPU
-// (measured: 2.4 warps per SM, five times slower), so a batch holds hundreds of
-// windows, each walked by CTAs of kTallyReadsPerChunk reads.  A window whose
-// table fills up (a probe sequence longer than the kernel's bound) is counted
-// again with a table four times larger before its edges are built; the
-// results do not depend on the table size.
-constexpr int64_t kTallyBatchBytes = (int64_t)1 << 30;
-constexpr int64_t kTallyReadsPerChunk = 64;
+// into batches of about kTallyBatchBytes of tables, so that a batch's probes
+// and counter atomics stay in L2.  A batch of a few dozen windows still fills
+// the GPU: one warp per read, CTAs of kTallyReadsPerChunk reads.  The batches
+// run back to back on the stream with no host wait; a window whose table fills
+// up (a probe sequence longer than the kernel's bound) writes no edges and is
+// counted again, after all batches, with a table four times larger.  The
+// results do not depend on the table size or the batching.
+constexpr int64_t kTallyBatchBytes = (int64_t)64 << 20;
+constexpr int64_t kTallyReadsPerChunk = 8;
 
 static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_params* params, int32_t min_depth,
                            bool wide, void* edges, int64_t cap, int64_t* n_edges) {
   cudaStream_t st = c->stream;
-  // bytes per slot: key (8 or 16), count 4 x 4, qualSum 4 x 8, mqSum, qSum; exotic slots hold
-  // 2 or 4 key words and a used byte (rounded up)
-  const int64_t slot_b = wide ? 72 : 64, xslot_b = wide ? 96 : 80, kw = wide ? 2 : 1, xkw = wide ? 4 : 2;
+  // bytes per slot: KmerSlot / KmerSlotWide; exotic slots hold 2 or 4 key words, a used byte and
+  // the counters (rounded up)
+  const int64_t slot_b = wide ? (int64_t)sizeof(KmerSlotWide) : (int64_t)sizeof(KmerSlot);
+  const int64_t xslot_b = wide ? 96 : 80, xkw = wide ? 4 : 2;
   const size_t edge_b = wide ? sizeof(pg_kmer_edge_wide) : sizeof(pg_kmer_edge);
   pg_status s;
   c->tally_ms = 0;
@@ -944,121 +945,121 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
     c->tally_events += pre[3 * w + 1];
   }
   const int64_t edge_cap = std::max<int64_t>(cap, 1);
+  const size_t nwb = (size_t)std::max<int32_t>(n_windows, 1);
   if ((s = ensure(c, c->kedges, edge_b * edge_cap))) return s;
   if ((s = ensure(c, c->kcount, 16))) return s;
-  if ((s = ensure(c, c->kwflag, 4 * (size_t)n_windows))) return s;
-  if ((s = ensure(c, c->kused, 8 * (size_t)n_windows))) return s;
-  if ((s = ensure(c, c->kslot_base, 8 * (size_t)n_windows))) return s;
-  if ((s = ensure(c, c->kslot_cap, 8 * (size_t)n_windows))) return s;
-  if ((s = ensure(c, c->kx_base, 8 * (size_t)n_windows))) return s;
-  if ((s = ensure(c, c->kx_cap, 8 * (size_t)n_windows))) return s;
-  if ((s = ensure(c, c->kx_evbase, 8 * (size_t)n_windows))) return s;
-  if ((s = ensure(c, c->kx_evcap, 8 * (size_t)n_windows))) return s;
-  if ((s = ensure(c, c->kx_evfill, 8 * (size_t)n_windows))) return s;
+  if ((s = ensure(c, c->kwflag, 4 * nwb))) return s;
+  if ((s = ensure(c, c->kused, 8 * nwb))) return s;
+  if ((s = ensure(c, c->kwlist, 4 * nwb))) return s;
+  if ((s = ensure(c, c->kslot_base, 8 * nwb))) return s;
+  if ((s = ensure(c, c->kslot_cap, 8 * nwb))) return s;
+  if ((s = ensure(c, c->kx_base, 8 * nwb))) return s;
+  if ((s = ensure(c, c->kx_cap, 8 * nwb))) return s;
+  if ((s = ensure(c, c->kx_evbase, 8 * nwb))) return s;
+  if ((s = ensure(c, c->kx_evcap, 8 * nwb))) return s;
+  if ((s = ensure(c, c->kx_evfill, 8 * nwb))) return s;
   CK(cudaMemsetAsync(c->kcount.p, 0, 16, st));
-  CK(cudaMemsetAsync(c->kused.p, 0, 8 * (size_t)n_windows, st));
+  CK(cudaMemsetAsync(c->kused.p, 0, 8 * nwb, st));
+  CK(cudaMemsetAsync(c->kwflag.p, 0, 4 * nwb, st));
+  CK(cudaMemsetAsync(c->kx_evfill.p, 0, 8 * nwb, st));
   auto table_bytes = [&](int32_t w) { return scap[w] * slot_b + xcap[w] * xslot_b + evcap[w] * 16; };
+  struct Batch {
+    int32_t l0, l1;      // windows list[l0, l1)
+    int64_t c0, c1;      // chunks [c0, c1)
+    int64_t ns, nx, ne;  // table slots, exotic slots, exotic events
+  };
+  std::vector<int32_t> list(n_windows);
+  for (int32_t w = 0; w < n_windows; w++) list[w] = w;
   std::vector<KmerChunk> chunks;
-  std::vector<int32_t> flags;
-  int32_t w0 = 0;
-  while (w0 < n_windows) {
-    int32_t w1 = w0;
-    int64_t bytes = 0;
-    while (w1 < n_windows && (w1 == w0 || bytes + table_bytes(w1) <= kTallyBatchBytes)) bytes += table_bytes(w1++);
-    // read chunks of the batch: several CTAs per window
+  std::vector<Batch> batches;
+  KmerArgs a;
+  a.R = c->R; a.K = K; a.wide = wide;
+  a.min_qual = params->min_qual; a.default_qual = params->default_qual; a.min_depth = min_depth;
+  a.full = P<int32_t>(c->kwflag); a.used = P<unsigned long long>(c->kused);
+  a.slot_base = P<int64_t>(c->kslot_base); a.slot_cap = P<int64_t>(c->kslot_cap);
+  a.x_base = P<int64_t>(c->kx_base); a.x_cap = P<int64_t>(c->kx_cap);
+  a.x_ev_base = P<int64_t>(c->kx_evbase); a.x_ev_cap = P<int64_t>(c->kx_evcap);
+  a.x_ev_fill = P<unsigned long long>(c->kx_evfill);
+  a.edges = P<pg_kmer_edge>(c->kedges); a.wedges = P<pg_kmer_edge_wide>(c->kedges); a.edge_cap = edge_cap;
+  a.n_edges = P<unsigned long long>(c->kcount); a.overflow = (int32_t*)(P<unsigned long long>(c->kcount) + 1);
+  for (int pass = 0; !list.empty(); pass++) {
+    if (pass > 8) return fail(c, PG_ERR_LIMIT, "K-mer table overflow");
+    // batches over the listed windows; table offsets are relative to the batch
+    batches.clear();
     chunks.clear();
-    for (int32_t w = w0; w < w1; w++)
-      for (int64_t lo = wins[w].read_begin; lo < wins[w].read_end; lo += kTallyReadsPerChunk)
-        chunks.push_back(KmerChunk{lo, std::min<int64_t>(lo + kTallyReadsPerChunk, wins[w].read_end), w, 0});
+    int64_t max_ns = 1, max_nx = 1, max_ne = 1;
+    for (int32_t l0 = 0; l0 < (int32_t)list.size();) {
+      Batch b{l0, l0, (int64_t)chunks.size(), 0, 0, 0, 0};
+      int64_t bytes = 0;
+      while (b.l1 < (int32_t)list.size() && (b.l1 == l0 || bytes + table_bytes(list[b.l1]) <= kTallyBatchBytes)) {
+        const int32_t w = list[b.l1++];
+        bytes += table_bytes(w);
+        sbase[w] = b.ns; xbase[w] = b.nx; evbase[w] = b.ne;
+        b.ns += scap[w]; b.nx += xcap[w]; b.ne += evcap[w];
+        for (int64_t lo = wins[w].read_begin; lo < wins[w].read_end; lo += kTallyReadsPerChunk)
+          chunks.push_back(KmerChunk{lo, std::min<int64_t>(lo + kTallyReadsPerChunk, wins[w].read_end), w, 0});
+      }
+      b.c1 = (int64_t)chunks.size();
+      max_ns = std::max(max_ns, b.ns); max_nx = std::max(max_nx, b.nx); max_ne = std::max(max_ne, b.ne);
+      c->tally_max_batch_bytes = std::max(c->tally_max_batch_bytes, bytes);
+      batches.push_back(b);
+      l0 = b.l1;
+    }
+    if ((s = ensure(c, c->kslots, (size_t)(slot_b * max_ns)))) return s;
+    if ((s = ensure(c, c->kx_ev, 16 * (size_t)max_ne))) return s;
+    if ((s = ensure(c, c->kx_keys, 8 * xkw * (size_t)max_nx))) return s;
+    if ((s = ensure(c, c->kx_used, (size_t)max_nx))) return s;
+    if ((s = ensure(c, c->kx_cnt, 16 * (size_t)max_nx))) return s;
+    if ((s = ensure(c, c->kx_qs, 32 * (size_t)max_nx))) return s;
+    if ((s = ensure(c, c->kx_q, 4 * (size_t)max_nx))) return s;
     if ((s = ensure(c, c->kchunks, sizeof(KmerChunk) * std::max<size_t>(chunks.size(), 1)))) return s;
     if (!chunks.empty())
       CK(cudaMemcpyAsync(c->kchunks.p, chunks.data(), sizeof(KmerChunk) * chunks.size(), cudaMemcpyHostToDevice, st));
-    for (int attempt = 0;; attempt++) {
-      int64_t ns = 0, nx = 0, ne = 0;
-      for (int32_t w = w0; w < w1; w++) {  // table bases are relative to this batch
-        sbase[w] = ns; xbase[w] = nx; evbase[w] = ne;
-        ns += scap[w]; nx += xcap[w]; ne += evcap[w];
-      }
-      c->tally_max_batch_bytes = std::max(c->tally_max_batch_bytes, ns * slot_b + nx * xslot_b + ne * 16);
-      const size_t nxs = (size_t)std::max<int64_t>(nx, 1);
-      if ((s = ensure(c, c->kkeys, 8 * kw * (size_t)ns))) return s;
-      if ((s = ensure(c, c->kcnt, 16 * (size_t)ns))) return s;
-      if ((s = ensure(c, c->kqs, 32 * (size_t)ns))) return s;
-      if ((s = ensure(c, c->kmq, 4 * (size_t)ns))) return s;
-      if ((s = ensure(c, c->kq, 4 * (size_t)ns))) return s;
-      if ((s = ensure(c, c->kx_ev, 16 * (size_t)std::max<int64_t>(ne, 1)))) return s;
-      if ((s = ensure(c, c->kx_keys, 8 * xkw * nxs))) return s;
-      if ((s = ensure(c, c->kx_used, nxs))) return s;
-      if ((s = ensure(c, c->kx_cnt, 16 * nxs))) return s;
-      if ((s = ensure(c, c->kx_qs, 32 * nxs))) return s;
-      if ((s = ensure(c, c->kx_mq, 4 * nxs))) return s;
-      if ((s = ensure(c, c->kx_q, 4 * nxs))) return s;
-      const size_t nw = (size_t)(w1 - w0);
-      CK(cudaMemcpyAsync(P<int64_t>(c->kslot_base) + w0, sbase.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
-      CK(cudaMemcpyAsync(P<int64_t>(c->kslot_cap) + w0, scap.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
-      CK(cudaMemcpyAsync(P<int64_t>(c->kx_base) + w0, xbase.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
-      CK(cudaMemcpyAsync(P<int64_t>(c->kx_cap) + w0, xcap.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
-      CK(cudaMemcpyAsync(P<int64_t>(c->kx_evbase) + w0, evbase.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
-      CK(cudaMemcpyAsync(P<int64_t>(c->kx_evcap) + w0, evcap.data() + w0, 8 * nw, cudaMemcpyHostToDevice, st));
-      CK(cudaMemsetAsync(P<unsigned long long>(c->kx_evfill) + w0, 0, 8 * nw, st));
-      CK(cudaMemsetAsync(P<int32_t>(c->kwflag) + w0, 0, 4 * nw, st));
-      CK(cudaMemsetAsync(P<unsigned long long>(c->kused) + w0, 0, 8 * nw, st));
-      CK(cudaMemsetAsync(c->kkeys.p, 0xFF, 8 * kw * (size_t)ns, st));
-      CK(cudaMemsetAsync(c->kcnt.p, 0, 16 * (size_t)ns, st));
-      CK(cudaMemsetAsync(c->kqs.p, 0, 32 * (size_t)ns, st));
-      CK(cudaMemsetAsync(c->kmq.p, 0, 4 * (size_t)ns, st));
-      CK(cudaMemsetAsync(c->kq.p, 0, 4 * (size_t)ns, st));
-      CK(cudaMemsetAsync(c->kx_used.p, 0, nxs, st));
-      CK(cudaMemsetAsync(c->kx_cnt.p, 0, 16 * nxs, st));
-      CK(cudaMemsetAsync(c->kx_qs.p, 0, 32 * nxs, st));
-      CK(cudaMemsetAsync(c->kx_mq.p, 0, 4 * nxs, st));
-      CK(cudaMemsetAsync(c->kx_q.p, 0, 4 * nxs, st));
-      KmerArgs a;
-      a.R = c->R; a.windows = P<pg_window>(c->kwin); a.win_begin = w0; a.K = K; a.wide = wide;
-      a.min_qual = params->min_qual; a.default_qual = params->default_qual; a.min_depth = min_depth;
-      a.chunks = P<KmerChunk>(c->kchunks); a.n_chunks = (int32_t)chunks.size();
-      a.slot_base = P<int64_t>(c->kslot_base); a.slot_cap = P<int64_t>(c->kslot_cap);
-      a.keys = P<unsigned long long>(c->kkeys); a.cnt = P<uint32_t>(c->kcnt); a.qs = P<unsigned long long>(c->kqs);
-      a.mq_sum = P<uint32_t>(c->kmq); a.q_sum = P<uint32_t>(c->kq);
-      a.full = P<int32_t>(c->kwflag); a.used = P<unsigned long long>(c->kused);
-      a.x_base = P<int64_t>(c->kx_base); a.x_cap = P<int64_t>(c->kx_cap);
-      a.x_keys = P<unsigned long long>(c->kx_keys); a.x_used = P<uint8_t>(c->kx_used);
-      a.x_cnt = P<uint32_t>(c->kx_cnt); a.x_qs = P<unsigned long long>(c->kx_qs); a.x_mq = P<uint32_t>(c->kx_mq);
-      a.x_q = P<uint32_t>(c->kx_q);
-      a.x_ev_base = P<int64_t>(c->kx_evbase); a.x_ev_cap = P<int64_t>(c->kx_evcap);
-      a.x_ev_fill = P<unsigned long long>(c->kx_evfill); a.x_events = P<longlong2>(c->kx_ev);
-      a.edges = P<pg_kmer_edge>(c->kedges); a.wedges = P<pg_kmer_edge_wide>(c->kedges); a.edge_cap = edge_cap;
-      a.n_edges = P<unsigned long long>(c->kcount); a.overflow = (int32_t*)(P<unsigned long long>(c->kcount) + 1);
-      CK(cudaEventRecord(c->e0, st));
-      launch_kmer_count(a, w1 - w0, st);
-      CK(cudaEventRecord(c->e1, st));
-      CK(cudaGetLastError());
-      flags.assign(nw, 0);
-      CK(cudaMemcpyAsync(flags.data(), P<int32_t>(c->kwflag) + w0, 4 * nw, cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      float ms = 0;
-      CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
-      c->tally_ms += ms;
-      bool full = false;
-      for (size_t k = 0; k < nw; k++)
-        if (flags[k]) {
-          full = true;
-          scap[w0 + k] *= 4;
-        }
-      if (!full) {
-        CK(cudaEventRecord(c->e0, st));
-        launch_kmer_edges(a, w1 - w0, st);
-        CK(cudaEventRecord(c->e1, st));
-        CK(cudaGetLastError());
-        CK(cudaStreamSynchronize(st));
-        CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
-        c->tally_ms += ms;
-        break;
-      }
-      if (attempt >= 8) return fail(c, PG_ERR_LIMIT, "K-mer table overflow");
+    CK(cudaMemcpyAsync(c->kwlist.p, list.data(), 4 * list.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->kslot_base.p, sbase.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->kslot_cap.p, scap.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->kx_base.p, xbase.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->kx_cap.p, xcap.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->kx_evbase.p, evbase.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->kx_evcap.p, evcap.data(), 8 * (size_t)n_windows, cudaMemcpyHostToDevice, st));
+    a.slots = c->kslots.p;
+    a.x_keys = P<unsigned long long>(c->kx_keys); a.x_used = P<uint8_t>(c->kx_used);
+    a.x_cnt = P<uint32_t>(c->kx_cnt); a.x_qs = P<unsigned long long>(c->kx_qs); a.x_q = P<uint32_t>(c->kx_q);
+    a.x_events = P<longlong2>(c->kx_ev);
+    CK(cudaEventRecord(c->e0, st));
+    if (pass > 0) {  // the windows counted again start from zero
+      a.win_list = P<int32_t>(c->kwlist); a.n_win = (int32_t)list.size();
+      launch_kmer_reset(a, st);
     }
-    c->tally_batches++;
-    w0 = w1;
+    for (const Batch& b : batches) {
+      CK(cudaMemsetAsync(c->kslots.p, 0, (size_t)(slot_b * b.ns), st));
+      if (b.nx > 0) {
+        CK(cudaMemsetAsync(c->kx_used.p, 0, (size_t)b.nx, st));
+        CK(cudaMemsetAsync(c->kx_cnt.p, 0, 16 * (size_t)b.nx, st));
+        CK(cudaMemsetAsync(c->kx_qs.p, 0, 32 * (size_t)b.nx, st));
+        CK(cudaMemsetAsync(c->kx_q.p, 0, 4 * (size_t)b.nx, st));
+      }
+      a.win_list = P<int32_t>(c->kwlist) + b.l0; a.n_win = b.l1 - b.l0;
+      a.chunks = P<KmerChunk>(c->kchunks) + b.c0; a.n_chunks = (int32_t)(b.c1 - b.c0);
+      launch_kmer_count(a, st);
+      launch_kmer_edges(a, st);
+      c->tally_batches++;
+    }
+    CK(cudaEventRecord(c->e1, st));
+    CK(cudaGetLastError());
+    std::vector<int32_t> all(n_windows);
+    CK(cudaMemcpyAsync(all.data(), c->kwflag.p, 4 * (size_t)n_windows, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+    c->tally_ms += ms;
+    std::vector<int32_t> again;
+    for (int32_t w : list)
+      if (all[w]) {
+        again.push_back(w);
+        scap[w] *= 4;
+      }
+    list.swap(again);
   }
   unsigned long long hc[2];
   std::vector<unsigned long long> used(n_windows);

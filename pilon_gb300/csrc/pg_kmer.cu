@@ -3,16 +3,19 @@
 // (S/Assembler.scala:132-154), for many local-reassembly windows at once.
 //
 // Every window owns a power-of-two open-addressing table keyed by the 2-bit
-// packed K-mer (K <= 31, so the all-ones word marks an empty slot); the host
-// groups windows into batches of tables.  One thread walks one read (several
-// CTAs per window, each a chunk of its reads), forward strand then reverse
-// complement, and for each K-mer adds the following base into the K-mer's
-// PileUp counters with global integer atomics (count[4], qualSum[4], mqSum,
-// qSum).  A probe sequence is at most kMaxProbe slots: a longer one marks the
-// window full and the host counts it again in a table four times larger.  K-mers containing a
+// packed K-mer (KmerSlot: the key and the K-mer's PileUp counters in one
+// 64-byte line; 128-bit keys in KmerSlotWide for K <= 63).  The host groups
+// windows into batches whose tables stay in L2, so the probes and the counter
+// atomics of a batch are L2 operations.  One warp walks one read: lane l takes
+// the l-th 32nd of the strand's K-mer starts, primes its key with the K - 1
+// bases before its first start, then rolls it one base per K-mer and adds the
+// following base to the K-mer's counters with global integer atomics; forward
+// strand, then reverse complement.  A probe sequence is at most kMaxProbe
+// slots: a longer one marks the window full, its edges are not written, and
+// the host counts it again in a table four times larger.  K-mers containing a
 // base other than A/C/G/T (N, IUPAC codes, '=') cannot be 2-bit packed; they
-// are tallied exactly by k_kmer_exotic, one thread per window, in a private
-// table keyed by the 4-bit codes of the K-mer.
+// are tallied exactly by k_kmer_exotic, one warp per window, in a table keyed
+// by the 4-bit codes of the K-mer.
 #include <cuda_runtime.h>
 
 #include "pg_internal.cuh"
@@ -20,7 +23,8 @@
 
 namespace pg {
 
-constexpr unsigned long long kEmpty = ~0ull;
+constexpr unsigned long long kTop = 1ull << 63;  // set in every stored key
+constexpr unsigned FULL = 0xffffffffu;
 
 __device__ inline int code2(uint32_t nib) { return nib == 1 ? 0 : nib == 2 ? 1 : nib == 4 ? 2 : nib == 8 ? 3 : -1; }
 __device__ inline uint32_t comp_nib(uint32_t n) {  // Bases.complement: A<->T, C<->G, others unchanged
@@ -73,31 +77,71 @@ __global__ void k_kmer_prepass(Reads R, const pg_window* wins, int32_t K, long l
 }
 
 constexpr int64_t kMaxProbe = 256;
+constexpr int kKmerThreads = 128;  // 4 warps, one read each at a time
 
-// A 2-bit packed K-mer of up to 63 bases (the wide tables): bases in the low
-// 2K bits of hi:lo, so hi < 2^62 and the all-ones key marks an empty slot.
+// A 2-bit packed K-mer of up to 63 bases: bases in the low 2K bits of hi:lo.
 struct __align__(16) Key128 {
   unsigned long long lo, hi;
 };
 __device__ inline bool same_key(const Key128& a, const Key128& b) { return a.lo == b.lo && a.hi == b.hi; }
 
-// WIDE = 0: 64-bit keys (K <= 31); WIDE = 1: 128-bit keys (K <= 63), inserted
-// with the 16-byte compare-and-swap of sm_90 and later (the compare-and-swap is
-// also the probe's read, so a probe never sees half of a key).
+// The slot of a K-mer in its window's table (inserted when absent), or -1
+// when the probe sequence runs past the bound.  The narrow probe reads the key
+// first and swaps only into an empty slot; keys are never removed, so a stale
+// read can only be "empty", which the compare-and-swap corrects.  The wide
+// probe's read is the 16-byte compare-and-swap itself, so it never sees half
+// of a key.
 template <bool WIDE>
-__global__ void __launch_bounds__(64) k_kmer_count(KmerArgs a) {
+__device__ __forceinline__ int64_t kmer_slot(const KmerArgs& a, int32_t w, int64_t base, int64_t cap,
+                                             unsigned long long key, unsigned long long key_hi) {
+  int64_t h = (int64_t)((WIDE ? mix64(key ^ mix64(key_hi)) : mix64(key)) & (unsigned long long)(cap - 1));
+  const int64_t probes = cap < kMaxProbe ? cap : kMaxProbe;
+  for (int64_t probe = 0; probe < probes; probe++) {
+    const int64_t s = base + h;
+    if (WIDE) {
+      KmerSlotWide* sl = static_cast<KmerSlotWide*>(a.slots) + s;
+      const Key128 kk{key, key_hi | kTop}, empty{0ull, 0ull};
+      const Key128 prev = atomicCAS(reinterpret_cast<Key128*>(&sl->lo), empty, kk);
+      if (same_key(prev, empty)) atomicAdd(&a.used[w], 1ull);
+      if (same_key(prev, empty) || same_key(prev, kk)) return s;
+    } else {
+      KmerSlot* sl = static_cast<KmerSlot*>(a.slots) + s;
+      const unsigned long long kk = key | kTop;
+      const unsigned long long k = sl->key;
+      if (k == kk) return s;
+      if (k == 0ull) {
+        const unsigned long long prev = atomicCAS(&sl->key, 0ull, kk);
+        if (prev == 0ull) atomicAdd(&a.used[w], 1ull);
+        if (prev == 0ull || prev == kk) return s;
+      }
+    }
+    h = (h + 1) & (cap - 1);
+  }
+  return -1;
+}
+
+// WIDE = 0: 64-bit keys (K <= 31); WIDE = 1: 128-bit keys (K <= 63).  One warp
+// per read of the CTA's chunk; lane l walks K-mer starts [l S, (l + 1) S) of
+// each strand, S = ceil((L - K) / 32).
+template <bool WIDE>
+__global__ void __launch_bounds__(kKmerThreads) k_kmer_count(KmerArgs a) {
   const KmerChunk ch = a.chunks[blockIdx.x];
   const int32_t w = ch.w;
+  if (a.full[w]) return;  // the window's table is full: it is counted again, larger, after this batch
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int32_t K = a.K;
   const unsigned long long mask = (K >= 32) ? ~0ull : ((1ull << (2 * K)) - 1);
   const unsigned long long mask_hi = (K > 32) ? ((1ull << (2 * K - 64)) - 1) : 0ull;
-  Key128* const keys2 = reinterpret_cast<Key128*>(a.keys);
   const int64_t base = a.slot_base[w], cap = a.slot_cap[w];
   const int64_t xev0 = a.x_ev_base[w], xev_cap = a.x_ev_cap[w];
   const Reads& R = a.R;
-  for (int64_t i = ch.lo + threadIdx.x; i < ch.hi; i += blockDim.x) {
+  for (int64_t i = ch.lo + warp; i < ch.hi; i += nwarps) {
     const int32_t L = R.l_seq[i];
     if (L <= K) continue;
+    const int32_t nev = L - K;  // K-mer starts per strand
+    const int32_t per = (nev + 31) >> 5;
+    const int32_t o0 = lane * per, o1 = min(o0 + per, nev);
+    if (o0 >= o1) continue;
     const uint32_t mq1 = (uint32_t)R.mapq[i] + 1u;
     const uint8_t* seq = R.seq + R.seq_off[i];
     const uint8_t* qual = R.qual + R.qual_off[i];
@@ -105,53 +149,43 @@ __global__ void __launch_bounds__(64) k_kmer_count(KmerArgs a) {
     for (int strand = 0; strand < 2; strand++) {
       unsigned long long key = 0, key_hi = 0;
       int32_t lastBad = -1;
-      uint32_t nib = strand_nib(seq, L, strand, 0);
-      for (int32_t j = 0; j < L - 1; j++) {
+      // bases o0 .. o0 + K - 2, then one base per K-mer start
+      for (int32_t j = o0; j < o0 + K - 1; j++) {
+        int c = code2(strand_nib(seq, L, strand, j));
+        if (c < 0) { lastBad = j; c = 0; }
+        if (WIDE) key_hi = ((key_hi << 2) | (key >> 62)) & mask_hi;
+        key = ((key << 2) | (unsigned long long)c) & mask;
+      }
+      uint32_t nib = strand_nib(seq, L, strand, o0 + K - 1);
+      for (int32_t o = o0; o < o1; o++) {
+        const int32_t j = o + K - 1;  // last base of the K-mer at o
         int c = code2(nib);
         if (c < 0) { lastBad = j; c = 0; }
         if (WIDE) key_hi = ((key_hi << 2) | (key >> 62)) & mask_hi;
         key = ((key << 2) | (unsigned long long)c) & mask;
         const uint32_t next = strand_nib(seq, L, strand, j + 1);
-        const int32_t o = j - K + 1;
-        if (o >= 0) {
-          const int bi = code2(next);
-          const int32_t q = strand_qual(qual, L, strand, j + 1, hasQual, a.default_qual);
-          if (bi >= 0 && q >= a.min_qual) {
-            if (lastBad >= o) {
-              // a K-mer with a base other than A/C/G/T: listed for k_kmer_exotic
-              const unsigned long long k = atomicAdd(&a.x_ev_fill[w], 1ull);
-              if ((int64_t)k < xev_cap) a.x_events[xev0 + k] = make_longlong2((long long)i, ((long long)strand << 32) | (long long)o);
-              else atomicExch(a.overflow, 1);
+        const int bi = code2(next);
+        const int32_t q = strand_qual(qual, L, strand, j + 1, hasQual, a.default_qual);
+        if (bi >= 0 && q >= a.min_qual) {
+          if (lastBad >= o) {
+            // a K-mer with a base other than A/C/G/T: listed for k_kmer_exotic
+            const unsigned long long k = atomicAdd(&a.x_ev_fill[w], 1ull);
+            if ((int64_t)k < xev_cap) a.x_events[xev0 + k] = make_longlong2((long long)i, ((long long)strand << 32) | (long long)o);
+            else atomicExch(a.overflow, 1);
+          } else {
+            const int64_t slot = kmer_slot<WIDE>(a, w, base, cap, key, key_hi);
+            if (slot < 0) {
+              a.full[w] = 1;  // counted again with a larger table
+            } else if (WIDE) {
+              KmerSlotWide* sl = static_cast<KmerSlotWide*>(a.slots) + slot;
+              atomicAdd(&sl->cnt[bi], 1u);
+              atomicAdd(&sl->qs[bi], (unsigned long long)((uint32_t)q * mq1));
+              atomicAdd(&sl->q_sum, (uint32_t)q);
             } else {
-              int64_t h = (int64_t)((WIDE ? mix64(key ^ mix64(key_hi)) : mix64(key)) & (unsigned long long)(cap - 1));
-              int64_t slot = -1;
-              const int64_t probes = cap < kMaxProbe ? cap : kMaxProbe;
-              for (int64_t probe = 0; probe < probes; probe++) {
-                const int64_t s = base + h;
-                if (WIDE) {
-                  const Key128 kk{key, key_hi}, empty{kEmpty, kEmpty};
-                  const Key128 prev = atomicCAS(&keys2[s], empty, kk);
-                  if (same_key(prev, empty)) atomicAdd(&a.used[w], 1ull);
-                  if (same_key(prev, empty) || same_key(prev, kk)) { slot = s; break; }
-                } else {
-                  unsigned long long k = a.keys[s];
-                  if (k == key) { slot = s; break; }
-                  if (k == kEmpty) {
-                    unsigned long long prev = atomicCAS(&a.keys[s], kEmpty, key);
-                    if (prev == kEmpty) atomicAdd(&a.used[w], 1ull);
-                    if (prev == kEmpty || prev == key) { slot = s; break; }
-                  }
-                }
-                h = (h + 1) & (cap - 1);
-              }
-              if (slot < 0) {
-                a.full[w] = 1;  // counted again with a larger table
-              } else {
-                atomicAdd(&a.cnt[4 * slot + bi], 1u);
-                atomicAdd(&a.qs[4 * slot + bi], (unsigned long long)((uint32_t)q * mq1));
-                atomicAdd(&a.mq_sum[slot], mq1);
-                atomicAdd(&a.q_sum[slot], (uint32_t)q);
-              }
+              KmerSlot* sl = static_cast<KmerSlot*>(a.slots) + slot;
+              atomicAdd(&sl->cnt[bi], 1u);
+              atomicAdd(&sl->qs[bi], (unsigned long long)((uint32_t)q * mq1));
+              atomicAdd(&sl->q_sum, (uint32_t)q);
             }
           }
         }
@@ -197,9 +231,9 @@ __device__ inline void store_edge(const KmerArgs& a, unsigned long long k, const
 }
 
 template <bool WIDE>
-__global__ void k_kmer_edges(KmerArgs a) {
-  const int32_t w = a.win_begin + blockIdx.x;
-  const Key128* const keys2 = reinterpret_cast<const Key128*>(a.keys);
+__global__ void __launch_bounds__(256) k_kmer_edges(KmerArgs a) {
+  const int32_t w = a.win_list[blockIdx.x];
+  if (a.full[w]) return;
   const int64_t base = a.slot_base[w], cap = a.slot_cap[w];
   const int32_t K = a.K;
   const int lane = threadIdx.x & 31;
@@ -208,23 +242,28 @@ __global__ void k_kmer_edges(KmerArgs a) {
     const int64_t s = s0 + threadIdx.x;
     bool emit = false;
     uint32_t cnt[4] = {0, 0, 0, 0};
-    unsigned long long key = kEmpty, key_hi = kEmpty;
+    unsigned long long key = 0, key_hi = 0;
     int32_t depth = 0;
     int b0 = 0, alt = -1;
     if (s < base + cap) {
+      unsigned long long qs[4];
+      uint32_t q_sum;
+      bool used;
       if (WIDE) {
-        const Key128 k2 = keys2[s];
-        key = k2.lo;
-        key_hi = k2.hi;
+        const KmerSlotWide& sl = static_cast<const KmerSlotWide*>(a.slots)[s];
+        key = sl.lo; key_hi = sl.hi & ~kTop; used = sl.hi != 0ull;
+        for (int b = 0; b < 4; b++) { cnt[b] = sl.cnt[b]; qs[b] = sl.qs[b]; }
+        q_sum = sl.q_sum;
       } else {
-        key = a.keys[s];
+        const KmerSlot& sl = static_cast<const KmerSlot*>(a.slots)[s];
+        key = sl.key & ~kTop; used = sl.key != 0ull;
+        for (int b = 0; b < 4; b++) { cnt[b] = sl.cnt[b]; qs[b] = sl.qs[b]; }
+        q_sum = sl.q_sum;
       }
-      if (key != kEmpty || key_hi != kEmpty) {
-        unsigned long long qs[4];
-        for (int b = 0; b < 4; b++) { cnt[b] = a.cnt[4 * s + b]; qs[b] = a.qs[4 * s + b]; }
+      if (used) {
         depth = (int32_t)(cnt[0] + cnt[1] + cnt[2] + cnt[3]);
         if (depth >= a.min_depth) {
-          kmer_call(cnt, qs, a.q_sum[s], b0, alt);
+          kmer_call(cnt, qs, q_sum, b0, alt);
           emit = true;
         }
       }
@@ -248,78 +287,148 @@ __global__ void k_kmer_edges(KmerArgs a) {
   }
 }
 
-// Exotic K-mers: one thread per window over the window's listed events, in a
-// private table keyed by 4-bit codes.
+// Exotic K-mers: one warp per window over the window's listed events, 32 at a
+// time, in the window's table keyed by 4-bit codes.  The warp owns the table,
+// so it inserts without atomics or waits: the lanes look their keys up, the
+// lanes whose key is absent group by key (__match_any_sync on every key word),
+// and the groups' first lanes insert one after another in lane order, each
+// from its hash slot to the next free one (keys inserted meanwhile differ from
+// it).  Every lane then adds its next base to its key's counters with global
+// atomics (the lanes of one key add to one slot).  Last, the warp reads the
+// table 32 slots at a time and writes the edges.
+constexpr int kExoticThreads = 128;
+
 template <bool WIDE>
-__global__ void k_kmer_exotic(KmerArgs a, int32_t n_win) {
+__global__ void __launch_bounds__(kExoticThreads) k_kmer_exotic(KmerArgs a, int32_t n_win) {
   constexpr int NW = WIDE ? 4 : 2;  // key words per slot
-  const int32_t wl = blockIdx.x * blockDim.x + threadIdx.x;
-  if (wl >= n_win) return;
-  const int32_t w = a.win_begin + wl;
+  const int lane = threadIdx.x & 31;
+  const int32_t wl = (int32_t)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  if (wl >= n_win) return;  // the whole warp leaves
+  const int32_t w = a.win_list[wl];
   const int64_t base = a.x_base[w], cap = a.x_cap[w];
-  if (cap == 0) return;
+  if (cap == 0 || a.full[w]) return;  // a full window is counted again, exotic K-mers included
   const int32_t K = a.K;
   const Reads& R = a.R;
   const int64_t nev = min((int64_t)a.x_ev_fill[w], a.x_ev_cap[w]);
-  for (int64_t k = 0; k < nev; k++) {
-    const longlong2 ev = a.x_events[a.x_ev_base[w] + k];
-    const int64_t i = ev.x;
-    const int strand = (int)(ev.y >> 32);
-    const int32_t o = (int32_t)(ev.y & 0xffffffffll);
-    const int32_t L = R.l_seq[i];
-    const uint32_t mq1 = (uint32_t)R.mapq[i] + 1u;
-    const uint8_t* seq = R.seq + R.seq_off[i];
-    const uint8_t* qual = R.qual + R.qual_off[i];
-    const bool hasQual = qual[0] != 0xFF;
-    const int bi = code2(strand_nib(seq, L, strand, o + K));
-    const int32_t q = strand_qual(qual, L, strand, o + K, hasQual, a.default_qual);
+  const int64_t ev0 = a.x_ev_base[w];
+  for (int64_t k0 = 0; k0 < nev; k0 += 32) {
+    const int64_t k = k0 + lane;
+    const bool have = k < nev;
     unsigned long long kw[NW];
 #pragma unroll
     for (int q = 0; q < NW; q++) kw[q] = 0;
-    for (int32_t t = 0; t < K; t++) {
-      const unsigned long long nb = strand_nib(seq, L, strand, o + t);
-      kw[t >> 4] |= nb << (60 - 4 * (t & 15));
-    }
-    unsigned long long hv = 0;
-#pragma unroll
-    for (int q = 0; q < NW; q++) hv = mix64(hv ^ kw[q]);
-    int64_t h = (int64_t)(hv & (unsigned long long)(cap - 1));
-    int64_t slot = -1;
-    for (int64_t probe = 0; probe < cap; probe++) {
-      const int64_t s = base + h;
-      bool same = a.x_used[s] != 0;
-#pragma unroll
-      for (int q = 0; q < NW; q++) same = same && a.x_keys[NW * s + q] == kw[q];
-      if (same) { slot = s; break; }
-      if (!a.x_used[s]) {
-        a.x_used[s] = 1;
-#pragma unroll
-        for (int q = 0; q < NW; q++) a.x_keys[NW * s + q] = kw[q];
-        slot = s;
-        break;
+    int bi = 0;
+    int32_t qv = 0;
+    uint32_t mq1 = 0;
+    int64_t h = 0;
+    if (have) {
+      const longlong2 ev = a.x_events[ev0 + k];
+      const int64_t i = ev.x;
+      const int strand = (int)(ev.y >> 32);
+      const int32_t o = (int32_t)(ev.y & 0xffffffffll);
+      const int32_t L = R.l_seq[i];
+      mq1 = (uint32_t)R.mapq[i] + 1u;
+      const uint8_t* seq = R.seq + R.seq_off[i];
+      const uint8_t* qual = R.qual + R.qual_off[i];
+      const bool hasQual = qual[0] != 0xFF;
+      bi = code2(strand_nib(seq, L, strand, o + K));
+      qv = strand_qual(qual, L, strand, o + K, hasQual, a.default_qual);
+      for (int32_t t = 0; t < K; t++) {
+        const unsigned long long nb = strand_nib(seq, L, strand, o + t);
+        kw[t >> 4] |= nb << (60 - 4 * (t & 15));
       }
-      h = (h + 1) & (cap - 1);
-    }
-    if (slot < 0) { atomicExch(a.overflow, 1); continue; }
-    a.x_cnt[4 * slot + bi] += 1u;
-    a.x_qs[4 * slot + bi] += (unsigned long long)((uint32_t)q * mq1);
-    a.x_mq[slot] += mq1;
-    a.x_q[slot] += (uint32_t)q;
-  }
-  for (int64_t s = base; s < base + cap; s++) {
-    if (!a.x_used[s]) continue;
-    uint32_t cnt[4];
-    unsigned long long qs[4];
-    for (int b = 0; b < 4; b++) { cnt[b] = a.x_cnt[4 * s + b]; qs[b] = a.x_qs[4 * s + b]; }
-    const int32_t depth = (int32_t)(cnt[0] + cnt[1] + cnt[2] + cnt[3]);
-    if (depth < a.min_depth) continue;
-    int b0, alt;
-    kmer_call(cnt, qs, a.x_q[s], b0, alt);
-    unsigned long long key4[4] = {0, 0, 0, 0};
+      unsigned long long hv = 0;
 #pragma unroll
-    for (int q = 0; q < NW; q++) key4[q] = a.x_keys[NW * s + q];
-    store_edge(a, atomicAdd(a.n_edges, 1ull), key4, w, b0, alt, depth,
-               (int32_t)(b0 == 0 ? cnt[0] : b0 == 1 ? cnt[1] : b0 == 2 ? cnt[2] : cnt[3]));
+      for (int q = 0; q < NW; q++) hv = mix64(hv ^ kw[q]);
+      h = (int64_t)(hv & (unsigned long long)(cap - 1));
+    }
+    // look-up: the key's slot, or absent when the probe meets a free slot first
+    int64_t slot = -1;
+    bool absent = false;
+    if (have) {
+      int64_t hh = h;
+      for (int64_t probe = 0; probe < cap; probe++) {
+        const int64_t sl = base + hh;
+        if (!a.x_used[sl]) { absent = true; break; }
+        bool same = true;
+#pragma unroll
+        for (int q = 0; q < NW; q++) same = same && a.x_keys[NW * sl + q] == kw[q];
+        if (same) { slot = sl; break; }
+        hh = (hh + 1) & (cap - 1);
+      }
+    }
+    const unsigned need = __ballot_sync(FULL, absent);
+    if (need) {
+      unsigned grp = FULL;
+#pragma unroll
+      for (int q = 0; q < NW; q++) grp &= __match_any_sync(FULL, kw[q]);
+      grp &= need;  // for an absent lane: the absent lanes with its key, itself included
+      const int first = absent ? __ffs(grp) - 1 : lane;
+      unsigned leaders = __ballot_sync(FULL, absent && first == lane);
+      while (leaders) {
+        const int l = __ffs(leaders) - 1;
+        if (lane == l) {
+          int64_t hh = h;
+          for (int64_t probe = 0; probe < cap; probe++) {
+            const int64_t sl = base + hh;
+            if (!a.x_used[sl]) {
+              a.x_used[sl] = 1;
+#pragma unroll
+              for (int q = 0; q < NW; q++) a.x_keys[NW * sl + q] = kw[q];
+              slot = sl;
+              break;
+            }
+            hh = (hh + 1) & (cap - 1);
+          }
+        }
+        __syncwarp();  // the inserted key is seen by the next leader's probe
+        leaders &= leaders - 1;
+      }
+      const long long ls = __shfl_sync(FULL, (long long)slot, first);
+      if (absent) slot = ls;
+    }
+    if (have) {
+      if (slot < 0) {
+        atomicExch(a.overflow, 1);
+      } else {
+        atomicAdd(&a.x_cnt[4 * slot + bi], 1u);
+        atomicAdd(&a.x_qs[4 * slot + bi], (unsigned long long)((uint32_t)qv * mq1));
+        atomicAdd(&a.x_q[slot], (uint32_t)qv);
+      }
+    }
+    __syncwarp();
+  }
+  __threadfence();
+  __syncwarp();
+  // edges of the window's exotic K-mers, 32 slots at a time
+  for (int64_t s0 = base; s0 < base + cap; s0 += 32) {
+    const int64_t sl = s0 + lane;
+    bool emit = false;
+    uint32_t cnt[4] = {0, 0, 0, 0};
+    int32_t depth = 0;
+    int b0 = 0, alt = -1;
+    if (sl < base + cap && a.x_used[sl]) {
+      // the counters were added by atomics of this kernel: read them from L2
+      unsigned long long qs[4];
+      for (int b = 0; b < 4; b++) { cnt[b] = __ldcg(&a.x_cnt[4 * sl + b]); qs[b] = __ldcg(&a.x_qs[4 * sl + b]); }
+      depth = (int32_t)(cnt[0] + cnt[1] + cnt[2] + cnt[3]);
+      if (depth >= a.min_depth) {
+        kmer_call(cnt, qs, __ldcg(&a.x_q[sl]), b0, alt);
+        emit = true;
+      }
+    }
+    const unsigned m = __ballot_sync(FULL, emit);
+    if (!m) continue;
+    unsigned long long e0 = 0;
+    if (lane == __ffs(m) - 1) e0 = atomicAdd(a.n_edges, (unsigned long long)__popc(m));
+    e0 = __shfl_sync(FULL, e0, __ffs(m) - 1);
+    if (emit) {
+      unsigned long long key4[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int q = 0; q < NW; q++) key4[q] = a.x_keys[NW * sl + q];
+      store_edge(a, e0 + __popc(m & ((1u << lane) - 1u)), key4, w, b0, alt, depth,
+                 (int32_t)(b0 == 0 ? cnt[0] : b0 == 1 ? cnt[1] : b0 == 2 ? cnt[2] : cnt[3]));
+    }
   }
 }
 
@@ -329,21 +438,36 @@ void launch_kmer_prepass(const Reads& R, const pg_window* wins, int32_t n, int32
   k_kmer_prepass<<<n, 256, 0, s>>>(R, wins, K, out);
 }
 
-void launch_kmer_count(const KmerArgs& a, int32_t n_win, cudaStream_t s) {
-  if (n_win <= 0) return;
+__global__ void k_kmer_reset(KmerArgs a) {
+  const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.n_win) return;
+  const int32_t w = a.win_list[k];
+  a.full[w] = 0;
+  a.used[w] = 0;
+  a.x_ev_fill[w] = 0;
+}
+
+void launch_kmer_reset(const KmerArgs& a, cudaStream_t s) {
+  if (a.n_win <= 0) return;
+  k_kmer_reset<<<(a.n_win + 127) / 128, 128, 0, s>>>(a);
+}
+
+void launch_kmer_count(const KmerArgs& a, cudaStream_t s) {
+  if (a.n_win <= 0) return;
+  const int32_t xg = (a.n_win * 32 + kExoticThreads - 1) / kExoticThreads;
   if (a.wide) {
-    if (a.n_chunks > 0) k_kmer_count<true><<<a.n_chunks, 64, 0, s>>>(a);
-    k_kmer_exotic<true><<<(n_win + 63) / 64, 64, 0, s>>>(a, n_win);
+    if (a.n_chunks > 0) k_kmer_count<true><<<a.n_chunks, kKmerThreads, 0, s>>>(a);
+    k_kmer_exotic<true><<<xg, kExoticThreads, 0, s>>>(a, a.n_win);
   } else {
-    if (a.n_chunks > 0) k_kmer_count<false><<<a.n_chunks, 64, 0, s>>>(a);
-    k_kmer_exotic<false><<<(n_win + 63) / 64, 64, 0, s>>>(a, n_win);
+    if (a.n_chunks > 0) k_kmer_count<false><<<a.n_chunks, kKmerThreads, 0, s>>>(a);
+    k_kmer_exotic<false><<<xg, kExoticThreads, 0, s>>>(a, a.n_win);
   }
 }
 
-void launch_kmer_edges(const KmerArgs& a, int32_t n_win, cudaStream_t s) {
-  if (n_win <= 0) return;
-  if (a.wide) k_kmer_edges<true><<<n_win, 256, 0, s>>>(a);
-  else k_kmer_edges<false><<<n_win, 256, 0, s>>>(a);
+void launch_kmer_edges(const KmerArgs& a, cudaStream_t s) {
+  if (a.n_win <= 0) return;
+  if (a.wide) k_kmer_edges<true><<<a.n_win, 256, 0, s>>>(a);
+  else k_kmer_edges<false><<<a.n_win, 256, 0, s>>>(a);
 }
 
 }  // namespace pg

@@ -219,3 +219,30 @@ def test_kmer_tally_wide_exotic_kmers(engine, cfg1):
     want = oracle.kmer_tally_wide(r2, p, wins, 47, min_depth=2)
     assert wide_edge_set(got) == wide_edge_set(want)
     assert any("f" in "".join(format(int(e[f"key{q}"]), "016x") for q in range(3)) for e in want)
+
+
+def test_kmer_tally_full_tables_counted_again(engine, cfg1):
+    """Windows whose reads share no K-mers fill tables sized at a quarter of
+    their K-mer events: they write no edges in the first pass and are counted
+    again in larger tables after the other windows, and every window's edges
+    equal the oracle's."""
+    ds = cfg1
+    r = ds.reads
+    assert np.all(np.diff(r.seq_off[:1501]) > 0)
+    seq = r.seq.copy()
+    rng = np.random.Generator(np.random.PCG64(11))
+    codes = np.array([1, 2, 4, 8], np.uint8)
+    lo, hi = int(r.seq_off[0]), int(r.seq_off[1500])
+    seq[lo:hi] = (codes[rng.integers(0, 4, hi - lo)] << 4) | codes[rng.integers(0, 4, hi - lo)]
+    r2 = r.subset(np.arange(r.n_reads))
+    r2.seq = seq
+    engine.set_reference(ds.contigs)
+    engine.set_reads(r2)
+    p = _abi.default_params()
+    wins = [(0, 1500), (1500, 3000), (100, 1400)]
+    got = engine.kmer_tally(wins, 25, p, min_depth=1)
+    want = oracle.kmer_tally(r2, p, wins, 25, min_depth=1)
+    assert edge_set(got) == edge_set(want)
+    _, _, distinct, _, batches = engine.last_tally_stats()
+    assert batches >= 2  # the first pass, then the full windows again
+    assert distinct > 300_000
