@@ -53,7 +53,7 @@ struct pg_ctx {
   DevBuf ent_off, ent_sums, entries;  // walk entries of the read store
   int64_t n_entries = 0;
   // per-call buffers
-  DevBuf regions, walk_tiles, call_tile_region, chunks, stats;
+  DevBuf regions, walk_tiles, call_tile_region, call_desc, chunks, stats;
   DevBuf rec_count, rec_qsum, rec_i32[10], rec_call, rec_score, rec_indel_len, rec_ins_str, rec_ev_end;
   DevBuf cand_count, cand_off, tile_sums;
   DevBuf events, events_sorted, cands, pool, counters, run_max, chunk_stats, spool, indel_list;
@@ -258,7 +258,7 @@ void pg_close(pg_ctx* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
   }
-  DevBuf* all[] = {&c->ref, &c->d_ext, &c->rdesc, &c->ent_off, &c->ent_sums, &c->entries, &c->regions, &c->walk_tiles, &c->call_tile_region, &c->chunks, &c->stats,
+  DevBuf* all[] = {&c->ref, &c->d_ext, &c->rdesc, &c->ent_off, &c->ent_sums, &c->entries, &c->regions, &c->walk_tiles, &c->call_tile_region, &c->call_desc, &c->chunks, &c->stats,
                    &c->rec_count, &c->rec_qsum, &c->rec_call, &c->rec_score, &c->rec_indel_len, &c->rec_ins_str,
                    &c->rec_ev_end, &c->cand_count, &c->cand_off, &c->tile_sums,
                    &c->events, &c->events_sorted, &c->cands, &c->pool, &c->counters, &c->run_max, &c->staging_dev,
@@ -345,7 +345,8 @@ pg_status pg_set_reference(pg_ctx* c, int32_t n, const int64_t* lens, const uint
     c->ref_off[i] = total;
     total += lens[i];
   }
-  pg_status s = ensure(c, c->ref, (size_t)std::max<int64_t>(total, 1));
+  // 16 bytes of slack: k_call stages the aligned word that holds a reference byte
+  pg_status s = ensure(c, c->ref, (size_t)std::max<int64_t>(total, 1) + 16);
   if (s) return s;
   for (int i = 0; i < n; i++)
     if (lens[i] > 0)
@@ -519,6 +520,7 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
 
   CallArgs ca;
   ca.R = c->R; ca.regions = d_regions; ca.call_tile_region = P<int32_t>(c->call_tile_region);
+  ca.call_desc = P<CallDesc>(c->call_desc);
   ca.n_call_tiles = tn; ca.rec = rec; ca.stats = d_stats; ca.P = dp; ca.ref = P<uint8_t>(c->ref);
   ca.ev_sorted = P<Event>(c->events_sorted);
   ca.event_cap = c->event_cap;
@@ -532,9 +534,9 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   launch_apply_spans(ca, P<Cand>(c->cands), P<int32_t>(c->cand_off) + t0 + tn, c->cand_cap, s);
   k_track<<<1, 1, 0, s>>>(counters, P<int32_t>(c->cand_off) + t0 + tn, P<unsigned long long>(c->run_max));
   // kernels of this run: tile ranges + walk, read events, region prep, three
-  // scan phases, event scatter, call, candidate scan, candidate list,
-  // resolve, span update, overflow tracking
-  c->launches += 2 * (wn > 0) + (chn > 0) + 1 + 3 * (tn > 0) + 1 + 2 * (tn > 0) + 1 + 1 + 1 + 1;
+  // scan phases, event scatter, call descriptors, call, candidate scan,
+  // candidate list, resolve, span update, overflow tracking
+  c->launches += 2 * (wn > 0) + (chn > 0) + 1 + 3 * (tn > 0) + 1 + 3 * (tn > 0) + 1 + 1 + 1 + 1;
 }
 
 pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions, const pg_params* params,
@@ -598,6 +600,7 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
   EN(c->stats, sizeof(StatsDev) * n_regions);
   EN(c->walk_tiles, sizeof(WalkTile) * std::max<size_t>(plan.walk.size(), 1));
   EN(c->call_tile_region, sizeof(int32_t) * (n_call + 1));
+  EN(c->call_desc, sizeof(CallDesc) * (n_call + 1));
   EN(c->chunks, sizeof(ReadChunk) * std::max<size_t>(plan.chunks.size(), 1));
   EN(c->chunk_stats, sizeof(ChunkStats) * std::max<size_t>(plan.chunks.size(), 1));
   EN(c->indel_list, sizeof(int64_t) * kReadsPerChunk * std::max<size_t>(plan.chunks.size(), 1));

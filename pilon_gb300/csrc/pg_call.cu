@@ -21,7 +21,7 @@ namespace pg {
 #define FULL 0xffffffffu
 
 // n_ev = insertions + deletions of the position before any deletion-span update
-__device__ inline CallCtx make_ctx(const CallArgs& a, const RegionDev& g, int64_t gp, int32_t n_ev) {
+__device__ inline CallCtx make_ctx(const CallArgs& a, int64_t ref_off, int64_t contig_len, int64_t gp, int32_t n_ev) {
   CallCtx c;
   c.ev = a.ev_sorted;
   c.ev_lo = c.ev_hi = 0;
@@ -32,33 +32,32 @@ __device__ inline CallCtx make_ctx(const CallArgs& a, const RegionDev& g, int64_
   }
   c.spool = a.spool;
   c.ref = a.ref;
-  c.ref_off = g.ref_off;
-  c.contig_len = g.contig_len;
+  c.ref_off = ref_off;
+  c.contig_len = contig_len;
   c.pool = a.pool;
   c.pool_fill = a.pool_fill;
   c.pool_cap = a.pool_cap;
   return c;
 }
 
-// BaseCall and the pass-1 disposition of position p of region r (global
-// position gp) from its loaded record; writes the call record and returns the
-// change kind (0: none).
-__device__ __forceinline__ uint32_t call_position(const CallArgs& a, const RegionDev& g, int32_t p, int64_t gp,
-                                                  const PosRec& rec, bool reads, int32_t min_depth) {
+// BaseCall and the pass-1 disposition of position p of the tile's region
+// (global position gp) from its record and its reference base rb; writes the
+// call record and returns the change kind (0: none).
+__device__ __forceinline__ uint32_t call_position(const CallArgs& a, const CallDesc& d, int32_t p, int64_t gp,
+                                                  const PosRec& rec, uint8_t rb) {
   uint32_t change = 0;
-  CallCtx c = make_ctx(a, g, gp, wadd(rec.insertions, rec.deletions));
-  const int64_t locus0 = (int64_t)g.start - 1 + p;
+  CallCtx c = make_ctx(a, d.ref_off, d.contig_len, gp, wadd(rec.insertions, rec.deletions));
+  const int64_t locus0 = (int64_t)d.start - 1 + p;
   CallOut o = base_call(rec, a.P, c, gp, locus0);
   int32_t ins = -1;
   if (o.flags & PG_CALL_INS) ins = pool_insertion(c, c.ev[o.win_event]);
   uint32_t f = o.flags;
-  if (reads) {
+  if (d.reads) {
     const int64_t n = rec.cnt[0] + rec.cnt[1] + rec.cnt[2] + rec.cnt[3];
     const int64_t depth = n + rec.deletions;
-    const uint8_t rb = upper(a.ref[g.ref_off + locus0]);
     const bool isIns = f & PG_CALL_INS, isDel = f & PG_CALL_DEL;
     const bool called = (f & PG_CALL_HAS_BASE) || isIns || isDel;
-    if (depth >= min_depth && rb != 'N' && called) {
+    if (depth >= d.min_depth && rb != 'N' && called) {
       // 'A','C','G','T' are the bytes of 0x54474341
       const uint8_t b = (f & PG_CALL_HAS_BASE) ? (uint8_t)(0x54474341u >> (8 * (f & 3u))) : (uint8_t)'N';
       const uint8_t alt = (uint8_t)(0x54474341u >> (8 * ((f >> 2) & 3u)));
@@ -82,41 +81,139 @@ __device__ __forceinline__ uint32_t call_position(const CallArgs& a, const Regio
   return change;
 }
 
-// 256 threads per CTA, one position per thread, four CTAs per call tile: a
-// thread that runs a long indel vote holds back only its own small CTA.  (Two
-// positions per thread, both records loaded before either call, needed 80
-// registers, fell to 3 CTAs per SM and made the kernel 1.5x slower.)
-constexpr int kCallThreads = 256;
-constexpr int kCallPer = 1;
-constexpr int kCallCtas = kCallTile / (kCallThreads * kCallPer);
-static_assert(kCallCtas * kCallThreads * kCallPer == kCallTile, "call tile split");
-
-__global__ void __launch_bounds__(kCallThreads, 6) k_call(CallArgs a, int32_t tile_begin) {
-  const int32_t t = tile_begin + blockIdx.x / kCallCtas;
+// One thread per call tile: the tile's descriptor (after k_region_prep).
+__global__ void k_call_desc(CallArgs a, int32_t tile_begin) {
+  const int32_t t = tile_begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tile_begin + a.n_call_tiles) return;
   const int32_t r = a.call_tile_region[t];
-  const RegionDev g = a.regions[r];
-  const int32_t p0 = (t - g.call_tile0) * kCallTile + (blockIdx.x % kCallCtas) * (kCallThreads * kCallPer) +
-                     threadIdx.x;
+  const RegionDev& g = a.regions[r];
   const StatsDev& st = a.stats[r];
-  const bool reads = st.read_count > 0;
-  const int32_t min_depth = st.min_depth;
-  PosRec rec[kCallPer];
-#pragma unroll
-  for (int k = 0; k < kCallPer; k++)
-    if (p0 + k * kCallThreads < g.size) load_rec(a.rec, g.pos_base + p0 + k * kCallThreads, rec[k]);
-  uint32_t changes = 0;
-#pragma unroll
-  for (int k = 0; k < kCallPer; k++) {
-    const int32_t p = p0 + k * kCallThreads;
-    if (p < g.size) changes += call_position(a, g, p, g.pos_base + p, rec[k], reads, min_depth) != 0;
+  CallDesc d;
+  d.p0 = (t - g.call_tile0) * kCallTile;
+  d.gp0 = g.pos_base + d.p0;
+  d.ref_off = g.ref_off;
+  d.contig_len = g.contig_len;
+  d.start = g.start;
+  d.n = min(g.size - d.p0, kCallTile);
+  d.min_depth = st.min_depth;
+  d.reads = st.read_count > 0;
+  d.pad = 0;
+  a.call_desc[t] = d;
+}
+
+// k_call: persistent CTAs over units of kCallThreads positions (a quarter of
+// a call tile); unit u of the launch is quarter u % kCallUnits of tile
+// tile_begin + u / kCallUnits, and a CTA takes units blockIdx.x, + gridDim.x,
+// ...  Each thread owns one position of a unit and its slots in two shared
+// buffers: while it calls its position of one unit, its position's record in
+// the CTA's next unit is on its way into the other buffer by cp.async (the
+// 16-byte base counts, the 32-byte quality sums, six 4-byte counters and the
+// aligned word that holds the reference base: 76 bytes), so the record loads
+// of the next unit overlap the calls of this one.  A thread reads only the
+// slots it filled, so no barrier is needed.
+constexpr int kCallThreads = 256;
+constexpr int kCallUnits = kCallTile / kCallThreads;
+static_assert(kCallUnits * kCallThreads == kCallTile, "call tile split");
+
+struct CallStage {
+  int4 cnt[kCallThreads];
+  longlong2 qs0[kCallThreads], qs1[kCallThreads];
+  int32_t f[6][kCallThreads];  // mq_sum, q_sum, deletions, del_qual, insertions, ins_qual
+  uint32_t ref[kCallThreads];  // the aligned reference word holding the position's base
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// Queues the copies of position i of unit (tile t, quarter q) into stage buffer b.
+__device__ __forceinline__ void stage_position(const CallArgs& a, const CallDesc& d, int32_t q, CallStage& b, int i) {
+  const int32_t k = q * kCallThreads + i;  // index in the tile
+  if (k >= d.n) return;
+  const int64_t gp = d.gp0 + k;
+  const Records& R = a.rec;
+  cp_async16(&b.cnt[i], &R.count[gp]);
+  cp_async16(&b.qs0[i], &R.qual_sum[2 * gp]);
+  cp_async16(&b.qs1[i], &R.qual_sum[2 * gp + 1]);
+  cp_async4(&b.f[0][i], &R.mq_sum[gp]);
+  cp_async4(&b.f[1][i], &R.q_sum[gp]);
+  cp_async4(&b.f[2][i], &R.deletions[gp]);
+  cp_async4(&b.f[3][i], &R.del_qual[gp]);
+  cp_async4(&b.f[4][i], &R.insertions[gp]);
+  cp_async4(&b.f[5][i], &R.ins_qual[gp]);
+  // locus0 = start - 1 + p; the reference buffer has 16 bytes of slack after its end
+  const uintptr_t ra = (uintptr_t)(a.ref + d.ref_off + (int64_t)d.start - 1 + d.p0 + k);
+  cp_async4(&b.ref[i], (const void*)(ra & ~(uintptr_t)3));
+}
+
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
+}
+
+// The descriptors are read where they are used (from L1: the one two units
+// ahead is prefetched each iteration) rather than carried in registers.
+__global__ void __launch_bounds__(kCallThreads, 4) k_call(CallArgs a, int32_t tile_begin) {
+  __shared__ CallStage stage[2];
+  const int i = threadIdx.x;
+  const int32_t n_units = a.n_call_tiles * kCallUnits;
+  const int32_t G = gridDim.x;
+  const CallDesc* desc = a.call_desc + tile_begin;
+  int32_t u = blockIdx.x;
+  if (u >= n_units) return;
+  if (u + G < n_units) prefetch_l1(&desc[(u + G) / kCallUnits]);
+  stage_position(a, desc[u / kCallUnits], u % kCallUnits, stage[0], i);
+  cp_async_commit();
+  for (int k = 0; u < n_units; k++, u += G) {
+    const int32_t u1 = u + G, u2 = u + 2 * G;
+    if (u2 < n_units) {
+      const char* pd = reinterpret_cast<const char*>(&desc[u2 / kCallUnits]);
+      prefetch_l1(pd);
+      prefetch_l1(pd + sizeof(CallDesc) - 1);
+    }
+    if (u1 < n_units) stage_position(a, desc[u1 / kCallUnits], u1 % kCallUnits, stage[(k + 1) & 1], i);
+    cp_async_commit();
+    cp_async_wait_prev();  // this unit's copies are in
+    const CallStage& b = stage[k & 1];
+    const CallDesc d = desc[u / kCallUnits];
+    const int32_t kk = (u % kCallUnits) * kCallThreads + i;
+    uint32_t changes = 0;
+    if (kk < d.n) {
+      PosRec rec;
+      const int4 c = b.cnt[i];
+      rec.cnt[0] = c.x; rec.cnt[1] = c.y; rec.cnt[2] = c.z; rec.cnt[3] = c.w;
+      const longlong2 q0 = b.qs0[i], q1 = b.qs1[i];
+      rec.qs[0] = q0.x; rec.qs[1] = q0.y; rec.qs[2] = q1.x; rec.qs[3] = q1.y;
+      rec.mq_sum = b.f[0][i]; rec.q_sum = b.f[1][i];
+      rec.deletions = b.f[2][i]; rec.del_qual = b.f[3][i];
+      rec.insertions = b.f[4][i]; rec.ins_qual = b.f[5][i];
+      const uintptr_t ra = (uintptr_t)(a.ref + d.ref_off + (int64_t)d.start - 1 + d.p0 + kk);
+      const uint8_t rb = upper((uint8_t)(b.ref[i] >> (8 * (ra & 3u))));
+      changes = call_position(a, d, d.p0 + kk, d.gp0 + kk, rec, rb) != 0;
+    }
+    changes = __reduce_add_sync(FULL, changes);
+    if ((i & 31) == 0 && changes) atomicAdd(&a.cand_count[tile_begin + u / kCallUnits], (int32_t)changes);
   }
-  changes = __reduce_add_sync(FULL, changes);
-  if ((threadIdx.x & 31) == 0 && changes) atomicAdd(&a.cand_count[t], (int32_t)changes);
 }
 
 void launch_call(const CallArgs& a, int32_t tile_begin, int32_t n_tiles, cudaStream_t s) {
   if (n_tiles <= 0) return;
-  k_call<<<n_tiles * kCallCtas, kCallThreads, 0, s>>>(a, tile_begin);
+  k_call_desc<<<(n_tiles + 255) / 256, 256, 0, s>>>(a, tile_begin);
+  static int grid_max = 0;
+  if (grid_max == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_call, kCallThreads, 0);
+    grid_max = std::max(1, sms * std::max(per_sm, 1));
+  }
+  const int64_t units = (int64_t)n_tiles * kCallUnits;
+  k_call<<<(int)std::min<int64_t>(units, grid_max), kCallThreads, 0, s>>>(a, tile_begin);
 }
 
 // The change candidates of a call tile in position order, at the tile's offset
@@ -313,7 +410,7 @@ __global__ void k_apply_spans(CallArgs a, const Cand* cands, const int32_t* cand
       a.rec.deletions[gp] = wadd(del0, d);
       PosRec rec;
       load_rec(a.rec, gp, rec);
-      CallCtx cx = make_ctx(a, g, gp, wadd(rec.insertions, del0));
+      CallCtx cx = make_ctx(a, g.ref_off, g.contig_len, gp, wadd(rec.insertions, del0));
       CallOut o = base_call(rec, a.P, cx, gp, (int64_t)g.start - 1 + p);
       const uint32_t old = a.rec.call[gp];
       if (PG_CALL_CHANGE(old)) removed++;

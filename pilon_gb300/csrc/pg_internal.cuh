@@ -398,10 +398,27 @@ struct EventArgs {
   int64_t* indel_list;             // per chunk kReadsPerChunk slots: its reads with I/D
 };
 
+// Per call tile, written by k_call_desc once the region statistics exist:
+// what k_call needs of the tile's region, so that a unit of the call needs one
+// descriptor load instead of the tile -> region -> statistics chain.
+struct __align__(16) CallDesc {
+  int64_t gp0;         // global position of the tile's first position
+  int64_t ref_off;     // the contig's offset in the concatenated reference
+  int64_t contig_len;
+  int32_t start;       // the region's first locus
+  int32_t p0;          // region index of the tile's first position
+  int32_t n;           // positions of the tile
+  int32_t min_depth;   // the region's minDepth
+  int32_t reads;       // 1 when reads were fed to the region
+  int32_t pad;
+};
+static_assert(sizeof(CallDesc) == 48, "call tile descriptor");
+
 struct CallArgs {
   Reads R;
   const RegionDev* regions;
   const int32_t* call_tile_region;  // region of each call tile
+  CallDesc* call_desc;              // per call tile (k_call_desc)
   int32_t n_call_tiles;
   Records rec;
   StatsDev* stats;
