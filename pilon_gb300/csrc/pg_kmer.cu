@@ -230,22 +230,27 @@ __device__ inline void store_edge(const KmerArgs& a, unsigned long long k, const
   }
 }
 
+// kEdgeSlices CTAs per window, each over a slice of its table.
+constexpr int kEdgeSlices = 16;
+
 template <bool WIDE>
 __global__ void __launch_bounds__(256) k_kmer_edges(KmerArgs a) {
-  const int32_t w = a.win_list[blockIdx.x];
+  const int32_t w = a.win_list[blockIdx.x / kEdgeSlices];
   if (a.full[w]) return;
-  const int64_t base = a.slot_base[w], cap = a.slot_cap[w];
+  const int64_t cap = a.slot_cap[w], per = (cap + kEdgeSlices - 1) / kEdgeSlices;
+  const int64_t lo = a.slot_base[w] + (blockIdx.x % kEdgeSlices) * per;
+  const int64_t hi = min(lo + per, a.slot_base[w] + cap);
   const int32_t K = a.K;
   const int lane = threadIdx.x & 31;
   // every warp runs the same number of iterations, so the whole warp meets the ballot
-  for (int64_t s0 = base; s0 < base + cap; s0 += blockDim.x) {
+  for (int64_t s0 = lo; s0 < hi; s0 += blockDim.x) {
     const int64_t s = s0 + threadIdx.x;
     bool emit = false;
     uint32_t cnt[4] = {0, 0, 0, 0};
     unsigned long long key = 0, key_hi = 0;
     int32_t depth = 0;
     int b0 = 0, alt = -1;
-    if (s < base + cap) {
+    if (s < hi) {
       unsigned long long qs[4];
       uint32_t q_sum;
       bool used;
@@ -466,8 +471,8 @@ void launch_kmer_count(const KmerArgs& a, cudaStream_t s) {
 
 void launch_kmer_edges(const KmerArgs& a, cudaStream_t s) {
   if (a.n_win <= 0) return;
-  if (a.wide) k_kmer_edges<true><<<a.n_win, 256, 0, s>>>(a);
-  else k_kmer_edges<false><<<a.n_win, 256, 0, s>>>(a);
+  if (a.wide) k_kmer_edges<true><<<a.n_win * kEdgeSlices, 256, 0, s>>>(a);
+  else k_kmer_edges<false><<<a.n_win * kEdgeSlices, 256, 0, s>>>(a);
 }
 
 }  // namespace pg
