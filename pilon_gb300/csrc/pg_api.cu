@@ -152,7 +152,9 @@ T* P(DevBuf& b) {
 }
 
 DevParams to_dev(const pg_params* p) {
+  // zeroed first: the graph key hashes the whole struct, tail padding included
   DevParams d;
+  memset(&d, 0, sizeof d);
   d.min_mq = p->min_mq; d.min_qual = p->min_qual; d.flank = p->flank; d.default_qual = p->default_qual;
   d.min_min_depth = p->min_min_depth; d.nonpf = p->nonpf; d.duplicates = p->duplicates;
   d.old_indel = p->old_indel; d.fix_amb = p->fix_amb; d.long_read = p->long_read; d.bam_type = p->bam_type;
@@ -648,7 +650,8 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
     const void* ptrs[] = {c->ref.p, c->events.p, c->events_sorted.p, c->cands.p, c->pool.p, c->spool.p,
                           c->rec_count.p, c->rec_qsum.p, c->rec_call.p, c->rec_score.p, c->rec_indel_len.p,
                           c->rec_ins_str.p, c->rec_ev_end.p, c->chunk_stats.p, c->stats.p, c->tile_sums.p,
-                          c->regions.p, c->walk_tiles.p, c->call_tile_region.p, c->chunks.p, c->cand_count.p,
+                          c->regions.p, c->walk_tiles.p, c->call_tile_region.p, c->call_desc.p, c->chunks.p,
+                          c->cand_count.p,
                           c->cand_off.p, c->indel_list.p, c->counters.p, c->run_max.p, c->d_ext.p, c->rdesc.p,
                           c->staging_host};
     key = fnv(key, ptrs, sizeof ptrs);
