@@ -251,11 +251,12 @@ def kmer_bench(eng, ds, params, args, threads, K=31, radius=500):
     sec = sum(t) / len(t)
     dev_ms, dev_events, distinct, batch_bytes, batches = eng.last_tally_stats()
     # algorithmic bytes: every window read once (2-bit bases, qualities and 16 B of
-    # offsets, length and mapq), then per distinct K-mer its 8-byte key and 48-byte
-    # value written once
+    # offsets, length and mapq), then per distinct K-mer its 8-byte key and the
+    # PileUp fields buildGraph reads (4 counts, 4 Long quality sums, qSum: 52 B)
+    # written once
     rb = np.concatenate([[0], np.cumsum((L + 3) // 4 + L + 16)])
     read_bytes = int(sum(rb[b] - rb[a] for a, b in wins))
-    tally_bytes = read_bytes + 56 * distinct
+    tally_bytes = read_bytes + 60 * distinct
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
     hbm = peaks["hbm_gbs"] if peaks else 6800.0

@@ -925,7 +925,7 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
   // bytes per slot: KmerSlot / KmerSlotWide; exotic slots hold 2 or 4 key words, a used byte and
   // the counters (rounded up)
   const int64_t slot_b = wide ? (int64_t)sizeof(KmerSlotWide) : (int64_t)sizeof(KmerSlot);
-  const int64_t xslot_b = wide ? 96 : 80, xkw = wide ? 4 : 2;
+  const int64_t xkw = wide ? 4 : 2;
   const size_t edge_b = wide ? sizeof(pg_kmer_edge_wide) : sizeof(pg_kmer_edge);
   pg_status s;
   c->tally_ms = 0;
@@ -968,11 +968,11 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
   CK(cudaMemsetAsync(c->kused.p, 0, 8 * nwb, st));
   CK(cudaMemsetAsync(c->kwflag.p, 0, 4 * nwb, st));
   CK(cudaMemsetAsync(c->kx_evfill.p, 0, 8 * nwb, st));
-  auto table_bytes = [&](int32_t w) { return scap[w] * slot_b + xcap[w] * xslot_b + evcap[w] * 16; };
+  auto table_bytes = [&](int32_t w) { return scap[w] * slot_b; };
   struct Batch {
-    int32_t l0, l1;      // windows list[l0, l1)
-    int64_t c0, c1;      // chunks [c0, c1)
-    int64_t ns, nx, ne;  // table slots, exotic slots, exotic events
+    int32_t l0, l1;  // windows list[l0, l1)
+    int64_t c0, c1;  // chunks [c0, c1)
+    int64_t ns;      // table slots
   };
   std::vector<int32_t> list(n_windows);
   for (int32_t w = 0; w < n_windows; w++) list[w] = w;
@@ -993,31 +993,37 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
     // batches over the listed windows; table offsets are relative to the batch
     batches.clear();
     chunks.clear();
-    int64_t max_ns = 1, max_nx = 1, max_ne = 1;
+    int64_t max_ns = 1, nx = 0, ne = 0;
+    for (int32_t w : list) {  // exotic tables and event lists: the whole pass
+      xbase[w] = nx; evbase[w] = ne;
+      nx += xcap[w]; ne += evcap[w];
+    }
+    nx = std::max<int64_t>(nx, 1);
+    ne = std::max<int64_t>(ne, 1);
     for (int32_t l0 = 0; l0 < (int32_t)list.size();) {
-      Batch b{l0, l0, (int64_t)chunks.size(), 0, 0, 0, 0};
+      Batch b{l0, l0, (int64_t)chunks.size(), 0, 0};
       int64_t bytes = 0;
       while (b.l1 < (int32_t)list.size() && (b.l1 == l0 || bytes + table_bytes(list[b.l1]) <= kTallyBatchBytes)) {
         const int32_t w = list[b.l1++];
         bytes += table_bytes(w);
-        sbase[w] = b.ns; xbase[w] = b.nx; evbase[w] = b.ne;
-        b.ns += scap[w]; b.nx += xcap[w]; b.ne += evcap[w];
+        sbase[w] = b.ns;
+        b.ns += scap[w];
         for (int64_t lo = wins[w].read_begin; lo < wins[w].read_end; lo += kTallyReadsPerChunk)
           chunks.push_back(KmerChunk{lo, std::min<int64_t>(lo + kTallyReadsPerChunk, wins[w].read_end), w, 0});
       }
       b.c1 = (int64_t)chunks.size();
-      max_ns = std::max(max_ns, b.ns); max_nx = std::max(max_nx, b.nx); max_ne = std::max(max_ne, b.ne);
+      max_ns = std::max(max_ns, b.ns);
       c->tally_max_batch_bytes = std::max(c->tally_max_batch_bytes, bytes);
       batches.push_back(b);
       l0 = b.l1;
     }
     if ((s = ensure(c, c->kslots, (size_t)(slot_b * max_ns)))) return s;
-    if ((s = ensure(c, c->kx_ev, 16 * (size_t)max_ne))) return s;
-    if ((s = ensure(c, c->kx_keys, 8 * xkw * (size_t)max_nx))) return s;
-    if ((s = ensure(c, c->kx_used, (size_t)max_nx))) return s;
-    if ((s = ensure(c, c->kx_cnt, 16 * (size_t)max_nx))) return s;
-    if ((s = ensure(c, c->kx_qs, 32 * (size_t)max_nx))) return s;
-    if ((s = ensure(c, c->kx_q, 4 * (size_t)max_nx))) return s;
+    if ((s = ensure(c, c->kx_ev, 16 * (size_t)ne))) return s;
+    if ((s = ensure(c, c->kx_keys, 8 * xkw * (size_t)nx))) return s;
+    if ((s = ensure(c, c->kx_used, (size_t)nx))) return s;
+    if ((s = ensure(c, c->kx_cnt, 16 * (size_t)nx))) return s;
+    if ((s = ensure(c, c->kx_qs, 32 * (size_t)nx))) return s;
+    if ((s = ensure(c, c->kx_q, 4 * (size_t)nx))) return s;
     if ((s = ensure(c, c->kchunks, sizeof(KmerChunk) * std::max<size_t>(chunks.size(), 1)))) return s;
     if (!chunks.empty())
       CK(cudaMemcpyAsync(c->kchunks.p, chunks.data(), sizeof(KmerChunk) * chunks.size(), cudaMemcpyHostToDevice, st));
@@ -1037,20 +1043,22 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
       a.win_list = P<int32_t>(c->kwlist); a.n_win = (int32_t)list.size();
       launch_kmer_reset(a, st);
     }
+    CK(cudaMemsetAsync(c->kx_used.p, 0, (size_t)nx, st));
+    CK(cudaMemsetAsync(c->kx_cnt.p, 0, 16 * (size_t)nx, st));
+    CK(cudaMemsetAsync(c->kx_qs.p, 0, 32 * (size_t)nx, st));
+    CK(cudaMemsetAsync(c->kx_q.p, 0, 4 * (size_t)nx, st));
     for (const Batch& b : batches) {
       CK(cudaMemsetAsync(c->kslots.p, 0, (size_t)(slot_b * b.ns), st));
-      if (b.nx > 0) {
-        CK(cudaMemsetAsync(c->kx_used.p, 0, (size_t)b.nx, st));
-        CK(cudaMemsetAsync(c->kx_cnt.p, 0, 16 * (size_t)b.nx, st));
-        CK(cudaMemsetAsync(c->kx_qs.p, 0, 32 * (size_t)b.nx, st));
-        CK(cudaMemsetAsync(c->kx_q.p, 0, 4 * (size_t)b.nx, st));
-      }
       a.win_list = P<int32_t>(c->kwlist) + b.l0; a.n_win = b.l1 - b.l0;
       a.chunks = P<KmerChunk>(c->kchunks) + b.c0; a.n_chunks = (int32_t)(b.c1 - b.c0);
       launch_kmer_count(a, st);
       launch_kmer_edges(a, st);
       c->tally_batches++;
     }
+    // the exotic K-mers of every window of the pass, a warp per window (windows
+    // found full skip theirs: they are counted again, exotic K-mers included)
+    a.win_list = P<int32_t>(c->kwlist); a.n_win = (int32_t)list.size();
+    launch_kmer_exotic(a, st);
     CK(cudaEventRecord(c->e1, st));
     CK(cudaGetLastError());
     std::vector<int32_t> all(n_windows);

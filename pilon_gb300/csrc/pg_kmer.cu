@@ -458,15 +458,16 @@ void launch_kmer_reset(const KmerArgs& a, cudaStream_t s) {
 }
 
 void launch_kmer_count(const KmerArgs& a, cudaStream_t s) {
+  if (a.n_win <= 0 || a.n_chunks <= 0) return;
+  if (a.wide) k_kmer_count<true><<<a.n_chunks, kKmerThreads, 0, s>>>(a);
+  else k_kmer_count<false><<<a.n_chunks, kKmerThreads, 0, s>>>(a);
+}
+
+void launch_kmer_exotic(const KmerArgs& a, cudaStream_t s) {
   if (a.n_win <= 0) return;
-  const int32_t xg = (a.n_win * 32 + kExoticThreads - 1) / kExoticThreads;
-  if (a.wide) {
-    if (a.n_chunks > 0) k_kmer_count<true><<<a.n_chunks, kKmerThreads, 0, s>>>(a);
-    k_kmer_exotic<true><<<xg, kExoticThreads, 0, s>>>(a, a.n_win);
-  } else {
-    if (a.n_chunks > 0) k_kmer_count<false><<<a.n_chunks, kKmerThreads, 0, s>>>(a);
-    k_kmer_exotic<false><<<xg, kExoticThreads, 0, s>>>(a, a.n_win);
-  }
+  const int32_t xg = (int32_t)(((int64_t)a.n_win * 32 + kExoticThreads - 1) / kExoticThreads);
+  if (a.wide) k_kmer_exotic<true><<<xg, kExoticThreads, 0, s>>>(a, a.n_win);
+  else k_kmer_exotic<false><<<xg, kExoticThreads, 0, s>>>(a, a.n_win);
 }
 
 void launch_kmer_edges(const KmerArgs& a, cudaStream_t s) {

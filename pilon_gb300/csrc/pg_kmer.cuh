@@ -44,10 +44,11 @@ struct KmerArgs {
   int32_t* full;              // per window: 1 when a probe sequence ran past the bound (count again, larger)
   unsigned long long* used;   // per window: distinct K-mers inserted
   // tables: slots [slot_base[w], slot_base[w] + slot_cap[w]) of window w, relative to the batch
+  // (the exotic tables and event lists are relative to the pass)
   const int64_t* slot_base;
   const int64_t* slot_cap;
   void* slots;                // KmerSlot or KmerSlotWide
-  // exotic tables (4-bit keys), one warp per window
+  // exotic tables (4-bit keys) of every window of the pass, one warp per window
   const int64_t* x_base;
   const int64_t* x_cap;
   unsigned long long* x_keys; // 2 per slot (wide: 4)
@@ -72,8 +73,10 @@ void launch_kmer_prepass(const Reads& R, const pg_window* wins, int32_t n, int32
                          cudaStream_t s);
 // clears full / used / x_ev_fill of the windows in win_list
 void launch_kmer_reset(const KmerArgs& a, cudaStream_t s);
-// k_kmer_count over the batch's chunks, then k_kmer_exotic over its windows
+// k_kmer_count over the batch's chunks
 void launch_kmer_count(const KmerArgs& a, cudaStream_t s);
+// k_kmer_exotic over the windows of win_list (after every batch of them was counted)
+void launch_kmer_exotic(const KmerArgs& a, cudaStream_t s);
 // k_kmer_edges over the batch's windows (windows marked full write none)
 void launch_kmer_edges(const KmerArgs& a, cudaStream_t s);
 
