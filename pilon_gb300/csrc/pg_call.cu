@@ -101,119 +101,37 @@ __global__ void k_call_desc(CallArgs a, int32_t tile_begin) {
   a.call_desc[t] = d;
 }
 
-// k_call: persistent CTAs over units of kCallThreads positions (a quarter of
-// a call tile); unit u of the launch is quarter u % kCallUnits of tile
-// tile_begin + u / kCallUnits, and a CTA takes units blockIdx.x, + gridDim.x,
-// ...  Each thread owns one position of a unit and its slots in two shared
-// buffers: while it calls its position of one unit, its position's record in
-// the CTA's next unit is on its way into the other buffer by cp.async (the
-// 16-byte base counts, the 32-byte quality sums, six 4-byte counters and the
-// aligned word that holds the reference base: 76 bytes), so the record loads
-// of the next unit overlap the calls of this one.  A thread reads only the
-// slots it filled, so no barrier is needed.
+// k_call: one thread per position, kCallUnits CTAs of kCallThreads per call
+// tile.  A thread's loads start from its tile's descriptor (one load), and the
+// reference byte is loaded with the record, so every load of a position is in
+// flight at once.  (A persistent form that staged the next unit's record into
+// shared memory by cp.async while calling the current one ran 15% slower: the
+// two stage buffers and the carried state cut residency to 19 warps per SM and
+// one unit of work did not cover the load latency.)
 constexpr int kCallThreads = 256;
 constexpr int kCallUnits = kCallTile / kCallThreads;
 static_assert(kCallUnits * kCallThreads == kCallTile, "call tile split");
 
-struct CallStage {
-  int4 cnt[kCallThreads];
-  longlong2 qs0[kCallThreads], qs1[kCallThreads];
-  int32_t f[6][kCallThreads];  // mq_sum, q_sum, deletions, del_qual, insertions, ins_qual
-  uint32_t ref[kCallThreads];  // the aligned reference word holding the position's base
-};
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-
-// Queues the copies of position i of unit (tile t, quarter q) into stage buffer b.
-__device__ __forceinline__ void stage_position(const CallArgs& a, const CallDesc& d, int32_t q, CallStage& b, int i) {
-  const int32_t k = q * kCallThreads + i;  // index in the tile
-  if (k >= d.n) return;
-  const int64_t gp = d.gp0 + k;
-  const Records& R = a.rec;
-  cp_async16(&b.cnt[i], &R.count[gp]);
-  cp_async16(&b.qs0[i], &R.qual_sum[2 * gp]);
-  cp_async16(&b.qs1[i], &R.qual_sum[2 * gp + 1]);
-  cp_async4(&b.f[0][i], &R.mq_sum[gp]);
-  cp_async4(&b.f[1][i], &R.q_sum[gp]);
-  cp_async4(&b.f[2][i], &R.deletions[gp]);
-  cp_async4(&b.f[3][i], &R.del_qual[gp]);
-  cp_async4(&b.f[4][i], &R.insertions[gp]);
-  cp_async4(&b.f[5][i], &R.ins_qual[gp]);
-  // locus0 = start - 1 + p; the reference buffer has 16 bytes of slack after its end
-  const uintptr_t ra = (uintptr_t)(a.ref + d.ref_off + (int64_t)d.start - 1 + d.p0 + k);
-  cp_async4(&b.ref[i], (const void*)(ra & ~(uintptr_t)3));
-}
-
-__device__ __forceinline__ void prefetch_l1(const void* p) {
-  asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
-}
-
-// The descriptors are read where they are used (from L1: the one two units
-// ahead is prefetched each iteration) rather than carried in registers.
-__global__ void __launch_bounds__(kCallThreads, 4) k_call(CallArgs a, int32_t tile_begin) {
-  __shared__ CallStage stage[2];
-  const int i = threadIdx.x;
-  const int32_t n_units = a.n_call_tiles * kCallUnits;
-  const int32_t G = gridDim.x;
-  const CallDesc* desc = a.call_desc + tile_begin;
-  int32_t u = blockIdx.x;
-  if (u >= n_units) return;
-  if (u + G < n_units) prefetch_l1(&desc[(u + G) / kCallUnits]);
-  stage_position(a, desc[u / kCallUnits], u % kCallUnits, stage[0], i);
-  cp_async_commit();
-  for (int k = 0; u < n_units; k++, u += G) {
-    const int32_t u1 = u + G, u2 = u + 2 * G;
-    if (u2 < n_units) {
-      const char* pd = reinterpret_cast<const char*>(&desc[u2 / kCallUnits]);
-      prefetch_l1(pd);
-      prefetch_l1(pd + sizeof(CallDesc) - 1);
-    }
-    if (u1 < n_units) stage_position(a, desc[u1 / kCallUnits], u1 % kCallUnits, stage[(k + 1) & 1], i);
-    cp_async_commit();
-    cp_async_wait_prev();  // this unit's copies are in
-    const CallStage& b = stage[k & 1];
-    const CallDesc d = desc[u / kCallUnits];
-    const int32_t kk = (u % kCallUnits) * kCallThreads + i;
-    uint32_t changes = 0;
-    if (kk < d.n) {
-      PosRec rec;
-      const int4 c = b.cnt[i];
-      rec.cnt[0] = c.x; rec.cnt[1] = c.y; rec.cnt[2] = c.z; rec.cnt[3] = c.w;
-      const longlong2 q0 = b.qs0[i], q1 = b.qs1[i];
-      rec.qs[0] = q0.x; rec.qs[1] = q0.y; rec.qs[2] = q1.x; rec.qs[3] = q1.y;
-      rec.mq_sum = b.f[0][i]; rec.q_sum = b.f[1][i];
-      rec.deletions = b.f[2][i]; rec.del_qual = b.f[3][i];
-      rec.insertions = b.f[4][i]; rec.ins_qual = b.f[5][i];
-      const uintptr_t ra = (uintptr_t)(a.ref + d.ref_off + (int64_t)d.start - 1 + d.p0 + kk);
-      const uint8_t rb = upper((uint8_t)(b.ref[i] >> (8 * (ra & 3u))));
-      changes = call_position(a, d, d.p0 + kk, d.gp0 + kk, rec, rb) != 0;
-    }
-    changes = __reduce_add_sync(FULL, changes);
-    if ((i & 31) == 0 && changes) atomicAdd(&a.cand_count[tile_begin + u / kCallUnits], (int32_t)changes);
+__global__ void __launch_bounds__(kCallThreads, 6) k_call(CallArgs a, int32_t tile_begin) {
+  const int32_t t = tile_begin + blockIdx.x / kCallUnits;
+  const CallDesc d = a.call_desc[t];
+  const int32_t k = (blockIdx.x % kCallUnits) * kCallThreads + threadIdx.x;  // index in the tile
+  uint32_t changes = 0;
+  if (k < d.n) {
+    const int64_t gp = d.gp0 + k;
+    PosRec rec;
+    load_rec(a.rec, gp, rec);
+    const uint8_t rb = upper(a.ref[d.ref_off + (int64_t)d.start - 1 + d.p0 + k]);
+    changes = call_position(a, d, d.p0 + k, gp, rec, rb) != 0;
   }
+  changes = __reduce_add_sync(FULL, changes);
+  if ((threadIdx.x & 31) == 0 && changes) atomicAdd(&a.cand_count[t], (int32_t)changes);
 }
 
 void launch_call(const CallArgs& a, int32_t tile_begin, int32_t n_tiles, cudaStream_t s) {
   if (n_tiles <= 0) return;
   k_call_desc<<<(n_tiles + 255) / 256, 256, 0, s>>>(a, tile_begin);
-  static int grid_max = 0;
-  if (grid_max == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_call, kCallThreads, 0);
-    grid_max = std::max(1, sms * std::max(per_sm, 1));
-  }
-  const int64_t units = (int64_t)n_tiles * kCallUnits;
-  k_call<<<(int)std::min<int64_t>(units, grid_max), kCallThreads, 0, s>>>(a, tile_begin);
+  k_call<<<n_tiles * kCallUnits, kCallThreads, 0, s>>>(a, tile_begin);
 }
 
 // The change candidates of a call tile in position order, at the tile's offset

@@ -408,38 +408,6 @@ __device__ __forceinline__ void walk_chunks(uint32_t* cbase, const uint32_t* qw,
 // entry kinds of a lane's word w1
 enum : uint32_t { kSkip = 0, kFast = 1, kInvalid = 2, kSlow = 3, kClip = 4 };
 
-__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p)); }
-
-// Prefetches tile t's walk entries and the read bytes they point into, thread
-// k of the CTA taking the 128-byte lines k, k + blockDim.x, ... of the three
-// ranges.  Every address lies between two entries' own addresses, so inside
-// the arrays.
-__device__ __noinline__ void prefetch_tile(const WalkArgs& a, int32_t t) {
-  const WalkTile nt = a.tiles[t];
-  if (nt.ent_hi <= nt.ent_lo) return;
-  const int4* ent = a.R.entries;
-  const int4 f = ent[3 * nt.ent_lo + 2], l = ent[3 * (nt.ent_hi - 1) + 2];
-  const uintptr_t e0 = (uintptr_t)(ent + 3 * nt.ent_lo) & ~(uintptr_t)127;
-  const uintptr_t e1 = (uintptr_t)(ent + 3 * nt.ent_hi) - 1;
-  const uintptr_t q0 = (uintptr_t)(a.R.qual + ((int64_t)f.y << 32 | (uint32_t)f.x)) & ~(uintptr_t)127;
-  const uintptr_t q1 = (uintptr_t)(a.R.qual + ((int64_t)l.y << 32 | (uint32_t)l.x));
-  const uintptr_t s0 = (uintptr_t)(a.R.seq + (((int64_t)f.w << 32 | (uint32_t)f.z) >> 1)) & ~(uintptr_t)127;
-  const uintptr_t s1 = (uintptr_t)(a.R.seq + (((int64_t)l.w << 32 | (uint32_t)l.z) >> 1));
-  // a store whose reads' bytes are not in read order gives no useful range: at
-  // most kMaxLines lines per range
-  constexpr int64_t kMaxLines = 4096;
-  auto lines = [](uintptr_t lo, uintptr_t hi) {
-    const int64_t n = hi >= lo ? (int64_t)((hi - lo) >> 7) + 1 : 0;
-    return n <= kMaxLines ? n : (int64_t)0;
-  };
-  const int64_t ne = lines(e0, e1), nq = lines(q0, q1), ns = lines(s0, s1);
-  for (int64_t k = threadIdx.x; k < ne + nq + ns; k += blockDim.x) {
-    const uintptr_t p = k < ne ? e0 + (uintptr_t)(k << 7)
-                               : k < ne + nq ? q0 + (uintptr_t)((k - ne) << 7) : s0 + (uintptr_t)((k - ne - nq) << 7);
-    prefetch_l2((const void*)p);
-  }
-}
-
 // dynamic shared memory of a walk CTA: the counters and 4 words of padding
 template <int T>
 constexpr size_t walk_smem() {
@@ -672,11 +640,6 @@ __global__ void __launch_bounds__(MINB >= 4 ? 256 : 512, MINB) k_walk(WalkArgs a
         }
         __syncwarp();
       }
-      // A warp whose claims are done would wait at the barrier: it asks L2 for
-      // a share of the CTA's next tile (its walk entries, and the quality and
-      // sequence bytes between its first and last entry's), so that tile's
-      // loads find them there.
-      if (c1 == tile.ent_hi && t + (int32_t)gridDim.x < tile_end) prefetch_tile(a, t + (int32_t)gridDim.x);
       __syncthreads();
 
       // flush: the first pass stores, later passes add (the CTA owns the tile)
