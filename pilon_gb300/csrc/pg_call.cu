@@ -135,76 +135,52 @@ void launch_call(const CallArgs& a, int32_t tile_begin, int32_t n_tiles, cudaStr
 }
 
 // The change candidates of a call tile in position order, at the tile's offset
-// from the scan of k_call's per-tile counts.  A CTA of 256 threads takes 256
-// consecutive tiles, lists those with changes, and for each loads its call
-// words coalesced into shared memory; each thread ranks four consecutive
-// positions, and a block scan joins the threads.
+// from the scan of k_call's per-tile counts.  256 threads per 1024-position
+// tile: the call words are loaded coalesced into shared memory, each thread
+// ranks four consecutive positions, and a block scan joins the threads.
 constexpr int kCandThreads = 256;
 __global__ void __launch_bounds__(kCandThreads) k_cand_list(CallArgs a, const int32_t* cand_off, Cand* cands,
-                                                             int32_t cand_cap, int32_t tile_begin, int32_t n_tiles) {
+                                                             int32_t cand_cap, int32_t tile_begin) {
   __shared__ __align__(16) uint32_t s_k[kCallTile];
   __shared__ int32_t s_w[kCandThreads / 32];
-  __shared__ int32_t s_tiles[kCandThreads];  // the group's tiles with changes
-  __shared__ int32_t s_n;
-  // this CTA's group: kCandThreads consecutive tiles, one count each, and the
-  // tiles k_call found changes in (most have none) listed in order
-  const int32_t g0 = tile_begin + blockIdx.x * kCandThreads;
+  const int32_t t = tile_begin + blockIdx.x;
+  if (a.cand_count[t] == 0) return;  // k_call counted the tile's changes: none (the whole CTA leaves)
+  const int32_t r = a.call_tile_region[t];
+  const RegionDev g = a.regions[r];
+  const int32_t p0 = (t - g.call_tile0) * kCallTile;
+  const int32_t n = min(kCallTile, g.size - p0);
+  for (int32_t i = threadIdx.x; i < kCallTile; i += kCandThreads)
+    s_k[i] = i < n ? PG_CALL_CHANGE(a.rec.call[g.pos_base + p0 + i]) : 0u;
+  __syncthreads();
+  const uint4 k4 = reinterpret_cast<const uint4*>(s_k)[threadIdx.x];  // positions 4 tid .. 4 tid + 3
+  const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
+  const int32_t mine = (k4.x != 0) + (k4.y != 0) + (k4.z != 0) + (k4.w != 0);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  {
-    const int32_t t = g0 + threadIdx.x;
-    const bool has = t < tile_begin + n_tiles && a.cand_count[t] != 0;
-    const unsigned m = __ballot_sync(FULL, has);
-    if (lane == 0) s_w[warp] = __popc(m);
-    __syncthreads();
-    int32_t before = __popc(m & ((1u << lane) - 1u)), total = 0;
-    for (int w = 0; w < kCandThreads / 32; w++) {
-      if (w < warp) before += s_w[w];
-      total += s_w[w];
-    }
-    if (has) s_tiles[before] = t;
-    if (threadIdx.x == 0) s_n = total;
-    __syncthreads();
+  int32_t incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t y = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += y;
   }
-  const int32_t n_list = s_n;
-  for (int32_t q = 0; q < n_list; q++) {
-    const int32_t t = s_tiles[q];
-    const int32_t r = a.call_tile_region[t];
-    const RegionDev g = a.regions[r];
-    const int32_t p0 = (t - g.call_tile0) * kCallTile;
-    const int32_t n = min(kCallTile, g.size - p0);
-    __syncthreads();  // the previous tile's s_k and s_w reads are done
-    for (int32_t i = threadIdx.x; i < kCallTile; i += kCandThreads)
-      s_k[i] = i < n ? PG_CALL_CHANGE(a.rec.call[g.pos_base + p0 + i]) : 0u;
-    __syncthreads();
-    const uint4 k4 = reinterpret_cast<const uint4*>(s_k)[threadIdx.x];  // positions 4 tid .. 4 tid + 3
-    const uint32_t kk[4] = {k4.x, k4.y, k4.z, k4.w};
-    const int32_t mine = (k4.x != 0) + (k4.y != 0) + (k4.z != 0) + (k4.w != 0);
-    int32_t incl = mine;
+  if (lane == 31) s_w[warp] = incl;
+  __syncthreads();
+  int32_t before = incl - mine;
+  for (int w = 0; w < warp; w++) before += s_w[w];
+  if (mine) {
+    int32_t slot = cand_off[t] + before;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int32_t y = __shfl_up_sync(FULL, incl, o);
-      if (lane >= o) incl += y;
-    }
-    if (lane == 31) s_w[warp] = incl;
-    __syncthreads();
-    int32_t before = incl - mine;
-    for (int w = 0; w < warp; w++) before += s_w[w];
-    if (mine) {
-      int32_t slot = cand_off[t] + before;
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        if (!kk[j]) continue;
-        const int32_t p = p0 + 4 * (int32_t)threadIdx.x + j;
-        const int64_t gp = g.pos_base + p;
-        Cand c;
-        c.gpos = gp;
-        c.region = r;
-        c.p = p;
-        c.kind = (int32_t)kk[j];
-        c.len = a.rec.indel_len[gp];
-        if (slot < cand_cap) cands[slot] = c;
-        slot++;
-      }
+    for (int j = 0; j < 4; j++) {
+      if (!kk[j]) continue;
+      const int32_t p = p0 + 4 * (int32_t)threadIdx.x + j;
+      const int64_t gp = g.pos_base + p;
+      Cand c;
+      c.gpos = gp;
+      c.region = r;
+      c.p = p;
+      c.kind = (int32_t)kk[j];
+      c.len = a.rec.indel_len[gp];
+      if (slot < cand_cap) cands[slot] = c;
+      slot++;
     }
   }
 }
@@ -289,8 +265,7 @@ void launch_change_write(const RegionDev* regions, const int32_t* tile_region, c
 void launch_cand_list(const CallArgs& a, const int32_t* cand_off, Cand* cands, int32_t cand_cap,
                       int32_t tile_begin, int32_t n_tiles, cudaStream_t s) {
   if (n_tiles <= 0) return;
-  k_cand_list<<<(n_tiles + kCandThreads - 1) / kCandThreads, kCandThreads, 0, s>>>(a, cand_off, cands, cand_cap,
-                                                                                   tile_begin, n_tiles);
+  k_cand_list<<<n_tiles, kCandThreads, 0, s>>>(a, cand_off, cands, cand_cap, tile_begin);
 }
 
 // Pass 1 is a left-to-right scan: a candidate inside an earlier accepted
