@@ -846,21 +846,18 @@ __global__ void __launch_bounds__(kEvThreads, 16) k_read_events(EventArgs a, int
 
 // The I and D operators of the listed reads (S/PileUpRegion.scala:150-183):
 // left shift, H1 double count, the indel counters and the events for the
-// vote.  A warp takes the lists of kIndelChunks chunks at a time (a few per
-// cent of their reads have indels; persistent CTAs, the warp loops over its
-// groups) and walks their union 32 reads at a time, one read per thread: the
-// in-warp scan of the lists' lengths gives each entry's list, as the last list
-// starting at or before it.
+// vote.  Each warp takes the lists of kIndelChunks chunks (a few per cent of
+// their reads have indels) and walks their union 32 reads at a time, one
+// read per thread: the in-warp scan of the lists' lengths gives each entry's
+// list, as the last list starting at or before it.
 constexpr int kIndelThreads = 128, kIndelChunks = 2;
-__global__ void __launch_bounds__(kIndelThreads, 8) k_read_indels(EventArgs a, int32_t chunk_begin, int32_t chunk_end) {
+__global__ void __launch_bounds__(kIndelThreads) k_read_indels(EventArgs a, int32_t chunk_begin, int32_t chunk_end) {
   __shared__ uint8_t s_lane[kIndelThreads / 32][32];  // per warp: lane of the k-th non-empty list
   const Reads& R = a.R;
   const DevParams& P = a.P;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int64_t warps = (int64_t)gridDim.x * (kIndelThreads / 32);
-  for (int64_t wg = ((int64_t)blockIdx.x * kIndelThreads + threadIdx.x) >> 5;
-       chunk_begin + wg * kIndelChunks < chunk_end; wg += warps) {  // whole warps loop together
-  const int32_t c0 = chunk_begin + (int32_t)(wg * kIndelChunks);
+  const int32_t c0 = chunk_begin + (int32_t)(((int64_t)blockIdx.x * kIndelThreads + threadIdx.x) >> 5) * kIndelChunks;
+  if (c0 >= chunk_end) return;  // whole warps leave together
   const int32_t cnt = (lane < kIndelChunks && c0 + lane < chunk_end) ? a.chunk_stats[c0 + lane].n_indel : 0;
   int32_t incl = cnt;
 #pragma unroll
@@ -870,7 +867,6 @@ __global__ void __launch_bounds__(kIndelThreads, 8) k_read_indels(EventArgs a, i
   }
   const int32_t E = incl - cnt, total = __shfl_sync(FULL, incl, 31);
   const unsigned ne = __ballot_sync(FULL, cnt > 0);
-  __syncwarp();  // the previous group's reads of s_lane are done
   if (cnt > 0) s_lane[wib][__popc(ne & ((1u << lane) - 1u))] = (uint8_t)lane;
   __syncwarp();
   for (int32_t k0 = 0; k0 < total; k0 += 32) {
@@ -1070,28 +1066,15 @@ __global__ void __launch_bounds__(kIndelThreads, 8) k_read_indels(EventArgs a, i
     if (bc_n) atomicAdd(&cs.base_count, bc_n);
     if (err) atomicMax(&cs.error, err);
   }
-  }
 }
 
 void launch_read_events(const EventArgs& a, int32_t chunk_begin, int32_t chunk_count, cudaStream_t s) {
   if (chunk_count <= 0) return;
   cudaMemsetAsync(a.chunk_stats + chunk_begin, 0, sizeof(ChunkStats) * (size_t)chunk_count, s);
   k_read_events<<<chunk_count * kEvPerChunk, kEvThreads, 0, s>>>(a, chunk_begin, chunk_begin + chunk_count);
-  // persistent: at most the CTAs the GPU holds at once, each warp looping over
-  // its groups of chunks (a warp's group is one dependent chain of loads; short
-  // CTAs left the SMs a few warps each)
-  static int indel_ctas = 0;
-  if (indel_ctas == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_read_indels, kIndelThreads, 0);
-    indel_ctas = std::max(1, sms * std::max(per_sm, 1));
-  }
   const int64_t warps = ((int64_t)chunk_count + kIndelChunks - 1) / kIndelChunks;
-  const int64_t ctas = (warps * 32 + kIndelThreads - 1) / kIndelThreads;
-  k_read_indels<<<(int)std::min<int64_t>(ctas, indel_ctas), kIndelThreads, 0, s>>>(a, chunk_begin,
-                                                                                  chunk_begin + chunk_count);
+  k_read_indels<<<(int)((warps * 32 + kIndelThreads - 1) / kIndelThreads), kIndelThreads, 0, s>>>(
+      a, chunk_begin, chunk_begin + chunk_count);
 }
 
 // ---------------------------------------------------------------------------
