@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -206,6 +207,11 @@ inline uint64_t fnv(uint64_t h, const void* p, size_t n) {
   for (size_t k = 0; k < n; k++) h = (h ^ b[k]) * 0x100000001b3ull;
   return h;
 }
+std::mutex& upload_mutex(int device) {
+  static std::mutex m[64];
+  return m[(unsigned)device % 64u];
+}
+
 // the same over 64-bit words, each mixed before it is folded in
 inline uint64_t fnv64(uint64_t h, const int64_t* w, size_t n) {
   for (size_t k = 0; k < n; k++) {
@@ -422,7 +428,18 @@ pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
     if (bytes[k] && !src[k]) return fail(c, PG_ERR_ARG, "reads field %d is null", k);
     pg_status s = ensure(c, c->rd[k], std::max<size_t>(bytes[k], 16));
     if (s) return s;
-    if (bytes[k]) CK(cudaMemcpyAsync(c->rd[k].p, src[k], bytes[k], cudaMemcpyHostToDevice, c->stream));
+  }
+  {
+    // Uploads to one device take turns: the host link is saturated by one
+    // upload (about 210 GB/s on a GB300 whatever the number of streams), so two
+    // contexts uploading at once only split it and then compute at once; in
+    // turns, one context's upload overlaps the other's kernels.  The context's
+    // earlier work is waited for before the turn is taken.
+    CK(cudaStreamSynchronize(c->stream));
+    std::lock_guard<std::mutex> turn(upload_mutex(c->device));
+    for (int k = 0; k < 15; k++)
+      if (bytes[k]) CK(cudaMemcpyAsync(c->rd[k].p, src[k], bytes[k], cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
   }
   Reads& R = c->R;
   R.n = n;
