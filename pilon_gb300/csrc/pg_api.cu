@@ -96,6 +96,8 @@ struct pg_ctx {
   cudaGraphExec_t graph_exec = nullptr;
   uint64_t graph_key = 0;
   bool graph_valid = false;  // cleared whenever a buffer the graph uses is reallocated
+  uint64_t plan_key = 0;     // the plan now in the device buffers (0: none); cleared with graph_valid
+  uint64_t ref_gen = 0;      // counts pg_set_reference calls
   int32_t use_graph = 1;
   int32_t graph_replays = 0;
   bool capturing = false;
@@ -128,6 +130,7 @@ pg_status ensure(pg_ctx* c, DevBuf& b, size_t bytes) {
   // a captured graph holds the old address: it must not be replayed again
   c->graph_valid = false;
   c->graph_key = 0;
+  c->plan_key = 0;  // the plan buffers may be among those reallocated
   if (b.p) cudaFree(b.p);
   b.p = nullptr;
   b.cap = 0;
@@ -355,6 +358,8 @@ pg_status pg_set_reference(pg_ctx* c, int32_t n, const int64_t* lens, const uint
   }
   if (!c->stream) return not_open(c);
   cudaSetDevice(c->device);
+  c->ref_gen++;  // region offsets into the reference change: the next plan is uploaded again
+  c->plan_key = 0;
   c->ref_off.assign(n, 0);
   c->ref_len.assign(lens, lens + n);
   int64_t total = 0;
@@ -471,8 +476,9 @@ pg_status pg_set_reads_device(pg_ctx* c, const pg_reads* d) {
 
 static pg_status stage(pg_ctx* c, size_t bytes) {
   if (bytes <= c->staging_cap) return PG_OK;
-  c->graph_valid = false;  // the graph's copy nodes read the old staging buffer
+  c->graph_valid = false;
   c->graph_key = 0;
+  c->plan_key = 0;
   if (c->staging_host) cudaFreeHost(c->staging_host);
   c->staging_host = nullptr;
   size_t want = bytes + bytes / 4 + 4096;
@@ -678,8 +684,23 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
       const int64_t f[5] = {regs[r].contig, regs[r].start, regs[r].stop, regs[r].read_begin, regs[r].read_end};
       key = fnv64(key, f, 5);
     }
-    const int64_t sizes[5] = {n_regions, (int64_t)b_reg, (int64_t)b_walk, (int64_t)b_call, (int64_t)b_ch};
-    key = fnv64(key, sizes, 5);
+    const int64_t sizes[7] = {n_regions, (int64_t)b_reg, (int64_t)b_walk, (int64_t)b_call, (int64_t)b_ch,
+                              (int64_t)c->tile_width, (int64_t)c->ref_gen};
+    key = fnv64(key, sizes, 7);
+    // the plan is a function of the regions asked for, the tile width and the
+    // reference: copied to the device only when it differs from the one there
+    // (outside the recorded graph, so a replay does not queue host-to-device
+    // copies behind another context's upload)
+    const uint64_t plan_key = key | 1ull;
+    if (c->plan_key != plan_key) {
+      CK(cudaMemcpyAsync(c->regions.p, c->staging_host, b_reg, cudaMemcpyHostToDevice, st));
+      if (b_walk) CK(cudaMemcpyAsync(c->walk_tiles.p, (char*)c->staging_host + b_reg, b_walk, cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(c->call_tile_region.p, (char*)c->staging_host + b_reg + b_walk, b_call,
+                         cudaMemcpyHostToDevice, st));
+      if (b_ch) CK(cudaMemcpyAsync(c->chunks.p, (char*)c->staging_host + b_reg + b_walk + b_call, b_ch,
+                                   cudaMemcpyHostToDevice, st));
+      c->plan_key = plan_key;
+    }
     key = fnv(key, &dp, sizeof dp);
     key = fnv(key, &c->R, sizeof c->R);
     // every buffer the recorded launches and copies read or write, host staging included
@@ -709,12 +730,6 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
       c->capturing = capture;
       c->launches = 0;
       c->n_runs = 0;
-      cudaMemcpyAsync(c->regions.p, c->staging_host, b_reg, cudaMemcpyHostToDevice, st);
-      if (b_walk) cudaMemcpyAsync(c->walk_tiles.p, (char*)c->staging_host + b_reg, b_walk, cudaMemcpyHostToDevice, st);
-      cudaMemcpyAsync(c->call_tile_region.p, (char*)c->staging_host + b_reg + b_walk, b_call, cudaMemcpyHostToDevice,
-                      st);
-      if (b_ch) cudaMemcpyAsync(c->chunks.p, (char*)c->staging_host + b_reg + b_walk + b_call, b_ch,
-                                cudaMemcpyHostToDevice, st);
       cudaMemsetAsync(c->stats.p, 0, sizeof(StatsDev) * n_regions, st);
       cudaMemsetAsync(c->counters.p, 0, sizeof(unsigned long long) * CNT_N, st);
       cudaMemsetAsync(c->run_max.p, 0, sizeof(unsigned long long) * 2, st);
