@@ -295,6 +295,59 @@ pg_status pg_kmer_tally_wide(pg_ctx *ctx, const pg_window *windows, int32_t n_wi
                              int32_t K, const pg_params *params, int32_t min_depth,
                              pg_kmer_edge_wide *edges, int64_t cap, int64_t *n_edges);
 
+/* The tally of pg_kmer_tally_wide over windows of listed reads: window w
+ * holds reads[windows[w].read_begin .. windows[w].read_end) (indices into the
+ * read store, in the order Assembler.addReads sees them), so a window can
+ * hold the reads GapFiller.recruitReads collects (S/GapFiller.scala:364-402):
+ * the reads overlapping the flanks of a break, which are not one index range
+ * of the store, and their stray mates anywhere in it. */
+pg_status pg_kmer_tally_reads(pg_ctx *ctx, const int64_t *reads, int64_t n_reads, const pg_window *windows,
+                              int32_t n_windows, int32_t K, const pg_params *params, int32_t min_depth,
+                              pg_kmer_edge_wide *edges, int64_t cap, int64_t *n_edges);
+
+/* ---- local reassembly (host) ---------------------------------------------
+ * One gap or break to reassemble: GapFiller.fillGap (is_gap = 1) or
+ * GapFiller.fixBreak (is_gap = 0) of a GenomeRegion (S/GapFiller.scala:39-47),
+ * walked over the K-mer graph of window `window` of the edges given to
+ * pg_reassemble (the tally of GapFiller.recruitReads' reads). */
+typedef struct pg_reassembly {
+  int32_t window;            /* window of the edges that holds this break's reads */
+  int32_t is_gap;            /* 1: a gap of Ns (fillGap); 0: a possible break (fixBreak) */
+  int32_t region_start;      /* the GenomeRegion, 1-based loci, inclusive */
+  int32_t region_stop;
+  int32_t break_start;       /* the gap or break, 1-based loci, inclusive */
+  int32_t break_stop;
+  int32_t break_radius;      /* GapFiller.breakRadius (S/GapFiller.scala:357-362) */
+  int32_t pad_;
+  const char *bases;         /* the region's bases after its SNP fixes (region size bytes) */
+  const char *orig;          /* the region's original bases (region size bytes) */
+} pg_reassembly;
+
+/* The fix of one pg_reassembly, GenomeRegion.Fix (locus, was, patch). */
+typedef struct pg_reassembly_fix {
+  int32_t start;             /* first locus of the fix; 0 when there is no solution */
+  int32_t status;            /* PG_OK, or PG_ERR_INDEX where the reference's require(...) fails */
+  int32_t loop_len;          /* length of the shortest K-mer loop the walk met (a tandem repeat), 0 if none */
+  int32_t pad_;
+  int64_t was_off, was_len;     /* the replaced bases (refSubString), in text */
+  int64_t patch_off, patch_len; /* the new bases, in text */
+} pg_reassembly_fix;
+
+/* GapFiller.assembleAcrossBreak (S/GapFiller.scala:49-100) for every job, on
+ * the host: the walk of Assembler.multiBridge from both sides of the break
+ * over the window's graph (S/Assembler.scala:164-284), the joins of
+ * breakJoins / properOverlap / trimPatch (S/GapFiller.scala:161-262), and for
+ * gaps the partial fill from each side's consensus.  `edges` are the output of
+ * pg_kmer_tally_reads (any order); K is Assembler.K.  Jobs run on `threads`
+ * host threads (0 = all cores).  The fixes' strings are copied into `text`
+ * when they fit in text_cap bytes; *text_len receives their total size either
+ * way (PG_ERR_LIMIT when it does not fit).  Needs no context or device.
+ * Scala's Set of solutions is taken in insertion order, which is its order up
+ * to four elements. */
+pg_status pg_reassemble(const pg_kmer_edge_wide *edges, int64_t n_edges, int32_t K, const pg_reassembly *jobs,
+                        int32_t n_jobs, int32_t threads, pg_reassembly_fix *fixes, char *text, int64_t text_cap,
+                        int64_t *text_len);
+
 /* ---- VCF ----------------------------------------------------------------
  * The per-position records of GenomeRegion.writeVcf / Vcf.writeRecord
  * (S/GenomeRegion.scala:623-643, S/Vcf.scala:74-176) for one region of the
@@ -305,6 +358,13 @@ pg_status pg_kmer_tally_wide(pg_ctx *ctx, const pg_window *windows, int32_t n_wi
  * only records whose ALT is not "." (a delta for serving). */
 pg_status pg_format_vcf(pg_ctx *ctx, int32_t region, const char *name, int32_t diploid, int32_t vcf_qe,
                         int32_t variants_only, char *out, int64_t cap, int64_t *n_bytes);
+
+/* Marks loci first_locus .. first_locus + count - 1 of region `region` of the
+ * last pg_pileup_regions call as deleted, as GenomeRegion.writeVcf does for
+ * the bases a local-reassembly fix replaces before it writes their records
+ * (S/GenomeRegion.scala:632-638): pg_format_vcf then writes them as records
+ * inside a change (filter Del, no indel record after them). */
+pg_status pg_mark_deleted(pg_ctx *ctx, int32_t region, int32_t first_locus, int32_t count);
 
 /* ---- break candidates ---------------------------------------------------
  * GenomeRegion.possibleBreaks (S/GenomeRegion.scala:659-763) with

@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
@@ -478,6 +479,12 @@ struct Fix {
   bool operator==(const Fix& o) const { return locus == o.locus && was == o.was && patch == o.patch; }
 };
 
+struct GenomeRegion;
+// Local reassembly of one gap or break (GapFiller.fillGap / fixBreak,
+// S/GapFiller.scala:39-100); defined with the graph walk below.
+struct Reassembly;
+Fix reassemble(const GenomeRegion& g, Reassembly& ra, int32_t bs, int32_t be, bool isGap);
+
 struct GenomeRegion {
   std::string name;
   int32_t contigId;
@@ -637,8 +644,9 @@ struct GenomeRegion {
     changeMap[i] = {kind, i};
   }
 
-  // identifyAndFixIssues for fix types snps / indels / amb (:307-414)
-  void identifyAndFixIssues(bool fixSnps, bool fixIndels, bool iupac, bool longread) {
+  // identifyAndFixIssues (:307-414); ra (fix types gaps / local) may be null
+  void identifyAndFixIssues(bool fixSnps, bool fixIndels, bool iupac, bool longread, Reassembly* ra = nullptr,
+                            bool fixGaps = false, bool fixLocal = false) {
     for (auto& kv : changeMap) {
       int32_t i = kv.first;
       int kind = kv.second.first;
@@ -665,6 +673,19 @@ struct GenomeRegion {
     std::reverse(snpFixList.begin(), snpFixList.end());
     std::reverse(smallFixList.begin(), smallFixList.end());
     fixIssues(snpFixList);
+    if (ra && fixGaps) {  // :383-393, each gap in locus order
+      for (auto& gp : gaps()) {
+        Fix f = reassemble(*this, *ra, gp.first, gp.second, true);
+        if (f.locus > 0) bigFixList.push_back(f);
+      }
+    }
+    if (ra && fixLocal) {  // :396-410
+      for (auto& br : possibleBreaks()) {
+        Fix f = reassemble(*this, *ra, br.first, br.second, false);
+        if (f.locus > 0 && std::max(f.was.size(), f.patch.size()) > 10) bigFixList.push_back(f);
+      }
+    }
+    std::reverse(bigFixList.begin(), bigFixList.end());  // prepended (::=) in the reference
     std::vector<Fix> sb = smallFixList;
     sb.insert(sb.end(), bigFixList.begin(), bigFixList.end());
     fixIssues(sb);
@@ -767,13 +788,34 @@ struct GenomeRegion {
     for (int32_t i = 0; i < size(); i++) { bad += badCoverage[i]; good += coverage[i]; }
     return pctL(bad, good + bad);
   }
+  std::vector<std::pair<int32_t, int32_t>> gaps() const {  // :700
+    auto gapsR = summaryRegions([&](int32_t i) { return refBase(locus(i)) == 'N'; });
+    std::vector<std::pair<int32_t, int32_t>> out;
+    for (auto& g : gapsR)
+      if (g.second + 1 - g.first >= 10) out.push_back(g);
+    return out;
+  }
+  // :771-781: originalBaseAt, subString (current bases), refSubString (the contig)
+  char originalBaseAt(int32_t l) const {
+    if (!inRegion(l)) throw IndexError();
+    return upper((char)contigBases[l - 1]);
+  }
+  std::string subString(int32_t l, int32_t n) const {
+    if (!(inRegion(l) && inRegion(l + n - 1))) throw IndexError();
+    std::string s;
+    for (int32_t k = index(l); k < index(l + n); k++) s.push_back(upper((char)bases[k]));
+    return s;
+  }
+  std::string refSubString(int32_t l, int32_t n) const {
+    if (!(inRegion(l) && inRegion(l + n - 1))) throw IndexError();
+    std::string s;
+    for (int32_t k = l - 1; k < l + n - 1; k++) s.push_back(upper((char)contigBases[k]));
+    return s;
+  }
   std::vector<std::pair<int32_t, int32_t>> possibleBreaks() const {  // :659-720
     double mean = fragMean();
     int64_t pbo = pctBadOverall();
-    auto gapsR = summaryRegions([&](int32_t i) { return refBase(locus(i)) == 'N'; });
-    std::vector<std::pair<int32_t, int32_t>> gaps;
-    for (auto& g : gapsR)
-      if (g.second + 1 - g.first >= 10) gaps.push_back(g);
+    auto gaps = this->gaps();
     auto breakp = [&](int32_t i) {
       bool lowCov = coverage[i] < P.minMinDepth && refBase(locus(i)) != 'N';
       bool highClip = coverage[i] >= P.minMinDepth && pctI(clips[i], coverage[i]) >= 33;
@@ -934,18 +976,433 @@ struct VcfWriter {
             rb, d.second + 1 - d.first, d.second);
   }
 
-  void writeRegion(GenomeRegion& g) {  // GenomeRegion.writeVcf (:623-643), snps/indels fixes only
+  void writeFixRecord(GenomeRegion& g, const Fix& fx) {  // :178-192
+    int32_t loc = fx.locus - 1;
+    char rb = g.refBase(loc);
+    std::string ref = std::string(1, rb) + fx.was, alt = std::string(1, rb) + fx.patch;
+    int32_t svlen = (int32_t)alt.size() - (int32_t)ref.size();
+    int32_t svend = loc + (int32_t)ref.size() - 1;
+    fprintf(f, "%s\t%d\t.\t%s\t%s\t.\tPASS\tSVTYPE=%s;SVLEN=%d;END=%d%s\tGT\t1/1\n", g.name.c_str(), loc, ref.c_str(),
+            alt.c_str(), svlen < 0 ? "DEL" : "INS", svlen, svend,
+            fx.patch.find('N') != std::string::npos ? ";IMPRECISE" : "");
+  }
+
+  void writeRegion(GenomeRegion& g) {  // GenomeRegion.writeVcf (:623-643)
     std::vector<Fix> fixes = g.allFixes();
     auto dupes = g.duplicationEvents();
+    auto in = [](const std::vector<Fix>& l, const Fix& x) { return std::find(l.begin(), l.end(), x) != l.end(); };
     size_t fh = 0, dh = 0;
     for (int32_t i = 0; i < g.size(); i++) {
       int32_t loc = g.locus(i);
       if (dh < dupes.size() && dupes[dh].first == loc) { writeDup(g, dupes[dh]); dh++; }
-      if (fh < fixes.size() && fixes[fh].locus == loc) fh++;  // big fixes are out of scope here
+      if (fh < fixes.size() && fixes[fh].locus == loc) {
+        const Fix& fx = fixes[fh];
+        if (in(g.bigFixList, fx) && !in(g.smallFixList, fx)) {  // a local reassembly
+          writeFixRecord(g, fx);
+          for (size_t j = 0; j < fx.was.size(); j++) {
+            if (i + (int32_t)j >= g.size()) throw IndexError();
+            g.deleted[i + j] = 1;
+          }
+        }
+        fh++;
+      }
       writeRecord(g, i, g.deleted[i] != 0, true);
     }
   }
 };
+
+// ---- Local reassembly ---------------------------------------------------------
+// BamFile.scan / MateMap / recruitment (S/BamFile.scala:156-220, 222-403), the
+// Assembler's K-mer tally and graph walk (S/Assembler.scala:46-284) and the
+// GapFiller (S/GapFiller.scala:28-402) for one BAM of type frags or unpaired.
+// Read names are given as ids (mates share an id); Pilon.trSafe is always
+// true and Pilon.multiClosure / fixBreaks / fixNovel are off (their defaults).
+
+static double isMean(const InsertStats& s) {  // :167
+  return s.count > 0 ? (double)s.sum / (double)s.count : 0.0;
+}
+static double isSigma(const InsertStats& s) {  // :169-173
+  if (s.sum > 0) return std::sqrt(std::fabs((double)s.sumSq / (double)s.count - isMean(s) * isMean(s)));
+  return 0.0;
+}
+static int32_t isMaxInsert(const InsertStats& s) {  // :181-183
+  return s.count > 1000 ? javaL2I(javaRound(isMean(s) + 3.0 * isSigma(s))) : 0;
+}
+
+static std::string revComp(const std::string& s) {  // S/Bases.scala:28-40
+  std::string r(s.rbegin(), s.rend());
+  for (auto& c : r) c = c == 'A' ? 'T' : c == 'C' ? 'G' : c == 'G' ? 'C' : c == 'T' ? 'A' : c;
+  return r;
+}
+
+// Assembler.addReads + buildGraph (S/Assembler.scala:46-87, 132-154) over reads
+// `idx` in that order; returns the K-mer -> pileup map before the depth filter.
+static std::unordered_map<std::string, PileUp> tallyReads(const pg_reads* R, const Params& P, const int64_t* idx,
+                                                          int64_t n, int32_t K) {
+  std::unordered_map<std::string, PileUp> pileups;
+  int64_t nReads = 0;
+  auto addToPileups = [&](const std::string& b, const std::vector<int32_t>& q, int32_t mq) {
+    int32_t length = (int32_t)b.size();
+    for (int32_t off = 0; off <= length - K - 1; off++) {
+      PileUp& pu = pileups[b.substr(off, K)];
+      pu.add(b[off + K], q[off + K], mq, P);
+    }
+  };
+  for (int64_t t = 0; t < n; t++) {
+    ReadView rv{R, idx[t]};
+    std::string b = rv.length() > 0 ? rv.bases() : std::string("*");
+    int32_t length = (int32_t)b.size();
+    if (length > K) {
+      std::vector<int32_t> q(length);
+      for (int32_t k = 0; k < length; k++) q[k] = rv.qual(k, P);
+      int32_t mq = rv.mq();
+      addToPileups(b, q, mq);
+      std::vector<int32_t> rq(q.rbegin(), q.rend());
+      addToPileups(revComp(b), rq, mq);
+      nReads++;
+      if (nReads % 100000 == 0) {  // prunePileups(2)
+        for (auto it = pileups.begin(); it != pileups.end();)
+          if (it->second.count() < 2) it = pileups.erase(it); else ++it;
+      }
+    }
+  }
+  return pileups;
+}
+
+struct Reassembly {
+  const pg_reads* R;
+  const int64_t* nameId;  // the read name of each read as an id; null: no names (no stray mates)
+  const Params& P;
+  int32_t K;
+  bool strays;
+  InsertStats fr, rf, un;  // insertStatsFR / RF / Unpaired: the scan plus every region processed so far
+  std::unordered_map<int64_t, int64_t> stray1, stray2;  // strayMateMap readMap1 / readMap2 (:222-281)
+  std::vector<int64_t> cb, ce;                           // each contig's read range
+  std::vector<int32_t> span;                             // longest alignment span of each contig's reads
+  int64_t tiedSets = 0;  // solution sets of more than four with tied lengths (see breakJoins)
+
+  Reassembly(const pg_reads* r, const int64_t* names, const Params& p, int32_t k, int32_t nContigs)
+      : R(r), nameId(names), P(p), K(k), strays(names != nullptr) {
+    cb.assign(nContigs, 0); ce.assign(nContigs, 0); span.assign(nContigs, 1);
+    int64_t i = 0;
+    for (int32_t c = 0; c < nContigs; c++) {
+      while (i < R->n_reads && R->ref_id[i] < c) i++;
+      cb[c] = i;
+      while (i < R->n_reads && R->ref_id[i] == c) {
+        int32_t e = (R->flag[i] & 0x4) ? R->pos[i] : R->aend[i];
+        span[c] = std::max(span[c], e - R->pos[i] + 1);
+        i++;
+      }
+      ce[c] = i;
+    }
+    scan(nContigs);
+  }
+  void addInsert(int32_t insertSize, bool rc, bool unpaired) {  // :194-202
+    bool frr = (insertSize > 0) ^ rc;
+    if (insertSize > 0 && insertSize < hugeInsert(P.bamType)) {
+      if (unpaired) un.add(insertSize); else if (frr) fr.add(insertSize); else rf.add(insertSize);
+    }
+  }
+  void scan(int32_t nContigs) {  // :295-337 (every contig is of interest)
+    for (int64_t i = 0; i < R->n_reads; i++) {
+      uint16_t fl = R->flag[i];
+      if (!validateRead(fl, P) || (fl & 0x4)) continue;
+      if (fl & 0x1) {
+        if (fl & 0x2) addInsert(R->tlen[i], fl & 0x10, false);
+        else if (strays && !(fl & 0x8)) {
+          bool soi = (R->ref_id[i] >= 0 && R->ref_id[i] < nContigs) ||
+                     (R->mate_ref_id[i] >= 0 && R->mate_ref_id[i] < nContigs);
+          if (soi) ((fl & 0x40) ? stray1 : stray2)[nameId[i]] = i;
+        }
+      } else {
+        addInsert(R->l_seq[i], fl & 0x10, true);
+      }
+    }
+  }
+  void addRegion(const GenomeRegion& g) {  // BamFile.process's addInsert calls (:137)
+    fr.count += g.fr.count; fr.sum += g.fr.sum; fr.sumSq += g.fr.sumSq;
+    rf.count += g.rf.count; rf.sum += g.rf.sum; rf.sumSq += g.rf.sumSq;
+  }
+  int64_t pctFR() const { return pctL(fr.count, fr.count + rf.count + un.count); }  // :204
+  double insertSizeMean() const { return pctFR() >= 50 ? isMean(fr) : isMean(rf); }  // :208-210
+  int32_t maxInsertSize() const {  // :216-220
+    int32_t m = std::max(isMaxInsert(fr), std::max(isMaxInsert(rf), isMaxInsert(un)));
+    return m > 0 ? m : (P.bamType == PG_BAM_FRAGS ? 500 : 10000);
+  }
+  int32_t breakRadius() const {  // S/GapFiller.scala:357-362 (one frags BAM, or none)
+    int32_t insertMean = P.bamType == PG_BAM_FRAGS ? javaL2I(javaRound(insertSizeMean())) : 0;
+    return std::max(3 * K, insertMean);
+  }
+  std::vector<int64_t> readsInRegion(int32_t c, int32_t s, int32_t e) const {  // :339-344
+    // queryOverlapping: the alignment [start, end] (end = start when unmapped) meets [s, e]
+    const int32_t* pos = R->pos;
+    int64_t lo = std::lower_bound(pos + cb[c], pos + ce[c], (int64_t)s - span[c]) - pos;
+    int64_t hi = std::upper_bound(pos + cb[c], pos + ce[c], e) - pos;
+    std::vector<int64_t> out;
+    for (int64_t i = lo; i < hi; i++) {
+      int32_t end = (R->flag[i] & 0x4) ? R->pos[i] : R->aend[i];
+      if (R->pos[i] <= e && end >= s && validateRead(R->flag[i], P)) out.push_back(i);
+    }
+    return out;
+  }
+  std::vector<int64_t> recruitReads(int32_t c, int32_t s, int32_t e) const {
+    // GapFiller.recruitReads (S/GapFiller.scala:364-402) -> recruitFlankReads (S/BamFile.scala:346-364)
+    if (P.bamType == PG_BAM_UNPAIRED && P.longRead) return {};  // recruitUnpaired with --nanopore/--pacbio
+    int32_t flank = maxInsertSize();
+    std::vector<int64_t> reads = readsInRegion(c, std::max(s - flank, 1), e + flank);
+    if (strays && P.bamType != PG_BAM_UNPAIRED) {  // MateMap(reads).findStrays (:244-257)
+      std::unordered_map<int64_t, int64_t> m1, m2;
+      for (int64_t i : reads) ((R->flag[i] & 0x40) ? m1 : m2)[nameId[i]] = i;
+      std::vector<int64_t> found;
+      for (auto& kv : m1)
+        if (!m2.count(kv.first)) { auto it = stray2.find(kv.first); if (it != stray2.end()) found.push_back(it->second); }
+      for (auto& kv : m2)
+        if (!m1.count(kv.first)) {
+          auto& sm = (R->flag[kv.second] & 0x40) ? stray2 : stray1;
+          auto it = sm.find(kv.first);
+          if (it != sm.end()) found.push_back(it->second);
+        }
+      // appended in HashMap order in the reference; the tally does not depend on it
+      std::sort(found.begin(), found.end());
+      reads.insert(reads.end(), found.begin(), found.end());
+    }
+    return reads;
+  }
+};
+
+// The K-mer graph walk of one Assembler (S/Assembler.scala:164-284).
+struct GraphWalk {
+  std::unordered_map<std::string, std::string> kGraph, altGraph;
+  int32_t K;
+  int32_t loopLength = 0;
+  std::string loopSequence;
+
+  // A K-mer path: the reference's List has its newest K-mer at the head; here
+  // km is oldest first, with each K-mer's count and latest position.
+  struct Path {
+    std::vector<std::string> km;
+    std::unordered_map<std::string, std::pair<int32_t, int32_t>> at;
+    void push(const std::string& k) {
+      auto& e = at[k];
+      e.first++;
+      e.second = (int32_t)km.size();
+      km.push_back(k);
+    }
+    int32_t indexOf(const std::string& k) const {  // List.indexOf from the head
+      auto it = at.find(k);
+      return it == at.end() ? -1 : (int32_t)km.size() - 1 - it->second.second;
+    }
+    bool tailContains(const std::string& k) const {  // kmers.tail contains k
+      auto it = at.find(k);
+      if (it == at.end()) return false;
+      return it->second.first - (km.back() == k ? 1 : 0) > 0;
+    }
+  };
+
+  static std::string pathString(const std::vector<std::string>& km, size_t from) {  // kmerPathString (:164-171)
+    std::string s = km[from];
+    for (size_t i = from + 1; i < km.size(); i++) s.push_back(km[i].back());
+    return s;
+  }
+  void noteKmerLoop(int32_t loopIndex, const Path& p) {  // :173-181
+    int32_t length = loopIndex + 1;
+    if (loopLength == 0 || length < loopLength) {
+      loopLength = length;
+      loopSequence = pathString(p.km, p.km.size() - (size_t)length).substr(0, (size_t)length);
+    }
+  }
+  void pathsForwardFrom(Path p, int32_t branches, std::vector<Path>& out) {  // kmerPathsForward (:183-234)
+    while (true) {
+      const std::string kmer = p.km.back();
+      auto g = kGraph.find(kmer);
+      if (g == kGraph.end()) { out.push_back(std::move(p)); return; }
+      auto a = altGraph.find(kmer);
+      if (a != altGraph.end()) {
+        const std::string next1 = g->second, next2 = a->second;
+        bool seen1 = p.tailContains(next1), seen2 = p.tailContains(next2);
+        if (seen1 || seen2) {
+          noteKmerLoop(std::max(p.indexOf(next1), p.indexOf(next2)), p);
+          out.push_back(std::move(p));  // trSafe
+          return;
+        }
+        if (branches < 5) {  // maxBranches
+          Path p2 = p;
+          p.push(next1);
+          pathsForwardFrom(std::move(p), branches + 1, out);
+          p2.push(next2);
+          pathsForwardFrom(std::move(p2), branches + 1, out);
+        } else {
+          out.push_back(std::move(p));
+        }
+        return;
+      }
+      const std::string next = g->second;
+      int32_t loop = p.indexOf(next);
+      if (loop >= 0) {
+        noteKmerLoop(loop, p);
+        out.push_back(std::move(p));  // trSafe
+        return;
+      }
+      p.push(next);
+    }
+  }
+  std::vector<std::string> pathsForward(const std::string& start) {  // :236-247
+    Path p;
+    p.push(start);
+    std::vector<Path> kp;
+    pathsForwardFrom(std::move(p), 0, kp);
+    std::vector<std::string> paths;
+    for (auto& q : kp) paths.push_back(pathString(q.km, 0));
+    std::stable_sort(paths.begin(), paths.end(), [](const std::string& a, const std::string& b) {
+      return a.size() > b.size();
+    });
+    return paths;
+  }
+  std::vector<std::string> tryForward(const std::string& anchor) {  // :254-267
+    if ((int32_t)anchor.size() < K) return {anchor};
+    std::string startingKmer = anchor.substr(0, K);
+    std::vector<std::string> paths = pathsForward(startingKmer);
+    if (!paths.empty() && paths[0].size() > anchor.size() + 20) return paths;  // minExtend
+    std::vector<std::string> out;
+    for (auto& p : tryForward(anchor.substr(K))) out.push_back(startingKmer + p);
+    return out;
+  }
+  std::vector<std::string> tryReverse(const std::string& anchor) {  // :269-278
+    std::vector<std::string> out;
+    for (auto& p : tryForward(revComp(anchor))) out.push_back(revComp(p));
+    return out;
+  }
+};
+
+// properOverlap (S/GapFiller.scala:220-245)
+static std::string properOverlap(const std::string& left, const std::string& right, int32_t minOverlap) {
+  int32_t ll = (int32_t)left.size(), rl = (int32_t)right.size();
+  for (int32_t overlap = minOverlap; overlap <= ll + rl - 2 * minOverlap; overlap++) {
+    int32_t lo = std::max(ll - overlap, 0), ro = std::max(overlap - ll, 0);
+    int32_t len = std::min(ll - lo, rl - ro);
+    bool match = true;
+    for (int32_t i = 0; i < len; i++)
+      if (left[lo + i] != right[ro + i]) { match = false; break; }
+    if (match) return left.substr(0, lo) + right.substr(ro);
+  }
+  return "";
+}
+
+// trimPatch (S/GapFiller.scala:247-262)
+static Fix trimPatch(const GenomeRegion& g, int32_t start, std::string patch, int32_t stop) {
+  while (start < stop && !patch.empty() && (g.baseAt(start) == patch[0] || g.originalBaseAt(start) == patch[0])) {
+    start++;
+    patch.erase(0, 1);
+  }
+  while (start < stop && !patch.empty() &&
+         (g.baseAt(stop - 1) == patch.back() || g.originalBaseAt(stop - 1) == patch.back())) {
+    stop--;
+    patch.pop_back();
+  }
+  return Fix{start, g.refSubString(start, stop - start), patch, 2};
+}
+
+static std::string consensusFromLeft(const std::vector<std::string>& seqs) {  // :102-110
+  const std::string& s0 = seqs.front();
+  if (seqs.size() == 1) return s0;
+  size_t minLength = s0.size();
+  for (auto& s : seqs) minLength = std::min(minLength, s.size());
+  for (size_t i = 0; i < minLength; i++)
+    for (size_t k = 1; k < seqs.size(); k++)
+      if (seqs[k][i] != s0[i]) return s0.substr(0, i);
+  return s0.substr(0, minLength);
+}
+static std::string consensusFromRight(const std::vector<std::string>& seqs) {  // :112-123
+  const std::string& s0 = seqs.front();
+  if (seqs.size() == 1) return s0;
+  size_t minLength = s0.size();
+  for (auto& s : seqs) minLength = std::min(minLength, s.size());
+  for (size_t i = 0; i < minLength; i++)
+    for (size_t k = 1; k < seqs.size(); k++) {
+      size_t si = seqs[k].size() - 1 - i, s0i = s0.size() - 1 - i;
+      if (seqs[k][si] != s0[s0i]) return s0.substr(s0i + 1);
+    }
+  return s0.substr(s0.size() - minLength);
+}
+
+// GapFiller.assembleAcrossBreak (S/GapFiller.scala:49-100) with
+// assembleIntoBreak (:125-159) and breakJoins / joinBreak (:161-218).
+Fix reassemble(const GenomeRegion& g, Reassembly& ra, int32_t bs, int32_t be, bool isGap) {
+  const Fix noSolution{0, "", "", 2};
+  std::vector<int64_t> reads = ra.recruitReads(g.contigId, bs, be);
+  GraphWalk w;
+  w.K = ra.K;
+  {
+    auto pileups = tallyReads(ra.R, ra.P, reads.data(), (int64_t)reads.size(), ra.K);
+    for (auto& kv : pileups) {
+      const PileUp& pu = kv.second;
+      if (pu.depth() >= 5) {  // Assembler.minDepth
+        BaseCall bc = baseCall(pu, ra.P);
+        std::string prefix = kv.first.substr(1);
+        w.kGraph[kv.first] = prefix + bc.base;
+        if (!bc.homo) w.altGraph[kv.first] = prefix + bc.altBase;
+      }
+    }
+  }
+  int32_t radius = ra.breakRadius();
+  int32_t start = std::max(bs - radius, g.start);
+  int32_t stop = std::min(be + 1 + radius, g.stop);
+  std::string left = g.subString(start, bs - start);
+  std::string right = g.subString(be + 1, stop - be - 1);
+  std::vector<std::string> pathsFromLeft = w.tryForward(left);
+  std::vector<std::string> pathsFromRight = w.tryReverse(right);
+  const std::string& loop = w.loopSequence;
+  // breakJoins: a Set of solutions (insertion order for up to four elements)
+  std::vector<Fix> set;
+  int32_t k = 2 * ra.K + 1;  // GapFiller.k
+  for (auto& f : pathsFromLeft)
+    for (auto& r : pathsFromRight) {
+      std::string patch = properOverlap(f, r, k);
+      if (patch.empty()) continue;
+      Fix s = trimPatch(g, start, patch, stop);
+      if (std::find(set.begin(), set.end(), s) == set.end()) set.push_back(s);
+    }
+  std::vector<Fix> solutions = set;
+  std::stable_sort(solutions.begin(), solutions.end(), [](const Fix& a, const Fix& b) {
+    return a.patch.size() + a.was.size() < b.patch.size() + b.was.size();
+  });
+  std::vector<int64_t> lengths;
+  for (auto& s : set) {
+    int64_t d = (int64_t)s.patch.size() - (int64_t)s.was.size();
+    if (std::find(lengths.begin(), lengths.end(), d) == lengths.end()) lengths.push_back(d);
+  }
+  if (lengths.size() == 1) {
+    if (set.size() > 4 && solutions.size() > 1 &&
+        solutions[1].patch.size() + solutions[1].was.size() == solutions[0].patch.size() + solutions[0].was.size())
+      ra.tiedSets++;  // the reference takes the first of a HashSet's order here
+    solutions.resize(1);
+  }
+  Fix solution = solutions.size() == 1 ? solutions[0] : noSolution;
+  bool solutionOK = !(solution == noSolution) && loop.empty();
+  if (solutionOK && isGap) {
+    int64_t closedDiff = std::llabs((int64_t)solution.patch.size() - (int64_t)(be + 1 - bs));
+    if (closedDiff > 100000) solutionOK = false;  // Pilon.gapMargin
+  }
+  if (solutionOK) return solution;
+  if (!isGap) return noSolution;  // Pilon.fixBreaks is off
+  std::string fromRight = consensusFromRight(pathsFromRight);
+  std::string fromLeft = consensusFromLeft(pathsFromLeft);
+  int32_t newStart = start + (int32_t)fromLeft.size();
+  int32_t newStop = stop - (int32_t)fromRight.size();
+  auto partialMatchesReference = [&]() {  // :264-281
+    if (start + (int32_t)fromLeft.size() > g.stop || stop - (int32_t)fromRight.size() < g.start) return false;
+    std::string regionLeft = g.subString(start, (int32_t)fromLeft.size());
+    std::string regionRight = g.subString(stop - (int32_t)fromRight.size(), (int32_t)fromRight.size());
+    return fromLeft == regionLeft && fromRight == regionRight;
+  };
+  if ((newStart >= bs + 20 || newStop <= be - 20) && !partialMatchesReference()) {  // GapFiller.minExtend
+    int32_t newGapLength = std::max(10, newStop - newStart);  // Pilon.minGap
+    std::string seq = fromLeft + std::string((size_t)newGapLength, 'N') + fromRight;
+    Fix s = trimPatch(g, start, seq, stop);
+    return s.patch.empty() ? noSolution : s;
+  }
+  return noSolution;
+}
 
 std::string regionString(const std::string& name, int32_t s, int32_t e) {  // S/Region.scala:45
   int32_t size = e + 1 - s;
@@ -1057,13 +1514,17 @@ int32_t or_contig_regions(int64_t contig_len, int32_t chunk_size, int32_t* start
 // GenomeFile.processRegions (S/GenomeFile.scala:84-176) for one BAM, writing the
 // FASTA, VCF and changes files the reference writes.  Gap filling and local
 // reassembly are not part of this oracle.
-int or_polish(const pg_reads* R, const pg_params* params, int32_t n_contigs, const char* const* names,
-              const int64_t* lens, const uint8_t* const* bases, int32_t chunk_size, int32_t fix_snps,
-              int32_t fix_indels, int32_t iupac, int32_t diploid, int32_t vcf_qe, const char* fasta_path,
-              const char* vcf_path, const char* changes_path, const char* vcf_date, const char* vcf_source,
-              const char* vcf_args, const char* vcf_ref) {
+static int polishImpl(const pg_reads* R, const pg_params* params, int32_t n_contigs, const char* const* names,
+                      const int64_t* lens, const uint8_t* const* bases, int32_t chunk_size, int32_t fix_snps,
+                      int32_t fix_indels, int32_t iupac, int32_t diploid, int32_t vcf_qe, const char* fasta_path,
+                      const char* vcf_path, const char* changes_path, const char* vcf_date, const char* vcf_source,
+                      const char* vcf_args, const char* vcf_ref, int32_t fix_gaps, int32_t fix_local, int32_t K,
+                      const int64_t* name_id, int64_t* tied_sets) {
   Params P = toParams(params);
   try {
+    // BamFile.scan runs first when strays are tracked (S/GenomeFile.scala:89-92)
+    std::unique_ptr<Reassembly> ra;
+    if (fix_gaps || fix_local) ra.reset(new Reassembly(R, name_id, P, K, n_contigs));
     // region read ranges: reads are sorted by (ref_id, pos); take each contig's span
     std::vector<int64_t> cb(n_contigs, 0), ce(n_contigs, 0);
     {
@@ -1086,9 +1547,11 @@ int or_polish(const pg_reads* R, const pg_params* params, int32_t n_contigs, con
     for (int32_t c = 0; c < n_contigs; c++)
       for (GenomeRegion* g : regs[c]) {
         g->processBam(R, cb[c], ce[c]);
+        if (ra) ra->addRegion(*g);
         g->postProcess();
-        g->identifyAndFixIssues(fix_snps, fix_indels, iupac, P.longRead != 0);
+        g->identifyAndFixIssues(fix_snps, fix_indels, iupac, P.longRead != 0, ra.get(), fix_gaps, fix_local);
       }
+    if (ra && tied_sets) *tied_sets = ra->tiedSets;
     FILE* fc = changes_path ? fopen(changes_path, "w") : nullptr;
     FILE* ff = fasta_path ? fopen(fasta_path, "w") : nullptr;
     FILE* fv = vcf_path ? fopen(vcf_path, "w") : nullptr;
@@ -1140,6 +1603,39 @@ int or_polish(const pg_reads* R, const pg_params* params, int32_t n_contigs, con
     return PG_ERR_INDEX;
   }
   return 0;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// Whole-genome polish (GenomeFile.processRegions, S/GenomeFile.scala:84-176)
+// with --fix snps,indels[,amb] --vcf --changes.
+int or_polish(const pg_reads* R, const pg_params* params, int32_t n_contigs, const char* const* names,
+              const int64_t* lens, const uint8_t* const* bases, int32_t chunk_size, int32_t fix_snps,
+              int32_t fix_indels, int32_t iupac, int32_t diploid, int32_t vcf_qe, const char* fasta_path,
+              const char* vcf_path, const char* changes_path, const char* vcf_date, const char* vcf_source,
+              const char* vcf_args, const char* vcf_ref) {
+  return polishImpl(R, params, n_contigs, names, lens, bases, chunk_size, fix_snps, fix_indels, iupac, diploid,
+                    vcf_qe, fasta_path, vcf_path, changes_path, vcf_date, vcf_source, vcf_args, vcf_ref, 0, 0, 31,
+                    nullptr, nullptr);
+}
+
+// The same with the fix types gaps and local as well (GapFiller fillGap /
+// fixBreak, S/GenomeRegion.scala:382-410): K is Assembler.K (--K), name_id the
+// read name of each read as an id (mates share one; NULL: no stray mates, as
+// --nostrays).  *tied_sets receives the count of solution sets of more than
+// four elements whose first element had to be taken in an order the reference
+// gets from its HashSet (see reassemble).
+int or_polish_fix(const pg_reads* R, const pg_params* params, int32_t n_contigs, const char* const* names,
+                  const int64_t* lens, const uint8_t* const* bases, int32_t chunk_size, int32_t fix_snps,
+                  int32_t fix_indels, int32_t iupac, int32_t diploid, int32_t vcf_qe, const char* fasta_path,
+                  const char* vcf_path, const char* changes_path, const char* vcf_date, const char* vcf_source,
+                  const char* vcf_args, const char* vcf_ref, int32_t fix_gaps, int32_t fix_local, int32_t K,
+                  const int64_t* name_id, int64_t* tied_sets) {
+  return polishImpl(R, params, n_contigs, names, lens, bases, chunk_size, fix_snps, fix_indels, iupac, diploid,
+                    vcf_qe, fasta_path, vcf_path, changes_path, vcf_date, vcf_source, vcf_args, vcf_ref, fix_gaps,
+                    fix_local, K, name_id, tied_sets);
 }
 
 // One --targets region end to end (S/GenomeFile.scala:215-250): processBam,

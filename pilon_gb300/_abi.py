@@ -128,6 +128,21 @@ class pg_result(C.Structure):
     ]
 
 
+class pg_reassembly(C.Structure):
+    _fields_ = [
+        ("window", C.c_int32), ("is_gap", C.c_int32), ("region_start", C.c_int32), ("region_stop", C.c_int32),
+        ("break_start", C.c_int32), ("break_stop", C.c_int32), ("break_radius", C.c_int32), ("pad_", C.c_int32),
+        ("bases", C.c_void_p), ("orig", C.c_void_p),
+    ]
+
+
+class pg_reassembly_fix(C.Structure):
+    _fields_ = [
+        ("start", C.c_int32), ("status", C.c_int32), ("loop_len", C.c_int32), ("pad_", C.c_int32),
+        ("was_off", C.c_int64), ("was_len", C.c_int64), ("patch_off", C.c_int64), ("patch_len", C.c_int64),
+    ]
+
+
 class pg_break(C.Structure):
     _fields_ = [("region", C.c_int32), ("start", C.c_int32), ("stop", C.c_int32), ("pad_", C.c_int32)]
 
@@ -174,7 +189,8 @@ EXPORTED = [
     "pg_kmer_tally_breaks", "pg_fetch_all", "pg_graph_replays", "pg_last_tally_stats",
     "pg_find_duplications", "pg_kmer_tally_wide", "pg_kmer_tally_breaks_wide", "pg_fetch_changes",
     "pg_default_serve_config", "pg_serve_open", "pg_serve_submit", "pg_serve_poll", "pg_serve_release",
-    "pg_serve_stats", "pg_serve_error", "pg_serve_close",
+    "pg_serve_stats", "pg_serve_error", "pg_serve_close", "pg_kmer_tally_reads", "pg_reassemble",
+    "pg_mark_deleted",
 ]
 
 PG_STATIC_SCAN_MAX_POSITIONS = 16777216

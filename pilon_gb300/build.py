@@ -23,6 +23,7 @@ BAMLIB = os.path.join(BUILD, "libpg_bam.so")
 
 CU_SOURCES = ["pg_api.cu", "pg_pileup.cu", "pg_call.cu", "pg_kmer.cu", "pg_format.cu", "pg_noalloc.cu",
               "pg_breaks.cu", "pg_serve.cu"]
+CPP_SOURCES = ["pg_assemble.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-fwrapv", "--expt-relaxed-constexpr"]
 
@@ -64,6 +65,13 @@ def build(force=False, verbose=False):
         objs.append(obj)
         if force or not _newer(obj, [src] + headers):
             cmds.append([nvcc] + NVCC_FLAGS + ["-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj])
+    for s in CPP_SOURCES:  # host-only parts of the engine library
+        src = os.path.join(CSRC, s)
+        obj = os.path.join(BUILD, s.replace(".cpp", ".o"))
+        objs.append(obj)
+        if force or not _newer(obj, [src] + headers):
+            cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-fwrapv", "-I", INCLUDE, "-c", src,
+                         "-o", obj])
     synth_src = os.path.join(CSRC, "synth.cpp")
     if force or not _newer(SYNTH, [synth_src]):
         cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", synth_src, "-o", SYNTH])
@@ -77,7 +85,7 @@ def build(force=False, verbose=False):
         _run_all(cmds)
     if force or not _newer(ENGINE, objs):
         _run_all([[nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", ENGINE] + objs
-                  + ["-lcudart", "-ldl"]])
+                  + ["-lcudart", "-ldl", "-Xcompiler", "-pthread"]])
     return ENGINE
 
 

@@ -79,7 +79,7 @@ struct pg_ctx {
   // k-mer tally
   DevBuf kwin, kpre, kslot_base, kslot_cap, kx_base, kx_cap, kslots, kwlist;
   DevBuf kx_keys, kx_used, kx_cnt, kx_qs, kx_q, kedges, kcount, kx_ev, kx_evbase, kx_evcap, kx_evfill;
-  DevBuf kwflag, kused, kchunks;
+  DevBuf kwflag, kused, kchunks, klist;
   double tally_ms = 0;  // kernel time of the last tally (CUDA events)
   int64_t tally_events = 0, tally_distinct = 0, tally_max_batch_bytes = 0;
   int32_t tally_batches = 0;
@@ -287,7 +287,7 @@ void pg_close(pg_ctx* c) {
   DevBuf* km[] = {&c->kwin, &c->kpre, &c->kslot_base, &c->kslot_cap, &c->kx_base, &c->kx_cap, &c->kslots, &c->kwlist,
                   &c->kx_keys, &c->kx_used, &c->kx_cnt, &c->kx_qs, &c->kx_q,
                   &c->kedges, &c->kcount, &c->kx_ev, &c->kx_evbase, &c->kx_evcap, &c->kx_evfill, &c->kwflag,
-                  &c->kused, &c->kchunks, &c->vlen,
+                  &c->kused, &c->kchunks, &c->klist, &c->vlen,
                   &c->vsums, &c->vtext, &c->vname, &c->bfrag, &c->bsums, &c->btiles, &c->bgaps, &c->bruns,
                   &c->bcnt, &c->boff, &c->bout, &c->druns, &c->dout, &c->dcount, &c->chg_count, &c->chg_off,
                   &c->chg_out};
@@ -912,10 +912,10 @@ static int64_t next_pow2(int64_t x) {
 }
 
 static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_params* params, int32_t min_depth,
-                           bool wide, void* edges, int64_t cap, int64_t* n_edges);
+                           bool wide, void* edges, int64_t cap, int64_t* n_edges, const int64_t* rlist = nullptr);
 static pg_status kmer_windows(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K,
                               const pg_params* params, int32_t min_depth, bool wide, void* edges, int64_t cap,
-                              int64_t* n_edges);
+                              int64_t* n_edges, int64_t n_list = 0, const int64_t* rlist = nullptr);
 
 pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K, const pg_params* params,
                         int32_t min_depth, pg_kmer_edge* edges, int64_t cap, int64_t* n_edges) {
@@ -934,9 +934,31 @@ pg_status pg_kmer_tally_wide(pg_ctx* c, const pg_window* windows, int32_t n_wind
   return kmer_windows(c, windows, n_windows, K, params, min_depth, true, edges, cap, n_edges);
 }
 
+pg_status pg_kmer_tally_reads(pg_ctx* c, const int64_t* reads, int64_t n_reads, const pg_window* windows,
+                              int32_t n_windows, int32_t K, const pg_params* params, int32_t min_depth,
+                              pg_kmer_edge_wide* edges, int64_t cap, int64_t* n_edges) {
+  const Range nvtx_range("pg_kmer_tally_reads");
+  if (!c) return PG_ERR_ARG;
+  if (K < 1 || K > 63) return fail(c, PG_ERR_LIMIT, "K = %d: pg_kmer_tally_reads takes K <= 63", K);
+  if (n_reads < 0 || (n_reads > 0 && !reads) || (n_windows > 0 && !windows) || n_windows < 0)
+    return fail(c, PG_ERR_ARG, "bad arguments");
+  if (!c->have_reads) return fail(c, PG_ERR_STATE, "pg_set_reads must come first");
+  for (int64_t k = 0; k < n_reads; k++)
+    if (reads[k] < 0 || reads[k] >= c->R.n) return fail(c, PG_ERR_ARG, "read list entry %lld out of bounds", (long long)k);
+  for (int32_t w = 0; w < n_windows; w++)
+    if (windows[w].read_begin < 0 || windows[w].read_end < windows[w].read_begin || windows[w].read_end > n_reads)
+      return fail(c, PG_ERR_ARG, "window %d: range outside the read list", w);
+  cudaSetDevice(c->device);
+  pg_status s;
+  if ((s = ensure(c, c->klist, 8 * (size_t)std::max<int64_t>(n_reads, 1)))) return s;
+  if (n_reads > 0) CK(cudaMemcpyAsync(c->klist.p, reads, 8 * (size_t)n_reads, cudaMemcpyHostToDevice, c->stream));
+  return kmer_windows(c, windows, n_windows, K, params, min_depth, true, edges, cap, n_edges, n_reads,
+                      P<int64_t>(c->klist));
+}
+
 static pg_status kmer_windows(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K,
                               const pg_params* params, int32_t min_depth, bool wide, void* edges, int64_t cap,
-                              int64_t* n_edges) {
+                              int64_t* n_edges, int64_t n_list, const int64_t* rlist) {
   if (!c || (n_windows > 0 && !windows) || !params || n_windows < 0 || cap < 0 || !n_edges)
     return fail(c, PG_ERR_ARG, "bad arguments");
   if (min_depth < 1) return fail(c, PG_ERR_ARG, "min_depth must be >= 1");
@@ -946,13 +968,14 @@ static pg_status kmer_windows(pg_ctx* c, const pg_window* windows, int32_t n_win
   cudaSetDevice(c->device);
   *n_edges = 0;
   if (n_windows == 0) return PG_OK;
+  const int64_t n_idx = rlist ? n_list : c->R.n;
   for (int32_t w = 0; w < n_windows; w++)
-    if (windows[w].read_begin < 0 || windows[w].read_end < windows[w].read_begin || windows[w].read_end > c->R.n)
+    if (windows[w].read_begin < 0 || windows[w].read_end < windows[w].read_begin || windows[w].read_end > n_idx)
       return fail(c, PG_ERR_ARG, "window %d: read range out of bounds", w);
   pg_status s;
   if ((s = ensure(c, c->kwin, sizeof(pg_window) * n_windows))) return s;
   CK(cudaMemcpyAsync(c->kwin.p, windows, sizeof(pg_window) * n_windows, cudaMemcpyHostToDevice, c->stream));
-  return kmer_core(c, n_windows, K, params, min_depth, wide, edges, cap, n_edges);
+  return kmer_core(c, n_windows, K, params, min_depth, wide, edges, cap, n_edges, rlist);
 }
 
 // The tally over the n_windows windows in c->kwin (device).
@@ -971,7 +994,7 @@ constexpr int64_t kTallyBatchBytes = (int64_t)64 << 20;
 constexpr int64_t kTallyReadsPerChunk = 8;
 
 static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_params* params, int32_t min_depth,
-                           bool wide, void* edges, int64_t cap, int64_t* n_edges) {
+                           bool wide, void* edges, int64_t cap, int64_t* n_edges, const int64_t* rlist) {
   cudaStream_t st = c->stream;
   // bytes per slot: KmerSlot / KmerSlotWide; exotic slots hold 2 or 4 key words, a used byte and
   // the counters (rounded up)
@@ -983,7 +1006,7 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
   c->tally_events = c->tally_distinct = c->tally_max_batch_bytes = 0;
   c->tally_batches = 0;
   if ((s = ensure(c, c->kpre, sizeof(long long) * 3 * n_windows))) return s;
-  launch_kmer_prepass(c->R, P<pg_window>(c->kwin), n_windows, K, P<long long>(c->kpre), st);
+  launch_kmer_prepass(c->R, P<pg_window>(c->kwin), rlist, n_windows, K, P<long long>(c->kpre), st);
   std::vector<long long> pre(3 * (size_t)n_windows);
   std::vector<pg_window> wins(n_windows);
   CK(cudaMemcpyAsync(pre.data(), c->kpre.p, sizeof(long long) * pre.size(), cudaMemcpyDeviceToHost, st));
@@ -1030,7 +1053,7 @@ static pg_status kmer_core(pg_ctx* c, int32_t n_windows, int32_t K, const pg_par
   std::vector<KmerChunk> chunks;
   std::vector<Batch> batches;
   KmerArgs a;
-  a.R = c->R; a.K = K; a.wide = wide;
+  a.R = c->R; a.rlist = rlist; a.K = K; a.wide = wide;
   a.min_qual = params->min_qual; a.default_qual = params->default_qual; a.min_depth = min_depth;
   a.full = P<int32_t>(c->kwflag); a.used = P<unsigned long long>(c->kused);
   a.slot_base = P<int64_t>(c->kslot_base); a.slot_cap = P<int64_t>(c->kslot_cap);
@@ -1277,6 +1300,21 @@ static pg_status kmer_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius, i
                        P<pg_window>(c->kwin), c->stream);
   CK(cudaGetLastError());
   return kmer_core(c, n, K, params, min_depth, wide, edges, cap, n_edges);
+}
+
+pg_status pg_mark_deleted(pg_ctx* c, int32_t r, int32_t first_locus, int32_t count) {
+  if (!c || count < 0) return fail(c, PG_ERR_ARG, "bad arguments");
+  if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
+  if (r < 0 || r >= c->n_regions) return fail(c, PG_ERR_ARG, "region %d out of range", r);
+  const RegionDev& g = c->regions_h[r];
+  if (count == 0) return PG_OK;
+  if (first_locus < g.start || (int64_t)first_locus + count - 1 > (int64_t)g.stop)
+    return fail(c, PG_ERR_ARG, "loci %d..%lld outside region %d", first_locus, (long long)first_locus + count - 1, r);
+  cudaSetDevice(c->device);
+  launch_mark_deleted(P<uint32_t>(c->rec_call) + g.pos_base + (first_locus - g.start), count, c->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return PG_OK;
 }
 
 pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid, int32_t vcf_qe,

@@ -320,6 +320,16 @@ void launch_scan64(int64_t* io, int64_t n, int64_t* sums, cudaStream_t s) {
   k_scan64_c<<<nb, 1024, 0, s>>>(io, n, sums);
 }
 
+__global__ void k_mark_deleted(uint32_t* call, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) call[i] |= PG_CALL_DELETED;
+}
+
+void launch_mark_deleted(uint32_t* call, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  k_mark_deleted<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(call, n);
+}
+
 void launch_vcf_write(const FormatArgs& A, const int64_t* off, char* text, cudaStream_t s) {
   const int32_t n = A.region.size;
   if (n <= 0) return;

@@ -20,5 +20,7 @@ struct FormatArgs {
 void launch_vcf_lengths(const FormatArgs& A, int64_t* len, cudaStream_t s);
 void launch_scan64(int64_t* io, int64_t n, int64_t* sums, cudaStream_t s);
 void launch_vcf_write(const FormatArgs& A, const int64_t* off, char* text, cudaStream_t s);
+// sets PG_CALL_DELETED on call[0, n)
+void launch_mark_deleted(uint32_t* call, int64_t n, cudaStream_t s);
 
 }  // namespace pg

@@ -48,13 +48,16 @@ __device__ inline int32_t strand_qual(const uint8_t* qual, int32_t L, int strand
 }
 
 // Per window: reads longer than K, K-mer events and exotic K-mer events.
-__global__ void k_kmer_prepass(Reads R, const pg_window* wins, int32_t K, long long* out /* 3 per window */) {
+// rlist: when not null, a window's range indexes this list of reads.
+__global__ void k_kmer_prepass(Reads R, const pg_window* wins, const int64_t* rlist, int32_t K,
+                               long long* out /* 3 per window */) {
   __shared__ unsigned long long s[3];
   const pg_window w = wins[blockIdx.x];
   if (threadIdx.x < 3) s[threadIdx.x] = 0;
   __syncthreads();
   unsigned long long nr = 0, ne = 0, nx = 0;
-  for (int64_t i = w.read_begin + threadIdx.x; i < w.read_end; i += blockDim.x) {
+  for (int64_t ii = w.read_begin + threadIdx.x; ii < w.read_end; ii += blockDim.x) {
+    const int64_t i = rlist ? rlist[ii] : ii;
     const int32_t L = R.l_seq[i];
     if (L <= K) continue;
     nr++;
@@ -135,7 +138,8 @@ __global__ void __launch_bounds__(kKmerThreads) k_kmer_count(KmerArgs a) {
   const int64_t base = a.slot_base[w], cap = a.slot_cap[w];
   const int64_t xev0 = a.x_ev_base[w], xev_cap = a.x_ev_cap[w];
   const Reads& R = a.R;
-  for (int64_t i = ch.lo + warp; i < ch.hi; i += nwarps) {
+  for (int64_t ii = ch.lo + warp; ii < ch.hi; ii += nwarps) {
+    const int64_t i = a.rlist ? a.rlist[ii] : ii;
     const int32_t L = R.l_seq[i];
     if (L <= K) continue;
     const int32_t nev = L - K;  // K-mer starts per strand
@@ -437,10 +441,11 @@ __global__ void __launch_bounds__(kExoticThreads) k_kmer_exotic(KmerArgs a, int3
   }
 }
 
-void launch_kmer_prepass(const Reads& R, const pg_window* wins, int32_t n, int32_t K, long long* out,
+void launch_kmer_prepass(const Reads& R, const pg_window* wins, const int64_t* rlist, int32_t n, int32_t K,
+                         long long* out,
                          cudaStream_t s) {
   if (n <= 0) return;
-  k_kmer_prepass<<<n, 256, 0, s>>>(R, wins, K, out);
+  k_kmer_prepass<<<n, 256, 0, s>>>(R, wins, rlist, K, out);
 }
 
 __global__ void k_kmer_reset(KmerArgs a) {

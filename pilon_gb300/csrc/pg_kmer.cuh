@@ -4,7 +4,8 @@
 
 namespace pg {
 
-// reads [lo, hi) of window w, walked by one CTA of k_kmer_count
+// reads [lo, hi) of window w (or entries [lo, hi) of the read list), walked
+// by one CTA of k_kmer_count
 struct KmerChunk {
   int64_t lo, hi;
   int32_t w, pad;
@@ -34,6 +35,7 @@ static_assert(sizeof(KmerSlot) == 64 && sizeof(KmerSlotWide) == 96, "K-mer slot 
 
 struct KmerArgs {
   Reads R;
+  const int64_t* rlist;       // not null: window and chunk ranges index this list of reads
   const int32_t* win_list;    // the batch's windows (indices into the per-window arrays)
   int32_t n_win;
   int32_t K;
@@ -69,8 +71,8 @@ struct KmerArgs {
   int32_t* overflow;
 };
 
-void launch_kmer_prepass(const Reads& R, const pg_window* wins, int32_t n, int32_t K, long long* out,
-                         cudaStream_t s);
+void launch_kmer_prepass(const Reads& R, const pg_window* wins, const int64_t* rlist, int32_t n, int32_t K,
+                         long long* out, cudaStream_t s);
 // clears full / used / x_ev_fill of the windows in win_list
 void launch_kmer_reset(const KmerArgs& a, cudaStream_t s);
 // k_kmer_count over the batch's chunks

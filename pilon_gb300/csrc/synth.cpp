@@ -92,6 +92,7 @@ struct Sim {
   std::vector<uint32_t> cigar;
   std::vector<int64_t> cigoff, seqoff, qualoff;
   std::vector<int32_t> lseq;
+  std::vector<int64_t> pair;  // the pair each read belongs to (the two mates share a read name)
 };
 
 uint8_t drawQual(Rng& r) {
@@ -271,12 +272,13 @@ void* sy_simulate(const uint8_t* sample, int64_t slen, const int64_t* s2r, const
   size_t n = order.size();
   S->pos.resize(n); S->aend.resize(n); S->tlen.resize(n); S->refid.assign(n, P->ref_id);
   S->flag.resize(n); S->ncig.resize(n); S->mapq.resize(n); S->lseq.assign(n, L);
-  S->cigoff.resize(n); S->seqoff.resize(n); S->qualoff.resize(n);
+  S->cigoff.resize(n); S->seqoff.resize(n); S->qualoff.resize(n); S->pair.resize(n);
   S->seq.resize(n * (size_t)((L + 1) / 2));
   S->qual.resize(n * (size_t)L);
   S->cigar.reserve(S->cig.size());
   for (size_t i = 0; i < n; i++) {
     const Read& r = S->reads[order[i]];
+    S->pair[i] = (int64_t)(order[i] >> 1);  // mates are pushed one after the other
     S->pos[i] = r.pos; S->aend[i] = r.aend; S->tlen[i] = r.tlen; S->flag[i] = r.flag; S->mapq[i] = r.mapq;
     S->cigoff[i] = (int64_t)S->cigar.size();
     S->ncig[i] = (uint16_t)r.cig_n;
@@ -313,6 +315,13 @@ void sy_copy(void* h, int32_t* pos, int32_t* aend, uint16_t* flag, uint8_t* mapq
   memcpy(seqoff, S->seqoff.data(), n * 8); memcpy(lseq, S->lseq.data(), n * 4);
   memcpy(seq, S->seq.data(), S->seq.size()); memcpy(qualoff, S->qualoff.data(), n * 8);
   memcpy(qual, S->qual.data(), S->qual.size());
+}
+
+// The pair index of every read (sorted order): mates share it, as they share
+// a read name in a BAM.
+void sy_copy_pairs(void* h, int64_t* pair) {
+  Sim* S = (Sim*)h;
+  memcpy(pair, S->pair.data(), S->pair.size() * 8);
 }
 
 void sy_free(void* h) { delete (Sim*)h; }

@@ -72,6 +72,10 @@ def lib():
             "pg_fetch_changes": (C.c_int, [vp, vp, i64, C.POINTER(C.c_int64), vp, i64, C.POINTER(C.c_int64)]),
             "pg_kmer_tally_breaks": (C.c_int, [vp, i32, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
                                                C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+            "pg_kmer_tally_reads": (C.c_int, [vp, vp, i64, vp, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
+                                              C.POINTER(C.c_int64)]),
+            "pg_reassemble": (C.c_int, [vp, i64, i32, vp, i32, i32, vp, vp, i64, C.POINTER(C.c_int64)]),
+            "pg_mark_deleted": (C.c_int, [vp, i32, i32, i32]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -242,6 +246,34 @@ class Engine:
                 return edges[:n.value]
             cap = int(n.value)
 
+    def kmer_tally_reads(self, read_lists, K, params, min_depth=5, cap=None):
+        """pg_kmer_tally_reads: edges (pg_kmer_edge_wide records) of one window
+        per list of read indices."""
+        lens = np.array([len(x) for x in read_lists], np.int64)
+        bounds = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+        reads = (np.concatenate([np.asarray(x, np.int64) for x in read_lists]).astype(np.int64)
+                 if len(read_lists) else np.zeros(0, np.int64))
+        wins = np.stack([bounds[:-1], bounds[1:]], axis=1).astype(np.int64) if len(read_lists) else \
+            np.zeros((0, 2), np.int64)
+        wins = np.ascontiguousarray(wins)
+        reads = np.ascontiguousarray(reads)
+        dt = _abi.kmer_edge_wide_dtype()
+        cap = cap or getattr(self, "_kmer_cap", 1 << 20)
+        while True:
+            edges = np.zeros(cap, dt)
+            n = C.c_int64()
+            self._check(self.L.pg_kmer_tally_reads(self.h, reads.ctypes.data, reads.size, wins.ctypes.data,
+                                                   len(read_lists), K, C.byref(params), min_depth,
+                                                   edges.ctypes.data, cap, C.byref(n)))
+            if n.value <= cap:
+                self._kmer_cap = max(cap, int(n.value))
+                return edges[:n.value]
+            cap = int(n.value)
+
+    def mark_deleted(self, r, first_locus, count):
+        """pg_mark_deleted: loci of region r that a reassembly fix replaces."""
+        self._check(self.L.pg_mark_deleted(self.h, r, first_locus, count))
+
     def format_vcf(self, r, name, diploid=False, vcf_qe=False, variants_only=False):
         """The region's VCF records as bytes (pg_format_vcf)."""
         n = C.c_int64()
@@ -340,3 +372,44 @@ class Engine:
         n = C.c_int32()
         self._check(self.L.pg_graph_replays(self.h, C.byref(n)))
         return n.value
+
+
+def reassemble(edges, K, jobs, threads=0):
+    """pg_reassemble on the host: jobs are dicts (window, is_gap, region_start,
+    region_stop, break_start, break_stop, break_radius, bases, orig), the
+    region's bases as contiguous uint8 arrays (shared by the jobs of one
+    region); returns one (start, was, patch, status, loop_len) per job, start 0
+    when there is no solution."""
+    L = lib()
+    n = len(jobs)
+    arr = (_abi.pg_reassembly * max(1, n))()
+    for k, j in enumerate(jobs):
+        b, o = j["bases"], j["orig"]
+        for x in (b, o):
+            if not (isinstance(x, np.ndarray) and x.dtype == np.uint8 and x.flags.c_contiguous and
+                    x.size == j["region_stop"] + 1 - j["region_start"]):
+                raise ValueError("job bases must be contiguous uint8 arrays of the region's size")
+        arr[k] = _abi.pg_reassembly(j["window"], int(j["is_gap"]), j["region_start"], j["region_stop"],
+                                    j["break_start"], j["break_stop"], j["break_radius"], 0, b.ctypes.data,
+                                    o.ctypes.data)
+    fixes = (_abi.pg_reassembly_fix * max(1, n))()
+    edges = np.ascontiguousarray(edges)
+    cap = 1 << 16
+    while True:
+        text = np.zeros(cap, np.uint8)
+        tl = C.c_int64()
+        st = L.pg_reassemble(edges.ctypes.data if edges.size else None, edges.size, K, C.cast(arr, C.c_void_p), n,
+                             threads, C.cast(fixes, C.c_void_p), text.ctypes.data, cap, C.byref(tl))
+        if st == _abi.PG_ERR_LIMIT and tl.value > cap:
+            cap = int(tl.value)
+            continue
+        if st:
+            raise EngineError(st, "pg_reassemble: bad arguments")
+        break
+    t = text.tobytes()
+    out = []
+    for k in range(n):
+        f = fixes[k]
+        out.append((int(f.start), t[f.was_off:f.was_off + f.was_len].decode(),
+                    t[f.patch_off:f.patch_off + f.patch_len].decode(), int(f.status), int(f.loop_len)))
+    return out

@@ -1,14 +1,15 @@
 """Whole-genome polishing on the GB300 engine: the loop of
 GenomeFile.processRegions (S/GenomeFile.scala:84-176) for the fix types
-snps / indels (and amb / iupac), writing Pilon's three outputs.
+snps / indels (and amb / iupac) and gaps / local, writing Pilon's three
+outputs.
 
   pileup, BaseCall, pass 1      engine (pg_pileup_regions), batched over all regions
   fix lists, fixIssues          host, over the sparse change list (S/GenomeRegion.scala:307-414, 557-621)
-  VCF records                   engine (pg_format_vcf); header and <DUP> records here
+  gaps / local reassembly       reassembly.py: recruitment on the host, the K-mer tally of every
+                                window on the device (pg_kmer_tally_reads), the graph walk and
+                                GapFiller on host threads (pg_reassemble)
+  VCF records                   engine (pg_format_vcf); header, <DUP> and reassembly records here
   changes, FASTA                host (S/GenomeRegion.scala:645-657, S/GenomeFile.scala:79-82, 135-161)
-
-Gap filling and local reassembly (fix types gaps / local) are not part of
-this driver; their break windows feed the K-mer tally (pg_kmer_tally_breaks).
 """
 import ctypes as C
 from dataclasses import dataclass, field
@@ -17,6 +18,7 @@ import numpy as np
 
 from . import _abi
 from .regions import plan_regions
+from . import reassembly
 
 ACGT = "ACGT"
 IUPAC = {1: "A", 2: "C", 4: "G", 8: "T", 5: "R", 10: "Y", 6: "S", 9: "W", 12: "K", 3: "M", 14: "B", 13: "D",
@@ -28,6 +30,10 @@ class Options:
     """The command-line switches of Pilon that this path honours (S/Pilon.scala:28-73)."""
     fix_snps: bool = True
     fix_indels: bool = True
+    fix_gaps: bool = False          # "gaps": GapFiller.fillGap over runs of N
+    fix_local: bool = False         # "local": GapFiller.fixBreak over possibleBreaks
+    K: int = 47                     # --K, Assembler.K
+    strays: bool = True             # --nostrays clears it
     iupac: bool = False
     diploid: bool = False
     vcf: bool = True
@@ -103,11 +109,14 @@ class RegionResult:
     bases: bytearray
     snp: list = field(default_factory=list)
     small: list = field(default_factory=list)
+    big: list = field(default_factory=list)     # local reassemblies and gap fills
     dupes: list = field(default_factory=list)
     stats: object = None
+    bases_snp: bytearray = None                 # the bases after the SNP fixes alone
+    orig: bytes = None
 
     def all_fixes(self):
-        return fix_fix_list(self.snp + self.small)
+        return fix_fix_list(self.snp + self.small + self.big)
 
 
 def _region_outputs(engine, r, region, ref, opts, params, changes, chars, dupes=()):
@@ -150,19 +159,67 @@ def _region_outputs(engine, r, region, ref, opts, params, changes, chars, dupes=
     # the reference prepends to its lists: descending loci, then stable-sorted
     res.snp.reverse()
     res.small.reverse()
+    res.orig = orig
     res.bases = fix_issues(res.bases, s, res.snp)
+    res.bases_snp = res.bases
     res.bases = fix_issues(res.bases, s, res.small)
     res.dupes = list(dupes)
-    if res.dupes:
-        # records per position: one, plus one after an indel call at i > 0 outside a deletion
-        call = np.empty(size, np.uint32)
-        o = _abi.pg_region_out()
-        o.call = call.ctypes.data
-        engine._check(engine.L.pg_fetch_region(engine.h, r, C.byref(o)))
-        extra = ((call & (_abi.PG_CALL_INS | _abi.PG_CALL_DEL)) != 0) & ((call & _abi.PG_CALL_DELETED) == 0)
-        extra[0] = False
-        res.first_line = np.concatenate([[0], np.cumsum(1 + extra.astype(np.int64))])
     return res
+
+
+def _first_lines(engine, r, size):
+    """Line of the first VCF record of each position of region r: one record per
+    position, plus one after an indel call at i > 0 outside a deletion."""
+    call = np.empty(size, np.uint32)
+    o = _abi.pg_region_out()
+    o.call = call.ctypes.data
+    engine._check(engine.L.pg_fetch_region(engine.h, r, C.byref(o)))
+    extra = ((call & (_abi.PG_CALL_INS | _abi.PG_CALL_DEL)) != 0) & ((call & _abi.PG_CALL_DELETED) == 0)
+    extra[0] = False
+    return np.concatenate([[0], np.cumsum(1 + extra.astype(np.int64))])
+
+
+def _reassemble(engine, regions, results, contigs, reads, params, opts):
+    """The gaps and local steps of identifyAndFixIssues (S/GenomeRegion.scala:
+    382-413) for every region: one K-mer tally for all windows, then the walks.
+    The insert statistics a region's GapFiller sees are those of the scan and
+    of the regions processed up to it, as Pilon processes chunks in order."""
+    bam = reassembly.BamState(reads, params, len(contigs), strays=opts.strays)
+    breaks = engine.find_breaks() if opts.fix_local else {}
+    jobs, lists, owner = [], [], []
+    for r, (reg, res) in enumerate(zip(regions, results)):
+        bam.add_region(res.stats)
+        c, s, e = reg[0], reg[1], reg[2]
+        todo = []
+        if opts.fix_gaps:
+            todo += [(g, True) for g in reassembly.gaps(contigs[c], s, e)]
+        if opts.fix_local:
+            todo += [(b, False) for b in breaks.get(r, [])]
+        if not todo:
+            continue
+        radius = bam.break_radius(opts.K)
+        bases = np.frombuffer(bytes(res.bases_snp), np.uint8).copy()
+        orig = np.frombuffer(res.orig, np.uint8).copy()
+        for (bs, be), is_gap in todo:
+            lists.append(bam.recruit(c, bs, be))
+            jobs.append(dict(window=len(lists) - 1, is_gap=is_gap, region_start=s, region_stop=e, break_start=bs,
+                             break_stop=be, break_radius=radius, bases=bases, orig=orig))
+            owner.append(r)
+    if not jobs:
+        return
+    from .engine import reassemble, EngineError
+    edges = engine.kmer_tally_reads(lists, opts.K, params)
+    fixes = reassemble(edges, opts.K, jobs)
+    for j, r, (start, was, patch, status, _loop) in zip(jobs, owner, fixes):
+        if status:
+            raise EngineError(status, f"region {r}: the reference would throw reassembling "
+                                      f"{j['break_start']}-{j['break_stop']}")
+        if start > 0 and (j["is_gap"] or max(len(was), len(patch)) > 10):
+            results[r].big.append(Fix(start, was, patch))
+    for reg, res in zip(regions, results):
+        if res.big:
+            res.big.reverse()  # prepended (::=) in the reference
+            res.bases = fix_issues(res.bases_snp, reg[1], res.small + res.big)
 
 
 def _exclude_motifs(orig, s, e, nano):
@@ -247,6 +304,8 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
     bounds = np.searchsorted(changes["region"], np.arange(len(regions) + 1))
     results = [_region_outputs(engine, r, reg, contigs[reg[0]], opts, params, changes[bounds[r]:bounds[r + 1]],
                                chars, dups.get(r, ())) for r, reg in enumerate(regions)]
+    if opts.fix_gaps or opts.fix_local:
+        _reassemble(engine, regions, results, contigs, reads, params, opts)
     # The output groups of GenomeFile.regions (S/GenomeFile.scala:49-54): a contig
     # with its chunks, or with --targets one group per target (two targets on one
     # contig give two FASTA records, and each restarts the changes offset).
@@ -261,8 +320,11 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
             sizes = [(names[c], sum(results[r].stop - results[r].start + 1 for r in rs)) for c, rs in groups]
             vf.write(vcf_header(sizes, opts).encode())
             for r, res in enumerate(results):
+                inserts = _vcf_inserts(engine, r, res, names[res.contig], contigs[res.contig])
                 text = engine.format_vcf(r, names[res.contig], opts.diploid, opts.vcf_qe)
-                vf.write(_splice_dupes(text, res, names[res.contig], contigs[res.contig]))
+                if inserts:
+                    text = _splice(text, _first_lines(engine, r, res.stop - res.start + 1), inserts, res.start)
+                vf.write(text)
     if opts.changes:
         with open(out_prefix + ".changes", "w") as cf:
             for c, rs in groups:
@@ -278,7 +340,7 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
                                  (f.was or ".") + " " + (f.patch or ".") + "\n")
                         delta += len(f.patch) - len(f.was)
                     offset += len(res.bases) - (res.stop - res.start + 1)
-    if opts.fix_snps or opts.fix_indels:
+    if opts.fix_snps or opts.fix_indels or opts.fix_gaps or opts.fix_local:
         with open(out_prefix + ".fasta", "wb") as ff:
             for c, rs in groups:
                 seq = b"".join(bytes(results[r].bases) for r in rs)
@@ -288,21 +350,45 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
     return results
 
 
-def _splice_dupes(text, res, name, ref):
-    """Inserts Vcf.writeDup records (S/Vcf.scala:194-202) before the records of
-    each duplication's first position (S/GenomeRegion.scala:628-631)."""
-    if not res.dupes:
-        return text
+def _vcf_inserts(engine, r, res, name, ref):
+    """The records GenomeRegion.writeVcf writes before a position's own
+    (S/GenomeRegion.scala:623-643): Vcf.writeDup at a duplication's first
+    locus (S/Vcf.scala:194-202), then Vcf.writeFixRecord at the first locus of
+    a fix that only local reassembly made (S/Vcf.scala:178-192), whose
+    replaced loci are marked deleted on the device first.  A list of (locus,
+    line) in writing order."""
+    out = [(d[0], (f"{name}\t{d[0] - 1}\t.\t{chr(ref[d[0] - 2]).upper()}\t<DUP>\t.\tPASS\tSVTYPE=DUP;"
+                   f"SVLEN={d[1] + 1 - d[0]};END={d[1]};IMPRECISE\tGT\t./.").encode()) for d in res.dupes]
+    if res.big:
+        small = {(f.locus, f.was, f.patch) for f in res.small}
+        big = {(f.locus, f.was, f.patch) for f in res.big}
+        for f in res.all_fixes():
+            key = (f.locus, f.was, f.patch)
+            if key in big and key not in small:
+                loc = f.locus - 1
+                if loc < res.start:
+                    raise IndexError(f"{name}:{f.locus}: the reference's refBase({loc}) is outside the region")
+                rb = chr(ref[loc - 1]).upper()
+                rs, alt = rb + f.was, rb + f.patch
+                svlen = len(alt) - len(rs)
+                line = (f"{name}\t{loc}\t.\t{rs}\t{alt}\t.\tPASS\tSVTYPE={'DEL' if svlen < 0 else 'INS'};"
+                        f"SVLEN={svlen};END={loc + len(rs) - 1}{';IMPRECISE' if 'N' in f.patch else ''}\tGT\t1/1")
+                out.append((f.locus, line.encode()))
+                if f.was:
+                    engine.mark_deleted(r, f.locus, len(f.was))
+    out.sort(key=lambda x: x[0])  # stable: a duplication's record stays before a fix's at the same locus
+    return out
+
+
+def _splice(text, first_line, inserts, start):
+    """Inserts the (locus, line) records before the records of their locus."""
     lines = text.split(b"\n")
     out = []
     prev = 0
-    for d in res.dupes:
-        k = int(res.first_line[d[0] - res.start])
+    for locus, line in inserts:
+        k = int(first_line[locus - start])
         out.extend(lines[prev:k])
-        loc = d[0] - 1
-        rb = chr(ref[loc - 1]).upper()
-        out.append(f"{name}\t{loc}\t.\t{rb}\t<DUP>\t.\tPASS\tSVTYPE=DUP;SVLEN={d[1] + 1 - d[0]};"
-                   f"END={d[1]};IMPRECISE\tGT\t./.".encode())
+        out.append(line)
         prev = k
     out.extend(lines[prev:])
     return b"\n".join(out)

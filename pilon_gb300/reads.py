@@ -34,6 +34,9 @@ class ReadStore:
     seq: np.ndarray            # uint8, 4-bit codes, two per byte
     qual_off: np.ndarray       # int64
     qual: np.ndarray           # uint8
+    # getReadName as an id (mates share one); optional, host side only: the
+    # stray-mate recruitment of local reassembly pairs reads by name
+    name_id: np.ndarray = None  # int64
     _keep: list = field(default_factory=list, repr=False)
 
     @property
@@ -103,7 +106,8 @@ class ReadStore:
                          self.mapq[idx].copy(), self.tlen[idx].copy(), self.ref_id[idx].copy(),
                          self.mate_ref_id[idx].copy(), co.astype(np.int64), nc.astype(np.uint16),
                          cig.astype(np.uint32), so.astype(np.int64), self.l_seq[idx].copy(),
-                         seq.astype(np.uint8), qo.astype(np.int64), qual.astype(np.uint8))
+                         seq.astype(np.uint8), qo.astype(np.int64), qual.astype(np.uint8),
+                         None if self.name_id is None else self.name_id[idx].copy())
 
 
 FIELDS = ["pos", "aend", "flag", "mapq", "tlen", "ref_id", "mate_ref_id", "cigar_off", "n_cigar",
@@ -159,7 +163,8 @@ def build_store(records):
         cigar_off=np.array(co, np.int64), n_cigar=np.array([len(r["cigar"]) for r in records], np.uint16),
         cigar=cat(cig, np.uint32), seq_off=np.array(so, np.int64),
         l_seq=np.array([len(r["seq"]) for r in records], np.int32), seq=cat(seqb, np.uint8),
-        qual_off=np.array(qo, np.int64), qual=cat(qualb, np.uint8))
+        qual_off=np.array(qo, np.int64), qual=cat(qualb, np.uint8),
+        name_id=(np.array([r["name"] for r in records], np.int64) if records and "name" in records[0] else None))
 
 
 def concat_stores(stores):
@@ -168,6 +173,11 @@ def concat_stores(stores):
     seq_base = np.cumsum([0] + [s.seq.size for s in stores])[:-1]
     qual_base = np.cumsum([0] + [s.qual.size for s in stores])[:-1]
     cat = np.concatenate
+    names = None
+    if all(s.name_id is not None for s in stores):
+        # read names stay distinct across the stores (as the names of one BAM)
+        base = np.cumsum([0] + [int(s.name_id.max()) + 1 if s.n_reads else 0 for s in stores])[:-1]
+        names = cat([s.name_id + b for s, b in zip(stores, base)]).astype(np.int64)
     return ReadStore(
         cat([s.pos for s in stores]), cat([s.aend for s in stores]), cat([s.flag for s in stores]),
         cat([s.mapq for s in stores]), cat([s.tlen for s in stores]), cat([s.ref_id for s in stores]),
@@ -176,7 +186,7 @@ def concat_stores(stores):
         cat([s.cigar for s in stores]),
         cat([s.seq_off + b for s, b in zip(stores, seq_base)]), cat([s.l_seq for s in stores]),
         cat([s.seq for s in stores]),
-        cat([s.qual_off + b for s, b in zip(stores, qual_base)]), cat([s.qual for s in stores]))
+        cat([s.qual_off + b for s, b in zip(stores, qual_base)]), cat([s.qual for s in stores]), names)
 
 
 def merge_sorted(stores):

@@ -32,6 +32,7 @@ def _lib():
         _SYNTH.sy_n_cigar.restype = C.c_int64
         _SYNTH.sy_n_cigar.argtypes = [C.c_void_p]
         _SYNTH.sy_copy.argtypes = [C.c_void_p] + [C.c_void_p] * 14
+        _SYNTH.sy_copy_pairs.argtypes = [C.c_void_p, C.c_void_p]
         _SYNTH.sy_free.argtypes = [C.c_void_p]
     return _SYNTH
 
@@ -187,6 +188,8 @@ def simulate_contig(sample, s2r, ref_len, w, ref_id, seed, repeat_mask=None):
                     st.cigar.ctypes.data, st.seq_off.ctypes.data, st.l_seq.ctypes.data, st.seq.ctypes.data,
                     st.qual_off.ctypes.data, st.qual.ctypes.data)
         st.mate_ref_id[:] = st.ref_id
+        st.name_id = np.empty(n, np.int64)
+        lib.sy_copy_pairs(h, st.name_id.ctypes.data)
     finally:
         lib.sy_free(h)
     return st

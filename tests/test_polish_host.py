@@ -58,9 +58,10 @@ class OracleEngine:
     records, which polish() splices in itself."""
     h = None
 
-    def __init__(self, names=None, chunk=10_000_000):
+    def __init__(self, names=None, chunk=10_000_000, **fix):
         self.L = _OracleFetch(self)
         self.names, self.chunk, self._vcf = names, chunk, {}
+        self.fix = fix  # fix_gaps / fix_local / K / strays of the oracle run the VCF records come from
 
     def set_reference(self, contigs):
         self.contigs = contigs
@@ -115,6 +116,29 @@ class OracleEngine:
                 out[r] = d
         return out
 
+    def find_breaks(self, min_min_depth=5):
+        """possibleBreaks of every region, from the oracle (pg_find_breaks)."""
+        out = {}
+        for r, (c, s, e, rb, re) in enumerate(self.regions):
+            b = oracle.region_breaks(self.reads, self.params, self.contigs[c], c, s, e, rb, re)
+            if b:
+                out[r] = b
+        return out
+
+    def kmer_tally_reads(self, read_lists, K, params, min_depth=5):
+        """pg_kmer_tally_reads' edges from the oracle's tally of each list."""
+        parts = []
+        for w, lst in enumerate(read_lists):
+            sub = self.reads.subset(np.asarray(lst, np.int64))
+            e = oracle.kmer_tally_wide(sub, params, [(0, sub.n_reads)], K, min_depth)
+            e["window"] = w
+            parts.append(e)
+        return np.concatenate(parts) if parts else np.zeros(0, _abi.kmer_edge_wide_dtype())
+
+    def mark_deleted(self, r, first_locus, count):
+        s = self.regions[r][1]
+        self.results[r].call[first_locus - s:first_locus - s + count] |= _abi.PG_CALL_DELETED
+
     def _check(self, st):
         assert st == _abi.PG_OK, st
 
@@ -125,12 +149,12 @@ class OracleEngine:
             with tempfile.TemporaryDirectory() as d:
                 pre = os.path.join(d, "v")
                 assert oracle.polish(self.reads, self.params, self.names, self.contigs, pre, chunk_size=self.chunk,
-                                     diploid=diploid, vcf_qe=vcf_qe) == 0
+                                     diploid=diploid, vcf_qe=vcf_qe, **self.fix) == 0
                 body = [l for l in open(pre + ".vcf", "rb").read().split(b"\n") if l and not l.startswith(b"#")]
             by_contig = {}
             for l in body:
-                f = l.split(b"\t", 5)
-                if f[4] != b"<DUP>":
+                f = l.split(b"\t", 8)
+                if f[4] != b"<DUP>" and not f[7].startswith(b"SVTYPE="):  # not a <DUP> or reassembly record
                     lines, locs = by_contig.setdefault(f[0], ([], []))
                     lines.append(l)
                     locs.append(int(f[1]))
@@ -146,13 +170,14 @@ def compare(ds, params=None, chunk=10_000_000, no_frags=False, vcf=False, **kw):
     params = params or _abi.default_params()
     opts = Options(chunk_size=chunk, vcf=vcf, **kw)
     opts.no_frags = no_frags  # long reads only: excludeMotifs applies
+    fix = dict(fix_gaps=opts.fix_gaps, fix_local=opts.fix_local, K=opts.K, strays=opts.strays)
     with tempfile.TemporaryDirectory() as d:
         h, o = os.path.join(d, "host"), os.path.join(d, "ora")
-        polish(OracleEngine(ds.names, chunk), ds.names, ds.contigs, ds.reads, params, h, opts)
+        polish(OracleEngine(ds.names, chunk, **fix), ds.names, ds.contigs, ds.reads, params, h, opts)
         assert oracle.polish(ds.reads, params, ds.names, ds.contigs, o, chunk_size=chunk, fix_snps=opts.fix_snps,
                              fix_indels=opts.fix_indels, iupac=opts.iupac, diploid=opts.diploid,
                              vcf_qe=opts.vcf_qe, vcf_date=opts.vcf_date, vcf_source=opts.vcf_source,
-                             vcf_args=opts.vcf_args, vcf_ref=opts.vcf_ref) == 0
+                             vcf_args=opts.vcf_args, vcf_ref=opts.vcf_ref, **fix) == 0
         out = {}
         for ext in ("fasta", "changes") + (("vcf",) if vcf else ()):
             a, b = open(f"{h}.{ext}", "rb").read(), open(f"{o}.{ext}", "rb").read()

@@ -1,0 +1,192 @@
+"""Local reassembly (fix types gaps and local) on the CPU: the host half of the
+product path — BamFile.scan statistics and stray mates, GapFiller's read
+recruitment (pilon_gb300/reassembly.py), the graph walk and GapFiller in C++
+(pg_reassemble), and their fixes in the FASTA, changes and VCF
+(pilon_gb300/polish.py) — against the oracle's restatement of
+identifyAndFixIssues with gaps and local (S/GenomeRegion.scala:307-414,
+S/GapFiller.scala:28-402, S/Assembler.scala:46-284).
+
+The K-mer tally of each window is the device's job (pg_kmer_tally_reads,
+compared in tests/test_gpu_reassembly.py); here the test-only stand-in engine
+answers it from the oracle's tally of the same reads.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from pilon_gb300 import _abi, reassembly, synth
+from pilon_gb300.engine import reassemble
+from pilon_gb300.reads import build_store
+from tests.test_polish_host import compare
+
+
+@pytest.fixture(scope="module")
+def cfg4_small():
+    return synth.generate(4, 0.01)
+
+
+def _big_fixes(changes):
+    out = []
+    for line in changes.decode().splitlines():
+        was, patch = line.split()[2:4]
+        was, patch = was.strip("."), patch.strip(".")
+        if max(len(was), len(patch)) > 10:
+            out.append(line)
+    return out
+
+
+@pytest.mark.parametrize("K", [31, 47])
+def test_local_reassembly_matches_oracle(cfg4_small, K):
+    """--fix all on 1.2 Mb with repeats and 10-200 bp planted indels: FASTA,
+    changes and VCF byte-identical to the oracle, with local reassemblies."""
+    n, out = compare(cfg4_small, vcf=True, fix_gaps=True, fix_local=True, K=K)
+    big = _big_fixes(out["changes"])
+    assert len(big) >= 10, big
+    # the records of fixes only reassembly made (pileup indels keep their own records)
+    assert out["vcf"].count(b"SVTYPE=INS") + out["vcf"].count(b"SVTYPE=DEL") >= 3
+
+
+def test_local_reassembly_without_strays(cfg4_small):
+    compare(cfg4_small, vcf=True, fix_local=True, K=31, strays=False)
+
+
+def test_reassemblies_restore_the_sample(cfg4_small):
+    """Ground truth beside the oracle: the planted indels of 10 bp or more that
+    local reassembly fixes leave the sample's own sequence in the polished
+    FASTA around them.  Without --fix indels: a long indel that the pileup
+    calls too would otherwise be inserted twice, at loci a few bases apart
+    that fixFixList does not see as overlapping (S/GenomeRegion.scala:557-593),
+    as in the reference."""
+    d = cfg4_small
+    n, out = compare(d, fix_local=True, fix_indels=False, K=31)
+    fasta = b"".join(out["fasta"].split(b"\n")[1:])
+    ref = bytes(d.contigs[0])
+    fixed = restored = 0
+    for line in _big_fixes(out["changes"]):
+        loc = int(line.split()[0].split(":")[1].split("-")[0])
+        near = [v for v in d.variants[0] if v[1] != "snp" and abs(v[0] - loc) < 300 and
+                max(len(v[2]), len(v[3])) >= 10]
+        if len(near) != 1:
+            continue
+        p, kind, was, alt = near[0]
+        fixed += 1
+        if kind == "ins":  # inserted after locus p
+            sample = ref[p - 60:p] + alt.encode() + ref[p:p + 60]
+        else:  # loci p .. p + len(was) - 1 deleted
+            sample = ref[p - 61:p - 1] + ref[p - 1 + len(was):p - 1 + len(was) + 60]
+        restored += sample in fasta
+    assert fixed >= 10 and restored == fixed, (fixed, restored)
+
+
+def test_gaps_closed_and_opened(cfg4_small):
+    """GapFiller.fillGap on runs of N planted in the reference over sampled
+    sequence: a 60 bp gap the reads span is closed with the sample's bases; a
+    3 kb gap whose middle kilobase no read covers is filled from both sides
+    with Ns between (S/GapFiller.scala:76-99)."""
+    import copy
+    d = copy.copy(cfg4_small)
+    ref = d.contigs[0].copy()
+    truth = bytes(ref[199_990:200_070])
+    ref[200_000:200_060] = ord("N")
+    ref[500_000:503_000] = ord("N")
+    d.contigs = [ref]
+    r = d.reads
+    d.reads = r.subset(np.nonzero((r.aend < 501_000) | (r.pos > 502_000))[0])
+    assert reassembly.gaps(ref, 1, ref.size) == [(200001, 200060), (500001, 503000)]
+    for K in (31, 47):
+        n, out = compare(d, vcf=True, fix_gaps=True, fix_local=True, K=K)
+        lines = out["changes"].decode().splitlines()
+        closed = [l for l in lines if l.startswith("chr1:200001-200060 ")]
+        opened = [l for l in lines if l.split()[0].startswith("chr1:5000") and "N" in l.split()[3]]
+        assert len(closed) == 1 and "N" not in closed[0].split()[3]
+        assert len(opened) == 1 and len(opened[0].split()[3].strip("N")) > 0
+        fasta = b"".join(out["fasta"].split(b"\n")[1:])
+        assert truth in fasta
+
+
+def test_scan_statistics_and_strays(cfg4_small):
+    """BamFile.scan over the store: the insert statistics and the stray-mate
+    maps (one read per name and mate end) the recruitment looks mates up in."""
+    d = cfg4_small
+    P = _abi.default_params()
+    b = reassembly.BamState(d.reads, P, 1)
+    r = d.reads
+    ok = reassembly.validate(r.flag, P) & ((r.flag & 0x4) == 0)
+    proper = ok & ((r.flag & 0x3) == 0x3)
+    t = r.tlen[proper].astype(np.int64)
+    rc = (r.flag[proper] & 0x10) != 0
+    keep = (t > 0) & (t < 2500)
+    assert b.fr.count + b.rf.count == int(keep.sum())
+    assert b.fr.sum == int(t[keep & ~rc].sum())
+    assert 0 < b.max_insert_size() < 2500 and b.break_radius(47) >= 141
+    strays = ok & ((r.flag & 0x3) == 0x1)
+    n1, n2 = (b._stray[0][0].size, b._stray[1][0].size)
+    assert n1 + n2 == int(strays.sum()) > 0
+    # a window near a stray pair with one mate outside it recruits the other mate
+    s_idx = np.nonzero(strays)[0]
+    i = int(s_idx[len(s_idx) // 2])
+    mate = int(s_idx[(r.name_id[s_idx] == r.name_id[i]) & (s_idx != i)][0])
+    lo, hi = sorted((i, mate))
+    flank = b.max_insert_size()
+    win = b.recruit(0, int(r.pos[lo]) + flank, int(r.pos[lo]) + flank)  # overlaps read lo only
+    assert lo in win.tolist() or hi in win.tolist()
+    assert lo in win.tolist() and hi in win.tolist()
+
+
+def _tile(seq, length=60, step=3, name0=0):
+    """Forward reads tiling `seq` at `step`, quality 30, unpaired."""
+    recs = []
+    for k, p in enumerate(range(0, len(seq) - length + 1, step)):
+        recs.append(dict(pos=p + 1, cigar=[(length, "M")], seq=seq[p:p + length], qual=[30] * length, flag=0,
+                         mapq=60, name=name0 + k))
+    return recs
+
+
+def _graph(seq, K, **kw):
+    reads = build_store(_tile(seq, **kw))
+    e = oracle.kmer_tally_wide(reads, _abi.default_params(), [(0, reads.n_reads)], K)
+    return e
+
+
+def _job(region, bs, be, radius, gap=False):
+    b = np.frombuffer(region.encode(), np.uint8).copy()
+    return dict(window=0, is_gap=int(gap), region_start=1, region_stop=len(region), break_start=bs, break_stop=be,
+                break_radius=radius, bases=b, orig=b)
+
+
+def test_walk_closes_a_break_known_answer():
+    """A region missing 25 bases that the reads hold: the walk from the left
+    flank runs through the reads' sequence into the right flank, the joins give
+    one solution, and trimPatch leaves the 25-base insertion
+    (S/GapFiller.scala:49-262, S/Assembler.scala:183-284)."""
+    rng = np.random.default_rng(7)
+    sample = "".join("ACGT"[x] for x in rng.integers(0, 4, 1200))
+    region = sample[:600] + sample[625:]
+    edges = _graph(sample, 31)
+    [(start, was, patch, status, loop)] = reassemble(edges, 31, [_job(region, 580, 620, 200)])
+    assert status == 0 and loop == 0
+    assert was == "" and patch == sample[600:625] and start == 601
+
+
+def test_walk_stops_at_a_tandem_repeat_known_answer():
+    """A break inside a tandem repeat longer than the reads: the walk meets a
+    K-mer it has seen, notes the loop (its period) and, Pilon.trSafe being on,
+    the break gets no solution (S/Assembler.scala:173-234, S/GapFiller.scala:67)."""
+    rng = np.random.default_rng(11)
+    flank = lambda n: "".join("ACGT"[x] for x in rng.integers(0, 4, n))
+    unit = "ACCGTTAGC"
+    sample = flank(500) + unit * 40 + flank(500)
+    edges = _graph(sample, 31)
+    [(start, was, patch, status, loop)] = reassemble(edges, 31, [_job(sample, 600, 700, 300)])
+    assert status == 0 and start == 0 and loop == len(unit)
+
+
+def test_walk_edge_of_region_raises_like_the_reference():
+    """A break whose left flank would start before the region: subString's
+    require fails in the reference (an exception ends the run); the job
+    reports PG_ERR_INDEX."""
+    rng = np.random.default_rng(3)
+    sample = "".join("ACGT"[x] for x in rng.integers(0, 4, 400))
+    edges = _graph(sample, 31)
+    [(start, was, patch, status, loop)] = reassemble(edges, 31, [_job(sample, 1, 20, 50)])
+    assert status == _abi.PG_ERR_INDEX
