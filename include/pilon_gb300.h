@@ -318,7 +318,8 @@ typedef struct pg_reassembly {
   int32_t break_start;       /* the gap or break, 1-based loci, inclusive */
   int32_t break_stop;
   int32_t break_radius;      /* GapFiller.breakRadius (S/GapFiller.scala:357-362) */
-  int32_t pad_;
+  int32_t fix_breaks;        /* Pilon.fixBreaks (--fix breaks, --variant): an unjoined break gets
+                                the partial fill of a gap (S/GapFiller.scala:76) */
   const char *bases;         /* the region's bases after its SNP fixes (region size bytes) */
   const char *orig;          /* the region's original bases (region size bytes) */
 } pg_reassembly;

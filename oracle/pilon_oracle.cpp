@@ -1016,7 +1016,7 @@ struct VcfWriter {
 // Assembler's K-mer tally and graph walk (S/Assembler.scala:46-284) and the
 // GapFiller (S/GapFiller.scala:28-402) for one BAM of type frags or unpaired.
 // Read names are given as ids (mates share an id); Pilon.trSafe is always
-// true and Pilon.multiClosure / fixBreaks / fixNovel are off (their defaults).
+// true and Pilon.multiClosure / fixNovel are off (their defaults).
 
 static double isMean(const InsertStats& s) {  // :167
   return s.count > 0 ? (double)s.sum / (double)s.count : 0.0;
@@ -1075,6 +1075,7 @@ struct Reassembly {
   const Params& P;
   int32_t K;
   bool strays;
+  bool fixBreaks = false;  // --fix breaks (--variant): breaks get the partial fill of gaps
   InsertStats fr, rf, un;  // insertStatsFR / RF / Unpaired: the scan plus every region processed so far
   std::unordered_map<int64_t, int64_t> stray1, stray2;  // strayMateMap readMap1 / readMap2 (:222-281)
   std::vector<int64_t> cb, ce;                           // each contig's read range
@@ -1145,25 +1146,57 @@ struct Reassembly {
     }
     return out;
   }
+  // MateMap.findStrays (S/BamFile.scala:244-257) of the MateMap m1 / m2 (name ->
+  // read, first-of-pair reads in m1); in HashMap order in the reference, sorted
+  // here (the tally and the pairs below do not depend on the order)
+  std::vector<int64_t> findStrays(const std::unordered_map<int64_t, int64_t>& m1,
+                                  const std::unordered_map<int64_t, int64_t>& m2) const {
+    std::vector<int64_t> found;
+    for (auto& kv : m1)
+      if (!m2.count(kv.first)) { auto it = stray2.find(kv.first); if (it != stray2.end()) found.push_back(it->second); }
+    for (auto& kv : m2)
+      if (!m1.count(kv.first)) {
+        auto& sm = (R->flag[kv.second] & 0x40) ? stray2 : stray1;
+        auto it = sm.find(kv.first);
+        if (it != sm.end()) found.push_back(it->second);
+      }
+    std::sort(found.begin(), found.end());
+    return found;
+  }
   std::vector<int64_t> recruitReads(int32_t c, int32_t s, int32_t e) const {
-    // GapFiller.recruitReads (S/GapFiller.scala:364-402) -> recruitFlankReads (S/BamFile.scala:346-364)
+    // GapFiller.recruitReads (S/GapFiller.scala:364-402) for the one BAM
     if (P.bamType == PG_BAM_UNPAIRED && P.longRead) return {};  // recruitUnpaired with --nanopore/--pacbio
     int32_t flank = maxInsertSize();
-    std::vector<int64_t> reads = readsInRegion(c, std::max(s - flank, 1), e + flank);
-    if (strays && P.bamType != PG_BAM_UNPAIRED) {  // MateMap(reads).findStrays (:244-257)
-      std::unordered_map<int64_t, int64_t> m1, m2;
-      for (int64_t i : reads) ((R->flag[i] & 0x40) ? m1 : m2)[nameId[i]] = i;
-      std::vector<int64_t> found;
-      for (auto& kv : m1)
-        if (!m2.count(kv.first)) { auto it = stray2.find(kv.first); if (it != stray2.end()) found.push_back(it->second); }
-      for (auto& kv : m2)
-        if (!m1.count(kv.first)) {
-          auto& sm = (R->flag[kv.second] & 0x40) ? stray2 : stray1;
-          auto it = sm.find(kv.first);
-          if (it != sm.end()) found.push_back(it->second);
+    int32_t fs = std::max(s - flank, 1), fe = e + flank;  // flankRegion (S/BamFile.scala:359-364)
+    std::vector<int64_t> reads = readsInRegion(c, fs, fe);
+    std::unordered_map<int64_t, int64_t> m1, m2;  // MateMap(reads)
+    if (strays || P.bamType == PG_BAM_JUMPS)
+      for (int64_t i : reads) ((R->flag[i] & 0x40) ? m1 : m2)[nameId ? nameId[i] : i] = i;
+    if (P.bamType == PG_BAM_JUMPS) {  // recruitJumps -> recruitBadMates (S/BamFile.scala:366-403)
+      if (strays)
+        for (int64_t i : findStrays(m1, m2)) ((R->flag[i] & 0x40) ? m1 : m2)[nameId[i]] = i;  // addStrays
+      int32_t midpoint = (s + e) / 2;
+      int64_t frPct = pctFR();
+      std::vector<int64_t> mates;
+      for (auto& kv : m1) {  // pairs(): (read1, read2) and (read2, read1) of each name in both maps
+        auto it = m2.find(kv.first);
+        if (it == m2.end()) continue;
+        for (auto [a, b] : {std::pair<int64_t, int64_t>{kv.second, it->second}, {it->second, kv.second}}) {
+          uint16_t fl = R->flag[a];
+          if ((fl & 0x4) || (fl & 0x2)) continue;
+          bool rc = fl & 0x10;
+          int32_t st = R->pos[a], en = R->aend[a];
+          bool before = st < midpoint, after = en > midpoint;
+          bool frO = (before && !rc) || (after && rc);
+          bool good = frPct > 100 - 10 ? frO : frPct < 10 ? !frO : true;  // minOrientationPct
+          if (good && ((st >= fs && st <= fe) || (en >= fs && en <= fe))) mates.push_back(b);
         }
-      // appended in HashMap order in the reference; the tally does not depend on it
-      std::sort(found.begin(), found.end());
+      }
+      std::sort(mates.begin(), mates.end());  // prepended in HashMap order in the reference
+      return mates;
+    }
+    if (strays && P.bamType != PG_BAM_UNPAIRED) {  // recruitFlankReads (S/BamFile.scala:346-357)
+      std::vector<int64_t> found = findStrays(m1, m2);
       reads.insert(reads.end(), found.begin(), found.end());
     }
     return reads;
@@ -1384,7 +1417,7 @@ Fix reassemble(const GenomeRegion& g, Reassembly& ra, int32_t bs, int32_t be, bo
     if (closedDiff > 100000) solutionOK = false;  // Pilon.gapMargin
   }
   if (solutionOK) return solution;
-  if (!isGap) return noSolution;  // Pilon.fixBreaks is off
+  if (!(isGap || (ra.fixBreaks && loop.empty()))) return noSolution;
   std::string fromRight = consensusFromRight(pathsFromRight);
   std::string fromLeft = consensusFromLeft(pathsFromLeft);
   int32_t newStart = start + (int32_t)fromLeft.size();
@@ -1396,7 +1429,7 @@ Fix reassemble(const GenomeRegion& g, Reassembly& ra, int32_t bs, int32_t be, bo
     return fromLeft == regionLeft && fromRight == regionRight;
   };
   if ((newStart >= bs + 20 || newStop <= be - 20) && !partialMatchesReference()) {  // GapFiller.minExtend
-    int32_t newGapLength = std::max(10, newStop - newStart);  // Pilon.minGap
+    int32_t newGapLength = isGap ? std::max(10, newStop - newStart) : 10;  // Pilon.minGap
     std::string seq = fromLeft + std::string((size_t)newGapLength, 'N') + fromRight;
     Fix s = trimPatch(g, start, seq, stop);
     return s.patch.empty() ? noSolution : s;
@@ -1519,12 +1552,15 @@ static int polishImpl(const pg_reads* R, const pg_params* params, int32_t n_cont
                       int32_t fix_indels, int32_t iupac, int32_t diploid, int32_t vcf_qe, const char* fasta_path,
                       const char* vcf_path, const char* changes_path, const char* vcf_date, const char* vcf_source,
                       const char* vcf_args, const char* vcf_ref, int32_t fix_gaps, int32_t fix_local, int32_t K,
-                      const int64_t* name_id, int64_t* tied_sets) {
+                      const int64_t* name_id, int64_t* tied_sets, int32_t fix_breaks) {
   Params P = toParams(params);
   try {
     // BamFile.scan runs first when strays are tracked (S/GenomeFile.scala:89-92)
     std::unique_ptr<Reassembly> ra;
-    if (fix_gaps || fix_local) ra.reset(new Reassembly(R, name_id, P, K, n_contigs));
+    if (fix_gaps || fix_local) {
+      ra.reset(new Reassembly(R, name_id, P, K, n_contigs));
+      ra->fixBreaks = fix_breaks != 0;
+    }
     // region read ranges: reads are sorted by (ref_id, pos); take each contig's span
     std::vector<int64_t> cb(n_contigs, 0), ce(n_contigs, 0);
     {
@@ -1618,24 +1654,25 @@ int or_polish(const pg_reads* R, const pg_params* params, int32_t n_contigs, con
               const char* vcf_args, const char* vcf_ref) {
   return polishImpl(R, params, n_contigs, names, lens, bases, chunk_size, fix_snps, fix_indels, iupac, diploid,
                     vcf_qe, fasta_path, vcf_path, changes_path, vcf_date, vcf_source, vcf_args, vcf_ref, 0, 0, 31,
-                    nullptr, nullptr);
+                    nullptr, nullptr, 0);
 }
 
 // The same with the fix types gaps and local as well (GapFiller fillGap /
 // fixBreak, S/GenomeRegion.scala:382-410): K is Assembler.K (--K), name_id the
 // read name of each read as an id (mates share one; NULL: no stray mates, as
-// --nostrays).  *tied_sets receives the count of solution sets of more than
-// four elements whose first element had to be taken in an order the reference
-// gets from its HashSet (see reassemble).
+// --nostrays), fix_breaks the experimental "breaks" fix (--variant).
+// *tied_sets receives the count of solution sets of more than four elements
+// whose first element had to be taken in an order the reference gets from its
+// HashSet (see reassemble).
 int or_polish_fix(const pg_reads* R, const pg_params* params, int32_t n_contigs, const char* const* names,
                   const int64_t* lens, const uint8_t* const* bases, int32_t chunk_size, int32_t fix_snps,
                   int32_t fix_indels, int32_t iupac, int32_t diploid, int32_t vcf_qe, const char* fasta_path,
                   const char* vcf_path, const char* changes_path, const char* vcf_date, const char* vcf_source,
                   const char* vcf_args, const char* vcf_ref, int32_t fix_gaps, int32_t fix_local, int32_t K,
-                  const int64_t* name_id, int64_t* tied_sets) {
+                  const int64_t* name_id, int64_t* tied_sets, int32_t fix_breaks) {
   return polishImpl(R, params, n_contigs, names, lens, bases, chunk_size, fix_snps, fix_indels, iupac, diploid,
                     vcf_qe, fasta_path, vcf_path, changes_path, vcf_date, vcf_source, vcf_args, vcf_ref, fix_gaps,
-                    fix_local, K, name_id, tied_sets);
+                    fix_local, K, name_id, tied_sets, fix_breaks);
 }
 
 // One --targets region end to end (S/GenomeFile.scala:215-250): processBam,

@@ -131,7 +131,8 @@ class pg_result(C.Structure):
 class pg_reassembly(C.Structure):
     _fields_ = [
         ("window", C.c_int32), ("is_gap", C.c_int32), ("region_start", C.c_int32), ("region_stop", C.c_int32),
-        ("break_start", C.c_int32), ("break_stop", C.c_int32), ("break_radius", C.c_int32), ("pad_", C.c_int32),
+        ("break_start", C.c_int32), ("break_stop", C.c_int32), ("break_radius", C.c_int32),
+        ("fix_breaks", C.c_int32),
         ("bases", C.c_void_p), ("orig", C.c_void_p),
     ]
 

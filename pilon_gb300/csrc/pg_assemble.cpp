@@ -10,8 +10,8 @@
 // base.  A path keeps its K-mers in order with, per K-mer, how often it occurs
 // and where it last occurred, so the List.contains / List.indexOf tests of the
 // reference walk take constant time.  Pilon.trSafe is always true there, so a
-// walk that meets a K-mer it has seen stops; multiClosure, fixBreaks and
-// fixNovel are off (their defaults).
+// walk that meets a K-mer it has seen stops; multiClosure and fixNovel are off
+// (their defaults); fixBreaks is a field of each job.
 #include <algorithm>
 #include <atomic>
 #include <cstdint>
@@ -340,8 +340,8 @@ Solution reassemble(const Graph& G, const pg_reassembly& job, int32_t& loopLen) 
     if ((diff < 0 ? -diff : diff) > 100000) ok = false;  // Pilon.gapMargin
   }
   if (ok) return solution;
-  if (!isGap) return none;
-  // a gap not closed: each side's consensus, with Ns between (:76-99)
+  if (!(isGap || (job.fix_breaks && loopLen == 0))) return none;
+  // a gap not closed (or a break, with --fix breaks): each side's consensus, with Ns between (:76-99)
   const std::string cl = consensusLeft(fromLeft), cr = consensusRight(fromRight);
   const int32_t newStart = start + (int32_t)cl.size(), newStop = stop - (int32_t)cr.size();
   bool matchesRef = false;  // partialMatchesReference (:264-281)
@@ -349,7 +349,7 @@ Solution reassemble(const Graph& G, const pg_reassembly& job, int32_t& loopLen) 
     matchesRef = cl == R.sub(job.bases, start, (int32_t)cl.size()) &&
                  cr == R.sub(job.bases, stop - (int32_t)cr.size(), (int32_t)cr.size());
   if ((newStart >= bs + 20 || newStop <= be - 20) && !matchesRef) {  // GapFiller.minExtend
-    const int32_t gapLen = std::max(10, newStop - newStart);           // Pilon.minGap
+    const int32_t gapLen = isGap ? std::max(10, newStop - newStart) : 10;  // Pilon.minGap
     Solution s = trimPatch(R, start, cl + std::string((size_t)gapLen, 'N') + cr, stop);
     return s.patch.empty() ? none : s;
   }

@@ -32,6 +32,7 @@ class Options:
     fix_indels: bool = True
     fix_gaps: bool = False          # "gaps": GapFiller.fillGap over runs of N
     fix_local: bool = False         # "local": GapFiller.fixBreak over possibleBreaks
+    fix_breaks: bool = False        # experimental "breaks" (--variant): unjoined breaks are opened
     K: int = 47                     # --K, Assembler.K
     strays: bool = True             # --nostrays clears it
     iupac: bool = False
@@ -203,7 +204,8 @@ def _reassemble(engine, regions, results, contigs, reads, params, opts):
         for (bs, be), is_gap in todo:
             lists.append(bam.recruit(c, bs, be))
             jobs.append(dict(window=len(lists) - 1, is_gap=is_gap, region_start=s, region_stop=e, break_start=bs,
-                             break_stop=be, break_radius=radius, bases=bases, orig=orig))
+                             break_stop=be, break_radius=radius, bases=bases, orig=orig,
+                             fix_breaks=opts.fix_breaks))
             owner.append(r)
     if not jobs:
         return

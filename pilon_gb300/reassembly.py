@@ -177,29 +177,64 @@ class BamState:
         MateMap.findStrays (:244-257) after the flank reads."""
         if self.bam_type == _abi.PG_BAM_UNPAIRED and self.params.long_read:
             return np.zeros(0, np.int64)  # recruitUnpaired skips long reads
-        if self.bam_type not in (_abi.PG_BAM_FRAGS, _abi.PG_BAM_UNPAIRED):
-            raise ValueError("local reassembly takes a frags or unpaired BAM")
+        if self.bam_type == _abi.PG_BAM_BAM:
+            raise ValueError("local reassembly takes a BAM of type frags, jumps or unpaired")
         flank = self.max_insert_size()
-        reads = self.reads_in_region(contig, max(s - flank, 1), e + flank)
+        fs, fe = max(s - flank, 1), e + flank  # flankRegion (S/BamFile.scala:359-364)
+        reads = self.reads_in_region(contig, fs, fe)
+        if self.bam_type == _abi.PG_BAM_JUMPS:
+            return self._bad_mates(reads, s, e, fs, fe)
         if not self.strays or self.bam_type == _abi.PG_BAM_UNPAIRED:
             return reads
-        names = self.reads.name_id[reads]
+        extra = self._find_strays(reads)
+        return np.concatenate([reads, extra]) if extra.size else reads
+
+    def _mate_map(self, reads):
+        """MateMap.addRead (S/BamFile.scala:234-238): name -> read for the first
+        and the other reads of pairs, the last read of a name winning; as
+        (sorted names, reads) twice."""
         first = (self.reads.flag[reads] & 0x40) != 0
-        m1, m2 = np.unique(names[first]), np.unique(names[~first])
+        return self._name_map(reads[first]), self._name_map(reads[~first])
+
+    def _find_strays(self, reads):
+        """MateMap(reads).findStrays (S/BamFile.scala:244-257): the strays' mates
+        of the names that have one end among the reads (in HashMap order in the
+        reference; sorted here, which the tally does not see)."""
+        (m1, _), (m2, _) = self._mate_map(reads)
         found = []
         # a first-of-pair read's mate is looked up among the second-of-pair strays, and back
         for mine, other, table in ((m1, m2, self._stray[1]), (m2, m1, self._stray[0])):
             alone = np.setdiff1d(mine, other, assume_unique=True)
             tn, ti = table
             if alone.size and tn.size:
-                k = np.searchsorted(tn, alone)
-                k = np.minimum(k, tn.size - 1)
-                hit = tn[k] == alone
-                found.append(ti[k[hit]])
-        if found:
-            extra = np.sort(np.concatenate(found))
-            reads = np.concatenate([reads, extra])
-        return reads
+                k = np.minimum(np.searchsorted(tn, alone), tn.size - 1)
+                found.append(ti[k[tn[k] == alone]])
+        return np.sort(np.concatenate(found)) if found else np.zeros(0, np.int64)
+
+    def _bad_mates(self, reads, s, e, fs, fe):
+        """BamFile.recruitBadMates (S/BamFile.scala:366-403) for a jumps BAM: of
+        each pair with both ends in the MateMap (with the strays' mates added),
+        the mate of an end that is mapped, not in a proper pair, oriented
+        towards the region's midpoint (when the BAM is almost all FR or RF)
+        and inside the flanks."""
+        r = self.reads
+        if r.name_id is None:
+            return np.zeros(0, np.int64)  # without names no pair is known
+        if self.strays:
+            reads = np.concatenate([reads, self._find_strays(reads)])  # MateMap.addStrays
+        (n1, i1), (n2, i2) = self._mate_map(reads)
+        both, k1, k2 = np.intersect1d(n1, n2, assume_unique=True, return_indices=True)
+        a = np.concatenate([i1[k1], i2[k2]])  # pairs(): (read1, read2) and (read2, read1)
+        b = np.concatenate([i2[k2], i1[k1]])
+        fl = r.flag[a].astype(np.int64)
+        rc = (fl & 0x10) != 0
+        st, en = r.pos[a].astype(np.int64), r.aend[a].astype(np.int64)
+        mid = (s + e) // 2
+        fr = ((st < mid) & ~rc) | ((en > mid) & rc)
+        pct = self.pct_fr()
+        good = fr if pct > 90 else (~fr if pct < 10 else np.ones(a.size, bool))  # minOrientationPct 10
+        keep = ((fl & 0x6) == 0) & good & (((st >= fs) & (st <= fe)) | ((en >= fs) & (en <= fe)))
+        return np.sort(b[keep])
 
 
 def gaps(ref, start, stop):

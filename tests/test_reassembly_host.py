@@ -46,8 +46,29 @@ def test_local_reassembly_matches_oracle(cfg4_small, K):
     assert out["vcf"].count(b"SVTYPE=INS") + out["vcf"].count(b"SVTYPE=DEL") >= 3
 
 
+def test_variant_mode_opens_breaks(cfg4_small):
+    """--variant adds the experimental "breaks" fix: a break that no join
+    closes, away from a tandem repeat, is opened with each side's consensus and
+    ten Ns (S/GapFiller.scala:76-99, S/Pilon.scala:232-236)."""
+    n, out = compare(cfg4_small, vcf=True, fix_local=True, fix_breaks=True, K=31)
+    assert any("N" in l.split()[3] for l in out["changes"].decode().splitlines())
+
+
 def test_local_reassembly_without_strays(cfg4_small):
     compare(cfg4_small, vcf=True, fix_local=True, K=31, strays=False)
+
+
+def test_jumps_recruit_bad_mates(cfg4_small):
+    """A jumps BAM recruits the mates of its improper pairs' anchors
+    (recruitBadMates, S/BamFile.scala:366-403) instead of the flank reads."""
+    params = _abi.default_params(bam_type=_abi.PG_BAM_JUMPS)
+    b = reassembly.BamState(cfg4_small.reads, params, 1)
+    r = cfg4_small.reads
+    lists = [b.recruit(0, s, s + 200) for s in range(20_000, 1_100_000, 50_000)]
+    assert sum(x.size for x in lists) > 0
+    for x in lists:
+        assert np.all((r.flag[x] & 0x2) == 0)  # only improper pairs' ends
+    compare(cfg4_small, params=params, vcf=True, fix_local=True, fix_gaps=True, K=31)
 
 
 def test_reassemblies_restore_the_sample(cfg4_small):
