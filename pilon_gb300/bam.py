@@ -37,9 +37,11 @@ def _lib():
         L.bam_fill.restype = i64
         L.bam_fill.argtypes = [vp, vp, i64] + [vp] * 15 + [C.c_int32]
         L.bam_encoded_size.restype = i64
-        L.bam_encoded_size.argtypes = [i64, vp, vp]
+        L.bam_encoded_size.argtypes = [i64, vp, vp, vp]
         L.bam_encode.restype = i64
-        L.bam_encode.argtypes = [i64] + [vp] * 16
+        L.bam_encode.argtypes = [i64] + [vp] * 17
+        L.bam_name_ids.restype = None
+        L.bam_name_ids.argtypes = [vp, vp, i64, vp]
         L.bgzf_scan.restype = i64
         L.bgzf_scan.argtypes = [vp, i64, vp, vp, vp, i64, C.POINTER(i64), C.POINTER(C.c_int32)]
         L.bgzf_inflate_blocks.restype = i64
@@ -71,12 +73,14 @@ def write_bam(path, names, lengths, reads, threads=None):
     r = reads
     L = _lib()
     n = r.n_reads
-    size = L.bam_encoded_size(n, r.n_cigar.ctypes.data, r.l_seq.ctypes.data)
+    nid = None if r.name_id is None else np.ascontiguousarray(r.name_id, np.int64)
+    nptr = None if nid is None else nid.ctypes.data
+    size = L.bam_encoded_size(n, r.n_cigar.ctypes.data, r.l_seq.ctypes.data, nptr)
     recs = np.empty(max(size, 1), np.uint8)
     L.bam_encode(n, r.pos.ctypes.data, r.tlen.ctypes.data, r.ref_id.ctypes.data, r.mate_ref_id.ctypes.data,
                  r.l_seq.ctypes.data, r.flag.ctypes.data, r.n_cigar.ctypes.data, r.mapq.ctypes.data,
                  r.seq.ctypes.data, r.qual.ctypes.data, r.cigar_off.ctypes.data, r.seq_off.ctypes.data,
-                 r.qual_off.ctypes.data, r.cigar.ctypes.data, None, recs.ctypes.data)
+                 r.qual_off.ctypes.data, r.cigar.ctypes.data, None, nptr, recs.ctypes.data)
     payload = memoryview(bytes(hdr) + recs[:size].tobytes())
     chunks = [payload[k:k + _BLOCK] for k in range(0, len(payload), _BLOCK)]
     with ThreadPoolExecutor(_threads(threads)) as ex:
@@ -165,8 +169,11 @@ def _header(view):
     return names, lengths, off
 
 
-def read_bam(path, threads=None):
-    """Returns (reference names, reference lengths, ReadStore) of a BAM file."""
+def read_bam(path, threads=None, names=False):
+    """Returns (reference names, reference lengths, ReadStore) of a BAM file.
+    names=True also gives the store its read-name ids (store.name_id), which
+    local reassembly pairs mates by (one more pass over the records)."""
+    want_names = names
     with open(path, "rb") as f:
         # mapped, so that reading the file overlaps the threads' inflating
         raw = mmap.mmap(f.fileno(), 0, access=mmap.ACCESS_READ) if os.fstat(f.fileno()).st_size else b""
@@ -200,4 +207,7 @@ def read_bam(path, threads=None):
                st.n_cigar.ctypes.data, st.mapq.ctypes.data, st.seq.ctypes.data, st.qual.ctypes.data,
                st.cigar_off.ctypes.data, st.seq_off.ctypes.data, st.qual_off.ctypes.data, st.cigar.ctypes.data,
                _threads(threads))
+    if want_names:
+        st.name_id = np.empty(n, np.int64)
+        L.bam_name_ids(recs.ctypes.data, starts.ctypes.data, n, st.name_id.ctypes.data)
     return names, lengths, st

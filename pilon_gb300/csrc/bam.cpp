@@ -17,6 +17,8 @@
 #include <cstdio>
 #include <cstring>
 #include <thread>
+#include <string_view>
+#include <unordered_map>
 #include <vector>
 
 namespace {
@@ -156,12 +158,35 @@ int64_t bam_fill(const uint8_t* buf, const int64_t* starts, int64_t recs, int32_
   return recs;
 }
 
-// Bytes of the BAM records of reads [0, n) (read names "r<index>").
-int64_t bam_encoded_size(int64_t n, const uint16_t* n_cigar, const int32_t* l_seq) {
+// The read name of read i: "p<name_id[i]>" (mates share it) or, without name
+// ids, "r<i>"; returns its length with the NUL.
+static int read_name(char* name, size_t cap, const int64_t* name_id, int64_t i) {
+  return (name_id ? std::snprintf(name, cap, "p%lld", (long long)name_id[i])
+                  : std::snprintf(name, cap, "r%lld", (long long)i)) + 1;
+}
+
+// Read-name ids of the records at starts: the first record with a name gets
+// the next id, later records with the same name (mates, other alignments) its
+// id, as htsjdk's getReadName strings compare.  Single pass, exact.
+void bam_name_ids(const uint8_t* buf, const int64_t* starts, int64_t recs, int64_t* out) {
+  std::unordered_map<std::string_view, int64_t> ids;
+  ids.reserve((size_t)(recs / 2 + 1));
+  for (int64_t i = 0; i < recs; i++) {
+    const uint8_t* r = buf + starts[i] + 4;
+    const uint32_t l_name = r[8];
+    const char* nm = reinterpret_cast<const char*>(r + 32);
+    const size_t len = l_name > 0 ? strnlen(nm, l_name) : 0;  // up to the NUL
+    auto it = ids.emplace(std::string_view(nm, len), (int64_t)ids.size()).first;
+    out[i] = it->second;
+  }
+}
+
+// Bytes of the BAM records of reads [0, n) (read names as read_name gives them).
+int64_t bam_encoded_size(int64_t n, const uint16_t* n_cigar, const int32_t* l_seq, const int64_t* name_id) {
   int64_t total = 0;
   char name[32];
   for (int64_t i = 0; i < n; i++) {
-    const int ln = std::snprintf(name, sizeof name, "r%lld", (long long)i) + 1;
+    const int ln = read_name(name, sizeof name, name_id, i);
     total += 4 + 32 + ln + 4 * (int64_t)n_cigar[i] + (l_seq[i] + 1) / 2 + l_seq[i];
   }
   return total;
@@ -173,11 +198,11 @@ int64_t bam_encode(int64_t n, const int32_t* pos, const int32_t* tlen, const int
                    const int32_t* mate_ref_id, const int32_t* l_seq, const uint16_t* flag, const uint16_t* n_cigar,
                    const uint8_t* mapq, const uint8_t* seq, const uint8_t* qual, const int64_t* cigar_off,
                    const int64_t* seq_off, const int64_t* qual_off, const uint32_t* cigar,
-                   const int32_t* mate_pos, uint8_t* out) {
+                   const int32_t* mate_pos, const int64_t* name_id, uint8_t* out) {
   int64_t o = 0;
   char name[32];
   for (int64_t i = 0; i < n; i++) {
-    const int ln = std::snprintf(name, sizeof name, "r%lld", (long long)i) + 1;
+    const int ln = read_name(name, sizeof name, name_id, i);
     const int32_t ls = l_seq[i];
     const uint16_t nc = n_cigar[i];
     const int32_t bs = 32 + ln + 4 * nc + (ls + 1) / 2 + ls;

@@ -211,3 +211,22 @@ def test_walk_edge_of_region_raises_like_the_reference():
     edges = _graph(sample, 31)
     [(start, was, patch, status, loop)] = reassemble(edges, 31, [_job(sample, 1, 20, 50)])
     assert status == _abi.PG_ERR_INDEX
+
+
+def test_bam_read_names_pair_mates(cfg4_small, tmp_path):
+    """Read names survive a BAM round trip as ids (mates share one), so a store
+    read from a BAM recruits the same stray mates as the simulator's store."""
+    from pilon_gb300 import bam
+    d = cfg4_small
+    path = str(tmp_path / "reads.bam")
+    bam.write_bam(path, d.names, [c.size for c in d.contigs], d.reads)
+    _, _, st = bam.read_bam(path, names=True)
+    a, b = d.reads.name_id, st.name_id
+    # the same partition of reads into names
+    assert np.unique(np.stack([a, b], 1), axis=0).shape[0] == np.unique(a).size == np.unique(b).size
+    P = _abi.default_params()
+    x, y = reassembly.BamState(d.reads, P, 1), reassembly.BamState(st, P, 1)
+    for s in range(30_000, 1_100_000, 70_000):
+        assert np.array_equal(x.recruit(0, s, s + 300), y.recruit(0, s, s + 300))
+    _, _, plain = bam.read_bam(path)
+    assert plain.name_id is None
