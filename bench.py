@@ -313,6 +313,28 @@ def kmer_bench(eng, ds, params, args, threads, K=31, radius=500):
     return out
 
 
+def fix_all_bench(eng, ds, params, K=31):
+    """--fix snps,indels,gaps,local over the whole 120 Mb workload through the
+    polishing driver (FASTA and changes written, no VCF), against the same run
+    with --fix snps,indels: the local-reassembly steps' times (scan and
+    recruitment on the host, the K-mer tally of every window on the device,
+    the graph walks on host threads) and counts."""
+    import tempfile
+    from pilon_gb300.polish import Options, polish
+    out = {"K": K, "timing": "host wall clock of polish(); the reassembly steps timed inside it"}
+    with tempfile.TemporaryDirectory() as d:
+        for key, kw in (("snps_indels", {}), ("all", dict(fix_gaps=True, fix_local=True, K=K))):
+            opts = Options(vcf=False, **kw)
+            opts.stats = {}
+            t0 = time.perf_counter()
+            polish(eng, ds.names, ds.contigs, ds.reads, params, os.path.join(d, key), opts)
+            out[key + "_s"] = time.perf_counter() - t0
+            if opts.stats:
+                out["reassembly"] = opts.stats
+        out["changes_lines"] = sum(1 for _ in open(os.path.join(d, "all.changes")))
+    return out
+
+
 def extra_workload(config, args, params, device, peak, peaks):
     """A second workload on its own engine context: device-timed steps (CUDA
     events, after warm-up) and the walk kernel's roofline, as for the main one."""
@@ -677,6 +699,8 @@ def main():
                          "host threads take alternate steps"}
 
     kmer = kmer_bench(eng, ds, params, args, threads) if args.config == 4 and rank == 0 else None
+    if kmer is not None:
+        kmer["fix_all"] = fix_all_bench(eng, ds, params)
 
     # BAM decoding into the read store (the htsjdk side of BamFile), host threads
     bam_decode = None

@@ -185,7 +185,11 @@ def _reassemble(engine, regions, results, contigs, reads, params, opts):
     382-413) for every region: one K-mer tally for all windows, then the walks.
     The insert statistics a region's GapFiller sees are those of the scan and
     of the regions processed up to it, as Pilon processes chunks in order."""
+    import time
+    stats = getattr(opts, "stats", None)  # a dict receives the step times and counts when given
+    t0 = time.perf_counter()
     bam = reassembly.BamState(reads, params, len(contigs), strays=opts.strays)
+    t1 = time.perf_counter()
     breaks = engine.find_breaks() if opts.fix_local else {}
     jobs, lists, owner = [], [], []
     for r, (reg, res) in enumerate(zip(regions, results)):
@@ -207,11 +211,19 @@ def _reassemble(engine, regions, results, contigs, reads, params, opts):
                              break_stop=be, break_radius=radius, bases=bases, orig=orig,
                              fix_breaks=opts.fix_breaks))
             owner.append(r)
+    t2 = time.perf_counter()
     if not jobs:
         return
     from .engine import reassemble, EngineError
     edges = engine.kmer_tally_reads(lists, opts.K, params)
+    t3 = time.perf_counter()
     fixes = reassemble(edges, opts.K, jobs)
+    t4 = time.perf_counter()
+    if stats is not None:
+        stats.update(scan_s=t1 - t0, recruit_s=t2 - t1, tally_s=t3 - t2, walk_s=t4 - t3, windows=len(jobs),
+                     reads=int(sum(len(x) for x in lists)), edges=int(edges.size),
+                     tally_device_ms=engine.last_tally_stats()[0] if hasattr(engine, "last_tally_stats") else None,
+                     fixes=int(sum(1 for f in fixes if f[0] > 0)))
     for j, r, (start, was, patch, status, _loop) in zip(jobs, owner, fixes):
         if status:
             raise EngineError(status, f"region {r}: the reference would throw reassembling "

@@ -115,6 +115,7 @@ class BamState:
         placed = rid[:int(unplaced[0])] if unplaced.size else rid
         self.cb = np.searchsorted(placed, np.arange(n_contigs), side="left").astype(np.int64)
         self.ce = np.searchsorted(placed, np.arange(n_contigs), side="right").astype(np.int64)
+        self.pos = reads.pos.astype(np.int64)  # searched with int64 bounds without a cast per search
         self.end = np.where((flag & 0x4) != 0, reads.pos, reads.aend).astype(np.int64)
         span = self.end - reads.pos.astype(np.int64) + 1
         self.span = np.array([int(span[a:b].max()) if b > a else 1 for a, b in zip(self.cb, self.ce)], np.int64)
@@ -164,9 +165,9 @@ class BamState:
         queryOverlapping, the alignment [start, end] (end = start for an
         unmapped read) meeting [s, e], then validateRead."""
         a, b = int(self.cb[contig]), int(self.ce[contig])
-        pos = self.reads.pos
-        lo = a + int(np.searchsorted(pos[a:b], s - int(self.span[contig]), side="left"))
-        hi = a + int(np.searchsorted(pos[a:b], e, side="right"))
+        pos = self.pos
+        lo = a + int(np.searchsorted(pos[a:b], np.int64(s - int(self.span[contig])), side="left"))
+        hi = a + int(np.searchsorted(pos[a:b], np.int64(e), side="right"))
         idx = np.arange(lo, hi, dtype=np.int64)
         keep = (pos[lo:hi] <= e) & (self.end[lo:hi] >= s) & self.valid[lo:hi]
         return idx[keep]
