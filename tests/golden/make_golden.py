@@ -1,7 +1,7 @@
 """Writes tests/golden/oracle_small.json: digests of the oracle's FASTA, VCF and
 changes for a small seeded workload (the 50 kb workload scaled to 10 kb, plus
-the same 50 kb workload with 7 kb regions), and per-field array digests of one
-region.  The reference has no golden files; these pin the oracle against
+the same 50 kb workload with 7 kb regions, and 300 kb of the repeat workload
+with a gap under --fix all), and per-field array digests of one region.  The reference has no golden files; these pin the oracle against
 regressions.  Run: python tests/golden/make_golden.py"""
 import hashlib
 import json
@@ -27,6 +27,17 @@ def digests():
             assert rc == 0
             for ext in ("fasta", "vcf", "changes"):
                 out[f"{label}.{ext}"] = hashlib.sha256(open(f"{pre}.{ext}", "rb").read()).hexdigest()
+    # --fix snps,indels,gaps,local --K 31 on 300 kb of the repeat workload with a 60 bp gap
+    ds = synth.generate(4, scale=0.0025)
+    ref = ds.contigs[0].copy()
+    ref[150_000:150_060] = ord("N")
+    ds.contigs = [ref]
+    with tempfile.TemporaryDirectory() as d:
+        pre = os.path.join(d, "pilon")
+        assert oracle.polish(ds.reads, p, ds.names, ds.contigs, pre, fix_gaps=True, fix_local=True, K=31) == 0
+        for ext in ("fasta", "vcf", "changes"):
+            out[f"cfg4_300kb_fix_all.{ext}"] = hashlib.sha256(open(f"{pre}.{ext}", "rb").read()).hexdigest()
+        out["cfg4_300kb_fix_all.changes_lines"] = sum(1 for _ in open(pre + ".changes"))
     ds = synth.generate(1, scale=0.2)
     res = oracle.process_region(ds.reads, p, ds.contigs[0], 0, 1, ds.contigs[0].size)
     for f in ["count", "qual_sum", "mq_sum", "q_sum", "phys_cov", "insert_size", "bad_pair", "deletions",
