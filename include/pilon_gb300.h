@@ -276,7 +276,7 @@ pg_status pg_fetch_changes(pg_ctx *ctx, pg_change *out, int64_t cap, int64_t *n_
 
 /* Launch shape of the pileup walk kernel: tile width (positions per CTA,
  * a power of two in [256, 4096]), warps per CTA (1..16) and variant (lanes
- * per read: 0 = 32, 1 = 16, 2 = 8, 3 = 4, 4 = 2); 0 / -1 keep the current value.  The host
+ * per read: 0 = 32, 1 = 16, 2 = 8, 3 = 4); 0 / -1 keep the current value.  The host
  * package's autotuner picks these. */
 pg_status pg_set_tuning(pg_ctx *ctx, int32_t tile_width, int32_t warps_per_cta, int32_t variant);
 

@@ -10,7 +10,7 @@ from .build import BUILD
 CACHE = os.path.join(BUILD, "autotune.json")
 TILES = (256, 512, 1024, 2048, 4096)
 WARPS = (8, 16)
-VARIANTS = (0, 1, 2, 3, 4)   # lanes per simple read: 32, 16, 8, 4, 2
+VARIANTS = (0, 1, 2, 3)   # lanes per simple read: 32, 16, 8, 4
 
 
 def _load():

@@ -320,7 +320,7 @@ pg_status pg_set_tuning(pg_ctx* c, int32_t tile_width, int32_t warps_per_cta, in
     c->warps = warps_per_cta;
   }
   if (variant >= 0) {
-    if (variant > 4) return fail(c, PG_ERR_ARG, "variant must be 0, 1, 2, 3 or 4");
+    if (variant > 3) return fail(c, PG_ERR_ARG, "variant must be 0, 1, 2 or 3");
     c->packed = variant;
   }
   return PG_OK;

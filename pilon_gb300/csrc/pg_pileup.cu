@@ -417,7 +417,7 @@ constexpr size_t walk_smem() {
 // MINB: resident CTAs the register allocation must allow: 2 CTAs of up to 512
 // threads (16 warps, up to 64 registers per thread) or 5 CTAs of up to 256
 // threads (8 warps, up to 48 registers: 40 warps per SM).  G: lanes per entry
-// (2, 4, 8, 16, 32).
+// (4, 8, 16, 32).
 template <int T, int MINB, int G>
 __global__ void __launch_bounds__(MINB >= 4 ? 256 : 512, MINB) k_walk(WalkArgs a, int32_t tile_begin,
                                                                       int32_t tile_end) {
@@ -725,7 +725,7 @@ static void launch_walk_v(const WalkArgs& a, int32_t tile_begin, int32_t tile_co
   }
 }
 
-// variant: lanes per simple read (0: 32, 1: 16, 2: 8, 3: 4, 4: 2).
+// variant: lanes per simple read (0: 32, 1: 16, 2: 8, 3: 4).
 void launch_walk(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int warps, cudaStream_t s) {
   if (tile_count <= 0) return;
   const int lanes = a.packed;
@@ -733,14 +733,12 @@ void launch_walk(const WalkArgs& a, int32_t tile_begin, int32_t tile_count, int 
     if (lanes == 0) launch_walk_v<5, 32>(a, tile_begin, tile_count, warps, s);
     else if (lanes == 1) launch_walk_v<5, 16>(a, tile_begin, tile_count, warps, s);
     else if (lanes == 2) launch_walk_v<5, 8>(a, tile_begin, tile_count, warps, s);
-    else if (lanes == 3) launch_walk_v<5, 4>(a, tile_begin, tile_count, warps, s);
-    else launch_walk_v<5, 2>(a, tile_begin, tile_count, warps, s);
+    else launch_walk_v<5, 4>(a, tile_begin, tile_count, warps, s);
   } else {
     if (lanes == 0) launch_walk_v<2, 32>(a, tile_begin, tile_count, warps, s);
     else if (lanes == 1) launch_walk_v<2, 16>(a, tile_begin, tile_count, warps, s);
     else if (lanes == 2) launch_walk_v<2, 8>(a, tile_begin, tile_count, warps, s);
-    else if (lanes == 3) launch_walk_v<2, 4>(a, tile_begin, tile_count, warps, s);
-    else launch_walk_v<2, 2>(a, tile_begin, tile_count, warps, s);
+    else launch_walk_v<2, 4>(a, tile_begin, tile_count, warps, s);
   }
 }
 
