@@ -122,12 +122,12 @@ def contig_regions(contig_len, chunk_size=10_000_000):
 def polish(reads, params, names, contigs, out_prefix, chunk_size=10_000_000, fix_snps=True, fix_indels=True,
            iupac=False, diploid=False, vcf_qe=False, vcf_date="20260101", vcf_source="Pilon version [COMMIT] [DATE]",
            vcf_args="", vcf_ref="file:/genome.fasta", fix_gaps=False, fix_local=False, K=47, strays=True,
-           stats=None, fix_breaks=False):
+           stats=None, fix_breaks=False, vcf=True):
     """GenomeFile.processRegions with --fix snps,indels[,gaps,local] --vcf
     --changes; writes out_prefix.fasta / .vcf / .changes.  With gaps or local,
     K is --K and the stray mates come from reads.name_id (strays=False is
     --nostrays), fix_breaks is the experimental "breaks" fix; stats (a dict)
-    receives 'tied_sets'."""
+    receives 'tied_sets'; vcf=False writes no VCF."""
     L = lib()
     n = len(contigs)
     arrs = [np.ascontiguousarray(c, np.uint8) for c in contigs]
@@ -138,7 +138,7 @@ def polish(reads, params, names, contigs, out_prefix, chunk_size=10_000_000, fix
     ab = reads.to_abi()
     args = (C.byref(ab), C.byref(params), n, C.cast(nptrs, C.c_void_p), lens.ctypes.data,
             C.cast(ptrs, C.c_void_p), chunk_size, int(fix_snps), int(fix_indels), int(iupac), int(diploid),
-            int(vcf_qe), (out_prefix + ".fasta").encode(), (out_prefix + ".vcf").encode(),
+            int(vcf_qe), (out_prefix + ".fasta").encode(), (out_prefix + ".vcf").encode() if vcf else None,
             (out_prefix + ".changes").encode(), vcf_date.encode(), vcf_source.encode(), vcf_args.encode(),
             vcf_ref.encode())
     if not (fix_gaps or fix_local):

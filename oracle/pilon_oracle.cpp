@@ -20,8 +20,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <map>
 #include <memory>
+#include <thread>
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
@@ -481,9 +483,12 @@ struct Fix {
 
 struct GenomeRegion;
 // Local reassembly of one gap or break (GapFiller.fillGap / fixBreak,
-// S/GapFiller.scala:39-100); defined with the graph walk below.
+// S/GapFiller.scala:39-100) with the BAM's insert statistics as the region
+// sees them; defined with the graph walk below.
 struct Reassembly;
-Fix reassemble(const GenomeRegion& g, Reassembly& ra, int32_t bs, int32_t be, bool isGap);
+struct BamStats;
+Fix reassemble(const GenomeRegion& g, const Reassembly& ra, const BamStats& st, int32_t bs, int32_t be, bool isGap,
+               int64_t& tiedSets);
 
 struct GenomeRegion {
   std::string name;
@@ -644,9 +649,11 @@ struct GenomeRegion {
     changeMap[i] = {kind, i};
   }
 
-  // identifyAndFixIssues (:307-414); ra (fix types gaps / local) may be null
-  void identifyAndFixIssues(bool fixSnps, bool fixIndels, bool iupac, bool longread, Reassembly* ra = nullptr,
-                            bool fixGaps = false, bool fixLocal = false) {
+  int64_t tiedSets = 0;  // see breakJoins in reassemble
+
+  // identifyAndFixIssues (:307-414); ra and st (fix types gaps / local) may be null
+  void identifyAndFixIssues(bool fixSnps, bool fixIndels, bool iupac, bool longread, const Reassembly* ra = nullptr,
+                            const BamStats* st = nullptr, bool fixGaps = false, bool fixLocal = false) {
     for (auto& kv : changeMap) {
       int32_t i = kv.first;
       int kind = kv.second.first;
@@ -675,13 +682,13 @@ struct GenomeRegion {
     fixIssues(snpFixList);
     if (ra && fixGaps) {  // :383-393, each gap in locus order
       for (auto& gp : gaps()) {
-        Fix f = reassemble(*this, *ra, gp.first, gp.second, true);
+        Fix f = reassemble(*this, *ra, *st, gp.first, gp.second, true, tiedSets);
         if (f.locus > 0) bigFixList.push_back(f);
       }
     }
     if (ra && fixLocal) {  // :396-410
       for (auto& br : possibleBreaks()) {
-        Fix f = reassemble(*this, *ra, br.first, br.second, false);
+        Fix f = reassemble(*this, *ra, *st, br.first, br.second, false, tiedSets);
         if (f.locus > 0 && std::max(f.was.size(), f.patch.size()) > 10) bigFixList.push_back(f);
       }
     }
@@ -1069,6 +1076,30 @@ static std::unordered_map<std::string, PileUp> tallyReads(const pg_reads* R, con
   return pileups;
 }
 
+// BamFile's insert statistics (S/BamFile.scala:156-220): insertStatsFR / RF /
+// Unpaired, and what GapFiller reads of them.
+struct BamStats {
+  InsertStats fr, rf, un;
+  int32_t bamType = PG_BAM_FRAGS;
+  void addInsert(int32_t insertSize, bool rc, bool unpaired) {  // :194-202
+    bool frr = (insertSize > 0) ^ rc;
+    if (insertSize > 0 && insertSize < hugeInsert(bamType)) {
+      if (unpaired) un.add(insertSize); else if (frr) fr.add(insertSize); else rf.add(insertSize);
+    }
+  }
+  void addRegion(const GenomeRegion& g);  // BamFile.process's addInsert calls (:137)
+  int64_t pctFR() const { return pctL(fr.count, fr.count + rf.count + un.count); }  // :204
+  double insertSizeMean() const { return pctFR() >= 50 ? isMean(fr) : isMean(rf); }  // :208-210
+  int32_t maxInsertSize() const {  // :216-220
+    int32_t m = std::max(isMaxInsert(fr), std::max(isMaxInsert(rf), isMaxInsert(un)));
+    return m > 0 ? m : (bamType == PG_BAM_FRAGS ? 500 : 10000);
+  }
+  int32_t breakRadius(int32_t K) const {  // S/GapFiller.scala:357-362 (one frags BAM, or none)
+    int32_t insertMean = bamType == PG_BAM_FRAGS ? javaL2I(javaRound(insertSizeMean())) : 0;
+    return std::max(3 * K, insertMean);
+  }
+};
+
 struct Reassembly {
   const pg_reads* R;
   const int64_t* nameId;  // the read name of each read as an id; null: no names (no stray mates)
@@ -1076,14 +1107,14 @@ struct Reassembly {
   int32_t K;
   bool strays;
   bool fixBreaks = false;  // --fix breaks (--variant): breaks get the partial fill of gaps
-  InsertStats fr, rf, un;  // insertStatsFR / RF / Unpaired: the scan plus every region processed so far
+  BamStats scanStats;      // the statistics of BamFile.scan
   std::unordered_map<int64_t, int64_t> stray1, stray2;  // strayMateMap readMap1 / readMap2 (:222-281)
   std::vector<int64_t> cb, ce;                           // each contig's read range
   std::vector<int32_t> span;                             // longest alignment span of each contig's reads
-  int64_t tiedSets = 0;  // solution sets of more than four with tied lengths (see breakJoins)
 
   Reassembly(const pg_reads* r, const int64_t* names, const Params& p, int32_t k, int32_t nContigs)
       : R(r), nameId(names), P(p), K(k), strays(names != nullptr) {
+    scanStats.bamType = P.bamType;
     cb.assign(nContigs, 0); ce.assign(nContigs, 0); span.assign(nContigs, 1);
     int64_t i = 0;
     for (int32_t c = 0; c < nContigs; c++) {
@@ -1098,41 +1129,21 @@ struct Reassembly {
     }
     scan(nContigs);
   }
-  void addInsert(int32_t insertSize, bool rc, bool unpaired) {  // :194-202
-    bool frr = (insertSize > 0) ^ rc;
-    if (insertSize > 0 && insertSize < hugeInsert(P.bamType)) {
-      if (unpaired) un.add(insertSize); else if (frr) fr.add(insertSize); else rf.add(insertSize);
-    }
-  }
   void scan(int32_t nContigs) {  // :295-337 (every contig is of interest)
     for (int64_t i = 0; i < R->n_reads; i++) {
       uint16_t fl = R->flag[i];
       if (!validateRead(fl, P) || (fl & 0x4)) continue;
       if (fl & 0x1) {
-        if (fl & 0x2) addInsert(R->tlen[i], fl & 0x10, false);
+        if (fl & 0x2) scanStats.addInsert(R->tlen[i], fl & 0x10, false);
         else if (strays && !(fl & 0x8)) {
           bool soi = (R->ref_id[i] >= 0 && R->ref_id[i] < nContigs) ||
                      (R->mate_ref_id[i] >= 0 && R->mate_ref_id[i] < nContigs);
           if (soi) ((fl & 0x40) ? stray1 : stray2)[nameId[i]] = i;
         }
       } else {
-        addInsert(R->l_seq[i], fl & 0x10, true);
+        scanStats.addInsert(R->l_seq[i], fl & 0x10, true);
       }
     }
-  }
-  void addRegion(const GenomeRegion& g) {  // BamFile.process's addInsert calls (:137)
-    fr.count += g.fr.count; fr.sum += g.fr.sum; fr.sumSq += g.fr.sumSq;
-    rf.count += g.rf.count; rf.sum += g.rf.sum; rf.sumSq += g.rf.sumSq;
-  }
-  int64_t pctFR() const { return pctL(fr.count, fr.count + rf.count + un.count); }  // :204
-  double insertSizeMean() const { return pctFR() >= 50 ? isMean(fr) : isMean(rf); }  // :208-210
-  int32_t maxInsertSize() const {  // :216-220
-    int32_t m = std::max(isMaxInsert(fr), std::max(isMaxInsert(rf), isMaxInsert(un)));
-    return m > 0 ? m : (P.bamType == PG_BAM_FRAGS ? 500 : 10000);
-  }
-  int32_t breakRadius() const {  // S/GapFiller.scala:357-362 (one frags BAM, or none)
-    int32_t insertMean = P.bamType == PG_BAM_FRAGS ? javaL2I(javaRound(insertSizeMean())) : 0;
-    return std::max(3 * K, insertMean);
   }
   std::vector<int64_t> readsInRegion(int32_t c, int32_t s, int32_t e) const {  // :339-344
     // queryOverlapping: the alignment [start, end] (end = start when unmapped) meets [s, e]
@@ -1163,10 +1174,10 @@ struct Reassembly {
     std::sort(found.begin(), found.end());
     return found;
   }
-  std::vector<int64_t> recruitReads(int32_t c, int32_t s, int32_t e) const {
+  std::vector<int64_t> recruitReads(const BamStats& st, int32_t c, int32_t s, int32_t e) const {
     // GapFiller.recruitReads (S/GapFiller.scala:364-402) for the one BAM
     if (P.bamType == PG_BAM_UNPAIRED && P.longRead) return {};  // recruitUnpaired with --nanopore/--pacbio
-    int32_t flank = maxInsertSize();
+    int32_t flank = st.maxInsertSize();
     int32_t fs = std::max(s - flank, 1), fe = e + flank;  // flankRegion (S/BamFile.scala:359-364)
     std::vector<int64_t> reads = readsInRegion(c, fs, fe);
     std::unordered_map<int64_t, int64_t> m1, m2;  // MateMap(reads)
@@ -1176,7 +1187,7 @@ struct Reassembly {
       if (strays)
         for (int64_t i : findStrays(m1, m2)) ((R->flag[i] & 0x40) ? m1 : m2)[nameId[i]] = i;  // addStrays
       int32_t midpoint = (s + e) / 2;
-      int64_t frPct = pctFR();
+      int64_t frPct = st.pctFR();
       std::vector<int64_t> mates;
       for (auto& kv : m1) {  // pairs(): (read1, read2) and (read2, read1) of each name in both maps
         auto it = m2.find(kv.first);
@@ -1202,6 +1213,11 @@ struct Reassembly {
     return reads;
   }
 };
+
+void BamStats::addRegion(const GenomeRegion& g) {
+  fr.count += g.fr.count; fr.sum += g.fr.sum; fr.sumSq += g.fr.sumSq;
+  rf.count += g.rf.count; rf.sum += g.rf.sum; rf.sumSq += g.rf.sumSq;
+}
 
 // The K-mer graph walk of one Assembler (S/Assembler.scala:164-284).
 struct GraphWalk {
@@ -1360,9 +1376,10 @@ static std::string consensusFromRight(const std::vector<std::string>& seqs) {  /
 
 // GapFiller.assembleAcrossBreak (S/GapFiller.scala:49-100) with
 // assembleIntoBreak (:125-159) and breakJoins / joinBreak (:161-218).
-Fix reassemble(const GenomeRegion& g, Reassembly& ra, int32_t bs, int32_t be, bool isGap) {
+Fix reassemble(const GenomeRegion& g, const Reassembly& ra, const BamStats& st, int32_t bs, int32_t be, bool isGap,
+               int64_t& tiedSets) {
   const Fix noSolution{0, "", "", 2};
-  std::vector<int64_t> reads = ra.recruitReads(g.contigId, bs, be);
+  std::vector<int64_t> reads = ra.recruitReads(st, g.contigId, bs, be);
   GraphWalk w;
   w.K = ra.K;
   {
@@ -1377,7 +1394,7 @@ Fix reassemble(const GenomeRegion& g, Reassembly& ra, int32_t bs, int32_t be, bo
       }
     }
   }
-  int32_t radius = ra.breakRadius();
+  int32_t radius = st.breakRadius(ra.K);
   int32_t start = std::max(bs - radius, g.start);
   int32_t stop = std::min(be + 1 + radius, g.stop);
   std::string left = g.subString(start, bs - start);
@@ -1407,7 +1424,7 @@ Fix reassemble(const GenomeRegion& g, Reassembly& ra, int32_t bs, int32_t be, bo
   if (lengths.size() == 1) {
     if (set.size() > 4 && solutions.size() > 1 &&
         solutions[1].patch.size() + solutions[1].was.size() == solutions[0].patch.size() + solutions[0].was.size())
-      ra.tiedSets++;  // the reference takes the first of a HashSet's order here
+      tiedSets++;  // the reference takes the first of a HashSet's order here
     solutions.resize(1);
   }
   Fix solution = solutions.size() == 1 ? solutions[0] : noSolution;
@@ -1580,14 +1597,52 @@ static int polishImpl(const pg_reads* R, const pg_params* params, int32_t n_cont
         regs[c].push_back(new GenomeRegion(names[c], c, bases[c], lens[c], (int32_t)b,
                                            (int32_t)std::min<int64_t>(lens[c], b + cs - 1), P));
     }
-    for (int32_t c = 0; c < n_contigs; c++)
-      for (GenomeRegion* g : regs[c]) {
-        g->processBam(R, cb[c], ce[c]);
-        if (ra) ra->addRegion(*g);
-        g->postProcess();
-        g->identifyAndFixIssues(fix_snps, fix_indels, iupac, P.longRead != 0, ra.get(), fix_gaps, fix_local);
+    // GenomeFile.processRegions takes the regions one after another; a region's
+    // pileups do not depend on the others, and its reassembly reads the
+    // insert statistics of the scan and of the regions up to it, so the
+    // regions run on all host threads with those statistics taken in order.
+    std::vector<GenomeRegion*> flat;
+    for (auto& v : regs) flat.insert(flat.end(), v.begin(), v.end());
+    auto parallel = [&](auto&& body) {
+      std::atomic<size_t> next{0};
+      std::atomic<bool> failed{false};
+      auto work = [&]() {
+        for (size_t k; (k = next.fetch_add(1)) < flat.size();) {
+          try {
+            body(k);
+          } catch (IndexError&) {
+            failed = true;
+          }
+        }
+      };
+      unsigned nt = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)flat.size()));
+      std::vector<std::thread> th;
+      for (unsigned t = 1; t < nt; t++) th.emplace_back(work);
+      work();
+      for (auto& t : th) t.join();
+      if (failed) throw IndexError();
+    };
+    parallel([&](size_t k) {
+      GenomeRegion* g = flat[k];
+      g->processBam(R, cb[g->contigId], ce[g->contigId]);
+      g->postProcess();
+    });
+    std::vector<BamStats> seen(flat.size());
+    if (ra) {
+      BamStats acc = ra->scanStats;
+      for (size_t k = 0; k < flat.size(); k++) {
+        acc.addRegion(*flat[k]);
+        seen[k] = acc;
       }
-    if (ra && tied_sets) *tied_sets = ra->tiedSets;
+    }
+    parallel([&](size_t k) {
+      flat[k]->identifyAndFixIssues(fix_snps, fix_indels, iupac, P.longRead != 0, ra.get(), &seen[k], fix_gaps,
+                                    fix_local);
+    });
+    if (tied_sets) {
+      *tied_sets = 0;
+      for (auto* g : flat) *tied_sets += g->tiedSets;
+    }
     FILE* fc = changes_path ? fopen(changes_path, "w") : nullptr;
     FILE* ff = fasta_path ? fopen(fasta_path, "w") : nullptr;
     FILE* fv = vcf_path ? fopen(vcf_path, "w") : nullptr;

@@ -12,7 +12,9 @@ pileup counters, calls, scores, indel strings and statistics with the oracle
                             the per-region path
   eukaryotic-120Mb-repeats  twelve 10 Mb chunks of one contig (regions that
                             start inside the contig, reads fed to two chunks),
-                            and the K-mer graphs of all 2,000 reassembly windows
+                            the K-mer graphs of all 2,000 reassembly windows,
+                            and --fix snps,indels,gaps,local --K 31 end to end
+                            (FASTA and changes byte for byte)
 """
 import os
 
@@ -65,8 +67,13 @@ def test_full_many_contigs_batched_and_plain(engine):
     assert n_reg == 3000
 
 
-def test_full_eukaryotic_chunks_and_kmer_windows(engine):
-    ds = synth.generate(4)
+@pytest.fixture(scope="module")
+def cfg4():
+    return synth.generate(4)
+
+
+def test_full_eukaryotic_chunks_and_kmer_windows(engine, cfg4):
+    ds = cfg4
     regions = plan(ds)
     assert len(regions) == 12
     load(engine, ds)
@@ -106,3 +113,29 @@ def test_full_eukaryotic_chunks_and_kmer_windows(engine):
     have = rows(got, lambda w: w)
     assert have.shape == want.shape, (have.shape, want.shape)
     assert np.array_equal(have, want)
+
+
+def test_full_eukaryotic_fix_all(engine, cfg4):
+    """Pilon's default --fix (snps, indels, gaps, local) with --K 31 over the
+    whole 120 Mb workload: device pileups, breaks and K-mer tallies, host
+    recruitment and graph walks, against the oracle's restatement of
+    processRegions with GapFiller (on all host threads).  The FASTA and the
+    changes are compared byte for byte; the VCF, about 18 GB at this size, is
+    compared on 6 Mb of the workload in tests/test_gpu_reassembly.py."""
+    import tempfile
+    from pilon_gb300.polish import Options, polish
+    ds = cfg4
+    p = _abi.default_params()
+    stats = {}
+    with tempfile.TemporaryDirectory() as d:
+        g, o = os.path.join(d, "gpu"), os.path.join(d, "ora")
+        polish(engine, ds.names, ds.contigs, ds.reads, p, g, Options(vcf=False, fix_gaps=True, fix_local=True, K=31))
+        assert oracle.polish(ds.reads, p, ds.names, ds.contigs, o, fix_gaps=True, fix_local=True, K=31, vcf=False,
+                             stats=stats) == 0
+        for ext in ("changes", "fasta"):
+            a, b = open(f"{g}.{ext}", "rb").read(), open(f"{o}.{ext}", "rb").read()
+            assert a == b, ext
+        lines = open(f"{g}.changes").read().splitlines()
+    big = [l for l in lines if max(len(l.split()[2].strip(".")), len(l.split()[3].strip("."))) > 10]
+    assert len(big) >= 1000, len(big)
+    assert stats["tied_sets"] == 0  # no join set where the Scala HashSet's order would decide
