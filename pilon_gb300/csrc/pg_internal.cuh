@@ -219,6 +219,22 @@ __device__ inline void order2(const int64_t v[4], int& o0, int& o1) {
     if (i != o0 && (o1 < 0 || v[i] > m1)) { o1 = i; m1 = v[i]; }
 }
 
+__device__ inline int32_t pick4_32(const int32_t v[4], int i) {
+  return i == 0 ? v[0] : i == 1 ? v[1] : i == 2 ? v[2] : v[3];
+}
+__device__ inline void order2_32(const int32_t v[4], int& o0, int& o1) {  // order2 on 32-bit sums
+  o0 = 0;
+  int32_t m0 = v[0];
+#pragma unroll
+  for (int i = 1; i < 4; i++)
+    if (v[i] > m0) { o0 = i; m0 = v[i]; }
+  o1 = -1;
+  int32_t m1 = 0;
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+    if (i != o0 && (o1 < 0 || v[i] > m1)) { o1 = i; m1 = v[i]; }
+}
+
 struct CallCtx {         // what the indel vote needs
   const Event* ev;       // events grouped by position
   int64_t ev_lo, ev_hi;  // this position's events (clamped to the buffer)
@@ -291,15 +307,33 @@ __device__ inline CallOut base_call(const PosRec& r, const DevParams& P, const C
   CallOut o;
   int64_t n = r.cnt[0] + r.cnt[1] + r.cnt[2] + r.cnt[3];
   int o0, o1;
-  if (r.q_sum > 0) order2(r.qs, o0, o1); else order2(r.cnt, o0, o1);
-  int64_t baseSum = pick4(r.qs, o0), altBaseSum = pick4(r.qs, o1);
-  int64_t total = r.qs[0] + r.qs[1] + r.qs[2] + r.qs[3];
-  int64_t homoScore = baseSum - (total - baseSum);
-  int64_t half = total / 2;
-  int64_t d1 = half - baseSum, d2 = half - altBaseSum;
-  int64_t heteroScore = total - (d1 < 0 ? -d1 : d1) - (d2 < 0 ? -d2 : d2);
-  bool homo = homoScore >= heteroScore;
-  int64_t diff = homoScore - heteroScore;
+  bool homo;
+  int64_t diff;
+  if ((uint64_t)(r.qs[0] | r.qs[1] | r.qs[2] | r.qs[3]) < (1ull << 29)) {
+    // every quality sum in [0, 2^29): the same arithmetic in 32 bits (the
+    // total stays below 2^31, the scores within [-total, total])
+    const int32_t q[4] = {(int32_t)r.qs[0], (int32_t)r.qs[1], (int32_t)r.qs[2], (int32_t)r.qs[3]};
+    const int32_t c[4] = {(int32_t)r.cnt[0], (int32_t)r.cnt[1], (int32_t)r.cnt[2], (int32_t)r.cnt[3]};
+    if (r.q_sum > 0) order2_32(q, o0, o1); else order2_32(c, o0, o1);
+    const int32_t baseSum = pick4_32(q, o0), altBaseSum = pick4_32(q, o1);
+    const int32_t total = q[0] + q[1] + q[2] + q[3];
+    const int32_t homoScore = baseSum - (total - baseSum);
+    const int32_t half = total / 2;
+    const int32_t d1 = half - baseSum, d2 = half - altBaseSum;
+    const int32_t heteroScore = total - abs(d1) - abs(d2);
+    homo = homoScore >= heteroScore;
+    diff = (int64_t)homoScore - (int64_t)heteroScore;
+  } else {
+    if (r.q_sum > 0) order2(r.qs, o0, o1); else order2(r.cnt, o0, o1);
+    int64_t baseSum = pick4(r.qs, o0), altBaseSum = pick4(r.qs, o1);
+    int64_t total = r.qs[0] + r.qs[1] + r.qs[2] + r.qs[3];
+    int64_t homoScore = baseSum - (total - baseSum);
+    int64_t half = total / 2;
+    int64_t d1 = half - baseSum, d2 = half - altBaseSum;
+    int64_t heteroScore = total - (d1 < 0 ? -d1 : d1) - (d2 < 0 ? -d2 : d2);
+    homo = homoScore >= heteroScore;
+    diff = homoScore - heteroScore;
+  }
   if (diff < 0) diff = -diff;
   o.score = r.mq_sum > 0 ? div_s64(diff * n, (int64_t)r.mq_sum) : 0;
   o.flags = (uint32_t)o0 | ((uint32_t)o1 << 2);
