@@ -116,14 +116,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def pinned_store(reads):
-    """Copies the read store into page-locked host memory (torch pinned tensors)."""
+# the fields pg_set_reads_packed derives on the device instead of uploading
+PACKED_DERIVED = ("aend", "cigar_off", "seq_off", "qual_off")
+
+
+def pinned_store(reads, packed=False):
+    """Copies the read store into page-locked host memory (torch pinned tensors);
+    packed=True leaves out the fields the packed upload derives on the device."""
     import torch
     from pilon_gb300.reads import FIELDS, ReadStore
     keep = []
     arrs = {}
     for f in FIELDS:
         a = np.ascontiguousarray(getattr(reads, f))
+        if packed and f in PACKED_DERIVED:
+            arrs[f] = np.zeros(0, a.dtype)
+            continue
         t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
         v = t.numpy().view(a.dtype)
         v[:] = a.reshape(-1)
@@ -629,7 +637,10 @@ def main():
     e2e = None
     if not args.no_e2e:
         fields = args.e2e_fields if args.e2e_fields != "auto" else "changes"
-        pin = pinned_store(ds.reads)
+        # the store is packed (each read's CIGAR, bases and qualities after the
+        # previous read's), so its offsets and alignment ends are derived on the
+        # device (pg_set_reads_packed) and only the other fields are uploaded
+        pin = pinned_store(ds.reads, packed=True)
         n_pos = sum(e - s + 1 for (c, s, e, a, b) in regions)
         outs = [PinnedOut(n_pos, fields) if fields != "changes" else None]  # all regions, one after another
         h2d = pin.nbytes()
@@ -641,7 +652,7 @@ def main():
             d2h = outs[0].nbytes()
 
         def e2e_step(e, o):
-            e.set_reads(pin)
+            e.set_reads(pin, packed=True)
             e.pileup_regions(regions, params, batched=bool(args.batched))
             if o is None:
                 e.fetch_changes()

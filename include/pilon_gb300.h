@@ -230,6 +230,13 @@ pg_status pg_set_reference(pg_ctx *ctx, int32_t n_contigs, const int64_t *lens,
  * pointers (pg_set_reads_device): used in place, must outlive their use. */
 pg_status pg_set_reads(pg_ctx *ctx, const pg_reads *host_reads);
 pg_status pg_set_reads_device(pg_ctx *ctx, const pg_reads *device_reads);
+/* pg_set_reads for a packed store (each read's CIGAR words, base bytes and
+ * qualities right after the previous read's, as a BAM decoder lays them out):
+ * cigar_off, seq_off, qual_off and aend are not read (they may be NULL) but
+ * derived on the device from n_cigar, l_seq and the CIGARs, so 28 bytes less
+ * per read cross the host link.  PG_ERR_ARG when the lengths do not fill
+ * n_cigar_words, seq_bytes and qual_bytes exactly. */
+pg_status pg_set_reads_packed(pg_ctx *ctx, const pg_reads *host_reads);
 
 /* ---- pileup + calls -------------------------------------------------------
  * For every region: BamFile.process + PileUpRegion.addRead

@@ -415,9 +415,26 @@ static pg_status finish_reads(pg_ctx* c) {
   return PG_OK;
 }
 
+static pg_status upload_reads(pg_ctx* c, const pg_reads* h, bool packed);
+
 pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
   const Range nvtx_range("pg_set_reads");
+  return upload_reads(c, h, false);
+}
+
+pg_status pg_set_reads_packed(pg_ctx* c, const pg_reads* h) {
+  const Range nvtx_range("pg_set_reads_packed");
+  return upload_reads(c, h, true);
+}
+
+// packed: the offsets and alignment ends are not read from the host (they may
+// be NULL); the device derives them from the lengths and the CIGARs
+static pg_status upload_reads(pg_ctx* c, const pg_reads* h, bool packed) {
   if (!c || !h || h->n_reads < 0) return fail(c, PG_ERR_ARG, "bad reads");
+  // the store is replaced from here on: until it is complete and checked no
+  // call may use it (a failed upload leaves the context without reads)
+  c->have_reads = false;
+  c->have_results = false;
   if (h->n_cigar_words < 0 || h->seq_bytes < 0 || h->qual_bytes < 0)
     return fail(c, PG_ERR_ARG, "negative array length in the read store");
   if (!c->stream) return not_open(c);
@@ -429,8 +446,10 @@ pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
                             (size_t)n * 4, (size_t)n * 2, (size_t)n * 2, (size_t)n,
                             (size_t)h->seq_bytes, (size_t)h->qual_bytes, (size_t)n * 8, (size_t)n * 8,
                             (size_t)n * 8, (size_t)h->n_cigar_words * 4};
+  // fields the packed upload derives on the device: aend (1) and the three offsets (11-13)
+  auto derived = [&](int k) { return packed && (k == 1 || k == 11 || k == 12 || k == 13); };
   for (int k = 0; k < 15; k++) {
-    if (bytes[k] && !src[k]) return fail(c, PG_ERR_ARG, "reads field %d is null", k);
+    if (bytes[k] && !src[k] && !derived(k)) return fail(c, PG_ERR_ARG, "reads field %d is null", k);
     pg_status s = ensure(c, c->rd[k], std::max<size_t>(bytes[k], 16));
     if (s) return s;
   }
@@ -443,7 +462,8 @@ pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
     CK(cudaStreamSynchronize(c->stream));
     std::lock_guard<std::mutex> turn(upload_mutex(c->device));
     for (int k = 0; k < 15; k++)
-      if (bytes[k]) CK(cudaMemcpyAsync(c->rd[k].p, src[k], bytes[k], cudaMemcpyHostToDevice, c->stream));
+      if (bytes[k] && !derived(k))
+        CK(cudaMemcpyAsync(c->rd[k].p, src[k], bytes[k], cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
   }
   Reads& R = c->R;
@@ -454,6 +474,25 @@ pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
   R.seq = P<uint8_t>(c->rd[9]); R.qual = P<uint8_t>(c->rd[10]); R.cigar_off = P<int64_t>(c->rd[11]);
   R.seq_off = P<int64_t>(c->rd[12]); R.qual_off = P<int64_t>(c->rd[13]); R.cigar = P<uint32_t>(c->rd[14]);
   R.n_cigar_words = h->n_cigar_words; R.seq_bytes = h->seq_bytes; R.qual_bytes = h->qual_bytes;
+  if (packed && n > 0) {
+    const int32_t nb = (int32_t)((n + 1023) / 1024);
+    pg_status s = ensure(c, c->ent_sums, 8 * (size_t)(nb + 2));
+    if (s) return s;
+    launch_packed_lengths(R, P<int64_t>(c->rd[11]), P<int64_t>(c->rd[12]), P<int64_t>(c->rd[13]), c->stream);
+    int64_t totals[3] = {0, 0, 0};
+    for (int k = 0; k < 3; k++) {  // exclusive scans: the offsets; the totals must be the arrays' lengths
+      launch_scan64(P<int64_t>(c->rd[11 + k]), n, P<int64_t>(c->ent_sums), c->stream);
+      CK(cudaMemcpyAsync(&totals[k], P<int64_t>(c->ent_sums) + nb, 8, cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+    }
+    if (totals[0] != h->n_cigar_words || totals[1] != h->seq_bytes || totals[2] != h->qual_bytes)
+      return fail(c, PG_ERR_ARG, "packed read store: the reads' CIGAR words, bases or qualities do not fill "
+                  "their arrays (%lld / %lld / %lld against %lld / %lld / %lld)", (long long)totals[0],
+                  (long long)totals[1], (long long)totals[2], (long long)h->n_cigar_words,
+                  (long long)h->seq_bytes, (long long)h->qual_bytes);
+    launch_packed_aend(R, P<int32_t>(c->rd[1]), c->stream);
+    CK(cudaGetLastError());
+  }
   return finish_reads(c);
 }
 

@@ -468,6 +468,9 @@ struct CallArgs {
 };
 
 void launch_read_extent(const Reads& R, ReadExtent* out, int4* desc, cudaStream_t s);
+// a packed store's per-read lengths (for the offset scans) and alignment ends
+void launch_packed_lengths(const Reads& R, int64_t* cig, int64_t* seq, int64_t* qual, cudaStream_t s);
+void launch_packed_aend(const Reads& R, int32_t* aend, cudaStream_t s);
 // Builds R.entry_off (n + 1 int64; `sums` holds (n + 1) / 1024 + 2 int64 of
 // scan scratch) and R.entries (3 int4 per entry), after the store passed
 // k_read_extent's checks.  Returns nothing: the host reads entry_off[n].

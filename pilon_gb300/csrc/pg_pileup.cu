@@ -148,6 +148,44 @@ void launch_read_extent(const Reads& R, ReadExtent* out, int4* desc, cudaStream_
 }
 
 // ---------------------------------------------------------------------------
+// A packed read store: each read's CIGAR words, base bytes and qualities follow
+// the previous read's, so their offsets are prefix sums of the lengths, and
+// the alignment end (htsjdk getAlignmentEnd: 0 for an unmapped read, else pos
+// plus the reference-consuming lengths minus 1) follows from the CIGAR.
+__global__ void k_packed_lengths(Reads R, int64_t* cig, int64_t* seq, int64_t* qual) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < R.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t L = R.l_seq[i];
+    cig[i] = R.n_cigar[i];
+    seq[i] = ((int64_t)L + 1) / 2;
+    qual[i] = L;
+  }
+}
+
+__global__ void k_packed_aend(Reads R, int32_t* aend) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < R.n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (R.flag[i] & 0x4) { aend[i] = 0; continue; }
+    const int64_t co = R.cigar_off[i];
+    const int nc = R.n_cigar[i];
+    int64_t reflen = 0;
+    for (int k = 0; k < nc; k++) {
+      const uint32_t w = R.cigar[co + k], op = w & 15u;
+      if (op == 0 || op == 2 || op == 3 || op == 7 || op == 8) reflen += w >> 4;
+    }
+    aend[i] = (int32_t)((uint32_t)R.pos[i] + (uint32_t)reflen - 1u);  // Java int arithmetic: wraps
+  }
+}
+
+void launch_packed_lengths(const Reads& R, int64_t* cig, int64_t* seq, int64_t* qual, cudaStream_t s) {
+  if (R.n <= 0) return;
+  k_packed_lengths<<<(int)std::min<int64_t>((R.n + 255) / 256, 152 * 16), 256, 0, s>>>(R, cig, seq, qual);
+}
+
+void launch_packed_aend(const Reads& R, int32_t* aend, cudaStream_t s) {
+  if (R.n <= 0) return;
+  k_packed_aend<<<(int)std::min<int64_t>((R.n + 255) / 256, 152 * 16), 256, 0, s>>>(R, aend);
+}
+
+// ---------------------------------------------------------------------------
 // Walk entries: one per M/=/X or S operator (the operators whose bases the walk
 // adds, S/PileUpRegion.scala:184-206), with everything of the read the walk
 // needs beside it, so that a walk tile reads its entries as one coalesced

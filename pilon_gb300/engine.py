@@ -40,6 +40,7 @@ def lib():
             "pg_set_reference": (C.c_int, [vp, i32, vp, vp]),
             "pg_set_reads": (C.c_int, [vp, C.POINTER(_abi.pg_reads)]),
             "pg_set_reads_device": (C.c_int, [vp, C.POINTER(_abi.pg_reads)]),
+            "pg_set_reads_packed": (C.c_int, [vp, C.POINTER(_abi.pg_reads)]),
             "pg_pileup_regions": (C.c_int, [vp, vp, i32, C.POINTER(_abi.pg_params), i32]),
             "pg_fetch_stats": (C.c_int, [vp, i32, C.POINTER(_abi.pg_region_stats)]),
             "pg_fetch_region": (C.c_int, [vp, i32, C.POINTER(_abi.pg_region_out)]),
@@ -160,9 +161,12 @@ class Engine:
         self._check(self.L.pg_set_reference(self.h, len(arrs), lens.ctypes.data, C.cast(ptrs, C.c_void_p)))
         self.contig_lens = lens
 
-    def set_reads(self, reads):
+    def set_reads(self, reads, packed=False):
+        """pg_set_reads, or pg_set_reads_packed (packed=True: the store's offsets
+        and alignment ends are derived on the device and not uploaded)."""
         ab = reads.to_abi()
-        self._check(self.L.pg_set_reads(self.h, C.byref(ab)))
+        fn = self.L.pg_set_reads_packed if packed else self.L.pg_set_reads
+        self._check(fn(self.h, C.byref(ab)))
         self.n_reads = reads.n_reads
 
     def set_tuning(self, tile_width=0, warps=0, variant=-1):

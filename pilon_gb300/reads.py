@@ -65,7 +65,7 @@ class ReadStore:
         r.n_reads = self.n_reads
         for f in FIELDS:
             setattr(r, f, arrs[f].ctypes.data if arrs[f].size else 0)
-        r.n_cigar_words = int(arrs["cigar"].size)
+        r.n_cigar_words = int(arrs["cigar"].size)  # the packed upload checks the lengths against these
         r.seq_bytes = int(arrs["seq"].size)
         r.qual_bytes = int(arrs["qual"].size)
         return r

@@ -247,3 +247,29 @@ def test_fetch_changes_equals_call_arrays(engine):
             chars[int(ch["ins_str"]):int(ch["ins_str"]) + int(ch["indel_len"])].decode() if ch["ins_str"] >= 0 else "")
            for ch in changes]
     assert len(want) > 100 and got == want
+
+
+def test_packed_upload(engine, cfg1):
+    """pg_set_reads_packed derives the offsets and alignment ends of a packed
+    store on the device: the same pileups as the full upload, also when the
+    derived fields are left out, and a store whose lengths do not fill its
+    arrays is refused."""
+    import copy
+    from pilon_gb300.engine import EngineError
+    p = _abi.default_params()
+    regions = plan(cfg1, chunk_size=12_000)
+    ora = oracle_regions(cfg1, p, regions)
+    engine.set_reference(cfg1.contigs)
+    lean = copy.copy(cfg1.reads)
+    for f in ("aend", "cigar_off", "seq_off", "qual_off"):
+        setattr(lean, f, np.zeros(0, getattr(cfg1.reads, f).dtype))
+    for store in (cfg1.reads, lean):
+        engine.set_reads(store, packed=True)
+        engine.pileup_regions(regions, p, batched=True)
+        for r in range(len(regions)):
+            compare_region(engine.fetch(r), ora[r], label=f"packed region {r}")
+    gappy = copy.copy(cfg1.reads)
+    gappy.qual = np.concatenate([cfg1.reads.qual, np.zeros(7, np.uint8)])
+    with pytest.raises(EngineError):
+        engine.set_reads(gappy, packed=True)
+    engine.set_reads(cfg1.reads)
