@@ -1,5 +1,5 @@
-"""The Python examples of INTEGRATION.md compile and name functions the
-package has."""
+"""The Python examples of the integration guide at the repository root compile
+and name functions the package has."""
 import ast
 import importlib
 import os
