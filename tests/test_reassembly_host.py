@@ -230,3 +230,47 @@ def test_bam_read_names_pair_mates(cfg4_small, tmp_path):
         assert np.array_equal(x.recruit(0, s, s + 300), y.recruit(0, s, s + 300))
     _, _, plain = bam.read_bam(path)
     assert plain.name_id is None
+
+
+def test_reassemble_arguments_and_empty_graphs():
+    """pg_reassemble refuses bad jobs with PG_ERR_ARG, and a window without
+    edges (no K-mer reached depth 5) gives no solution, like an Assembler
+    whose graph is empty (S/Assembler.scala:183-190)."""
+    import ctypes as C
+    from pilon_gb300.engine import EngineError, lib
+    rng = np.random.default_rng(5)
+    region = "".join("ACGT"[x] for x in rng.integers(0, 4, 900))
+    none = np.zeros(0, _abi.kmer_edge_wide_dtype())
+    [(start, was, patch, status, loop)] = reassemble(none, 47, [_job(region, 400, 450, 150)])
+    assert (start, status, loop) == (0, 0, 0)
+    # a gap with an empty graph: both sides' consensus is its anchor, which matches the
+    # region, so no partial fill either (partialMatchesReference)
+    [(start, was, patch, status, loop)] = reassemble(none, 47, [_job(region, 400, 450, 150, gap=True)])
+    assert (start, status) == (0, 0)
+    with pytest.raises(EngineError):
+        reassemble(none, 64, [_job(region, 400, 450, 150)])
+    bad = _job(region, 400, 450, 150)
+    bad["break_start"], bad["break_stop"] = 450, 400
+    with pytest.raises(EngineError):
+        reassemble(none, 47, [bad])
+    with pytest.raises(ValueError):
+        j = _job(region, 400, 450, 150)
+        j["bases"] = j["bases"][:-1]
+        reassemble(none, 47, [j])
+    L = lib()
+    n = C.c_int64()
+    assert L.pg_reassemble(None, 0, 31, None, 0, 0, None, None, 0, C.byref(n)) == 0 and n.value == 0
+    assert L.pg_reassemble(None, 0, 31, None, 1, 0, None, None, 0, C.byref(n)) == _abi.PG_ERR_ARG
+
+
+@pytest.mark.parametrize("K", [31, 47, 63])
+def test_walk_closes_a_break_for_each_K(K):
+    """The known-answer insertion of test_walk_closes_a_break_known_answer at
+    K = 31, 47 and 63 (the 4-bit keys span one to four words)."""
+    rng = np.random.default_rng(7)
+    sample = "".join("ACGT"[x] for x in rng.integers(0, 4, 1200))
+    region = sample[:600] + sample[625:]
+    edges = _graph(sample, K, length=100, step=2)
+    [(start, was, patch, status, loop)] = reassemble(edges, K, [_job(region, 580, 620, 3 * K)])
+    assert status == 0 and loop == 0
+    assert was == "" and patch == sample[600:625] and start == 601
