@@ -586,8 +586,13 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   int32_t max_chunks = 0;
   for (int32_t r = r0; r < r1; r++) max_chunks = std::max(max_chunks, c->regions_h[r].n_chunks);
   launch_region_prep(d_regions + r0, d_stats + r0, P<ChunkStats>(c->chunk_stats), r1 - r0, max_chunks, dp, s);
-  launch_physcov_scan(d_regions, P<int32_t>(c->call_tile_region), t0, tn, rec, d_stats, P<int32_t>(c->tile_sums),
-                      r0, r1 - r0, s);
+  // the tiles' sums, their segmented prefixes, then the scan's block sums (3 words per 1024 tiles)
+  {
+    int32_t* ts = P<int32_t>(c->tile_sums);
+    const int64_t w = 3 * ((int64_t)c->n_call_tiles + 1);
+    launch_physcov_scan(d_regions, P<int32_t>(c->call_tile_region), t0, tn, rec, d_stats, ts, ts + w, ts + 2 * w,
+                        r0, r1 - r0, s);
+  }
   launch_event_scatter(P<Event>(c->events), &counters[CNT_EVENTS], rec.ev_end, P<Event>(c->events_sorted), s,
                        c->event_cap);
 
@@ -686,7 +691,7 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
   EN(c->rec_ins_str, 4 * (size_t)pos);
   EN(c->rec_ev_end, 4 * (size_t)pos);
   for (DevBuf* b : {&c->cand_count, &c->cand_off}) EN(*b, sizeof(int32_t) * (n_call + 2));
-  EN(c->tile_sums, sizeof(int32_t) * 3 * (n_call + 1));
+  EN(c->tile_sums, sizeof(int32_t) * 3 * (2 * (n_call + 1) + (n_call / 1024 + 2)));
   EN(c->counters, sizeof(unsigned long long) * CNT_N);
   EN(c->run_max, sizeof(unsigned long long) * 2);
   if (c->event_cap == 0) c->event_cap = (int64_t)(2 * c->ext.n_indel_ops + 4096);

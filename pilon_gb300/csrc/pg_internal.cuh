@@ -484,8 +484,8 @@ void launch_scan_small(const int32_t* in, int32_t* out_excl, int32_t n, cudaStre
 void launch_event_scatter(const Event* ev, const unsigned long long* n_events, int32_t* ev_end, Event* out,
                           cudaStream_t s, int64_t max_events);
 void launch_physcov_scan(const RegionDev* regions, const int32_t* call_tile_region, int32_t tile_begin,
-                         int32_t n_tiles, Records rec, const StatsDev* stats, int32_t* tile_sums,
-                         int32_t region_begin, int32_t n_regions, cudaStream_t s);
+                         int32_t n_tiles, Records rec, const StatsDev* stats, int32_t* tile_sums, int32_t* seg,
+                         int32_t* block_sums, int32_t region_begin, int32_t n_regions, cudaStream_t s);
 void launch_region_prep(const RegionDev* regions, StatsDev* stats, const ChunkStats* chunk_stats,
                         int32_t n_regions, int32_t max_chunks, DevParams P, cudaStream_t s);
 void launch_call(const CallArgs& a, int32_t tile_begin, int32_t n_tiles, cudaStream_t s);

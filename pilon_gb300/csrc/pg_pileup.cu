@@ -1248,71 +1248,92 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles_a(const RegionDev* 
   }
 }
 
-// One CTA over the tiles [t0, t0 + tn).  Coverage sums restart at each
-// region's first tile, seeded with physCovStart / insertSizeStart.
-__global__ void __launch_bounds__(1024) k_scan_tiles_b(const RegionDev* regions, const int32_t* tile_region,
-                                                        const StatsDev* stats, int32_t* ts, int32_t t0, int32_t tn) {
-  __shared__ uint32_t s_a[32], s_b[32], s_c[32];
-  __shared__ uint32_t s_f[32];
-  __shared__ uint32_t s_ca, s_cb, s_cc;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) { s_ca = 0; s_cb = 0; s_cc = 0; }
-  __syncthreads();
-  for (int32_t base = 0; base < tn; base += blockDim.x) {
-    const int32_t i = base + threadIdx.x;
-    const int32_t t = t0 + i;
-    uint32_t va = 0, vb = 0, vc = 0, f = 0;
-    uint32_t a = 0, b = 0;
-    if (i < tn) {
-      const int32_t r = tile_region[t];
-      va = (uint32_t)ts[3 * t]; vb = (uint32_t)ts[3 * t + 1]; vc = (uint32_t)ts[3 * t + 2];
-      f = t == regions[r].call_tile0;
-      a = va + (f ? (uint32_t)stats[r].phys_cov_start : 0u);
-      b = vb + (f ? (uint32_t)stats[r].insert_size_start : 0u);
-    }
-    uint32_t c = vc;
-    // segmented inclusive scan of (a, b) with head flags f; plain scan of c
+// Phase b: plain exclusive scans of the tiles' three sums (32-bit, wrapping) over
+// [t0, t0 + tn): within blocks of 1024 tiles by one CTA each, then over the
+// blocks' totals by one CTA; then k_scan_tiles_b3 turns the plain prefixes
+// into the region-segmented ones: the prefix at a tile minus the prefix at its
+// region's first tile, plus the region's physCovStart / insertSizeStart
+// (wrapping arithmetic keeps every difference exact).
+__device__ inline void block_excl_scan3(uint32_t (&v)[3], uint32_t (&tot)[3], uint32_t (*s_w)[32]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t x[3] = {v[0], v[1], v[2]};
+#pragma unroll
+  for (int k = 0; k < 3; k++)
     for (int o = 1; o < 32; o <<= 1) {
-      uint32_t ya = __shfl_up_sync(FULL, a, o), yb = __shfl_up_sync(FULL, b, o), yc = __shfl_up_sync(FULL, c, o);
-      uint32_t yf = __shfl_up_sync(FULL, f, o);
-      if (lane >= o) {
-        if (!f) { a += ya; b += yb; }
-        f |= yf;
-        c += yc;
-      }
+      const uint32_t y = __shfl_up_sync(FULL, x[k], o);
+      if (lane >= o) x[k] += y;
     }
-    if (lane == 31) { s_a[warp] = a; s_b[warp] = b; s_c[warp] = c; s_f[warp] = f; }
-    __syncthreads();
-    if (warp == 0) {
-      uint32_t wa = s_a[lane], wb = s_b[lane], wc = s_c[lane], wf = s_f[lane];
+  if (lane == 31)
+    for (int k = 0; k < 3; k++) s_w[k][warp] = x[k];
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      uint32_t w = lane < nw ? s_w[k][lane] : 0u;
       for (int o = 1; o < 32; o <<= 1) {
-        uint32_t ya = __shfl_up_sync(FULL, wa, o), yb = __shfl_up_sync(FULL, wb, o);
-        uint32_t yc = __shfl_up_sync(FULL, wc, o), yf = __shfl_up_sync(FULL, wf, o);
-        if (lane >= o) {
-          if (!wf) { wa += ya; wb += yb; }
-          wf |= yf;
-          wc += yc;
-        }
+        const uint32_t y = __shfl_up_sync(FULL, w, o);
+        if (lane >= o) w += y;
       }
-      s_a[lane] = wa; s_b[lane] = wb; s_c[lane] = wc; s_f[lane] = wf;
+      if (lane < nw) s_w[k][lane] = w;  // inclusive over the warps
     }
-    __syncthreads();
-    if (warp > 0) {  // combine with the inclusive result of the previous warps
-      if (!f) { a += s_a[warp - 1]; b += s_b[warp - 1]; }
-      f |= s_f[warp - 1];
-      c += s_c[warp - 1];
-    }
-    if (!f) { a += s_ca; b += s_cb; }  // carry of the previous chunk
-    c += s_cc;
-    if (i < tn) {
-      ts[3 * t] = (int32_t)(a - va);
-      ts[3 * t + 1] = (int32_t)(b - vb);
-      ts[3 * t + 2] = (int32_t)(c - vc);
-    }
-    __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) { s_ca = a; s_cb = b; s_cc = c; }
-    __syncthreads();
   }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const uint32_t before = warp > 0 ? s_w[k][warp - 1] : 0u;
+    tot[k] = s_w[k][nw - 1];
+    v[k] = before + x[k] - v[k];  // exclusive
+  }
+  __syncthreads();  // s_w is read by every thread before it is reused
+}
+
+__global__ void __launch_bounds__(1024) k_scan_tiles_b(int32_t* ts, int32_t* bsum, int32_t t0, int32_t tn) {
+  __shared__ uint32_t s_w[3][32];
+  const int32_t i = blockIdx.x * 1024 + threadIdx.x;
+  uint32_t v[3], tot[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) v[k] = i < tn ? (uint32_t)ts[3 * (int64_t)(t0 + i) + k] : 0u;
+  block_excl_scan3(v, tot, s_w);
+  if (i < tn)
+    for (int k = 0; k < 3; k++) ts[3 * (int64_t)(t0 + i) + k] = (int32_t)v[k];
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 3; k++) bsum[3 * blockIdx.x + k] = (int32_t)tot[k];
+}
+
+// the exclusive scan of the nb blocks' totals, 1024 at a time with a carry
+__global__ void __launch_bounds__(1024) k_scan_tiles_b2(int32_t* bsum, int32_t nb) {
+  __shared__ uint32_t s_w[3][32];
+  uint32_t carry[3] = {0u, 0u, 0u};
+  for (int32_t base = 0; base < nb; base += 1024) {
+    const int32_t i = base + threadIdx.x;
+    uint32_t v[3], tot[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) v[k] = i < nb ? (uint32_t)bsum[3 * i + k] : 0u;
+    block_excl_scan3(v, tot, s_w);
+    if (i < nb)
+      for (int k = 0; k < 3; k++) bsum[3 * i + k] = (int32_t)(carry[k] + v[k]);
+    for (int k = 0; k < 3; k++) carry[k] += tot[k];
+  }
+}
+
+// Per tile its region-segmented exclusive prefixes into seg: the plain prefix
+// (its offset in its block plus the block's) minus the plain prefix at its
+// region's first tile, plus the region's start values; the event count stays
+// plain (event slots are global).
+__global__ void __launch_bounds__(256) k_scan_tiles_b3(const RegionDev* regions, const int32_t* tile_region,
+                                                        const StatsDev* stats, const int32_t* ts, const int32_t* bsum,
+                                                        int32_t* seg, int32_t t0, int32_t tn) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= tn) return;
+  const int32_t t = t0 + i;
+  const int32_t r = tile_region[t];
+  const int32_t h = regions[r].call_tile0;  // the region's first tile (>= t0)
+  auto plain = [&](int32_t tt, int k) {
+    return (uint32_t)ts[3 * (int64_t)tt + k] + (uint32_t)bsum[3 * ((tt - t0) >> 10) + k];
+  };
+  seg[3 * (int64_t)t] = (int32_t)(plain(t, 0) - plain(h, 0) + (uint32_t)stats[r].phys_cov_start);
+  seg[3 * (int64_t)t + 1] = (int32_t)(plain(t, 1) - plain(h, 1) + (uint32_t)stats[r].insert_size_start);
+  seg[3 * (int64_t)t + 2] = (int32_t)plain(t, 2);
 }
 
 // Phase c: the inclusive scan inside each tile plus the tile's prefix from
@@ -1380,14 +1401,18 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles_c(const RegionDev* 
 }
 
 void launch_physcov_scan(const RegionDev* regions, const int32_t* call_tile_region, int32_t tile_begin,
-                         int32_t n_tiles, Records rec, const StatsDev* stats, int32_t* tile_sums,
-                         int32_t region_begin, int32_t n_regions, cudaStream_t s) {
+                         int32_t n_tiles, Records rec, const StatsDev* stats, int32_t* tile_sums, int32_t* seg,
+                         int32_t* block_sums, int32_t region_begin, int32_t n_regions, cudaStream_t s) {
   (void)region_begin;
   (void)n_regions;
   if (n_tiles <= 0) return;
+  const int32_t nb = (n_tiles + 1023) / 1024;
   k_scan_tiles_a<<<n_tiles, kScanThreads, 0, s>>>(regions, call_tile_region, rec, tile_sums, tile_begin);
-  k_scan_tiles_b<<<1, 1024, 0, s>>>(regions, call_tile_region, stats, tile_sums, tile_begin, n_tiles);
-  k_scan_tiles_c<<<n_tiles, kScanThreads, 0, s>>>(regions, call_tile_region, rec, tile_sums, tile_begin);
+  k_scan_tiles_b<<<nb, 1024, 0, s>>>(tile_sums, block_sums, tile_begin, n_tiles);
+  k_scan_tiles_b2<<<1, 1024, 0, s>>>(block_sums, nb);
+  k_scan_tiles_b3<<<(n_tiles + 255) / 256, 256, 0, s>>>(regions, call_tile_region, stats, tile_sums, block_sums, seg,
+                                                        tile_begin, n_tiles);
+  k_scan_tiles_c<<<n_tiles, kScanThreads, 0, s>>>(regions, call_tile_region, rec, seg, tile_begin);
 }
 
 // ---------------------------------------------------------------------------
