@@ -274,3 +274,27 @@ def test_walk_closes_a_break_for_each_K(K):
     [(start, was, patch, status, loop)] = reassemble(edges, K, [_job(region, 580, 620, 3 * K)])
     assert status == 0 and loop == 0
     assert was == "" and patch == sample[600:625] and start == 601
+
+
+def test_gap_filled_with_the_reads_sequence_known_answer(tmp_path):
+    """Worked by hand from S/GapFiller.scala:49-262: reads tiling a 2 kb sample
+    aligned onto a reference that has its bases 900-959 replaced by N.  Pass 1
+    skips the N positions; fillGap walks from the 93 bases before the gap
+    (breakRadius = 3K for K = 31 without pairs) through the reads' K-mers, the
+    join trims to the 60 bases under the Ns, and the gap closes with exactly
+    the sample's bases: the polished FASTA is the sample, one changes line, and
+    a reassembly VCF record of SVLEN 0 (written as INS)."""
+    from types import SimpleNamespace
+    from tests.test_oracle_kat import ref_from
+    rng = np.random.default_rng(21)
+    sample = "".join("ACGT"[x] for x in rng.integers(0, 4, 2000))
+    ref = sample[:899] + "N" * 60 + sample[959:]
+    recs = _tile(sample, length=100, step=5)
+    ds = SimpleNamespace(names=["chr1"], contigs=[ref_from(ref)], reads=build_store(recs))
+    n, out = compare(ds, vcf=True, fix_gaps=True, K=31)
+    fasta = b"".join(out["fasta"].split(b"\n")[1:])
+    assert fasta == sample.encode()
+    assert out["changes"].decode() == f"chr1:900-959 chr1_pilon:900-959 {'N' * 60} {sample[899:959]}\n"
+    fix = [l for l in out["vcf"].decode().splitlines() if "SVTYPE" in l and not l.startswith("#")]
+    assert fix == [f"chr1\t899\t.\t{sample[898]}{'N' * 60}\t{sample[898:959]}\t.\tPASS\tSVTYPE=INS;SVLEN=0;"
+                   f"END=959\tGT\t1/1"]
