@@ -298,3 +298,39 @@ def test_gap_filled_with_the_reads_sequence_known_answer(tmp_path):
     fix = [l for l in out["vcf"].decode().splitlines() if "SVTYPE" in l and not l.startswith("#")]
     assert fix == [f"chr1\t899\t.\t{sample[898]}{'N' * 60}\t{sample[898:959]}\t.\tPASS\tSVTYPE=INS;SVLEN=0;"
                    f"END=959\tGT\t1/1"]
+
+
+def test_break_reassembled_over_clipped_reads_known_answer():
+    """A 30-base insertion that the aligner left as soft clips (reads are
+    aligned up to the insertion and clipped after it, or clipped before it and
+    aligned after): the clips mark a possible break (highClipping,
+    S/GenomeRegion.scala:705-720), and fixBreak's walk through the reads'
+    K-mers, clipped bases included, joins the flanks across it
+    (S/GapFiller.scala:49-262): the polished sequence is the sample's."""
+    from types import SimpleNamespace
+    from tests.test_oracle_kat import ref_from
+    rng = np.random.default_rng(33)
+    ref = "".join("ACGT"[x] for x in rng.integers(0, 4, 3000))
+    ins = "".join("ACGT"[x] for x in rng.integers(0, 4, 30))
+    at = 1500  # the insertion follows reference base 1500 (1-based)
+    sample = ref[:at] + ins + ref[at:]
+    L, recs = 100, []
+    for k, p in enumerate(range(0, len(sample) - L + 1, 3)):  # p: 0-based start in the sample
+        seq = sample[p:p + L]
+        if p + L <= at:  # left of the insertion
+            cig, pos = [(L, "M")], p + 1
+        elif p >= at + len(ins):  # right of it
+            cig, pos = [(L, "M")], p - len(ins) + 1
+        elif p < at:  # aligned up to the insertion, clipped after
+            cig, pos = [(at - p, "M"), (L - (at - p), "S")], p + 1
+        else:  # starts inside the insertion: clipped up to its end, aligned after
+            c = at + len(ins) - p
+            cig, pos = [(c, "S"), (L - c, "M")], at + 1
+        recs.append(dict(pos=pos, cigar=cig, seq=seq, qual=[30] * L, flag=0, mapq=60, name=k))
+    recs.sort(key=lambda r: r["pos"])
+    ds = SimpleNamespace(names=["chr1"], contigs=[ref_from(ref)], reads=build_store(recs))
+    n, out = compare(ds, vcf=True, fix_local=True, fix_indels=False, K=31)
+    fasta = b"".join(out["fasta"].split(b"\n")[1:])
+    assert fasta == sample.encode()
+    lines = out["changes"].decode().splitlines()
+    assert len(lines) == 1 and lines[0].split()[2] == "." and len(lines[0].split()[3]) == len(ins)
