@@ -1571,6 +1571,8 @@ static int polishImpl(const pg_reads* R, const pg_params* params, int32_t n_cont
                       const char* vcf_args, const char* vcf_ref, int32_t fix_gaps, int32_t fix_local, int32_t K,
                       const int64_t* name_id, int64_t* tied_sets, int32_t fix_breaks) {
   Params P = toParams(params);
+  // a BAM of type "bam" is typed by autoBam during the scan, which this oracle does not restate
+  if ((fix_gaps || fix_local) && P.bamType == PG_BAM_BAM) return PG_ERR_ARG;
   try {
     // BamFile.scan runs first when strays are tracked (S/GenomeFile.scala:89-92)
     std::unique_ptr<Reassembly> ra;
