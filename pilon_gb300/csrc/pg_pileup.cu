@@ -795,7 +795,7 @@ constexpr int kEvThreads = 64;
 constexpr int kEvPerChunk = kReadsPerChunk / kEvThreads;
 static_assert(kEvPerChunk * kEvThreads == kReadsPerChunk, "one read per thread of k_read_events");
 
-__global__ void __launch_bounds__(kEvThreads, 16) k_read_events(EventArgs a, int32_t chunk_begin, int32_t chunk_end) {
+__global__ void __launch_bounds__(kEvThreads, 20) k_read_events(EventArgs a, int32_t chunk_begin, int32_t chunk_end) {
   const Reads& R = a.R;
   const DevParams& P = a.P;
   for (int32_t bq = chunk_begin * kEvPerChunk + blockIdx.x; bq < chunk_end * kEvPerChunk; bq += gridDim.x) {
