@@ -47,6 +47,8 @@ def test_struct_layouts_match_header():
     assert C.sizeof(_abi.pg_serve_config) == 48  # 4 + 4, the int64 budget at 8, then 7 int32 + padding
     assert C.sizeof(_abi.pg_result) == 96
     assert _abi.pg_result.latency_ms.offset == 80 and _abi.pg_serve_config.hbm_budget.offset == 8
+    assert C.sizeof(_abi.pg_reassembly) == 8 * 4 + 2 * 8 and _abi.pg_reassembly.bases.offset == 32
+    assert C.sizeof(_abi.pg_reassembly_fix) == 4 * 4 + 4 * 8 and _abi.pg_reassembly_fix.patch_off.offset == 32
 
 
 def test_default_params_match_pilon():
@@ -149,7 +151,11 @@ int main(void) {
   if (strcmp(pg_last_error(ctx), "no CUDA device -1") != 0) return 4;
   if (pg_sync(ctx) != PG_ERR_STATE) return 5;
   pg_close(ctx);
-  printf("%s|%zu|%zu|%zu\n", pg_version(), sizeof(pg_region), sizeof(pg_params), sizeof(pg_kmer_edge));
+  /* local reassembly needs no context: an empty batch of jobs */
+  int64_t text_len = -1;
+  if (pg_reassemble(NULL, 0, 47, NULL, 0, 1, NULL, NULL, 0, &text_len) != PG_OK || text_len != 0) return 6;
+  printf("%s|%zu|%zu|%zu|%zu|%zu\n", pg_version(), sizeof(pg_region), sizeof(pg_params), sizeof(pg_kmer_edge),
+         sizeof(pg_reassembly), sizeof(pg_reassembly_fix));
   return 0;
 }
 """
@@ -175,5 +181,5 @@ def test_header_compiles_as_c99_and_links(tmp_path):
                    check=True, capture_output=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, (out.returncode, out.stderr)
-    version, r, p, e = out.stdout.strip().split("|")
-    assert version.startswith("pilon_gb300") and (int(r), int(p), int(e)) == (32, 56, 32)
+    version, r, p, e, j, f = out.stdout.strip().split("|")
+    assert version.startswith("pilon_gb300") and (int(r), int(p), int(e), int(j), int(f)) == (32, 56, 32, 48, 48)
