@@ -107,8 +107,10 @@ def test_open_errors_are_statuses():
     reads.seq_bytes = -1
     assert lib.pg_set_reads(bad, C.byref(reads)) == _abi.PG_ERR_ARG
     assert lib.pg_set_reads_device(bad, C.byref(reads)) == _abi.PG_ERR_ARG
+    assert lib.pg_set_reads_packed(bad, C.byref(reads)) == _abi.PG_ERR_ARG
     assert lib.pg_last_error(bad) == b"negative array length in the read store"
     reads.seq_bytes = 0
+    assert lib.pg_set_reads_packed(bad, C.byref(reads)) == _abi.PG_ERR_STATE
     assert lib.pg_set_reads(bad, C.byref(reads)) == _abi.PG_ERR_STATE
     assert lib.pg_set_reads_device(bad, C.byref(reads)) == _abi.PG_ERR_STATE
     p = _abi.default_params()
