@@ -334,3 +334,12 @@ def test_break_reassembled_over_clipped_reads_known_answer():
     assert fasta == sample.encode()
     lines = out["changes"].decode().splitlines()
     assert len(lines) == 1 and lines[0].split()[2] == "." and len(lines[0].split()[3]) == len(ins)
+
+
+def test_local_reassembly_many_contigs():
+    """--fix all over 15 uneven contigs of the draft workload (1% of bases
+    carry SNPs and indels): every contig's regions see the insert statistics
+    of the scan and of the regions before them (H7)."""
+    ds = synth.generate(3, scale=0.005)
+    n, out = compare(ds, vcf=True, fix_gaps=True, fix_local=True, K=31)
+    assert n > 100
