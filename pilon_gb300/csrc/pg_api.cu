@@ -614,7 +614,11 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
   // kernels of this run: tile ranges + walk, read events, region prep, three
   // scan phases, event scatter, call descriptors, call, candidate scan,
   // candidate list, resolve, span update, overflow tracking
-  c->launches += 2 * (wn > 0) + (chn > 0) + 1 + 3 * (tn > 0) + 1 + 3 * (tn > 0) + 1 + 1 + 1 + 1;
+  // kernels of this call: tile ranges and walk; read events and indels; region prep; the five scan
+  // phases; event scatter; call descriptors and calls; the candidate count scan and list; resolve;
+  // spans; k_track
+  c->launches += 2 * (wn > 0) + 2 * (chn > 0) + 1 + 5 * (tn > 0) + (c->event_cap > 0) + 2 * (tn > 0) + 1 +
+                 (tn > 0) + 1 + (c->cand_cap > 0) + 1;
 }
 
 pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions, const pg_params* params,

@@ -1180,9 +1180,10 @@ void launch_event_scatter(const Event* ev, const unsigned long long* n_events, i
 // computePhysCov as a segmented scan over call tiles (kCallTile positions),
 // fused with the exclusive scan of per-position event counts (insertions +
 // deletions) that groups indel events by position.
-// Phase A: tile sums.  Phase B: one CTA scans all tile sums, segmented by
-// region for coverage (seeded with each region's start carry) and global for
-// events.  Phase C: in-tile scan, insertSize /= physCov, event offsets.
+// Phase A: tile sums.  Phase B: plain scans of the tile sums (blocks, then
+// the blocks), made segmented by region for coverage (seeded with each
+// region's start carry) and kept global for events.  Phase C: in-tile scan,
+// insertSize /= physCov, event offsets.
 __device__ inline void block_scan3(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t* s_a, uint32_t* s_b,
                                    uint32_t* s_c) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
