@@ -350,6 +350,8 @@ typedef struct pg_reassembly_fix {
  * host threads (0 = all cores).  The fixes' strings are copied into `text`
  * when they fit in text_cap bytes; *text_len receives their total size either
  * way (PG_ERR_LIMIT when it does not fit).  Needs no context or device.
+ * When host memory runs out the job's status (and the call's) is
+ * PG_ERR_NOMEM; no C++ exception leaves the call.
  * Scala's Set of solutions is taken in insertion order, which is its order up
  * to four elements. */
 pg_status pg_reassemble(const pg_kmer_edge_wide *edges, int64_t n_edges, int32_t K, const pg_reassembly *jobs,

@@ -16,7 +16,9 @@
 #include <atomic>
 #include <cstdint>
 #include <cstring>
+#include <new>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -363,6 +365,9 @@ extern "C" {
 pg_status pg_reassemble(const pg_kmer_edge_wide* edges, int64_t n_edges, int32_t K, const pg_reassembly* jobs,
                         int32_t n_jobs, int32_t threads, pg_reassembly_fix* fixes, char* text, int64_t text_cap,
                         int64_t* text_len) {
+  // no C++ exception crosses the C boundary: a host allocation that fails is PG_ERR_NOMEM, and
+  // threads that cannot be started leave the jobs to the threads that did start
+  try {
   if ((n_edges > 0 && !edges) || n_edges < 0 || n_jobs < 0 || (n_jobs > 0 && (!jobs || !fixes)) || !text_len ||
       text_cap < 0 || (text_cap > 0 && !text) || K < 1 || K > 63)
     return PG_ERR_ARG;
@@ -394,23 +399,33 @@ pg_status pg_reassemble(const pg_kmer_edge_wide* edges, int64_t n_edges, int32_t
     for (int32_t i; (i = next.fetch_add(1)) < n_jobs;) {
       const pg_reassembly& j = jobs[i];
       const int64_t e0 = start[j.window], e1 = start[j.window + 1];
-      Graph G(K, (size_t)(e1 - e0));
-      for (int64_t t = e0; t < e1; t++) {
-        const pg_kmer_edge_wide& e = edges[order[t]];
-        Edge* v = G.g.insert(Key{{e.key[0], e.key[1], e.key[2], e.key[3]}});
-        v->next = e.next;
-        v->alt = e.alt;
-      }
       try {
+        Graph G(K, (size_t)(e1 - e0));
+        for (int64_t t = e0; t < e1; t++) {
+          const pg_kmer_edge_wide& e = edges[order[t]];
+          Edge* v = G.g.insert(Key{{e.key[0], e.key[1], e.key[2], e.key[3]}});
+          v->next = e.next;
+          v->alt = e.alt;
+        }
         sol[i] = reassemble(G, j, loops[i]);
       } catch (RangeError&) {
         status[i] = PG_ERR_INDEX;
+      } catch (std::bad_alloc&) {
+        sol[i] = Solution();
+        status[i] = PG_ERR_NOMEM;
       }
     }
   };
   const int32_t nt = std::max(1, std::min(threads > 0 ? threads : (int32_t)std::thread::hardware_concurrency(), n_jobs));
   std::vector<std::thread> pool;
-  for (int32_t t = 1; t < nt; t++) pool.emplace_back(work);
+  pool.reserve((size_t)nt);
+  for (int32_t t = 1; t < nt; t++) {
+    try {
+      pool.emplace_back(work);
+    } catch (std::system_error&) {
+      break;
+    }
+  }
   work();
   for (auto& t : pool) t.join();
   int64_t off = 0;
@@ -432,7 +447,12 @@ pg_status pg_reassemble(const pg_kmer_edge_wide* edges, int64_t n_edges, int32_t
   }
   *text_len = off;
   if (off > text_cap) rc = PG_ERR_LIMIT;
+  for (int32_t i = 0; i < n_jobs; i++)
+    if (status[i] == PG_ERR_NOMEM) rc = PG_ERR_NOMEM;
   return rc;
+  } catch (std::bad_alloc&) {
+    return PG_ERR_NOMEM;
+  }
 }
 
 }  // extern "C"
