@@ -31,7 +31,8 @@ typedef enum pg_status {
   PG_OK = 0,
   PG_ERR_ARG = 1,        /* bad argument (null pointer, bad size, bad option) */
   PG_ERR_CUDA = 2,       /* CUDA runtime error; context should be closed */
-  PG_ERR_NOMEM = 3,      /* device memory budget exceeded */
+  PG_ERR_NOMEM = 3,      /* device memory budget exceeded, or host memory or threads
+                            could not be had (no C++ exception leaves a call) */
   PG_ERR_INDEX = 4,      /* an index left its array; the reference throws
                             ArrayIndexOutOfBoundsException here (indel left
                             shift below the region start,

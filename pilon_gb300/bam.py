@@ -40,7 +40,7 @@ def _lib():
         L.bam_encoded_size.argtypes = [i64, vp, vp, vp]
         L.bam_encode.restype = i64
         L.bam_encode.argtypes = [i64] + [vp] * 17
-        L.bam_name_ids.restype = None
+        L.bam_name_ids.restype = i64
         L.bam_name_ids.argtypes = [vp, vp, i64, vp]
         L.bgzf_scan.restype = i64
         L.bgzf_scan.argtypes = [vp, i64, vp, vp, vp, i64, C.POINTER(i64), C.POINTER(C.c_int32)]
@@ -202,12 +202,15 @@ def read_bam(path, threads=None, names=False):
                    n_cigar=np.empty(n, np.uint16), cigar=np.empty(nc.value, np.uint32),
                    seq_off=np.empty(n, np.int64), l_seq=np.empty(n, np.int32), seq=np.empty(sb.value, np.uint8),
                    qual_off=np.empty(n, np.int64), qual=np.empty(qb.value, np.uint8))
-    L.bam_fill(recs.ctypes.data, starts.ctypes.data, n, st.pos.ctypes.data, st.aend.ctypes.data, st.tlen.ctypes.data,
-               st.ref_id.ctypes.data, st.mate_ref_id.ctypes.data, st.l_seq.ctypes.data, st.flag.ctypes.data,
-               st.n_cigar.ctypes.data, st.mapq.ctypes.data, st.seq.ctypes.data, st.qual.ctypes.data,
-               st.cigar_off.ctypes.data, st.seq_off.ctypes.data, st.qual_off.ctypes.data, st.cigar.ctypes.data,
-               _threads(threads))
+    got = L.bam_fill(recs.ctypes.data, starts.ctypes.data, n, st.pos.ctypes.data, st.aend.ctypes.data,
+                     st.tlen.ctypes.data, st.ref_id.ctypes.data, st.mate_ref_id.ctypes.data, st.l_seq.ctypes.data,
+                     st.flag.ctypes.data, st.n_cigar.ctypes.data, st.mapq.ctypes.data, st.seq.ctypes.data,
+                     st.qual.ctypes.data, st.cigar_off.ctypes.data, st.seq_off.ctypes.data, st.qual_off.ctypes.data,
+                     st.cigar.ctypes.data, _threads(threads))
+    if got != n:
+        raise MemoryError("BAM record fill: host memory exhausted")
     if want_names:
         st.name_id = np.empty(n, np.int64)
-        L.bam_name_ids(recs.ctypes.data, starts.ctypes.data, n, st.name_id.ctypes.data)
+        if L.bam_name_ids(recs.ctypes.data, starts.ctypes.data, n, st.name_id.ctypes.data) < 0:
+            raise MemoryError("BAM read-name ids: host memory exhausted")
     return names, lengths, st

@@ -16,6 +16,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <thread>
 #include <string_view>
 #include <unordered_map>
@@ -86,17 +87,25 @@ int64_t bam_index(const uint8_t* buf, int64_t n, int64_t* starts, int64_t cap, i
 // Fills the store (arrays sized by bam_index) from the records at starts, on
 // `threads` threads over contiguous ranges of records: each thread first sums
 // its records' CIGAR words, base bytes and qualities, and after a prefix over
-// the threads fills its range from its own offsets.  Returns the record count.
+// the threads fills its range from its own offsets.  Returns the record count,
+// or -1 when host memory runs out (threads that cannot be started leave their
+// ranges to the calling thread).
 int64_t bam_fill(const uint8_t* buf, const int64_t* starts, int64_t recs, int32_t* pos, int32_t* aend, int32_t* tlen,
                  int32_t* ref_id, int32_t* mate_ref_id, int32_t* l_seq_out, uint16_t* flag, uint16_t* n_cigar,
                  uint8_t* mapq, uint8_t* seq, uint8_t* qual, int64_t* cigar_off, int64_t* seq_off, int64_t* qual_off,
-                 uint32_t* cigar, int32_t threads) {
+                 uint32_t* cigar, int32_t threads) try {
   const int64_t nt = std::max<int64_t>(1, std::min<int64_t>(threads < 1 ? 1 : threads, recs));
   std::vector<int64_t> tc(nt + 1, 0), ts(nt + 1, 0), tq(nt + 1, 0);
   auto lo = [&](int64_t t) { return recs * t / nt; };
   auto run = [&](auto&& body) {
     std::vector<std::thread> pool;
-    for (int64_t t = 1; t < nt; t++) pool.emplace_back(body, t);
+    int64_t t = 1;
+    try {
+      pool.reserve((size_t)nt);
+      for (; t < nt; t++) pool.emplace_back(body, t);
+    } catch (const std::exception&) {
+    }
+    for (int64_t u = t; u < nt; u++) body(u);
     body(0);
     for (auto& th : pool) th.join();
   };
@@ -156,6 +165,8 @@ int64_t bam_fill(const uint8_t* buf, const int64_t* starts, int64_t recs, int32_
     }
   });
   return recs;
+} catch (const std::exception&) {
+  return -1;
 }
 
 // The read name of read i: "p<name_id[i]>" (mates share it) or, without name
@@ -167,8 +178,9 @@ static int read_name(char* name, size_t cap, const int64_t* name_id, int64_t i) 
 
 // Read-name ids of the records at starts: the first record with a name gets
 // the next id, later records with the same name (mates, other alignments) its
-// id, as htsjdk's getReadName strings compare.  Single pass, exact.
-void bam_name_ids(const uint8_t* buf, const int64_t* starts, int64_t recs, int64_t* out) {
+// id, as htsjdk's getReadName strings compare.  Single pass, exact.  Returns
+// the number of distinct names, or -1 when host memory runs out.
+int64_t bam_name_ids(const uint8_t* buf, const int64_t* starts, int64_t recs, int64_t* out) try {
   std::unordered_map<std::string_view, int64_t> ids;
   ids.reserve((size_t)(recs / 2 + 1));
   for (int64_t i = 0; i < recs; i++) {
@@ -179,6 +191,9 @@ void bam_name_ids(const uint8_t* buf, const int64_t* starts, int64_t recs, int64
     auto it = ids.emplace(std::string_view(nm, len), (int64_t)ids.size()).first;
     out[i] = it->second;
   }
+  return (int64_t)ids.size();
+} catch (const std::exception&) {
+  return -1;
 }
 
 // Bytes of the BAM records of reads [0, n) (read names as read_name gives them).

@@ -11,6 +11,7 @@
 #include <atomic>
 #include <cstdint>
 #include <cstring>
+#include <exception>
 #include <thread>
 #include <vector>
 
@@ -439,7 +440,11 @@ int64_t bgzf_inflate_blocks(const uint8_t* in, int64_t n_blocks, const int64_t* 
   };
   const int nt = threads < 1 ? 1 : threads;
   std::vector<std::thread> pool;
-  for (int t = 1; t < nt; t++) pool.emplace_back(work);
+  try {  // blocks are taken from a shared counter: threads that cannot start leave them to the others
+    pool.reserve((size_t)nt);
+    for (int t = 1; t < nt; t++) pool.emplace_back(work);
+  } catch (const std::exception&) {
+  }
   work();
   for (auto& t : pool) t.join();
   return bad.load() < 0 ? 0 : -(bad.load() + 1);

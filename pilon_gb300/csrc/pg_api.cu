@@ -16,6 +16,7 @@
 #include "pg_kmer.cuh"
 #include "pg_breaks.cuh"
 #include "pg_format.cuh"
+#include "pg_host_guard.h"
 
 // NVTX range over one entry point (a profiler shows the host side of each call;
 // without a tool attached a push/pop costs a few nanoseconds)
@@ -243,7 +244,7 @@ void pg_default_params(pg_params* p) {
   p->bam_type = PG_BAM_FRAGS;
 }
 
-pg_status pg_open(pg_ctx** out, int device) {
+pg_status pg_open(pg_ctx** out, int device) try {
   if (!out) return PG_ERR_ARG;
   *out = nullptr;
   pg_ctx* c = new pg_ctx();
@@ -270,7 +271,7 @@ pg_status pg_open(pg_ctx** out, int device) {
   cudaEventCreate(&c->w1);
   *out = c;
   return PG_OK;
-}
+} PG_HOST_CATCH(out ? *out : nullptr)
 
 void pg_close(pg_ctx* c) {
   if (!c) return;
@@ -308,7 +309,7 @@ void pg_close(pg_ctx* c) {
 
 const char* pg_last_error(const pg_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
-pg_status pg_set_tuning(pg_ctx* c, int32_t tile_width, int32_t warps_per_cta, int32_t variant) {
+pg_status pg_set_tuning(pg_ctx* c, int32_t tile_width, int32_t warps_per_cta, int32_t variant) try {
   if (!c) return PG_ERR_ARG;
   if (tile_width) {
     if (tile_width < 256 || tile_width > 4096 || (tile_width & (tile_width - 1)))
@@ -324,7 +325,7 @@ pg_status pg_set_tuning(pg_ctx* c, int32_t tile_width, int32_t warps_per_cta, in
     c->packed = variant;
   }
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
 // Pilon's --defaultqual is a Byte (S/Pilon.scala:53, 144: value.toByte throws
 // outside -128..127); the walk's packed counters rely on that range too.
@@ -340,15 +341,15 @@ static pg_status not_open(pg_ctx* c) {
   return fail(c, PG_ERR_STATE, "the context is not open (pg_open failed: %s)", c->open_err.c_str());
 }
 
-pg_status pg_sync(pg_ctx* c) {
+pg_status pg_sync(pg_ctx* c) try {
   if (!c) return PG_ERR_ARG;
   if (!c->stream) return not_open(c);
   cudaSetDevice(c->device);
   CK(cudaStreamSynchronize(c->stream));
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
-pg_status pg_set_reference(pg_ctx* c, int32_t n, const int64_t* lens, const uint8_t* const* bases) {
+pg_status pg_set_reference(pg_ctx* c, int32_t n, const int64_t* lens, const uint8_t* const* bases) try {
   const Range nvtx_range("pg_set_reference");
   if (!c || n < 0 || (n > 0 && (!lens || !bases))) return fail(c, PG_ERR_ARG, "bad reference arguments");
   for (int i = 0; i < n; i++) {
@@ -375,7 +376,7 @@ pg_status pg_set_reference(pg_ctx* c, int32_t n, const int64_t* lens, const uint
       CK(cudaMemcpyAsync(P<uint8_t>(c->ref) + c->ref_off[i], bases[i], lens[i], cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
 static pg_status finish_reads(pg_ctx* c) {
   c->have_reads = false;
@@ -417,15 +418,15 @@ static pg_status finish_reads(pg_ctx* c) {
 
 static pg_status upload_reads(pg_ctx* c, const pg_reads* h, bool packed);
 
-pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) {
+pg_status pg_set_reads(pg_ctx* c, const pg_reads* h) try {
   const Range nvtx_range("pg_set_reads");
   return upload_reads(c, h, false);
-}
+} PG_HOST_CATCH(c)
 
-pg_status pg_set_reads_packed(pg_ctx* c, const pg_reads* h) {
+pg_status pg_set_reads_packed(pg_ctx* c, const pg_reads* h) try {
   const Range nvtx_range("pg_set_reads_packed");
   return upload_reads(c, h, true);
-}
+} PG_HOST_CATCH(c)
 
 // packed: the offsets and alignment ends are not read from the host (they may
 // be NULL); the device derives them from the lengths and the CIGARs
@@ -496,7 +497,7 @@ static pg_status upload_reads(pg_ctx* c, const pg_reads* h, bool packed) {
   return finish_reads(c);
 }
 
-pg_status pg_set_reads_device(pg_ctx* c, const pg_reads* d) {
+pg_status pg_set_reads_device(pg_ctx* c, const pg_reads* d) try {
   const Range nvtx_range("pg_set_reads_device");
   if (!c || !d || d->n_reads < 0) return fail(c, PG_ERR_ARG, "bad reads");
   if (d->n_cigar_words < 0 || d->seq_bytes < 0 || d->qual_bytes < 0)
@@ -511,7 +512,7 @@ pg_status pg_set_reads_device(pg_ctx* c, const pg_reads* d) {
   R.cigar = d->cigar;
   R.n_cigar_words = d->n_cigar_words; R.seq_bytes = d->seq_bytes; R.qual_bytes = d->qual_bytes;
   return finish_reads(c);
-}
+} PG_HOST_CATCH(c)
 
 static pg_status stage(pg_ctx* c, size_t bytes) {
   if (bytes <= c->staging_cap) return PG_OK;
@@ -622,7 +623,7 @@ static void run_range(pg_ctx* c, const Plan& plan, int32_t r0, int32_t r1, const
 }
 
 pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions, const pg_params* params,
-                            int32_t batched) {
+                            int32_t batched) try {
   const Range nvtx_range("pg_pileup_regions");
   if (!c || (n_regions > 0 && !regs) || !params || n_regions < 0) return fail(c, PG_ERR_ARG, "bad arguments");
   if (params->min_qual < 0 || params->flank < 0 || params->min_mq < 0)
@@ -839,9 +840,9 @@ pg_status pg_pileup_regions(pg_ctx* c, const pg_region* regs, int32_t n_regions,
     }
   }
   return fail(c, PG_ERR_LIMIT, "event/candidate buffers kept overflowing");
-}
+} PG_HOST_CATCH(c)
 
-pg_status pg_fetch_stats(pg_ctx* c, int32_t r, pg_region_stats* out) {
+pg_status pg_fetch_stats(pg_ctx* c, int32_t r, pg_region_stats* out) try {
   if (!c || !out) return PG_ERR_ARG;
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
   if (r < 0 || r >= c->n_regions) return fail(c, PG_ERR_ARG, "region %d out of range", r);
@@ -858,7 +859,7 @@ pg_status pg_fetch_stats(pg_ctx* c, int32_t r, pg_region_stats* out) {
   out->error = s.error;
   out->n_ins_strings = 0;
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
 // Copies positions [b, b + n) of every non-null array of o, then the
 // insertion characters; one synchronisation.
@@ -899,7 +900,7 @@ static pg_status fetch_positions(pg_ctx* c, int64_t b, size_t n, pg_region_out* 
   return PG_OK;
 }
 
-pg_status pg_fetch_region(pg_ctx* c, int32_t r, pg_region_out* o) {
+pg_status pg_fetch_region(pg_ctx* c, int32_t r, pg_region_out* o) try {
   const Range nvtx_range("pg_fetch_region");
   if (!c || !o) return PG_ERR_ARG;
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
@@ -907,18 +908,18 @@ pg_status pg_fetch_region(pg_ctx* c, int32_t r, pg_region_out* o) {
   cudaSetDevice(c->device);
   const RegionDev& g = c->regions_h[r];
   return fetch_positions(c, g.pos_base, (size_t)g.size, o);
-}
+} PG_HOST_CATCH(c)
 
-pg_status pg_fetch_all(pg_ctx* c, pg_region_out* o) {
+pg_status pg_fetch_all(pg_ctx* c, pg_region_out* o) try {
   const Range nvtx_range("pg_fetch_all");
   if (!c || !o) return PG_ERR_ARG;
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
   cudaSetDevice(c->device);
   return fetch_positions(c, 0, (size_t)c->n_positions, o);
-}
+} PG_HOST_CATCH(c)
 
 pg_status pg_fetch_changes(pg_ctx* c, pg_change* out, int64_t cap, int64_t* n_changes, char* ins_chars,
-                           int64_t ins_cap, int64_t* n_ins_chars) {
+                           int64_t ins_cap, int64_t* n_ins_chars) try {
   const Range nvtx_range("pg_fetch_changes");
   if (!c || !n_changes || !n_ins_chars || cap < 0 || (cap > 0 && !out) || ins_cap < 0)
     return fail(c, PG_ERR_ARG, "bad arguments");
@@ -951,7 +952,7 @@ pg_status pg_fetch_changes(pg_ctx* c, pg_change* out, int64_t cap, int64_t* n_ch
   *n_changes = total;
   *n_ins_chars = (int64_t)pool_fill;
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
 static int64_t next_pow2(int64_t x) {
   int64_t p = 1;
@@ -966,25 +967,25 @@ static pg_status kmer_windows(pg_ctx* c, const pg_window* windows, int32_t n_win
                               int64_t* n_edges, int64_t n_list = 0, const int64_t* rlist = nullptr);
 
 pg_status pg_kmer_tally(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K, const pg_params* params,
-                        int32_t min_depth, pg_kmer_edge* edges, int64_t cap, int64_t* n_edges) {
+                        int32_t min_depth, pg_kmer_edge* edges, int64_t cap, int64_t* n_edges) try {
   const Range nvtx_range("pg_kmer_tally");
   if (c && (K < 1 || K > 31))
     return fail(c, PG_ERR_LIMIT, "K = %d: pg_kmer_tally packs K-mers in 64 bits (K <= 31); pg_kmer_tally_wide "
                 "takes K <= 63", K);
   return kmer_windows(c, windows, n_windows, K, params, min_depth, false, edges, cap, n_edges);
-}
+} PG_HOST_CATCH(c)
 
 pg_status pg_kmer_tally_wide(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K,
                              const pg_params* params, int32_t min_depth, pg_kmer_edge_wide* edges, int64_t cap,
-                             int64_t* n_edges) {
+                             int64_t* n_edges) try {
   const Range nvtx_range("pg_kmer_tally_wide");
   if (c && (K < 1 || K > 63)) return fail(c, PG_ERR_LIMIT, "K = %d: pg_kmer_tally_wide takes K <= 63", K);
   return kmer_windows(c, windows, n_windows, K, params, min_depth, true, edges, cap, n_edges);
-}
+} PG_HOST_CATCH(c)
 
 pg_status pg_kmer_tally_reads(pg_ctx* c, const int64_t* reads, int64_t n_reads, const pg_window* windows,
                               int32_t n_windows, int32_t K, const pg_params* params, int32_t min_depth,
-                              pg_kmer_edge_wide* edges, int64_t cap, int64_t* n_edges) {
+                              pg_kmer_edge_wide* edges, int64_t cap, int64_t* n_edges) try {
   const Range nvtx_range("pg_kmer_tally_reads");
   if (!c) return PG_ERR_ARG;
   if (K < 1 || K > 63) return fail(c, PG_ERR_LIMIT, "K = %d: pg_kmer_tally_reads takes K <= 63", K);
@@ -1002,7 +1003,7 @@ pg_status pg_kmer_tally_reads(pg_ctx* c, const int64_t* reads, int64_t n_reads, 
   if (n_reads > 0) CK(cudaMemcpyAsync(c->klist.p, reads, 8 * (size_t)n_reads, cudaMemcpyHostToDevice, c->stream));
   return kmer_windows(c, windows, n_windows, K, params, min_depth, true, edges, cap, n_edges, n_reads,
                       P<int64_t>(c->klist));
-}
+} PG_HOST_CATCH(c)
 
 static pg_status kmer_windows(pg_ctx* c, const pg_window* windows, int32_t n_windows, int32_t K,
                               const pg_params* params, int32_t min_depth, bool wide, void* edges, int64_t cap,
@@ -1247,7 +1248,7 @@ static pg_status find_breaks_device(pg_ctx* c, int32_t min_min_depth) {
   return PG_OK;
 }
 
-pg_status pg_find_breaks(pg_ctx* c, int32_t min_min_depth, pg_break* out, int64_t cap, int64_t* n_breaks) {
+pg_status pg_find_breaks(pg_ctx* c, int32_t min_min_depth, pg_break* out, int64_t cap, int64_t* n_breaks) try {
   const Range nvtx_range("pg_find_breaks");
   if (!c || !n_breaks || cap < 0 || (cap > 0 && !out)) return fail(c, PG_ERR_ARG, "bad arguments");
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no pileup results: call pg_pileup_regions first");
@@ -1263,9 +1264,9 @@ pg_status pg_find_breaks(pg_ctx* c, int32_t min_min_depth, pg_break* out, int64_
     CK(cudaStreamSynchronize(c->stream));
   }
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
-pg_status pg_find_duplications(pg_ctx* c, pg_break* out, int64_t cap, int64_t* n_dups) {
+pg_status pg_find_duplications(pg_ctx* c, pg_break* out, int64_t cap, int64_t* n_dups) try {
   const Range nvtx_range("pg_find_duplications");
   if (!c || !n_dups || cap < 0 || (cap > 0 && !out)) return fail(c, PG_ERR_ARG, "bad arguments");
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no pileup results: call pg_pileup_regions first");
@@ -1302,7 +1303,7 @@ pg_status pg_find_duplications(pg_ctx* c, pg_break* out, int64_t cap, int64_t* n
   *n_dups = (int64_t)v.size();
   for (int64_t k = 0; k < std::min<int64_t>(cap, (int64_t)v.size()); k++) out[k] = v[k];
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
 static pg_status kmer_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius, int32_t K, const pg_params* params,
                              int32_t min_depth, bool wide, void* edges, int64_t cap, int64_t* n_windows,
@@ -1310,21 +1311,21 @@ static pg_status kmer_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius, i
 
 pg_status pg_kmer_tally_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius, int32_t K, const pg_params* params,
                                int32_t min_depth, pg_kmer_edge* edges, int64_t cap, int64_t* n_windows,
-                               int64_t* n_edges) {
+                               int64_t* n_edges) try {
   const Range nvtx_range("pg_kmer_tally_breaks");
   if (c && (K < 1 || K > 31))
     return fail(c, PG_ERR_LIMIT, "K = %d: pg_kmer_tally_breaks packs K-mers in 64 bits (K <= 31); "
                 "pg_kmer_tally_breaks_wide takes K <= 63", K);
   return kmer_breaks(c, min_min_depth, radius, K, params, min_depth, false, edges, cap, n_windows, n_edges);
-}
+} PG_HOST_CATCH(c)
 
 pg_status pg_kmer_tally_breaks_wide(pg_ctx* c, int32_t min_min_depth, int32_t radius, int32_t K,
                                     const pg_params* params, int32_t min_depth, pg_kmer_edge_wide* edges,
-                                    int64_t cap, int64_t* n_windows, int64_t* n_edges) {
+                                    int64_t cap, int64_t* n_windows, int64_t* n_edges) try {
   const Range nvtx_range("pg_kmer_tally_breaks_wide");
   if (c && (K < 1 || K > 63)) return fail(c, PG_ERR_LIMIT, "K = %d: pg_kmer_tally_breaks_wide takes K <= 63", K);
   return kmer_breaks(c, min_min_depth, radius, K, params, min_depth, true, edges, cap, n_windows, n_edges);
-}
+} PG_HOST_CATCH(c)
 
 static pg_status kmer_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius, int32_t K, const pg_params* params,
                              int32_t min_depth, bool wide, void* edges, int64_t cap, int64_t* n_windows,
@@ -1350,7 +1351,7 @@ static pg_status kmer_breaks(pg_ctx* c, int32_t min_min_depth, int32_t radius, i
   return kmer_core(c, n, K, params, min_depth, wide, edges, cap, n_edges);
 }
 
-pg_status pg_mark_deleted(pg_ctx* c, int32_t r, int32_t first_locus, int32_t count) {
+pg_status pg_mark_deleted(pg_ctx* c, int32_t r, int32_t first_locus, int32_t count) try {
   if (!c || count < 0) return fail(c, PG_ERR_ARG, "bad arguments");
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
   if (r < 0 || r >= c->n_regions) return fail(c, PG_ERR_ARG, "region %d out of range", r);
@@ -1363,10 +1364,10 @@ pg_status pg_mark_deleted(pg_ctx* c, int32_t r, int32_t first_locus, int32_t cou
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->stream));
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
 pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid, int32_t vcf_qe,
-                        int32_t variants_only, char* out, int64_t cap, int64_t* n_bytes) {
+                        int32_t variants_only, char* out, int64_t cap, int64_t* n_bytes) try {
   const Range nvtx_range("pg_format_vcf");
   if (!c || !name || !n_bytes || cap < 0) return fail(c, PG_ERR_ARG, "bad arguments");
   if (!c->have_results) return fail(c, PG_ERR_STATE, "no results: run pg_pileup_regions first");
@@ -1406,10 +1407,10 @@ pg_status pg_format_vcf(pg_ctx* c, int32_t r, const char* name, int32_t diploid,
   if (total && out) CK(cudaMemcpyAsync(out, c->vtext.p, (size_t)total, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
 pg_status pg_last_tally_stats(pg_ctx* c, double* kernel_ms, int64_t* kmer_events, int64_t* distinct_kmers,
-                              int64_t* max_batch_table_bytes, int32_t* batches) {
+                              int64_t* max_batch_table_bytes, int32_t* batches) try {
   if (!c) return PG_ERR_ARG;
   if (kernel_ms) *kernel_ms = c->tally_ms;
   if (kmer_events) *kmer_events = c->tally_events;
@@ -1417,20 +1418,20 @@ pg_status pg_last_tally_stats(pg_ctx* c, double* kernel_ms, int64_t* kmer_events
   if (max_batch_table_bytes) *max_batch_table_bytes = c->tally_max_batch_bytes;
   if (batches) *batches = c->tally_batches;
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
-pg_status pg_graph_replays(pg_ctx* c, int32_t* replays) {
+pg_status pg_graph_replays(pg_ctx* c, int32_t* replays) try {
   if (!c || !replays) return PG_ERR_ARG;
   *replays = c->graph_replays;
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
-pg_status pg_last_kernel_ms(pg_ctx* c, double* walk_ms, double* total_ms, int32_t* launches) {
+pg_status pg_last_kernel_ms(pg_ctx* c, double* walk_ms, double* total_ms, int32_t* launches) try {
   if (!c) return PG_ERR_ARG;
   if (walk_ms) *walk_ms = c->walk_ms;
   if (total_ms) *total_ms = c->total_ms;
   if (launches) *launches = c->launches;
   return PG_OK;
-}
+} PG_HOST_CATCH(c)
 
 }  // extern "C"

@@ -16,13 +16,12 @@
 #include <atomic>
 #include <cstdint>
 #include <cstring>
-#include <new>
 #include <string>
-#include <system_error>
 #include <thread>
 #include <vector>
 
 #include "pilon_gb300.h"
+#include "pg_host_guard.h"
 
 namespace {
 
@@ -364,10 +363,9 @@ extern "C" {
 
 pg_status pg_reassemble(const pg_kmer_edge_wide* edges, int64_t n_edges, int32_t K, const pg_reassembly* jobs,
                         int32_t n_jobs, int32_t threads, pg_reassembly_fix* fixes, char* text, int64_t text_cap,
-                        int64_t* text_len) {
+                        int64_t* text_len) try {
   // no C++ exception crosses the C boundary: a host allocation that fails is PG_ERR_NOMEM, and
   // threads that cannot be started leave the jobs to the threads that did start
-  try {
   if ((n_edges > 0 && !edges) || n_edges < 0 || n_jobs < 0 || (n_jobs > 0 && (!jobs || !fixes)) || !text_len ||
       text_cap < 0 || (text_cap > 0 && !text) || K < 1 || K > 63)
     return PG_ERR_ARG;
@@ -410,9 +408,9 @@ pg_status pg_reassemble(const pg_kmer_edge_wide* edges, int64_t n_edges, int32_t
         sol[i] = reassemble(G, j, loops[i]);
       } catch (RangeError&) {
         status[i] = PG_ERR_INDEX;
-      } catch (std::bad_alloc&) {
+      } catch (...) {
         sol[i] = Solution();
-        status[i] = PG_ERR_NOMEM;
+        status[i] = pg::host_exception_status(nullptr);
       }
     }
   };
@@ -422,7 +420,7 @@ pg_status pg_reassemble(const pg_kmer_edge_wide* edges, int64_t n_edges, int32_t
   for (int32_t t = 1; t < nt; t++) {
     try {
       pool.emplace_back(work);
-    } catch (std::system_error&) {
+    } catch (const std::exception&) {
       break;
     }
   }
@@ -448,11 +446,8 @@ pg_status pg_reassemble(const pg_kmer_edge_wide* edges, int64_t n_edges, int32_t
   *text_len = off;
   if (off > text_cap) rc = PG_ERR_LIMIT;
   for (int32_t i = 0; i < n_jobs; i++)
-    if (status[i] == PG_ERR_NOMEM) rc = PG_ERR_NOMEM;
+    if (status[i] == PG_ERR_NOMEM || status[i] == PG_ERR_LIMIT) rc = (pg_status)status[i];
   return rc;
-  } catch (std::bad_alloc&) {
-    return PG_ERR_NOMEM;
-  }
-}
+} PG_HOST_CATCH(nullptr)
 
 }  // extern "C"

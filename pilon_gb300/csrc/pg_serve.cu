@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "pilon_gb300.h"
+#include "pg_host_guard.h"
 
 namespace {
 
@@ -228,27 +229,36 @@ pg_status answer(pg_server* S, pg_ctx* ctx, int32_t r, Job& j) {
 }
 
 // A free worker's next batch: from the head of the queue, every request whose
-// device bytes still fit the budget beside the batches in flight.
-std::vector<uint64_t> take(pg_server* S, std::unique_lock<std::mutex>& lk, int64_t& bytes) {
-  std::vector<uint64_t> batch;
+// device bytes still fit the budget beside the batches in flight.  The batch's
+// room is reserved before anything leaves the queue, so an allocation that
+// fails here leaves the queue as it was.
+void take(pg_server* S, std::unique_lock<std::mutex>& lk, int64_t& bytes, std::vector<Job*>& js) {
+  js.clear();
   bytes = 0;
   for (;;) {
-    if (S->closing && S->queue.empty()) return batch;
+    if (S->closing && S->queue.empty()) return;
     if (!S->queue.empty() && S->in_flight + S->jobs[S->queue.front()].bytes <= S->cfg.hbm_budget) break;
     S->cv_work.wait(lk);
   }
-  while (!S->queue.empty()) {
-    Job& j = S->jobs[S->queue.front()];
-    if (S->in_flight + bytes + j.bytes > S->cfg.hbm_budget) break;
-    if (S->cfg.max_batch > 0 && (int32_t)batch.size() >= S->cfg.max_batch) break;
-    bytes += j.bytes;
-    batch.push_back(S->queue.front());
+  size_t count = 0;
+  for (uint64_t t : S->queue) {
+    const int64_t b = S->jobs[t].bytes;
+    if (S->in_flight + bytes + b > S->cfg.hbm_budget) break;
+    if (S->cfg.max_batch > 0 && (int32_t)count >= S->cfg.max_batch) break;
+    bytes += b;
+    count++;
+  }
+  js.reserve(count);
+  for (size_t k = 0; k < count; k++) {
+    js.push_back(&S->jobs[S->queue.front()]);  // map nodes stay put until released
     S->queue.pop_front();
   }
   S->in_flight += bytes;
   S->peak_in_flight = std::max(S->peak_in_flight, S->in_flight);
-  return batch;
 }
+
+// A request that fails on a host exception: its status and message.
+void fail_on_exception(Job& j) noexcept { j.status = pg::host_exception_status(&j.message); }
 
 void worker(pg_server* S, pg_ctx* ctx) {
   cudaSetDevice(S->device);
@@ -256,41 +266,62 @@ void worker(pg_server* S, pg_ctx* ctx) {
   std::vector<Job*> js;
   for (;;) {
     int64_t bytes = 0;
-    std::vector<uint64_t> batch;
     int32_t bno = 0;
     {
       std::unique_lock<std::mutex> lk(S->mu);
-      batch = take(S, lk, bytes);
-      if (batch.empty()) return;
+      try {
+        take(S, lk, bytes, js);
+      } catch (...) {
+        // no room for a batch: the request at the head fails alone, so the queue still moves
+        if (S->queue.empty()) continue;
+        Job& j = S->jobs[S->queue.front()];
+        S->queue.pop_front();
+        fail_on_exception(j);
+        j.finished = Clock::now();
+        j.done = true;
+        lk.unlock();
+        S->cv_done.notify_all();
+        continue;
+      }
+      if (js.empty()) return;
       bno = (int32_t)++S->batches;
-      js.clear();
-      for (uint64_t t : batch) js.push_back(&S->jobs[t]);  // map nodes stay put until released
     }
     const Clock::time_point t0 = Clock::now();
-    regions.clear();
     for (Job* j : js) {
       j->started = t0;
       j->batch = bno;
-      regions.push_back(pg_region{j->req.contig, j->req.start, j->req.stop, 0, j->rb, j->re});
     }
-    pg_status st = pg_pileup_regions(ctx, regions.data(), (int32_t)regions.size(), &S->params, S->cfg.batched);
-    std::string msg = st ? pg_last_error(ctx) : "";
+    pg_status st = PG_OK;
+    std::string msg;
+    try {
+      regions.clear();
+      regions.reserve(js.size());
+      for (Job* j : js) regions.push_back(pg_region{j->req.contig, j->req.start, j->req.stop, 0, j->rb, j->re});
+      st = pg_pileup_regions(ctx, regions.data(), (int32_t)regions.size(), &S->params, S->cfg.batched);
+      if (st) msg = pg_last_error(ctx);
+    } catch (...) {
+      st = pg::host_exception_status(&msg);
+    }
     for (size_t r = 0; r < js.size(); r++) {
       Job& j = *js[r];
-      if (st == PG_OK || st == PG_ERR_INDEX) {
-        pg_region_stats rs{};
-        pg_status s2 = pg_fetch_stats(ctx, (int32_t)r, &rs);
-        if (s2) { j.status = s2; j.message = pg_last_error(ctx); }
-        else if (rs.error) {
-          j.status = PG_ERR_INDEX;
-          j.message = "an indel left shift leaves the target (Pilon throws ArrayIndexOutOfBoundsException)";
-        } else if ((s2 = answer(S, ctx, (int32_t)r, j))) {
-          j.status = s2;
-          j.message = pg_last_error(ctx);
+      try {
+        if (st == PG_OK || st == PG_ERR_INDEX) {
+          pg_region_stats rs{};
+          pg_status s2 = pg_fetch_stats(ctx, (int32_t)r, &rs);
+          if (s2) { j.status = s2; j.message = pg_last_error(ctx); }
+          else if (rs.error) {
+            j.status = PG_ERR_INDEX;
+            j.message = "an indel left shift leaves the target (Pilon throws ArrayIndexOutOfBoundsException)";
+          } else if ((s2 = answer(S, ctx, (int32_t)r, j))) {
+            j.status = s2;
+            j.message = pg_last_error(ctx);
+          }
+        } else {
+          j.status = st;
+          j.message = msg;
         }
-      } else {
-        j.status = st;
-        j.message = msg;
+      } catch (...) {
+        fail_on_exception(j);
       }
     }
     {
@@ -332,7 +363,7 @@ void pg_default_serve_config(pg_serve_config* c) {
 
 pg_status pg_serve_open(pg_server** out, const pg_serve_config* cfg, const pg_params* params, int32_t n_contigs,
                         const char* const* names, const int64_t* lens, const uint8_t* const* bases,
-                        const pg_reads* h) {
+                        const pg_reads* h) try {
   if (!out) return PG_ERR_ARG;
   *out = nullptr;
   pg_server* S = new pg_server();
@@ -424,9 +455,9 @@ pg_status pg_serve_open(pg_server** out, const pg_serve_config* cfg, const pg_pa
   }
   for (pg_ctx* ctx : S->workers) S->threads.emplace_back(worker, S, ctx);
   return PG_OK;
-}
+} PG_HOST_CATCH(out ? *out : nullptr)
 
-pg_status pg_serve_submit(pg_server* S, const pg_request* q, uint64_t* ticket) {
+pg_status pg_serve_submit(pg_server* S, const pg_request* q, uint64_t* ticket) try {
   if (!S || !q || !ticket) return PG_ERR_ARG;
   if (S->threads.empty()) return serr(S, PG_ERR_STATE, "the server is not open");
   if (q->contig < 0 || q->contig >= (int32_t)S->lens.size() || q->start < 1 || q->stop < q->start ||
@@ -455,9 +486,9 @@ pg_status pg_serve_submit(pg_server* S, const pg_request* q, uint64_t* ticket) {
   }
   S->cv_work.notify_one();
   return PG_OK;
-}
+} PG_HOST_CATCH(S)
 
-pg_status pg_serve_poll(pg_server* S, uint64_t ticket, int32_t wait_ms, pg_result* out) {
+pg_status pg_serve_poll(pg_server* S, uint64_t ticket, int32_t wait_ms, pg_result* out) try {
   if (!S || !out) return PG_ERR_ARG;
   std::unique_lock<std::mutex> lk(S->mu);
   auto it = S->jobs.find(ticket);
@@ -486,9 +517,9 @@ pg_status pg_serve_poll(pg_server* S, uint64_t ticket, int32_t wait_ms, pg_resul
   out->latency_ms = ms(j.submitted, j.finished);
   out->device_bytes = j.bytes;
   return PG_OK;
-}
+} PG_HOST_CATCH(S)
 
-pg_status pg_serve_release(pg_server* S, uint64_t ticket) {
+pg_status pg_serve_release(pg_server* S, uint64_t ticket) try {
   if (!S) return PG_ERR_ARG;
   std::lock_guard<std::mutex> lk(S->mu);
   auto it = S->jobs.find(ticket);
@@ -496,16 +527,16 @@ pg_status pg_serve_release(pg_server* S, uint64_t ticket) {
   if (!it->second.done) return serr(S, PG_ERR_STATE, "ticket %llu is not answered yet", (unsigned long long)ticket);
   S->jobs.erase(it);
   return PG_OK;
-}
+} PG_HOST_CATCH(S)
 
-pg_status pg_serve_stats(pg_server* S, int64_t* batches, int64_t* in_flight_bytes, int64_t* peak_in_flight_bytes) {
+pg_status pg_serve_stats(pg_server* S, int64_t* batches, int64_t* in_flight_bytes, int64_t* peak_in_flight_bytes) try {
   if (!S) return PG_ERR_ARG;
   std::lock_guard<std::mutex> lk(S->mu);
   if (batches) *batches = S->batches;
   if (in_flight_bytes) *in_flight_bytes = S->in_flight;
   if (peak_in_flight_bytes) *peak_in_flight_bytes = S->peak_in_flight;
   return PG_OK;
-}
+} PG_HOST_CATCH(S)
 
 const char* pg_serve_error(const pg_server* S) { return S ? S->err.c_str() : "null server"; }
 

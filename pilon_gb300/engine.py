@@ -408,7 +408,8 @@ def reassemble(edges, K, jobs, threads=0):
             cap = int(tl.value)
             continue
         if st:
-            raise EngineError(st, "pg_reassemble: bad arguments")
+            raise EngineError(st, "pg_reassemble: bad arguments" if st == _abi.PG_ERR_ARG
+                              else "pg_reassemble: host memory or threads exhausted")
         break
     t = text.tobytes()
     out = []

@@ -185,3 +185,66 @@ def test_header_compiles_as_c99_and_links(tmp_path):
     assert out.returncode == 0, (out.returncode, out.stderr)
     version, r, p, e, j, f = out.stdout.strip().split("|")
     assert version.startswith("pilon_gb300") and (int(r), int(p), int(e), int(j), int(f)) == (32, 56, 32, 48, 48)
+
+
+C_NOMEM_CLIENT = r"""
+#define _GNU_SOURCE
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/resource.h>
+#include <unistd.h>
+#include "pilon_gb300.h"
+
+int main(void) {
+  /* one window of 2^21 edges: its graph table needs about 150 MB of host memory */
+  const int64_t n_edges = (int64_t)1 << 21;
+  pg_kmer_edge_wide *edges = calloc((size_t)n_edges, sizeof *edges);
+  char *bases = malloc(100), *orig = malloc(100), *text = malloc(4096);
+  if (!edges || !bases || !orig || !text) return 2;
+  memset(edges, 0, (size_t)n_edges * sizeof *edges);
+  memset(bases, 'A', 100);
+  memcpy(orig, bases, 100);
+  pg_reassembly job = {0, 0, 1, 100, 40, 60, 50, 0, bases, orig};
+  pg_reassembly_fix fix;
+  int64_t text_len = -1;
+  /* room for the call's own bookkeeping (about 20 MB), not for the graph */
+  long vm_pages = 0;
+  FILE *f = fopen("/proc/self/statm", "r");
+  if (!f || fscanf(f, "%ld", &vm_pages) != 1) return 3;
+  fclose(f);
+  struct rlimit rl;
+  rl.rlim_cur = rl.rlim_max = (rlim_t)vm_pages * (rlim_t)sysconf(_SC_PAGESIZE) + ((rlim_t)48 << 20);
+  if (setrlimit(RLIMIT_AS, &rl) != 0) return 4;
+  pg_status st = pg_reassemble(edges, n_edges, 31, &job, 1, 1, &fix, text, 4096, &text_len);
+  printf("%d|%d\n", (int)st, (int)fix.status);
+  return 0;
+}
+"""
+
+
+def test_reassemble_host_memory_exhaustion_is_a_status(tmp_path):
+    """A host allocation that fails inside pg_reassemble comes back as
+    PG_ERR_NOMEM, for the call and the job, instead of a C++ exception that
+    would end the caller's process (run in a child with a capped address
+    space)."""
+    import shutil
+    import subprocess
+    from pilon_gb300 import _abi
+    from pilon_gb300.build import ENGINE, build
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    if not os.path.exists(ENGINE):
+        build()
+    src = tmp_path / "nomem.c"
+    src.write_text(C_NOMEM_CLIENT)
+    exe = tmp_path / "nomem"
+    lib_dir = os.path.dirname(ENGINE)
+    lib_name = os.path.basename(ENGINE)[3:-3]
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe), "-L", lib_dir, "-l" + lib_name, "-Wl,-rpath," + lib_dir], check=True,
+                   capture_output=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, (out.returncode, out.stderr)
+    st, job = (int(x) for x in out.stdout.strip().split("|"))
+    assert st == _abi.PG_ERR_NOMEM and job == _abi.PG_ERR_NOMEM
