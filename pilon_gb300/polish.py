@@ -87,15 +87,55 @@ def fix_fix_list(fixes):
 
 
 def fix_issues(bases, start, fixes):
-    """GenomeRegion.fixIssues (S/GenomeRegion.scala:595-621) on a bytearray."""
+    """GenomeRegion.fixIssues (S/GenomeRegion.scala:595-621) on a bytearray.
+
+    Pilon applies the fixes from the last locus to the first, each on the
+    original coordinates.  fixFixList leaves fixes whose replaced ranges follow
+    one another, so that is the original bases between the ranges and each
+    patch in order, joined once (linear in the region, where splicing each
+    indel into the whole region is quadratic).  A fix that starts before the
+    end of the one before it (only a locus before the region's start can) is
+    applied the step-by-step way, as Pilon does."""
+    fx = fix_fix_list(fixes)
+    src = bytes(bases)
+    parts, at = [], 0
+    for f in fx:
+        s = f.locus - start
+        if s < at:
+            return _fix_issues_in_turn(src, start, fx)
+        parts.append(src[at:s])
+        parts.append(f.patch.encode())
+        at = s + len(f.was)
+    parts.append(src[at:])
+    return bytearray(b"".join(parts))
+
+
+def _fix_issues_in_turn(bases, start, fx):
+    """fixIssues step by step: the fixes of fx from the last to the first."""
     nb = bytearray(bases)
-    for f in reversed(fix_fix_list(fixes)):
+    for f in reversed(fx):
         s = f.locus - start
         if len(f.was) == len(f.patch):
             nb[s:s + len(f.patch)] = f.patch.encode()
         else:
             nb = nb[:s] + f.patch.encode() + nb[s + len(f.was):]
     return nb
+
+
+def fasta_lines(seq, width=80):
+    """A FASTA record's sequence lines (FastaWriter's 80 bases per line, the
+    last line shorter), as one buffer with a newline after each line."""
+    a = np.frombuffer(seq, np.uint8)
+    n = a.size
+    full = n // width
+    out = np.empty(n + (n + width - 1) // width, np.uint8)
+    body = out[:full * (width + 1)].reshape(full, width + 1)
+    body[:, :width] = a[:full * width].reshape(full, width)
+    body[:, width] = 10
+    if n > full * width:
+        out[full * (width + 1):-1] = a[full * width:]
+        out[-1] = 10
+    return out.tobytes()
 
 
 def region_string(name, s, e):  # Region.regionString (S/Region.scala:45)
@@ -359,8 +399,7 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
             for c, rs in groups:
                 seq = b"".join(bytes(results[r].bases) for r in rs)
                 ff.write(b">" + new_name(names[c]).encode() + b"\n")
-                for k in range(0, len(seq), 80):
-                    ff.write(seq[k:k + 80] + b"\n")
+                ff.write(fasta_lines(seq))
     return results
 
 

@@ -402,3 +402,39 @@ def test_served_requests_equal_target_outputs():
         got_ch += res.changes
     assert [f.replace("\n", "") for f in fasta] == got_fa
     assert got_ch == changes and changes.count("\n") == 4
+
+
+def test_fix_issues_joined_matches_fixes_applied_in_turn():
+    """fix_issues joins the unchanged stretches and the patches once; on random
+    fix lists (SNPs, insertions, deletions, replacements, overlaps, several at
+    one locus) the result is the one of applying the fixes one by one from the
+    last locus, as GenomeRegion.fixIssues does (S/GenomeRegion.scala:595-621)."""
+    from pilon_gb300.polish import Fix, _fix_issues_in_turn, fix_fix_list, fix_issues
+    rng = np.random.default_rng(7)
+    for trial in range(400):
+        n = int(rng.integers(1, 60))
+        start = int(rng.integers(1, 1000))
+        bases = bytes(rng.choice(list(b"ACGT"), n).astype(np.uint8))
+        fixes = []
+        for _ in range(int(rng.integers(0, 8))):
+            locus = start + int(rng.integers(0, n))
+            kind = int(rng.integers(0, 4))
+            wl = {0: 1, 1: 0, 2: int(rng.integers(1, 5)), 3: int(rng.integers(1, 4))}[kind]
+            pl = {0: 1, 1: int(rng.integers(1, 5)), 2: 0, 3: int(rng.integers(1, 6))}[kind]
+            was = bases[locus - start:locus - start + wl].decode()
+            patch = "".join(rng.choice(list("ACGTN"), pl))
+            fixes.append(Fix(locus, was, patch))
+        want = _fix_issues_in_turn(bases, start, fix_fix_list(fixes))
+        assert fix_issues(bases, start, fixes) == want, (trial, fixes)
+        assert fix_issues(np.frombuffer(bases, np.uint8), start, fixes) == want
+    # a fix before the region's start goes the step-by-step way
+    fixes = [Fix(8, "", "GG"), Fix(12, "A", "T")]
+    assert fix_issues(b"CCAAC", 10, fixes) == _fix_issues_in_turn(b"CCAAC", 10, fix_fix_list(fixes))
+
+
+def test_fasta_lines_wraps_at_80():
+    from pilon_gb300.polish import fasta_lines
+    for n in (0, 1, 79, 80, 81, 159, 160, 161, 1000):
+        seq = bytes(np.arange(n, dtype=np.uint8) % 26 + 65)
+        want = b"".join(seq[k:k + 80] + b"\n" for k in range(0, n, 80))
+        assert fasta_lines(seq) == want, n
