@@ -277,19 +277,18 @@ def _reassemble(engine, regions, results, contigs, reads, params, opts):
 
 
 def _exclude_motifs(orig, s, e, nano):
-    """GenomeRegion.excludeMotifs (S/GenomeRegion.scala:432-439)."""
+    """GenomeRegion.excludeMotifs (S/GenomeRegion.scala:416-439): homoRun(i) >= 4,
+    the run of equal bases from i rightwards inside the region, is the base at i
+    equal to the next three; nanoporeExclude(i) is C C x G G around i with all
+    five inside the region."""
     b = np.frombuffer(bytes(orig).upper(), np.uint8)
     n = b.size
-    run = np.ones(n, np.int64)
-    for i in range(n - 2, -1, -1):
-        if b[i] == b[i + 1]:
-            run[i] = run[i + 1] + 1
-    ex = run >= 4
-    if nano:
+    ex = np.zeros(n, bool)
+    if n >= 4:
+        ex[:n - 3] = (b[:-3] == b[1:-2]) & (b[1:-2] == b[2:-1]) & (b[2:-1] == b[3:])
+    if nano and n >= 5:
         C, G = ord("C"), ord("G")
-        for i in range(2, n - 2):
-            if b[i - 2] == C and b[i - 1] == C and b[i + 1] == G and b[i + 2] == G:
-                ex[i] = True
+        ex[2:n - 2] |= (b[:n - 4] == C) & (b[1:n - 3] == C) & (b[3:n - 1] == G) & (b[4:] == G)
     return ex
 
 

@@ -438,3 +438,30 @@ def test_fasta_lines_wraps_at_80():
         seq = bytes(np.arange(n, dtype=np.uint8) % 26 + 65)
         want = b"".join(seq[k:k + 80] + b"\n" for k in range(0, n, 80))
         assert fasta_lines(seq) == want, n
+
+
+def _exclude_motifs_by_locus(orig, nano):
+    """excludeMotifs as the reference states it, locus by locus: homoRun walks
+    right from each locus to the region's stop (S/GenomeRegion.scala:416-439)."""
+    b = bytes(orig).upper()
+    n = len(b)
+    ex = []
+    for i in range(n):
+        run = 1
+        while i + run < n and b[i + run] == b[i]:
+            run += 1
+        cc_gg = 2 <= i < n - 2 and b[i - 2:i] == b"CC" and b[i + 1:i + 3] == b"GG"
+        ex.append(run >= 4 or (nano and cc_gg))
+    return np.array(ex, bool)
+
+
+def test_exclude_motifs_matches_homorun_by_locus():
+    from pilon_gb300.polish import _exclude_motifs
+    rng = np.random.default_rng(11)
+    for n in (0, 1, 3, 4, 5, 6, 9, 40, 300):
+        for _ in range(20):
+            seq = bytes(rng.choice(list(b"CCGGAT"), n).astype(np.uint8)).lower() if rng.random() < 0.3 else \
+                bytes(rng.choice(list(b"CCGGAT"), n).astype(np.uint8))
+            for nano in (False, True):
+                got = _exclude_motifs(seq, 1, n, nano)
+                assert np.array_equal(got, _exclude_motifs_by_locus(seq, nano)), (seq, nano)
