@@ -12,6 +12,7 @@ outputs.
   changes, FASTA                host (S/GenomeRegion.scala:645-657, S/GenomeFile.scala:79-82, 135-161)
 """
 import ctypes as C
+import operator
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -21,6 +22,7 @@ from .regions import plan_regions
 from . import reassembly
 
 ACGT = "ACGT"
+_UPPER = [chr(b).upper() for b in range(256)]  # Scala's toChar.toUpper of a reference byte
 IUPAC = {1: "A", 2: "C", 4: "G", 8: "T", 5: "R", 10: "Y", 6: "S", 9: "W", 12: "K", 3: "M", 14: "B", 13: "D",
          11: "H", 7: "V", 15: "N"}
 
@@ -62,10 +64,21 @@ def to_iupac(a, b):  # Bases.toIUPAC (S/Bases.scala:85-88)
     return IUPAC[(1 << ACGT.index(a)) | (1 << ACGT.index(b))]
 
 
+def _locus(f):
+    return f.locus
+
+
 def fix_fix_list(fixes):
     """GenomeRegion.fixFixList (S/GenomeRegion.scala:557-593): stable sort by
-    locus, then of two overlapping fixes keep the one with more bases."""
-    fx = sorted(fixes, key=lambda f: f.locus)
+    locus, then of two overlapping fixes keep the one with more bases.  After
+    the sort a fix overlaps the next one when the next starts at or before
+    its last replaced locus; a list without such a pair comes back as sorted."""
+    fx = sorted(fixes, key=_locus)
+    if len(fx) > 1:
+        loci = [f.locus for f in fx]
+        last = [f.locus + (len(f.was) - 1 if f.was else 0) for f in fx]
+        if not any(map(operator.le, loci[1:], last[:-1])):
+            return fx
     out = []
     k = 0
     while k < len(fx):
@@ -172,31 +185,31 @@ def _region_outputs(engine, r, region, ref, opts, params, changes, chars, dupes=
     excluded = None
     if opts.longread and opts.nanopore is not None and opts.longread_only:
         excluded = _exclude_motifs(orig, s, e, opts.nanopore)
-    for ch in changes:
-        loc = int(ch["locus"])
+    n = len(changes)
+    cols = [changes[k].tolist() for k in ("locus", "call", "indel_len", "ins_str")] if n else [[]] * 4
+    fix_snps, fix_indels, amb_fix = opts.fix_snps, opts.fix_indels, opts.fix_snps and not opts.longread
+    has_base = _abi.PG_CALL_HAS_BASE
+    snp, small = res.snp, res.small
+    for loc, f, ilen, ioff in zip(*cols):
         if excluded is not None and excluded[loc - s]:
             continue
-        f = int(ch["call"])
         k = (f >> 9) & 7
-        rb = chr(ref[loc - 1]).upper()
-        cb = ACGT[f & 3] if f & _abi.PG_CALL_HAS_BASE else "N"
-        alt = ACGT[(f >> 2) & 3]
         if k == _abi.PG_CHANGE_SNP:
-            if opts.fix_snps:
-                res.snp.append(Fix(loc, rb, cb))
+            if fix_snps:
+                snp.append(Fix(loc, _UPPER[orig[loc - s]], ACGT[f & 3] if f & has_base else "N"))
         elif k == _abi.PG_CHANGE_AMB:
-            if opts.fix_snps and not opts.longread:
+            if amb_fix:
+                cb = ACGT[f & 3] if f & has_base else "N"
                 if opts.iupac:
-                    res.small.append(Fix(loc, rb, to_iupac(cb, alt)))
+                    small.append(Fix(loc, _UPPER[orig[loc - s]], to_iupac(cb, ACGT[(f >> 2) & 3])))
                 else:
-                    res.snp.append(Fix(loc, rb, cb))
+                    snp.append(Fix(loc, _UPPER[orig[loc - s]], cb))
         elif k == _abi.PG_CHANGE_INS:
-            if opts.fix_indels:
-                off = int(ch["ins_str"])
-                res.small.append(Fix(loc, "", chars[off:off + int(ch["indel_len"])].decode()))
+            if fix_indels:
+                small.append(Fix(loc, "", chars[ioff:ioff + ilen].decode()))
         elif k == _abi.PG_CHANGE_DEL:
-            if opts.fix_indels:
-                res.small.append(Fix(loc, bytes(ref[loc - 1:loc - 1 + int(ch["indel_len"])]).decode(), ""))
+            if fix_indels:
+                small.append(Fix(loc, bytes(ref[loc - 1:loc - 1 + ilen]).decode(), ""))
     # the reference prepends to its lists: descending loci, then stable-sorted
     res.snp.reverse()
     res.small.reverse()
@@ -381,18 +394,21 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
     if opts.changes:
         with open(out_prefix + ".changes", "w") as cf:
             for c, rs in groups:
-                nn = new_name(names[c])
+                name, nn = names[c], new_name(names[c])
                 offset = 0
+                lines = []
                 for r in rs:
                     res = results[r]
                     delta = 0
                     for f in res.all_fixes():
-                        nl = f.locus + delta
-                        cf.write(region_string(names[c], f.locus, f.locus + len(f.was) - 1) + " " +
-                                 region_string(nn, nl + offset, nl + offset + len(f.patch) - 1) + " " +
-                                 (f.was or ".") + " " + (f.patch or ".") + "\n")
-                        delta += len(f.patch) - len(f.was)
+                        lw, lp = len(f.was), len(f.patch)
+                        nl = f.locus + delta + offset
+                        lines.append(f"{name}:{f.locus}{'' if lw < 2 else f'-{f.locus + lw - 1}'} "
+                                     f"{nn}:{nl}{'' if lp < 2 else f'-{nl + lp - 1}'} "
+                                     f"{f.was or '.'} {f.patch or '.'}\n")
+                        delta += lp - lw
                     offset += len(res.bases) - (res.stop - res.start + 1)
+                cf.write("".join(lines))
     if opts.fix_snps or opts.fix_indels or opts.fix_gaps or opts.fix_local:
         with open(out_prefix + ".fasta", "wb") as ff:
             for c, rs in groups:
