@@ -8,7 +8,9 @@ graph-replayed plan.  A step is one pg_pileup_regions call over all regions:
 BamFile.process + PileUpRegion.addRead, computePhysCov, BaseCall and pass 1.
 The line also carries the 5 Mb / 100x bacterial workload (--config 2) measured
 the same way under "bacterial_5mb", and "parity_full": every region of the
-full-size workload compared with the oracle (outside the timed region).
+full-size workload compared with the oracle (outside the timed region), and
+"polish_driver": the whole polishing run (--fix snps,indels, FASTA and changes)
+on the workload, host wall clock.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--config 3] [--impl reference]
 
@@ -341,6 +343,49 @@ def fix_all_bench(eng, ds, params, K=31):
                 out["reassembly"] = opts.stats
         out["changes_lines"] = sum(1 for _ in open(os.path.join(d, "all.changes")))
     return out
+
+
+def polish_bench(eng, ds, params, reps=2):
+    """The whole polishing driver on the workload, --fix snps,indels with the
+    FASTA and changes written (no VCF): reference and read store upload,
+    pg_pileup_regions, the change list, the fix lists, fixIssues and the
+    writers, as Pilon's processRegions runs them.  Host wall clock; the
+    engine calls' share timed inside it."""
+    import tempfile
+    from pilon_gb300.polish import Options, polish
+    calls = {}
+
+    class Timed:  # the engine, with the time of each call polish() makes summed by name
+        def __init__(self, inner):
+            self._inner = inner
+
+        def __getattr__(self, name):
+            f = getattr(self._inner, name)
+            if not callable(f):
+                return f
+
+            def g(*a, **k):
+                t = time.perf_counter()
+                try:
+                    return f(*a, **k)
+                finally:
+                    calls[name] = calls.get(name, 0.0) + time.perf_counter() - t
+            return g
+
+    runs = []
+    with tempfile.TemporaryDirectory() as d:
+        for _ in range(reps):
+            calls.clear()
+            t0 = time.perf_counter()
+            polish(Timed(eng), ds.names, ds.contigs, ds.reads, params, os.path.join(d, "o"), Options(vcf=False))
+            runs.append((time.perf_counter() - t0, dict(calls)))
+        lines = sum(1 for _ in open(os.path.join(d, "o.changes")))
+        fasta = os.path.getsize(os.path.join(d, "o.fasta"))
+    best, engine_calls = min(runs, key=lambda x: x[0])
+    return {"seconds": best, "runs_s": [r[0] for r in runs], "engine_calls_s": engine_calls,
+            "changes_lines": lines, "fasta_bytes": fasta, "fix": "snps,indels", "outputs": "FASTA, changes",
+            "timing": "host wall clock of polish(), the best of the runs; engine_calls_s sums the engine calls "
+                      "it makes (uploads, pileup, change list, region statistics)"}
 
 
 def extra_workload(config, args, params, device, peak, peaks):
@@ -759,6 +804,7 @@ def main():
                            "compared": "every pileup counter, call flag, score, indel length and string and "
                                        "region statistic of every region, bit for bit",
                            "seconds": time.perf_counter() - t0})
+    driver = polish_bench(eng, ds, params) if args.config in (1, 2, 3) and rank == 0 else None
     extra = None
     xc = args.extra_config if args.extra_config >= 0 else (2 if args.config == 3 else 0)
     if xc and xc != args.config and rank == 0:
@@ -795,6 +841,8 @@ def main():
         line["bam_decode"] = bam_decode
     if kmer:
         line["kmer_tally"] = kmer
+    if driver:
+        line["polish_driver"] = driver
     print(json.dumps(line))
 
 
