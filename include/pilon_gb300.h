@@ -328,6 +328,10 @@ typedef struct pg_reassembly {
   int32_t break_radius;      /* GapFiller.breakRadius (S/GapFiller.scala:357-362) */
   int32_t fix_breaks;        /* Pilon.fixBreaks (--fix breaks, --variant): an unjoined break gets
                                 the partial fill of a gap (S/GapFiller.scala:76) */
+  int32_t gap_margin;        /* Pilon.gapMargin (--gapmargin, default 100000): a closed gap whose
+                                length differs from the gap's by more is not taken (S/GapFiller.scala:69-73) */
+  int32_t min_gap;           /* Pilon.minGap (--mingap, default 10): the Ns a partial fill leaves at least
+                                (S/GapFiller.scala:92) */
   const char *bases;         /* the region's bases after its SNP fixes (region size bytes) */
   const char *orig;          /* the region's original bases (region size bytes) */
 } pg_reassembly;

@@ -42,7 +42,7 @@ def lib():
                                 C.c_char_p, C.c_char_p]
         L.or_polish_fix.restype = C.c_int
         L.or_polish_fix.argtypes = L.or_polish.argtypes + [C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
-                                                           C.c_void_p, C.c_int32]
+                                                           C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
         L.or_region_breaks.restype = C.c_int32
         L.or_region_breaks.argtypes = [C.POINTER(_abi.pg_reads), C.POINTER(_abi.pg_params), C.c_void_p, C.c_int64,
                                        C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_int32]
@@ -122,11 +122,12 @@ def contig_regions(contig_len, chunk_size=10_000_000):
 def polish(reads, params, names, contigs, out_prefix, chunk_size=10_000_000, fix_snps=True, fix_indels=True,
            iupac=False, diploid=False, vcf_qe=False, vcf_date="20260101", vcf_source="Pilon version [COMMIT] [DATE]",
            vcf_args="", vcf_ref="file:/genome.fasta", fix_gaps=False, fix_local=False, K=47, strays=True,
-           stats=None, fix_breaks=False, vcf=True):
+           stats=None, fix_breaks=False, vcf=True, gap_margin=100000, min_gap=10):
     """GenomeFile.processRegions with --fix snps,indels[,gaps,local] --vcf
     --changes; writes out_prefix.fasta / .vcf / .changes.  With gaps or local,
     K is --K and the stray mates come from reads.name_id (strays=False is
-    --nostrays), fix_breaks is the experimental "breaks" fix; stats (a dict)
+    --nostrays), fix_breaks is the experimental "breaks" fix, gap_margin and
+    min_gap are --gapmargin and --mingap; stats (a dict)
     receives 'tied_sets'; vcf=False writes no VCF."""
     L = lib()
     n = len(contigs)
@@ -149,7 +150,7 @@ def polish(reads, params, names, contigs, out_prefix, chunk_size=10_000_000, fix
     tied = C.c_int64(0)
     rc = L.or_polish_fix(*args, int(fix_gaps), int(fix_local), int(K),
                          names_arr.ctypes.data if names_arr is not None else None, C.byref(tied),
-                         int(fix_breaks))
+                         int(fix_breaks), int(gap_margin), int(min_gap))
     if stats is not None:
         stats["tied_sets"] = int(tied.value)
     return rc

@@ -1107,6 +1107,8 @@ struct Reassembly {
   int32_t K;
   bool strays;
   bool fixBreaks = false;  // --fix breaks (--variant): breaks get the partial fill of gaps
+  int32_t gapMargin = 100000;  // Pilon.gapMargin (--gapmargin)
+  int32_t minGap = 10;         // Pilon.minGap (--mingap)
   BamStats scanStats;      // the statistics of BamFile.scan
   std::unordered_map<int64_t, int64_t> stray1, stray2;  // strayMateMap readMap1 / readMap2 (:222-281)
   std::vector<int64_t> cb, ce;                           // each contig's read range
@@ -1431,7 +1433,7 @@ Fix reassemble(const GenomeRegion& g, const Reassembly& ra, const BamStats& st, 
   bool solutionOK = !(solution == noSolution) && loop.empty();
   if (solutionOK && isGap) {
     int64_t closedDiff = std::llabs((int64_t)solution.patch.size() - (int64_t)(be + 1 - bs));
-    if (closedDiff > 100000) solutionOK = false;  // Pilon.gapMargin
+    if (closedDiff > ra.gapMargin) solutionOK = false;  // Pilon.gapMargin
   }
   if (solutionOK) return solution;
   if (!(isGap || (ra.fixBreaks && loop.empty()))) return noSolution;
@@ -1446,8 +1448,9 @@ Fix reassemble(const GenomeRegion& g, const Reassembly& ra, const BamStats& st, 
     return fromLeft == regionLeft && fromRight == regionRight;
   };
   if ((newStart >= bs + 20 || newStop <= be - 20) && !partialMatchesReference()) {  // GapFiller.minExtend
-    int32_t newGapLength = isGap ? std::max(10, newStop - newStart) : 10;  // Pilon.minGap
-    std::string seq = fromLeft + std::string((size_t)newGapLength, 'N') + fromRight;
+    int32_t newGapLength = isGap ? std::max(ra.minGap, newStop - newStart) : ra.minGap;  // Pilon.minGap
+    // (1 to newGapLength) map {_ => "N"}: empty when newGapLength <= 0
+    std::string seq = fromLeft + std::string((size_t)std::max(newGapLength, 0), 'N') + fromRight;
     Fix s = trimPatch(g, start, seq, stop);
     return s.patch.empty() ? noSolution : s;
   }
@@ -1569,7 +1572,8 @@ static int polishImpl(const pg_reads* R, const pg_params* params, int32_t n_cont
                       int32_t fix_indels, int32_t iupac, int32_t diploid, int32_t vcf_qe, const char* fasta_path,
                       const char* vcf_path, const char* changes_path, const char* vcf_date, const char* vcf_source,
                       const char* vcf_args, const char* vcf_ref, int32_t fix_gaps, int32_t fix_local, int32_t K,
-                      const int64_t* name_id, int64_t* tied_sets, int32_t fix_breaks) {
+                      const int64_t* name_id, int64_t* tied_sets, int32_t fix_breaks, int32_t gap_margin,
+                      int32_t min_gap) {
   Params P = toParams(params);
   // a BAM of type "bam" is typed by autoBam during the scan, which this oracle does not restate
   if ((fix_gaps || fix_local) && P.bamType == PG_BAM_BAM) return PG_ERR_ARG;
@@ -1579,6 +1583,8 @@ static int polishImpl(const pg_reads* R, const pg_params* params, int32_t n_cont
     if (fix_gaps || fix_local) {
       ra.reset(new Reassembly(R, name_id, P, K, n_contigs));
       ra->fixBreaks = fix_breaks != 0;
+      ra->gapMargin = gap_margin;
+      ra->minGap = min_gap;
     }
     // region read ranges: reads are sorted by (ref_id, pos); take each contig's span
     std::vector<int64_t> cb(n_contigs, 0), ce(n_contigs, 0);
@@ -1711,13 +1717,14 @@ int or_polish(const pg_reads* R, const pg_params* params, int32_t n_contigs, con
               const char* vcf_args, const char* vcf_ref) {
   return polishImpl(R, params, n_contigs, names, lens, bases, chunk_size, fix_snps, fix_indels, iupac, diploid,
                     vcf_qe, fasta_path, vcf_path, changes_path, vcf_date, vcf_source, vcf_args, vcf_ref, 0, 0, 31,
-                    nullptr, nullptr, 0);
+                    nullptr, nullptr, 0, 100000, 10);
 }
 
 // The same with the fix types gaps and local as well (GapFiller fillGap /
 // fixBreak, S/GenomeRegion.scala:382-410): K is Assembler.K (--K), name_id the
 // read name of each read as an id (mates share one; NULL: no stray mates, as
-// --nostrays), fix_breaks the experimental "breaks" fix (--variant).
+// --nostrays), fix_breaks the experimental "breaks" fix (--variant),
+// gap_margin and min_gap Pilon's --gapmargin and --mingap.
 // *tied_sets receives the count of solution sets of more than four elements
 // whose first element had to be taken in an order the reference gets from its
 // HashSet (see reassemble).
@@ -1726,10 +1733,11 @@ int or_polish_fix(const pg_reads* R, const pg_params* params, int32_t n_contigs,
                   int32_t fix_indels, int32_t iupac, int32_t diploid, int32_t vcf_qe, const char* fasta_path,
                   const char* vcf_path, const char* changes_path, const char* vcf_date, const char* vcf_source,
                   const char* vcf_args, const char* vcf_ref, int32_t fix_gaps, int32_t fix_local, int32_t K,
-                  const int64_t* name_id, int64_t* tied_sets, int32_t fix_breaks) {
+                  const int64_t* name_id, int64_t* tied_sets, int32_t fix_breaks, int32_t gap_margin,
+                  int32_t min_gap) {
   return polishImpl(R, params, n_contigs, names, lens, bases, chunk_size, fix_snps, fix_indels, iupac, diploid,
                     vcf_qe, fasta_path, vcf_path, changes_path, vcf_date, vcf_source, vcf_args, vcf_ref, fix_gaps,
-                    fix_local, K, name_id, tied_sets, fix_breaks);
+                    fix_local, K, name_id, tied_sets, fix_breaks, gap_margin, min_gap);
 }
 
 // One --targets region end to end (S/GenomeFile.scala:215-250): processBam,

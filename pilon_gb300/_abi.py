@@ -132,7 +132,7 @@ class pg_reassembly(C.Structure):
     _fields_ = [
         ("window", C.c_int32), ("is_gap", C.c_int32), ("region_start", C.c_int32), ("region_stop", C.c_int32),
         ("break_start", C.c_int32), ("break_stop", C.c_int32), ("break_radius", C.c_int32),
-        ("fix_breaks", C.c_int32),
+        ("fix_breaks", C.c_int32), ("gap_margin", C.c_int32), ("min_gap", C.c_int32),
         ("bases", C.c_void_p), ("orig", C.c_void_p),
     ]
 

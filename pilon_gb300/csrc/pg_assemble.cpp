@@ -338,7 +338,7 @@ Solution reassemble(const Graph& G, const pg_reassembly& job, int32_t& loopLen) 
   bool ok = solution.start > 0 && loopLen == 0;
   if (ok && isGap) {
     const int64_t diff = (int64_t)solution.patch.size() - (int64_t)(be + 1 - bs);
-    if ((diff < 0 ? -diff : diff) > 100000) ok = false;  // Pilon.gapMargin
+    if ((diff < 0 ? -diff : diff) > job.gap_margin) ok = false;  // Pilon.gapMargin
   }
   if (ok) return solution;
   if (!(isGap || (job.fix_breaks && loopLen == 0))) return none;
@@ -350,8 +350,9 @@ Solution reassemble(const Graph& G, const pg_reassembly& job, int32_t& loopLen) 
     matchesRef = cl == R.sub(job.bases, start, (int32_t)cl.size()) &&
                  cr == R.sub(job.bases, stop - (int32_t)cr.size(), (int32_t)cr.size());
   if ((newStart >= bs + 20 || newStop <= be - 20) && !matchesRef) {  // GapFiller.minExtend
-    const int32_t gapLen = isGap ? std::max(10, newStop - newStart) : 10;  // Pilon.minGap
-    Solution s = trimPatch(R, start, cl + std::string((size_t)gapLen, 'N') + cr, stop);
+    // Pilon.minGap; (1 to n) is empty for n <= 0
+    const int32_t gapLen = isGap ? std::max(job.min_gap, newStop - newStart) : job.min_gap;
+    Solution s = trimPatch(R, start, cl + std::string((size_t)std::max(gapLen, 0), 'N') + cr, stop);
     return s.patch.empty() ? none : s;
   }
   return none;

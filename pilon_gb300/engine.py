@@ -395,7 +395,8 @@ def reassemble(edges, K, jobs, threads=0):
                 raise ValueError("job bases must be contiguous uint8 arrays of the region's size")
         arr[k] = _abi.pg_reassembly(j["window"], int(j["is_gap"]), j["region_start"], j["region_stop"],
                                     j["break_start"], j["break_stop"], j["break_radius"],
-                                    int(j.get("fix_breaks", 0)), b.ctypes.data, o.ctypes.data)
+                                    int(j.get("fix_breaks", 0)), int(j.get("gap_margin", 100000)),
+                                    int(j.get("min_gap", 10)), b.ctypes.data, o.ctypes.data)
     fixes = (_abi.pg_reassembly_fix * max(1, n))()
     edges = np.ascontiguousarray(edges)
     cap = 1 << 16

@@ -37,6 +37,8 @@ class Options:
     fix_breaks: bool = False        # experimental "breaks" (--variant): unjoined breaks are opened
     K: int = 47                     # --K, Assembler.K
     strays: bool = True             # --nostrays clears it
+    gap_margin: int = 100000        # --gapmargin: a closed gap may differ from the gap's length by this much
+    min_gap: int = 10               # --mingap: the Ns a partial gap fill leaves at least
     iupac: bool = False
     diploid: bool = False
     vcf: bool = True
@@ -262,7 +264,7 @@ def _reassemble(engine, regions, results, contigs, reads, params, opts):
             lists.append(bam.recruit(c, bs, be))
             jobs.append(dict(window=len(lists) - 1, is_gap=is_gap, region_start=s, region_stop=e, break_start=bs,
                              break_stop=be, break_radius=radius, bases=bases, orig=orig,
-                             fix_breaks=opts.fix_breaks))
+                             fix_breaks=opts.fix_breaks, gap_margin=opts.gap_margin, min_gap=opts.min_gap))
             owner.append(r)
     t2 = time.perf_counter()
     if not jobs:

@@ -47,7 +47,7 @@ def test_struct_layouts_match_header():
     assert C.sizeof(_abi.pg_serve_config) == 48  # 4 + 4, the int64 budget at 8, then 7 int32 + padding
     assert C.sizeof(_abi.pg_result) == 96
     assert _abi.pg_result.latency_ms.offset == 80 and _abi.pg_serve_config.hbm_budget.offset == 8
-    assert C.sizeof(_abi.pg_reassembly) == 8 * 4 + 2 * 8 and _abi.pg_reassembly.bases.offset == 32
+    assert C.sizeof(_abi.pg_reassembly) == 10 * 4 + 2 * 8 and _abi.pg_reassembly.bases.offset == 40
     assert C.sizeof(_abi.pg_reassembly_fix) == 4 * 4 + 4 * 8 and _abi.pg_reassembly_fix.patch_off.offset == 32
 
 
@@ -184,7 +184,7 @@ def test_header_compiles_as_c99_and_links(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, (out.returncode, out.stderr)
     version, r, p, e, j, f = out.stdout.strip().split("|")
-    assert version.startswith("pilon_gb300") and (int(r), int(p), int(e), int(j), int(f)) == (32, 56, 32, 48, 48)
+    assert version.startswith("pilon_gb300") and (int(r), int(p), int(e), int(j), int(f)) == (32, 56, 32, 56, 48)
 
 
 C_NOMEM_CLIENT = r"""
@@ -205,7 +205,7 @@ int main(void) {
   memset(edges, 0, (size_t)n_edges * sizeof *edges);
   memset(bases, 'A', 100);
   memcpy(orig, bases, 100);
-  pg_reassembly job = {0, 0, 1, 100, 40, 60, 50, 0, bases, orig};
+  pg_reassembly job = {0, 0, 1, 100, 40, 60, 50, 0, 100000, 10, bases, orig};
   pg_reassembly_fix fix;
   int64_t text_len = -1;
   /* room for the call's own bookkeeping (about 20 MB), not for the graph */

@@ -171,7 +171,7 @@ def compare(ds, params=None, chunk=10_000_000, no_frags=False, vcf=False, **kw):
     opts = Options(chunk_size=chunk, vcf=vcf, **kw)
     opts.no_frags = no_frags  # long reads only: excludeMotifs applies
     fix = dict(fix_gaps=opts.fix_gaps, fix_local=opts.fix_local, K=opts.K, strays=opts.strays,
-               fix_breaks=opts.fix_breaks)
+               fix_breaks=opts.fix_breaks, gap_margin=opts.gap_margin, min_gap=opts.min_gap)
     with tempfile.TemporaryDirectory() as d:
         h, o = os.path.join(d, "host"), os.path.join(d, "ora")
         polish(OracleEngine(ds.names, chunk, **fix), ds.names, ds.contigs, ds.reads, params, h, opts)

@@ -125,6 +125,35 @@ def test_gaps_closed_and_opened(cfg4_small):
         assert truth in fasta
 
 
+def test_gap_margin_and_min_gap(cfg4_small):
+    """--gapmargin and --mingap (S/GapFiller.scala:69-73, 92): with a margin
+    of -1 even the closed 60 bp gap (closed length 60, gap 60, difference 0)
+    is refused and falls to the partial fill, and a minimum of 2,000 Ns
+    widens the opened 3 kb gap's Ns to at least 2,000; both against the
+    oracle with the same options."""
+    import copy
+    d = copy.copy(cfg4_small)
+    ref = d.contigs[0].copy()
+    ref[200_000:200_060] = ord("N")
+    ref[500_000:503_000] = ord("N")
+    d.contigs = [ref]
+    r = d.reads
+    d.reads = r.subset(np.nonzero((r.aend < 501_000) | (r.pos > 502_000))[0])
+
+    def patches(out, first):
+        return [l.split()[3] for l in out["changes"].decode().splitlines() if l.split()[0].startswith(first)]
+
+    _, base = compare(d, fix_gaps=True, K=31)
+    _, wide = compare(d, fix_gaps=True, K=31, min_gap=2000)
+    _, tight = compare(d, fix_gaps=True, K=31, gap_margin=-1)
+    assert patches(base, "chr1:200001-200060") and "N" not in patches(base, "chr1:200001-200060")[0]
+    assert all("N" in p for p in patches(tight, "chr1:200001-200060"))
+    opened_base = [p for p in patches(base, "chr1:5000") if "N" in p]
+    opened_wide = [p for p in patches(wide, "chr1:5000") if "N" in p]
+    assert len(opened_base) == 1 and len(opened_wide) == 1
+    assert opened_base[0].count("N") < 2000 <= opened_wide[0].count("N")
+
+
 def test_scan_statistics_and_strays(cfg4_small):
     """BamFile.scan over the store: the insert statistics and the stray-mate
     maps (one read per name and mate end) the recruitment looks mates up in."""
