@@ -791,8 +791,8 @@ def main():
                           f"the whole workload split into {njobs} regions") + f" on {threads} host threads, one pass",
                "same_units_as_gpu": same}
         if not args.no_parity:
-            # every region of the full-size workload against the oracle (the
-            # checker), outside the timed region
+            # every region of the full-size workload against the oracle,
+            # outside the timed region
             from oracle.parity import full_parity
             t0 = time.perf_counter()
             try:

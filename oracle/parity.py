@@ -1,6 +1,6 @@
 """Region-by-region comparison of the engine's results with the oracle's.
 
-TEST INFRASTRUCTURE ONLY (the checker): used by tests/ and by bench.py's CPU
+TEST INFRASTRUCTURE ONLY: used by tests/ and by bench.py's CPU
 baseline leg, never by the pilon_gb300 product path.  Every pileup counter,
 call flag, score, indel length and string and region statistic must be equal
 bit for bit.
