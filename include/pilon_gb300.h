@@ -282,6 +282,53 @@ typedef struct pg_change {
 pg_status pg_fetch_changes(pg_ctx *ctx, pg_change *out, int64_t cap, int64_t *n_changes, char *ins_chars,
                            int64_t ins_cap, int64_t *n_ins_chars);
 
+/* ---- fix lists and the changes file (host only: no context or device) ----
+ * One Fix of GenomeRegion (locus, was, patch): its strings are text[was_off ..
+ * was_off + was_len) and text[patch_off .. patch_off + patch_len). */
+typedef struct pg_fix {
+  int32_t locus;             /* first replaced locus (1-based) */
+  int32_t list;              /* 0: snpFixList, 1: smallFixList, 2: bigFixList */
+  int64_t was_off, was_len;
+  int64_t patch_off, patch_len;
+} pg_fix;
+
+/* The --fix switches that decide which changes become fixes. */
+typedef struct pg_fix_options {
+  int32_t fix_snps;          /* --fix snps (AMB changes too, as bases or with iupac as codes) */
+  int32_t fix_indels;        /* --fix indels */
+  int32_t iupac;             /* --iupac: an AMB change is fixed as its IUPAC code, in the small list */
+  int32_t long_read;         /* long-read only: AMB changes are not fixed */
+} pg_fix_options;
+
+/* The fix lists of one region from its changes (the region's slice of
+ * pg_fetch_changes), as GenomeRegion.identifyAndFixIssues builds them
+ * (S/GenomeRegion.scala:307-380): SNP and AMB changes in snpFixList (AMB with
+ * --iupac in smallFixList as a code, Bases.toIUPAC), insertions and deletions
+ * in smallFixList, each list last change first, as the reference prepends;
+ * `excluded` (NULL or one byte per region position) drops the changes that
+ * excludeMotifs marks.  `contig` is the whole contig (a deletion may run past
+ * the region).  bases_snp (region size bytes) receives the region's bases
+ * after fixIssues(snpFixList) and bases (bases_cap bytes) those after
+ * fixIssues(smallFixList) on top (S/GenomeRegion.scala:557-621).  The fixes,
+ * snp list first, go to fixes with their strings in text.  *n_fixes,
+ * *text_len and *bases_len receive the full sizes; PG_ERR_LIMIT when one of
+ * them does not fit (nothing is copied then).  Reference bytes are ASCII. */
+pg_status pg_region_fixes(const pg_change *changes, int64_t n_changes, const char *ins_chars, int64_t n_ins_chars,
+                          const uint8_t *contig, int64_t contig_len, int32_t start, int32_t stop,
+                          const pg_fix_options *opts, const uint8_t *excluded, pg_fix *fixes, int64_t fix_cap,
+                          int64_t *n_fixes, char *text, int64_t text_cap, int64_t *text_len, uint8_t *bases_snp,
+                          uint8_t *bases, int64_t bases_cap, int64_t *bases_len);
+
+/* The changes file's lines of one region (S/GenomeRegion.scala:645-657):
+ * fixFixList over the fixes in the order given (snpFixList ++ smallFixList ++
+ * bigFixList), then per fix "name:from[-to] new_name:from[-to] was patch"
+ * with "." for an empty string, the new loci shifted by `offset` (the length
+ * change of the contig's earlier regions) and by the fixes before it.
+ * *out_len receives the full size; PG_ERR_LIMIT when it exceeds cap. */
+pg_status pg_changes_lines(const pg_fix *fixes, int64_t n_fixes, const char *text, int64_t text_len,
+                           const char *name, const char *new_name, int64_t offset, char *out, int64_t cap,
+                           int64_t *out_len);
+
 /* Launch shape of the pileup walk kernel: tile width (positions per CTA,
  * a power of two in [256, 4096]), warps per CTA (1..16) and variant (lanes
  * per read: 0 = 32, 1 = 16, 2 = 8, 3 = 4); 0 / -1 keep the current value.  The host

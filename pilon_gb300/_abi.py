@@ -162,6 +162,17 @@ def change_dtype():
                      ("pad_", "<i4")])
 
 
+# numpy dtype of pg_fix
+def fix_dtype():
+    import numpy as np
+    return np.dtype([("locus", "<i4"), ("list", "<i4"), ("was_off", "<i8"), ("was_len", "<i8"),
+                     ("patch_off", "<i8"), ("patch_len", "<i8")])
+
+
+class pg_fix_options(C.Structure):
+    _fields_ = [("fix_snps", C.c_int32), ("fix_indels", C.c_int32), ("iupac", C.c_int32), ("long_read", C.c_int32)]
+
+
 # numpy dtype of pg_kmer_edge_wide (K <= 63)
 def kmer_edge_wide_dtype():
     import numpy as np
@@ -191,7 +202,7 @@ EXPORTED = [
     "pg_find_duplications", "pg_kmer_tally_wide", "pg_kmer_tally_breaks_wide", "pg_fetch_changes",
     "pg_default_serve_config", "pg_serve_open", "pg_serve_submit", "pg_serve_poll", "pg_serve_release",
     "pg_serve_stats", "pg_serve_error", "pg_serve_close", "pg_kmer_tally_reads", "pg_reassemble",
-    "pg_mark_deleted", "pg_set_reads_packed",
+    "pg_mark_deleted", "pg_set_reads_packed", "pg_region_fixes", "pg_changes_lines",
 ]
 
 PG_STATIC_SCAN_MAX_POSITIONS = 16777216

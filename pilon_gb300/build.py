@@ -23,7 +23,7 @@ BAMLIB = os.path.join(BUILD, "libpg_bam.so")
 
 CU_SOURCES = ["pg_api.cu", "pg_pileup.cu", "pg_call.cu", "pg_kmer.cu", "pg_format.cu", "pg_noalloc.cu",
               "pg_breaks.cu", "pg_serve.cu"]
-CPP_SOURCES = ["pg_assemble.cpp"]
+CPP_SOURCES = ["pg_assemble.cpp", "pg_fixes.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-fwrapv", "--expt-relaxed-constexpr"]
 

@@ -76,6 +76,11 @@ def lib():
             "pg_kmer_tally_reads": (C.c_int, [vp, vp, i64, vp, i32, i32, C.POINTER(_abi.pg_params), i32, vp, i64,
                                               C.POINTER(C.c_int64)]),
             "pg_reassemble": (C.c_int, [vp, i64, i32, vp, i32, i32, vp, vp, i64, C.POINTER(C.c_int64)]),
+            "pg_region_fixes": (C.c_int, [vp, i64, vp, i64, vp, i64, i32, i32, C.POINTER(_abi.pg_fix_options), vp,
+                                          vp, i64, C.POINTER(C.c_int64), vp, i64, C.POINTER(C.c_int64), vp, vp,
+                                          i64, C.POINTER(C.c_int64)]),
+            "pg_changes_lines": (C.c_int, [vp, i64, vp, i64, C.c_char_p, C.c_char_p, i64, vp, i64,
+                                           C.POINTER(C.c_int64)]),
             "pg_mark_deleted": (C.c_int, [vp, i32, i32, i32]),
         }
         for name, (res, args) in sig.items():
@@ -376,6 +381,59 @@ class Engine:
         n = C.c_int32()
         self._check(self.L.pg_graph_replays(self.h, C.byref(n)))
         return n.value
+
+
+def region_fixes(changes, chars, contig, start, stop, fix_snps=True, fix_indels=True, iupac=False,
+                 long_read=False, excluded=None):
+    """pg_region_fixes on the host: one region's pg_change records (a slice of
+    fetch_changes) and the insertion characters -> (fixes as a pg_fix array,
+    snp list then small list, each last change first; their strings; the bases
+    after the SNP fixes; the bases after the small fixes too)."""
+    L = lib()
+    ch = np.ascontiguousarray(changes, _abi.change_dtype())
+    ins = np.frombuffer(chars, np.uint8) if len(chars) else np.zeros(1, np.uint8)
+    contig = np.ascontiguousarray(contig, np.uint8)
+    ex = None if excluded is None else np.ascontiguousarray(excluded, np.uint8)
+    opts = _abi.pg_fix_options(int(fix_snps), int(fix_indels), int(iupac), int(long_read))
+    size = stop - start + 1
+    nf, tl, bl = C.c_int64(), C.c_int64(), C.c_int64()
+    fcap, tcap, bcap = max(1, ch.size), max(16, 4 * ch.size), size + 64
+    while True:
+        fixes = np.zeros(fcap, _abi.fix_dtype())
+        text = np.zeros(tcap, np.uint8)
+        snp = np.zeros(size, np.uint8)
+        out = np.zeros(bcap, np.uint8)
+        st = L.pg_region_fixes(ch.ctypes.data if ch.size else None, ch.size, ins.ctypes.data, len(chars),
+                               contig.ctypes.data, contig.size, start, stop, C.byref(opts),
+                               ex.ctypes.data if ex is not None else None, fixes.ctypes.data, fcap, C.byref(nf),
+                               text.ctypes.data, tcap, C.byref(tl), snp.ctypes.data, out.ctypes.data, bcap,
+                               C.byref(bl))
+        if st == _abi.PG_ERR_LIMIT and (nf.value > fcap or tl.value > tcap or bl.value > bcap):
+            fcap, tcap, bcap = max(fcap, nf.value), max(tcap, tl.value), max(bcap, bl.value)
+            continue
+        if st:
+            raise EngineError(st, "pg_region_fixes: bad changes for the region")
+        return fixes[:nf.value], text[:tl.value].tobytes(), snp.tobytes(), out[:bl.value].tobytes()
+
+
+def changes_lines(fixes, text, name, new_name, offset):
+    """pg_changes_lines on the host: the changes file's lines of one region
+    from its fixes (pg_fix array, snp ++ small ++ big), as bytes."""
+    L = lib()
+    fx = np.ascontiguousarray(fixes, _abi.fix_dtype())
+    tb = np.frombuffer(text, np.uint8) if len(text) else np.zeros(1, np.uint8)
+    cap = max(256, 64 * fx.size)
+    n = C.c_int64()
+    while True:
+        out = np.zeros(cap, np.uint8)
+        st = L.pg_changes_lines(fx.ctypes.data if fx.size else None, fx.size, tb.ctypes.data, len(text),
+                                name.encode(), new_name.encode(), offset, out.ctypes.data, cap, C.byref(n))
+        if st == _abi.PG_ERR_LIMIT and n.value > cap:
+            cap = n.value
+            continue
+        if st:
+            raise EngineError(st, "pg_changes_lines: bad fixes")
+        return out[:n.value].tobytes()
 
 
 def reassemble(edges, K, jobs, threads=0):

@@ -13,18 +13,14 @@ outputs.
 """
 import ctypes as C
 import operator
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 
 from . import _abi
+from .engine import changes_lines, region_fixes
 from .regions import plan_regions
 from . import reassembly
-
-ACGT = "ACGT"
-_UPPER = [chr(b).upper() for b in range(256)]  # Scala's toChar.toUpper of a reference byte
-IUPAC = {1: "A", 2: "C", 4: "G", 8: "T", 5: "R", 10: "Y", 6: "S", 9: "W", 12: "K", 3: "M", 14: "B", 13: "D",
-         11: "H", 7: "V", 15: "N"}
 
 
 @dataclass
@@ -60,10 +56,6 @@ class Fix:
     locus: int
     was: str
     patch: str
-
-
-def to_iupac(a, b):  # Bases.toIUPAC (S/Bases.scala:85-88)
-    return IUPAC[(1 << ACGT.index(a)) | (1 << ACGT.index(b))]
 
 
 def _locus(f):
@@ -157,68 +149,72 @@ def region_string(name, s, e):  # Region.regionString (S/Region.scala:45)
     return f"{name}:{s}" + ("" if e + 1 - s < 2 else f"-{e}")
 
 
-@dataclass
 class RegionResult:
-    contig: int
-    start: int
-    stop: int
-    bases: bytearray
-    snp: list = field(default_factory=list)
-    small: list = field(default_factory=list)
-    big: list = field(default_factory=list)     # local reassemblies and gap fills
-    dupes: list = field(default_factory=list)
-    stats: object = None
-    bases_snp: bytearray = None                 # the bases after the SNP fixes alone
-    orig: bytes = None
+    """One region's outputs: the fix lists of GenomeRegion (snpFixList and
+    smallFixList from pass 1, bigFixList from local reassembly), its bases
+    before and after the fixes, its statistics and its <DUP> spans.  The snp
+    and small lists stay in pg_region_fixes' packed form (`fixes`, `text`)
+    and become Fix objects only where reassembly or the VCF asks for them."""
+
+    def __init__(self, contig, start, stop, bases, stats=None):
+        self.contig, self.start, self.stop, self.bases, self.stats = contig, start, stop, bases, stats
+        self.big = []           # local reassemblies and gap fills
+        self.dupes = []
+        self.bases_snp = None   # the bases after the SNP fixes alone
+        self.orig = None
+        self.fixes = np.zeros(0, _abi.fix_dtype())
+        self.text = b""
+        self._lists = None
+
+    def _decoded(self):
+        if self._lists is None:
+            snp, small, t = [], [], self.text
+            for locus, lst, wo, wl, po, pl in self.fixes.tolist():
+                (snp if lst == 0 else small).append(Fix(locus, t[wo:wo + wl].decode(), t[po:po + pl].decode()))
+            self._lists = (snp, small)
+        return self._lists
+
+    @property
+    def snp(self):
+        return self._decoded()[0]
+
+    @property
+    def small(self):
+        return self._decoded()[1]
 
     def all_fixes(self):
         return fix_fix_list(self.snp + self.small + self.big)
 
+    def packed_fixes(self):
+        """snpFixList ++ smallFixList ++ bigFixList as (pg_fix array, text)."""
+        if not self.big:
+            return self.fixes, self.text
+        text = bytearray(self.text)
+        big = np.zeros(len(self.big), _abi.fix_dtype())
+        for k, f in enumerate(self.big):
+            was, patch = f.was.encode(), f.patch.encode()
+            big[k] = (f.locus, 2, len(text), len(was), len(text) + len(was), len(patch))
+            text += was + patch
+        return np.concatenate([self.fixes, big]), bytes(text)
+
 
 def _region_outputs(engine, r, region, ref, opts, params, changes, chars, dupes=()):
     """The region's changes (pg_fetch_changes: pass-1 changes in locus order,
-    insertion characters) -> fix lists and fixed bases; its duplication events
-    (pg_find_duplications) -> where its <DUP> records go."""
+    insertion characters) -> fix lists and fixed bases (pg_region_fixes); its
+    duplication events (pg_find_duplications) -> where its <DUP> records go."""
     c, s, e, _, _ = region
-    size = e - s + 1
     st = engine.stats(r)
     orig = bytes(ref[s - 1:e])
-    res = RegionResult(c, s, e, bytearray(orig), stats=st)
     excluded = None
     if opts.longread and opts.nanopore is not None and opts.longread_only:
         excluded = _exclude_motifs(orig, s, e, opts.nanopore)
-    n = len(changes)
-    cols = [changes[k].tolist() for k in ("locus", "call", "indel_len", "ins_str")] if n else [[]] * 4
-    fix_snps, fix_indels, amb_fix = opts.fix_snps, opts.fix_indels, opts.fix_snps and not opts.longread
-    has_base = _abi.PG_CALL_HAS_BASE
-    snp, small = res.snp, res.small
-    for loc, f, ilen, ioff in zip(*cols):
-        if excluded is not None and excluded[loc - s]:
-            continue
-        k = (f >> 9) & 7
-        if k == _abi.PG_CHANGE_SNP:
-            if fix_snps:
-                snp.append(Fix(loc, _UPPER[orig[loc - s]], ACGT[f & 3] if f & has_base else "N"))
-        elif k == _abi.PG_CHANGE_AMB:
-            if amb_fix:
-                cb = ACGT[f & 3] if f & has_base else "N"
-                if opts.iupac:
-                    small.append(Fix(loc, _UPPER[orig[loc - s]], to_iupac(cb, ACGT[(f >> 2) & 3])))
-                else:
-                    snp.append(Fix(loc, _UPPER[orig[loc - s]], cb))
-        elif k == _abi.PG_CHANGE_INS:
-            if fix_indels:
-                small.append(Fix(loc, "", chars[ioff:ioff + ilen].decode()))
-        elif k == _abi.PG_CHANGE_DEL:
-            if fix_indels:
-                small.append(Fix(loc, bytes(ref[loc - 1:loc - 1 + ilen]).decode(), ""))
-    # the reference prepends to its lists: descending loci, then stable-sorted
-    res.snp.reverse()
-    res.small.reverse()
+    fixes, text, bases_snp, bases = region_fixes(changes, chars, ref, s, e, fix_snps=opts.fix_snps,
+                                                 fix_indels=opts.fix_indels, iupac=opts.iupac,
+                                                 long_read=bool(opts.longread), excluded=excluded)
+    res = RegionResult(c, s, e, bytearray(bases), stats=st)
+    res.fixes, res.text = fixes, text
+    res.bases_snp = bytearray(bases_snp)
     res.orig = orig
-    res.bases = fix_issues(res.bases, s, res.snp)
-    res.bases_snp = res.bases
-    res.bases = fix_issues(res.bases, s, res.small)
     res.dupes = list(dupes)
     return res
 
@@ -394,23 +390,15 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
                     text = _splice(text, _first_lines(engine, r, res.stop - res.start + 1), inserts, res.start)
                 vf.write(text)
     if opts.changes:
-        with open(out_prefix + ".changes", "w") as cf:
+        with open(out_prefix + ".changes", "wb") as cf:
             for c, rs in groups:
                 name, nn = names[c], new_name(names[c])
                 offset = 0
-                lines = []
                 for r in rs:
                     res = results[r]
-                    delta = 0
-                    for f in res.all_fixes():
-                        lw, lp = len(f.was), len(f.patch)
-                        nl = f.locus + delta + offset
-                        lines.append(f"{name}:{f.locus}{'' if lw < 2 else f'-{f.locus + lw - 1}'} "
-                                     f"{nn}:{nl}{'' if lp < 2 else f'-{nl + lp - 1}'} "
-                                     f"{f.was or '.'} {f.patch or '.'}\n")
-                        delta += lp - lw
+                    fixes, text = res.packed_fixes()
+                    cf.write(changes_lines(fixes, text, name, nn, offset))
                     offset += len(res.bases) - (res.stop - res.start + 1)
-                cf.write("".join(lines))
     if opts.fix_snps or opts.fix_indels or opts.fix_gaps or opts.fix_local:
         with open(out_prefix + ".fasta", "wb") as ff:
             for c, rs in groups:
