@@ -43,7 +43,7 @@ class InsertStats:
         s = np.asarray(sizes, np.int64)
         self.count += int(s.size)
         self.sum += int(s.sum())
-        self.sumsq += int(_wrap32(s * s).sum())  # size * size is a Scala Int
+        self.sumsq += int((s * s).astype(np.int32).sum(dtype=np.int64))  # size * size is a Scala Int: wraps
 
     def add(self, count, total, sumsq):
         self.count += int(count)
@@ -91,14 +91,18 @@ class BamState:
         self.huge = 5 * MAX_INSERT_DEFAULT[self.bam_type]
         self.fr, self.rf, self.un = InsertStats(), InsertStats(), InsertStats()
         self.strays = bool(strays) and reads.name_id is not None
-        flag = reads.flag.astype(np.int64)
-        ok = validate(flag, params) & ((flag & 0x4) == 0)
+        flag = reads.flag  # uint16: the bit tests need no wider copy
+        self.valid = validate(flag, params)
+        unmapped = (flag & 0x4) != 0
+        ok = self.valid & ~unmapped
         paired = (flag & 0x1) != 0
         proper = (flag & 0x2) != 0
         rc = (flag & 0x10) != 0
         # proper pairs: addInsert(getInferredInsertSize, rc); unpaired: addInsert(getReadLength, rc, true)
-        self._add_inserts(reads.tlen[ok & paired & proper].astype(np.int64), rc[ok & paired & proper], False)
-        self._add_inserts(reads.l_seq[ok & ~paired].astype(np.int64), rc[ok & ~paired], True)
+        pp = ok & paired & proper
+        up = ok & ~paired
+        self._add_inserts(reads.tlen[pp], rc[pp], False)
+        self._add_inserts(reads.l_seq[up], rc[up], True)
         # stray mates: paired, not proper, mate mapped, on a reference of interest (every one here)
         self._stray = [(np.zeros(0, np.int64), np.zeros(0, np.int64))] * 2
         if self.strays:
@@ -113,17 +117,17 @@ class BamState:
         rid = reads.ref_id
         unplaced = np.nonzero(rid < 0)[0]  # the unplaced reads close a coordinate-sorted store
         placed = rid[:int(unplaced[0])] if unplaced.size else rid
-        self.cb = np.searchsorted(placed, np.arange(n_contigs), side="left").astype(np.int64)
-        self.ce = np.searchsorted(placed, np.arange(n_contigs), side="right").astype(np.int64)
+        ids = np.arange(n_contigs, dtype=placed.dtype)  # keys of the ids' own type: no widened copy
+        self.cb = np.searchsorted(placed, ids, side="left").astype(np.int64)
+        self.ce = np.searchsorted(placed, ids, side="right").astype(np.int64)
         self.pos = reads.pos.astype(np.int64)  # searched with int64 bounds without a cast per search
-        self.end = np.where((flag & 0x4) != 0, reads.pos, reads.aend).astype(np.int64)
-        span = self.end - reads.pos.astype(np.int64) + 1
+        self.end = np.where(unmapped, reads.pos, reads.aend).astype(np.int64)
+        span = self.end - self.pos + 1
         self.span = np.array([int(span[a:b].max()) if b > a else 1 for a, b in zip(self.cb, self.ce)], np.int64)
-        self.valid = validate(flag, params)
 
     def _add_inserts(self, size, rc, unpaired):  # BamFile.addInsert (S/BamFile.scala:194-202)
         keep = (size > 0) & (size < self.huge)
-        size, rc = size[keep], rc[keep]
+        size, rc = size[keep].astype(np.int64), rc[keep]
         if unpaired:
             self.un.add_sizes(size)
         else:
