@@ -58,23 +58,26 @@ class ReadIndex:
         # A coordinate-sorted BAM ends with its unplaced reads (reference -1),
         # which no region query returns; the placed reads before them are
         # sorted by reference.
-        placed = np.nonzero(rid >= 0)[0]
-        m = int(placed[-1]) + 1 if placed.size else 0
+        # one past the last placed read (found from the end, without listing every placed read)
+        tail_placed = rid[::-1] >= 0
+        m = rid.size - int(np.argmax(tail_placed)) if rid.size and bool(tail_placed.any()) else 0
         head = rid[:m]
         if m and (int(head.min()) < 0 or bool(np.any(head[1:] < head[:-1]))):
             raise ValueError("reads are not coordinate-sorted: unplaced reads (reference -1) must come last")
-        self.contig_lo = np.searchsorted(head, np.arange(n_contigs), side="left")
-        self.contig_hi = np.searchsorted(head, np.arange(n_contigs), side="right")
-        span = (reads.aend[:m].astype(np.int64) - reads.pos[:m].astype(np.int64) + 1)
-        self.max_span = int(span.max()) if span.size else 0
+        # search keys in the arrays' own types: an int64 key would widen the whole array per search
+        ids = np.arange(n_contigs, dtype=head.dtype)
+        self.contig_lo = np.searchsorted(head, ids, side="left")
+        self.contig_hi = np.searchsorted(head, ids, side="right")
+        self.max_span = int((reads.aend[:m] - reads.pos[:m]).max()) + 1 if m else 0
 
     def range_for(self, contig, start, stop, contig_len, slop=SLOP):
         lo, hi = int(self.contig_lo[contig]), int(self.contig_hi[contig])
         qs = max(start - slop, 0)
         qe = min(stop + slop, contig_len)
         pos = self.reads.pos[lo:hi]
-        a = lo + int(np.searchsorted(pos, qs - self.max_span, side="left"))
-        b = lo + int(np.searchsorted(pos, qe, side="right"))
+        key = pos.dtype.type
+        a = lo + int(np.searchsorted(pos, key(max(qs - self.max_span, np.iinfo(pos.dtype).min)), side="left"))
+        b = lo + int(np.searchsorted(pos, key(min(qe, np.iinfo(pos.dtype).max)), side="right"))
         return a, b
 
 
