@@ -365,7 +365,7 @@ def polish(engine, names, contigs, reads, params, out_prefix, opts=None, batched
     dups = engine.find_duplications() if opts.vcf else {}
     # the pass-1 changes of all regions at once, ordered by region and locus
     changes, chars = engine.fetch_changes()
-    bounds = np.searchsorted(changes["region"], np.arange(len(regions) + 1))
+    bounds = np.searchsorted(changes["region"], np.arange(len(regions) + 1, dtype=changes["region"].dtype))
     results = [_region_outputs(engine, r, reg, contigs[reg[0]], opts, params, changes[bounds[r]:bounds[r + 1]],
                                chars, dups.get(r, ())) for r, reg in enumerate(regions)]
     if opts.fix_gaps or opts.fix_local:
