@@ -804,7 +804,12 @@ def main():
                            "compared": "every pileup counter, call flag, score, indel length and string and "
                                        "region statistic of every region, bit for bit",
                            "seconds": time.perf_counter() - t0})
-    driver = polish_bench(eng, ds, params) if args.config in (1, 2, 3) and rank == 0 else None
+    driver = None
+    if args.config in (1, 2, 3) and rank == 0:
+        try:  # a failure of the host driver is reported in the line, not fatal to it
+            driver = polish_bench(eng, ds, params)
+        except Exception as ex:  # noqa: BLE001
+            driver = {"error": f"{type(ex).__name__}: {ex}"[:300]}
     extra = None
     xc = args.extra_config if args.extra_config >= 0 else (2 if args.config == 3 else 0)
     if xc and xc != args.config and rank == 0:
