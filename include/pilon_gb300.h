@@ -383,6 +383,21 @@ typedef struct pg_reassembly {
   const char *orig;          /* the region's original bases (region size bytes) */
 } pg_reassembly;
 
+/* BamFile.scan's pass over a read store (S/BamFile.scala:295-337) on host
+ * threads (0 = all cores), for local reassembly; no context or device.  Of
+ * the reads that pass validateRead and are mapped, addInsert (:194-202) adds
+ * a proper pair's inferred insert size, or an unpaired read's length, when it
+ * lies in (0, huge): stats receives count, sum and sum of squares (each square
+ * a wrapping 32-bit Int) for FR, RF and unpaired, in that order (9 values).
+ * strays receives the indices, in store order, of the reads MateMap files as
+ * stray mates (paired, not proper, mate mapped, on a reference below
+ * n_contigs or with its mate on one): the first-of-pair reads, then the
+ * second-of-pair ones; *n_first and *n_second their counts.  PG_ERR_LIMIT when
+ * they exceed stray_cap (stats are filled all the same). */
+pg_status pg_scan_reads(const pg_reads *reads, const pg_params *params, int32_t n_contigs, int32_t huge,
+                        int32_t threads, int64_t *stats, int64_t *strays, int64_t stray_cap, int64_t *n_first,
+                        int64_t *n_second);
+
 /* The fix of one pg_reassembly, GenomeRegion.Fix (locus, was, patch). */
 typedef struct pg_reassembly_fix {
   int32_t start;             /* first locus of the fix; 0 when there is no solution */

@@ -202,7 +202,7 @@ EXPORTED = [
     "pg_find_duplications", "pg_kmer_tally_wide", "pg_kmer_tally_breaks_wide", "pg_fetch_changes",
     "pg_default_serve_config", "pg_serve_open", "pg_serve_submit", "pg_serve_poll", "pg_serve_release",
     "pg_serve_stats", "pg_serve_error", "pg_serve_close", "pg_kmer_tally_reads", "pg_reassemble",
-    "pg_mark_deleted", "pg_set_reads_packed", "pg_region_fixes", "pg_changes_lines",
+    "pg_mark_deleted", "pg_set_reads_packed", "pg_region_fixes", "pg_changes_lines", "pg_scan_reads",
 ]
 
 PG_STATIC_SCAN_MAX_POSITIONS = 16777216

@@ -362,6 +362,77 @@ Solution reassemble(const Graph& G, const pg_reassembly& job, int32_t& loopLen) 
 
 extern "C" {
 
+pg_status pg_scan_reads(const pg_reads* reads, const pg_params* params, int32_t n_contigs, int32_t huge,
+                        int32_t threads, int64_t* stats, int64_t* strays, int64_t stray_cap, int64_t* n_first,
+                        int64_t* n_second) try {
+  if (!reads || !params || !stats || !n_first || !n_second || reads->n_reads < 0 || n_contigs < 0 ||
+      stray_cap < 0 || (stray_cap > 0 && !strays) ||
+      (reads->n_reads > 0 && (!reads->flag || !reads->tlen || !reads->l_seq || !reads->ref_id ||
+                              !reads->mate_ref_id)))
+    return PG_ERR_ARG;
+  const int64_t n = reads->n_reads;
+  const int32_t nt = (int32_t)std::max<int64_t>(1, std::min<int64_t>(
+      threads > 0 ? threads : (int32_t)std::thread::hardware_concurrency(), std::max<int64_t>(1, n >> 16)));
+  struct Part {
+    int64_t st[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // fr, rf, unpaired: count, sum, sumSq
+    std::vector<int64_t> first, second;
+  };
+  std::vector<Part> part((size_t)nt);
+  auto work = [&](int32_t t) {
+    Part& p = part[(size_t)t];
+    const int64_t lo = n * t / nt, hi = n * (t + 1) / nt;
+    for (int64_t i = lo; i < hi; i++) {
+      const uint32_t f = reads->flag[i];
+      // validateRead (S/BamFile.scala:101-105), and mapped
+      if ((f & 0x100) || (!params->nonpf && (f & 0x200)) || (!params->duplicates && (f & 0x400)) || (f & 0x4))
+        continue;
+      const bool paired = f & 0x1, proper = f & 0x2, rc = f & 0x10;
+      int64_t size = -1;
+      bool unpaired = false;
+      if (paired && proper) size = reads->tlen[i];        // addInsert(getInferredInsertSize, reverse)
+      else if (!paired) size = reads->l_seq[i], unpaired = true;  // addInsert(getReadLength, reverse, true)
+      if (size > 0 && size < huge) {  // addInsert (:194-202); a kept size is positive, so FR is !reverse
+        const int k = unpaired ? 6 : (rc ? 3 : 0);
+        p.st[k] += 1;
+        p.st[k + 1] += size;
+        p.st[k + 2] += (int32_t)(uint32_t)(uint64_t)(size * size);  // size * size is a Scala Int
+      }
+      // strayMateMap candidates: paired, not proper, mate mapped, on a reference of interest
+      if (paired && !proper && !(f & 0x8)) {
+        const int32_t rid = reads->ref_id[i], mrid = reads->mate_ref_id[i];
+        if ((rid >= 0 && rid < n_contigs) || (mrid >= 0 && mrid < n_contigs))
+          ((f & 0x40) ? p.first : p.second).push_back(i);
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  int32_t started = 1;
+  try {
+    pool.reserve((size_t)nt);
+    for (; started < nt; started++) pool.emplace_back(work, started);
+  } catch (const std::exception&) {
+  }
+  for (int32_t t = started; t < nt; t++) work(t);  // the shares of threads that did not start
+  work(0);
+  for (auto& th : pool) th.join();
+  for (int k = 0; k < 9; k++) stats[k] = 0;
+  int64_t nf = 0, ns = 0;
+  for (const Part& p : part) {
+    for (int k = 0; k < 9; k++) stats[k] += p.st[k];
+    nf += (int64_t)p.first.size();
+    ns += (int64_t)p.second.size();
+  }
+  *n_first = nf;
+  *n_second = ns;
+  if (nf + ns > stray_cap) return PG_ERR_LIMIT;
+  int64_t o = 0;
+  for (const Part& p : part)
+    for (int64_t i : p.first) strays[o++] = i;
+  for (const Part& p : part)
+    for (int64_t i : p.second) strays[o++] = i;
+  return PG_OK;
+} PG_HOST_CATCH(nullptr)
+
 pg_status pg_reassemble(const pg_kmer_edge_wide* edges, int64_t n_edges, int32_t K, const pg_reassembly* jobs,
                         int32_t n_jobs, int32_t threads, pg_reassembly_fix* fixes, char* text, int64_t text_cap,
                         int64_t* text_len) try {

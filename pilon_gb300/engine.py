@@ -81,6 +81,8 @@ def lib():
                                           i64, C.POINTER(C.c_int64)]),
             "pg_changes_lines": (C.c_int, [vp, i64, vp, i64, C.c_char_p, C.c_char_p, i64, vp, i64,
                                            C.POINTER(C.c_int64)]),
+            "pg_scan_reads": (C.c_int, [C.POINTER(_abi.pg_reads), C.POINTER(_abi.pg_params), i32, i32, i32, vp, vp,
+                                        i64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
             "pg_mark_deleted": (C.c_int, [vp, i32, i32, i32]),
         }
         for name, (res, args) in sig.items():
@@ -434,6 +436,29 @@ def changes_lines(fixes, text, name, new_name, offset):
         if st:
             raise EngineError(st, "pg_changes_lines: bad fixes")
         return out[:n.value].tobytes()
+
+
+def scan_reads(reads, params, n_contigs, huge, strays=True, threads=0):
+    """pg_scan_reads on the host: (the 9 insert statistics: FR, RF, unpaired
+    count, sum, sumSq; the first-of-pair stray-mate read indices; the
+    second-of-pair ones), the index arrays empty when strays is False."""
+    L = lib()
+    ab = reads.to_abi()
+    stats = np.zeros(9, np.int64)
+    nf, ns = C.c_int64(), C.c_int64()
+    cap = max(1024, reads.n_reads // 64) if strays else 0
+    while True:
+        out = np.zeros(max(cap, 1), np.int64)
+        st = L.pg_scan_reads(C.byref(ab), C.byref(params), n_contigs, huge, threads, stats.ctypes.data,
+                             out.ctypes.data, cap, C.byref(nf), C.byref(ns))
+        if st == _abi.PG_ERR_LIMIT and strays:
+            cap = nf.value + ns.value
+            continue
+        if st and not (st == _abi.PG_ERR_LIMIT and not strays):
+            raise EngineError(st, "pg_scan_reads: bad arguments")
+        if not strays:
+            return stats, np.zeros(0, np.int64), np.zeros(0, np.int64)
+        return stats, out[:nf.value].copy(), out[nf.value:nf.value + ns.value].copy()
 
 
 def reassemble(edges, K, jobs, threads=0):

@@ -14,6 +14,7 @@ recruitment is that of --nostrays.
 import numpy as np
 
 from . import _abi
+from .engine import scan_reads
 
 MAX_INSERT_DEFAULT = {_abi.PG_BAM_FRAGS: 500, _abi.PG_BAM_JUMPS: 10000, _abi.PG_BAM_UNPAIRED: 10000,
                       _abi.PG_BAM_BAM: 10000}  # BamFile.maxInsertSizes (S/BamFile.scala:29)
@@ -38,12 +39,6 @@ class InsertStats:
 
     def __init__(self, count=0, total=0, sumsq=0):
         self.count, self.sum, self.sumsq = int(count), int(total), int(sumsq)
-
-    def add_sizes(self, sizes):
-        s = np.asarray(sizes, np.int64)
-        self.count += int(s.size)
-        self.sum += int(s.sum())
-        self.sumsq += int((s * s).astype(np.int32).sum(dtype=np.int64))  # size * size is a Scala Int: wraps
 
     def add(self, count, total, sumsq):
         self.count += int(count)
@@ -94,24 +89,16 @@ class BamState:
         flag = reads.flag  # uint16: the bit tests need no wider copy
         self.valid = validate(flag, params)
         unmapped = (flag & 0x4) != 0
-        ok = self.valid & ~unmapped
-        paired = (flag & 0x1) != 0
-        proper = (flag & 0x2) != 0
-        rc = (flag & 0x10) != 0
-        # proper pairs: addInsert(getInferredInsertSize, rc); unpaired: addInsert(getReadLength, rc, true)
-        pp = ok & paired & proper
-        up = ok & ~paired
-        self._add_inserts(reads.tlen[pp], rc[pp], False)
-        self._add_inserts(reads.l_seq[up], rc[up], True)
-        # stray mates: paired, not proper, mate mapped, on a reference of interest (every one here)
+        # the insert statistics (proper pairs by inferred insert size, unpaired reads by length) and
+        # the stray-mate candidates (paired, not proper, mate mapped, on a reference of interest) of
+        # BamFile.scan: one pass on host threads (pg_scan_reads)
+        stats, first, second = scan_reads(reads, params, n_contigs, self.huge, strays=self.strays)
+        self.fr.add(*stats[0:3])
+        self.rf.add(*stats[3:6])
+        self.un.add(*stats[6:9])
         self._stray = [(np.zeros(0, np.int64), np.zeros(0, np.int64))] * 2
         if self.strays:
-            rid, mrid = reads.ref_id, reads.mate_ref_id
-            soi = ((rid >= 0) & (rid < n_contigs)) | ((mrid >= 0) & (mrid < n_contigs))
-            st = ok & paired & ~proper & ((flag & 0x8) == 0) & soi
-            idx = np.nonzero(st)[0]
-            first = (flag[idx] & 0x40) != 0
-            self._stray = [self._name_map(idx[first]), self._name_map(idx[~first])]
+            self._stray = [self._name_map(first), self._name_map(second)]
         # each contig's reads and the longest alignment span among them
         self.n_contigs = n_contigs
         rid = reads.ref_id
@@ -124,16 +111,6 @@ class BamState:
         self.end = np.where(unmapped, reads.pos, reads.aend).astype(np.int64)
         span = self.end - self.pos + 1
         self.span = np.array([int(span[a:b].max()) if b > a else 1 for a, b in zip(self.cb, self.ce)], np.int64)
-
-    def _add_inserts(self, size, rc, unpaired):  # BamFile.addInsert (S/BamFile.scala:194-202)
-        keep = (size > 0) & (size < self.huge)
-        size, rc = size[keep].astype(np.int64), rc[keep]
-        if unpaired:
-            self.un.add_sizes(size)
-        else:
-            fr = (size > 0) ^ rc
-            self.fr.add_sizes(size[fr])
-            self.rf.add_sizes(size[~fr])
 
     def _name_map(self, idx):
         """HashMap name -> read of MateMap.addRead, the last read of a name

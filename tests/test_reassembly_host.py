@@ -372,3 +372,51 @@ def test_local_reassembly_many_contigs():
     ds = synth.generate(3, scale=0.005)
     n, out = compare(ds, vcf=True, fix_gaps=True, fix_local=True, K=31)
     assert n > 100
+
+
+def test_scan_reads_matches_numpy_restatement():
+    """pg_scan_reads against BamFile.scan restated in numpy on a store of
+    random flags, insert sizes, lengths and references: the nine insert
+    statistics (sumSq wrapping as a Scala Int) and the stray-mate indices, for
+    each BAM type's size cut and with --nonpf / --duplicates."""
+    from pilon_gb300.engine import scan_reads
+    rng = np.random.default_rng(21)
+    n = 200_000
+    recs = dict(flag=rng.integers(0, 1 << 12, n).astype(np.uint16),
+                tlen=rng.integers(-60_000, 60_000, n).astype(np.int32),
+                l_seq=rng.integers(0, 60_000, n).astype(np.int32),
+                ref_id=rng.integers(-1, 4, n).astype(np.int32), mate_ref_id=rng.integers(-1, 4, n).astype(np.int32))
+
+    class Store:  # the fields pg_scan_reads reads; the others empty
+        n_reads = n
+
+        def to_abi(self):
+            r = _abi.pg_reads()
+            r.n_reads = n
+            self._keep = recs
+            for k, v in recs.items():
+                setattr(r, k, v.ctypes.data)
+            return r
+
+    for nonpf, dups, bam_type in ((0, 0, _abi.PG_BAM_FRAGS), (1, 0, _abi.PG_BAM_JUMPS), (0, 1, _abi.PG_BAM_UNPAIRED)):
+        P = _abi.default_params(nonpf=nonpf, duplicates=dups, bam_type=bam_type)
+        huge = 5 * reassembly.MAX_INSERT_DEFAULT[bam_type]
+        stats, first, second = scan_reads(Store(), P, 3, huge, strays=True, threads=3)
+        f = recs["flag"]
+        ok = reassembly.validate(f, P) & ((f & 0x4) == 0)
+        paired, proper, rc = (f & 1) != 0, (f & 2) != 0, (f & 0x10) != 0
+        want = []
+        for sizes, sel in ((recs["tlen"], ok & paired & proper & ~rc), (recs["tlen"], ok & paired & proper & rc),
+                           (recs["l_seq"], ok & ~paired)):
+            s = sizes[sel].astype(np.int64)
+            s = s[(s > 0) & (s < huge)]
+            want += [s.size, int(s.sum()), int((s * s).astype(np.int32).sum(dtype=np.int64))]
+        assert stats.tolist() == want
+        rid, mrid = recs["ref_id"], recs["mate_ref_id"]
+        soi = ((rid >= 0) & (rid < 3)) | ((mrid >= 0) & (mrid < 3))
+        st = ok & paired & ~proper & ((f & 0x8) == 0) & soi
+        idx = np.nonzero(st)[0]
+        assert first.tolist() == idx[(f[idx] & 0x40) != 0].tolist()
+        assert second.tolist() == idx[(f[idx] & 0x40) == 0].tolist()
+        stats2, f2, s2 = scan_reads(Store(), P, 3, huge, strays=False)
+        assert stats2.tolist() == want and f2.size == s2.size == 0
